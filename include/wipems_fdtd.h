@@ -1,0 +1,309 @@
+/*
+ * wipems_fdtd.h -- C ABI of the GB300 FDTD engine (libwipems_fdtd.so).
+ *
+ * Three layers, each replacing one piece of the openEMS call chain that the
+ * reference runs on the host CPU:
+ *
+ *   scene     stand-in for the CSXCAD geometry/material database and the
+ *             openEMS XML <FDTD> setup (openems.cpp:798-936): rectilinear mesh
+ *             lines, priority-ordered boxes of material / metal / lumped
+ *             element / excitation / probe, boundary conditions, pulse.
+ *   operator  Operator::CalcECOperator and the operator extensions' builds
+ *             (FDTD/operator.cpp:973-1084, operator_ext_upml.cpp:365-466,
+ *             operator_ext_lorentzmaterial.cpp:117-438,
+ *             operator_ext_excitation.cpp:101-285).  Produces the reference's
+ *             own per-edge FP32 coefficient arrays (vv/vi/ii/iv, UPML slabs,
+ *             ADE lists, excitation lists) in host memory.
+ *   engine    Engine_CUDA: the Yee time stepping of Engine::IterateTS
+ *             (FDTD/engine.cpp:255-274) with UPML, Lorentz/Drude ADE and
+ *             excitation fused into the two half-step kernels, probes and the
+ *             energy end criterion reduced on the device.
+ *
+ * Every function returns an int status: 0 = success, < 0 = error.  The text of
+ * the last error of the calling thread is returned by fdtd_last_error().  No
+ * function calls exit(); invalid input is reported, never trapped.
+ *
+ * Array layout used across the ABI ("reference form"): a field or coefficient
+ * array of component n at node (x,y,z) lives at
+ *     base[((n*Nx + x)*Ny + y)*Nz + z]          (z fastest, no padding)
+ * which is the reference's FDTD_FLOAT**** [n][x][y][z] flattened.
+ */
+#ifndef WIPEMS_FDTD_H
+#define WIPEMS_FDTD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+
+#define FDTD_OK              0
+#define FDTD_ERR_ARG        -1   /* invalid argument / size */
+#define FDTD_ERR_CUDA       -2   /* CUDA runtime error */
+#define FDTD_ERR_NOMEM      -3   /* host or device allocation failed */
+#define FDTD_ERR_STATE      -4   /* call not valid in the object's state */
+#define FDTD_ERR_UNSUPPORTED -5  /* feature not provided by this engine */
+#define FDTD_ERR_TIMEOUT    -6   /* a bounded device wait gave up */
+#define FDTD_ERR_NONFINITE  -7   /* energy reduction saw NaN/Inf */
+
+/* Copies the calling thread's last error message (NUL terminated, truncated
+ * to cap).  Returns the full message length. */
+size_t fdtd_last_error(char* buf, size_t cap);
+
+/* ------------------------------------------------------------------- scene */
+
+typedef struct fdtd_scene_s* fdtd_scene_t;
+
+/* Boundary condition codes, as openEMS::m_BC_type (openems.cpp:850-880). */
+#define FDTD_BC_PEC 0
+#define FDTD_BC_PMC 1
+#define FDTD_BC_MUR 2   /* rejected: Mur ABC is not provided */
+#define FDTD_BC_PML 3
+
+/* Mesh lines in drawing units (strictly increasing), unit = metres per
+ * drawing unit (CSRectGrid::GetDeltaUnit, operator.cpp:806-812).
+ * Replaces Operator::SetGeometryCSX + SetupCSXGrid (operator.cpp:821-836). */
+int fdtd_scene_create(const double* lines_x, uint32_t nx,
+                      const double* lines_y, uint32_t ny,
+                      const double* lines_z, uint32_t nz,
+                      double unit, fdtd_scene_t* out);
+int fdtd_scene_destroy(fdtd_scene_t scene);
+
+/* CSBackgroundMaterial (operator.cpp:825-830). */
+int fdtd_scene_set_background(fdtd_scene_t s, double eps_r, double mue_r,
+                              double kappa, double sigma);
+/* bc[6] = xmin,xmax,ymin,ymax,zmin,zmax; pml_size[6] cells (PML_n).
+ * openEMS::SetupBoundaryConditions (openems.cpp:380-406). */
+int fdtd_scene_set_boundary(fdtd_scene_t s, const int bc[6],
+                            const uint32_t pml_size[6]);
+/* Gaussian pulse excitation signal, Excitation::SetupGaussianPulse
+ * (excitation.cpp:55-62).  nr_ts = NumberOfTimesteps (signal length cap). */
+int fdtd_scene_set_gauss_excite(fdtd_scene_t s, double f0, double fc,
+                                uint32_t nr_ts);
+/* <FDTD OverSampling=...> (openems.cpp:830-832, default 4). */
+int fdtd_scene_set_oversampling(fdtd_scene_t s, uint32_t oversampling);
+
+/* Primitive boxes.  priority: the highest priority box containing a
+ * coordinate wins (CSXCAD GetPropertyByCoordPriority); among equal
+ * priorities the box added first wins.  Boxes contain their surface. */
+int fdtd_scene_add_material(fdtd_scene_t s, int priority,
+                            const double start[3], const double stop[3],
+                            double eps_r, double kappa, double mue_r,
+                            double sigma);
+int fdtd_scene_add_metal(fdtd_scene_t s, int priority,
+                         const double start[3], const double stop[3]);
+/* Parallel R/C lumped element (Operator::Calc_LumpedElements,
+ * operator.cpp:1535-1712).  R<0 or C<=0 mean "not given". */
+int fdtd_scene_add_lumped(fdtd_scene_t s, int priority,
+                          const double start[3], const double stop[3],
+                          int direction, double R, double C, int caps);
+/* Excitation box: exc_type 0 soft-E, 1 hard-E, 2 soft-H, 3 hard-H;
+ * vec = weighted excitation per direction; delay in seconds
+ * (operator_ext_excitation.cpp:134-220). */
+int fdtd_scene_add_excitation(fdtd_scene_t s, int priority,
+                              const double start[3], const double stop[3],
+                              int exc_type, const double vec[3], double delay);
+/* Drude / Lorentz material (CSPropLorentzMaterial): a material box with
+ * eps_r/kappa/mue_r/sigma plus, per dispersion order o < order:
+ * eps_plasma_f[o] (Hz), eps_relax_t[o] (s), eps_lor_pole_f[o] (Hz, 0 = Drude).
+ * Read by Operator_Ext_LorentzMaterial::BuildExtension
+ * (operator_ext_lorentzmaterial.cpp:117-438). */
+int fdtd_scene_add_lorentz(fdtd_scene_t s, int priority,
+                           const double start[3], const double stop[3],
+                           double eps_r, double kappa, double mue_r,
+                           double sigma, int order,
+                           const double* eps_plasma_f,
+                           const double* eps_relax_t,
+                           const double* eps_lor_pole_f);
+/* Probe box: type 0 voltage (line integral, ProcessVoltage), type 1 current
+ * (loop around a surface, ProcessCurrent); weight multiplies the integral;
+ * norm_dir = normal direction of a current probe or -1.
+ * openEMS::SetupProcessing (openems.cpp:480-560). */
+int fdtd_scene_add_probe(fdtd_scene_t s, int type,
+                         const double start[3], const double stop[3],
+                         double weight, int norm_dir);
+
+/* ---------------------------------------------------------------- operator */
+
+typedef struct fdtd_operator_s* fdtd_operator_t;
+
+/* Operator::CalcECOperator + extension builds (operator.cpp:973-1084) and
+ * Excitation::buildExcitationSignal (openems.cpp:1124).  num_threads <= 0
+ * picks the hardware concurrency (Operator_Multithread does the same). */
+int fdtd_operator_build(fdtd_scene_t scene, int num_threads,
+                        fdtd_operator_t* out);
+int fdtd_operator_destroy(fdtd_operator_t op);
+
+typedef struct {
+    uint32_t num_lines[3];
+    double   dT;                 /* Operator::GetTimestep */
+    double   unit;               /* grid delta (m per drawing unit) */
+    uint32_t nyquist;            /* Excitation::GetNyquistNum */
+    uint32_t probe_interval;     /* max(1, Nyquist/OverSampling), openems.cpp:529 */
+    uint32_t signal_length;      /* Excitation::GetLength */
+    uint32_t max_excite_ts;      /* Excitation::GetMaxExcitationTimestep */
+    uint32_t num_upml;           /* UPML slab extensions */
+    uint32_t ade_order;          /* Lorentz/Drude dispersion order (0 = none) */
+    uint32_t volt_exc_count;     /* Operator_Ext_Excitation::Volt_Count */
+    uint32_t curr_exc_count;
+    uint32_t num_probes;
+    double   num_cells;          /* Operator::GetNumberCells (node count) */
+} fdtd_operator_info;
+
+int fdtd_operator_get_info(fdtd_operator_t op, fdtd_operator_info* info);
+
+/* ---- reference-form operator description (what Engine_CUDA reads) ------ */
+
+/* One Operator_Ext_UPML slab (operator_ext_upml.h:61-79): start/num_lines of
+ * the slab in the full grid; the six coefficient arrays are
+ * [3][nx][ny][nz] over the slab (z fastest). */
+typedef struct {
+    uint32_t start[3];
+    uint32_t num_lines[3];
+    const float* vv;   const float* vvfo; const float* vvfn;
+    const float* ii;   const float* iifo; const float* iifn;
+} fdtd_upml_desc;
+
+/* One dispersion order of Operator_Ext_LorentzMaterial
+ * (operator_ext_dispersive.h:47-53, operator_ext_lorentzmaterial.h): count
+ * positions pos_x/y/z; coefficient arrays are [3][count] or NULL when the
+ * corresponding *_on flag is 0. */
+typedef struct {
+    uint32_t count;
+    const uint32_t* pos[3];
+    int volt_on, curr_on, volt_lor_on, curr_lor_on;
+    const float* v_int; const float* v_ext; const float* v_lor;
+    const float* i_int; const float* i_ext; const float* i_lor;
+} fdtd_ade_desc;
+
+/* Everything Engine_CUDA needs from an Operator after CalcECOperator. */
+typedef struct {
+    uint32_t num_lines[3];
+    double   dT;
+    const float* vv; const float* vi; const float* ii; const float* iv;
+    uint32_t num_upml;
+    const fdtd_upml_desc* upml;
+    uint32_t num_ade_orders;
+    const fdtd_ade_desc* ade;
+    /* Operator_Ext_Excitation lists (operator_ext_excitation.h) */
+    uint32_t volt_count;
+    const uint32_t* volt_index[3];
+    const uint16_t* volt_dir;
+    const float*    volt_amp;
+    const uint32_t* volt_delay;
+    uint32_t curr_count;
+    const uint32_t* curr_index[3];
+    const uint16_t* curr_dir;
+    const float*    curr_amp;
+    const uint32_t* curr_delay;
+    /* Excitation::GetVoltageSignal/GetCurrentSignal, GetLength */
+    uint32_t signal_length;
+    const float* signal_volt;
+    const float* signal_curr;
+    uint32_t signal_period_ts;   /* int(period/dT), 0 = not periodic */
+} fdtd_op_desc;
+
+/* Fills desc with pointers into op's host arrays (valid while op lives). */
+int fdtd_operator_describe(fdtd_operator_t op, fdtd_op_desc* desc);
+
+/* Snapped probe of the operator (ProcessIntegral after
+ * DefineStartStopCoord).  type 0 voltage, 1 current. */
+typedef struct {
+    int      type;
+    uint32_t start[3], stop[3];
+    int      start_inside[3], stop_inside[3];
+    int      norm_dir;
+    double   weight;
+    int      enabled;
+} fdtd_probe_desc;
+
+int fdtd_operator_get_probe(fdtd_operator_t op, uint32_t i,
+                            fdtd_probe_desc* out);
+
+/* Copies the per-edge material store (eps_r-weighted C, G, L, R arrays are
+ * freed after the build, as in the reference) -- used by tests. */
+int fdtd_operator_get_timestep_scan(fdtd_operator_t op, double* dT_var3);
+
+/* ------------------------------------------------------------------ engine */
+
+typedef struct fdtd_engine_s* fdtd_engine_t;
+
+typedef struct {
+    int      device;          /* CUDA device ordinal */
+    uint32_t max_timesteps;   /* sizes the probe/energy ring (0 = 100000) */
+    uint32_t probe_interval;  /* samples at ts % interval == 0 (0 = off) */
+    int      use_graphs;      /* capture chunks of interval steps */
+    int      energy_on_probe; /* fuse the energy reduction into sample steps */
+    int      tile_y;          /* kernel tile rows (0 = autotuned default) */
+    int      x_chunk;         /* x planes per block (0 = default) */
+} fdtd_engine_opts;
+
+/* Operator::CreateEngine for the CUDA engine: compresses the coefficient
+ * arrays into a per-node uint16 (or uint32) index plus coefficient tables
+ * (the Operator_SSE_Compressed idea, operator_sse_compressed.cpp:120-176,
+ * extended by the UPML/ADE/excitation terms fused into the kernels) and
+ * uploads everything to the device.  Field arrays start at zero
+ * (Engine::Init, engine.cpp:49-57). */
+int fdtd_engine_create(const fdtd_op_desc* desc, const fdtd_engine_opts* opts,
+                       fdtd_engine_t* out);
+/* Engine::Reset (engine.cpp:98-106): frees device memory. */
+int fdtd_engine_destroy(fdtd_engine_t eng);
+
+/* Registers a probe (ProcessVoltage::CalcIntegral / ProcessCurrent::
+ * CalcIntegral, processvoltage.cpp:43-47, processcurrent.cpp:93-168) to be
+ * reduced on the device at every sample step.  Must precede the first
+ * iterate.  Returns the probe slot in *slot. */
+int fdtd_engine_add_probe(fdtd_engine_t eng, const fdtd_probe_desc* p,
+                          uint32_t* slot);
+
+/* Engine::IterateTS (engine.cpp:255-274). */
+int fdtd_engine_iterate(fdtd_engine_t eng, uint32_t n_steps);
+/* Engine::GetNumberOfTimesteps. */
+int fdtd_engine_num_timesteps(fdtd_engine_t eng, uint32_t* ts);
+
+/* Number of recorded samples and the per-sample record layout:
+ * ts[k], probe values [k][num_probes] (already multiplied by the weight),
+ * energy[k] (eps0*sum V^2 + mu0*sum I^2, or -1 when not computed).
+ * Reads all samples recorded so far (device -> host). */
+int fdtd_engine_num_samples(fdtd_engine_t eng, uint32_t* n);
+int fdtd_engine_read_samples(fdtd_engine_t eng, uint32_t first, uint32_t count,
+                             uint32_t* ts, double* probe_values,
+                             double* energy);
+
+/* Engine_Interface_FDTD::CalcFastEnergy (engine_interface_fdtd.cpp:292-337)
+ * computed now on the device. */
+int fdtd_engine_energy(fdtd_engine_t eng, double* energy);
+
+/* Copies all fields to host in reference form ([3][Nx][Ny][Nz]).  Either
+ * pointer may be NULL.  Test / final-field use only. */
+int fdtd_engine_get_fields(fdtd_engine_t eng, float* volt, float* curr);
+/* Engine::GetVolt / GetCurr for one edge (device -> host read). */
+int fdtd_engine_get_volt(fdtd_engine_t eng, uint32_t n, uint32_t x,
+                         uint32_t y, uint32_t z, float* v);
+int fdtd_engine_get_curr(fdtd_engine_t eng, uint32_t n, uint32_t x,
+                         uint32_t y, uint32_t z, float* v);
+
+typedef struct {
+    uint32_t num_tuples;      /* unique coefficient tuples after compression */
+    uint32_t index_bytes;     /* 2 (uint16) or 4 (uint32) */
+    uint32_t num_upml_nodes;  /* nodes inside UPML slabs */
+    uint32_t num_ade_nodes;   /* nodes carrying ADE state */
+    uint32_t padded_nz;       /* z row stride on the device */
+    uint64_t device_bytes;    /* device memory held by the engine */
+    uint32_t tile_y, x_chunk; /* kernel tiling in use */
+} fdtd_engine_stats;
+
+int fdtd_engine_get_stats(fdtd_engine_t eng, fdtd_engine_stats* st);
+
+/* Device time of the last iterate call's kernels, measured with CUDA events
+ * on the engine stream (ms) and the number of kernel launches it issued. */
+int fdtd_engine_last_timing(fdtd_engine_t eng, double* ms, uint64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WIPEMS_FDTD_H */

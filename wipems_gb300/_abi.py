@@ -1,0 +1,144 @@
+"""ctypes mirror of include/wipems_fdtd.h and the loader of libwipems_fdtd.so.
+
+The library is the in-tree build under wipems_gb300/_build.  There is no
+fallback: if it is missing or fails to load, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_build" / "libwipems_fdtd.so"
+
+u32 = C.c_uint32
+PF = C.POINTER(C.c_float)
+PU32 = C.POINTER(C.c_uint32)
+PU16 = C.POINTER(C.c_uint16)
+
+
+class FdtdOperatorInfo(C.Structure):
+    _fields_ = [("num_lines", u32 * 3), ("dT", C.c_double), ("unit", C.c_double),
+                ("nyquist", u32), ("probe_interval", u32), ("signal_length", u32),
+                ("max_excite_ts", u32), ("num_upml", u32), ("ade_order", u32),
+                ("volt_exc_count", u32), ("curr_exc_count", u32), ("num_probes", u32),
+                ("num_cells", C.c_double)]
+
+
+class FdtdUpmlDesc(C.Structure):
+    _fields_ = [("start", u32 * 3), ("num_lines", u32 * 3),
+                ("vv", PF), ("vvfo", PF), ("vvfn", PF), ("ii", PF), ("iifo", PF), ("iifn", PF)]
+
+
+class FdtdAdeDesc(C.Structure):
+    _fields_ = [("count", u32), ("pos", PU32 * 3),
+                ("volt_on", C.c_int), ("curr_on", C.c_int), ("volt_lor_on", C.c_int), ("curr_lor_on", C.c_int),
+                ("v_int", PF), ("v_ext", PF), ("v_lor", PF), ("i_int", PF), ("i_ext", PF), ("i_lor", PF)]
+
+
+class FdtdOpDesc(C.Structure):
+    _fields_ = [("num_lines", u32 * 3), ("dT", C.c_double),
+                ("vv", PF), ("vi", PF), ("ii", PF), ("iv", PF),
+                ("num_upml", u32), ("upml", C.POINTER(FdtdUpmlDesc)),
+                ("num_ade_orders", u32), ("ade", C.POINTER(FdtdAdeDesc)),
+                ("volt_count", u32), ("volt_index", PU32 * 3), ("volt_dir", PU16), ("volt_amp", PF),
+                ("volt_delay", PU32),
+                ("curr_count", u32), ("curr_index", PU32 * 3), ("curr_dir", PU16), ("curr_amp", PF),
+                ("curr_delay", PU32),
+                ("signal_length", u32), ("signal_volt", PF), ("signal_curr", PF), ("signal_period_ts", u32)]
+
+
+class FdtdProbeDesc(C.Structure):
+    _fields_ = [("type", C.c_int), ("start", u32 * 3), ("stop", u32 * 3),
+                ("start_inside", C.c_int * 3), ("stop_inside", C.c_int * 3),
+                ("norm_dir", C.c_int), ("weight", C.c_double), ("enabled", C.c_int)]
+
+
+class FdtdEngineOpts(C.Structure):
+    _fields_ = [("device", C.c_int), ("max_timesteps", u32), ("probe_interval", u32),
+                ("use_graphs", C.c_int), ("energy_on_probe", C.c_int), ("tile_y", C.c_int),
+                ("x_chunk", C.c_int)]
+
+
+class FdtdEngineStats(C.Structure):
+    _fields_ = [("num_tuples", u32), ("index_bytes", u32), ("num_upml_nodes", u32),
+                ("num_ade_nodes", u32), ("padded_nz", u32), ("device_bytes", C.c_uint64),
+                ("tile_y", u32), ("x_chunk", u32)]
+
+
+class FdtdError(RuntimeError):
+    def __init__(self, code: int, where: str, msg: str):
+        super().__init__(f"{where} failed ({code}): {msg}")
+        self.code = code
+
+
+_lib = None
+
+# (name, restype, argtypes) for every entry point declared in the header.
+_P = C.c_void_p
+PD = C.POINTER(C.c_double)
+SIGNATURES = [
+    ("fdtd_last_error", C.c_size_t, [C.c_char_p, C.c_size_t]),
+    ("fdtd_scene_create", C.c_int, [PD, u32, PD, u32, PD, u32, C.c_double, C.POINTER(_P)]),
+    ("fdtd_scene_destroy", C.c_int, [_P]),
+    ("fdtd_scene_set_background", C.c_int, [_P, C.c_double, C.c_double, C.c_double, C.c_double]),
+    ("fdtd_scene_set_boundary", C.c_int, [_P, C.POINTER(C.c_int), PU32]),
+    ("fdtd_scene_set_gauss_excite", C.c_int, [_P, C.c_double, C.c_double, u32]),
+    ("fdtd_scene_set_oversampling", C.c_int, [_P, u32]),
+    ("fdtd_scene_add_material", C.c_int, [_P, C.c_int, PD, PD, C.c_double, C.c_double, C.c_double, C.c_double]),
+    ("fdtd_scene_add_metal", C.c_int, [_P, C.c_int, PD, PD]),
+    ("fdtd_scene_add_lumped", C.c_int, [_P, C.c_int, PD, PD, C.c_int, C.c_double, C.c_double, C.c_int]),
+    ("fdtd_scene_add_excitation", C.c_int, [_P, C.c_int, PD, PD, C.c_int, PD, C.c_double]),
+    ("fdtd_scene_add_lorentz", C.c_int, [_P, C.c_int, PD, PD, C.c_double, C.c_double, C.c_double, C.c_double,
+                                         C.c_int, PD, PD, PD]),
+    ("fdtd_scene_add_probe", C.c_int, [_P, C.c_int, PD, PD, C.c_double, C.c_int]),
+    ("fdtd_operator_build", C.c_int, [_P, C.c_int, C.POINTER(_P)]),
+    ("fdtd_operator_destroy", C.c_int, [_P]),
+    ("fdtd_operator_get_info", C.c_int, [_P, C.POINTER(FdtdOperatorInfo)]),
+    ("fdtd_operator_describe", C.c_int, [_P, C.POINTER(FdtdOpDesc)]),
+    ("fdtd_operator_get_probe", C.c_int, [_P, u32, C.POINTER(FdtdProbeDesc)]),
+    ("fdtd_engine_create", C.c_int, [C.POINTER(FdtdOpDesc), C.POINTER(FdtdEngineOpts), C.POINTER(_P)]),
+    ("fdtd_engine_destroy", C.c_int, [_P]),
+    ("fdtd_engine_add_probe", C.c_int, [_P, C.POINTER(FdtdProbeDesc), PU32]),
+    ("fdtd_engine_iterate", C.c_int, [_P, u32]),
+    ("fdtd_engine_num_timesteps", C.c_int, [_P, PU32]),
+    ("fdtd_engine_num_samples", C.c_int, [_P, PU32]),
+    ("fdtd_engine_read_samples", C.c_int, [_P, u32, u32, PU32, PD, PD]),
+    ("fdtd_engine_energy", C.c_int, [_P, PD]),
+    ("fdtd_engine_get_fields", C.c_int, [_P, PF, PF]),
+    ("fdtd_engine_get_volt", C.c_int, [_P, u32, u32, u32, u32, PF]),
+    ("fdtd_engine_get_curr", C.c_int, [_P, u32, u32, u32, u32, PF]),
+    ("fdtd_engine_get_stats", C.c_int, [_P, C.POINTER(FdtdEngineStats)]),
+    ("fdtd_engine_last_timing", C.c_int, [_P, PD, C.POINTER(C.c_uint64)]),
+]
+
+
+def lib() -> C.CDLL:
+    """Loads libwipems_fdtd.so (building it first if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists() or os.environ.get("WIPEMS_REBUILD"):
+        from . import build as _build
+        _build.build()
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"{LIB_PATH} is missing: the CUDA engine library was not built")
+    L = C.CDLL(str(LIB_PATH))
+    for name, res, args in SIGNATURES:
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    buf = C.create_string_buffer(4096)
+    lib().fdtd_last_error(buf, 4096)
+    return buf.value.decode(errors="replace")
+
+
+def check(rc: int, where: str) -> None:
+    if rc != 0:
+        raise FdtdError(rc, where, last_error())

@@ -1,0 +1,119 @@
+// Host-side data structures of the FDTD operator (setup-time C++).
+//
+// The scene is the stand-in for the CSXCAD geometry database: rectilinear
+// mesh lines plus priority-ordered boxes.  The operator holds the
+// reference-form coefficient arrays that openEMS's Operator and its
+// extensions hold after CalcECOperator (FDTD/operator.h:285-288,
+// extensions/operator_ext_upml.h:61-79, operator_ext_lorentzmaterial.h,
+// operator_ext_excitation.h).
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/wipems_fdtd.h"
+
+namespace wipems {
+
+// tools/constants.h:21-27
+constexpr double kEps0 = 8.85418781762e-12;
+constexpr double kMue0 = 1.256637062e-6;
+constexpr double kC0 = 299792458;
+constexpr double kZ0 = 376.730313461;
+constexpr double kPi = 3.141592653589793238462643383279;
+
+enum PrimKind { PK_MATERIAL = 1, PK_METAL = 2, PK_LUMPED = 3, PK_EXCITATION = 4, PK_PROBE = 5 };
+
+constexpr int kMaxDispOrder = 4;
+
+struct Prim {
+    int kind = 0;
+    int priority = 0;
+    double start[3] = {0, 0, 0}, stop[3] = {0, 0, 0};
+    double bmin[3] = {0, 0, 0}, bmax[3] = {0, 0, 0};  // ordered bounds
+    // material / lorentz
+    double eps = 1, kappa = 0, mue = 1, sigma = 0;
+    bool lorentz = false;
+    int disp_order = 0;
+    double eps_plasma_f[kMaxDispOrder] = {0, 0, 0, 0};
+    double eps_relax_t[kMaxDispOrder] = {0, 0, 0, 0};
+    double eps_lor_pole_f[kMaxDispOrder] = {0, 0, 0, 0};
+    // lumped element
+    int ny = 2;
+    double R = -1, C = -1;
+    bool caps = false;
+    // excitation
+    int exc_type = 0;
+    double exc_vec[3] = {0, 0, 0};
+    double delay = 0;
+    // probe
+    int probe_type = 0;
+    double weight = 1;
+    int norm_dir = -1;
+};
+
+}  // namespace wipems
+
+struct fdtd_scene_s {
+    std::vector<double> lines[3];
+    double unit = 1;
+    double bg_eps = 1, bg_mue = 1, bg_kappa = 0, bg_sigma = 0;
+    int bc[6] = {0, 0, 0, 0, 0, 0};
+    uint32_t pml_size[6] = {0, 0, 0, 0, 0, 0};
+    double f0 = 0, fc = 0;
+    bool have_excite = false;
+    uint32_t nr_ts = 0;
+    uint32_t oversampling = 4;
+    std::vector<wipems::Prim> prims;
+};
+
+namespace wipems {
+
+struct UpmlSlab {
+    uint32_t start[3];
+    uint32_t num_lines[3];
+    // [3][nx][ny][nz]
+    std::vector<float> vv, vvfo, vvfn, ii, iifo, iifn;
+};
+
+struct AdeOrder {
+    uint32_t count = 0;
+    std::vector<uint32_t> pos[3];
+    bool volt_on = false, curr_on = false, volt_lor_on = false, curr_lor_on = false;
+    std::vector<float> v_int, v_ext, v_lor, i_int, i_ext, i_lor;  // [3][count]
+};
+
+struct ExcList {
+    std::vector<uint32_t> index[3];
+    std::vector<uint16_t> dir;
+    std::vector<float> amp;
+    std::vector<uint32_t> delay;
+};
+
+}  // namespace wipems
+
+struct fdtd_operator_s {
+    uint32_t N[3] = {0, 0, 0};
+    double unit = 1;
+    std::vector<double> lines[3];
+    double dT = 0;
+    // reference-form coefficient arrays [3][Nx][Ny][Nz]
+    std::vector<float> vv, vi, ii, iv;
+    std::vector<wipems::UpmlSlab> upml;
+    std::vector<wipems::AdeOrder> ade;
+    wipems::ExcList volt_exc, curr_exc;
+    std::vector<float> sig_volt, sig_curr;
+    uint32_t signal_length = 0;
+    uint32_t nyquist = 0;
+    uint32_t probe_interval = 1;
+    uint32_t max_excite_ts = 0;
+    std::vector<fdtd_probe_desc> probes;
+    // descriptor scratch kept alive for fdtd_operator_describe
+    std::vector<fdtd_upml_desc> upml_desc;
+    std::vector<fdtd_ade_desc> ade_desc;
+};
+
+namespace wipems {
+void set_error(const std::string& msg);
+}

@@ -1,0 +1,330 @@
+"""Host-side mirror of openEMS's Operator / Engine interface for the CUDA engine.
+
+    Scene     ContinuousStructure + the <FDTD> setup (mesh, boxes, boundary
+              conditions, Gaussian excitation, probes).
+    Operator  Operator::CalcECOperator (FDTD/operator.cpp:973-1084) with the
+              excitation, UPML and Lorentz extension builds, run in C++.
+    Engine    Engine_CUDA: IterateTS / GetNumberOfTimesteps / GetVolt /
+              GetCurr (FDTD/engine.h:39-61) on the GPU, probes and energy
+              reduced on the device.
+    run_fdtd  openEMS::RunFDTD's loop (openems.cpp:1241-1345): iterate in
+              probe-interval chunks until NrTS or the energy end criterion.
+
+All compute goes through libwipems_fdtd.so; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi
+from ._abi import check, lib
+
+EPS0 = 8.85418781762e-12
+MUE0 = 1.256637062e-6
+C0 = 299792458.0
+
+BC_PEC, BC_PMC, BC_MUR, BC_PML = 0, 1, 2, 3
+
+
+def _d3(v) -> C.Array:
+    a = (C.c_double * 3)(*[float(x) for x in v])
+    return a
+
+
+class Scene:
+    """Mesh + primitives; the stand-in for CSXCAD (see DESIGN: box model)."""
+
+    def __init__(self, lines_x, lines_y, lines_z, unit: float):
+        self._lines = [np.ascontiguousarray(l, dtype=np.float64) for l in (lines_x, lines_y, lines_z)]
+        h = C.c_void_p()
+        L = lib()
+        ptr = [l.ctypes.data_as(C.POINTER(C.c_double)) for l in self._lines]
+        check(L.fdtd_scene_create(ptr[0], len(self._lines[0]), ptr[1], len(self._lines[1]), ptr[2],
+                                  len(self._lines[2]), float(unit), C.byref(h)), "fdtd_scene_create")
+        self._h = h
+        self.unit = unit
+        self.nr_ts = 0
+        self.probes: list[dict] = []
+        self.meta: dict = {}
+
+    @property
+    def lines(self):
+        return self._lines
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            try:
+                lib().fdtd_scene_destroy(self._h)
+            except Exception:
+                pass
+            self._h = None
+
+    def set_background(self, eps_r=1.0, mue_r=1.0, kappa=0.0, sigma=0.0):
+        check(lib().fdtd_scene_set_background(self._h, eps_r, mue_r, kappa, sigma), "set_background")
+
+    def set_boundary(self, bc, pml_size=(0,) * 6):
+        b = (C.c_int * 6)(*bc)
+        s = (C.c_uint32 * 6)(*pml_size)
+        check(lib().fdtd_scene_set_boundary(self._h, b, s), "set_boundary")
+
+    def set_gauss_excite(self, f0: float, fc: float, nr_ts: int):
+        self.nr_ts = int(nr_ts)
+        check(lib().fdtd_scene_set_gauss_excite(self._h, f0, fc, int(nr_ts)), "set_gauss_excite")
+
+    def set_oversampling(self, os_: int):
+        check(lib().fdtd_scene_set_oversampling(self._h, int(os_)), "set_oversampling")
+
+    def add_material(self, start, stop, eps_r=1.0, kappa=0.0, mue_r=1.0, sigma=0.0, priority=0):
+        check(lib().fdtd_scene_add_material(self._h, int(priority), _d3(start), _d3(stop), eps_r, kappa, mue_r,
+                                            sigma), "add_material")
+
+    def add_metal(self, start, stop, priority=0):
+        check(lib().fdtd_scene_add_metal(self._h, int(priority), _d3(start), _d3(stop)), "add_metal")
+
+    def add_lumped(self, start, stop, direction, R=-1.0, Cap=-1.0, caps=True, priority=0):
+        check(lib().fdtd_scene_add_lumped(self._h, int(priority), _d3(start), _d3(stop), int(direction), float(R),
+                                          float(Cap), int(bool(caps))), "add_lumped")
+
+    def add_excitation(self, start, stop, vec, exc_type=0, delay=0.0, priority=0):
+        check(lib().fdtd_scene_add_excitation(self._h, int(priority), _d3(start), _d3(stop), int(exc_type),
+                                              _d3(vec), float(delay)), "add_excitation")
+
+    def add_lorentz(self, start, stop, eps_r=1.0, kappa=0.0, mue_r=1.0, sigma=0.0, plasma_f=(), relax_t=(),
+                    pole_f=(), priority=0):
+        order = len(plasma_f)
+        pf = (C.c_double * max(order, 1))(*plasma_f)
+        rt = (C.c_double * max(order, 1))(*(relax_t or [0.0] * order))
+        lp = (C.c_double * max(order, 1))(*(pole_f or [0.0] * order))
+        check(lib().fdtd_scene_add_lorentz(self._h, int(priority), _d3(start), _d3(stop), eps_r, kappa, mue_r, sigma,
+                                           order, pf, rt, lp), "add_lorentz")
+
+    def add_probe(self, start, stop, ptype: int, weight=1.0, norm_dir=-1, name=""):
+        check(lib().fdtd_scene_add_probe(self._h, int(ptype), _d3(start), _d3(stop), float(weight), int(norm_dir)),
+              "add_probe")
+        self.probes.append(dict(name=name or f"probe{len(self.probes)}", type=ptype))
+
+    def add_lumped_port(self, start, stop, direction, R, excite=1.0, priority=5, name="port"):
+        """openEMS python LumpedPort (python/openEMS/ports.py:143-185):
+        parallel-R lumped element with caps, soft E excitation of
+        -direction*excite, voltage probe along the centre line (weight -1)
+        and current probe across the mid plane (weight = direction)."""
+        start = np.asarray(start, dtype=float)
+        stop = np.asarray(stop, dtype=float)
+        ny = int(direction)
+        sign = float(np.sign(stop[ny] - start[ny]))
+        if R > 0:
+            self.add_lumped(start, stop, ny, R=R, caps=True, priority=priority)
+        elif R == 0:
+            self.add_metal(start, stop, priority=priority)
+        if excite != 0:
+            vec = np.zeros(3)
+            vec[ny] = -1 * sign * excite
+            self.add_excitation(start, stop, vec, exc_type=0, priority=priority)
+        u_start = 0.5 * (start + stop)
+        u_start[ny] = start[ny]
+        u_stop = 0.5 * (start + stop)
+        u_stop[ny] = stop[ny]
+        self.add_probe(u_start, u_stop, 0, weight=-1, name=name + "_ut")
+        i_start = start.copy()
+        i_start[ny] = 0.5 * (start[ny] + stop[ny])
+        i_stop = stop.copy()
+        i_stop[ny] = 0.5 * (start[ny] + stop[ny])
+        self.add_probe(i_start, i_stop, 1, weight=sign, norm_dir=ny, name=name + "_it")
+
+
+class Operator:
+    """Operator::CalcECOperator + extension builds, run on the host."""
+
+    def __init__(self, scene: Scene, threads: int = 0):
+        h = C.c_void_p()
+        check(lib().fdtd_operator_build(scene._h, int(threads), C.byref(h)), "fdtd_operator_build")
+        self._h = h
+        self.scene = scene
+        info = _abi.FdtdOperatorInfo()
+        check(lib().fdtd_operator_get_info(h, C.byref(info)), "fdtd_operator_get_info")
+        self.info = info
+        self.num_lines = tuple(int(x) for x in info.num_lines)
+        self.dT = float(info.dT)
+        self.probe_interval = int(info.probe_interval)
+        self.nyquist = int(info.nyquist)
+        self.desc = _abi.FdtdOpDesc()
+        check(lib().fdtd_operator_describe(h, C.byref(self.desc)), "fdtd_operator_describe")
+        self.probes = []
+        for i in range(info.num_probes):
+            p = _abi.FdtdProbeDesc()
+            check(lib().fdtd_operator_get_probe(h, i, C.byref(p)), "fdtd_operator_get_probe")
+            self.probes.append(p)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            try:
+                lib().fdtd_operator_destroy(self._h)
+            except Exception:
+                pass
+            self._h = None
+
+    @property
+    def num_nodes(self) -> int:
+        n = self.num_lines
+        return n[0] * n[1] * n[2]
+
+    def coefficients(self):
+        """Reference-form vv, vi, ii, iv as numpy views [3][Nx][Ny][Nz]."""
+        shape = (3,) + self.num_lines
+        cnt = 3 * self.num_nodes
+        out = []
+        for name in ("vv", "vi", "ii", "iv"):
+            ptr = getattr(self.desc, name)
+            out.append(np.ctypeslib.as_array(ptr, shape=(cnt,)).reshape(shape))
+        return out
+
+    def signals(self):
+        n = self.desc.signal_length
+        if n == 0:
+            return np.zeros(0, np.float32), np.zeros(0, np.float32)
+        return (np.ctypeslib.as_array(self.desc.signal_volt, shape=(n,)).copy(),
+                np.ctypeslib.as_array(self.desc.signal_curr, shape=(n,)).copy())
+
+    def excitation(self):
+        d = self.desc
+        n = d.volt_count
+        if n == 0:
+            return dict(index=np.zeros((3, 0), np.uint32), dir=np.zeros(0, np.uint16), amp=np.zeros(0, np.float32))
+        idx = np.stack([np.ctypeslib.as_array(d.volt_index[a], shape=(n,)) for a in range(3)])
+        return dict(index=idx.copy(), dir=np.ctypeslib.as_array(d.volt_dir, shape=(n,)).copy(),
+                    amp=np.ctypeslib.as_array(d.volt_amp, shape=(n,)).copy())
+
+
+@dataclass
+class Samples:
+    ts: np.ndarray
+    values: np.ndarray      # [nsamples][nprobes]
+    energy: np.ndarray
+    dT: float
+    probe_types: list = field(default_factory=list)
+
+    def times(self, p: int) -> np.ndarray:
+        """Sample times of probe p: voltage probes at ts*dT, current probes on
+        the dual time (ts+0.5)*dT (openems.cpp:522-526)."""
+        dual = 0.5 if self.probe_types[p] == 1 else 0.0
+        return (self.ts + dual) * self.dT
+
+
+class Engine:
+    """Engine_CUDA on one GPU."""
+
+    def __init__(self, op: Operator, device: int = 0, max_timesteps: int = 0, probe_interval: int | None = None,
+                 use_graphs: bool = True, energy_on_probe: bool = True, tile_y: int = 0, x_chunk: int = 0,
+                 probes: bool = True):
+        self.op = op
+        o = _abi.FdtdEngineOpts()
+        o.device = device
+        o.max_timesteps = int(max_timesteps or op.scene.nr_ts or 100000)
+        o.probe_interval = int(op.probe_interval if probe_interval is None else probe_interval)
+        o.use_graphs = int(use_graphs)
+        o.energy_on_probe = int(energy_on_probe)
+        o.tile_y = int(tile_y)
+        o.x_chunk = int(x_chunk)
+        h = C.c_void_p()
+        check(lib().fdtd_engine_create(C.byref(op.desc), C.byref(o), C.byref(h)), "fdtd_engine_create")
+        self._h = h
+        self.interval = o.probe_interval
+        self.probe_types = []
+        if probes:
+            for p in op.probes:
+                check(lib().fdtd_engine_add_probe(h, C.byref(p), None), "fdtd_engine_add_probe")
+                self.probe_types.append(p.type)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fdtd_engine_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def iterate(self, n: int):
+        check(lib().fdtd_engine_iterate(self._h, int(n)), "fdtd_engine_iterate")
+
+    @property
+    def num_timesteps(self) -> int:
+        v = C.c_uint32()
+        check(lib().fdtd_engine_num_timesteps(self._h, C.byref(v)), "num_timesteps")
+        return v.value
+
+    def samples(self) -> Samples:
+        n = C.c_uint32()
+        check(lib().fdtd_engine_num_samples(self._h, C.byref(n)), "num_samples")
+        n = n.value
+        np_ = len(self.probe_types)
+        ts = np.zeros(n, np.uint32)
+        vals = np.zeros((n, max(np_, 1)), np.float64)
+        en = np.zeros(n, np.float64)
+        if n:
+            check(lib().fdtd_engine_read_samples(self._h, 0, n, ts.ctypes.data_as(_abi.PU32),
+                                                 vals.ctypes.data_as(_abi.PD), en.ctypes.data_as(_abi.PD)),
+                  "read_samples")
+        return Samples(ts=ts.astype(np.int64), values=vals[:, :np_], energy=en, dT=self.op.dT,
+                       probe_types=list(self.probe_types))
+
+    def energy(self) -> float:
+        v = C.c_double()
+        check(lib().fdtd_engine_energy(self._h, C.byref(v)), "energy")
+        return v.value
+
+    def fields(self):
+        shape = (3,) + self.op.num_lines
+        V = np.empty(shape, np.float32)
+        I = np.empty(shape, np.float32)
+        check(lib().fdtd_engine_get_fields(self._h, V.ctypes.data_as(_abi.PF), I.ctypes.data_as(_abi.PF)),
+              "get_fields")
+        return V, I
+
+    def get_volt(self, n, x, y, z) -> float:
+        v = C.c_float()
+        check(lib().fdtd_engine_get_volt(self._h, n, x, y, z, C.byref(v)), "get_volt")
+        return v.value
+
+    def get_curr(self, n, x, y, z) -> float:
+        v = C.c_float()
+        check(lib().fdtd_engine_get_curr(self._h, n, x, y, z, C.byref(v)), "get_curr")
+        return v.value
+
+    def stats(self) -> dict:
+        s = _abi.FdtdEngineStats()
+        check(lib().fdtd_engine_get_stats(self._h, C.byref(s)), "get_stats")
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+    def last_timing(self):
+        ms = C.c_double()
+        n = C.c_uint64()
+        check(lib().fdtd_engine_last_timing(self._h, C.byref(ms), C.byref(n)), "last_timing")
+        return ms.value, n.value
+
+
+def run_fdtd(engine: Engine, nr_ts: int, end_crit: float = 1e-6) -> dict:
+    """openEMS::RunFDTD's loop: iterate in probe-interval chunks until NrTS
+    or until the energy has decayed below end_crit relative to its maximum
+    (checked on every sample; the reference checks every ~4 s of wall time,
+    openems.cpp:1285-1314)."""
+    step = engine.interval or nr_ts
+    maxE = 0.0
+    change = 1.0
+    seen = 0
+    while engine.num_timesteps < nr_ts and change > end_crit:
+        n = min(step - engine.num_timesteps % step, nr_ts - engine.num_timesteps)
+        engine.iterate(n)
+        s = engine.samples()
+        for e in s.energy[seen:]:
+            if e >= 0:
+                maxE = max(maxE, e)
+                if maxE > 0:
+                    change = e / maxE
+        seen = len(s.energy)
+    return dict(timesteps=engine.num_timesteps, energy_change=change)
