@@ -1,0 +1,324 @@
+"""Benchmark of the GB300 FDTD engine on the single-large-job workload.
+
+Workload (L256): 256^3 cells (257^3 = 16.97 M nodes) on a uniform 0.5 mm
+mesh, 8-cell UPML on all six faces, 40 seeded dielectric bricks, a 50 ohm
+z-directed lumped port with a Gaussian pulse; FP32 fields.  One bench step
+is one full 1000-timestep simulation of that job (the hot path
+Engine::IterateTS over the whole grid, 1000 times), with the engine's
+fields reset to zero before each step.  Inputs (fields + operator, > 500 MB)
+are larger than the 129 MB L2, so no explicit flush is done.
+
+    value   Mcell-updates/s (node count x timesteps / device time, the
+            reference's own MC/s convention, openems.cpp:1303-1305), device
+            time = CUDA events on the engine stream around each step
+    e2e     the same metric through the C ABI with host buffers: per step,
+            fdtd_engine_create_compressed from the pinned compressed operator
+            (host -> device), fdtd_engine_iterate in probe-interval chunks
+            with each new probe/energy sample read back (device -> host),
+            fdtd_engine_destroy
+    roofline  the dominant half-step kernel against the measured HBM copy
+            bandwidth (MEASURED_PEAKS.json)
+    cpu_baseline  the oracle's restated SSE-compressed multithreaded engine
+            (the reference's default engine family) on the host cores
+
+--impl reference times that CPU engine alone on the same workload and metric.
+Multi-GPU (torchrun): every rank runs an independent replica of the job
+(the path has no exchange step: "replicas only"), value is the sum over
+ranks divided by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+TIMESTEPS = 1000
+BYTES_BASE_HALF = 38      # 3 V + 3 I read, 3 V (or I) written, 2 B index
+BYTES_UPML_HALF = 24      # 3 flux read + 3 flux written
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _traffic_from_profiles(kernel: str):
+    """DRAM bytes per launch of the kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "ncu_traffic.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        parts = line.split()
+        if len(parts) >= 3 and parts[0] == kernel and parts[1] == "l256":
+            try:
+                return float(parts[2])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if f[5 + k].lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_workload(threads: int = 0):
+    from wipems_gb300 import CompressedOperator, Operator, scenes
+    t0 = time.perf_counter()
+    sc = scenes.l256(nr_ts=TIMESTEPS)
+    op = Operator(sc, threads=threads)
+    t1 = time.perf_counter()
+    cop = CompressedOperator(op)
+    t2 = time.perf_counter()
+    return sc, op, cop, dict(operator_build_s=round(t1 - t0, 3), compress_s=round(t2 - t1, 3))
+
+
+def config_dict(op, cop, extra=None):
+    n = op.num_lines
+    d = {"workload": "L256: 256^3 cells (257^3 nodes), 0.5 mm uniform mesh, UPML-8 on 6 faces, 40 seeded "
+                     "dielectric bricks, 50 ohm z lumped port, Gaussian f0=fc=10 GHz; one step = one "
+                     f"{TIMESTEPS}-timestep simulation",
+         "nodes": n[0] * n[1] * n[2], "cells": (n[0] - 1) * (n[1] - 1) * (n[2] - 1), "timesteps_per_step": TIMESTEPS,
+         "upml_nodes": cop.info["num_upml_nodes"], "tuples": cop.info["num_tuples"],
+         "index_bytes": cop.info["index_bytes"], "l2_policy": "inputs larger than L2 (fields+operator > 500 MB)",
+         "parallelism": "replicas"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+def cpu_baseline(op, threads: int, target_s: float = 12.0):
+    """Oracle SSE-compressed MT engine on a bounded number of timesteps."""
+    import oracle
+    # calibrate on 2 timesteps, then run about target_s of stepping
+    r = oracle.run(op.desc, [], 2, 0, engine=oracle.SSE_COMPRESSED_MT, threads=threads, energy=False, fields=False)
+    per = max(r["seconds"] / 2, 1e-4)
+    n = int(max(4, min(400, target_s / per)))
+    r = oracle.run(op.desc, [], n, 0, engine=oracle.SSE_COMPRESSED_MT, threads=threads, energy=False, fields=False)
+    mcs = op.num_nodes * n / r["seconds"] / 1e6
+    return mcs, n, r["seconds"]
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    sc, op, cop, setup = build_workload()
+    threads = os.cpu_count() or 1
+    import oracle
+    per_step = max(4, args.ref_timesteps)
+    for _ in range(args.warmup):
+        oracle.run(op.desc, [], per_step, 0, engine=oracle.SSE_COMPRESSED_MT, threads=threads, energy=False,
+                   fields=False)
+    tot = 0.0
+    for _ in range(args.steps):
+        r = oracle.run(op.desc, [], per_step, 0, engine=oracle.SSE_COMPRESSED_MT, threads=threads, energy=False,
+                       fields=False)
+        tot += r["seconds"]
+    value = op.num_nodes * per_step * args.steps / tot / 1e6
+    line = {"metric": "Mcell-updates/s", "value": round(value, 2), "unit": "Mcell-updates/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(tot / args.steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "impl": "reference",
+            "config": config_dict(op, cop, {"cpu_timesteps_per_step": per_step}),
+            "cpu_baseline": {"value": round(value, 2), "unit": "Mcell-updates/s", "cores": threads, "kind": "port",
+                             "sample": f"{per_step} timesteps of L256 per step (restated SSE-compressed "
+                                       f"x-slab multithreaded engine)"},
+            "e2e": {"value": round(value, 2), "unit": "Mcell-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, rank, world, local_rank):
+    import torch
+    import wipems_gb300
+    from wipems_gb300 import Engine
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+    sc, op, cop, setup = build_workload()
+    nodes = op.num_nodes
+    eng = Engine(cop, device=local_rank, max_timesteps=TIMESTEPS)
+    # warm-up
+    for _ in range(args.warmup):
+        eng.reset()
+        eng.iterate(TIMESTEPS)
+    launches = 0
+    ms_total = 0.0
+    sampler = ClockSampler(local_rank)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        eng.reset()
+        eng.iterate(TIMESTEPS)
+        ms, n = eng.last_timing()
+        ms_total += ms
+        launches += n
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clocks = sampler.stop()
+    if dist:
+        dist.barrier()
+    dev_s = ms_total / 1e3
+    if dist:
+        t = torch.tensor([dev_s, wall], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_s, wall = float(t[0]), float(t[1])
+    value = nodes * TIMESTEPS * args.steps * world / dev_s / 1e6
+
+    # live per-kernel durations (events around each launch)
+    eng.reset()
+    ms_v, ms_c = eng.profile_kernels(60)
+    upml = cop.info["num_upml_nodes"]
+    bytes_half = BYTES_BASE_HALF * nodes + BYTES_UPML_HALF * upml
+    dominant, ms_dom = ("k_volt", ms_v) if ms_v >= ms_c else ("k_curr", ms_c)
+    peak, peak_kind = _peaks()
+    achieved = bytes_half / (ms_dom / 1e3) / 1e9
+    traffic = _traffic_from_profiles(dominant)
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": dominant,
+                "algorithmic_bytes_per_launch": bytes_half, "launch_ms": round(ms_dom, 5),
+                "other_kernel_ms": round(ms_c if dominant == "k_volt" else ms_v, 5),
+                "step_frac": round(2 * bytes_half / ((ms_v + ms_c) / 1e3) / 1e9 / peak, 4),
+                "peak_kind": f"{peak_kind} (HBM copy, MEASURED_PEAKS.json)" if peak_kind == "measured" else peak_kind}
+    eng.close()
+
+    # e2e through the C ABI with host buffers
+    e2e_steps = max(1, min(args.steps, 3))
+    h2d = cop.info["host_bytes"]
+    d2h = 0
+    torch.cuda.synchronize()
+    te = time.perf_counter()
+    for _ in range(e2e_steps):
+        e = Engine(cop, device=local_rank, max_timesteps=TIMESTEPS)
+        done = 0
+        nread = 0
+        while done < TIMESTEPS:
+            k = min(e.interval, TIMESTEPS - done)
+            e.iterate(k)
+            done += k
+            n = e.num_samples()
+            if n > nread:
+                ts, vals, en = e.read_samples(nread, n - nread)
+                d2h += ts.nbytes + vals.nbytes + en.nbytes + 4
+                nread = n
+        e.close()
+    torch.cuda.synchronize()
+    te = time.perf_counter() - te
+    e2e_value = nodes * TIMESTEPS * e2e_steps * world / te / 1e6
+
+    if rank == 0:
+        threads = os.cpu_count() or 1
+        cpu_v, cpu_n, cpu_s = cpu_baseline(op, threads)
+        line = {"metric": "Mcell-updates/s", "value": round(value, 2), "unit": "Mcell-updates/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dev_s / args.steps * 1e3, 3),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "config": config_dict(op, cop, {**setup, "wall_s": round(wall, 3)}),
+                "roofline": roofline,
+                "cpu_baseline": {"value": round(cpu_v, 2), "unit": "Mcell-updates/s", "cores": threads,
+                                 "kind": "port",
+                                 "sample": f"{cpu_n} timesteps of L256 ({cpu_s:.1f} s) with the restated "
+                                           f"SSE-compressed x-slab multithreaded engine"},
+                "e2e": {"value": round(e2e_value, 2), "unit": "Mcell-updates/s",
+                        "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h // e2e_steps),
+                        "steps": e2e_steps},
+                "gpu_launches": int(launches), "clocks": clocks}
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--ref-timesteps", type=int, default=20, help="CPU timesteps per reference-arm step")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "gloo" if args.impl == "reference" else "nccl"
+        dist.init_process_group(backend=backend)
+    try:
+        if args.impl == "reference":
+            run_reference(args, rank, world)
+        else:
+            import __graft_entry__
+            __graft_entry__.build()
+            run_gpu(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -223,13 +223,39 @@ typedef struct {
 int fdtd_operator_get_probe(fdtd_operator_t op, uint32_t i,
                             fdtd_probe_desc* out);
 
-/* Copies the per-edge material store (eps_r-weighted C, G, L, R arrays are
- * freed after the build, as in the reference) -- used by tests. */
-int fdtd_operator_get_timestep_scan(fdtd_operator_t op, double* dT_var3);
+typedef struct fdtd_engine_s* fdtd_engine_t;
+
+/* -------------------------------------------------- compressed operator */
+
+typedef struct fdtd_cop_s* fdtd_cop_t;
+
+/* Host-side compression of a reference-form operator into one per-node
+ * tuple index (uint16 when the unique tuples fit, else uint32) plus
+ * coefficient tables holding vv/vi/ii/iv and the fused UPML, ADE and
+ * excitation terms -- the Operator_SSE_Compressed::CompressOperator idea
+ * (operator_sse_compressed.cpp:120-176) applied per node.  The index is kept
+ * in pinned host memory when a CUDA device is present.  Runs without a GPU. */
+int fdtd_compress(const fdtd_op_desc* desc, fdtd_cop_t* out);
+int fdtd_cop_destroy(fdtd_cop_t cop);
+
+typedef struct {
+    uint32_t num_lines[3];
+    uint32_t num_tuples;
+    uint32_t index_bytes;
+    uint32_t padded_nz;
+    uint32_t num_upml_nodes;
+    uint32_t num_ade_nodes;
+    uint64_t host_bytes;
+    int      pinned;
+} fdtd_cop_info;
+
+int fdtd_cop_get_info(fdtd_cop_t cop, fdtd_cop_info* info);
+/* Expands the index + tables back to reference-form vv/vi/ii/iv and the
+ * per-node E/H flag words (any pointer may be NULL).  Test use. */
+int fdtd_cop_expand(fdtd_cop_t cop, float* vv, float* vi, float* ii, float* iv,
+                    uint32_t* flags_e, uint32_t* flags_h);
 
 /* ------------------------------------------------------------------ engine */
-
-typedef struct fdtd_engine_s* fdtd_engine_t;
 
 typedef struct {
     int      device;          /* CUDA device ordinal */
@@ -249,6 +275,13 @@ typedef struct {
  * (Engine::Init, engine.cpp:49-57). */
 int fdtd_engine_create(const fdtd_op_desc* desc, const fdtd_engine_opts* opts,
                        fdtd_engine_t* out);
+/* The upload half of fdtd_engine_create: device arrays from an already
+ * compressed operator (host -> device copies from pinned memory). */
+int fdtd_engine_create_compressed(fdtd_cop_t cop, const fdtd_engine_opts* opts,
+                                  fdtd_engine_t* out);
+/* Engine::Reset + Engine::Init without reallocation: fields, UPML flux and
+ * ADE states back to zero, numTS = 0, recorded samples dropped. */
+int fdtd_engine_reset(fdtd_engine_t eng);
 /* Engine::Reset (engine.cpp:98-106): frees device memory. */
 int fdtd_engine_destroy(fdtd_engine_t eng);
 
@@ -297,6 +330,13 @@ typedef struct {
 } fdtd_engine_stats;
 
 int fdtd_engine_get_stats(fdtd_engine_t eng, fdtd_engine_stats* st);
+
+/* Runs n_steps timesteps launching each half-step kernel individually with
+ * CUDA events around it on the engine stream; returns the mean duration of
+ * one voltage-kernel and one current-kernel launch (ms).  The simulation
+ * advances by n_steps exactly as fdtd_engine_iterate would. */
+int fdtd_engine_profile_kernels(fdtd_engine_t eng, uint32_t n_steps,
+                                double* ms_volt, double* ms_curr);
 
 /* Device time of the last iterate call's kernels, measured with CUDA events
  * on the engine stream (ms) and the number of kernel launches it issued. */

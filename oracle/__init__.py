@@ -10,7 +10,8 @@ from pathlib import Path
 
 import numpy as np
 
-from .build import LIB, build
+from .build import LIB
+from .build import build as build_lib
 
 _lib = None
 
@@ -21,7 +22,7 @@ SSE_COMPRESSED_MT = 1  # Engine_SSE_Compressed + Engine_Multithread
 def lib() -> C.CDLL:
     global _lib
     if _lib is None:
-        build()
+        build_lib()
         L = C.CDLL(str(LIB))
         L.oracle_run.restype = C.c_long
         L.oracle_run.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_uint, C.c_uint, C.c_int, C.c_int, C.c_int,

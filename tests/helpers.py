@@ -1,0 +1,90 @@
+"""Shared helpers of the test suite (comparison metrics and the frequency
+check of the reference's TESTSUITE)."""
+from __future__ import annotations
+
+import numpy as np
+
+
+def rel_l2(a, b) -> float:
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    n = np.linalg.norm(b)
+    if n == 0:
+        return float(np.linalg.norm(a))
+    return float(np.linalg.norm(a - b) / n)
+
+
+def rel_max(a, b) -> float:
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    m = np.max(np.abs(b))
+    if m == 0:
+        return float(np.max(np.abs(a)))
+    return float(np.max(np.abs(a - b)) / m)
+
+
+def fft_time2freq(t, val):
+    """matlab/FFT_time2freq.m: zero-padded single-sided spectrum."""
+    dt = t[1] - t[0]
+    L = len(t)
+    nfft = 1 << int(np.ceil(np.log2(L)))
+    v = np.fft.fft(val, nfft) * dt
+    f = 1 / (2 * dt) * np.linspace(0, 1, nfft // 2 + 1)
+    v = 2 * v[: nfft // 2 + 1]
+    return f, v
+
+
+def _nearest(f, x):
+    return int(np.argmin(np.abs(f - x)))
+
+
+def check_frequency(f, val, f_upper, f_lower, rel_amplitude, kind) -> bool:
+    """TESTSUITE/helperscripts/check_frequency.m."""
+    max1 = np.max(val)
+    for f1, f2 in zip(f_lower, f_upper):
+        i1, i2 = _nearest(f, f1), _nearest(f, f2)
+        seg = val[i1:i2 + 1]
+        if kind == "inside" and np.max(seg) < max1 * rel_amplitude:
+            return False
+        if kind == "outside" and np.max(seg) > max1 * rel_amplitude:
+            return False
+    return True
+
+
+def cavity_check(t_list, val_list, meta) -> dict:
+    """Analysis of TESTSUITE/combinedtests/cavity.m:125-214 on the probes
+    ut1x, ut1y, ut1z (time series); returns the four pass flags."""
+    c0 = 299792458.0
+    a, b, d = meta["a"], meta["b"], meta["d"]
+    f_start, f_stop = meta["f_start"], meta["f_stop"]
+    t_start = 7e-10
+    spec = []
+    for t, v in zip(t_list, val_list):
+        i0 = _nearest(t, t_start)
+        f, s = fft_time2freq(t[i0:], v[i0:])
+        spec.append((f, s))
+    f = spec[0][0]
+    i1, i2 = _nearest(f, f_start), _nearest(f, f_stop)
+    f = f[i1:i2 + 1]
+    uy = np.abs(spec[1][1][i1:i2 + 1])
+    uz = np.abs(spec[2][1][i1:i2 + 1])
+    k = lambda m, n, l: np.sqrt((m * np.pi / a) ** 2 + (n * np.pi / b) ** 2 + (l * np.pi / d) ** 2)
+    f_TE = np.array([c0 / (2 * np.pi) * k(*m) for m in [(1, 0, 1), (1, 0, 2), (2, 0, 1), (2, 0, 2)]])
+    f_TM = np.array([c0 / (2 * np.pi) * k(*m) for m in [(1, 1, 0), (1, 1, 1)]])
+    lower, upper, lower_TM, upper_TM = 1.3e-3, 1.3e-3, 2.5e-3, 0.0
+    min_amp, min_amp_TM, outer, max_amp = 0.6, 0.27, 0.02, 0.17
+
+    def outer_lims(fr):
+        temp = np.concatenate([[f_start], fr, [f_stop]])
+        o1 = temp[:-1] * (1 + outer)
+        o2 = temp[1:] * (1 - outer)
+        return o1, o2
+
+    o1, o2 = outer_lims(f_TE)
+    o1t, o2t = outer_lims(f_TM)
+    return dict(
+        te_inside=check_frequency(f, uy, f_TE * (1 + upper), f_TE * (1 - lower), min_amp, "inside"),
+        tm_inside=check_frequency(f, uz, f_TM * (1 + upper_TM), f_TM * (1 - lower_TM), min_amp_TM, "inside"),
+        te_outside=check_frequency(f, uy, o2, o1, max_amp, "outside"),
+        tm_outside=check_frequency(f, uz, o2t, o1t, max_amp, "outside"),
+    )

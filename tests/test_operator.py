@@ -1,0 +1,167 @@
+"""Host operator build (restated Operator::CalcECOperator and extension
+builds): closed-form known answers.  CPU only."""
+import math
+
+import numpy as np
+import pytest
+
+from wipems_gb300 import EPS0, MUE0, C0, CompressedOperator, Operator, Scene, scenes
+
+pytestmark = pytest.mark.usefixtures("libs")
+
+
+def f32(x):
+    return np.float32(x)
+
+
+def test_var3_timestep_is_courant_on_uniform_cube():
+    op = Operator(scenes.p64(nr_ts=100))
+    courant = 1e-3 / (C0 * math.sqrt(3))
+    assert abs(op.dT / courant - 1) < 1e-6
+
+
+def test_vacuum_coefficients_closed_form():
+    op = Operator(scenes.p64(nr_ts=100))
+    vv, vi, ii, iv = op.coefficients()
+    dT, d = op.dT, 1e-3
+    # interior edge: C = eps0*A/delta with A = delta^2 (float-rounded EC store)
+    C = float(np.float32(EPS0 * d * d / d))
+    L = float(np.float32(MUE0 * d * d / d))
+    assert vv[0, 10, 10, 10] == f32(1.0)
+    assert vi[0, 10, 10, 10] == f32((dT / C) / (1.0 + dT * 0.0 / 2.0 / C))
+    assert ii[2, 10, 10, 10] == f32(1.0)
+    assert iv[2, 10, 10, 10] == f32((dT / L) / 1.0)
+
+
+def test_pec_faces_and_last_current_lines():
+    op = Operator(scenes.p64(nr_ts=100))
+    vv, vi, ii, iv = op.coefficients()
+    # x = 0 face: tangential y/z voltages are PEC (operator.cpp:1086-1129)
+    assert not vi[1, 0].any() and not vi[2, 0].any()
+    assert vi[0, 0, 5, 5] != 0
+    # last lines: currents outside the domain are zero (operator.cpp:1160-1171)
+    assert not iv[:, -1].any() and not iv[:, :, -1].any() and not iv[:, :, :, -1].any()
+
+
+def test_gauss_signal_and_nyquist():
+    op = Operator(scenes.p64(nr_ts=2000))
+    sv, sc = op.signals()
+    dT, f0, fc = op.dT, 5e9, 5e9
+    n = np.arange(len(sv))
+    t = n * dT
+    ref = np.cos(2 * np.pi * f0 * (t - 9 / (2 * np.pi * fc))) * np.exp(-((2 * np.pi * fc * t / 3 - 3) ** 2))
+    assert np.array_equal(sv, ref.astype(np.float32))
+    t2 = t + 0.5 * dT
+    ref2 = np.cos(2 * np.pi * f0 * (t2 - 9 / (2 * np.pi * fc))) * np.exp(-((2 * np.pi * fc * t2 / 3 - 3) ** 2))
+    assert np.array_equal(sc, ref2.astype(np.float32))
+    assert len(sv) == math.ceil(2 * 9 / (2 * np.pi * fc) / dT)
+    assert op.nyquist == math.floor(1 / (f0 + fc) / 2 / dT)
+    assert op.probe_interval == op.nyquist // 4
+
+
+def test_p64_excitation_and_probe_snapping():
+    op = Operator(scenes.p64(nr_ts=100))
+    ex = op.excitation()
+    assert ex["index"].T.tolist() == [[32, 32, 32]] and ex["dir"].tolist() == [2]
+    assert ex["amp"][0] == np.float32(1e-3)
+    pv, pc = op.probes
+    assert list(pv.start) == [42, 32, 22] and list(pv.stop) == [42, 32, 42]
+    assert list(pc.start) == [31, 31, 32] and list(pc.stop) == [32, 32, 32] and pc.norm_dir == 2
+
+
+def test_lumped_port_conductance():
+    """Parallel R lumped element: G = (1/R/unitGC) * A/delta on the port edges
+    (operator.cpp:1535-1712), vv/vi recomputed from it; caps set PEC."""
+    L = scenes.uniform_lines(20, 1.0)
+    s = Scene(L, L, L, 1e-3)
+    s.set_boundary([0] * 6)
+    s.set_gauss_excite(5e9, 5e9, 100)
+    s.add_lumped_port([10, 10, 8], [11, 11, 12], 2, 50.0)
+    op = Operator(s)
+    vv, vi, _, _ = op.coefficients()
+    d = 1e-3
+    # 2x2 parallel edges per plane, 4 planes in series
+    plane = 4 * (d * d / d)
+    unitGC = 1 / (4 * (1 / plane))
+    kappa = 1 / 50.0 / unitGC
+    G = float(np.float32(kappa * d * d / d))
+    C = float(np.float32(EPS0 * d * d / d))
+    dT = op.dT
+    assert vv[2, 10, 10, 9] == f32((1.0 - dT * G / 2.0 / C) / (1.0 + dT * G / 2.0 / C))
+    assert vi[2, 10, 10, 9] == f32((dT / C) / (1.0 + dT * G / 2.0 / C))
+    # caps: x/y edges on the end planes are PEC
+    assert vi[0, 10, 10, 8] == 0 and vi[1, 10, 10, 12] == 0
+
+
+def test_upml_grading_closed_form():
+    """Operator_Ext_UPML with the default grading function
+    (operator_ext_upml.cpp:31, 289-466) at the outermost E-edge of the
+    x-lower slab."""
+    L = scenes.uniform_lines(30, 1.0)
+    s = Scene(L, L, L, 1e-3)
+    s.set_boundary([3] * 6, [8] * 6)
+    s.set_gauss_excite(5e9, 5e9, 100)
+    op = Operator(s)
+    assert op.info.num_upml == 6
+    vv, vi, _, _ = op.coefficients()
+    dT = op.dT
+    W = 8e-3
+    dl = W / 8
+    grad = lambda D: -math.log(1e-6) * math.log(2.5) / (2 * dl * 376.730313461 * (2.5 ** (W / dl) - 1)) * 2.5 ** (D / dl)
+    # y-edge at x=1 (in the x slab only, y/z interior): kappa_v[x] for an edge
+    # normal to x at depth W - 1mm  (n != ny -> no half-cell shift)
+    kx = grad(W - 1e-3)
+    # nP of y is z (no grading), so main vv = 1 and vi = 2eps0 dT/(2eps0) * d/A
+    assert vv[1, 1, 15, 15] == f32((2 * EPS0 - 0 * dT) / (2 * EPS0 + 0 * dT))
+    assert vi[1, 1, 15, 15] == f32((2 * EPS0 * dT) / (2 * EPS0) * 1e-3 / 1e-6)
+    # z-edge: nP = x -> graded main vv
+    assert vv[2, 1, 15, 15] == f32((2 * EPS0 - kx * dT) / (2 * EPS0 + kx * dT))
+
+
+def test_drude_coefficients_closed_form():
+    """Operator_Ext_LorentzMaterial for a Drude brick interior edge
+    (operator_ext_lorentzmaterial.cpp:231-351)."""
+    L = scenes.uniform_lines(20, 1.0)
+    s = Scene(L, L, L, 1e-3)
+    s.set_boundary([0] * 6)
+    s.set_gauss_excite(5e9, 5e9, 100)
+    fp, tau = 2e9, 1e-8
+    s.add_lorentz([5, 5, 5], [15, 15, 15], plasma_f=[fp], relax_t=[tau], pole_f=[0.0])
+    op = Operator(s)
+    d = op.desc
+    assert d.num_ade_orders == 1
+    a = d.ade[0]
+    cnt = a.count
+    pos = np.stack([np.ctypeslib.as_array(a.pos[k], shape=(cnt,)) for k in range(3)], 1)
+    i = int(np.where((pos == [10, 10, 10]).all(1))[0][0])
+    v_int = np.ctypeslib.as_array(a.v_int, shape=(3 * cnt,)).reshape(3, cnt)
+    v_ext = np.ctypeslib.as_array(a.v_ext, shape=(3 * cnt,)).reshape(3, cnt)
+    _, vi, _, _ = op.coefficients()
+    dT = op.dT
+    C = float(np.float32(EPS0 * 1e-3))
+    wp = fp * 2 * math.pi
+    LD = 1 / (wp * wp * C)
+    RD = LD / tau
+    assert v_int[0, i] == f32((2.0 * LD - dT * RD) / (2.0 * LD + dT * RD))
+    assert v_ext[0, i] == f32(dT / (LD + dT * RD / 2.0) * float(vi[0, 10, 10, 10]))
+    assert not a.volt_lor_on
+
+
+def test_compression_round_trip_all_features():
+    for kind in ("pec", "upml", "graded", "drude", "lorentz", "mixed"):
+        op = Operator(scenes.mini(kind))
+        cop = CompressedOperator(op)
+        ex = cop.expand()
+        for a, b in zip(ex[:4], op.coefficients()):
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), kind
+        fe = ex[4]
+        assert (cop.info["num_upml_nodes"] > 0) == (kind != "pec")
+        assert int(((fe & 1) != 0).sum()) == cop.info["num_upml_nodes"]
+        if kind in ("drude", "lorentz", "mixed"):
+            assert int(((fe & 2) != 0).sum()) == cop.info["num_ade_nodes"] > 0
+
+
+def test_uniform_mesh_fits_uint16_index():
+    op = Operator(scenes.l256(cells=96, n_bricks=40))
+    cop = CompressedOperator(op)
+    assert cop.info["index_bytes"] == 2

@@ -1,0 +1,57 @@
+"""The oracle itself, pinned without a GPU:
+  * its two engine restatements (basic Engine and the multithreaded
+    SSE-compressed engine) agree bitwise, the property the reference's
+    TESTSUITE/enginetests/cavity.m:144-167 demands of its own engines;
+  * the PEC cavity of TESTSUITE/combinedtests/cavity.m resonates at the
+    analytic TE/TM frequencies within the test's own limits;
+  * golden fixtures committed under tests/golden (generated by
+    tests/golden/make_golden.py) are reproduced.
+"""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle
+from wipems_gb300 import Operator, scenes
+
+from helpers import cavity_check
+
+pytestmark = pytest.mark.usefixtures("libs")
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+@pytest.mark.parametrize("kind", ["pec", "upml", "drude", "lorentz", "mixed"])
+def test_basic_and_sse_compressed_engines_agree_bitwise(kind):
+    op = Operator(scenes.mini(kind, nr_ts=200))
+    a = oracle.run(op.desc, op.probes, 150, op.probe_interval, engine=oracle.BASIC)
+    b = oracle.run(op.desc, op.probes, 150, op.probe_interval, engine=oracle.SSE_COMPRESSED_MT, threads=3)
+    assert np.array_equal(a["volt"].view(np.uint32), b["volt"].view(np.uint32))
+    assert np.array_equal(a["curr"].view(np.uint32), b["curr"].view(np.uint32))
+    assert np.array_equal(a["values"], b["values"])
+    assert np.abs(a["volt"]).max() > 0
+
+
+def test_cavity_resonances_within_reference_limits():
+    sc = scenes.cavity(nr_ts=20000)
+    op = Operator(sc)
+    r = oracle.run(op.desc, op.probes, 20000, 1, engine=oracle.SSE_COMPRESSED_MT, threads=8, energy=False,
+                   fields=False)
+    t = r["ts"] * op.dT
+    res = cavity_check([t] * 3, [r["values"][:, k] for k in range(3)], sc.meta)
+    assert all(res.values()), res
+
+
+@pytest.mark.parametrize("name", ["p64_200", "mini_upml_150", "mini_mixed_120"])
+def test_golden_fixtures(name):
+    meta = json.loads((GOLDEN / f"{name}.json").read_text())
+    data = np.load(GOLDEN / f"{name}.npz")
+    kind, nsteps = meta["scene"], meta["steps"]
+    sc = scenes.p64(nr_ts=meta["nr_ts"]) if kind == "p64" else scenes.mini(kind, nr_ts=meta["nr_ts"])
+    op = Operator(sc)
+    r = oracle.run(op.desc, op.probes, nsteps, op.probe_interval, engine=oracle.BASIC)
+    assert np.array_equal(r["values"], data["values"])
+    assert np.array_equal(r["energy"], data["energy"])
+    crc = int(np.bitwise_xor.reduce(r["volt"].view(np.uint32).ravel()))
+    assert crc == meta["volt_xor"]

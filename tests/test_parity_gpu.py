@@ -1,0 +1,131 @@
+"""GPU parity: the CUDA engine (through the C ABI) against the oracle.
+
+Bar (BASELINE the benchmark spec): probe series within 1e-5 relative L2, final
+fields within 1e-4 relative max-norm.  The kernels keep the reference's
+FP32 operation order, so fields are in fact required to be bit-identical;
+probe sums differ only by reduction order (device warp sums in double vs the
+reference's sequential double / float accumulation), energy likewise.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from wipems_gb300 import CompressedOperator, Engine, Operator, scenes
+
+from helpers import cavity_check, rel_l2, rel_max
+
+pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("libs")]
+
+PROBE_TOL = 1e-5
+FIELD_TOL = 1e-4
+
+
+def compare(op, eng, ref, bitwise=True):
+    s = eng.samples()
+    assert np.array_equal(s.ts, ref["ts"]), (s.ts[:5], ref["ts"][:5])
+    for p in range(s.values.shape[1]):
+        assert rel_l2(s.values[:, p], ref["values"][:, p]) <= PROBE_TOL, p
+    e_ok = ref["energy"] > 0
+    if e_ok.any():
+        assert np.max(np.abs(s.energy[e_ok] / ref["energy"][e_ok] - 1)) < 1e-6
+    V, I = eng.fields()
+    assert rel_max(V, ref["volt"]) <= FIELD_TOL
+    assert rel_max(I, ref["curr"]) <= FIELD_TOL
+    if bitwise:
+        dv = int((V.view(np.uint32) != ref["volt"].view(np.uint32)).sum())
+        di = int((I.view(np.uint32) != ref["curr"].view(np.uint32)).sum())
+        assert dv == 0 and di == 0, (dv, di, rel_max(V, ref["volt"]), rel_max(I, ref["curr"]))
+
+
+@pytest.mark.parametrize("kind", ["pec", "upml", "graded", "drude", "lorentz", "mixed"])
+def test_mini_scenes_match_oracle(kind):
+    op = Operator(scenes.mini(kind, nr_ts=400))
+    ref = oracle.run(op.desc, op.probes, 400, op.probe_interval, engine=oracle.BASIC)
+    eng = Engine(op)
+    eng.iterate(400)
+    compare(op, eng, ref)
+
+
+def test_p64_full_2000_steps():
+    op = Operator(scenes.p64(nr_ts=2000))
+    ref = oracle.run(op.desc, op.probes, 2000, op.probe_interval, engine=oracle.SSE_COMPRESSED_MT,
+                     threads=os.cpu_count())
+    eng = Engine(op)
+    eng.iterate(2000)
+    compare(op, eng, ref)
+
+
+def test_chunking_graphs_and_tiles_are_invisible():
+    op = Operator(scenes.mini("upml", nr_ts=300))
+    base = Engine(op, use_graphs=False)
+    base.iterate(300)
+    V0, I0 = base.fields()
+    s0 = base.samples()
+    for kw, chunks in [(dict(use_graphs=True), [300]), (dict(use_graphs=True), [7, 1, 50, 242]),
+                       (dict(tile_y=4, x_chunk=5), [300]), (dict(tile_y=1, x_chunk=64), [100, 200])]:
+        e = Engine(op, **kw)
+        for c in chunks:
+            e.iterate(c)
+        V, I = e.fields()
+        assert np.array_equal(V.view(np.uint32), V0.view(np.uint32)), kw
+        assert np.array_equal(I.view(np.uint32), I0.view(np.uint32)), kw
+        s = e.samples()
+        assert np.array_equal(s.ts, s0.ts)
+        assert np.allclose(s.values, s0.values, rtol=0, atol=0), kw
+
+
+def test_reset_and_compressed_upload_reproduce():
+    op = Operator(scenes.mini("mixed", nr_ts=200))
+    cop = CompressedOperator(op)
+    e1 = Engine(cop)
+    e1.iterate(200)
+    V1, I1 = e1.fields()
+    s1 = e1.samples()
+    e1.reset()
+    assert e1.num_timesteps == 0
+    e1.iterate(200)
+    V2, I2 = e1.fields()
+    assert np.array_equal(V1, V2) and np.array_equal(I1, I2)
+    assert np.array_equal(e1.samples().values, s1.values)
+    e2 = Engine(op)
+    e2.iterate(200)
+    assert np.array_equal(e2.fields()[0], V1)
+
+
+def test_l256_full_size_first_steps_bitwise():
+    op = Operator(scenes.l256(nr_ts=1000))
+    n = 18
+    ref = oracle.run(op.desc, op.probes, n, op.probe_interval, engine=oracle.SSE_COMPRESSED_MT,
+                     threads=os.cpu_count())
+    eng = Engine(op)
+    st = eng.stats()
+    assert st["index_bytes"] == 2
+    eng.iterate(n)
+    compare(op, eng, ref)
+
+
+def test_cavity_resonances_on_gpu():
+    sc = scenes.cavity(nr_ts=20000)
+    op = Operator(sc)
+    eng = Engine(op, probe_interval=1, max_timesteps=20000)
+    eng.iterate(20000)
+    s = eng.samples()
+    t = s.ts * op.dT
+    res = cavity_check([t] * 3, [s.values[:, k] for k in range(3)], sc.meta)
+    assert all(res.values()), res
+
+
+def test_field_access_and_energy():
+    op = Operator(scenes.mini("pec", nr_ts=100))
+    eng = Engine(op)
+    eng.iterate(60)
+    V, I = eng.fields()
+    assert eng.get_volt(2, 10, 8, 18) == V[2, 10, 8, 18]
+    assert eng.get_curr(1, 5, 6, 7) == I[1, 5, 6, 7]
+    ref = oracle.run(op.desc, [], 60, 0, engine=oracle.BASIC)
+    eps0, mue0 = 8.85418781762e-12, 1.256637062e-6
+    Vr, Ir = ref["volt"][:, :-1, :-1, :-1].astype(np.float64), ref["curr"][:, :-1, :-1, :-1].astype(np.float64)
+    e_ref = eps0 * np.sum(Vr * Vr) + mue0 * np.sum(Ir * Ir)
+    assert abs(eng.energy() / e_ref - 1) < 1e-6

@@ -67,6 +67,11 @@ class FdtdEngineStats(C.Structure):
                 ("tile_y", u32), ("x_chunk", u32)]
 
 
+class FdtdCopInfo(C.Structure):
+    _fields_ = [("num_lines", u32 * 3), ("num_tuples", u32), ("index_bytes", u32), ("padded_nz", u32),
+                ("num_upml_nodes", u32), ("num_ade_nodes", u32), ("host_bytes", C.c_uint64), ("pinned", C.c_int)]
+
+
 class FdtdError(RuntimeError):
     def __init__(self, code: int, where: str, msg: str):
         super().__init__(f"{where} failed ({code}): {msg}")
@@ -98,7 +103,13 @@ SIGNATURES = [
     ("fdtd_operator_get_info", C.c_int, [_P, C.POINTER(FdtdOperatorInfo)]),
     ("fdtd_operator_describe", C.c_int, [_P, C.POINTER(FdtdOpDesc)]),
     ("fdtd_operator_get_probe", C.c_int, [_P, u32, C.POINTER(FdtdProbeDesc)]),
+    ("fdtd_compress", C.c_int, [C.POINTER(FdtdOpDesc), C.POINTER(_P)]),
+    ("fdtd_cop_destroy", C.c_int, [_P]),
+    ("fdtd_cop_get_info", C.c_int, [_P, C.POINTER(FdtdCopInfo)]),
+    ("fdtd_cop_expand", C.c_int, [_P, PF, PF, PF, PF, PU32, PU32]),
     ("fdtd_engine_create", C.c_int, [C.POINTER(FdtdOpDesc), C.POINTER(FdtdEngineOpts), C.POINTER(_P)]),
+    ("fdtd_engine_create_compressed", C.c_int, [_P, C.POINTER(FdtdEngineOpts), C.POINTER(_P)]),
+    ("fdtd_engine_reset", C.c_int, [_P]),
     ("fdtd_engine_destroy", C.c_int, [_P]),
     ("fdtd_engine_add_probe", C.c_int, [_P, C.POINTER(FdtdProbeDesc), PU32]),
     ("fdtd_engine_iterate", C.c_int, [_P, u32]),
@@ -111,6 +122,7 @@ SIGNATURES = [
     ("fdtd_engine_get_curr", C.c_int, [_P, u32, u32, u32, u32, PF]),
     ("fdtd_engine_get_stats", C.c_int, [_P, C.POINTER(FdtdEngineStats)]),
     ("fdtd_engine_last_timing", C.c_int, [_P, PD, C.POINTER(C.c_uint64)]),
+    ("fdtd_engine_profile_kernels", C.c_int, [_P, u32, PD, PD]),
 ]
 
 

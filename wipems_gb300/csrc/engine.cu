@@ -129,6 +129,7 @@ struct fdtd_engine_s {
     // state
     uint32_t ts = 0;
     bool started = false;
+    bool need_initial_sample = true;
     int feat = 0;
     bool idx16 = true;
     int TY = 8;
@@ -499,13 +500,46 @@ void pack4(std::vector<float4>& out, size_t entry, int per, const float* vals, i
     for (int k = 0; k < nvals; ++k) f[k] = vals[k];
 }
 
-int create_engine(const fdtd_op_desc* d, const fdtd_engine_opts* opts, fdtd_engine_s* e) {
+}  // namespace
+}  // namespace wipems
+
+// Host-side compressed operator: per-node tuple index (padded device layout)
+// plus the coefficient tables, ready to be copied to the device.
+struct fdtd_cop_s {
+    uint32_t N[3] = {0, 0, 0};
+    int Nzp = 0;
+    long long comp = 0;
+    bool idx16 = true;
+    uint8_t* idx = nullptr;  // pinned when a CUDA device is present
+    bool idx_pinned = false;
+    size_t idx_bytes = 0;
+    std::vector<float4> hE, hH, hEU, hHU, hEA, hHA, hEX, hHX;
+    std::vector<float> sigV, sigC;
+    uint32_t sig_len = 0, sig_period = 0;
+    int feat = 0;
+    bool any_upml = false, any_ade_e = false, any_ade_h = false, any_lor_e = false, any_lor_h = false;
+    uint32_t num_tuples = 0, upml_nodes = 0, ade_nodes = 0;
+    double dT = 0;
+    ~fdtd_cop_s() {
+        if (idx) {
+            if (idx_pinned)
+                cudaFreeHost(idx);
+            else
+                std::free(idx);
+        }
+    }
+};
+
+namespace wipems {
+namespace {
+
+int compress_op(const fdtd_op_desc* d, fdtd_cop_s* c) {
     for (int a = 0; a < 3; ++a) {
         if (d->num_lines[a] < 2) {
             set_error("every axis needs at least two lines");
             return FDTD_ERR_ARG;
         }
-        e->N[a] = d->num_lines[a];
+        c->N[a] = d->num_lines[a];
     }
     if (!d->vv || !d->vi || !d->ii || !d->iv) {
         set_error("coefficient arrays missing");
@@ -515,7 +549,122 @@ int create_engine(const fdtd_op_desc* d, const fdtd_engine_opts* opts, fdtd_engi
         set_error("excitation points without an excitation signal");
         return FDTD_ERR_ARG;
     }
-    e->dT = d->dT;
+    c->dT = d->dT;
+    fdtd_engine_s dummy;  // receives node counts
+    std::vector<uint32_t> node_idx;
+    std::vector<Tuple> tuples;
+    int threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    int rc = compress(d, &dummy, node_idx, tuples, threads);
+    if (rc) return rc;
+    c->upml_nodes = dummy.upml_nodes;
+    c->ade_nodes = dummy.ade_nodes;
+    c->num_tuples = (uint32_t)tuples.size();
+    c->idx16 = tuples.size() <= 65536;
+    const uint32_t Nx = c->N[0], Ny = c->N[1], Nz = c->N[2];
+    c->Nzp = (int)((Nz + 31) / 32 * 32);
+    c->comp = (long long)Nx * Ny * c->Nzp;
+    for (const Tuple& t : tuples) {
+        c->any_upml |= (t.fe & TF_UPML) != 0;
+        c->any_ade_e |= (t.fe & TF_ADE) != 0;
+        c->any_ade_h |= (t.fh & TF_ADE) != 0;
+        c->any_lor_e |= (t.fe & TF_LOR) != 0;
+        c->any_lor_h |= (t.fh & TF_LOR) != 0;
+    }
+    c->feat = (c->any_upml ? FEAT_UPML : 0) | ((c->any_ade_e || c->any_ade_h) ? FEAT_ADE : 0);
+    const size_t T = tuples.size();
+    const float4 z4 = make_float4(0, 0, 0, 0);
+    c->hE.assign(2 * T, z4);
+    c->hH.assign(2 * T, z4);
+    c->hEX.assign(2 * T, z4);
+    c->hHX.assign(2 * T, z4);
+    if (c->any_upml) {
+        c->hEU.assign(3 * T, z4);
+        c->hHU.assign(3 * T, z4);
+    }
+    if (c->feat & FEAT_ADE) {
+        c->hEA.assign(3 * T, z4);
+        c->hHA.assign(3 * T, z4);
+    }
+    for (size_t k = 0; k < T; ++k) {
+        const Tuple& t = tuples[k];
+        float e8[8] = {t.e[0], t.e[1], t.e[2], t.e[3], t.e[4], t.e[5], 0, 0};
+        std::memcpy(&e8[6], &t.fe, 4);
+        pack4(c->hE, k, 2, e8, 8);
+        float h8[8] = {t.h[0], t.h[1], t.h[2], t.h[3], t.h[4], t.h[5], 0, 0};
+        std::memcpy(&h8[6], &t.fh, 4);
+        pack4(c->hH, k, 2, h8, 8);
+        if (c->any_upml) {
+            pack4(c->hEU, k, 3, t.eu, 9);
+            pack4(c->hHU, k, 3, t.hu, 9);
+        }
+        if (c->feat & FEAT_ADE) {
+            pack4(c->hEA, k, 3, t.ea, 9);
+            pack4(c->hHA, k, 3, t.ha, 9);
+        }
+        float x8[8] = {t.ex[0], t.ex[1], t.ex[2], 0, 0, 0, 0, 0};
+        std::memcpy(&x8[4], t.exd, 12);
+        pack4(c->hEX, k, 2, x8, 8);
+        float y8[8] = {t.hx[0], t.hx[1], t.hx[2], 0, 0, 0, 0, 0};
+        std::memcpy(&y8[4], t.hxd, 12);
+        pack4(c->hHX, k, 2, y8, 8);
+    }
+    const size_t ib = c->idx16 ? 2 : 4;
+    c->idx_bytes = (size_t)c->comp * ib;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) == cudaSuccess && ndev > 0 &&
+        cudaMallocHost(reinterpret_cast<void**>(&c->idx), c->idx_bytes) == cudaSuccess) {
+        c->idx_pinned = true;
+    } else {
+        cudaGetLastError();  // clear the sticky "no device" error of the probe
+        c->idx = static_cast<uint8_t*>(std::malloc(c->idx_bytes));
+        if (!c->idx) {
+            set_error("host allocation of the tuple index failed");
+            return FDTD_ERR_NOMEM;
+        }
+    }
+    std::memset(c->idx, 0, c->idx_bytes);
+    for (uint32_t x = 0; x < Nx; ++x)
+        for (uint32_t y = 0; y < Ny; ++y) {
+            const size_t src = ((size_t)x * Ny + y) * Nz;
+            const size_t dst = ((size_t)x * Ny + y) * c->Nzp;
+            if (c->idx16) {
+                uint16_t* p = reinterpret_cast<uint16_t*>(c->idx) + dst;
+                for (uint32_t z = 0; z < Nz; ++z) p[z] = (uint16_t)node_idx[src + z];
+            } else {
+                uint32_t* p = reinterpret_cast<uint32_t*>(c->idx) + dst;
+                for (uint32_t z = 0; z < Nz; ++z) p[z] = node_idx[src + z];
+            }
+        }
+    c->sig_len = d->signal_length;
+    c->sig_period = d->signal_period_ts;
+    if (d->signal_length) {
+        c->sigV.assign(d->signal_volt, d->signal_volt + d->signal_length);
+        c->sigC.assign(d->signal_curr, d->signal_curr + d->signal_length);
+    }
+    return FDTD_OK;
+}
+
+// Engine::Init state: all fields and extension states zero, numTS = 0,
+// no recorded samples (the ts = 0 sample is taken again on the next iterate).
+int reset_state(fdtd_engine_s* e) {
+    cudaStream_t s = e->stream;
+    const size_t F = 3 * (size_t)e->comp * sizeof(float);
+    for (DevBuf<float>* b : {&e->V, &e->I, &e->FV, &e->FI, &e->AV, &e->LV, &e->AI, &e->LI})
+        if (b->p) CK(cudaMemsetAsync(b->p, 0, F, s));
+    CK(cudaMemsetAsync(e->d_ts.p, 0, sizeof(int), s));
+    CK(cudaMemsetAsync(e->d_eacc.p, 0, 2 * sizeof(double), s));
+    CK(cudaMemsetAsync(e->d_nsamp.p, 0, sizeof(int), s));
+    CK(cudaMemsetAsync(e->d_err.p, 0, sizeof(int), s));
+    e->ts = 0;
+    e->need_initial_sample = true;
+    return FDTD_OK;
+}
+
+// Operator::CreateEngine + Engine::Init for the CUDA engine: allocate the
+// device arrays (fields start at zero) and copy the compressed operator.
+int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine_s* e) {
+    for (int a = 0; a < 3; ++a) e->N[a] = c->N[a];
+    e->dT = c->dT;
     e->device = opts ? opts->device : 0;
     CK(cudaSetDevice(e->device));
     CK(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
@@ -532,139 +681,62 @@ int create_engine(const fdtd_op_desc* d, const fdtd_engine_opts* opts, fdtd_engi
     e->use_graphs = opts ? opts->use_graphs != 0 : true;
     uint32_t maxts = (opts && opts->max_timesteps) ? opts->max_timesteps : 100000;
     e->cap = (e->interval ? maxts / e->interval : 0) + 2;
-
-    std::vector<uint32_t> node_idx;
-    std::vector<Tuple> tuples;
-    int threads = (int)std::max(1u, std::thread::hardware_concurrency());
-    int rc = compress(d, e, node_idx, tuples, threads);
-    if (rc) return rc;
-    e->num_tuples = (uint32_t)tuples.size();
-    e->idx16 = tuples.size() <= 65536;
-
+    e->num_tuples = c->num_tuples;
+    e->upml_nodes = c->upml_nodes;
+    e->ade_nodes = c->ade_nodes;
+    e->idx16 = c->idx16;
+    e->feat = c->feat;
+    e->Nzp = c->Nzp;
+    e->comp = c->comp;
     const uint32_t Nx = e->N[0], Ny = e->N[1], Nz = e->N[2];
-    e->Nzp = (int)((Nz + 31) / 32 * 32);
-    e->comp = (long long)Nx * Ny * e->Nzp;
-    const size_t NN = (size_t)Nx * Ny * Nz;
 
-    bool any_upml = false, any_ade_e = false, any_ade_h = false, any_lor_e = false, any_lor_h = false;
-    for (const Tuple& t : tuples) {
-        any_upml |= (t.fe & TF_UPML) != 0;
-        any_ade_e |= (t.fe & TF_ADE) != 0;
-        any_ade_h |= (t.fh & TF_ADE) != 0;
-        any_lor_e |= (t.fe & TF_LOR) != 0;
-        any_lor_h |= (t.fh & TF_LOR) != 0;
-    }
-    e->feat = (any_upml ? FEAT_UPML : 0) | ((any_ade_e || any_ade_h) ? FEAT_ADE : 0);
-
-    // tables
-    const size_t T = tuples.size();
-    std::vector<float4> hE(2 * T), hH(2 * T), hEU, hHU, hEA, hHA, hEX(2 * T), hHX(2 * T);
-    std::memset(hE.data(), 0, hE.size() * sizeof(float4));
-    std::memset(hH.data(), 0, hH.size() * sizeof(float4));
-    std::memset(hEX.data(), 0, hEX.size() * sizeof(float4));
-    std::memset(hHX.data(), 0, hHX.size() * sizeof(float4));
-    if (any_upml) {
-        hEU.assign(3 * T, make_float4(0, 0, 0, 0));
-        hHU.assign(3 * T, make_float4(0, 0, 0, 0));
-    }
-    if (e->feat & FEAT_ADE) {
-        hEA.assign(3 * T, make_float4(0, 0, 0, 0));
-        hHA.assign(3 * T, make_float4(0, 0, 0, 0));
-    }
-    for (size_t k = 0; k < T; ++k) {
-        const Tuple& t = tuples[k];
-        float e8[8] = {t.e[0], t.e[1], t.e[2], t.e[3], t.e[4], t.e[5], 0, 0};
-        std::memcpy(&e8[6], &t.fe, 4);
-        pack4(hE, k, 2, e8, 8);
-        float h8[8] = {t.h[0], t.h[1], t.h[2], t.h[3], t.h[4], t.h[5], 0, 0};
-        std::memcpy(&h8[6], &t.fh, 4);
-        pack4(hH, k, 2, h8, 8);
-        if (any_upml) {
-            pack4(hEU, k, 3, t.eu, 9);
-            pack4(hHU, k, 3, t.hu, 9);
-        }
-        if (e->feat & FEAT_ADE) {
-            pack4(hEA, k, 3, t.ea, 9);
-            pack4(hHA, k, 3, t.ha, 9);
-        }
-        float x8[8] = {t.ex[0], t.ex[1], t.ex[2], 0, 0, 0, 0, 0};
-        std::memcpy(&x8[4], t.exd, 12);
-        pack4(hEX, k, 2, x8, 8);
-        float y8[8] = {t.hx[0], t.hx[1], t.hx[2], 0, 0, 0, 0, 0};
-        std::memcpy(&y8[4], t.hxd, 12);
-        pack4(hHX, k, 2, y8, 8);
-    }
-
+    int rc;
     uint64_t& tot = e->device_bytes;
     const size_t F = 3 * (size_t)e->comp;
     if ((rc = e->V.alloc(F, tot)) || (rc = e->I.alloc(F, tot))) return rc;
-    if (any_upml && ((rc = e->FV.alloc(F, tot)) || (rc = e->FI.alloc(F, tot)))) return rc;
-    if (any_ade_e && (rc = e->AV.alloc(F, tot))) return rc;
-    if (any_lor_e && (rc = e->LV.alloc(F, tot))) return rc;
-    if (any_ade_h && (rc = e->AI.alloc(F, tot))) return rc;
-    if (any_lor_h && (rc = e->LI.alloc(F, tot))) return rc;
-    const size_t ib = e->idx16 ? 2 : 4;
-    if ((rc = e->idx.alloc((size_t)e->comp * ib, tot))) return rc;
-    if ((rc = e->tabE.alloc(hE.size(), tot)) || (rc = e->tabH.alloc(hH.size(), tot)) ||
-        (rc = e->tabEX.alloc(hEX.size(), tot)) || (rc = e->tabHX.alloc(hHX.size(), tot)))
+    if (c->any_upml && ((rc = e->FV.alloc(F, tot)) || (rc = e->FI.alloc(F, tot)))) return rc;
+    if (c->any_ade_e && (rc = e->AV.alloc(F, tot))) return rc;
+    if (c->any_lor_e && (rc = e->LV.alloc(F, tot))) return rc;
+    if (c->any_ade_h && (rc = e->AI.alloc(F, tot))) return rc;
+    if (c->any_lor_h && (rc = e->LI.alloc(F, tot))) return rc;
+    if ((rc = e->idx.alloc(c->idx_bytes, tot))) return rc;
+    if ((rc = e->tabE.alloc(c->hE.size(), tot)) || (rc = e->tabH.alloc(c->hH.size(), tot)) ||
+        (rc = e->tabEX.alloc(c->hEX.size(), tot)) || (rc = e->tabHX.alloc(c->hHX.size(), tot)))
         return rc;
-    if (any_upml && ((rc = e->tabEU.alloc(hEU.size(), tot)) || (rc = e->tabHU.alloc(hHU.size(), tot)))) return rc;
-    if ((e->feat & FEAT_ADE) && ((rc = e->tabEA.alloc(hEA.size(), tot)) || (rc = e->tabHA.alloc(hHA.size(), tot))))
+    if (c->any_upml && ((rc = e->tabEU.alloc(c->hEU.size(), tot)) || (rc = e->tabHU.alloc(c->hHU.size(), tot))))
         return rc;
-    uint32_t sl = std::max<uint32_t>(1, d->signal_length);
+    if ((c->feat & FEAT_ADE) && ((rc = e->tabEA.alloc(c->hEA.size(), tot)) || (rc = e->tabHA.alloc(c->hHA.size(), tot))))
+        return rc;
+    uint32_t sl = std::max<uint32_t>(1, c->sig_len);
     if ((rc = e->sigV.alloc(sl, tot)) || (rc = e->sigC.alloc(sl, tot))) return rc;
     if ((rc = e->d_ts.alloc(1, tot)) || (rc = e->d_eacc.alloc(2, tot)) || (rc = e->d_energy_tmp.alloc(2, tot)) ||
         (rc = e->d_nsamp.alloc(1, tot)) || (rc = e->d_err.alloc(1, tot)))
         return rc;
 
     cudaStream_t s = e->stream;
-    CK(cudaMemsetAsync(e->V.p, 0, F * sizeof(float), s));
-    CK(cudaMemsetAsync(e->I.p, 0, F * sizeof(float), s));
-    for (DevBuf<float>* b : {&e->FV, &e->FI, &e->AV, &e->LV, &e->AI, &e->LI})
-        if (b->p) CK(cudaMemsetAsync(b->p, 0, F * sizeof(float), s));
-    CK(cudaMemsetAsync(e->d_ts.p, 0, sizeof(int), s));
-    CK(cudaMemsetAsync(e->d_eacc.p, 0, 2 * sizeof(double), s));
-    CK(cudaMemsetAsync(e->d_nsamp.p, 0, sizeof(int), s));
-    CK(cudaMemsetAsync(e->d_err.p, 0, sizeof(int), s));
-
-    // index in the padded device layout
-    {
-        std::vector<uint8_t> hidx((size_t)e->comp * ib, 0);
-        for (uint32_t x = 0; x < Nx; ++x)
-            for (uint32_t y = 0; y < Ny; ++y) {
-                const size_t src = ((size_t)x * Ny + y) * Nz;
-                const size_t dst = ((size_t)x * Ny + y) * e->Nzp;
-                if (e->idx16) {
-                    uint16_t* p = reinterpret_cast<uint16_t*>(hidx.data()) + dst;
-                    for (uint32_t z = 0; z < Nz; ++z) p[z] = (uint16_t)node_idx[src + z];
-                } else {
-                    uint32_t* p = reinterpret_cast<uint32_t*>(hidx.data()) + dst;
-                    for (uint32_t z = 0; z < Nz; ++z) p[z] = node_idx[src + z];
-                }
-            }
-        CK(cudaMemcpyAsync(e->idx.p, hidx.data(), hidx.size(), cudaMemcpyHostToDevice, s));
-        CK(cudaMemcpyAsync(e->tabE.p, hE.data(), hE.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
-        CK(cudaMemcpyAsync(e->tabH.p, hH.data(), hH.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
-        CK(cudaMemcpyAsync(e->tabEX.p, hEX.data(), hEX.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
-        CK(cudaMemcpyAsync(e->tabHX.p, hHX.data(), hHX.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
-        if (any_upml) {
-            CK(cudaMemcpyAsync(e->tabEU.p, hEU.data(), hEU.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
-            CK(cudaMemcpyAsync(e->tabHU.p, hHU.data(), hHU.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
-        }
-        if (e->feat & FEAT_ADE) {
-            CK(cudaMemcpyAsync(e->tabEA.p, hEA.data(), hEA.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
-            CK(cudaMemcpyAsync(e->tabHA.p, hHA.data(), hHA.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
-        }
-        if (d->signal_length) {
-            CK(cudaMemcpyAsync(e->sigV.p, d->signal_volt, d->signal_length * sizeof(float), cudaMemcpyHostToDevice, s));
-            CK(cudaMemcpyAsync(e->sigC.p, d->signal_curr, d->signal_length * sizeof(float), cudaMemcpyHostToDevice, s));
-        } else {
-            CK(cudaMemsetAsync(e->sigV.p, 0, sizeof(float), s));
-            CK(cudaMemsetAsync(e->sigC.p, 0, sizeof(float), s));
-        }
-        CK(cudaStreamSynchronize(s));
+    auto h2d = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+        return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s) : cudaSuccess;
+    };
+    CK(h2d(e->idx.p, c->idx, c->idx_bytes));
+    CK(h2d(e->tabE.p, c->hE.data(), c->hE.size() * sizeof(float4)));
+    CK(h2d(e->tabH.p, c->hH.data(), c->hH.size() * sizeof(float4)));
+    CK(h2d(e->tabEX.p, c->hEX.data(), c->hEX.size() * sizeof(float4)));
+    CK(h2d(e->tabHX.p, c->hHX.data(), c->hHX.size() * sizeof(float4)));
+    if (c->any_upml) {
+        CK(h2d(e->tabEU.p, c->hEU.data(), c->hEU.size() * sizeof(float4)));
+        CK(h2d(e->tabHU.p, c->hHU.data(), c->hHU.size() * sizeof(float4)));
     }
-    (void)NN;
+    if (c->feat & FEAT_ADE) {
+        CK(h2d(e->tabEA.p, c->hEA.data(), c->hEA.size() * sizeof(float4)));
+        CK(h2d(e->tabHA.p, c->hHA.data(), c->hHA.size() * sizeof(float4)));
+    }
+    if (c->sig_len) {
+        CK(h2d(e->sigV.p, c->sigV.data(), c->sig_len * sizeof(float)));
+        CK(h2d(e->sigC.p, c->sigC.data(), c->sig_len * sizeof(float)));
+    } else {
+        CK(cudaMemsetAsync(e->sigV.p, 0, sizeof(float), s));
+        CK(cudaMemsetAsync(e->sigC.p, 0, sizeof(float), s));
+    }
 
     DevGrid& g = e->g;
     g.Nx = (int)Nx;
@@ -692,12 +764,12 @@ int create_engine(const fdtd_op_desc* d, const fdtd_engine_opts* opts, fdtd_engi
     g.tabHX = e->tabHX.p;
     g.sigV = e->sigV.p;
     g.sigC = e->sigC.p;
-    g.sig_len = (int)d->signal_length;
-    g.sig_period = (int)d->signal_period_ts;
+    g.sig_len = (int)c->sig_len;
+    g.sig_period = (int)c->sig_period;
     g.d_ts = e->d_ts.p;
     g.d_eacc = e->d_eacc.p;
     e->smem_bytes = 2 * 3 * (size_t)(e->TY + 1) * 33 * sizeof(float);
-    return FDTD_OK;
+    return reset_state(e);
 }
 
 // Probe entries for ProcessVoltage (Engine_Interface_FDTD::CalcVoltageIntegral,
@@ -783,19 +855,87 @@ int probe_entries(const fdtd_engine_s* e, const fdtd_probe_desc* p, std::vector<
 // ===================================================================== C ABI
 extern "C" {
 
-int fdtd_engine_create(const fdtd_op_desc* desc, const fdtd_engine_opts* opts, fdtd_engine_t* out) {
+int fdtd_compress(const fdtd_op_desc* desc, fdtd_cop_t* out) {
     if (!desc || !out) {
-        set_error("fdtd_engine_create: null argument");
+        set_error("fdtd_compress: null argument");
+        return FDTD_ERR_ARG;
+    }
+    fdtd_cop_s* c = new (std::nothrow) fdtd_cop_s();
+    if (!c) return FDTD_ERR_NOMEM;
+    int rc;
+    try {
+        rc = compress_op(desc, c);
+    } catch (const std::bad_alloc&) {
+        set_error("fdtd_compress: host allocation failed");
+        rc = FDTD_ERR_NOMEM;
+    }
+    if (rc != FDTD_OK) {
+        delete c;
+        return rc;
+    }
+    *out = c;
+    return FDTD_OK;
+}
+
+int fdtd_cop_destroy(fdtd_cop_t c) {
+    delete c;
+    return FDTD_OK;
+}
+
+int fdtd_cop_get_info(fdtd_cop_t c, fdtd_cop_info* info) {
+    if (!c || !info) return FDTD_ERR_ARG;
+    std::memset(info, 0, sizeof(*info));
+    for (int a = 0; a < 3; ++a) info->num_lines[a] = c->N[a];
+    info->num_tuples = c->num_tuples;
+    info->index_bytes = c->idx16 ? 2 : 4;
+    info->padded_nz = (uint32_t)c->Nzp;
+    info->num_upml_nodes = c->upml_nodes;
+    info->num_ade_nodes = c->ade_nodes;
+    info->host_bytes = c->idx_bytes + (c->hE.size() + c->hH.size() + c->hEU.size() + c->hHU.size() + c->hEA.size() +
+                                       c->hHA.size() + c->hEX.size() + c->hHX.size()) * sizeof(float4);
+    info->pinned = c->idx_pinned ? 1 : 0;
+    return FDTD_OK;
+}
+
+int fdtd_cop_expand(fdtd_cop_t c, float* vv, float* vi, float* ii, float* iv, uint32_t* flags_e, uint32_t* flags_h) {
+    if (!c) return FDTD_ERR_ARG;
+    const uint32_t Nx = c->N[0], Ny = c->N[1], Nz = c->N[2];
+    const size_t NN = (size_t)Nx * Ny * Nz;
+    for (uint32_t x = 0; x < Nx; ++x)
+        for (uint32_t y = 0; y < Ny; ++y)
+            for (uint32_t z = 0; z < Nz; ++z) {
+                const size_t pi = ((size_t)x * Ny + y) * c->Nzp + z;
+                const uint32_t t = c->idx16 ? reinterpret_cast<const uint16_t*>(c->idx)[pi]
+                                            : reinterpret_cast<const uint32_t*>(c->idx)[pi];
+                const float* e = reinterpret_cast<const float*>(&c->hE[2 * (size_t)t]);
+                const float* h = reinterpret_cast<const float*>(&c->hH[2 * (size_t)t]);
+                const size_t gi = ((size_t)x * Ny + y) * Nz + z;
+                for (int n = 0; n < 3; ++n) {
+                    if (vv) vv[n * NN + gi] = e[n];
+                    if (vi) vi[n * NN + gi] = e[3 + n];
+                    if (ii) ii[n * NN + gi] = h[n];
+                    if (iv) iv[n * NN + gi] = h[3 + n];
+                }
+                if (flags_e) std::memcpy(&flags_e[gi], &e[6], 4);
+                if (flags_h) std::memcpy(&flags_h[gi], &h[6], 4);
+            }
+    return FDTD_OK;
+}
+
+int fdtd_engine_create_compressed(fdtd_cop_t cop, const fdtd_engine_opts* opts, fdtd_engine_t* out) {
+    if (!cop || !out) {
+        set_error("fdtd_engine_create_compressed: null argument");
         return FDTD_ERR_ARG;
     }
     fdtd_engine_s* e = new (std::nothrow) fdtd_engine_s();
     if (!e) return FDTD_ERR_NOMEM;
-    int rc;
-    try {
-        rc = create_engine(desc, opts, e);
-    } catch (const std::bad_alloc&) {
-        set_error("fdtd_engine_create: host allocation failed");
-        rc = FDTD_ERR_NOMEM;
+    int rc = upload_engine(cop, opts, e);
+    if (rc == FDTD_OK) {
+        cudaError_t ce = cudaStreamSynchronize(e->stream);
+        if (ce != cudaSuccess) {
+            set_error(std::string("engine upload: ") + cudaGetErrorString(ce));
+            rc = FDTD_ERR_CUDA;
+        }
     }
     if (rc != FDTD_OK) {
         delete e;
@@ -803,6 +943,21 @@ int fdtd_engine_create(const fdtd_op_desc* desc, const fdtd_engine_opts* opts, f
     }
     *out = e;
     return FDTD_OK;
+}
+
+int fdtd_engine_create(const fdtd_op_desc* desc, const fdtd_engine_opts* opts, fdtd_engine_t* out) {
+    fdtd_cop_t c = nullptr;
+    int rc = fdtd_compress(desc, &c);
+    if (rc) return rc;
+    rc = fdtd_engine_create_compressed(c, opts, out);
+    fdtd_cop_destroy(c);
+    return rc;
+}
+
+int fdtd_engine_reset(fdtd_engine_t e) {
+    if (!e) return FDTD_ERR_ARG;
+    CK(cudaSetDevice(e->device));
+    return reset_state(e);
 }
 
 int fdtd_engine_destroy(fdtd_engine_t e) {
@@ -837,12 +992,15 @@ int fdtd_engine_iterate(fdtd_engine_t e, uint32_t n) {
     if (!e->started) {
         if ((rc = upload_probes(e))) return rc;
         e->started = true;
-        if (e->interval) {  // sample at ts = 0 (RunFDTD's PA->Process() before the loop)
-            if ((rc = launch_advance(e, 0, true, e->energy_on_probe))) return rc;
-        }
         if (e->interval && e->use_graphs && (rc = build_chunk_graph(e))) return rc;
     }
     CK(cudaEventRecord(e->ev0, e->stream));
+    if (e->need_initial_sample) {
+        e->need_initial_sample = false;
+        if (e->interval) {  // sample at ts = 0 (RunFDTD's PA->Process() before the loop)
+            if ((rc = launch_advance(e, 0, true, e->energy_on_probe))) return rc;
+        }
+    }
     uint32_t left = n;
     while (left > 0) {
         if (e->interval && e->use_graphs && e->chunk && (e->ts % e->interval) == 0 && left >= e->interval) {
@@ -969,6 +1127,53 @@ int fdtd_engine_get_volt(fdtd_engine_t e, uint32_t n, uint32_t x, uint32_t y, ui
 }
 int fdtd_engine_get_curr(fdtd_engine_t e, uint32_t n, uint32_t x, uint32_t y, uint32_t z, float* v) {
     return get_one(e, e ? e->I.p : nullptr, n, x, y, z, v);
+}
+
+int fdtd_engine_profile_kernels(fdtd_engine_t e, uint32_t n_steps, double* ms_volt, double* ms_curr) {
+    if (!e || n_steps == 0) return FDTD_ERR_ARG;
+    CK(cudaSetDevice(e->device));
+    int rc;
+    if (!e->started) {
+        if ((rc = upload_probes(e))) return rc;
+        e->started = true;
+        if (e->interval && e->use_graphs && (rc = build_chunk_graph(e))) return rc;
+    }
+    if (e->need_initial_sample) {
+        e->need_initial_sample = false;
+        if (e->interval && (rc = launch_advance(e, 0, true, e->energy_on_probe))) return rc;
+    }
+    std::vector<cudaEvent_t> ev(3 * (size_t)n_steps);
+    for (auto& x : ev) CK(cudaEventCreate(&x));
+    dim3 block(32, e->TY);
+    dim3 gv((e->N[2] + 31) / 32, (e->N[1] + e->TY - 1) / e->TY, (e->N[0] + e->XC - 1) / e->XC);
+    dim3 gc((e->N[2] + 31) / 32, (e->N[1] + e->TY - 1) / e->TY, (e->N[0] - 1 + e->XC - 1) / e->XC);
+    for (uint32_t k = 0; k < n_steps; ++k) {
+        bool sample = e->interval && ((e->ts + 1) % e->interval) == 0;
+        bool energy = sample && e->energy_on_probe;
+        VoltFn fv = e->idx16 ? pick_volt<uint16_t>(e->feat) : pick_volt<uint32_t>(e->feat);
+        CurrFn fc = e->idx16 ? pick_curr<uint16_t>(e->feat, energy) : pick_curr<uint32_t>(e->feat, energy);
+        CK(cudaEventRecord(ev[3 * k], e->stream));
+        fv<<<gv, block, e->smem_bytes, e->stream>>>(e->g, 0, e->XC);
+        CK(cudaEventRecord(ev[3 * k + 1], e->stream));
+        fc<<<gc, block, e->smem_bytes, e->stream>>>(e->g, 0, e->XC);
+        CK(cudaEventRecord(ev[3 * k + 2], e->stream));
+        CK(cudaGetLastError());
+        if ((rc = launch_advance(e, 1, sample, e->energy_on_probe))) return rc;
+        e->ts += 1;
+    }
+    CK(cudaStreamSynchronize(e->stream));
+    double sv = 0, sc = 0;
+    for (uint32_t k = 0; k < n_steps; ++k) {
+        float a = 0, b = 0;
+        CK(cudaEventElapsedTime(&a, ev[3 * k], ev[3 * k + 1]));
+        CK(cudaEventElapsedTime(&b, ev[3 * k + 1], ev[3 * k + 2]));
+        sv += a;
+        sc += b;
+    }
+    for (auto& x : ev) cudaEventDestroy(x);
+    if (ms_volt) *ms_volt = sv / n_steps;
+    if (ms_curr) *ms_curr = sc / n_steps;
+    return FDTD_OK;
 }
 
 int fdtd_engine_get_stats(fdtd_engine_t e, fdtd_engine_stats* st) {

@@ -213,12 +213,50 @@ class Samples:
         return (self.ts + dual) * self.dT
 
 
-class Engine:
-    """Engine_CUDA on one GPU."""
+class CompressedOperator:
+    """Operator_SSE_Compressed::CompressOperator analogue, per node: the
+    uint16/uint32 tuple index + coefficient tables in (pinned) host memory.
+    Runs without a GPU."""
 
-    def __init__(self, op: Operator, device: int = 0, max_timesteps: int = 0, probe_interval: int | None = None,
+    def __init__(self, op: Operator):
+        h = C.c_void_p()
+        check(lib().fdtd_compress(C.byref(op.desc), C.byref(h)), "fdtd_compress")
+        self._h = h
+        self.op = op
+        info = _abi.FdtdCopInfo()
+        check(lib().fdtd_cop_get_info(h, C.byref(info)), "fdtd_cop_get_info")
+        self.info = {k: (list(getattr(info, k)) if k == "num_lines" else getattr(info, k)) for k, _ in info._fields_}
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            try:
+                lib().fdtd_cop_destroy(self._h)
+            except Exception:
+                pass
+            self._h = None
+
+    def expand(self):
+        """Reference-form vv, vi, ii, iv and the E/H flag words rebuilt from
+        the index and tables."""
+        shape = (3,) + self.op.num_lines
+        out = [np.empty(shape, np.float32) for _ in range(4)]
+        fe = np.empty(self.op.num_lines, np.uint32)
+        fh = np.empty(self.op.num_lines, np.uint32)
+        check(lib().fdtd_cop_expand(self._h, *[a.ctypes.data_as(_abi.PF) for a in out], fe.ctypes.data_as(_abi.PU32),
+                                    fh.ctypes.data_as(_abi.PU32)), "fdtd_cop_expand")
+        return out + [fe, fh]
+
+
+class Engine:
+    """Engine_CUDA on one GPU.  op is an Operator (compressed here) or a
+    CompressedOperator (upload only)."""
+
+    def __init__(self, op, device: int = 0, max_timesteps: int = 0, probe_interval: int | None = None,
                  use_graphs: bool = True, energy_on_probe: bool = True, tile_y: int = 0, x_chunk: int = 0,
                  probes: bool = True):
+        cop = op if isinstance(op, CompressedOperator) else None
+        if cop is not None:
+            op = cop.op
         self.op = op
         o = _abi.FdtdEngineOpts()
         o.device = device
@@ -229,7 +267,10 @@ class Engine:
         o.tile_y = int(tile_y)
         o.x_chunk = int(x_chunk)
         h = C.c_void_p()
-        check(lib().fdtd_engine_create(C.byref(op.desc), C.byref(o), C.byref(h)), "fdtd_engine_create")
+        if cop is not None:
+            check(lib().fdtd_engine_create_compressed(cop._h, C.byref(o), C.byref(h)), "fdtd_engine_create_compressed")
+        else:
+            check(lib().fdtd_engine_create(C.byref(op.desc), C.byref(o), C.byref(h)), "fdtd_engine_create")
         self._h = h
         self.interval = o.probe_interval
         self.probe_types = []
@@ -248,6 +289,10 @@ class Engine:
             self.close()
         except Exception:
             pass
+
+    def reset(self):
+        """Engine::Reset + Init: zero fields/states, numTS = 0."""
+        check(lib().fdtd_engine_reset(self._h), "fdtd_engine_reset")
 
     def iterate(self, n: int):
         check(lib().fdtd_engine_iterate(self._h, int(n)), "fdtd_engine_iterate")
@@ -300,6 +345,30 @@ class Engine:
         s = _abi.FdtdEngineStats()
         check(lib().fdtd_engine_get_stats(self._h, C.byref(s)), "get_stats")
         return {k: getattr(s, k) for k, _ in s._fields_}
+
+    def profile_kernels(self, n: int):
+        """Mean device ms of one voltage and one current kernel launch over
+        n timesteps (CUDA events on the engine stream)."""
+        a = C.c_double()
+        b = C.c_double()
+        check(lib().fdtd_engine_profile_kernels(self._h, int(n), C.byref(a), C.byref(b)), "profile_kernels")
+        return a.value, b.value
+
+    def num_samples(self) -> int:
+        n = C.c_uint32()
+        check(lib().fdtd_engine_num_samples(self._h, C.byref(n)), "num_samples")
+        return n.value
+
+    def read_samples(self, first: int, count: int):
+        np_ = len(self.probe_types)
+        ts = np.zeros(count, np.uint32)
+        vals = np.zeros((count, max(np_, 1)), np.float64)
+        en = np.zeros(count, np.float64)
+        if count:
+            check(lib().fdtd_engine_read_samples(self._h, first, count, ts.ctypes.data_as(_abi.PU32),
+                                                 vals.ctypes.data_as(_abi.PD), en.ctypes.data_as(_abi.PD)),
+                  "read_samples")
+        return ts, vals[:, :np_], en
 
     def last_timing(self):
         ms = C.c_double()
