@@ -1,0 +1,46 @@
+"""Profiling driver: builds one workload and runs a few timesteps, so that an
+external profiler (ncu) can capture the half-step kernels.
+
+    python -m wipems_gb300.profile --workload l256 --steps 8 [--no-graphs]
+
+Kernels are launched individually (no CUDA graph) unless --graphs is given,
+so a launch list shows every E / H kernel separately.
+"""
+from __future__ import annotations
+
+import argparse
+import time
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="l256", choices=["l256", "p64", "d192", "l160"])
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--graphs", action="store_true")
+    ap.add_argument("--tile-y", type=int, default=0)
+    ap.add_argument("--x-chunk", type=int, default=0)
+    args = ap.parse_args()
+    from . import CompressedOperator, Engine, Operator, scenes
+    if args.workload == "l256":
+        sc = scenes.l256()
+    elif args.workload == "l160":
+        sc = scenes.l256(cells=160)
+    elif args.workload == "p64":
+        sc = scenes.p64()
+    else:
+        sc = scenes.d192()
+    t0 = time.perf_counter()
+    op = Operator(sc)
+    cop = CompressedOperator(op)
+    eng = Engine(cop, use_graphs=args.graphs, tile_y=args.tile_y, x_chunk=args.x_chunk)
+    t1 = time.perf_counter()
+    eng.iterate(args.steps)
+    ms, launches = eng.last_timing()
+    n = op.num_nodes
+    print(f"{args.workload}: nodes={n} setup={t1 - t0:.2f}s steps={args.steps} device_ms={ms:.3f} "
+          f"launches={launches} Mcell-updates/s={n * args.steps / (ms / 1e3) / 1e6:.1f} stats={eng.stats()}")
+    eng.close()
+
+
+if __name__ == "__main__":
+    main()
