@@ -265,6 +265,8 @@ typedef struct {
     int      energy_on_probe; /* fuse the energy reduction into sample steps */
     int      tile_y;          /* kernel tile rows (0 = autotuned default) */
     int      x_chunk;         /* x planes per block (0 = default) */
+    int      kernel;          /* 0 = TMA-pipelined kernels (default),
+                                 1 = direct-load kernels */
 } fdtd_engine_opts;
 
 /* Operator::CreateEngine for the CUDA engine: compresses the coefficient

@@ -39,11 +39,12 @@ def compare(op, eng, ref, bitwise=True):
         assert dv == 0 and di == 0, (dv, di, rel_max(V, ref["volt"]), rel_max(I, ref["curr"]))
 
 
+@pytest.mark.parametrize("kernel", ["tma", "direct"])
 @pytest.mark.parametrize("kind", ["pec", "upml", "graded", "drude", "lorentz", "mixed"])
-def test_mini_scenes_match_oracle(kind):
+def test_mini_scenes_match_oracle(kind, kernel):
     op = Operator(scenes.mini(kind, nr_ts=400))
     ref = oracle.run(op.desc, op.probes, 400, op.probe_interval, engine=oracle.BASIC)
-    eng = Engine(op)
+    eng = Engine(op, kernel=kernel)
     eng.iterate(400)
     compare(op, eng, ref)
 
@@ -64,7 +65,10 @@ def test_chunking_graphs_and_tiles_are_invisible():
     V0, I0 = base.fields()
     s0 = base.samples()
     for kw, chunks in [(dict(use_graphs=True), [300]), (dict(use_graphs=True), [7, 1, 50, 242]),
-                       (dict(tile_y=4, x_chunk=5), [300]), (dict(tile_y=1, x_chunk=64), [100, 200])]:
+                       (dict(tile_y=4, x_chunk=5, kernel="direct"), [300]),
+                       (dict(tile_y=1, x_chunk=64, kernel="direct"), [100, 200]),
+                       (dict(x_chunk=3), [300]), (dict(x_chunk=64), [300]),
+                       (dict(kernel="direct", use_graphs=True), [300])]:
         e = Engine(op, **kw)
         for c in chunks:
             e.iterate(c)

@@ -24,6 +24,9 @@
 
 #include "fdtd_host.h"
 #include "kernels.cuh"
+#include "kernels_tma.cuh"
+
+#include <cudaTypedefs.h>
 
 namespace wipems {
 
@@ -134,6 +137,9 @@ struct fdtd_engine_s {
     bool idx16 = true;
     int TY = 8;
     int XC = 16;
+    bool use_tma = true;
+    TmaMaps maps{};
+    TileInfo ti{};
     size_t smem_bytes = 0;
     uint32_t num_tuples = 0, upml_nodes = 0, ade_nodes = 0;
     uint64_t device_bytes = 0;
@@ -185,7 +191,63 @@ CurrFn pick_curr(int feat, bool energy) {
     }
 }
 
+template <typename IdxT>
+void launch_tma_half(fdtd_engine_s* e, int ts_off, bool energy, bool volt) {
+    dim3 block(32, TMA_TY);
+    const bool up = (e->feat & FEAT_UPML) != 0;
+    const size_t sm = up ? StageLayout<IdxT, true>::SMEM : StageLayout<IdxT, false>::SMEM;
+    const DevGrid& g = e->g;
+    const TmaMaps& m = e->maps;
+    const TileInfo& ti = e->ti;
+    const int XC = e->XC;
+    if (volt) {
+        dim3 gv((e->N[2] + 31) / 32, (e->N[1] + TMA_TY - 1) / TMA_TY, (e->N[0] + XC - 1) / XC);
+        switch (e->feat) {
+            case 0: k_volt_tma<IdxT, 0><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
+            case 1: k_volt_tma<IdxT, 1><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
+            case 2: k_volt_tma<IdxT, 2><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
+            default: k_volt_tma<IdxT, 3><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
+        }
+        return;
+    }
+    dim3 gc((e->N[2] + 31) / 32, (e->N[1] + TMA_TY - 1) / TMA_TY, (e->N[0] - 1 + XC - 1) / XC);
+    if (energy) {
+        switch (e->feat) {
+            case 0: k_curr_tma<IdxT, 0, true><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
+            case 1: k_curr_tma<IdxT, 1, true><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
+            case 2: k_curr_tma<IdxT, 2, true><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
+            default: k_curr_tma<IdxT, 3, true><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
+        }
+    } else {
+        switch (e->feat) {
+            case 0: k_curr_tma<IdxT, 0, false><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
+            case 1: k_curr_tma<IdxT, 1, false><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
+            case 2: k_curr_tma<IdxT, 2, false><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
+            default: k_curr_tma<IdxT, 3, false><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
+        }
+    }
+}
+
+template <typename IdxT>
+void launch_tma(fdtd_engine_s* e, int ts_off, bool energy) {
+    launch_tma_half<IdxT>(e, ts_off, energy, true);
+    launch_tma_half<IdxT>(e, ts_off, energy, false);
+}
+
 int launch_step(fdtd_engine_s* e, int ts_off, bool energy) {
+    if (e->use_tma) {
+        if (e->idx16)
+            launch_tma<uint16_t>(e, ts_off, energy);
+        else
+            launch_tma<uint32_t>(e, ts_off, energy);
+        e->last_launches += 2;
+        cudaError_t err = cudaGetLastError();
+        if (err != cudaSuccess) {
+            set_error(std::string("kernel launch: ") + cudaGetErrorString(err));
+            return FDTD_ERR_CUDA;
+        }
+        return FDTD_OK;
+    }
     dim3 block(32, e->TY);
     dim3 gv((e->N[2] + 31) / 32, (e->N[1] + e->TY - 1) / e->TY, (e->N[0] + e->XC - 1) / e->XC);
     dim3 gc((e->N[2] + 31) / 32, (e->N[1] + e->TY - 1) / e->TY, (e->N[0] - 1 + e->XC - 1) / e->XC);
@@ -519,6 +581,7 @@ struct fdtd_cop_s {
     int feat = 0;
     bool any_upml = false, any_ade_e = false, any_ade_h = false, any_lor_e = false, any_lor_h = false;
     uint32_t num_tuples = 0, upml_nodes = 0, ade_nodes = 0;
+    int inner_lo[3] = {0, 0, 0}, inner_hi[3] = {0, 0, 0};  // nodes outside are (possibly) UPML
     double dT = 0;
     ~fdtd_cop_s() {
         if (idx) {
@@ -635,12 +698,91 @@ int compress_op(const fdtd_op_desc* d, fdtd_cop_s* c) {
                 for (uint32_t z = 0; z < Nz; ++z) p[z] = node_idx[src + z];
             }
         }
+    // inner box outside of which UPML slabs lie (slabs touching a face)
+    for (int a = 0; a < 3; ++a) {
+        c->inner_lo[a] = 0;
+        c->inner_hi[a] = (int)c->N[a] - 1;
+    }
+    for (uint32_t k = 0; k < d->num_upml; ++k) {
+        const fdtd_upml_desc& u = d->upml[k];
+        for (int a = 0; a < 3; ++a) {
+            if (u.num_lines[a] == c->N[a]) continue;
+            if (u.start[a] == 0) c->inner_lo[a] = std::max(c->inner_lo[a], (int)u.num_lines[a]);
+            if (u.start[a] + u.num_lines[a] == c->N[a]) c->inner_hi[a] = std::min(c->inner_hi[a], (int)u.start[a] - 1);
+        }
+    }
     c->sig_len = d->signal_length;
     c->sig_period = d->signal_period_ts;
     if (d->signal_length) {
         c->sigV.assign(d->signal_volt, d->signal_volt + d->signal_length);
         c->sigC.assign(d->signal_curr, d->signal_curr + d->signal_length);
     }
+    return FDTD_OK;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// 4-D map over one field array [3][Nx][Ny][Nzp] (dims z, y, x, component)
+int field_map(CUtensorMap* m, float* base, const fdtd_engine_s* e, uint32_t box_z, uint32_t box_y) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) {
+        set_error("cuTensorMapEncodeTiled is not available from the driver");
+        return FDTD_ERR_CUDA;
+    }
+    cuuint64_t dims[4] = {e->N[2], e->N[1], e->N[0], 3};
+    cuuint64_t strides[3] = {(cuuint64_t)e->Nzp * 4, (cuuint64_t)e->N[1] * e->Nzp * 4, (cuuint64_t)e->comp * 4};
+    cuuint32_t box[4] = {box_z, box_y, 1, 3};
+    cuuint32_t es[4] = {1, 1, 1, 1};
+    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled (field) failed: " + std::to_string((int)r));
+        return FDTD_ERR_CUDA;
+    }
+    return FDTD_OK;
+}
+
+int index_map(CUtensorMap* m, void* base, const fdtd_engine_s* e) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) {
+        set_error("cuTensorMapEncodeTiled is not available from the driver");
+        return FDTD_ERR_CUDA;
+    }
+    const cuuint64_t ib = e->idx16 ? 2 : 4;
+    cuuint64_t dims[3] = {e->N[2], e->N[1], e->N[0]};
+    cuuint64_t strides[2] = {(cuuint64_t)e->Nzp * ib, (cuuint64_t)e->N[1] * e->Nzp * ib};
+    cuuint32_t box[3] = {32, TMA_TY, 1};
+    cuuint32_t es[3] = {1, 1, 1};
+    CUresult r = enc(m, e->idx16 ? CU_TENSOR_MAP_DATA_TYPE_UINT16 : CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, base, dims,
+                     strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled (index) failed: " + std::to_string((int)r));
+        return FDTD_ERR_CUDA;
+    }
+    return FDTD_OK;
+}
+
+int make_maps(fdtd_engine_s* e) {
+    int rc;
+    if ((rc = field_map(&e->maps.I_halo, e->I.p, e, 36, TMA_TY + 1)) || (rc = field_map(&e->maps.I_own, e->I.p, e, 32, TMA_TY)) ||
+        (rc = field_map(&e->maps.V_halo, e->V.p, e, 36, TMA_TY + 1)) || (rc = field_map(&e->maps.V_own, e->V.p, e, 32, TMA_TY)) ||
+        (rc = index_map(&e->maps.idx, e->idx.p, e)))
+        return rc;
+    if (e->FV.p && ((rc = field_map(&e->maps.FV_own, e->FV.p, e, 32, TMA_TY)) ||
+                    (rc = field_map(&e->maps.FI_own, e->FI.p, e, 32, TMA_TY))))
+        return rc;
     return FDTD_OK;
 }
 
@@ -769,6 +911,13 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     g.d_ts = e->d_ts.p;
     g.d_eacc = e->d_eacc.p;
     e->smem_bytes = 2 * 3 * (size_t)(e->TY + 1) * 33 * sizeof(float);
+    e->use_tma = !(opts && opts->kernel == 1);
+    for (int a = 0; a < 3; ++a) {
+        e->ti.lo[a] = c->inner_lo[a];
+        e->ti.hi[a] = c->inner_hi[a];
+    }
+    e->ti.d_err = e->d_err.p;
+    if (e->use_tma && (rc = make_maps(e))) return rc;
     return reset_state(e);
 }
 
@@ -1027,6 +1176,10 @@ int fdtd_engine_iterate(fdtd_engine_t e, uint32_t n) {
         set_error("probe sample ring overflow: raise max_timesteps");
         return FDTD_ERR_STATE;
     }
+    if (err & 4) {
+        set_error("a bounded device wait gave up: a TMA copy did not complete in time");
+        return FDTD_ERR_TIMEOUT;
+    }
     if (err & 2) {
         set_error("energy reduction is not finite (NaN/Inf in the fields)");
         return FDTD_ERR_NONFINITE;
@@ -1153,9 +1306,24 @@ int fdtd_engine_profile_kernels(fdtd_engine_t e, uint32_t n_steps, double* ms_vo
         VoltFn fv = e->idx16 ? pick_volt<uint16_t>(e->feat) : pick_volt<uint32_t>(e->feat);
         CurrFn fc = e->idx16 ? pick_curr<uint16_t>(e->feat, energy) : pick_curr<uint32_t>(e->feat, energy);
         CK(cudaEventRecord(ev[3 * k], e->stream));
-        fv<<<gv, block, e->smem_bytes, e->stream>>>(e->g, 0, e->XC);
+        if (e->use_tma) {
+            // volt then curr with an event in between
+            if (e->idx16)
+                launch_tma_half<uint16_t>(e, 0, energy, true);
+            else
+                launch_tma_half<uint32_t>(e, 0, energy, true);
+        } else {
+            fv<<<gv, block, e->smem_bytes, e->stream>>>(e->g, 0, e->XC);
+        }
         CK(cudaEventRecord(ev[3 * k + 1], e->stream));
-        fc<<<gc, block, e->smem_bytes, e->stream>>>(e->g, 0, e->XC);
+        if (e->use_tma) {
+            if (e->idx16)
+                launch_tma_half<uint16_t>(e, 0, energy, false);
+            else
+                launch_tma_half<uint32_t>(e, 0, energy, false);
+        } else {
+            fc<<<gc, block, e->smem_bytes, e->stream>>>(e->g, 0, e->XC);
+        }
         CK(cudaEventRecord(ev[3 * k + 2], e->stream));
         CK(cudaGetLastError());
         if ((rc = launch_advance(e, 1, sample, e->energy_on_probe))) return rc;

@@ -253,7 +253,7 @@ class Engine:
 
     def __init__(self, op, device: int = 0, max_timesteps: int = 0, probe_interval: int | None = None,
                  use_graphs: bool = True, energy_on_probe: bool = True, tile_y: int = 0, x_chunk: int = 0,
-                 probes: bool = True):
+                 probes: bool = True, kernel: str = "tma"):
         cop = op if isinstance(op, CompressedOperator) else None
         if cop is not None:
             op = cop.op
@@ -266,6 +266,9 @@ class Engine:
         o.energy_on_probe = int(energy_on_probe)
         o.tile_y = int(tile_y)
         o.x_chunk = int(x_chunk)
+        if kernel not in ("tma", "direct"):
+            raise ValueError("kernel must be 'tma' or 'direct'")
+        o.kernel = 0 if kernel == "tma" else 1
         h = C.c_void_p()
         if cop is not None:
             check(lib().fdtd_engine_create_compressed(cop._h, C.byref(o), C.byref(h)), "fdtd_engine_create_compressed")
