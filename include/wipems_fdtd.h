@@ -267,6 +267,7 @@ typedef struct {
     int      x_chunk;         /* x planes per block (0 = default) */
     int      kernel;          /* 0 = TMA-pipelined kernels (default),
                                  1 = direct-load kernels */
+    int      stages;          /* TMA ring depth in x-planes, 3..8 (0 = 4) */
 } fdtd_engine_opts;
 
 /* Operator::CreateEngine for the CUDA engine: compresses the coefficient

@@ -138,6 +138,7 @@ struct fdtd_engine_s {
     int TY = 8;
     int XC = 16;
     bool use_tma = true;
+    int stages = 4;
     TmaMaps maps{};
     TileInfo ti{};
     size_t smem_bytes = 0;
@@ -195,7 +196,8 @@ template <typename IdxT>
 void launch_tma_half(fdtd_engine_s* e, int ts_off, bool energy, bool volt) {
     dim3 block(32, TMA_TY);
     const bool up = (e->feat & FEAT_UPML) != 0;
-    const size_t sm = up ? StageLayout<IdxT, true>::SMEM : StageLayout<IdxT, false>::SMEM;
+    const int S = e->stages;
+    const size_t sm = up ? StageLayout<IdxT, true>::smem(S) : StageLayout<IdxT, false>::smem(S);
     const DevGrid& g = e->g;
     const TmaMaps& m = e->maps;
     const TileInfo& ti = e->ti;
@@ -203,27 +205,27 @@ void launch_tma_half(fdtd_engine_s* e, int ts_off, bool energy, bool volt) {
     if (volt) {
         dim3 gv((e->N[2] + 31) / 32, (e->N[1] + TMA_TY - 1) / TMA_TY, (e->N[0] + XC - 1) / XC);
         switch (e->feat) {
-            case 0: k_volt_tma<IdxT, 0><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
-            case 1: k_volt_tma<IdxT, 1><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
-            case 2: k_volt_tma<IdxT, 2><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
-            default: k_volt_tma<IdxT, 3><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
+            case 0: k_volt_tma<IdxT, 0><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
+            case 1: k_volt_tma<IdxT, 1><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
+            case 2: k_volt_tma<IdxT, 2><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
+            default: k_volt_tma<IdxT, 3><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
         }
         return;
     }
     dim3 gc((e->N[2] + 31) / 32, (e->N[1] + TMA_TY - 1) / TMA_TY, (e->N[0] - 1 + XC - 1) / XC);
     if (energy) {
         switch (e->feat) {
-            case 0: k_curr_tma<IdxT, 0, true><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
-            case 1: k_curr_tma<IdxT, 1, true><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
-            case 2: k_curr_tma<IdxT, 2, true><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
-            default: k_curr_tma<IdxT, 3, true><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
+            case 0: k_curr_tma<IdxT, 0, true><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
+            case 1: k_curr_tma<IdxT, 1, true><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
+            case 2: k_curr_tma<IdxT, 2, true><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
+            default: k_curr_tma<IdxT, 3, true><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
         }
     } else {
         switch (e->feat) {
-            case 0: k_curr_tma<IdxT, 0, false><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
-            case 1: k_curr_tma<IdxT, 1, false><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
-            case 2: k_curr_tma<IdxT, 2, false><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
-            default: k_curr_tma<IdxT, 3, false><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC); break;
+            case 0: k_curr_tma<IdxT, 0, false><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
+            case 1: k_curr_tma<IdxT, 1, false><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
+            case 2: k_curr_tma<IdxT, 2, false><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
+            default: k_curr_tma<IdxT, 3, false><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
         }
     }
 }
@@ -786,6 +788,28 @@ int make_maps(fdtd_engine_s* e) {
     return FDTD_OK;
 }
 
+template <typename IdxT, int FEAT>
+cudaError_t set_attr_one(int bytes) {
+    cudaError_t e1 = cudaFuncSetAttribute(k_volt_tma<IdxT, FEAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaError_t e2 = cudaFuncSetAttribute(k_curr_tma<IdxT, FEAT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaError_t e3 = cudaFuncSetAttribute(k_curr_tma<IdxT, FEAT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    return e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3);
+}
+
+int set_smem_attrs(int bytes) {
+    cudaError_t r = cudaSuccess;
+    cudaError_t t;
+#define WIPEMS_ATTR(I, F) if ((t = set_attr_one<I, F>(bytes)) != cudaSuccess) r = t;
+    WIPEMS_ATTR(uint16_t, 0) WIPEMS_ATTR(uint16_t, 1) WIPEMS_ATTR(uint16_t, 2) WIPEMS_ATTR(uint16_t, 3)
+    WIPEMS_ATTR(uint32_t, 0) WIPEMS_ATTR(uint32_t, 1) WIPEMS_ATTR(uint32_t, 2) WIPEMS_ATTR(uint32_t, 3)
+#undef WIPEMS_ATTR
+    if (r != cudaSuccess) {
+        set_error(std::string("cudaFuncSetAttribute(MaxDynamicSharedMemorySize): ") + cudaGetErrorString(r));
+        return FDTD_ERR_CUDA;
+    }
+    return FDTD_OK;
+}
+
 // Engine::Init state: all fields and extension states zero, numTS = 0,
 // no recorded samples (the ts = 0 sample is taken again on the next iterate).
 int reset_state(fdtd_engine_s* e) {
@@ -912,6 +936,19 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     g.d_eacc = e->d_eacc.p;
     e->smem_bytes = 2 * 3 * (size_t)(e->TY + 1) * 33 * sizeof(float);
     e->use_tma = !(opts && opts->kernel == 1);
+    e->stages = (opts && opts->stages > 0) ? opts->stages : 4;
+    if (e->stages < 3 || e->stages > TMA_MAX_STAGES) {
+        set_error("stages must be 3..8");
+        return FDTD_ERR_ARG;
+    }
+    if (e->use_tma) {
+        // opt in to more than 48 KB of dynamic shared memory where needed
+        const size_t need = (e->feat & FEAT_UPML) ? StageLayout<uint32_t, true>::smem(e->stages)
+                                                  : StageLayout<uint32_t, false>::smem(e->stages);
+        if (need > 48 * 1024) {
+            if ((rc = set_smem_attrs((int)need))) return rc;
+        }
+    }
     for (int a = 0; a < 3; ++a) {
         e->ti.lo[a] = c->inner_lo[a];
         e->ti.hi[a] = c->inner_hi[a];

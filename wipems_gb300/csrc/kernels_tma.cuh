@@ -33,7 +33,7 @@
 
 namespace wipems {
 
-constexpr int TMA_STAGES = 4;
+constexpr int TMA_MAX_STAGES = 8;
 constexpr int TMA_TY = 8;
 constexpr unsigned long long TMA_WAIT_CYCLES = 4000000000ull;  // ~2 s at 2 GHz
 
@@ -114,7 +114,7 @@ struct StageLayout {
     static constexpr int OWN_BYTES = OWN * 4;
     static constexpr int IDX_BYTES = TMA_TY * 32 * (int)sizeof(IdxT);
     // + barriers + slack to align the dynamic shared memory base to 128 bytes
-    static constexpr size_t SMEM = (size_t)STAGE * 4 * TMA_STAGES + 64 + 128;
+    static size_t smem(int stages) { return (size_t)STAGE * 4 * stages + 8 * TMA_MAX_STAGES + 128; }
 };
 
 __device__ __forceinline__ bool tile_has_upml(const TileInfo& ti, int x, int y0, int y1, int z0, int z1) {
@@ -128,12 +128,13 @@ __device__ __forceinline__ bool tile_has_upml(const TileInfo& ti, int x, int y0,
 // ------------------------------------------------------------- E half-step
 template <typename IdxT, int FEAT>
 __global__ void __launch_bounds__(TMA_TY * 32) k_volt_tma(const DevGrid g, const __grid_constant__ TmaMaps m,
-                                                          const TileInfo ti, int ts_off, int XC) {
+                                                          const TileInfo ti, int ts_off, int XC,
+                                                          int STAGES) {
     constexpr bool UPML = (FEAT & FEAT_UPML) != 0;
     using L = StageLayout<IdxT, UPML>;
     extern __shared__ __align__(128) float smem_raw[];
     float* smem = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * TMA_STAGES);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * STAGES);
     const int tz = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * 32 + tz;
     const int z0 = blockIdx.x * 32, y0 = blockIdx.y * TMA_TY;
@@ -147,13 +148,13 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_volt_tma(const DevGrid g, const
     const int zl = min(z0 + 31, g.Nz - 1), yl = min(y0 + TMA_TY - 1, g.Ny - 1);
 
     if (tid == 0) {
-        for (int s = 0; s < TMA_STAGES; ++s) mbar_init(&bars[s], 1);
+        for (int s = 0; s < STAGES; ++s) mbar_init(&bars[s], 1);
         fence_barrier_init();
     }
     __syncthreads();
 
     auto issue = [&](int r) {  // thread 0: plane x0+r into stage r % STAGES
-        const int s = r % TMA_STAGES;
+        const int s = r % STAGES;
         const int x = x0 + r;
         float* st = smem + (size_t)s * L::STAGE;
         const bool up = UPML && tile_has_upml(ti, x, y0, yl, z0, zl);
@@ -167,7 +168,7 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_volt_tma(const DevGrid g, const
 
     int issued = 0;
     if (tid == 0) {
-        for (; issued < min(TMA_STAGES - 1, nplanes); ++issued) issue(issued);
+        for (; issued < min(STAGES - 1, nplanes); ++issued) issue(issued);
     }
     float p1 = 0.f, p2 = 0.f;  // I1, I2 at x-1
     const long long yz = (long long)y * g.Nzp + z;
@@ -179,13 +180,13 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_volt_tma(const DevGrid g, const
     bool aborted = false;
     int r = 0;
     for (; r < nplanes; ++r) {
-        if (tid == 0 && issued < nplanes && issued == r + TMA_STAGES - 1) {
+        if (tid == 0 && issued < nplanes && issued == r + STAGES - 1) {
             fence_proxy_async();
             issue(issued);
             ++issued;
         }
-        const int s = r % TMA_STAGES;
-        const bool ok = mbar_wait(&bars[s], (uint32_t)((r / TMA_STAGES) & 1));
+        const int s = r % STAGES;
+        const bool ok = mbar_wait(&bars[s], (uint32_t)((r / STAGES) & 1));
         const int x = x0 + r;
         const float* st = smem + (size_t)s * L::STAGE;
         const float* sI0 = st;
@@ -301,19 +302,20 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_volt_tma(const DevGrid g, const
     if (aborted && tid == 0) {
         atomicOr(ti.d_err, 4);
         // wait (bounded) for the copies this block still has in flight
-        for (int q = r; q < issued; ++q) mbar_wait(&bars[q % TMA_STAGES], (uint32_t)((q / TMA_STAGES) & 1));
+        for (int q = r; q < issued; ++q) mbar_wait(&bars[q % STAGES], (uint32_t)((q / STAGES) & 1));
     }
 }
 
 // ------------------------------------------------------------- H half-step
 template <typename IdxT, int FEAT, bool ENERGY>
 __global__ void __launch_bounds__(TMA_TY * 32) k_curr_tma(const DevGrid g, const __grid_constant__ TmaMaps m,
-                                                          const TileInfo ti, int ts_off, int XC) {
+                                                          const TileInfo ti, int ts_off, int XC,
+                                                          int STAGES) {
     constexpr bool UPML = (FEAT & FEAT_UPML) != 0;
     using L = StageLayout<IdxT, UPML>;
     extern __shared__ __align__(128) float smem_raw[];
     float* smem = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * TMA_STAGES);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * STAGES);
     const int tz = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * 32 + tz;
     const int z0 = blockIdx.x * 32, y0 = blockIdx.y * TMA_TY;
@@ -328,13 +330,13 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_curr_tma(const DevGrid g, const
     const int zl = min(z0 + 31, g.Nz - 1), yl = min(y0 + TMA_TY - 1, g.Ny - 1);
 
     if (tid == 0) {
-        for (int s = 0; s < TMA_STAGES; ++s) mbar_init(&bars[s], 1);
+        for (int s = 0; s < STAGES; ++s) mbar_init(&bars[s], 1);
         fence_barrier_init();
     }
     __syncthreads();
 
     auto issue = [&](int r) {
-        const int s = r % TMA_STAGES;
+        const int s = r % STAGES;
         const int x = x0 + r;
         float* st = smem + (size_t)s * L::STAGE;
         const bool upd = r < nplanes;  // plane x1 only contributes V
@@ -351,22 +353,22 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_curr_tma(const DevGrid g, const
 
     int issued = 0;
     if (nplanes > 0 && tid == 0) {
-        for (; issued < min(TMA_STAGES - 1, nload); ++issued) issue(issued);
+        for (; issued < min(STAGES - 1, nload); ++issued) issue(issued);
     }
     double esum = 0.0, hsum = 0.0;
     const long long yz = (long long)y * g.Nzp + z;
     bool aborted = false;
     int r = 0;
     for (; r < nplanes; ++r) {
-        if (tid == 0 && issued < nload && issued == r + TMA_STAGES - 1) {
+        if (tid == 0 && issued < nload && issued == r + STAGES - 1) {
             fence_proxy_async();
             issue(issued);
             ++issued;
         }
-        const int s = r % TMA_STAGES;
-        const int sn = (r + 1) % TMA_STAGES;
-        bool ok = mbar_wait(&bars[s], (uint32_t)((r / TMA_STAGES) & 1));
-        ok = ok && mbar_wait(&bars[sn], (uint32_t)(((r + 1) / TMA_STAGES) & 1));
+        const int s = r % STAGES;
+        const int sn = (r + 1) % STAGES;
+        bool ok = mbar_wait(&bars[s], (uint32_t)((r / STAGES) & 1));
+        ok = ok && mbar_wait(&bars[sn], (uint32_t)(((r + 1) / STAGES) & 1));
         const int x = x0 + r;
         if (ok && active) {
             const float* st = smem + (size_t)s * L::STAGE;
@@ -482,7 +484,7 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_curr_tma(const DevGrid g, const
     }
     if (aborted && tid == 0) {
         atomicOr(ti.d_err, 4);
-        for (int q = r; q < issued; ++q) mbar_wait(&bars[q % TMA_STAGES], (uint32_t)((q / TMA_STAGES) & 1));
+        for (int q = r; q < issued; ++q) mbar_wait(&bars[q % STAGES], (uint32_t)((q / STAGES) & 1));
     }
     if (ENERGY) {
 #pragma unroll
