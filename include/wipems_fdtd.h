@@ -267,7 +267,8 @@ typedef struct {
     int      x_chunk;         /* x planes per block (0 = default) */
     int      kernel;          /* 0 = TMA-pipelined kernels (default),
                                  1 = direct-load kernels */
-    int      stages;          /* TMA ring depth in x-planes, 3..8 (0 = 4) */
+    int      stages;          /* TMA ring depth in x-planes, 3..8 (0 = 3) */
+    int      z_per_thread;    /* nodes per thread along z, 1 or 2 (0 = 2) */
 } fdtd_engine_opts;
 
 /* Operator::CreateEngine for the CUDA engine: compresses the coefficient

@@ -58,7 +58,8 @@ class FdtdProbeDesc(C.Structure):
 class FdtdEngineOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("max_timesteps", u32), ("probe_interval", u32),
                 ("use_graphs", C.c_int), ("energy_on_probe", C.c_int), ("tile_y", C.c_int),
-                ("x_chunk", C.c_int), ("kernel", C.c_int), ("stages", C.c_int)]
+                ("x_chunk", C.c_int), ("kernel", C.c_int), ("stages", C.c_int),
+                ("z_per_thread", C.c_int)]
 
 
 class FdtdEngineStats(C.Structure):

@@ -138,7 +138,8 @@ struct fdtd_engine_s {
     int TY = 8;
     int XC = 16;
     bool use_tma = true;
-    int stages = 4;
+    int stages = 3;
+    int zw = 2;
     TmaMaps maps{};
     TileInfo ti{};
     size_t smem_bytes = 0;
@@ -192,42 +193,51 @@ CurrFn pick_curr(int feat, bool energy) {
     }
 }
 
-template <typename IdxT>
-void launch_tma_half(fdtd_engine_s* e, int ts_off, bool energy, bool volt) {
+template <typename IdxT, int ZW>
+void launch_tma_half_zw(fdtd_engine_s* e, int ts_off, bool energy, bool volt) {
+    constexpr int TZ = 32 * ZW;
     dim3 block(32, TMA_TY);
     const bool up = (e->feat & FEAT_UPML) != 0;
     const int S = e->stages;
-    const size_t sm = up ? StageLayout<IdxT, true>::smem(S) : StageLayout<IdxT, false>::smem(S);
+    const size_t sm = up ? StageLayout<IdxT, true, ZW>::smem(S) : StageLayout<IdxT, false, ZW>::smem(S);
     const DevGrid& g = e->g;
     const TmaMaps& m = e->maps;
     const TileInfo& ti = e->ti;
     const int XC = e->XC;
     if (volt) {
-        dim3 gv((e->N[2] + 31) / 32, (e->N[1] + TMA_TY - 1) / TMA_TY, (e->N[0] + XC - 1) / XC);
+        dim3 gv((ti.ne[2] + TZ - 1) / TZ, (ti.ne[1] + TMA_TY - 1) / TMA_TY, (ti.ne[0] + XC - 1) / XC);
         switch (e->feat) {
-            case 0: k_volt_tma<IdxT, 0><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
-            case 1: k_volt_tma<IdxT, 1><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
-            case 2: k_volt_tma<IdxT, 2><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
-            default: k_volt_tma<IdxT, 3><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
+            case 0: k_volt_tma<IdxT, 0, ZW><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
+            case 1: k_volt_tma<IdxT, 1, ZW><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
+            case 2: k_volt_tma<IdxT, 2, ZW><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
+            default: k_volt_tma<IdxT, 3, ZW><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
         }
         return;
     }
-    dim3 gc((e->N[2] + 31) / 32, (e->N[1] + TMA_TY - 1) / TMA_TY, (e->N[0] - 1 + XC - 1) / XC);
+    dim3 gc((e->N[2] - 1 + TZ - 1) / TZ, (e->N[1] - 1 + TMA_TY - 1) / TMA_TY, (e->N[0] - 1 + XC - 1) / XC);
     if (energy) {
         switch (e->feat) {
-            case 0: k_curr_tma<IdxT, 0, true><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
-            case 1: k_curr_tma<IdxT, 1, true><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
-            case 2: k_curr_tma<IdxT, 2, true><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
-            default: k_curr_tma<IdxT, 3, true><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
+            case 0: k_curr_tma<IdxT, 0, true, ZW><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
+            case 1: k_curr_tma<IdxT, 1, true, ZW><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
+            case 2: k_curr_tma<IdxT, 2, true, ZW><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
+            default: k_curr_tma<IdxT, 3, true, ZW><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
         }
     } else {
         switch (e->feat) {
-            case 0: k_curr_tma<IdxT, 0, false><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
-            case 1: k_curr_tma<IdxT, 1, false><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
-            case 2: k_curr_tma<IdxT, 2, false><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
-            default: k_curr_tma<IdxT, 3, false><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
+            case 0: k_curr_tma<IdxT, 0, false, ZW><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
+            case 1: k_curr_tma<IdxT, 1, false, ZW><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
+            case 2: k_curr_tma<IdxT, 2, false, ZW><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
+            default: k_curr_tma<IdxT, 3, false, ZW><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
         }
     }
+}
+
+template <typename IdxT>
+void launch_tma_half(fdtd_engine_s* e, int ts_off, bool energy, bool volt) {
+    if (e->zw == 2)
+        launch_tma_half_zw<IdxT, 2>(e, ts_off, energy, volt);
+    else
+        launch_tma_half_zw<IdxT, 1>(e, ts_off, energy, volt);
 }
 
 template <typename IdxT>
@@ -584,6 +594,7 @@ struct fdtd_cop_s {
     bool any_upml = false, any_ade_e = false, any_ade_h = false, any_lor_e = false, any_lor_h = false;
     uint32_t num_tuples = 0, upml_nodes = 0, ade_nodes = 0;
     int inner_lo[3] = {0, 0, 0}, inner_hi[3] = {0, 0, 0};  // nodes outside are (possibly) UPML
+    bool trim_e[3] = {false, false, false};  // last line of the axis is inert for the voltage update
     double dT = 0;
     ~fdtd_cop_s() {
         if (idx) {
@@ -700,6 +711,33 @@ int compress_op(const fdtd_op_desc* d, fdtd_cop_s* c) {
                 for (uint32_t z = 0; z < Nz; ++z) p[z] = node_idx[src + z];
             }
         }
+    // An axis' last line is inert for the voltage update when every node on it
+    // has only PEC voltage edges (vv = vi = 0), no ADE / excitation and, in
+    // UPML slabs, vvp = vvfo = 0: starting from zero its voltages stay zero.
+    {
+        std::vector<uint8_t> inert(tuples.size());
+        for (size_t k = 0; k < tuples.size(); ++k) {
+            const Tuple& t = tuples[k];
+            bool z = true;
+            for (int n = 0; n < 6; ++n) z = z && t.e[n] == 0.f;
+            if (t.fe & (TF_ADE | TF_EXC)) z = false;
+            if (t.fe & TF_UPML)
+                for (int n = 0; n < 6; ++n) z = z && t.eu[n] == 0.f;
+            inert[k] = z;
+        }
+        for (int a = 0; a < 3; ++a) {
+            bool all = true;
+            uint32_t pos[3];
+            const int b = (a + 1) % 3, cc = (a + 2) % 3;
+            pos[a] = c->N[a] - 1;
+            for (pos[b] = 0; pos[b] < c->N[b] && all; ++pos[b])
+                for (pos[cc] = 0; pos[cc] < c->N[cc] && all; ++pos[cc]) {
+                    const size_t gi = ((size_t)pos[0] * Ny + pos[1]) * Nz + pos[2];
+                    all = inert[node_idx[gi]] != 0;
+                }
+            c->trim_e[a] = all;
+        }
+    }
     // inner box outside of which UPML slabs lie (slabs touching a face)
     for (int a = 0; a < 3; ++a) {
         c->inner_lo[a] = 0;
@@ -755,7 +793,7 @@ int field_map(CUtensorMap* m, float* base, const fdtd_engine_s* e, uint32_t box_
     return FDTD_OK;
 }
 
-int index_map(CUtensorMap* m, void* base, const fdtd_engine_s* e) {
+int index_map(CUtensorMap* m, void* base, const fdtd_engine_s* e, uint32_t box_z) {
     PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
     if (!enc) {
         set_error("cuTensorMapEncodeTiled is not available from the driver");
@@ -764,7 +802,7 @@ int index_map(CUtensorMap* m, void* base, const fdtd_engine_s* e) {
     const cuuint64_t ib = e->idx16 ? 2 : 4;
     cuuint64_t dims[3] = {e->N[2], e->N[1], e->N[0]};
     cuuint64_t strides[2] = {(cuuint64_t)e->Nzp * ib, (cuuint64_t)e->N[1] * e->Nzp * ib};
-    cuuint32_t box[3] = {32, TMA_TY, 1};
+    cuuint32_t box[3] = {box_z, TMA_TY, 1};
     cuuint32_t es[3] = {1, 1, 1};
     CUresult r = enc(m, e->idx16 ? CU_TENSOR_MAP_DATA_TYPE_UINT16 : CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, base, dims,
                      strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -778,28 +816,32 @@ int index_map(CUtensorMap* m, void* base, const fdtd_engine_s* e) {
 
 int make_maps(fdtd_engine_s* e) {
     int rc;
-    if ((rc = field_map(&e->maps.I_halo, e->I.p, e, 36, TMA_TY + 1)) || (rc = field_map(&e->maps.I_own, e->I.p, e, 32, TMA_TY)) ||
-        (rc = field_map(&e->maps.V_halo, e->V.p, e, 36, TMA_TY + 1)) || (rc = field_map(&e->maps.V_own, e->V.p, e, 32, TMA_TY)) ||
-        (rc = index_map(&e->maps.idx, e->idx.p, e)))
+    const uint32_t TZ = 32u * (uint32_t)e->zw;
+    if ((rc = field_map(&e->maps.I_halo, e->I.p, e, TZ + 4, TMA_TY + 1)) ||
+        (rc = field_map(&e->maps.I_own, e->I.p, e, TZ, TMA_TY)) ||
+        (rc = field_map(&e->maps.V_halo, e->V.p, e, TZ + 4, TMA_TY + 1)) ||
+        (rc = field_map(&e->maps.V_own, e->V.p, e, TZ, TMA_TY)) || (rc = index_map(&e->maps.idx, e->idx.p, e, TZ)))
         return rc;
-    if (e->FV.p && ((rc = field_map(&e->maps.FV_own, e->FV.p, e, 32, TMA_TY)) ||
-                    (rc = field_map(&e->maps.FI_own, e->FI.p, e, 32, TMA_TY))))
+    if (e->FV.p && ((rc = field_map(&e->maps.FV_own, e->FV.p, e, TZ, TMA_TY)) ||
+                    (rc = field_map(&e->maps.FI_own, e->FI.p, e, TZ, TMA_TY))))
         return rc;
     return FDTD_OK;
 }
 
-template <typename IdxT, int FEAT>
+template <typename IdxT, int FEAT, int ZW>
 cudaError_t set_attr_one(int bytes) {
-    cudaError_t e1 = cudaFuncSetAttribute(k_volt_tma<IdxT, FEAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaError_t e2 = cudaFuncSetAttribute(k_curr_tma<IdxT, FEAT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaError_t e3 = cudaFuncSetAttribute(k_curr_tma<IdxT, FEAT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaError_t e1 = cudaFuncSetAttribute(k_volt_tma<IdxT, FEAT, ZW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaError_t e2 = cudaFuncSetAttribute(k_curr_tma<IdxT, FEAT, true, ZW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaError_t e3 = cudaFuncSetAttribute(k_curr_tma<IdxT, FEAT, false, ZW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     return e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3);
 }
 
 int set_smem_attrs(int bytes) {
     cudaError_t r = cudaSuccess;
     cudaError_t t;
-#define WIPEMS_ATTR(I, F) if ((t = set_attr_one<I, F>(bytes)) != cudaSuccess) r = t;
+#define WIPEMS_ATTR(I, F)                                                  \
+    if ((t = set_attr_one<I, F, 1>(bytes)) != cudaSuccess) r = t;          \
+    if ((t = set_attr_one<I, F, 2>(bytes)) != cudaSuccess) r = t;
     WIPEMS_ATTR(uint16_t, 0) WIPEMS_ATTR(uint16_t, 1) WIPEMS_ATTR(uint16_t, 2) WIPEMS_ATTR(uint16_t, 3)
     WIPEMS_ATTR(uint32_t, 0) WIPEMS_ATTR(uint32_t, 1) WIPEMS_ATTR(uint32_t, 2) WIPEMS_ATTR(uint32_t, 3)
 #undef WIPEMS_ATTR
@@ -936,15 +978,20 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     g.d_eacc = e->d_eacc.p;
     e->smem_bytes = 2 * 3 * (size_t)(e->TY + 1) * 33 * sizeof(float);
     e->use_tma = !(opts && opts->kernel == 1);
-    e->stages = (opts && opts->stages > 0) ? opts->stages : 4;
+    e->stages = (opts && opts->stages > 0) ? opts->stages : 3;
+    e->zw = (opts && opts->z_per_thread > 0) ? opts->z_per_thread : 2;
+    if (e->zw != 1 && e->zw != 2) {
+        set_error("z_per_thread must be 1 or 2");
+        return FDTD_ERR_ARG;
+    }
     if (e->stages < 3 || e->stages > TMA_MAX_STAGES) {
         set_error("stages must be 3..8");
         return FDTD_ERR_ARG;
     }
     if (e->use_tma) {
         // opt in to more than 48 KB of dynamic shared memory where needed
-        const size_t need = (e->feat & FEAT_UPML) ? StageLayout<uint32_t, true>::smem(e->stages)
-                                                  : StageLayout<uint32_t, false>::smem(e->stages);
+        const size_t need = (e->feat & FEAT_UPML) ? StageLayout<uint32_t, true, 2>::smem(e->stages)
+                                                  : StageLayout<uint32_t, false, 2>::smem(e->stages);
         if (need > 48 * 1024) {
             if ((rc = set_smem_attrs((int)need))) return rc;
         }
@@ -952,6 +999,7 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     for (int a = 0; a < 3; ++a) {
         e->ti.lo[a] = c->inner_lo[a];
         e->ti.hi[a] = c->inner_hi[a];
+        e->ti.ne[a] = (int)e->N[a] - (c->trim_e[a] ? 1 : 0);
     }
     e->ti.d_err = e->d_err.p;
     if (e->use_tma && (rc = make_maps(e))) return rc;

@@ -253,7 +253,7 @@ class Engine:
 
     def __init__(self, op, device: int = 0, max_timesteps: int = 0, probe_interval: int | None = None,
                  use_graphs: bool = True, energy_on_probe: bool = True, tile_y: int = 0, x_chunk: int = 0,
-                 probes: bool = True, kernel: str = "tma", stages: int = 0):
+                 probes: bool = True, kernel: str = "tma", stages: int = 0, z_per_thread: int = 0):
         cop = op if isinstance(op, CompressedOperator) else None
         if cop is not None:
             op = cop.op
@@ -270,6 +270,7 @@ class Engine:
             raise ValueError("kernel must be 'tma' or 'direct'")
         o.kernel = 0 if kernel == "tma" else 1
         o.stages = int(stages)
+        o.z_per_thread = int(z_per_thread)
         h = C.c_void_p()
         if cop is not None:
             check(lib().fdtd_engine_create_compressed(cop._h, C.byref(o), C.byref(h)), "fdtd_engine_create_compressed")
