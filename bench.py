@@ -142,8 +142,8 @@ def config_dict(op, cop, extra=None):
                      "dielectric bricks, 50 ohm z lumped port, Gaussian f0=fc=10 GHz; one step = one "
                      f"{TIMESTEPS}-timestep simulation",
          "nodes": n[0] * n[1] * n[2], "cells": (n[0] - 1) * (n[1] - 1) * (n[2] - 1), "timesteps_per_step": TIMESTEPS,
-         "upml_nodes": cop.info["num_upml_nodes"], "tuples": cop.info["num_tuples"],
-         "index_bytes": cop.info["index_bytes"], "l2_policy": "inputs larger than L2 (fields+operator > 500 MB)",
+         "upml_nodes": cop.info["num_upml_nodes"], "tuples_e": cop.info["num_tuples_e"],
+         "tuples_h": cop.info["num_tuples_h"], "index_bytes": cop.info["index_bytes_e"], "l2_policy": "inputs larger than L2 (fields+operator > 500 MB)",
          "parallelism": "replicas"}
     if extra:
         d.update(extra)
@@ -201,7 +201,14 @@ def run_gpu(args, rank, world, local_rank):
         import torch.distributed as dist
     sc, op, cop, setup = build_workload()
     nodes = op.num_nodes
-    eng = Engine(cop, device=local_rank, max_timesteps=TIMESTEPS)
+    # kernel tiling from the project's autotuner (setup, not timed)
+    from wipems_gb300 import autotune
+    t_tune = time.perf_counter()
+    best, _ = autotune.tune(cop, stages=(3, 4), xchunks=(4, 8, 16), steps=12, device=local_rank)
+    setup["autotune_s"] = round(time.perf_counter() - t_tune, 2)
+    setup["tiling"] = {"stages": best["stages"], "x_chunk": best["x_chunk"], "tile": "32z x 8y"}
+    tiling = dict(stages=best["stages"], x_chunk=best["x_chunk"])
+    eng = Engine(cop, device=local_rank, max_timesteps=TIMESTEPS, **tiling)
     # warm-up
     for _ in range(args.warmup):
         eng.reset()
@@ -256,7 +263,7 @@ def run_gpu(args, rank, world, local_rank):
     torch.cuda.synchronize()
     te = time.perf_counter()
     for _ in range(e2e_steps):
-        e = Engine(cop, device=local_rank, max_timesteps=TIMESTEPS)
+        e = Engine(cop, device=local_rank, max_timesteps=TIMESTEPS, **tiling)
         done = 0
         nread = 0
         while done < TIMESTEPS:

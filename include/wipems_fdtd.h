@@ -204,6 +204,11 @@ typedef struct {
     const float* signal_volt;
     const float* signal_curr;
     uint32_t signal_period_ts;   /* int(period/dT), 0 = not periodic */
+    /* Mesh lines in drawing units and the grid delta (Operator::discLines,
+     * GetGridDelta).  Optional (NULL / 0): needed only to compress graded
+     * meshes with the factorized geometry. */
+    const double* lines[3];
+    double unit;
 } fdtd_op_desc;
 
 /* Fills desc with pointers into op's host arrays (valid while op lives). */
@@ -229,28 +234,37 @@ typedef struct fdtd_engine_s* fdtd_engine_t;
 
 typedef struct fdtd_cop_s* fdtd_cop_t;
 
-/* Host-side compression of a reference-form operator into one per-node
- * tuple index (uint16 when the unique tuples fit, else uint32) plus
- * coefficient tables holding vv/vi/ii/iv and the fused UPML, ADE and
- * excitation terms -- the Operator_SSE_Compressed::CompressOperator idea
- * (operator_sse_compressed.cpp:120-176) applied per node.  The index is kept
- * in pinned host memory when a CUDA device is present.  Runs without a GPU. */
+/* Host-side compression of a reference-form operator into per-node E and H
+ * tuple indices (uint16 when the unique tuples of that half fit, else
+ * uint32) plus coefficient tables holding vv/vi (ii/iv) and the fused UPML,
+ * ADE and excitation terms -- the Operator_SSE_Compressed::CompressOperator
+ * idea (operator_sse_compressed.cpp:120-176) applied per node and half-step.
+ * Index arrays live in pinned host memory when a CUDA device is present.
+ * Runs without a GPU.  fdtd_compress picks the mode automatically: exact on
+ * uniform meshes (bit-identical coefficients), factorized geometry on graded
+ * meshes when desc->lines is given (vi / iv rebuilt in-kernel as
+ * VI * delta_n / A_n from per-axis arrays, within a few float ulps). */
 int fdtd_compress(const fdtd_op_desc* desc, fdtd_cop_t* out);
+/* mode: 0 = automatic, 1 = exact, 2 = factorized geometry */
+int fdtd_compress_ex(const fdtd_op_desc* desc, int mode, fdtd_cop_t* out);
 int fdtd_cop_destroy(fdtd_cop_t cop);
 
 typedef struct {
     uint32_t num_lines[3];
-    uint32_t num_tuples;
-    uint32_t index_bytes;
+    uint32_t num_tuples_e, num_tuples_h;
+    uint32_t index_bytes_e, index_bytes_h;
     uint32_t padded_nz;
     uint32_t num_upml_nodes;
     uint32_t num_ade_nodes;
+    int      geometry_factored;
+    int      trim_e[3];       /* last line of the axis is inert for E */
     uint64_t host_bytes;
     int      pinned;
 } fdtd_cop_info;
 
 int fdtd_cop_get_info(fdtd_cop_t cop, fdtd_cop_info* info);
-/* Expands the index + tables back to reference-form vv/vi/ii/iv and the
+/* Expands the index + tables back to reference-form vv/vi/ii/iv -- the
+ * coefficients the kernels apply, geometry factor included -- and the
  * per-node E/H flag words (any pointer may be NULL).  Test use. */
 int fdtd_cop_expand(fdtd_cop_t cop, float* vv, float* vi, float* ii, float* iv,
                     uint32_t* flags_e, uint32_t* flags_h);
@@ -264,11 +278,10 @@ typedef struct {
     int      use_graphs;      /* capture chunks of interval steps */
     int      energy_on_probe; /* fuse the energy reduction into sample steps */
     int      tile_y;          /* kernel tile rows (0 = autotuned default) */
-    int      x_chunk;         /* x planes per block (0 = default) */
+    int      x_chunk;         /* x planes per block (0 = 8) */
     int      kernel;          /* 0 = TMA-pipelined kernels (default),
                                  1 = direct-load kernels */
     int      stages;          /* TMA ring depth in x-planes, 3..8 (0 = 3) */
-    int      z_per_thread;    /* nodes per thread along z, 1 or 2 (0 = 2) */
 } fdtd_engine_opts;
 
 /* Operator::CreateEngine for the CUDA engine: compresses the coefficient

@@ -147,21 +147,44 @@ def test_drude_coefficients_closed_form():
     assert not a.volt_lor_on
 
 
-def test_compression_round_trip_all_features():
-    for kind in ("pec", "upml", "graded", "drude", "lorentz", "mixed"):
-        op = Operator(scenes.mini(kind))
-        cop = CompressedOperator(op)
-        ex = cop.expand()
-        for a, b in zip(ex[:4], op.coefficients()):
-            assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), kind
-        fe = ex[4]
-        assert (cop.info["num_upml_nodes"] > 0) == (kind != "pec")
-        assert int(((fe & 1) != 0).sum()) == cop.info["num_upml_nodes"]
-        if kind in ("drude", "lorentz", "mixed"):
-            assert int(((fe & 2) != 0).sum()) == cop.info["num_ade_nodes"] > 0
+@pytest.mark.parametrize("kind", ["pec", "upml", "graded", "drude", "lorentz", "mixed"])
+def test_compression_round_trip_exact(kind):
+    """Exact mode: index + tables expand back to the operator bit for bit."""
+    op = Operator(scenes.mini(kind))
+    cop = CompressedOperator(op, mode="exact")
+    assert not cop.factorized
+    ex = cop.expand()
+    for a, b in zip(ex[:4], op.coefficients()):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), kind
+    fe = ex[4]
+    assert (cop.info["num_upml_nodes"] > 0) == (kind != "pec")
+    assert int(((fe & 1) != 0).sum()) == cop.info["num_upml_nodes"]
+    if kind in ("drude", "lorentz", "mixed"):
+        assert int(((fe & 2) != 0).sum()) == cop.info["num_ade_nodes"] > 0
 
 
-def test_uniform_mesh_fits_uint16_index():
+@pytest.mark.parametrize("kind", ["graded", "mixed"])
+def test_factorized_geometry_on_graded_meshes(kind):
+    """Graded meshes compress with vi = VI * delta/A rebuilt per node: few
+    tuples, coefficients within a few float ulps of the operator's."""
+    op = Operator(scenes.mini(kind))
+    auto = CompressedOperator(op)
+    exact = CompressedOperator(op, mode="exact")
+    assert auto.factorized
+    assert auto.info["num_tuples_e"] < exact.info["num_tuples_e"] / 4
+    vv, vi, ii, iv = op.coefficients()
+    evv, evi, eii, eiv = auto.expand()[:4]
+    assert np.array_equal(evv, vv) and np.array_equal(eii, ii)
+    for a, b in ((evi, vi), (eiv, iv)):
+        nz = b != 0
+        assert np.array_equal(a[~nz], b[~nz])
+        rel = np.abs(a[nz].astype(np.float64) / b[nz] - 1)
+        assert rel.max() < 4e-7, rel.max()
+
+
+def test_uniform_mesh_is_exact_and_fits_uint16_index():
     op = Operator(scenes.l256(cells=96, n_bricks=40))
     cop = CompressedOperator(op)
-    assert cop.info["index_bytes"] == 2
+    assert not cop.factorized
+    assert cop.info["index_bytes_e"] == 2 and cop.info["index_bytes_h"] == 2
+    assert cop.info["trim_e"] == [1, 1, 1]

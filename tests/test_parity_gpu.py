@@ -23,6 +23,8 @@ FIELD_TOL = 1e-4
 
 
 def compare(op, eng, ref, bitwise=True):
+    """Probe series and fields against an oracle run; bit-identical fields
+    unless bitwise is False (factorized geometry on graded meshes)."""
     s = eng.samples()
     assert np.array_equal(s.ts, ref["ts"]), (s.ts[:5], ref["ts"][:5])
     for p in range(s.values.shape[1]):
@@ -42,11 +44,42 @@ def compare(op, eng, ref, bitwise=True):
 @pytest.mark.parametrize("kernel", ["tma", "direct"])
 @pytest.mark.parametrize("kind", ["pec", "upml", "graded", "drude", "lorentz", "mixed"])
 def test_mini_scenes_match_oracle(kind, kernel):
+    """Uniform meshes: bit-identical.  Graded meshes (automatic factorized
+    geometry): within the probe / field tolerance of the oracle on the
+    operator's own coefficients."""
     op = Operator(scenes.mini(kind, nr_ts=400))
     ref = oracle.run(op.desc, op.probes, 400, op.probe_interval, engine=oracle.BASIC)
-    eng = Engine(op, kernel=kernel)
+    cop = CompressedOperator(op)
+    eng = Engine(cop, kernel=kernel)
     eng.iterate(400)
-    compare(op, eng, ref)
+    compare(op, eng, ref, bitwise=not cop.factorized)
+
+
+@pytest.mark.parametrize("kind", ["graded", "mixed"])
+def test_factorized_kernels_bitwise_against_expanded_operator(kind):
+    """The factorized kernels apply exactly the coefficients fdtd_cop_expand
+    reports: run the oracle on those and require bit-identical fields."""
+    op = Operator(scenes.mini(kind, nr_ts=300))
+    cop = CompressedOperator(op)
+    assert cop.factorized
+    vv, vi, ii, iv = [np.ascontiguousarray(a) for a in cop.expand()[:4]]
+    d = type(op.desc).from_buffer_copy(op.desc)
+    import ctypes
+    PF = ctypes.POINTER(ctypes.c_float)
+    d.vv, d.vi, d.ii, d.iv = (a.ctypes.data_as(PF) for a in (vv, vi, ii, iv))
+    ref = oracle.run(d, op.probes, 300, op.probe_interval, engine=oracle.BASIC)
+    eng = Engine(cop)
+    eng.iterate(300)
+    compare(op, eng, ref, bitwise=True)
+
+
+def test_exact_mode_on_graded_mesh_is_bitwise():
+    op = Operator(scenes.mini("mixed", nr_ts=200))
+    cop = CompressedOperator(op, mode="exact")
+    ref = oracle.run(op.desc, op.probes, 200, op.probe_interval, engine=oracle.BASIC)
+    eng = Engine(cop)
+    eng.iterate(200)
+    compare(op, eng, ref, bitwise=True)
 
 
 def test_p64_full_2000_steps():
@@ -81,7 +114,7 @@ def test_chunking_graphs_and_tiles_are_invisible():
 
 
 def test_reset_and_compressed_upload_reproduce():
-    op = Operator(scenes.mini("mixed", nr_ts=200))
+    op = Operator(scenes.mini("lorentz", nr_ts=200))
     cop = CompressedOperator(op)
     e1 = Engine(cop)
     e1.iterate(200)

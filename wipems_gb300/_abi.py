@@ -46,7 +46,8 @@ class FdtdOpDesc(C.Structure):
                 ("volt_delay", PU32),
                 ("curr_count", u32), ("curr_index", PU32 * 3), ("curr_dir", PU16), ("curr_amp", PF),
                 ("curr_delay", PU32),
-                ("signal_length", u32), ("signal_volt", PF), ("signal_curr", PF), ("signal_period_ts", u32)]
+                ("signal_length", u32), ("signal_volt", PF), ("signal_curr", PF), ("signal_period_ts", u32),
+                ("lines", C.POINTER(C.c_double) * 3), ("unit", C.c_double)]
 
 
 class FdtdProbeDesc(C.Structure):
@@ -58,8 +59,7 @@ class FdtdProbeDesc(C.Structure):
 class FdtdEngineOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("max_timesteps", u32), ("probe_interval", u32),
                 ("use_graphs", C.c_int), ("energy_on_probe", C.c_int), ("tile_y", C.c_int),
-                ("x_chunk", C.c_int), ("kernel", C.c_int), ("stages", C.c_int),
-                ("z_per_thread", C.c_int)]
+                ("x_chunk", C.c_int), ("kernel", C.c_int), ("stages", C.c_int)]
 
 
 class FdtdEngineStats(C.Structure):
@@ -69,8 +69,10 @@ class FdtdEngineStats(C.Structure):
 
 
 class FdtdCopInfo(C.Structure):
-    _fields_ = [("num_lines", u32 * 3), ("num_tuples", u32), ("index_bytes", u32), ("padded_nz", u32),
-                ("num_upml_nodes", u32), ("num_ade_nodes", u32), ("host_bytes", C.c_uint64), ("pinned", C.c_int)]
+    _fields_ = [("num_lines", u32 * 3), ("num_tuples_e", u32), ("num_tuples_h", u32), ("index_bytes_e", u32),
+                ("index_bytes_h", u32), ("padded_nz", u32), ("num_upml_nodes", u32), ("num_ade_nodes", u32),
+                ("geometry_factored", C.c_int), ("trim_e", C.c_int * 3), ("host_bytes", C.c_uint64),
+                ("pinned", C.c_int)]
 
 
 class FdtdError(RuntimeError):
@@ -105,6 +107,7 @@ SIGNATURES = [
     ("fdtd_operator_describe", C.c_int, [_P, C.POINTER(FdtdOpDesc)]),
     ("fdtd_operator_get_probe", C.c_int, [_P, u32, C.POINTER(FdtdProbeDesc)]),
     ("fdtd_compress", C.c_int, [C.POINTER(FdtdOpDesc), C.POINTER(_P)]),
+    ("fdtd_compress_ex", C.c_int, [C.POINTER(FdtdOpDesc), C.c_int, C.POINTER(_P)]),
     ("fdtd_cop_destroy", C.c_int, [_P]),
     ("fdtd_cop_get_info", C.c_int, [_P, C.POINTER(FdtdCopInfo)]),
     ("fdtd_cop_expand", C.c_int, [_P, PF, PF, PF, PF, PU32, PU32]),

@@ -14,9 +14,8 @@ import json
 import os
 from pathlib import Path
 
-DEFAULT_STAGES = (3, 4, 5)
-DEFAULT_XCHUNK = (8, 16, 32)
-DEFAULT_ZW = (1, 2)
+DEFAULT_STAGES = (3, 4)
+DEFAULT_XCHUNK = (4, 8, 16)
 
 
 def _cache_path() -> Path:
@@ -27,27 +26,25 @@ def _cache_path() -> Path:
 def signature(cop) -> str:
     i = cop.info
     n = i["num_lines"]
-    return f"{n[0]}x{n[1]}x{n[2]}_u{int(i['num_upml_nodes'] > 0)}_a{int(i['num_ade_nodes'] > 0)}_i{i['index_bytes']}"
+    return (f"{n[0]}x{n[1]}x{n[2]}_u{int(i['num_upml_nodes'] > 0)}_a{int(i['num_ade_nodes'] > 0)}"
+            f"_i{i['index_bytes_e']}{i['index_bytes_h']}_g{i['geometry_factored']}")
 
 
-def tune(cop, stages=DEFAULT_STAGES, xchunks=DEFAULT_XCHUNK, zws=DEFAULT_ZW, steps: int = 30, device: int = 0,
-         verbose=False):
-    """Times every (z_per_thread, stages, x_chunk) triple; returns (best,
-    table) where best minimises the sum of the two half-step kernel times."""
+def tune(cop, stages=DEFAULT_STAGES, xchunks=DEFAULT_XCHUNK, steps: int = 30, device: int = 0, verbose=False):
+    """Times every (stages, x_chunk) pair; returns (best, table) where best
+    minimises the sum of the two half-step kernel times."""
     from .fdtd import Engine
     table = []
-    for zw in zws:
-        for s in stages:
-            for xc in xchunks:
-                eng = Engine(cop, device=device, stages=s, x_chunk=xc, z_per_thread=zw, probe_interval=0,
-                             max_timesteps=steps + 10)
-                eng.profile_kernels(4)  # warm-up
-                mv, mc = eng.profile_kernels(steps)
-                eng.close()
-                table.append(dict(z_per_thread=zw, stages=s, x_chunk=xc, ms_volt=mv, ms_curr=mc))
-                if verbose:
-                    print(f"zw={zw} stages={s} x_chunk={xc:3d}  volt {mv * 1e3:7.1f} us  curr {mc * 1e3:7.1f} us  "
-                          f"sum {(mv + mc) * 1e3:7.1f} us", flush=True)
+    for s in stages:
+        for xc in xchunks:
+            eng = Engine(cop, device=device, stages=s, x_chunk=xc, probe_interval=0, max_timesteps=steps + 10)
+            eng.profile_kernels(4)  # warm-up
+            mv, mc = eng.profile_kernels(steps)
+            eng.close()
+            table.append(dict(stages=s, x_chunk=xc, ms_volt=mv, ms_curr=mc))
+            if verbose:
+                print(f"stages={s} x_chunk={xc:3d}  volt {mv * 1e3:7.1f} us  curr {mc * 1e3:7.1f} us  "
+                      f"sum {(mv + mc) * 1e3:7.1f} us", flush=True)
     best = min(table, key=lambda r: r["ms_volt"] + r["ms_curr"])
     return best, table
 

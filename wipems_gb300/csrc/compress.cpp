@@ -1,0 +1,571 @@
+// Host-side compression of a reference-form operator into per-node E/H
+// tuple indices and coefficient tables (see cop.h).  Runs without a GPU; the
+// index arrays go to pinned memory when a CUDA device is present so that the
+// engine upload is a plain DMA.
+#include <cuda_runtime_api.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "cop.h"
+#include "fdtd_host.h"
+
+fdtd_cop_s::~fdtd_cop_s() {
+    for (wipems::HalfTables* h : {&E, &H}) {
+        if (!h->idx) continue;
+        if (h->pinned)
+            cudaFreeHost(h->idx);
+        else
+            std::free(h->idx);
+        h->idx = nullptr;
+    }
+}
+
+namespace wipems {
+namespace {
+
+struct TupleHash {
+    size_t operator()(const HalfTuple& t) const {
+        const uint64_t* p = reinterpret_cast<const uint64_t*>(&t);
+        uint64_t h = 1469598103934665603ull;
+        for (size_t i = 0; i < sizeof(HalfTuple) / 8; ++i) h ^= p[i] + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2);
+        return (size_t)h;
+    }
+};
+struct TupleEq {
+    bool operator()(const HalfTuple& a, const HalfTuple& b) const {
+        return std::memcmp(&a, &b, sizeof(HalfTuple)) == 0;
+    }
+};
+using TupleMap = std::unordered_map<HalfTuple, uint32_t, TupleHash, TupleEq>;
+
+// Operator::GetEdgeLength (main / dual) from the mesh lines, operator.cpp:136-185
+double edge_len(const double* l, uint32_t N, uint32_t pos, bool dual, double unit) {
+    auto line = [&](uint32_t p, bool du) -> double {
+        if (!du) return l[p];
+        if (p < N - 1) return 0.5 * (l[p] + l[p + 1]);
+        return l[p] + 0.5 * (l[p] - l[p - 1]);
+    };
+    double d;
+    if (!dual)
+        d = (pos < N - 1) ? line(pos + 1, false) - line(pos, false) : line(pos, false) - line(pos - 1, false);
+    else
+        d = (pos > 0) ? line(pos, true) - line(pos - 1, true) : line(1, false) - line(0, false);
+    return d * unit;
+}
+
+bool mesh_uniform(const fdtd_op_desc* d) {
+    for (int a = 0; a < 3; ++a) {
+        const double* l = d->lines[a];
+        const uint32_t N = d->num_lines[a];
+        const double d0 = l[1] - l[0];
+        for (uint32_t i = 1; i + 1 < N; ++i)
+            if (std::fabs((l[i + 1] - l[i]) - d0) > 1e-9 * std::fabs(d0)) return false;
+    }
+    return true;
+}
+
+struct Plan {
+    const fdtd_op_desc* d;
+    uint32_t N[3];
+    size_t NN;
+    bool geo;
+    const float* gf[4][3];  // dE, iD, dH, iM per axis (float arrays in cop->geom)
+    std::vector<int8_t> slab;
+    std::vector<int32_t> ade;
+    std::unordered_map<uint64_t, uint32_t> vexc, cexc;
+};
+
+int prepare(const fdtd_op_desc* d, Plan& P) {
+    const uint32_t Nx = P.N[0], Ny = P.N[1], Nz = P.N[2];
+    if (d->num_upml) {
+        if (d->num_upml > 127) {
+            set_error("too many UPML slabs");
+            return FDTD_ERR_ARG;
+        }
+        P.slab.assign(P.NN, -1);
+        for (uint32_t s = 0; s < d->num_upml; ++s) {
+            const fdtd_upml_desc& u = d->upml[s];
+            for (int a = 0; a < 3; ++a)
+                if (u.start[a] + u.num_lines[a] > P.N[a]) {
+                    set_error("UPML slab exceeds the grid");
+                    return FDTD_ERR_ARG;
+                }
+            for (uint32_t x = 0; x < u.num_lines[0]; ++x)
+                for (uint32_t y = 0; y < u.num_lines[1]; ++y)
+                    for (uint32_t z = 0; z < u.num_lines[2]; ++z) {
+                        size_t gi = ((size_t)(x + u.start[0]) * Ny + (y + u.start[1])) * Nz + (z + u.start[2]);
+                        if (P.slab[gi] >= 0) {
+                            set_error("UPML slabs overlap");
+                            return FDTD_ERR_ARG;
+                        }
+                        P.slab[gi] = (int8_t)s;
+                    }
+        }
+    }
+    if (d->num_ade_orders > 1) {
+        set_error("dispersion order > 1 is not provided by the fused kernels");
+        return FDTD_ERR_UNSUPPORTED;
+    }
+    if (d->num_ade_orders == 1) {
+        const fdtd_ade_desc& A = d->ade[0];
+        P.ade.assign(P.NN, -1);
+        for (uint32_t i = 0; i < A.count; ++i) {
+            uint32_t x = A.pos[0][i], y = A.pos[1][i], z = A.pos[2][i];
+            if (x >= Nx || y >= Ny || z >= Nz) {
+                set_error("ADE position outside the grid");
+                return FDTD_ERR_ARG;
+            }
+            P.ade[((size_t)x * Ny + y) * Nz + z] = (int32_t)i;
+        }
+    }
+    for (int half = 0; half < 2; ++half) {
+        const uint32_t cnt = half ? d->curr_count : d->volt_count;
+        for (uint32_t i = 0; i < cnt; ++i) {
+            const uint32_t x = (half ? d->curr_index : d->volt_index)[0][i];
+            const uint32_t y = (half ? d->curr_index : d->volt_index)[1][i];
+            const uint32_t z = (half ? d->curr_index : d->volt_index)[2][i];
+            const uint16_t dir = (half ? d->curr_dir : d->volt_dir)[i];
+            const uint32_t lim = half ? 1 : 0;
+            if (x >= Nx - lim || y >= Ny - lim || z >= Nz - lim || dir > 2) {
+                set_error(half ? "current excitation outside the current domain" : "voltage excitation outside the grid");
+                return FDTD_ERR_ARG;
+            }
+            const uint64_t key = (((uint64_t)x * Ny + y) * Nz + z) * 3 + dir;
+            auto& m = half ? P.cexc : P.vexc;
+            if (m.count(key)) {
+                set_error("duplicate excitation on one edge");
+                return FDTD_ERR_ARG;
+            }
+            m[key] = i;
+        }
+    }
+    return FDTD_OK;
+}
+
+// Builds the E (half = 0) or H (half = 1) tuple of a node.
+void make_tuple(const Plan& P, int half, uint32_t x, uint32_t y, uint32_t z, size_t gi, HalfTuple& t) {
+    const fdtd_op_desc* d = P.d;
+    std::memset(&t, 0, sizeof(t));
+    const float* c1 = half ? d->ii : d->vv;
+    const float* c2 = half ? d->iv : d->vi;
+    const uint32_t pos[3] = {x, y, z};
+    for (int n = 0; n < 3; ++n) {
+        t.c[n] = c1[n * P.NN + gi];
+        float v = c2[n * P.NN + gi];
+        if (P.geo && v != 0.f) {
+            const int nP = (n + 1) % 3, nPP = (n + 2) % 3;
+            const float* a0 = P.gf[half ? 2 : 0][n];
+            const float* a1 = P.gf[half ? 3 : 1][nP];
+            const float* a2 = P.gf[half ? 3 : 1][nPP];
+            const double g = (double)a0[pos[n]] * (double)a1[pos[nP]] * (double)a2[pos[nPP]];
+            v = (float)((double)v / g);
+        }
+        t.c[3 + n] = v;
+        t.xd[n] = -1;
+    }
+    if (!P.slab.empty() && P.slab[gi] >= 0) {
+        const fdtd_upml_desc& u = d->upml[P.slab[gi]];
+        const size_t nloc = (size_t)u.num_lines[0] * u.num_lines[1] * u.num_lines[2];
+        const size_t li =
+            ((size_t)(x - u.start[0]) * u.num_lines[1] + (y - u.start[1])) * u.num_lines[2] + (z - u.start[2]);
+        const float* a = half ? u.ii : u.vv;
+        const float* b = half ? u.iifo : u.vvfo;
+        const float* c = half ? u.iifn : u.vvfn;
+        for (int n = 0; n < 3; ++n) {
+            t.u[n] = a[n * nloc + li];
+            t.u[3 + n] = b[n * nloc + li];
+            t.u[6 + n] = c[n * nloc + li];
+        }
+        t.flags |= TF_UPML;
+    }
+    if (!P.ade.empty() && P.ade[gi] >= 0) {
+        const fdtd_ade_desc& A = d->ade[0];
+        const uint32_t i = (uint32_t)P.ade[gi];
+        const bool on = half ? A.curr_on : A.volt_on;
+        if (on) {
+            const float* ai = half ? A.i_int : A.v_int;
+            const float* ae = half ? A.i_ext : A.v_ext;
+            const float* al = half ? A.i_lor : A.v_lor;
+            const bool lor_on = half ? A.curr_lor_on : A.volt_lor_on;
+            bool lor = false;
+            for (int n = 0; n < 3; ++n) {
+                t.a[n] = ai[n * A.count + i];
+                t.a[3 + n] = ae[n * A.count + i];
+                t.a[6 + n] = (lor_on && al) ? al[n * A.count + i] : 0.f;
+                if (t.a[6 + n] != 0.f) lor = true;
+            }
+            t.flags |= TF_ADE | (lor ? TF_LOR : 0u);
+        }
+    }
+    const auto& m = half ? P.cexc : P.vexc;
+    if (!m.empty())
+        for (int n = 0; n < 3; ++n) {
+            auto it = m.find((uint64_t)gi * 3 + n);
+            if (it != m.end()) {
+                t.x[n] = (half ? d->curr_amp : d->volt_amp)[it->second];
+                t.xd[n] = (int32_t)(half ? d->curr_delay : d->volt_delay)[it->second];
+                t.flags |= TF_EXC;
+            }
+        }
+}
+
+void pack(const std::vector<HalfTuple>& tuples, HalfTables& T) {
+    const size_t n = tuples.size();
+    T.num_tuples = (uint32_t)n;
+    T.main.assign(n * TAB_MAIN * 4, 0.f);
+    T.exc.assign(n * TAB_EXC * 4, 0.f);
+    for (const HalfTuple& t : tuples) {
+        T.any_upml |= (t.flags & TF_UPML) != 0;
+        T.any_ade |= (t.flags & TF_ADE) != 0;
+        T.any_lor |= (t.flags & TF_LOR) != 0;
+        T.any_exc |= (t.flags & TF_EXC) != 0;
+    }
+    if (T.any_upml) T.upml.assign(n * TAB_UPML * 4, 0.f);
+    if (T.any_ade) T.ade.assign(n * TAB_ADE * 4, 0.f);
+    for (size_t k = 0; k < n; ++k) {
+        const HalfTuple& t = tuples[k];
+        float* m = &T.main[k * TAB_MAIN * 4];
+        for (int i = 0; i < 6; ++i) m[i] = t.c[i];
+        std::memcpy(&m[6], &t.flags, 4);
+        if (T.any_upml) std::memcpy(&T.upml[k * TAB_UPML * 4], t.u, sizeof(t.u));
+        if (T.any_ade) std::memcpy(&T.ade[k * TAB_ADE * 4], t.a, sizeof(t.a));
+        float* x = &T.exc[k * TAB_EXC * 4];
+        for (int i = 0; i < 3; ++i) x[i] = t.x[i];
+        std::memcpy(&x[4], t.xd, sizeof(t.xd));
+    }
+}
+
+int alloc_index(HalfTables& T, size_t bytes, bool try_pinned) {
+    T.idx_bytes = bytes;
+    if (try_pinned && cudaMallocHost(reinterpret_cast<void**>(&T.idx), bytes) == cudaSuccess) {
+        T.pinned = true;
+    } else {
+        cudaGetLastError();
+        T.idx = static_cast<uint8_t*>(std::malloc(bytes));
+        T.pinned = false;
+        if (!T.idx) {
+            set_error("host allocation of a tuple index failed");
+            return FDTD_ERR_NOMEM;
+        }
+    }
+    std::memset(T.idx, 0, bytes);
+    return FDTD_OK;
+}
+
+int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
+    for (int a = 0; a < 3; ++a) {
+        if (d->num_lines[a] < 2) {
+            set_error("every axis needs at least two lines");
+            return FDTD_ERR_ARG;
+        }
+        c->N[a] = d->num_lines[a];
+    }
+    if (!d->vv || !d->vi || !d->ii || !d->iv) {
+        set_error("coefficient arrays missing");
+        return FDTD_ERR_ARG;
+    }
+    if ((d->volt_count || d->curr_count) && (!d->signal_length || !d->signal_volt || !d->signal_curr)) {
+        set_error("excitation points without an excitation signal");
+        return FDTD_ERR_ARG;
+    }
+    const bool have_lines = d->lines[0] && d->lines[1] && d->lines[2] && d->unit > 0;
+    if (mode == 2 && !have_lines) {
+        set_error("factorized compression needs the mesh lines in the operator description");
+        return FDTD_ERR_ARG;
+    }
+    c->dT = d->dT;
+    Plan P;
+    P.d = d;
+    for (int a = 0; a < 3; ++a) P.N[a] = c->N[a];
+    const uint32_t Nx = P.N[0], Ny = P.N[1], Nz = P.N[2];
+    P.NN = (size_t)Nx * Ny * Nz;
+    P.geo = (mode == 2) || (mode == 0 && have_lines && !mesh_uniform(d));
+    c->geo = P.geo;
+    if (P.geo) {
+        const size_t tot = (size_t)Nx + Ny + Nz;
+        c->geom.assign(4 * tot, 0.f);
+        size_t off = 0;
+        for (int a = 0; a < 3; ++a) {
+            const uint32_t N = P.N[a];
+            for (uint32_t i = 0; i < N; ++i) {
+                const double m = edge_len(d->lines[a], N, i, false, d->unit);
+                const double du = edge_len(d->lines[a], N, i, true, d->unit);
+                c->geom[0 * tot + off + i] = (float)m;
+                c->geom[1 * tot + off + i] = (float)(1.0 / du);
+                c->geom[2 * tot + off + i] = (float)du;
+                c->geom[3 * tot + off + i] = (float)(1.0 / m);
+            }
+            for (int k = 0; k < 4; ++k) P.gf[k][a] = &c->geom[k * tot + off];
+            off += N;
+        }
+    }
+    int rc = prepare(d, P);
+    if (rc) return rc;
+
+    // per x-plane dedup in parallel, then a sequential global merge
+    std::vector<std::vector<HalfTuple>> pt[2];
+    std::vector<std::vector<uint32_t>> pl[2];
+    for (int h = 0; h < 2; ++h) {
+        pt[h].resize(Nx);
+        pl[h].resize(Nx);
+    }
+    std::vector<uint32_t> cnt_u(Nx, 0), cnt_a(Nx, 0);
+    auto worker = [&](uint32_t x) {
+        for (int h = 0; h < 2; ++h) {
+            TupleMap local;
+            std::vector<HalfTuple>& tv = pt[h][x];
+            std::vector<uint32_t>& lv = pl[h][x];
+            lv.resize((size_t)Ny * Nz);
+            HalfTuple t, last;
+            uint32_t last_id = UINT32_MAX;
+            for (uint32_t y = 0; y < Ny; ++y)
+                for (uint32_t z = 0; z < Nz; ++z) {
+                    const size_t gi = ((size_t)x * Ny + y) * Nz + z;
+                    make_tuple(P, h, x, y, z, gi, t);
+                    if (h == 0) {
+                        if (t.flags & TF_UPML) cnt_u[x]++;
+                        if (!P.ade.empty() && P.ade[gi] >= 0) cnt_a[x]++;
+                    }
+                    uint32_t id;
+                    if (last_id != UINT32_MAX && std::memcmp(&t, &last, sizeof(t)) == 0) {
+                        id = last_id;
+                    } else {
+                        auto it = local.find(t);
+                        if (it == local.end()) {
+                            id = (uint32_t)tv.size();
+                            local.emplace(t, id);
+                            tv.push_back(t);
+                        } else {
+                            id = it->second;
+                        }
+                        last = t;
+                        last_id = id;
+                    }
+                    lv[(size_t)y * Nz + z] = id;
+                }
+        }
+    };
+    {
+        std::atomic<uint32_t> next{0};
+        std::vector<std::thread> pool;
+        const int nt = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), (int)Nx));
+        for (int t = 0; t < nt; ++t)
+            pool.emplace_back([&] {
+                for (;;) {
+                    const uint32_t x = next.fetch_add(1);
+                    if (x >= Nx) break;
+                    worker(x);
+                }
+            });
+        for (auto& th : pool) th.join();
+    }
+    int ndev = 0;
+    const bool try_pinned = cudaGetDeviceCount(&ndev) == cudaSuccess && ndev > 0;
+    if (!try_pinned) cudaGetLastError();
+    c->Nzp = (int)((Nz + 31) / 32 * 32);
+    c->comp = (long long)Nx * Ny * c->Nzp;
+    std::vector<uint32_t> node_e;  // E tuple per node, for the trim test
+    node_e.resize(P.NN);
+    std::vector<HalfTuple> all[2];
+    for (int h = 0; h < 2; ++h) {
+        TupleMap global;
+        std::vector<HalfTuple>& tuples = all[h];
+        std::vector<std::vector<uint32_t>> remap(Nx);
+        for (uint32_t x = 0; x < Nx; ++x) {
+            remap[x].resize(pt[h][x].size());
+            for (size_t k = 0; k < pt[h][x].size(); ++k) {
+                auto it = global.find(pt[h][x][k]);
+                if (it == global.end()) {
+                    const uint32_t id = (uint32_t)tuples.size();
+                    global.emplace(pt[h][x][k], id);
+                    tuples.push_back(pt[h][x][k]);
+                    remap[x][k] = id;
+                } else {
+                    remap[x][k] = it->second;
+                }
+            }
+            std::vector<HalfTuple>().swap(pt[h][x]);
+        }
+        HalfTables& T = h ? c->H : c->E;
+        T.idx16 = tuples.size() <= 65536;
+        const size_t ib = T.idx16 ? 2 : 4;
+        if ((rc = alloc_index(T, (size_t)c->comp * ib, try_pinned))) return rc;
+        for (uint32_t x = 0; x < Nx; ++x) {
+            const std::vector<uint32_t>& lv = pl[h][x];
+            for (uint32_t y = 0; y < Ny; ++y) {
+                const size_t src = (size_t)y * Nz;
+                const size_t dst = ((size_t)x * Ny + y) * c->Nzp;
+                for (uint32_t z = 0; z < Nz; ++z) {
+                    const uint32_t id = remap[x][lv[src + z]];
+                    if (T.idx16)
+                        reinterpret_cast<uint16_t*>(T.idx)[dst + z] = (uint16_t)id;
+                    else
+                        reinterpret_cast<uint32_t*>(T.idx)[dst + z] = id;
+                    if (h == 0) node_e[((size_t)x * Ny + y) * Nz + z] = id;
+                }
+            }
+            std::vector<uint32_t>().swap(pl[h][x]);
+        }
+        pack(tuples, T);
+    }
+    for (uint32_t x = 0; x < Nx; ++x) {
+        c->upml_nodes += cnt_u[x];
+        c->ade_nodes += cnt_a[x];
+    }
+    // An axis' last line is inert for the voltage update when every node on it
+    // has only PEC voltage edges (vv = vi = 0), no ADE / excitation and, in
+    // UPML slabs, vvp = vvfo = 0: starting from zero its voltages stay zero.
+    {
+        std::vector<uint8_t> inert(all[0].size());
+        for (size_t k = 0; k < all[0].size(); ++k) {
+            const HalfTuple& t = all[0][k];
+            bool z = true;
+            for (int n = 0; n < 6; ++n) z = z && t.c[n] == 0.f;
+            if (t.flags & (TF_ADE | TF_EXC)) z = false;
+            if (t.flags & TF_UPML)
+                for (int n = 0; n < 6; ++n) z = z && t.u[n] == 0.f;
+            inert[k] = z;
+        }
+        for (int a = 0; a < 3; ++a) {
+            bool allz = true;
+            uint32_t pos[3];
+            const int b = (a + 1) % 3, cc = (a + 2) % 3;
+            pos[a] = P.N[a] - 1;
+            for (pos[b] = 0; pos[b] < P.N[b] && allz; ++pos[b])
+                for (pos[cc] = 0; pos[cc] < P.N[cc] && allz; ++pos[cc])
+                    allz = inert[node_e[((size_t)pos[0] * Ny + pos[1]) * Nz + pos[2]]] != 0;
+            c->trim_e[a] = allz;
+        }
+    }
+    // inner box outside of which the UPML slabs lie (slabs touching a face)
+    for (int a = 0; a < 3; ++a) {
+        c->inner_lo[a] = 0;
+        c->inner_hi[a] = (int)c->N[a] - 1;
+    }
+    for (uint32_t k = 0; k < d->num_upml; ++k) {
+        const fdtd_upml_desc& u = d->upml[k];
+        for (int a = 0; a < 3; ++a) {
+            if (u.num_lines[a] == c->N[a]) continue;
+            if (u.start[a] == 0) c->inner_lo[a] = std::max(c->inner_lo[a], (int)u.num_lines[a]);
+            if (u.start[a] + u.num_lines[a] == c->N[a]) c->inner_hi[a] = std::min(c->inner_hi[a], (int)u.start[a] - 1);
+        }
+    }
+    c->sig_len = d->signal_length;
+    c->sig_period = d->signal_period_ts;
+    if (d->signal_length) {
+        c->sigV.assign(d->signal_volt, d->signal_volt + d->signal_length);
+        c->sigC.assign(d->signal_curr, d->signal_curr + d->signal_length);
+    }
+    return FDTD_OK;
+}
+
+}  // namespace
+}  // namespace wipems
+
+using namespace wipems;
+
+extern "C" {
+
+int fdtd_compress_ex(const fdtd_op_desc* desc, int mode, fdtd_cop_t* out) {
+    if (!desc || !out || mode < 0 || mode > 2) {
+        set_error("fdtd_compress_ex: invalid argument");
+        return FDTD_ERR_ARG;
+    }
+    fdtd_cop_s* c = new (std::nothrow) fdtd_cop_s();
+    if (!c) return FDTD_ERR_NOMEM;
+    int rc;
+    try {
+        rc = compress_impl(desc, mode, c);
+    } catch (const std::bad_alloc&) {
+        set_error("fdtd_compress: host allocation failed");
+        rc = FDTD_ERR_NOMEM;
+    }
+    if (rc != FDTD_OK) {
+        delete c;
+        return rc;
+    }
+    *out = c;
+    return FDTD_OK;
+}
+
+int fdtd_compress(const fdtd_op_desc* desc, fdtd_cop_t* out) { return fdtd_compress_ex(desc, 0, out); }
+
+int fdtd_cop_destroy(fdtd_cop_t c) {
+    delete c;
+    return FDTD_OK;
+}
+
+int fdtd_cop_get_info(fdtd_cop_t c, fdtd_cop_info* info) {
+    if (!c || !info) return FDTD_ERR_ARG;
+    std::memset(info, 0, sizeof(*info));
+    for (int a = 0; a < 3; ++a) {
+        info->num_lines[a] = c->N[a];
+        info->trim_e[a] = c->trim_e[a] ? 1 : 0;
+    }
+    info->num_tuples_e = c->E.num_tuples;
+    info->num_tuples_h = c->H.num_tuples;
+    info->index_bytes_e = c->E.idx16 ? 2 : 4;
+    info->index_bytes_h = c->H.idx16 ? 2 : 4;
+    info->padded_nz = (uint32_t)c->Nzp;
+    info->num_upml_nodes = c->upml_nodes;
+    info->num_ade_nodes = c->ade_nodes;
+    info->geometry_factored = c->geo ? 1 : 0;
+    size_t tab = 0;
+    for (const HalfTables* T : {&c->E, &c->H})
+        tab += T->idx_bytes + (T->main.size() + T->upml.size() + T->ade.size() + T->exc.size()) * sizeof(float);
+    info->host_bytes = tab + c->geom.size() * sizeof(float) + (c->sigV.size() + c->sigC.size()) * sizeof(float);
+    info->pinned = (c->E.pinned && c->H.pinned) ? 1 : 0;
+    return FDTD_OK;
+}
+
+int fdtd_cop_expand(fdtd_cop_t c, float* vv, float* vi, float* ii, float* iv, uint32_t* flags_e, uint32_t* flags_h) {
+    if (!c) return FDTD_ERR_ARG;
+    const uint32_t Nx = c->N[0], Ny = c->N[1], Nz = c->N[2];
+    const size_t NN = (size_t)Nx * Ny * Nz;
+    const size_t tot = (size_t)Nx + Ny + Nz;
+    const size_t off[3] = {0, Nx, (size_t)Nx + Ny};
+    for (uint32_t x = 0; x < Nx; ++x)
+        for (uint32_t y = 0; y < Ny; ++y)
+            for (uint32_t z = 0; z < Nz; ++z) {
+                const size_t pi = ((size_t)x * Ny + y) * c->Nzp + z;
+                const size_t gi = ((size_t)x * Ny + y) * Nz + z;
+                const uint32_t pos[3] = {x, y, z};
+                for (int h = 0; h < 2; ++h) {
+                    const HalfTables& T = h ? c->H : c->E;
+                    const uint32_t t = T.idx16 ? reinterpret_cast<const uint16_t*>(T.idx)[pi]
+                                               : reinterpret_cast<const uint32_t*>(T.idx)[pi];
+                    const float* m = &T.main[(size_t)t * TAB_MAIN * 4];
+                    float* o1 = h ? ii : vv;
+                    float* o2 = h ? iv : vi;
+                    for (int n = 0; n < 3; ++n) {
+                        if (o1) o1[n * NN + gi] = m[n];
+                        float v = m[3 + n];
+                        if (c->geo) {
+                            // the kernels' float product ((V * g0) * g1) * g2
+                            const int nP = (n + 1) % 3, nPP = (n + 2) % 3;
+                            const float* g = c->geom.data();
+                            const float g0 = g[(h ? 2 : 0) * tot + off[n] + pos[n]];
+                            const float g1 = g[(h ? 3 : 1) * tot + off[nP] + pos[nP]];
+                            const float g2 = g[(h ? 3 : 1) * tot + off[nPP] + pos[nPP]];
+                            v = v * g0;
+                            v = v * g1;
+                            v = v * g2;
+                        }
+                        if (o2) o2[n * NN + gi] = v;
+                    }
+                    uint32_t* f = h ? flags_h : flags_e;
+                    if (f) std::memcpy(&f[gi], &m[6], 4);
+                }
+            }
+    return FDTD_OK;
+}
+
+}  // extern "C"

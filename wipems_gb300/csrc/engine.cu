@@ -1,76 +1,39 @@
 // Engine_CUDA: the device-resident FDTD time stepper behind the C ABI.
 //
-// fdtd_engine_create plays the part of Operator::CreateEngine + Engine::Init
-// (FDTD/operator.cpp:63-67, FDTD/engine.cpp:49-57) for the CUDA engine: it
-// compresses the reference-form coefficient arrays into one per-node tuple
-// index (the Operator_SSE_Compressed idea, operator_sse_compressed.cpp:120-176,
-// here per node and extended by the UPML / ADE / excitation terms the kernels
-// fuse), uploads index + tables, and allocates the zeroed field arrays.
-// fdtd_engine_iterate is Engine::IterateTS (engine.cpp:255-274): per
-// timestep one voltage and one current kernel, with probe sampling and the
-// energy reduction at the probe interval; chunks of one probe interval are
-// captured once into a CUDA graph and replayed.
+// fdtd_engine_create_compressed plays the part of Operator::CreateEngine +
+// Engine::Init (FDTD/operator.cpp:63-67, FDTD/engine.cpp:49-57) for the CUDA
+// engine: it allocates the zeroed field arrays and copies the compressed
+// operator (compress.cpp) to the device.  fdtd_engine_iterate is
+// Engine::IterateTS (engine.cpp:255-274): per timestep one voltage and one
+// current kernel, with probe sampling and the energy reduction at the probe
+// interval; chunks of one probe interval are captured once into a CUDA graph
+// and replayed.
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
-#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <memory>
 #include <string>
-#include <thread>
-#include <unordered_map>
 #include <vector>
 
+#include "cop.h"
 #include "fdtd_host.h"
 #include "kernels.cuh"
 #include "kernels_tma.cuh"
 
-#include <cudaTypedefs.h>
-
 namespace wipems {
-
 namespace {
 
-#define CK(call)                                                                   \
-    do {                                                                           \
-        cudaError_t e_ = (call);                                                   \
-        if (e_ != cudaSuccess) {                                                   \
-            set_error(std::string(#call) + ": " + cudaGetErrorString(e_));         \
-            return FDTD_ERR_CUDA;                                                  \
-        }                                                                          \
+#define CK(call)                                                           \
+    do {                                                                   \
+        cudaError_t e_ = (call);                                           \
+        if (e_ != cudaSuccess) {                                           \
+            set_error(std::string(#call) + ": " + cudaGetErrorString(e_)); \
+            return FDTD_ERR_CUDA;                                          \
+        }                                                                  \
     } while (0)
-
-// One compressed coefficient tuple: everything the two kernels read per node.
-// Unused terms are zero so that equal tuples compare equal bytewise.
-struct Tuple {
-    float e[6];        // vv0..2, vi0..2
-    float h[6];        // ii0..2, iv0..2
-    uint32_t fe, fh;   // flags
-    float eu[9];       // vvp, vvfo, vvfn
-    float hu[9];       // iip, iifo, iifn
-    float ea[9];       // v_int, v_ext, v_lor
-    float ha[9];       // i_int, i_ext, i_lor
-    float ex[3];       // volt excitation amplitude
-    int32_t exd[3];    // volt excitation delay (-1 = none)
-    float hx[3];
-    int32_t hxd[3];
-};
-
-struct TupleHash {
-    size_t operator()(const Tuple& t) const {
-        const uint64_t* p = reinterpret_cast<const uint64_t*>(&t);
-        uint64_t h = 1469598103934665603ull;
-        for (size_t i = 0; i < sizeof(Tuple) / 8; ++i) {
-            h ^= p[i] + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2);
-        }
-        return (size_t)h;
-    }
-};
-struct TupleEq {
-    bool operator()(const Tuple& a, const Tuple& b) const { return std::memcmp(&a, &b, sizeof(Tuple)) == 0; }
-};
-static_assert(sizeof(Tuple) % 8 == 0, "tuple must be 8-byte sized");
 
 template <class T>
 struct DevBuf {
@@ -93,6 +56,12 @@ struct DevBuf {
     }
 };
 
+struct DevHalfBufs {
+    DevBuf<uint8_t> idx;
+    DevBuf<float> main, upml, ade, exc;
+    bool idx16 = true;
+};
+
 }  // namespace
 }  // namespace wipems
 
@@ -107,8 +76,8 @@ struct fdtd_engine_s {
     double dT = 0;
     DevGrid g{};
     DevBuf<float> V, I, FV, FI, AV, LV, AI, LI;
-    DevBuf<uint8_t> idx;
-    DevBuf<float4> tabE, tabH, tabEU, tabHU, tabEA, tabHA, tabEX, tabHX;
+    DevHalfBufs E, H;
+    DevBuf<float> geo;
     DevBuf<float> sigV, sigC;
     DevBuf<int> d_ts;
     DevBuf<double> d_eacc;
@@ -134,20 +103,17 @@ struct fdtd_engine_s {
     bool started = false;
     bool need_initial_sample = true;
     int feat = 0;
-    bool idx16 = true;
+    bool geo_on = false;
     int TY = 8;
-    int XC = 16;
+    int XC = 8;
     bool use_tma = true;
     int stages = 3;
-    int zw = 2;
     TmaMaps maps{};
     TileInfo ti{};
-    size_t smem_bytes = 0;
-    uint32_t num_tuples = 0, upml_nodes = 0, ade_nodes = 0;
+    size_t smem_direct = 0;
+    uint32_t num_tuples_e = 0, num_tuples_h = 0, upml_nodes = 0, ade_nodes = 0;
     uint64_t device_bytes = 0;
-    // graph of one probe interval
     cudaGraphExec_t chunk = nullptr;
-    // timing
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double last_ms = 0;
     uint64_t last_launches = 0;
@@ -163,134 +129,112 @@ struct fdtd_engine_s {
 namespace wipems {
 namespace {
 
-typedef void (*VoltFn)(DevGrid, int, int);
-typedef void (*CurrFn)(DevGrid, int, int);
-
-template <typename IdxT>
-VoltFn pick_volt(int feat) {
-    switch (feat) {
-        case 0: return k_volt<IdxT, 0>;
-        case 1: return k_volt<IdxT, 1>;
-        case 2: return k_volt<IdxT, 2>;
-        default: return k_volt<IdxT, 3>;
-    }
-}
-template <typename IdxT>
-CurrFn pick_curr(int feat, bool energy) {
-    if (energy) {
-        switch (feat) {
-            case 0: return k_curr<IdxT, 0, true>;
-            case 1: return k_curr<IdxT, 1, true>;
-            case 2: return k_curr<IdxT, 2, true>;
-            default: return k_curr<IdxT, 3, true>;
-        }
-    }
-    switch (feat) {
-        case 0: return k_curr<IdxT, 0, false>;
-        case 1: return k_curr<IdxT, 1, false>;
-        case 2: return k_curr<IdxT, 2, false>;
-        default: return k_curr<IdxT, 3, false>;
+// ------------------------------------------------------------ kernel launch
+template <typename IdxT, int FEAT, bool GEO>
+void launch_volt_t(fdtd_engine_s* e, int ts_off) {
+    if (e->use_tma) {
+        constexpr bool UP = (FEAT & FEAT_UPML) != 0;
+        const size_t sm = StageLayout<IdxT, UP>::smem(e->stages);
+        dim3 grid((e->ti.ne[2] + 31) / 32, (e->ti.ne[1] + TMA_TY - 1) / TMA_TY, (e->ti.ne[0] + e->XC - 1) / e->XC);
+        k_volt_tma<IdxT, FEAT, GEO><<<grid, dim3(32, TMA_TY), sm, e->stream>>>(e->g, e->maps, e->ti, ts_off, e->XC,
+                                                                               e->stages);
+    } else {
+        dim3 grid((e->N[2] + 31) / 32, (e->N[1] + e->TY - 1) / e->TY, (e->N[0] + e->XC - 1) / e->XC);
+        k_volt<IdxT, FEAT, GEO><<<grid, dim3(32, e->TY), e->smem_direct, e->stream>>>(e->g, ts_off, e->XC);
     }
 }
 
-template <typename IdxT, int ZW>
-void launch_tma_half_zw(fdtd_engine_s* e, int ts_off, bool energy, bool volt) {
-    constexpr int TZ = 32 * ZW;
-    dim3 block(32, TMA_TY);
-    const bool up = (e->feat & FEAT_UPML) != 0;
-    const int S = e->stages;
-    const size_t sm = up ? StageLayout<IdxT, true, ZW>::smem(S) : StageLayout<IdxT, false, ZW>::smem(S);
-    const DevGrid& g = e->g;
-    const TmaMaps& m = e->maps;
-    const TileInfo& ti = e->ti;
-    const int XC = e->XC;
-    if (volt) {
-        dim3 gv((ti.ne[2] + TZ - 1) / TZ, (ti.ne[1] + TMA_TY - 1) / TMA_TY, (ti.ne[0] + XC - 1) / XC);
-        switch (e->feat) {
-            case 0: k_volt_tma<IdxT, 0, ZW><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
-            case 1: k_volt_tma<IdxT, 1, ZW><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
-            case 2: k_volt_tma<IdxT, 2, ZW><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
-            default: k_volt_tma<IdxT, 3, ZW><<<gv, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
-        }
-        return;
+template <typename IdxT, int FEAT, bool GEO, bool EN>
+void launch_curr_t(fdtd_engine_s* e, int ts_off) {
+    if (e->use_tma) {
+        constexpr bool UP = (FEAT & FEAT_UPML) != 0;
+        const size_t sm = StageLayout<IdxT, UP>::smem(e->stages);
+        dim3 grid((e->N[2] - 1 + 31) / 32, (e->N[1] - 1 + TMA_TY - 1) / TMA_TY, (e->N[0] - 1 + e->XC - 1) / e->XC);
+        k_curr_tma<IdxT, FEAT, GEO, EN><<<grid, dim3(32, TMA_TY), sm, e->stream>>>(e->g, e->maps, e->ti, ts_off,
+                                                                                   e->XC, e->stages);
+    } else {
+        dim3 grid((e->N[2] + 31) / 32, (e->N[1] + e->TY - 1) / e->TY, (e->N[0] - 1 + e->XC - 1) / e->XC);
+        k_curr<IdxT, FEAT, GEO, EN><<<grid, dim3(32, e->TY), e->smem_direct, e->stream>>>(e->g, ts_off, e->XC);
     }
-    dim3 gc((e->N[2] - 1 + TZ - 1) / TZ, (e->N[1] - 1 + TMA_TY - 1) / TMA_TY, (e->N[0] - 1 + XC - 1) / XC);
-    if (energy) {
-        switch (e->feat) {
-            case 0: k_curr_tma<IdxT, 0, true, ZW><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
-            case 1: k_curr_tma<IdxT, 1, true, ZW><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
-            case 2: k_curr_tma<IdxT, 2, true, ZW><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
-            default: k_curr_tma<IdxT, 3, true, ZW><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
+}
+
+template <typename IdxT, bool GEO>
+void launch_volt_f(fdtd_engine_s* e, int ts_off) {
+    switch (e->feat) {
+        case 0: launch_volt_t<IdxT, 0, GEO>(e, ts_off); break;
+        case 1: launch_volt_t<IdxT, 1, GEO>(e, ts_off); break;
+        case 2: launch_volt_t<IdxT, 2, GEO>(e, ts_off); break;
+        default: launch_volt_t<IdxT, 3, GEO>(e, ts_off); break;
+    }
+}
+
+template <typename IdxT, bool GEO, bool EN>
+void launch_curr_f(fdtd_engine_s* e, int ts_off) {
+    switch (e->feat) {
+        case 0: launch_curr_t<IdxT, 0, GEO, EN>(e, ts_off); break;
+        case 1: launch_curr_t<IdxT, 1, GEO, EN>(e, ts_off); break;
+        case 2: launch_curr_t<IdxT, 2, GEO, EN>(e, ts_off); break;
+        default: launch_curr_t<IdxT, 3, GEO, EN>(e, ts_off); break;
+    }
+}
+
+void launch_volt(fdtd_engine_s* e, int ts_off) {
+    if (e->E.idx16) {
+        if (e->geo_on) launch_volt_f<uint16_t, true>(e, ts_off);
+        else launch_volt_f<uint16_t, false>(e, ts_off);
+    } else {
+        if (e->geo_on) launch_volt_f<uint32_t, true>(e, ts_off);
+        else launch_volt_f<uint32_t, false>(e, ts_off);
+    }
+}
+
+void launch_curr(fdtd_engine_s* e, int ts_off, bool energy) {
+    if (e->H.idx16) {
+        if (e->geo_on) {
+            if (energy) launch_curr_f<uint16_t, true, true>(e, ts_off);
+            else launch_curr_f<uint16_t, true, false>(e, ts_off);
+        } else {
+            if (energy) launch_curr_f<uint16_t, false, true>(e, ts_off);
+            else launch_curr_f<uint16_t, false, false>(e, ts_off);
         }
     } else {
-        switch (e->feat) {
-            case 0: k_curr_tma<IdxT, 0, false, ZW><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
-            case 1: k_curr_tma<IdxT, 1, false, ZW><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
-            case 2: k_curr_tma<IdxT, 2, false, ZW><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
-            default: k_curr_tma<IdxT, 3, false, ZW><<<gc, block, sm, e->stream>>>(g, m, ti, ts_off, XC, S); break;
+        if (e->geo_on) {
+            if (energy) launch_curr_f<uint32_t, true, true>(e, ts_off);
+            else launch_curr_f<uint32_t, true, false>(e, ts_off);
+        } else {
+            if (energy) launch_curr_f<uint32_t, false, true>(e, ts_off);
+            else launch_curr_f<uint32_t, false, false>(e, ts_off);
         }
     }
 }
 
-template <typename IdxT>
-void launch_tma_half(fdtd_engine_s* e, int ts_off, bool energy, bool volt) {
-    if (e->zw == 2)
-        launch_tma_half_zw<IdxT, 2>(e, ts_off, energy, volt);
-    else
-        launch_tma_half_zw<IdxT, 1>(e, ts_off, energy, volt);
-}
-
-template <typename IdxT>
-void launch_tma(fdtd_engine_s* e, int ts_off, bool energy) {
-    launch_tma_half<IdxT>(e, ts_off, energy, true);
-    launch_tma_half<IdxT>(e, ts_off, energy, false);
+int check_launch() {
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) {
+        set_error(std::string("kernel launch: ") + cudaGetErrorString(err));
+        return FDTD_ERR_CUDA;
+    }
+    return FDTD_OK;
 }
 
 int launch_step(fdtd_engine_s* e, int ts_off, bool energy) {
-    if (e->use_tma) {
-        if (e->idx16)
-            launch_tma<uint16_t>(e, ts_off, energy);
-        else
-            launch_tma<uint32_t>(e, ts_off, energy);
-        e->last_launches += 2;
-        cudaError_t err = cudaGetLastError();
-        if (err != cudaSuccess) {
-            set_error(std::string("kernel launch: ") + cudaGetErrorString(err));
-            return FDTD_ERR_CUDA;
-        }
-        return FDTD_OK;
-    }
-    dim3 block(32, e->TY);
-    dim3 gv((e->N[2] + 31) / 32, (e->N[1] + e->TY - 1) / e->TY, (e->N[0] + e->XC - 1) / e->XC);
-    dim3 gc((e->N[2] + 31) / 32, (e->N[1] + e->TY - 1) / e->TY, (e->N[0] - 1 + e->XC - 1) / e->XC);
-    VoltFn fv = e->idx16 ? pick_volt<uint16_t>(e->feat) : pick_volt<uint32_t>(e->feat);
-    CurrFn fc = e->idx16 ? pick_curr<uint16_t>(e->feat, energy) : pick_curr<uint32_t>(e->feat, energy);
-    fv<<<gv, block, e->smem_bytes, e->stream>>>(e->g, ts_off, e->XC);
-    fc<<<gc, block, e->smem_bytes, e->stream>>>(e->g, ts_off, e->XC);
+    launch_volt(e, ts_off);
+    launch_curr(e, ts_off, energy);
     e->last_launches += 2;
-    cudaError_t err = cudaGetLastError();
-    if (err != cudaSuccess) {
-        set_error(std::string("kernel launch: ") + cudaGetErrorString(err));
-        return FDTD_ERR_CUDA;
-    }
-    return FDTD_OK;
+    return check_launch();
 }
 
 int launch_advance(fdtd_engine_s* e, int adv, bool sample, bool energy_valid) {
-    k_advance_sample<<<1, 256, 0, e->stream>>>(e->d_ts.p, adv, sample ? 1 : 0, e->ps, e->g,
-                                                energy_valid ? 1 : 0, kEps0, kMue0);
+    k_advance_sample<<<1, 256, 0, e->stream>>>(e->d_ts.p, adv, sample ? 1 : 0, e->ps, e->g, energy_valid ? 1 : 0,
+                                                kEps0, kMue0);
     e->last_launches += 1;
-    cudaError_t err = cudaGetLastError();
-    if (err != cudaSuccess) {
-        set_error(std::string("kernel launch: ") + cudaGetErrorString(err));
-        return FDTD_ERR_CUDA;
-    }
-    return FDTD_OK;
+    return check_launch();
 }
 
+// ------------------------------------------------------------------ probes
 int upload_probes(fdtd_engine_s* e) {
     if (e->probes_uploaded) return FDTD_OK;
-    uint32_t np = (uint32_t)e->h_weight.size();
+    const uint32_t np = (uint32_t)e->h_weight.size();
     int rc;
     if ((rc = e->d_entries.alloc(std::max<size_t>(1, e->h_entries.size()), e->device_bytes))) return rc;
     if ((rc = e->d_first.alloc(np + 1, e->device_bytes))) return rc;
@@ -302,7 +246,7 @@ int upload_probes(fdtd_engine_s* e) {
     if (np)
         CK(cudaMemcpyAsync(e->d_weight.p, e->h_weight.data(), np * sizeof(double), cudaMemcpyHostToDevice,
                            e->stream));
-    int row = 2 + (int)np;
+    const int row = 2 + (int)np;
     if ((rc = e->ring.alloc((size_t)e->cap * row, e->device_bytes))) return rc;
     e->ps.entries = e->d_entries.p;
     e->ps.first = e->d_first.p;
@@ -322,7 +266,7 @@ int build_chunk_graph(fdtd_engine_s* e) {
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
     int rc = FDTD_OK;
-    uint64_t saved = e->last_launches;
+    const uint64_t saved = e->last_launches;
     for (uint32_t k = 0; k < e->interval && rc == FDTD_OK; ++k)
         rc = launch_step(e, (int)k, e->energy_on_probe && (k + 1 == e->interval));
     if (rc == FDTD_OK) rc = launch_advance(e, (int)e->interval, true, e->energy_on_probe);
@@ -346,420 +290,42 @@ int build_chunk_graph(fdtd_engine_s* e) {
     return FDTD_OK;
 }
 
-// -------------------------------------------------------------- compression
-struct NodeMaps {
-    std::vector<int8_t> slab;           // UPML slab id per node or -1
-    std::vector<int32_t> ade;           // ADE list position (order 0) or -1
-    std::unordered_map<uint64_t, uint32_t> vexc, cexc;  // node*3+dir -> list entry
-};
-
-int compress(const fdtd_op_desc* d, fdtd_engine_s* e, std::vector<uint32_t>& node_idx, std::vector<Tuple>& tuples,
-             int threads) {
-    const uint32_t Nx = d->num_lines[0], Ny = d->num_lines[1], Nz = d->num_lines[2];
-    const size_t NN = (size_t)Nx * Ny * Nz;
-    NodeMaps m;
-    if (d->num_upml) {
-        m.slab.assign(NN, -1);
-        for (uint32_t s = 0; s < d->num_upml; ++s) {
-            const fdtd_upml_desc& u = d->upml[s];
-            for (uint32_t a = 0; a < 3; ++a)
-                if (u.start[a] + u.num_lines[a] > d->num_lines[a]) {
-                    set_error("UPML slab exceeds the grid");
-                    return FDTD_ERR_ARG;
-                }
-            for (uint32_t x = 0; x < u.num_lines[0]; ++x)
-                for (uint32_t y = 0; y < u.num_lines[1]; ++y)
-                    for (uint32_t z = 0; z < u.num_lines[2]; ++z) {
-                        size_t gi = ((size_t)(x + u.start[0]) * Ny + (y + u.start[1])) * Nz + (z + u.start[2]);
-                        if (m.slab[gi] >= 0) {
-                            set_error("UPML slabs overlap");
-                            return FDTD_ERR_ARG;
-                        }
-                        m.slab[gi] = (int8_t)s;
-                    }
+int start(fdtd_engine_s* e) {
+    int rc;
+    if (!e->started) {
+        if ((rc = upload_probes(e))) return rc;
+        e->started = true;
+        if (e->interval && e->use_graphs && (rc = build_chunk_graph(e))) return rc;
+    }
+    if (e->need_initial_sample) {
+        e->need_initial_sample = false;
+        if (e->interval) {  // sample at ts = 0 (RunFDTD's PA->Process() before the loop)
+            if ((rc = launch_advance(e, 0, true, e->energy_on_probe))) return rc;
         }
-    }
-    if (d->num_ade_orders > 1) {
-        set_error("dispersion order > 1 is not provided by the fused kernels");
-        return FDTD_ERR_UNSUPPORTED;
-    }
-    const fdtd_ade_desc* A = d->num_ade_orders ? &d->ade[0] : nullptr;
-    if (A && A->curr_on) {
-        // magnetic dispersion: supported by the kernels through the H tables
-    }
-    if (A) {
-        m.ade.assign(NN, -1);
-        for (uint32_t i = 0; i < A->count; ++i) {
-            uint32_t x = A->pos[0][i], y = A->pos[1][i], z = A->pos[2][i];
-            if (x >= Nx || y >= Ny || z >= Nz) {
-                set_error("ADE position outside the grid");
-                return FDTD_ERR_ARG;
-            }
-            m.ade[((size_t)x * Ny + y) * Nz + z] = (int32_t)i;
-        }
-    }
-    for (uint32_t i = 0; i < d->volt_count; ++i) {
-        uint32_t x = d->volt_index[0][i], y = d->volt_index[1][i], z = d->volt_index[2][i];
-        if (x >= Nx || y >= Ny || z >= Nz || d->volt_dir[i] > 2) {
-            set_error("voltage excitation outside the grid");
-            return FDTD_ERR_ARG;
-        }
-        uint64_t key = (((uint64_t)x * Ny + y) * Nz + z) * 3 + d->volt_dir[i];
-        if (m.vexc.count(key)) {
-            set_error("duplicate voltage excitation on one edge");
-            return FDTD_ERR_ARG;
-        }
-        m.vexc[key] = i;
-    }
-    for (uint32_t i = 0; i < d->curr_count; ++i) {
-        uint32_t x = d->curr_index[0][i], y = d->curr_index[1][i], z = d->curr_index[2][i];
-        if (x >= Nx - 1 || y >= Ny - 1 || z >= Nz - 1 || d->curr_dir[i] > 2) {
-            set_error("current excitation outside the current domain");
-            return FDTD_ERR_ARG;
-        }
-        uint64_t key = (((uint64_t)x * Ny + y) * Nz + z) * 3 + d->curr_dir[i];
-        if (m.cexc.count(key)) {
-            set_error("duplicate current excitation on one edge");
-            return FDTD_ERR_ARG;
-        }
-        m.cexc[key] = i;
-    }
-
-    node_idx.assign(NN, 0);
-    // Build tuples per x-plane in parallel, dedup per plane, then merge.
-    std::vector<std::vector<Tuple>> plane_tuples(Nx);
-    std::vector<std::vector<uint32_t>> plane_local(Nx);
-    uint32_t upml_nodes = 0, ade_nodes = 0;
-    std::vector<uint32_t> cnt_u(Nx, 0), cnt_a(Nx, 0);
-    auto worker = [&](uint32_t x) {
-        std::unordered_map<Tuple, uint32_t, TupleHash, TupleEq> local;
-        std::vector<Tuple>& pt = plane_tuples[x];
-        std::vector<uint32_t>& pl = plane_local[x];
-        pl.resize((size_t)Ny * Nz);
-        Tuple last;
-        uint32_t last_id = UINT32_MAX;
-        for (uint32_t y = 0; y < Ny; ++y)
-            for (uint32_t z = 0; z < Nz; ++z) {
-                const size_t gi = ((size_t)x * Ny + y) * Nz + z;
-                Tuple t;
-                std::memset(&t, 0, sizeof(t));
-                for (int n = 0; n < 3; ++n) {
-                    t.e[n] = d->vv[n * NN + gi];
-                    t.e[3 + n] = d->vi[n * NN + gi];
-                    t.h[n] = d->ii[n * NN + gi];
-                    t.h[3 + n] = d->iv[n * NN + gi];
-                    t.exd[n] = -1;
-                    t.hxd[n] = -1;
-                }
-                if (!m.slab.empty() && m.slab[gi] >= 0) {
-                    const fdtd_upml_desc& u = d->upml[m.slab[gi]];
-                    size_t nloc = (size_t)u.num_lines[0] * u.num_lines[1] * u.num_lines[2];
-                    size_t li = ((size_t)(x - u.start[0]) * u.num_lines[1] + (y - u.start[1])) * u.num_lines[2] +
-                                (z - u.start[2]);
-                    for (int n = 0; n < 3; ++n) {
-                        t.eu[n] = u.vv[n * nloc + li];
-                        t.eu[3 + n] = u.vvfo[n * nloc + li];
-                        t.eu[6 + n] = u.vvfn[n * nloc + li];
-                        t.hu[n] = u.ii[n * nloc + li];
-                        t.hu[3 + n] = u.iifo[n * nloc + li];
-                        t.hu[6 + n] = u.iifn[n * nloc + li];
-                    }
-                    t.fe |= TF_UPML;
-                    t.fh |= TF_UPML;
-                    cnt_u[x]++;
-                }
-                if (A && m.ade[gi] >= 0) {
-                    uint32_t i = (uint32_t)m.ade[gi];
-                    if (A->volt_on) {
-                        bool lor = false;
-                        for (int n = 0; n < 3; ++n) {
-                            t.ea[n] = A->v_int[n * A->count + i];
-                            t.ea[3 + n] = A->v_ext[n * A->count + i];
-                            t.ea[6 + n] = (A->volt_lor_on && A->v_lor) ? A->v_lor[n * A->count + i] : 0.f;
-                            if (t.ea[6 + n] != 0.f) lor = true;
-                        }
-                        t.fe |= TF_ADE | (lor ? TF_LOR : 0u);
-                    }
-                    if (A->curr_on) {
-                        bool lor = false;
-                        for (int n = 0; n < 3; ++n) {
-                            t.ha[n] = A->i_int[n * A->count + i];
-                            t.ha[3 + n] = A->i_ext[n * A->count + i];
-                            t.ha[6 + n] = (A->curr_lor_on && A->i_lor) ? A->i_lor[n * A->count + i] : 0.f;
-                            if (t.ha[6 + n] != 0.f) lor = true;
-                        }
-                        t.fh |= TF_ADE | (lor ? TF_LOR : 0u);
-                    }
-                    cnt_a[x]++;
-                }
-                if (!m.vexc.empty())
-                    for (int n = 0; n < 3; ++n) {
-                        auto it = m.vexc.find((uint64_t)gi * 3 + n);
-                        if (it != m.vexc.end()) {
-                            t.ex[n] = d->volt_amp[it->second];
-                            t.exd[n] = (int32_t)d->volt_delay[it->second];
-                            t.fe |= TF_EXC;
-                        }
-                    }
-                if (!m.cexc.empty())
-                    for (int n = 0; n < 3; ++n) {
-                        auto it = m.cexc.find((uint64_t)gi * 3 + n);
-                        if (it != m.cexc.end()) {
-                            t.hx[n] = d->curr_amp[it->second];
-                            t.hxd[n] = (int32_t)d->curr_delay[it->second];
-                            t.fh |= TF_EXC;
-                        }
-                    }
-                uint32_t id;
-                if (last_id != UINT32_MAX && std::memcmp(&t, &last, sizeof(Tuple)) == 0) {
-                    id = last_id;
-                } else {
-                    auto it = local.find(t);
-                    if (it == local.end()) {
-                        id = (uint32_t)pt.size();
-                        local.emplace(t, id);
-                        pt.push_back(t);
-                    } else {
-                        id = it->second;
-                    }
-                    last = t;
-                    last_id = id;
-                }
-                pl[(size_t)y * Nz + z] = id;
-            }
-    };
-    {
-        std::atomic<uint32_t> next{0};
-        std::vector<std::thread> pool;
-        int nt = std::max(1, std::min<int>(threads, (int)Nx));
-        for (int t = 0; t < nt; ++t)
-            pool.emplace_back([&] {
-                for (;;) {
-                    uint32_t x = next.fetch_add(1);
-                    if (x >= Nx) break;
-                    worker(x);
-                }
-            });
-        for (auto& th : pool) th.join();
-    }
-    std::unordered_map<Tuple, uint32_t, TupleHash, TupleEq> global;
-    tuples.clear();
-    for (uint32_t x = 0; x < Nx; ++x) {
-        std::vector<uint32_t> remap(plane_tuples[x].size());
-        for (size_t k = 0; k < plane_tuples[x].size(); ++k) {
-            auto it = global.find(plane_tuples[x][k]);
-            if (it == global.end()) {
-                uint32_t id = (uint32_t)tuples.size();
-                global.emplace(plane_tuples[x][k], id);
-                tuples.push_back(plane_tuples[x][k]);
-                remap[k] = id;
-            } else {
-                remap[k] = it->second;
-            }
-        }
-        const std::vector<uint32_t>& pl = plane_local[x];
-        for (size_t k = 0; k < pl.size(); ++k) node_idx[(size_t)x * Ny * Nz + k] = remap[pl[k]];
-        upml_nodes += cnt_u[x];
-        ade_nodes += cnt_a[x];
-        std::vector<Tuple>().swap(plane_tuples[x]);
-        std::vector<uint32_t>().swap(plane_local[x]);
-    }
-    e->upml_nodes = upml_nodes;
-    e->ade_nodes = ade_nodes;
-    return FDTD_OK;
-}
-
-void pack4(std::vector<float4>& out, size_t entry, int per, const float* vals, int nvals) {
-    float* f = reinterpret_cast<float*>(&out[entry * per]);
-    for (int k = 0; k < nvals; ++k) f[k] = vals[k];
-}
-
-}  // namespace
-}  // namespace wipems
-
-// Host-side compressed operator: per-node tuple index (padded device layout)
-// plus the coefficient tables, ready to be copied to the device.
-struct fdtd_cop_s {
-    uint32_t N[3] = {0, 0, 0};
-    int Nzp = 0;
-    long long comp = 0;
-    bool idx16 = true;
-    uint8_t* idx = nullptr;  // pinned when a CUDA device is present
-    bool idx_pinned = false;
-    size_t idx_bytes = 0;
-    std::vector<float4> hE, hH, hEU, hHU, hEA, hHA, hEX, hHX;
-    std::vector<float> sigV, sigC;
-    uint32_t sig_len = 0, sig_period = 0;
-    int feat = 0;
-    bool any_upml = false, any_ade_e = false, any_ade_h = false, any_lor_e = false, any_lor_h = false;
-    uint32_t num_tuples = 0, upml_nodes = 0, ade_nodes = 0;
-    int inner_lo[3] = {0, 0, 0}, inner_hi[3] = {0, 0, 0};  // nodes outside are (possibly) UPML
-    bool trim_e[3] = {false, false, false};  // last line of the axis is inert for the voltage update
-    double dT = 0;
-    ~fdtd_cop_s() {
-        if (idx) {
-            if (idx_pinned)
-                cudaFreeHost(idx);
-            else
-                std::free(idx);
-        }
-    }
-};
-
-namespace wipems {
-namespace {
-
-int compress_op(const fdtd_op_desc* d, fdtd_cop_s* c) {
-    for (int a = 0; a < 3; ++a) {
-        if (d->num_lines[a] < 2) {
-            set_error("every axis needs at least two lines");
-            return FDTD_ERR_ARG;
-        }
-        c->N[a] = d->num_lines[a];
-    }
-    if (!d->vv || !d->vi || !d->ii || !d->iv) {
-        set_error("coefficient arrays missing");
-        return FDTD_ERR_ARG;
-    }
-    if ((d->volt_count || d->curr_count) && (!d->signal_length || !d->signal_volt || !d->signal_curr)) {
-        set_error("excitation points without an excitation signal");
-        return FDTD_ERR_ARG;
-    }
-    c->dT = d->dT;
-    fdtd_engine_s dummy;  // receives node counts
-    std::vector<uint32_t> node_idx;
-    std::vector<Tuple> tuples;
-    int threads = (int)std::max(1u, std::thread::hardware_concurrency());
-    int rc = compress(d, &dummy, node_idx, tuples, threads);
-    if (rc) return rc;
-    c->upml_nodes = dummy.upml_nodes;
-    c->ade_nodes = dummy.ade_nodes;
-    c->num_tuples = (uint32_t)tuples.size();
-    c->idx16 = tuples.size() <= 65536;
-    const uint32_t Nx = c->N[0], Ny = c->N[1], Nz = c->N[2];
-    c->Nzp = (int)((Nz + 31) / 32 * 32);
-    c->comp = (long long)Nx * Ny * c->Nzp;
-    for (const Tuple& t : tuples) {
-        c->any_upml |= (t.fe & TF_UPML) != 0;
-        c->any_ade_e |= (t.fe & TF_ADE) != 0;
-        c->any_ade_h |= (t.fh & TF_ADE) != 0;
-        c->any_lor_e |= (t.fe & TF_LOR) != 0;
-        c->any_lor_h |= (t.fh & TF_LOR) != 0;
-    }
-    c->feat = (c->any_upml ? FEAT_UPML : 0) | ((c->any_ade_e || c->any_ade_h) ? FEAT_ADE : 0);
-    const size_t T = tuples.size();
-    const float4 z4 = make_float4(0, 0, 0, 0);
-    c->hE.assign(2 * T, z4);
-    c->hH.assign(2 * T, z4);
-    c->hEX.assign(2 * T, z4);
-    c->hHX.assign(2 * T, z4);
-    if (c->any_upml) {
-        c->hEU.assign(3 * T, z4);
-        c->hHU.assign(3 * T, z4);
-    }
-    if (c->feat & FEAT_ADE) {
-        c->hEA.assign(3 * T, z4);
-        c->hHA.assign(3 * T, z4);
-    }
-    for (size_t k = 0; k < T; ++k) {
-        const Tuple& t = tuples[k];
-        float e8[8] = {t.e[0], t.e[1], t.e[2], t.e[3], t.e[4], t.e[5], 0, 0};
-        std::memcpy(&e8[6], &t.fe, 4);
-        pack4(c->hE, k, 2, e8, 8);
-        float h8[8] = {t.h[0], t.h[1], t.h[2], t.h[3], t.h[4], t.h[5], 0, 0};
-        std::memcpy(&h8[6], &t.fh, 4);
-        pack4(c->hH, k, 2, h8, 8);
-        if (c->any_upml) {
-            pack4(c->hEU, k, 3, t.eu, 9);
-            pack4(c->hHU, k, 3, t.hu, 9);
-        }
-        if (c->feat & FEAT_ADE) {
-            pack4(c->hEA, k, 3, t.ea, 9);
-            pack4(c->hHA, k, 3, t.ha, 9);
-        }
-        float x8[8] = {t.ex[0], t.ex[1], t.ex[2], 0, 0, 0, 0, 0};
-        std::memcpy(&x8[4], t.exd, 12);
-        pack4(c->hEX, k, 2, x8, 8);
-        float y8[8] = {t.hx[0], t.hx[1], t.hx[2], 0, 0, 0, 0, 0};
-        std::memcpy(&y8[4], t.hxd, 12);
-        pack4(c->hHX, k, 2, y8, 8);
-    }
-    const size_t ib = c->idx16 ? 2 : 4;
-    c->idx_bytes = (size_t)c->comp * ib;
-    int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) == cudaSuccess && ndev > 0 &&
-        cudaMallocHost(reinterpret_cast<void**>(&c->idx), c->idx_bytes) == cudaSuccess) {
-        c->idx_pinned = true;
-    } else {
-        cudaGetLastError();  // clear the sticky "no device" error of the probe
-        c->idx = static_cast<uint8_t*>(std::malloc(c->idx_bytes));
-        if (!c->idx) {
-            set_error("host allocation of the tuple index failed");
-            return FDTD_ERR_NOMEM;
-        }
-    }
-    std::memset(c->idx, 0, c->idx_bytes);
-    for (uint32_t x = 0; x < Nx; ++x)
-        for (uint32_t y = 0; y < Ny; ++y) {
-            const size_t src = ((size_t)x * Ny + y) * Nz;
-            const size_t dst = ((size_t)x * Ny + y) * c->Nzp;
-            if (c->idx16) {
-                uint16_t* p = reinterpret_cast<uint16_t*>(c->idx) + dst;
-                for (uint32_t z = 0; z < Nz; ++z) p[z] = (uint16_t)node_idx[src + z];
-            } else {
-                uint32_t* p = reinterpret_cast<uint32_t*>(c->idx) + dst;
-                for (uint32_t z = 0; z < Nz; ++z) p[z] = node_idx[src + z];
-            }
-        }
-    // An axis' last line is inert for the voltage update when every node on it
-    // has only PEC voltage edges (vv = vi = 0), no ADE / excitation and, in
-    // UPML slabs, vvp = vvfo = 0: starting from zero its voltages stay zero.
-    {
-        std::vector<uint8_t> inert(tuples.size());
-        for (size_t k = 0; k < tuples.size(); ++k) {
-            const Tuple& t = tuples[k];
-            bool z = true;
-            for (int n = 0; n < 6; ++n) z = z && t.e[n] == 0.f;
-            if (t.fe & (TF_ADE | TF_EXC)) z = false;
-            if (t.fe & TF_UPML)
-                for (int n = 0; n < 6; ++n) z = z && t.eu[n] == 0.f;
-            inert[k] = z;
-        }
-        for (int a = 0; a < 3; ++a) {
-            bool all = true;
-            uint32_t pos[3];
-            const int b = (a + 1) % 3, cc = (a + 2) % 3;
-            pos[a] = c->N[a] - 1;
-            for (pos[b] = 0; pos[b] < c->N[b] && all; ++pos[b])
-                for (pos[cc] = 0; pos[cc] < c->N[cc] && all; ++pos[cc]) {
-                    const size_t gi = ((size_t)pos[0] * Ny + pos[1]) * Nz + pos[2];
-                    all = inert[node_idx[gi]] != 0;
-                }
-            c->trim_e[a] = all;
-        }
-    }
-    // inner box outside of which UPML slabs lie (slabs touching a face)
-    for (int a = 0; a < 3; ++a) {
-        c->inner_lo[a] = 0;
-        c->inner_hi[a] = (int)c->N[a] - 1;
-    }
-    for (uint32_t k = 0; k < d->num_upml; ++k) {
-        const fdtd_upml_desc& u = d->upml[k];
-        for (int a = 0; a < 3; ++a) {
-            if (u.num_lines[a] == c->N[a]) continue;
-            if (u.start[a] == 0) c->inner_lo[a] = std::max(c->inner_lo[a], (int)u.num_lines[a]);
-            if (u.start[a] + u.num_lines[a] == c->N[a]) c->inner_hi[a] = std::min(c->inner_hi[a], (int)u.start[a] - 1);
-        }
-    }
-    c->sig_len = d->signal_length;
-    c->sig_period = d->signal_period_ts;
-    if (d->signal_length) {
-        c->sigV.assign(d->signal_volt, d->signal_volt + d->signal_length);
-        c->sigC.assign(d->signal_curr, d->signal_curr + d->signal_length);
     }
     return FDTD_OK;
 }
 
+int check_error_word(fdtd_engine_s* e) {
+    int err = 0;
+    CK(cudaMemcpyAsync(&err, e->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    if (err & 4) {
+        set_error("a bounded device wait gave up: a TMA copy did not complete in time");
+        return FDTD_ERR_TIMEOUT;
+    }
+    if (err & 1) {
+        set_error("probe sample ring overflow: raise max_timesteps");
+        return FDTD_ERR_STATE;
+    }
+    if (err & 2) {
+        set_error("energy reduction is not finite (NaN/Inf in the fields)");
+        return FDTD_ERR_NONFINITE;
+    }
+    return FDTD_OK;
+}
+
+// --------------------------------------------------------------- TMA maps
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     if (!fn) {
@@ -793,19 +359,19 @@ int field_map(CUtensorMap* m, float* base, const fdtd_engine_s* e, uint32_t box_
     return FDTD_OK;
 }
 
-int index_map(CUtensorMap* m, void* base, const fdtd_engine_s* e, uint32_t box_z) {
+int index_map(CUtensorMap* m, void* base, const fdtd_engine_s* e, bool idx16) {
     PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
     if (!enc) {
         set_error("cuTensorMapEncodeTiled is not available from the driver");
         return FDTD_ERR_CUDA;
     }
-    const cuuint64_t ib = e->idx16 ? 2 : 4;
+    const cuuint64_t ib = idx16 ? 2 : 4;
     cuuint64_t dims[3] = {e->N[2], e->N[1], e->N[0]};
     cuuint64_t strides[2] = {(cuuint64_t)e->Nzp * ib, (cuuint64_t)e->N[1] * e->Nzp * ib};
-    cuuint32_t box[3] = {box_z, TMA_TY, 1};
+    cuuint32_t box[3] = {32, TMA_TY, 1};
     cuuint32_t es[3] = {1, 1, 1};
-    CUresult r = enc(m, e->idx16 ? CU_TENSOR_MAP_DATA_TYPE_UINT16 : CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, base, dims,
-                     strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+    CUresult r = enc(m, idx16 ? CU_TENSOR_MAP_DATA_TYPE_UINT16 : CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, base, dims, strides,
+                     box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         set_error("cuTensorMapEncodeTiled (index) failed: " + std::to_string((int)r));
@@ -816,32 +382,35 @@ int index_map(CUtensorMap* m, void* base, const fdtd_engine_s* e, uint32_t box_z
 
 int make_maps(fdtd_engine_s* e) {
     int rc;
-    const uint32_t TZ = 32u * (uint32_t)e->zw;
-    if ((rc = field_map(&e->maps.I_halo, e->I.p, e, TZ + 4, TMA_TY + 1)) ||
-        (rc = field_map(&e->maps.I_own, e->I.p, e, TZ, TMA_TY)) ||
-        (rc = field_map(&e->maps.V_halo, e->V.p, e, TZ + 4, TMA_TY + 1)) ||
-        (rc = field_map(&e->maps.V_own, e->V.p, e, TZ, TMA_TY)) || (rc = index_map(&e->maps.idx, e->idx.p, e, TZ)))
+    if ((rc = field_map(&e->maps.I_halo, e->I.p, e, 36, TMA_TY + 1)) ||
+        (rc = field_map(&e->maps.I_own, e->I.p, e, 32, TMA_TY)) ||
+        (rc = field_map(&e->maps.V_halo, e->V.p, e, 36, TMA_TY + 1)) ||
+        (rc = field_map(&e->maps.V_own, e->V.p, e, 32, TMA_TY)) ||
+        (rc = index_map(&e->maps.idxE, e->E.idx.p, e, e->E.idx16)) ||
+        (rc = index_map(&e->maps.idxH, e->H.idx.p, e, e->H.idx16)))
         return rc;
-    if (e->FV.p && ((rc = field_map(&e->maps.FV_own, e->FV.p, e, TZ, TMA_TY)) ||
-                    (rc = field_map(&e->maps.FI_own, e->FI.p, e, TZ, TMA_TY))))
+    if (e->FV.p && ((rc = field_map(&e->maps.FV_own, e->FV.p, e, 32, TMA_TY)) ||
+                    (rc = field_map(&e->maps.FI_own, e->FI.p, e, 32, TMA_TY))))
         return rc;
     return FDTD_OK;
 }
 
-template <typename IdxT, int FEAT, int ZW>
-cudaError_t set_attr_one(int bytes) {
-    cudaError_t e1 = cudaFuncSetAttribute(k_volt_tma<IdxT, FEAT, ZW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaError_t e2 = cudaFuncSetAttribute(k_curr_tma<IdxT, FEAT, true, ZW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaError_t e3 = cudaFuncSetAttribute(k_curr_tma<IdxT, FEAT, false, ZW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    return e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3);
+template <typename IdxT, int FEAT, bool GEO>
+cudaError_t smem_attr_one(int bytes) {
+    const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    cudaError_t r[3] = {cudaFuncSetAttribute(k_volt_tma<IdxT, FEAT, GEO>, a, bytes),
+                        cudaFuncSetAttribute(k_curr_tma<IdxT, FEAT, GEO, true>, a, bytes),
+                        cudaFuncSetAttribute(k_curr_tma<IdxT, FEAT, GEO, false>, a, bytes)};
+    for (cudaError_t x : r)
+        if (x != cudaSuccess) return x;
+    return cudaSuccess;
 }
 
 int set_smem_attrs(int bytes) {
-    cudaError_t r = cudaSuccess;
-    cudaError_t t;
-#define WIPEMS_ATTR(I, F)                                                  \
-    if ((t = set_attr_one<I, F, 1>(bytes)) != cudaSuccess) r = t;          \
-    if ((t = set_attr_one<I, F, 2>(bytes)) != cudaSuccess) r = t;
+    cudaError_t r = cudaSuccess, t;
+#define WIPEMS_ATTR(I, F)                                                 \
+    if ((t = smem_attr_one<I, F, false>(bytes)) != cudaSuccess) r = t;    \
+    if ((t = smem_attr_one<I, F, true>(bytes)) != cudaSuccess) r = t;
     WIPEMS_ATTR(uint16_t, 0) WIPEMS_ATTR(uint16_t, 1) WIPEMS_ATTR(uint16_t, 2) WIPEMS_ATTR(uint16_t, 3)
     WIPEMS_ATTR(uint32_t, 0) WIPEMS_ATTR(uint32_t, 1) WIPEMS_ATTR(uint32_t, 2) WIPEMS_ATTR(uint32_t, 3)
 #undef WIPEMS_ATTR
@@ -852,6 +421,7 @@ int set_smem_attrs(int bytes) {
     return FDTD_OK;
 }
 
+// ----------------------------------------------------------- engine state
 // Engine::Init state: all fields and extension states zero, numTS = 0,
 // no recorded samples (the ts = 0 sample is taken again on the next iterate).
 int reset_state(fdtd_engine_s* e) {
@@ -868,8 +438,30 @@ int reset_state(fdtd_engine_s* e) {
     return FDTD_OK;
 }
 
-// Operator::CreateEngine + Engine::Init for the CUDA engine: allocate the
-// device arrays (fields start at zero) and copy the compressed operator.
+int upload_half(fdtd_engine_s* e, const HalfTables& T, DevHalfBufs& B, DevHalf& D) {
+    int rc;
+    uint64_t& tot = e->device_bytes;
+    B.idx16 = T.idx16;
+    if ((rc = B.idx.alloc(T.idx_bytes, tot)) || (rc = B.main.alloc(T.main.size(), tot)) ||
+        (rc = B.exc.alloc(std::max<size_t>(4, T.exc.size()), tot)) || (rc = B.upml.alloc(T.upml.size(), tot)) ||
+        (rc = B.ade.alloc(T.ade.size(), tot)))
+        return rc;
+    auto h2d = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+        return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, e->stream) : cudaSuccess;
+    };
+    CK(h2d(B.idx.p, T.idx, T.idx_bytes));
+    CK(h2d(B.main.p, T.main.data(), T.main.size() * sizeof(float)));
+    CK(h2d(B.exc.p, T.exc.data(), T.exc.size() * sizeof(float)));
+    CK(h2d(B.upml.p, T.upml.data(), T.upml.size() * sizeof(float)));
+    CK(h2d(B.ade.p, T.ade.data(), T.ade.size() * sizeof(float)));
+    D.idx = B.idx.p;
+    D.main = reinterpret_cast<const float4*>(B.main.p);
+    D.upml = reinterpret_cast<const float4*>(B.upml.p);
+    D.ade = reinterpret_cast<const float4*>(B.ade.p);
+    D.exc = reinterpret_cast<const float4*>(B.exc.p);
+    return FDTD_OK;
+}
+
 int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine_s* e) {
     for (int a = 0; a < 3; ++a) e->N[a] = c->N[a];
     e->dT = c->dT;
@@ -883,75 +475,63 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
         set_error("tile_y must be 1..8");
         return FDTD_ERR_ARG;
     }
-    e->XC = (opts && opts->x_chunk > 0) ? opts->x_chunk : 16;
+    e->XC = (opts && opts->x_chunk > 0) ? opts->x_chunk : 8;
     e->interval = opts ? opts->probe_interval : 0;
     e->energy_on_probe = opts ? opts->energy_on_probe != 0 : true;
     e->use_graphs = opts ? opts->use_graphs != 0 : true;
-    uint32_t maxts = (opts && opts->max_timesteps) ? opts->max_timesteps : 100000;
+    e->use_tma = !(opts && opts->kernel == 1);
+    e->stages = (opts && opts->stages > 0) ? opts->stages : 3;
+    if (e->stages < 3 || e->stages > TMA_MAX_STAGES) {
+        set_error("stages must be 3..8");
+        return FDTD_ERR_ARG;
+    }
+    const uint32_t maxts = (opts && opts->max_timesteps) ? opts->max_timesteps : 100000;
     e->cap = (e->interval ? maxts / e->interval : 0) + 2;
-    e->num_tuples = c->num_tuples;
+    e->num_tuples_e = c->E.num_tuples;
+    e->num_tuples_h = c->H.num_tuples;
     e->upml_nodes = c->upml_nodes;
     e->ade_nodes = c->ade_nodes;
-    e->idx16 = c->idx16;
-    e->feat = c->feat;
     e->Nzp = c->Nzp;
     e->comp = c->comp;
-    const uint32_t Nx = e->N[0], Ny = e->N[1], Nz = e->N[2];
+    e->geo_on = c->geo;
+    const bool any_upml = c->E.any_upml || c->H.any_upml;
+    const bool any_ade = c->E.any_ade || c->H.any_ade;
+    e->feat = (any_upml ? FEAT_UPML : 0) | (any_ade ? FEAT_ADE : 0);
 
     int rc;
     uint64_t& tot = e->device_bytes;
     const size_t F = 3 * (size_t)e->comp;
     if ((rc = e->V.alloc(F, tot)) || (rc = e->I.alloc(F, tot))) return rc;
-    if (c->any_upml && ((rc = e->FV.alloc(F, tot)) || (rc = e->FI.alloc(F, tot)))) return rc;
-    if (c->any_ade_e && (rc = e->AV.alloc(F, tot))) return rc;
-    if (c->any_lor_e && (rc = e->LV.alloc(F, tot))) return rc;
-    if (c->any_ade_h && (rc = e->AI.alloc(F, tot))) return rc;
-    if (c->any_lor_h && (rc = e->LI.alloc(F, tot))) return rc;
-    if ((rc = e->idx.alloc(c->idx_bytes, tot))) return rc;
-    if ((rc = e->tabE.alloc(c->hE.size(), tot)) || (rc = e->tabH.alloc(c->hH.size(), tot)) ||
-        (rc = e->tabEX.alloc(c->hEX.size(), tot)) || (rc = e->tabHX.alloc(c->hHX.size(), tot)))
+    if (any_upml && ((rc = e->FV.alloc(F, tot)) || (rc = e->FI.alloc(F, tot)))) return rc;
+    if (c->E.any_ade && (rc = e->AV.alloc(F, tot))) return rc;
+    if (c->E.any_lor && (rc = e->LV.alloc(F, tot))) return rc;
+    if (c->H.any_ade && (rc = e->AI.alloc(F, tot))) return rc;
+    if (c->H.any_lor && (rc = e->LI.alloc(F, tot))) return rc;
+    if ((rc = e->sigV.alloc(std::max<uint32_t>(1, c->sig_len), tot)) ||
+        (rc = e->sigC.alloc(std::max<uint32_t>(1, c->sig_len), tot)))
         return rc;
-    if (c->any_upml && ((rc = e->tabEU.alloc(c->hEU.size(), tot)) || (rc = e->tabHU.alloc(c->hHU.size(), tot))))
-        return rc;
-    if ((c->feat & FEAT_ADE) && ((rc = e->tabEA.alloc(c->hEA.size(), tot)) || (rc = e->tabHA.alloc(c->hHA.size(), tot))))
-        return rc;
-    uint32_t sl = std::max<uint32_t>(1, c->sig_len);
-    if ((rc = e->sigV.alloc(sl, tot)) || (rc = e->sigC.alloc(sl, tot))) return rc;
     if ((rc = e->d_ts.alloc(1, tot)) || (rc = e->d_eacc.alloc(2, tot)) || (rc = e->d_energy_tmp.alloc(2, tot)) ||
         (rc = e->d_nsamp.alloc(1, tot)) || (rc = e->d_err.alloc(1, tot)))
         return rc;
-
-    cudaStream_t s = e->stream;
-    auto h2d = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
-        return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s) : cudaSuccess;
-    };
-    CK(h2d(e->idx.p, c->idx, c->idx_bytes));
-    CK(h2d(e->tabE.p, c->hE.data(), c->hE.size() * sizeof(float4)));
-    CK(h2d(e->tabH.p, c->hH.data(), c->hH.size() * sizeof(float4)));
-    CK(h2d(e->tabEX.p, c->hEX.data(), c->hEX.size() * sizeof(float4)));
-    CK(h2d(e->tabHX.p, c->hHX.data(), c->hHX.size() * sizeof(float4)));
-    if (c->any_upml) {
-        CK(h2d(e->tabEU.p, c->hEU.data(), c->hEU.size() * sizeof(float4)));
-        CK(h2d(e->tabHU.p, c->hHU.data(), c->hHU.size() * sizeof(float4)));
-    }
-    if (c->feat & FEAT_ADE) {
-        CK(h2d(e->tabEA.p, c->hEA.data(), c->hEA.size() * sizeof(float4)));
-        CK(h2d(e->tabHA.p, c->hHA.data(), c->hHA.size() * sizeof(float4)));
+    DevGrid& g = e->g;
+    if ((rc = upload_half(e, c->E, e->E, g.e)) || (rc = upload_half(e, c->H, e->H, g.h))) return rc;
+    if (c->geo) {
+        if ((rc = e->geo.alloc(c->geom.size(), tot))) return rc;
+        CK(cudaMemcpyAsync(e->geo.p, c->geom.data(), c->geom.size() * sizeof(float), cudaMemcpyHostToDevice,
+                           e->stream));
     }
     if (c->sig_len) {
-        CK(h2d(e->sigV.p, c->sigV.data(), c->sig_len * sizeof(float)));
-        CK(h2d(e->sigC.p, c->sigC.data(), c->sig_len * sizeof(float)));
+        CK(cudaMemcpyAsync(e->sigV.p, c->sigV.data(), c->sig_len * sizeof(float), cudaMemcpyHostToDevice, e->stream));
+        CK(cudaMemcpyAsync(e->sigC.p, c->sigC.data(), c->sig_len * sizeof(float), cudaMemcpyHostToDevice, e->stream));
     } else {
-        CK(cudaMemsetAsync(e->sigV.p, 0, sizeof(float), s));
-        CK(cudaMemsetAsync(e->sigC.p, 0, sizeof(float), s));
+        CK(cudaMemsetAsync(e->sigV.p, 0, sizeof(float), e->stream));
+        CK(cudaMemsetAsync(e->sigC.p, 0, sizeof(float), e->stream));
     }
-
-    DevGrid& g = e->g;
-    g.Nx = (int)Nx;
-    g.Ny = (int)Ny;
-    g.Nz = (int)Nz;
+    g.Nx = (int)e->N[0];
+    g.Ny = (int)e->N[1];
+    g.Nz = (int)e->N[2];
     g.Nzp = e->Nzp;
-    g.sx = (long long)Ny * e->Nzp;
+    g.sx = (long long)e->N[1] * e->Nzp;
     g.comp = e->comp;
     g.V = e->V.p;
     g.I = e->I.p;
@@ -961,48 +541,27 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     g.LV = e->LV.p;
     g.AI = e->AI.p;
     g.LI = e->LI.p;
-    g.idx = e->idx.p;
-    g.tabE = e->tabE.p;
-    g.tabH = e->tabH.p;
-    g.tabEU = e->tabEU.p;
-    g.tabHU = e->tabHU.p;
-    g.tabEA = e->tabEA.p;
-    g.tabHA = e->tabHA.p;
-    g.tabEX = e->tabEX.p;
-    g.tabHX = e->tabHX.p;
+    g.geo = e->geo.p;
+    g.geo_stride = (int)(e->N[0] + e->N[1] + e->N[2]);
     g.sigV = e->sigV.p;
     g.sigC = e->sigC.p;
     g.sig_len = (int)c->sig_len;
     g.sig_period = (int)c->sig_period;
     g.d_ts = e->d_ts.p;
     g.d_eacc = e->d_eacc.p;
-    e->smem_bytes = 2 * 3 * (size_t)(e->TY + 1) * 33 * sizeof(float);
-    e->use_tma = !(opts && opts->kernel == 1);
-    e->stages = (opts && opts->stages > 0) ? opts->stages : 3;
-    e->zw = (opts && opts->z_per_thread > 0) ? opts->z_per_thread : 2;
-    if (e->zw != 1 && e->zw != 2) {
-        set_error("z_per_thread must be 1 or 2");
-        return FDTD_ERR_ARG;
-    }
-    if (e->stages < 3 || e->stages > TMA_MAX_STAGES) {
-        set_error("stages must be 3..8");
-        return FDTD_ERR_ARG;
-    }
-    if (e->use_tma) {
-        // opt in to more than 48 KB of dynamic shared memory where needed
-        const size_t need = (e->feat & FEAT_UPML) ? StageLayout<uint32_t, true, 2>::smem(e->stages)
-                                                  : StageLayout<uint32_t, false, 2>::smem(e->stages);
-        if (need > 48 * 1024) {
-            if ((rc = set_smem_attrs((int)need))) return rc;
-        }
-    }
+    e->smem_direct = 2 * 3 * (size_t)(e->TY + 1) * 33 * sizeof(float);
     for (int a = 0; a < 3; ++a) {
         e->ti.lo[a] = c->inner_lo[a];
         e->ti.hi[a] = c->inner_hi[a];
         e->ti.ne[a] = (int)e->N[a] - (c->trim_e[a] ? 1 : 0);
     }
     e->ti.d_err = e->d_err.p;
-    if (e->use_tma && (rc = make_maps(e))) return rc;
+    if (e->use_tma) {
+        if ((rc = make_maps(e))) return rc;
+        const size_t need = (e->feat & FEAT_UPML) ? StageLayout<uint32_t, true>::smem(e->stages)
+                                                  : StageLayout<uint32_t, false>::smem(e->stages);
+        if (need > 48 * 1024 && (rc = set_smem_attrs((int)need))) return rc;
+    }
     return reset_state(e);
 }
 
@@ -1028,7 +587,7 @@ int probe_entries(const fdtd_engine_s* e, const fdtd_probe_desc* p, std::vector<
     const uint32_t* start = p->start;
     const uint32_t* stop = p->stop;
     if (p->type == 0) {
-        int dims = (start[0] != stop[0]) + (start[1] != stop[1]) + (start[2] != stop[2]);
+        const int dims = (start[0] != stop[0]) + (start[1] != stop[1]) + (start[2] != stop[2]);
         if (dims != 1) return FDTD_OK;  // the reference prints an error and returns 0
         for (int n = 0; n < 3; ++n) {
             if (start[n] < stop[n]) {
@@ -1089,73 +648,6 @@ int probe_entries(const fdtd_engine_s* e, const fdtd_probe_desc* p, std::vector<
 // ===================================================================== C ABI
 extern "C" {
 
-int fdtd_compress(const fdtd_op_desc* desc, fdtd_cop_t* out) {
-    if (!desc || !out) {
-        set_error("fdtd_compress: null argument");
-        return FDTD_ERR_ARG;
-    }
-    fdtd_cop_s* c = new (std::nothrow) fdtd_cop_s();
-    if (!c) return FDTD_ERR_NOMEM;
-    int rc;
-    try {
-        rc = compress_op(desc, c);
-    } catch (const std::bad_alloc&) {
-        set_error("fdtd_compress: host allocation failed");
-        rc = FDTD_ERR_NOMEM;
-    }
-    if (rc != FDTD_OK) {
-        delete c;
-        return rc;
-    }
-    *out = c;
-    return FDTD_OK;
-}
-
-int fdtd_cop_destroy(fdtd_cop_t c) {
-    delete c;
-    return FDTD_OK;
-}
-
-int fdtd_cop_get_info(fdtd_cop_t c, fdtd_cop_info* info) {
-    if (!c || !info) return FDTD_ERR_ARG;
-    std::memset(info, 0, sizeof(*info));
-    for (int a = 0; a < 3; ++a) info->num_lines[a] = c->N[a];
-    info->num_tuples = c->num_tuples;
-    info->index_bytes = c->idx16 ? 2 : 4;
-    info->padded_nz = (uint32_t)c->Nzp;
-    info->num_upml_nodes = c->upml_nodes;
-    info->num_ade_nodes = c->ade_nodes;
-    info->host_bytes = c->idx_bytes + (c->hE.size() + c->hH.size() + c->hEU.size() + c->hHU.size() + c->hEA.size() +
-                                       c->hHA.size() + c->hEX.size() + c->hHX.size()) * sizeof(float4);
-    info->pinned = c->idx_pinned ? 1 : 0;
-    return FDTD_OK;
-}
-
-int fdtd_cop_expand(fdtd_cop_t c, float* vv, float* vi, float* ii, float* iv, uint32_t* flags_e, uint32_t* flags_h) {
-    if (!c) return FDTD_ERR_ARG;
-    const uint32_t Nx = c->N[0], Ny = c->N[1], Nz = c->N[2];
-    const size_t NN = (size_t)Nx * Ny * Nz;
-    for (uint32_t x = 0; x < Nx; ++x)
-        for (uint32_t y = 0; y < Ny; ++y)
-            for (uint32_t z = 0; z < Nz; ++z) {
-                const size_t pi = ((size_t)x * Ny + y) * c->Nzp + z;
-                const uint32_t t = c->idx16 ? reinterpret_cast<const uint16_t*>(c->idx)[pi]
-                                            : reinterpret_cast<const uint32_t*>(c->idx)[pi];
-                const float* e = reinterpret_cast<const float*>(&c->hE[2 * (size_t)t]);
-                const float* h = reinterpret_cast<const float*>(&c->hH[2 * (size_t)t]);
-                const size_t gi = ((size_t)x * Ny + y) * Nz + z;
-                for (int n = 0; n < 3; ++n) {
-                    if (vv) vv[n * NN + gi] = e[n];
-                    if (vi) vi[n * NN + gi] = e[3 + n];
-                    if (ii) ii[n * NN + gi] = h[n];
-                    if (iv) iv[n * NN + gi] = h[3 + n];
-                }
-                if (flags_e) std::memcpy(&flags_e[gi], &e[6], 4);
-                if (flags_h) std::memcpy(&flags_h[gi], &h[6], 4);
-            }
-    return FDTD_OK;
-}
-
 int fdtd_engine_create_compressed(fdtd_cop_t cop, const fdtd_engine_opts* opts, fdtd_engine_t* out) {
     if (!cop || !out) {
         set_error("fdtd_engine_create_compressed: null argument");
@@ -1163,9 +655,15 @@ int fdtd_engine_create_compressed(fdtd_cop_t cop, const fdtd_engine_opts* opts, 
     }
     fdtd_engine_s* e = new (std::nothrow) fdtd_engine_s();
     if (!e) return FDTD_ERR_NOMEM;
-    int rc = upload_engine(cop, opts, e);
+    int rc;
+    try {
+        rc = upload_engine(cop, opts, e);
+    } catch (const std::bad_alloc&) {
+        set_error("fdtd_engine_create: host allocation failed");
+        rc = FDTD_ERR_NOMEM;
+    }
     if (rc == FDTD_OK) {
-        cudaError_t ce = cudaStreamSynchronize(e->stream);
+        const cudaError_t ce = cudaStreamSynchronize(e->stream);
         if (ce != cudaSuccess) {
             set_error(std::string("engine upload: ") + cudaGetErrorString(ce));
             rc = FDTD_ERR_CUDA;
@@ -1209,7 +707,7 @@ int fdtd_engine_add_probe(fdtd_engine_t e, const fdtd_probe_desc* p, uint32_t* s
         return FDTD_ERR_STATE;
     }
     std::vector<ProbeEntry> ent;
-    int rc = probe_entries(e, p, ent);
+    const int rc = probe_entries(e, p, ent);
     if (rc) return rc;
     e->h_entries.insert(e->h_entries.end(), ent.begin(), ent.end());
     e->h_first.push_back((int)e->h_entries.size());
@@ -1223,18 +721,8 @@ int fdtd_engine_iterate(fdtd_engine_t e, uint32_t n) {
     CK(cudaSetDevice(e->device));
     e->last_launches = 0;
     int rc;
-    if (!e->started) {
-        if ((rc = upload_probes(e))) return rc;
-        e->started = true;
-        if (e->interval && e->use_graphs && (rc = build_chunk_graph(e))) return rc;
-    }
     CK(cudaEventRecord(e->ev0, e->stream));
-    if (e->need_initial_sample) {
-        e->need_initial_sample = false;
-        if (e->interval) {  // sample at ts = 0 (RunFDTD's PA->Process() before the loop)
-            if ((rc = launch_advance(e, 0, true, e->energy_on_probe))) return rc;
-        }
-    }
+    if ((rc = start(e))) return rc;
     uint32_t left = n;
     while (left > 0) {
         if (e->interval && e->use_graphs && e->chunk && (e->ts % e->interval) == 0 && left >= e->interval) {
@@ -1244,7 +732,7 @@ int fdtd_engine_iterate(fdtd_engine_t e, uint32_t n) {
             left -= e->interval;
             continue;
         }
-        bool sample = e->interval && ((e->ts + 1) % e->interval) == 0;
+        const bool sample = e->interval && ((e->ts + 1) % e->interval) == 0;
         if ((rc = launch_step(e, 0, sample && e->energy_on_probe))) return rc;
         if ((rc = launch_advance(e, 1, sample, e->energy_on_probe))) return rc;
         e->ts += 1;
@@ -1255,21 +743,7 @@ int fdtd_engine_iterate(fdtd_engine_t e, uint32_t n) {
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
     e->last_ms = ms;
-    int err = 0;
-    CK(cudaMemcpy(&err, e->d_err.p, sizeof(int), cudaMemcpyDeviceToHost));
-    if (err & 1) {
-        set_error("probe sample ring overflow: raise max_timesteps");
-        return FDTD_ERR_STATE;
-    }
-    if (err & 4) {
-        set_error("a bounded device wait gave up: a TMA copy did not complete in time");
-        return FDTD_ERR_TIMEOUT;
-    }
-    if (err & 2) {
-        set_error("energy reduction is not finite (NaN/Inf in the fields)");
-        return FDTD_ERR_NONFINITE;
-    }
-    return FDTD_OK;
+    return check_error_word(e);
 }
 
 int fdtd_engine_num_timesteps(fdtd_engine_t e, uint32_t* ts) {
@@ -1296,7 +770,7 @@ int fdtd_engine_read_samples(fdtd_engine_t e, uint32_t first, uint32_t count, ui
                              double* energy) {
     if (!e) return FDTD_ERR_ARG;
     uint32_t n = 0;
-    int rc = fdtd_engine_num_samples(e, &n);
+    const int rc = fdtd_engine_num_samples(e, &n);
     if (rc) return rc;
     if (first + count > n) {
         set_error("fdtd_engine_read_samples: range beyond recorded samples");
@@ -1340,7 +814,7 @@ int fdtd_engine_get_fields(fdtd_engine_t e, float* volt, float* curr) {
         float* dst = which ? curr : volt;
         if (!dst) continue;
         const float* src = which ? e->I.p : e->V.p;
-        // strided 3-D copy: rows of Nz floats out of rows of Nzp floats
+        // rows of Nz floats out of rows of Nzp floats
         CK(cudaMemcpy2DAsync(dst, Nz * sizeof(float), src, e->Nzp * sizeof(float), Nz * sizeof(float),
                              (size_t)3 * Nx * Ny, cudaMemcpyDeviceToHost, e->stream));
     }
@@ -1354,7 +828,7 @@ static int get_one(fdtd_engine_t e, const float* base, uint32_t n, uint32_t x, u
         return FDTD_ERR_ARG;
     }
     CK(cudaSetDevice(e->device));
-    long long off = n * e->comp + (long long)x * e->g.sx + (long long)y * e->Nzp + z;
+    const long long off = n * e->comp + (long long)x * e->g.sx + (long long)y * e->Nzp + z;
     CK(cudaMemcpyAsync(v, base + off, sizeof(float), cudaMemcpyDeviceToHost, e->stream));
     CK(cudaStreamSynchronize(e->stream));
     return FDTD_OK;
@@ -1371,46 +845,17 @@ int fdtd_engine_profile_kernels(fdtd_engine_t e, uint32_t n_steps, double* ms_vo
     if (!e || n_steps == 0) return FDTD_ERR_ARG;
     CK(cudaSetDevice(e->device));
     int rc;
-    if (!e->started) {
-        if ((rc = upload_probes(e))) return rc;
-        e->started = true;
-        if (e->interval && e->use_graphs && (rc = build_chunk_graph(e))) return rc;
-    }
-    if (e->need_initial_sample) {
-        e->need_initial_sample = false;
-        if (e->interval && (rc = launch_advance(e, 0, true, e->energy_on_probe))) return rc;
-    }
+    if ((rc = start(e))) return rc;
     std::vector<cudaEvent_t> ev(3 * (size_t)n_steps);
     for (auto& x : ev) CK(cudaEventCreate(&x));
-    dim3 block(32, e->TY);
-    dim3 gv((e->N[2] + 31) / 32, (e->N[1] + e->TY - 1) / e->TY, (e->N[0] + e->XC - 1) / e->XC);
-    dim3 gc((e->N[2] + 31) / 32, (e->N[1] + e->TY - 1) / e->TY, (e->N[0] - 1 + e->XC - 1) / e->XC);
     for (uint32_t k = 0; k < n_steps; ++k) {
-        bool sample = e->interval && ((e->ts + 1) % e->interval) == 0;
-        bool energy = sample && e->energy_on_probe;
-        VoltFn fv = e->idx16 ? pick_volt<uint16_t>(e->feat) : pick_volt<uint32_t>(e->feat);
-        CurrFn fc = e->idx16 ? pick_curr<uint16_t>(e->feat, energy) : pick_curr<uint32_t>(e->feat, energy);
+        const bool sample = e->interval && ((e->ts + 1) % e->interval) == 0;
         CK(cudaEventRecord(ev[3 * k], e->stream));
-        if (e->use_tma) {
-            // volt then curr with an event in between
-            if (e->idx16)
-                launch_tma_half<uint16_t>(e, 0, energy, true);
-            else
-                launch_tma_half<uint32_t>(e, 0, energy, true);
-        } else {
-            fv<<<gv, block, e->smem_bytes, e->stream>>>(e->g, 0, e->XC);
-        }
+        launch_volt(e, 0);
         CK(cudaEventRecord(ev[3 * k + 1], e->stream));
-        if (e->use_tma) {
-            if (e->idx16)
-                launch_tma_half<uint16_t>(e, 0, energy, false);
-            else
-                launch_tma_half<uint32_t>(e, 0, energy, false);
-        } else {
-            fc<<<gc, block, e->smem_bytes, e->stream>>>(e->g, 0, e->XC);
-        }
+        launch_curr(e, 0, sample && e->energy_on_probe);
         CK(cudaEventRecord(ev[3 * k + 2], e->stream));
-        CK(cudaGetLastError());
+        if ((rc = check_launch())) return rc;
         if ((rc = launch_advance(e, 1, sample, e->energy_on_probe))) return rc;
         e->ts += 1;
     }
@@ -1426,19 +871,19 @@ int fdtd_engine_profile_kernels(fdtd_engine_t e, uint32_t n_steps, double* ms_vo
     for (auto& x : ev) cudaEventDestroy(x);
     if (ms_volt) *ms_volt = sv / n_steps;
     if (ms_curr) *ms_curr = sc / n_steps;
-    return FDTD_OK;
+    return check_error_word(e);
 }
 
 int fdtd_engine_get_stats(fdtd_engine_t e, fdtd_engine_stats* st) {
     if (!e || !st) return FDTD_ERR_ARG;
     std::memset(st, 0, sizeof(*st));
-    st->num_tuples = e->num_tuples;
-    st->index_bytes = e->idx16 ? 2 : 4;
+    st->num_tuples = std::max(e->num_tuples_e, e->num_tuples_h);
+    st->index_bytes = (e->E.idx16 && e->H.idx16) ? 2 : 4;
     st->num_upml_nodes = e->upml_nodes;
     st->num_ade_nodes = e->ade_nodes;
     st->padded_nz = (uint32_t)e->Nzp;
     st->device_bytes = e->device_bytes;
-    st->tile_y = (uint32_t)e->TY;
+    st->tile_y = (uint32_t)(e->use_tma ? TMA_TY : e->TY);
     st->x_chunk = (uint32_t)e->XC;
     return FDTD_OK;
 }

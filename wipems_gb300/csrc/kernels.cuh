@@ -1,88 +1,21 @@
-// Device side of the GB300 FDTD engine: the two fused half-step kernels,
-// the probe / energy reductions and the timestep counter.
-//
-// Per-cell math restated from the reference (citations relative to it):
-//   voltage update   FDTD/engine.cpp:108-161 (SSE twin engine_sse_compressed.cpp:48-156)
-//   current update   FDTD/engine.cpp:163-210 (SSE twin engine_sse_compressed.cpp:158-263)
-//   UPML flux swap   extensions/engine_ext_upml.cpp:57-239, fused as
-//                      f  = vvp*V - vvfo*F                     (pre)
-//                      Fn = F*vv + vi*curl                     (main, V<-F)
-//                      V  = f + vvfn*Fn ; F = Fn               (post)
-//   Lorentz/Drude    extensions/engine_ext_lorentzmaterial.cpp:79-173 (pre, old V)
-//                    extensions/engine_ext_dispersive.cpp:76-132 (V -= ADE after)
-//   excitation       extensions/engine_ext_excitation.cpp:33-99 (added last)
-// Hook order per half-step follows Engine::IterateTS (engine.cpp:255-274)
-// with the priorities of engine_extension.h:21-29: ADE-pre, UPML-pre, main,
-// UPML-post, ADE-apply, excitation.  Every product and sum is rounded in the
-// reference's order (__fmul_rn/__fadd_rn, no FMA contraction), so the device
-// result is bit-identical to the FP32 CPU engine.
+// Direct-load half-step kernels (fallback variant), the probe / energy
+// reductions and the timestep counter.  The per-node arithmetic lives in
+// node.cuh; the TMA-pipelined variant of the two half-step kernels is in
+// kernels_tma.cuh.
 #pragma once
 
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "node.cuh"
+
 namespace wipems {
 
-// table entry flags (bits of the 7th float of the main entry)
-constexpr uint32_t TF_UPML = 1u;
-constexpr uint32_t TF_ADE = 2u;
-constexpr uint32_t TF_LOR = 4u;
-constexpr uint32_t TF_EXC = 8u;
-
-// kernel feature bits (compile time)
-constexpr int FEAT_UPML = 1;
-constexpr int FEAT_ADE = 2;
-
-struct DevGrid {
-    int Nx, Ny, Nz;      // mesh lines
-    int Nzp;             // padded z stride (multiple of 32)
-    long long sx;        // x stride (Ny*Nzp)
-    long long comp;      // component stride (Nx*Ny*Nzp)
-    float* V;            // [3][comp]
-    float* I;            // [3][comp]
-    float* FV;           // UPML voltage flux [3][comp] or null
-    float* FI;           // UPML current flux
-    float* AV;           // ADE voltage state (order 1) [3][comp]
-    float* LV;           // Lorentz voltage state
-    float* AI;           // ADE current state
-    float* LI;
-    const void* idx;     // per-node tuple index (uint16 or uint32) [comp]
-    const float4* tabE;  // [T][2] {vv0,vv1,vv2,vi0},{vi1,vi2,flags,-}
-    const float4* tabH;  // [T][2] {ii0,ii1,ii2,iv0},{iv1,iv2,flags,-}
-    const float4* tabEU; // [T][3] {vvp0..2,vvfo0},{vvfo1,vvfo2,vvfn0,vvfn1},{vvfn2,-,-,-}
-    const float4* tabHU; // [T][3]
-    const float4* tabEA; // [T][3] {vint0..2,vext0},{vext1,vext2,vlor0,vlor1},{vlor2,-,-,-}
-    const float4* tabHA; // [T][3]
-    const float4* tabEX; // [T][2] {amp0..2,-},{delay0..2 (int bits),-}
-    const float4* tabHX; // [T][2]
-    const float* sigV;   // excitation signals
-    const float* sigC;
-    int sig_len;
-    int sig_period;      // 0 = none
-    const int* d_ts;     // timestep counter (numTS)
-    double* d_eacc;      // energy accumulators {sum V^2, sum I^2}
-};
-
-template <typename IdxT>
-__device__ __forceinline__ uint32_t load_idx(const void* p, long long o) {
-    return (uint32_t)__ldg(reinterpret_cast<const IdxT*>(p) + o);
-}
-
-__device__ __forceinline__ int exc_index(int numTS, int delay, int length, int period) {
-    // engine_ext_excitation.cpp:44-53
-    int exc_pos = numTS - delay;
-    exc_pos *= (exc_pos > 0);
-    int p = period > 0 ? period : numTS + 1;
-    exc_pos %= p;
-    exc_pos *= (exc_pos < length);
-    return exc_pos;
-}
-
 // --------------------------------------------------------------- E half-step
-// Block: 32 (z) x TY (y) threads, marching over x in [x0, x0+XC).
-// Shared memory double buffer: 3 components x (TY+1) rows x 33 cols; row 0 is
-// the y-1 halo, column 0 the z-1 halo.
-template <typename IdxT, int FEAT>
+// Block: 32 (z) x TY (y) threads, marching over x in [x0, x0+XC).  Shared
+// memory double buffer: 3 components x (TY+1) rows x 33 cols; row 0 is the
+// y-1 halo, column 0 the z-1 halo.
+template <typename IdxT, int FEAT, bool GEO>
 __global__ void __launch_bounds__(256) k_volt(const DevGrid g, int ts_off, int XC) {
     extern __shared__ float smem[];
     const int TY = blockDim.y;
@@ -142,88 +75,11 @@ __global__ void __launch_bounds__(256) k_volt(const DevGrid g, int ts_off, int X
             curl[0] = __fadd_rn(__fsub_rn(__fsub_rn(c2, i2ym), c1), i1zm);
             curl[1] = __fadd_rn(__fsub_rn(__fsub_rn(c0, i0zm), c2), i2xm);
             curl[2] = __fadd_rn(__fsub_rn(__fsub_rn(c1, i1xm), c0), i0ym);
-
-            const uint32_t t = load_idx<IdxT>(g.idx, o);
-            const float4 ta = __ldg(&g.tabE[2 * t]);
-            const float4 tb = __ldg(&g.tabE[2 * t + 1]);
-            const float vvc[3] = {ta.x, ta.y, ta.z};
-            const float vic[3] = {ta.w, tb.x, tb.y};
-            const uint32_t flags = __float_as_uint(tb.z);
-
-            float v[3];
-            v[0] = g.V[o];
-            v[1] = g.V[C + o];
-            v[2] = g.V[2 * C + o];
-
-            // ADE pre-update with the old voltage (Lorentz extension, priority 0)
-            float ade[3] = {0.f, 0.f, 0.f};
-            if ((FEAT & FEAT_ADE) && (flags & TF_ADE)) {
-                const float4 a0 = __ldg(&g.tabEA[3 * t]);
-                const float4 a1 = __ldg(&g.tabEA[3 * t + 1]);
-                const float4 a2 = __ldg(&g.tabEA[3 * t + 2]);
-                const float vint[3] = {a0.x, a0.y, a0.z};
-                const float vext[3] = {a0.w, a1.x, a1.y};
-                const float vlor[3] = {a1.z, a1.w, a2.x};
-                if (flags & TF_LOR) {
-#pragma unroll
-                    for (int n = 0; n < 3; ++n) {
-                        float lor = g.LV[n * C + o];
-                        float a = g.AV[n * C + o];
-                        lor = __fadd_rn(lor, __fmul_rn(vlor[n], a));
-                        a = __fmul_rn(a, vint[n]);
-                        a = __fadd_rn(a, __fmul_rn(vext[n], __fsub_rn(v[n], lor)));
-                        g.LV[n * C + o] = lor;
-                        g.AV[n * C + o] = a;
-                        ade[n] = a;
-                    }
-                } else {
-#pragma unroll
-                    for (int n = 0; n < 3; ++n) {
-                        float a = g.AV[n * C + o];
-                        a = __fmul_rn(a, vint[n]);
-                        a = __fadd_rn(a, __fmul_rn(vext[n], v[n]));
-                        g.AV[n * C + o] = a;
-                        ade[n] = a;
-                    }
-                }
-            }
-
-            if ((FEAT & FEAT_UPML) && (flags & TF_UPML)) {
-                const float4 u0 = __ldg(&g.tabEU[3 * t]);
-                const float4 u1 = __ldg(&g.tabEU[3 * t + 1]);
-                const float4 u2 = __ldg(&g.tabEU[3 * t + 2]);
-                const float vvp[3] = {u0.x, u0.y, u0.z};
-                const float vvfo[3] = {u0.w, u1.x, u1.y};
-                const float vvfn[3] = {u1.z, u1.w, u2.x};
-#pragma unroll
-                for (int n = 0; n < 3; ++n) {
-                    const float F = g.FV[n * C + o];
-                    const float f = __fsub_rn(__fmul_rn(vvp[n], v[n]), __fmul_rn(vvfo[n], F));
-                    const float Fn = __fadd_rn(__fmul_rn(F, vvc[n]), __fmul_rn(vic[n], curl[n]));
-                    g.FV[n * C + o] = Fn;
-                    v[n] = __fadd_rn(f, __fmul_rn(vvfn[n], Fn));
-                }
-            } else {
-#pragma unroll
-                for (int n = 0; n < 3; ++n)
-                    v[n] = __fadd_rn(__fmul_rn(v[n], vvc[n]), __fmul_rn(vic[n], curl[n]));
-            }
-            if ((FEAT & FEAT_ADE) && (flags & TF_ADE)) {
-#pragma unroll
-                for (int n = 0; n < 3; ++n) v[n] = __fsub_rn(v[n], ade[n]);
-            }
-            if (flags & TF_EXC) {
-                const float4 e0 = __ldg(&g.tabEX[2 * t]);
-                const float4 e1 = __ldg(&g.tabEX[2 * t + 1]);
-                const float amp[3] = {e0.x, e0.y, e0.z};
-                const int dly[3] = {__float_as_int(e1.x), __float_as_int(e1.y), __float_as_int(e1.z)};
-#pragma unroll
-                for (int n = 0; n < 3; ++n)
-                    if (dly[n] >= 0) {
-                        const int k = exc_index(numTS, dly[n], g.sig_len, g.sig_period);
-                        v[n] = __fadd_rn(v[n], __fmul_rn(amp[n], g.sigV[k]));
-                    }
-            }
+            const uint32_t t = load_idx<IdxT>(g.e.idx, o);
+            float v[3] = {g.V[o], g.V[C + o], g.V[2 * C + o]};
+            GeoF gf;
+            if (GEO) gf = geo_factors(g, false, x, y, z);
+            update_node<false, FEAT, GEO>(g, v, curl, t, o, numTS, nullptr, 0, gf);
             g.V[o] = v[0];
             g.V[C + o] = v[1];
             g.V[2 * C + o] = v[2];
@@ -237,7 +93,7 @@ __global__ void __launch_bounds__(256) k_volt(const DevGrid g, int ts_off, int X
 // Same tiling; marching over x needs plane x+1 (registers) and the y+1 / z+1
 // neighbours of plane x (shared memory: row TY is the y+1 halo, column 32
 // the z+1 halo).
-template <typename IdxT, int FEAT, bool ENERGY>
+template <typename IdxT, int FEAT, bool GEO, bool ENERGY>
 __global__ void __launch_bounds__(256) k_curr(const DevGrid g, int ts_off, int XC) {
     extern __shared__ float smem[];
     const int TY = blockDim.y;
@@ -254,7 +110,7 @@ __global__ void __launch_bounds__(256) k_curr(const DevGrid g, int ts_off, int X
 
     const long long yz = (long long)y * g.Nzp + z;
     const long long C = g.comp;
-    double esum = 0.0, hsum = 0.0;
+    float es = 0.f, ec = 0.f, hs = 0.f, hc = 0.f;
     float c0 = 0.f, c1 = 0.f, c2 = 0.f;  // V at plane x
     if (inplane && x0 < x1) {
         long long o = (long long)x0 * g.sx + yz;
@@ -299,94 +155,22 @@ __global__ void __launch_bounds__(256) k_curr(const DevGrid g, int ts_off, int X
             curl[0] = __fadd_rn(__fsub_rn(__fsub_rn(c2, v2yp), c1), v1zp);
             curl[1] = __fadd_rn(__fsub_rn(__fsub_rn(c0, v0zp), c2), n2);
             curl[2] = __fadd_rn(__fsub_rn(__fsub_rn(c1, n1), c0), v0yp);
-
-            const uint32_t t = load_idx<IdxT>(g.idx, o);
-            const float4 ta = __ldg(&g.tabH[2 * t]);
-            const float4 tb = __ldg(&g.tabH[2 * t + 1]);
-            const float iic[3] = {ta.x, ta.y, ta.z};
-            const float ivc[3] = {ta.w, tb.x, tb.y};
-            const uint32_t flags = __float_as_uint(tb.z);
-
-            float cu[3];
-            cu[0] = g.I[o];
-            cu[1] = g.I[C + o];
-            cu[2] = g.I[2 * C + o];
-
-            float ade[3] = {0.f, 0.f, 0.f};
-            if ((FEAT & FEAT_ADE) && (flags & TF_ADE)) {
-                const float4 a0 = __ldg(&g.tabHA[3 * t]);
-                const float4 a1 = __ldg(&g.tabHA[3 * t + 1]);
-                const float4 a2 = __ldg(&g.tabHA[3 * t + 2]);
-                const float iint[3] = {a0.x, a0.y, a0.z};
-                const float iext[3] = {a0.w, a1.x, a1.y};
-                const float ilor[3] = {a1.z, a1.w, a2.x};
-                if (flags & TF_LOR) {
-#pragma unroll
-                    for (int n = 0; n < 3; ++n) {
-                        float lor = g.LI[n * C + o];
-                        float a = g.AI[n * C + o];
-                        lor = __fadd_rn(lor, __fmul_rn(ilor[n], a));
-                        a = __fmul_rn(a, iint[n]);
-                        a = __fadd_rn(a, __fmul_rn(iext[n], __fsub_rn(cu[n], lor)));
-                        g.LI[n * C + o] = lor;
-                        g.AI[n * C + o] = a;
-                        ade[n] = a;
-                    }
-                } else {
-#pragma unroll
-                    for (int n = 0; n < 3; ++n) {
-                        float a = g.AI[n * C + o];
-                        a = __fmul_rn(a, iint[n]);
-                        a = __fadd_rn(a, __fmul_rn(iext[n], cu[n]));
-                        g.AI[n * C + o] = a;
-                        ade[n] = a;
-                    }
-                }
-            }
-            if ((FEAT & FEAT_UPML) && (flags & TF_UPML)) {
-                const float4 u0 = __ldg(&g.tabHU[3 * t]);
-                const float4 u1 = __ldg(&g.tabHU[3 * t + 1]);
-                const float4 u2 = __ldg(&g.tabHU[3 * t + 2]);
-                const float iip[3] = {u0.x, u0.y, u0.z};
-                const float iifo[3] = {u0.w, u1.x, u1.y};
-                const float iifn[3] = {u1.z, u1.w, u2.x};
-#pragma unroll
-                for (int n = 0; n < 3; ++n) {
-                    const float F = g.FI[n * C + o];
-                    const float f = __fsub_rn(__fmul_rn(iip[n], cu[n]), __fmul_rn(iifo[n], F));
-                    const float Fn = __fadd_rn(__fmul_rn(F, iic[n]), __fmul_rn(ivc[n], curl[n]));
-                    g.FI[n * C + o] = Fn;
-                    cu[n] = __fadd_rn(f, __fmul_rn(iifn[n], Fn));
-                }
-            } else {
-#pragma unroll
-                for (int n = 0; n < 3; ++n)
-                    cu[n] = __fadd_rn(__fmul_rn(cu[n], iic[n]), __fmul_rn(ivc[n], curl[n]));
-            }
-            if ((FEAT & FEAT_ADE) && (flags & TF_ADE)) {
-#pragma unroll
-                for (int n = 0; n < 3; ++n) cu[n] = __fsub_rn(cu[n], ade[n]);
-            }
-            if (flags & TF_EXC) {
-                const float4 e0 = __ldg(&g.tabHX[2 * t]);
-                const float4 e1 = __ldg(&g.tabHX[2 * t + 1]);
-                const float amp[3] = {e0.x, e0.y, e0.z};
-                const int dly[3] = {__float_as_int(e1.x), __float_as_int(e1.y), __float_as_int(e1.z)};
-#pragma unroll
-                for (int n = 0; n < 3; ++n)
-                    if (dly[n] >= 0) {
-                        const int k = exc_index(numTS, dly[n], g.sig_len, g.sig_period);
-                        cu[n] = __fadd_rn(cu[n], __fmul_rn(amp[n], g.sigC[k]));
-                    }
-            }
+            const uint32_t t = load_idx<IdxT>(g.h.idx, o);
+            float cu[3] = {g.I[o], g.I[C + o], g.I[2 * C + o]};
+            GeoF gf;
+            if (GEO) gf = geo_factors(g, true, x, y, z);
+            update_node<true, FEAT, GEO>(g, cu, curl, t, o, numTS, nullptr, 0, gf);
             g.I[o] = cu[0];
             g.I[C + o] = cu[1];
             g.I[2 * C + o] = cu[2];
             if (ENERGY) {
                 // Engine_Interface_FDTD::CalcFastEnergy terms (float products)
-                esum += (double)__fmul_rn(c0, c0) + (double)__fmul_rn(c1, c1) + (double)__fmul_rn(c2, c2);
-                hsum += (double)__fmul_rn(cu[0], cu[0]) + (double)__fmul_rn(cu[1], cu[1]) +
-                        (double)__fmul_rn(cu[2], cu[2]);
+                kahan_add(es, ec, __fmul_rn(c0, c0));
+                kahan_add(es, ec, __fmul_rn(c1, c1));
+                kahan_add(es, ec, __fmul_rn(c2, c2));
+                kahan_add(hs, hc, __fmul_rn(cu[0], cu[0]));
+                kahan_add(hs, hc, __fmul_rn(cu[1], cu[1]));
+                kahan_add(hs, hc, __fmul_rn(cu[2], cu[2]));
             }
         }
         c0 = n0;
@@ -394,6 +178,7 @@ __global__ void __launch_bounds__(256) k_curr(const DevGrid g, int ts_off, int X
         c2 = n2;
     }
     if (ENERGY) {
+        double esum = (double)es - (double)ec, hsum = (double)hs - (double)hc;
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) {
             esum += __shfl_down_sync(0xffffffffu, esum, off);
@@ -428,9 +213,10 @@ struct ProbeSet {
 };
 
 // Advances numTS by adv (Engine::IterateTS ++numTS) and, when sample is set,
-// records one probe/energy sample row (ProcessIntegral::Process).
-__global__ void k_advance_sample(int* d_ts, int adv, int sample, ProbeSet ps, const DevGrid g,
-                                 int energy_valid, double eps0, double mue0) {
+// records one probe/energy sample row (ProcessIntegral::Process): the probe
+// sums (ProcessVoltage / ProcessCurrent) as warp reductions in double.
+__global__ void k_advance_sample(int* d_ts, int adv, int sample, ProbeSet ps, const DevGrid g, int energy_valid,
+                                 double eps0, double mue0) {
     __shared__ int s_ts, s_row;
     if (threadIdx.x == 0) {
         int ts = *d_ts + adv;

@@ -1,23 +1,22 @@
 // TMA-pipelined half-step kernels (sm_100+/sm_103a).
 //
-// Same per-node arithmetic as kernels.cuh (k_volt / k_curr, which cite the
+// Same per-node arithmetic as the direct kernels (node.cuh, which cites the
 // reference); what changes is how data reaches the SM.  A block owns a tile
-// of TZ = 32*ZW (z) x TY (y) nodes -- each thread updates ZW consecutive z
-// nodes with vector shared/global accesses -- and marches over an x-chunk.  Each x-plane of the
-// tile -- the three field components of both halves with the one-node halo
-// the curl needs, the tuple index and, in UPML tiles, the flux -- is fetched
-// by one thread with cp.async.bulk.tensor (TMA) into a ring of STAGES
+// of 32 (z) x TY (y) nodes and marches over an x-chunk.  Each x-plane of the
+// tile -- the three components of both fields with the one-node halo the
+// curl needs, the tuple index and, in UPML tiles, the flux -- is fetched by
+// one thread with cp.async.bulk.tensor (TMA) into a ring of STAGES
 // shared-memory buffers, STAGES-1 planes ahead of the plane being computed,
 // completion tracked by one mbarrier per stage.  Compute threads read only
 // shared memory and registers; results are stored straight to global.
 //
 // TMA boxes (innermost first; the fourth dimension spans the 3 components):
-//   E kernel: I halo box {TZ+4, TY+1, 1, 3} at (z0-4, y0-1, x)  (z-1, y-1 halo)
-//             V own box  {TZ, TY, 1, 3}     at (z0, y0, x)
-//             idx box    {TZ, TY, 1}        at (z0, y0, x)
-//             V-flux box {TZ, TY, 1, 3}     (UPML tiles only)
-//   H kernel: V halo box {TZ+4, TY+1, 1, 3} at (z0, y0, x)      (z+1, y+1 halo)
-//             I own box  {TZ, TY, 1, 3}, idx box, I-flux box
+//   E kernel: I halo box {36, TY+1, 1, 3} at (z0-4, y0-1, x)  (z-1, y-1 halo)
+//             V own box  {32, TY, 1, 3}   at (z0, y0, x)
+//             E index    {32, TY, 1}      at (z0, y0, x)
+//             V-flux box {32, TY, 1, 3}   (UPML tiles only)
+//   H kernel: V halo box {36, TY+1, 1, 3} at (z0, y0, x)      (z+1, y+1 halo)
+//             I own box  {32, TY, 1, 3}, H index box, I-flux box
 // The innermost start coordinate is always a multiple of 4 floats (16 B);
 // out-of-range parts of a box (z<0, y<0, beyond the grid) read zeros.
 //
@@ -30,7 +29,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
-#include "kernels.cuh"
+#include "node.cuh"
 
 namespace wipems {
 
@@ -39,7 +38,7 @@ constexpr int TMA_TY = 8;
 constexpr unsigned long long TMA_WAIT_CYCLES = 4000000000ull;  // ~2 s at 2 GHz
 
 struct TmaMaps {
-    CUtensorMap I_halo, I_own, V_halo, V_own, FV_own, FI_own, idx;
+    CUtensorMap I_halo, I_own, V_halo, V_own, FV_own, FI_own, idxE, idxH;
 };
 
 // geometry of the UPML slabs: a node is in a slab iff one coordinate is
@@ -105,20 +104,19 @@ __device__ __forceinline__ void tma_3d(void* dst, const CUtensorMap* map, uint64
 }
 
 // stage layout (floats, every buffer 128-byte aligned)
-template <typename IdxT, bool UPML, int ZW>
+template <typename IdxT, bool UPML>
 struct StageLayout {
-    static constexpr int TZ = 32 * ZW;
-    static constexpr int HW = TZ + 4;                            // halo box row width
-    static constexpr int HALO = 3 * (TMA_TY + 1) * HW;           // halo box, 3 components
+    static constexpr int HW = 36;                               // halo box row width
+    static constexpr int HALO = 3 * (TMA_TY + 1) * HW;          // halo box, 3 components
     static constexpr int HALO_A = (HALO + 31) / 32 * 32;
-    static constexpr int OWN = 3 * TMA_TY * TZ;                  // own box, 3 components
-    static constexpr int IDX = TMA_TY * TZ * (int)sizeof(IdxT) / 4;
+    static constexpr int OWN = 3 * TMA_TY * 32;                  // own box, 3 components
+    static constexpr int IDX = TMA_TY * 32 * (int)sizeof(IdxT) / 4;
     static constexpr int IDX_A = (IDX + 31) / 32 * 32;
     static constexpr int FLUX = UPML ? OWN : 0;
     static constexpr int STAGE = HALO_A + OWN + IDX_A + FLUX;    // floats
     static constexpr int HALO_BYTES = HALO * 4;
     static constexpr int OWN_BYTES = OWN * 4;
-    static constexpr int IDX_BYTES = TMA_TY * TZ * (int)sizeof(IdxT);
+    static constexpr int IDX_BYTES = TMA_TY * 32 * (int)sizeof(IdxT);
     // + barriers + slack to align the dynamic shared memory base to 128 bytes
     static size_t smem(int stages) { return (size_t)STAGE * 4 * stages + 8 * TMA_MAX_STAGES + 128; }
 };
@@ -131,211 +129,27 @@ __device__ __forceinline__ bool tile_has_upml(const TileInfo& ti, int x, int y0,
     return false;
 }
 
-__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
-    const float y = __fsub_rn(x, c);
-    const float t = __fadd_rn(s, y);
-    c = __fsub_rn(__fsub_rn(t, s), y);
-    s = t;
-}
-
-// One voltage node: ADE pre-update (old V), main update with the UPML flux
-// swap fused, ADE apply, excitation -- the hook order of Engine::IterateTS.
-// F is the node's old UPML flux (read by the caller from shared or global
-// memory) and is only used for UPML nodes.
-template <int FEAT>
-__device__ __forceinline__ void volt_node(const DevGrid& g, float v[3], const float curl[3], uint32_t t,
-                                          long long o, int numTS, const float* fsrc, int fstride) {
-    const float4 ta = __ldg(&g.tabE[2 * t]);
-    const float4 tb = __ldg(&g.tabE[2 * t + 1]);
-    const float vvc[3] = {ta.x, ta.y, ta.z};
-    const float vic[3] = {ta.w, tb.x, tb.y};
-    const uint32_t flags = __float_as_uint(tb.z);
-    const long long C = g.comp;
-    float ade[3] = {0.f, 0.f, 0.f};
-    if ((FEAT & FEAT_ADE) && (flags & TF_ADE)) {
-        const float4 a0 = __ldg(&g.tabEA[3 * t]);
-        const float4 a1 = __ldg(&g.tabEA[3 * t + 1]);
-        const float4 a2 = __ldg(&g.tabEA[3 * t + 2]);
-        const float vint[3] = {a0.x, a0.y, a0.z};
-        const float vext[3] = {a0.w, a1.x, a1.y};
-        const float vlor[3] = {a1.z, a1.w, a2.x};
-        if (flags & TF_LOR) {
-#pragma unroll
-            for (int n = 0; n < 3; ++n) {
-                float lor = g.LV[n * C + o];
-                float a = g.AV[n * C + o];
-                lor = __fadd_rn(lor, __fmul_rn(vlor[n], a));
-                a = __fmul_rn(a, vint[n]);
-                a = __fadd_rn(a, __fmul_rn(vext[n], __fsub_rn(v[n], lor)));
-                g.LV[n * C + o] = lor;
-                g.AV[n * C + o] = a;
-                ade[n] = a;
-            }
-        } else {
-#pragma unroll
-            for (int n = 0; n < 3; ++n) {
-                float a = g.AV[n * C + o];
-                a = __fmul_rn(a, vint[n]);
-                a = __fadd_rn(a, __fmul_rn(vext[n], v[n]));
-                g.AV[n * C + o] = a;
-                ade[n] = a;
-            }
-        }
-    }
-    if ((FEAT & FEAT_UPML) && (flags & TF_UPML)) {
-        const float4 u0 = __ldg(&g.tabEU[3 * t]);
-        const float4 u1 = __ldg(&g.tabEU[3 * t + 1]);
-        const float4 u2 = __ldg(&g.tabEU[3 * t + 2]);
-        const float vvp[3] = {u0.x, u0.y, u0.z};
-        const float vvfo[3] = {u0.w, u1.x, u1.y};
-        const float vvfn[3] = {u1.z, u1.w, u2.x};
-#pragma unroll
-        for (int n = 0; n < 3; ++n) {
-            const float F = fsrc ? fsrc[n * fstride] : g.FV[n * C + o];
-            const float f = __fsub_rn(__fmul_rn(vvp[n], v[n]), __fmul_rn(vvfo[n], F));
-            const float Fn = __fadd_rn(__fmul_rn(F, vvc[n]), __fmul_rn(vic[n], curl[n]));
-            g.FV[n * C + o] = Fn;
-            v[n] = __fadd_rn(f, __fmul_rn(vvfn[n], Fn));
-        }
-    } else {
-#pragma unroll
-        for (int n = 0; n < 3; ++n) v[n] = __fadd_rn(__fmul_rn(v[n], vvc[n]), __fmul_rn(vic[n], curl[n]));
-    }
-    if ((FEAT & FEAT_ADE) && (flags & TF_ADE)) {
-#pragma unroll
-        for (int n = 0; n < 3; ++n) v[n] = __fsub_rn(v[n], ade[n]);
-    }
-    if (flags & TF_EXC) {
-        const float4 e0 = __ldg(&g.tabEX[2 * t]);
-        const float4 e1 = __ldg(&g.tabEX[2 * t + 1]);
-        const float amp[3] = {e0.x, e0.y, e0.z};
-        const int dly[3] = {__float_as_int(e1.x), __float_as_int(e1.y), __float_as_int(e1.z)};
-#pragma unroll
-        for (int n = 0; n < 3; ++n)
-            if (dly[n] >= 0) {
-                const int k = exc_index(numTS, dly[n], g.sig_len, g.sig_period);
-                v[n] = __fadd_rn(v[n], __fmul_rn(amp[n], g.sigV[k]));
-            }
-    }
-}
-
-// One current node (mirror of volt_node for the H half-step).
-template <int FEAT>
-__device__ __forceinline__ void curr_node(const DevGrid& g, float cu[3], const float curl[3], uint32_t t,
-                                          long long o, int numTS, const float* fsrc, int fstride) {
-    const float4 ta = __ldg(&g.tabH[2 * t]);
-    const float4 tb = __ldg(&g.tabH[2 * t + 1]);
-    const float iic[3] = {ta.x, ta.y, ta.z};
-    const float ivc[3] = {ta.w, tb.x, tb.y};
-    const uint32_t flags = __float_as_uint(tb.z);
-    const long long C = g.comp;
-    float ade[3] = {0.f, 0.f, 0.f};
-    if ((FEAT & FEAT_ADE) && (flags & TF_ADE)) {
-        const float4 a0 = __ldg(&g.tabHA[3 * t]);
-        const float4 a1 = __ldg(&g.tabHA[3 * t + 1]);
-        const float4 a2 = __ldg(&g.tabHA[3 * t + 2]);
-        const float iint[3] = {a0.x, a0.y, a0.z};
-        const float iext[3] = {a0.w, a1.x, a1.y};
-        const float ilor[3] = {a1.z, a1.w, a2.x};
-        if (flags & TF_LOR) {
-#pragma unroll
-            for (int n = 0; n < 3; ++n) {
-                float lor = g.LI[n * C + o];
-                float a = g.AI[n * C + o];
-                lor = __fadd_rn(lor, __fmul_rn(ilor[n], a));
-                a = __fmul_rn(a, iint[n]);
-                a = __fadd_rn(a, __fmul_rn(iext[n], __fsub_rn(cu[n], lor)));
-                g.LI[n * C + o] = lor;
-                g.AI[n * C + o] = a;
-                ade[n] = a;
-            }
-        } else {
-#pragma unroll
-            for (int n = 0; n < 3; ++n) {
-                float a = g.AI[n * C + o];
-                a = __fmul_rn(a, iint[n]);
-                a = __fadd_rn(a, __fmul_rn(iext[n], cu[n]));
-                g.AI[n * C + o] = a;
-                ade[n] = a;
-            }
-        }
-    }
-    if ((FEAT & FEAT_UPML) && (flags & TF_UPML)) {
-        const float4 u0 = __ldg(&g.tabHU[3 * t]);
-        const float4 u1 = __ldg(&g.tabHU[3 * t + 1]);
-        const float4 u2 = __ldg(&g.tabHU[3 * t + 2]);
-        const float iip[3] = {u0.x, u0.y, u0.z};
-        const float iifo[3] = {u0.w, u1.x, u1.y};
-        const float iifn[3] = {u1.z, u1.w, u2.x};
-#pragma unroll
-        for (int n = 0; n < 3; ++n) {
-            const float F = fsrc ? fsrc[n * fstride] : g.FI[n * C + o];
-            const float f = __fsub_rn(__fmul_rn(iip[n], cu[n]), __fmul_rn(iifo[n], F));
-            const float Fn = __fadd_rn(__fmul_rn(F, iic[n]), __fmul_rn(ivc[n], curl[n]));
-            g.FI[n * C + o] = Fn;
-            cu[n] = __fadd_rn(f, __fmul_rn(iifn[n], Fn));
-        }
-    } else {
-#pragma unroll
-        for (int n = 0; n < 3; ++n) cu[n] = __fadd_rn(__fmul_rn(cu[n], iic[n]), __fmul_rn(ivc[n], curl[n]));
-    }
-    if ((FEAT & FEAT_ADE) && (flags & TF_ADE)) {
-#pragma unroll
-        for (int n = 0; n < 3; ++n) cu[n] = __fsub_rn(cu[n], ade[n]);
-    }
-    if (flags & TF_EXC) {
-        const float4 e0 = __ldg(&g.tabHX[2 * t]);
-        const float4 e1 = __ldg(&g.tabHX[2 * t + 1]);
-        const float amp[3] = {e0.x, e0.y, e0.z};
-        const int dly[3] = {__float_as_int(e1.x), __float_as_int(e1.y), __float_as_int(e1.z)};
-#pragma unroll
-        for (int n = 0; n < 3; ++n)
-            if (dly[n] >= 0) {
-                const int k = exc_index(numTS, dly[n], g.sig_len, g.sig_period);
-                cu[n] = __fadd_rn(cu[n], __fmul_rn(amp[n], g.sigC[k]));
-            }
-    }
-}
-
-template <int ZW>
-struct VecT;
-template <>
-struct VecT<1> {
-    typedef float F;
-    __device__ static float get(const float& v, int) { return v; }
-};
-template <>
-struct VecT<2> {
-    typedef float2 F;
-    __device__ static float get(const float2& v, int k) { return k ? v.y : v.x; }
-};
-
 // ------------------------------------------------------------- E half-step
-template <typename IdxT, int FEAT, int ZW>
+template <typename IdxT, int FEAT, bool GEO>
 __global__ void __launch_bounds__(TMA_TY * 32) k_volt_tma(const DevGrid g, const __grid_constant__ TmaMaps m,
                                                           const TileInfo ti, int ts_off, int XC, int STAGES) {
     constexpr bool UPML = (FEAT & FEAT_UPML) != 0;
-    using L = StageLayout<IdxT, UPML, ZW>;
-    using V = VecT<ZW>;
-    typedef typename V::F VF;
-    constexpr int TZ = L::TZ, HW = L::HW;
+    using L = StageLayout<IdxT, UPML>;
+    constexpr int HW = L::HW;
     extern __shared__ __align__(128) float smem_raw[];
     float* smem = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * STAGES);
     const int tz = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * 32 + tz;
-    const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TMA_TY;
-    const int zt = ZW * tz;                 // first z of the thread within the tile
-    const int z = z0 + zt, y = y0 + ty;
+    const int z0 = blockIdx.x * 32, y0 = blockIdx.y * TMA_TY;
+    const int z = z0 + tz, y = y0 + ty;
     const int x0 = blockIdx.z * XC;
     const int x1 = min(x0 + XC, ti.ne[0]);
     const int nplanes = x1 - x0;
-    const bool rowok = y < ti.ne[1];
-    const int nzv = min(ZW, ti.ne[2] - z);  // valid nodes of this thread
-    const bool valid = rowok && nzv > 0;
+    const bool valid = (y < ti.ne[1]) && (z < ti.ne[2]);
     const int numTS = *g.d_ts + ts_off;
     const long long C = g.comp;
-    const int zl = min(z0 + TZ - 1, g.Nz - 1), yl = min(y0 + TMA_TY - 1, g.Ny - 1);
+    const int zl = min(z0 + 31, g.Nz - 1), yl = min(y0 + TMA_TY - 1, g.Ny - 1);
 
     if (tid == 0) {
         for (int s = 0; s < STAGES; ++s) mbar_init(&bars[s], 1);
@@ -352,7 +166,7 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_volt_tma(const DevGrid g, const
         mbar_expect_tx(&bars[s], bytes);
         tma_4d(st, &m.I_halo, &bars[s], z0 - 4, y0 - 1, x, 0);
         tma_4d(st + L::HALO_A, &m.V_own, &bars[s], z0, y0, x, 0);
-        tma_3d(st + L::HALO_A + L::OWN, &m.idx, &bars[s], z0, y0, x);
+        tma_3d(st + L::HALO_A + L::OWN, &m.idxE, &bars[s], z0, y0, x);
         if (up) tma_4d(st + L::HALO_A + L::OWN + L::IDX_A, &m.FV_own, &bars[s], z0, y0, x, 0);
     };
 
@@ -360,12 +174,21 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_volt_tma(const DevGrid g, const
     if (tid == 0) {
         for (; issued < min(STAGES - 1, nplanes); ++issued) issue(issued);
     }
-    VF p1 = VF(), p2 = VF();  // I1, I2 at x-1
+    float p1 = 0.f, p2 = 0.f;  // I1, I2 at x-1
     const long long yz = (long long)y * g.Nzp + z;
     if (valid && x0 > 0) {
         const long long o = (long long)(x0 - 1) * g.sx + yz;
-        p1 = *reinterpret_cast<const VF*>(g.I + C + o);
-        p2 = *reinterpret_cast<const VF*>(g.I + 2 * C + o);
+        p1 = g.I[C + o];
+        p2 = g.I[2 * C + o];
+    }
+    // geometry factors: y / z parts are fixed per thread, x part per plane
+    float gyE = 0.f, gyI = 0.f, gzE = 0.f, gzI = 0.f;
+    if (GEO && valid) {
+        const int S = g.geo_stride;
+        gyE = __ldg(g.geo + g.Nx + y);
+        gyI = __ldg(g.geo + S + g.Nx + y);
+        gzE = __ldg(g.geo + g.Nx + g.Ny + z);
+        gzI = __ldg(g.geo + S + g.Nx + g.Ny + z);
     }
     float* Vp = g.V + (long long)x0 * g.sx + yz;  // node (x0, y, z), advanced by sx per plane
     bool aborted = false;
@@ -380,67 +203,45 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_volt_tma(const DevGrid g, const
         const bool ok = mbar_wait(&bars[s], (uint32_t)((r / STAGES) & 1));
         const int x = x0 + r;
         const float* st = smem + (size_t)s * L::STAGE;
-        VF c1v = VF(), c2v = VF();
+        float c1 = 0.f, c2 = 0.f;
         if (ok && valid) {
-            const int hi = (ty + 1) * HW + 4 + zt;  // own position in the halo box
+            const int hi = (ty + 1) * HW + 4 + tz;  // own position in the halo box
             const float* sI0 = st;
             const float* sI1 = st + (TMA_TY + 1) * HW;
             const float* sI2 = st + 2 * (TMA_TY + 1) * HW;
-            const VF c0v = *reinterpret_cast<const VF*>(sI0 + hi);
-            c1v = *reinterpret_cast<const VF*>(sI1 + hi);
-            c2v = *reinterpret_cast<const VF*>(sI2 + hi);
-            const VF i2ymv = *reinterpret_cast<const VF*>(sI2 + hi - HW);
-            const VF i0ymv = *reinterpret_cast<const VF*>(sI0 + hi - HW);
-            const float i1zm0 = sI1[hi - 1];
-            const float i0zm0 = sI0[hi - 1];
-            const int oi = ty * TZ + zt;
+            const float c0 = sI0[hi];
+            c1 = sI1[hi];
+            c2 = sI2[hi];
+            const float i2ym = (y > 0) ? sI2[hi - HW] : c2;
+            const float i0ym = (y > 0) ? sI0[hi - HW] : c0;
+            const float i1zm = (z > 0) ? sI1[hi - 1] : c1;
+            const float i0zm = (z > 0) ? sI0[hi - 1] : c0;
+            const float i2xm = (x > 0) ? p2 : c2;
+            const float i1xm = (x > 0) ? p1 : c1;
+            float curl[3];
+            curl[0] = __fadd_rn(__fsub_rn(__fsub_rn(c2, i2ym), c1), i1zm);
+            curl[1] = __fadd_rn(__fsub_rn(__fsub_rn(c0, i0zm), c2), i2xm);
+            curl[2] = __fadd_rn(__fsub_rn(__fsub_rn(c1, i1xm), c0), i0ym);
+            const int oi = ty * 32 + tz;
             const float* sV = st + L::HALO_A;
-            const IdxT* sIdx = reinterpret_cast<const IdxT*>(st + L::HALO_A + L::OWN);
+            const uint32_t t = (uint32_t)reinterpret_cast<const IdxT*>(st + L::HALO_A + L::OWN)[oi];
             const bool up = UPML && tile_has_upml(ti, x, y0, yl, z0, zl);
-            const float* sF = up ? st + L::HALO_A + L::OWN + L::IDX_A : nullptr;
-            const VF v0v = *reinterpret_cast<const VF*>(sV + oi);
-            const VF v1v = *reinterpret_cast<const VF*>(sV + TMA_TY * TZ + oi);
-            const VF v2v = *reinterpret_cast<const VF*>(sV + 2 * TMA_TY * TZ + oi);
-            float outv[3][ZW];
-#pragma unroll
-            for (int k = 0; k < ZW; ++k) {
-                const float c0 = V::get(c0v, k), c1 = V::get(c1v, k), c2 = V::get(c2v, k);
-                const float i2ym = (y > 0) ? V::get(i2ymv, k) : c2;
-                const float i0ym = (y > 0) ? V::get(i0ymv, k) : c0;
-                const float i1zm = (k > 0) ? V::get(c1v, k - 1) : ((z > 0) ? i1zm0 : c1);
-                const float i0zm = (k > 0) ? V::get(c0v, k - 1) : ((z > 0) ? i0zm0 : c0);
-                const float i2xm = (x > 0) ? V::get(p2, k) : c2;
-                const float i1xm = (x > 0) ? V::get(p1, k) : c1;
-                float curl[3];
-                curl[0] = __fadd_rn(__fsub_rn(__fsub_rn(c2, i2ym), c1), i1zm);
-                curl[1] = __fadd_rn(__fsub_rn(__fsub_rn(c0, i0zm), c2), i2xm);
-                curl[2] = __fadd_rn(__fsub_rn(__fsub_rn(c1, i1xm), c0), i0ym);
-                float v[3] = {V::get(v0v, k), V::get(v1v, k), V::get(v2v, k)};
-                if (k < nzv) {
-                    const uint32_t t = (uint32_t)sIdx[oi + k];
-                    const long long o = (long long)x * g.sx + yz + k;
-                    volt_node<FEAT>(g, v, curl, t, o, numTS, sF ? sF + oi + k : nullptr, TMA_TY * TZ);
-                }
-                outv[0][k] = v[0];
-                outv[1][k] = v[1];
-                outv[2][k] = v[2];
+            const float* sF = up ? st + L::HALO_A + L::OWN + L::IDX_A + oi : nullptr;
+            float v[3] = {sV[oi], sV[TMA_TY * 32 + oi], sV[2 * TMA_TY * 32 + oi]};
+            GeoF gf;
+            if (GEO) {
+                const float gxE = __ldg(g.geo + x), gxI = __ldg(g.geo + g.geo_stride + x);
+                gf.f[0][0] = gxE; gf.f[0][1] = gyI; gf.f[0][2] = gzI;
+                gf.f[1][0] = gyE; gf.f[1][1] = gzI; gf.f[1][2] = gxI;
+                gf.f[2][0] = gzE; gf.f[2][1] = gxI; gf.f[2][2] = gyI;
             }
-            if (nzv == ZW) {
-#pragma unroll
-                for (int n = 0; n < 3; ++n) {
-                    VF w;
-                    if constexpr (ZW == 2) w = make_float2(outv[n][0], outv[n][1]);
-                    else w = outv[n][0];
-                    *reinterpret_cast<VF*>(Vp + n * C) = w;
-                }
-            } else {
-                for (int k = 0; k < nzv; ++k)
-#pragma unroll
-                    for (int n = 0; n < 3; ++n) Vp[n * C + k] = outv[n][k];
-            }
+            update_node<false, FEAT, GEO>(g, v, curl, t, (long long)x * g.sx + yz, numTS, sF, TMA_TY * 32, gf);
+            Vp[0] = v[0];
+            Vp[C] = v[1];
+            Vp[2 * C] = v[2];
         }
-        p1 = c1v;
-        p2 = c2v;
+        p1 = c1;
+        p2 = c2;
         if (__syncthreads_or(!ok)) {
             aborted = true;
             break;
@@ -454,31 +255,27 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_volt_tma(const DevGrid g, const
 }
 
 // ------------------------------------------------------------- H half-step
-template <typename IdxT, int FEAT, bool ENERGY, int ZW>
+template <typename IdxT, int FEAT, bool GEO, bool ENERGY>
 __global__ void __launch_bounds__(TMA_TY * 32) k_curr_tma(const DevGrid g, const __grid_constant__ TmaMaps m,
                                                           const TileInfo ti, int ts_off, int XC, int STAGES) {
     constexpr bool UPML = (FEAT & FEAT_UPML) != 0;
-    using L = StageLayout<IdxT, UPML, ZW>;
-    using V = VecT<ZW>;
-    typedef typename V::F VF;
-    constexpr int TZ = L::TZ, HW = L::HW;
+    using L = StageLayout<IdxT, UPML>;
+    constexpr int HW = L::HW;
     extern __shared__ __align__(128) float smem_raw[];
     float* smem = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * STAGES);
     const int tz = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * 32 + tz;
-    const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TMA_TY;
-    const int zt = ZW * tz;
-    const int z = z0 + zt, y = y0 + ty;
+    const int z0 = blockIdx.x * 32, y0 = blockIdx.y * TMA_TY;
+    const int z = z0 + tz, y = y0 + ty;
     const int x0 = blockIdx.z * XC;
     const int x1 = min(x0 + XC, g.Nx - 1);
     const int nplanes = x1 - x0;      // planes updated
     const int nload = nplanes + 1;    // plane x1 is read as the x+1 neighbour
-    const int nzv = min(ZW, g.Nz - 1 - z);
-    const bool active = (y < g.Ny - 1) && nzv > 0;
+    const bool active = (z < g.Nz - 1) && (y < g.Ny - 1);
     const int numTS = *g.d_ts + ts_off;
     const long long C = g.comp;
-    const int zl = min(z0 + TZ - 1, g.Nz - 1), yl = min(y0 + TMA_TY - 1, g.Ny - 1);
+    const int zl = min(z0 + 31, g.Nz - 1), yl = min(y0 + TMA_TY - 1, g.Ny - 1);
 
     if (tid == 0) {
         for (int s = 0; s < STAGES; ++s) mbar_init(&bars[s], 1);
@@ -498,7 +295,7 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_curr_tma(const DevGrid g, const
         tma_4d(st, &m.V_halo, &bars[s], z0, y0, x, 0);
         if (upd) {
             tma_4d(st + L::HALO_A, &m.I_own, &bars[s], z0, y0, x, 0);
-            tma_3d(st + L::HALO_A + L::OWN, &m.idx, &bars[s], z0, y0, x);
+            tma_3d(st + L::HALO_A + L::OWN, &m.idxH, &bars[s], z0, y0, x);
         }
         if (up) tma_4d(st + L::HALO_A + L::OWN + L::IDX_A, &m.FI_own, &bars[s], z0, y0, x, 0);
     };
@@ -509,6 +306,14 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_curr_tma(const DevGrid g, const
     }
     float es = 0.f, ec = 0.f, hs = 0.f, hc = 0.f;  // Kahan sums of V^2 and I^2
     const long long yz = (long long)y * g.Nzp + z;
+    float gyE = 0.f, gyI = 0.f, gzE = 0.f, gzI = 0.f;  // dH / iM parts
+    if (GEO && active) {
+        const int S = g.geo_stride;
+        gyE = __ldg(g.geo + 2 * S + g.Nx + y);
+        gyI = __ldg(g.geo + 3 * S + g.Nx + y);
+        gzE = __ldg(g.geo + 2 * S + g.Nx + g.Ny + z);
+        gzI = __ldg(g.geo + 3 * S + g.Nx + g.Ny + z);
+    }
     float* Ip = g.I + (long long)x0 * g.sx + yz;
     bool aborted = false;
     int r = 0;
@@ -529,64 +334,39 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_curr_tma(const DevGrid g, const
             const float* sV0 = st;
             const float* sV1 = st + (TMA_TY + 1) * HW;
             const float* sV2 = st + 2 * (TMA_TY + 1) * HW;
-            const int hi = ty * HW + zt;
-            const VF c0v = *reinterpret_cast<const VF*>(sV0 + hi);
-            const VF c1v = *reinterpret_cast<const VF*>(sV1 + hi);
-            const VF c2v = *reinterpret_cast<const VF*>(sV2 + hi);
-            const VF v2ypv = *reinterpret_cast<const VF*>(sV2 + hi + HW);
-            const VF v0ypv = *reinterpret_cast<const VF*>(sV0 + hi + HW);
-            const float v1zpL = sV1[hi + ZW];
-            const float v0zpL = sV0[hi + ZW];
-            const VF n1v = *reinterpret_cast<const VF*>(stn + (TMA_TY + 1) * HW + hi);
-            const VF n2v = *reinterpret_cast<const VF*>(stn + 2 * (TMA_TY + 1) * HW + hi);
+            const int hi = ty * HW + tz;
+            const float c0 = sV0[hi], c1 = sV1[hi], c2 = sV2[hi];
+            const float n1 = stn[(TMA_TY + 1) * HW + hi];
+            const float n2 = stn[2 * (TMA_TY + 1) * HW + hi];
+            float curl[3];
+            curl[0] = __fadd_rn(__fsub_rn(__fsub_rn(c2, sV2[hi + HW]), c1), sV1[hi + 1]);
+            curl[1] = __fadd_rn(__fsub_rn(__fsub_rn(c0, sV0[hi + 1]), c2), n2);
+            curl[2] = __fadd_rn(__fsub_rn(__fsub_rn(c1, n1), c0), sV0[hi + HW]);
+            const int oi = ty * 32 + tz;
             const float* sI = st + L::HALO_A;
-            const IdxT* sIdx = reinterpret_cast<const IdxT*>(st + L::HALO_A + L::OWN);
+            const uint32_t t = (uint32_t)reinterpret_cast<const IdxT*>(st + L::HALO_A + L::OWN)[oi];
             const bool up = UPML && tile_has_upml(ti, x, y0, yl, z0, zl);
-            const float* sF = up ? st + L::HALO_A + L::OWN + L::IDX_A : nullptr;
-            const int oi = ty * TZ + zt;
-            const VF i0v = *reinterpret_cast<const VF*>(sI + oi);
-            const VF i1v = *reinterpret_cast<const VF*>(sI + TMA_TY * TZ + oi);
-            const VF i2v = *reinterpret_cast<const VF*>(sI + 2 * TMA_TY * TZ + oi);
-            float outc[3][ZW];
-#pragma unroll
-            for (int k = 0; k < ZW; ++k) {
-                const float c0 = V::get(c0v, k), c1 = V::get(c1v, k), c2 = V::get(c2v, k);
-                const float v1zp = (k + 1 < ZW) ? V::get(c1v, k + 1) : v1zpL;
-                const float v0zp = (k + 1 < ZW) ? V::get(c0v, k + 1) : v0zpL;
-                float curl[3];
-                curl[0] = __fadd_rn(__fsub_rn(__fsub_rn(c2, V::get(v2ypv, k)), c1), v1zp);
-                curl[1] = __fadd_rn(__fsub_rn(__fsub_rn(c0, v0zp), c2), V::get(n2v, k));
-                curl[2] = __fadd_rn(__fsub_rn(__fsub_rn(c1, V::get(n1v, k)), c0), V::get(v0ypv, k));
-                float cu[3] = {V::get(i0v, k), V::get(i1v, k), V::get(i2v, k)};
-                if (k < nzv) {
-                    const uint32_t t = (uint32_t)sIdx[oi + k];
-                    const long long o = (long long)x * g.sx + yz + k;
-                    curr_node<FEAT>(g, cu, curl, t, o, numTS, sF ? sF + oi + k : nullptr, TMA_TY * TZ);
-                    if (ENERGY) {
-                        kahan_add(es, ec, __fmul_rn(c0, c0));
-                        kahan_add(es, ec, __fmul_rn(c1, c1));
-                        kahan_add(es, ec, __fmul_rn(c2, c2));
-                        kahan_add(hs, hc, __fmul_rn(cu[0], cu[0]));
-                        kahan_add(hs, hc, __fmul_rn(cu[1], cu[1]));
-                        kahan_add(hs, hc, __fmul_rn(cu[2], cu[2]));
-                    }
-                }
-                outc[0][k] = cu[0];
-                outc[1][k] = cu[1];
-                outc[2][k] = cu[2];
+            const float* sF = up ? st + L::HALO_A + L::OWN + L::IDX_A + oi : nullptr;
+            float cu[3] = {sI[oi], sI[TMA_TY * 32 + oi], sI[2 * TMA_TY * 32 + oi]};
+            GeoF gf;
+            if (GEO) {
+                const int S = g.geo_stride;
+                const float gxE = __ldg(g.geo + 2 * S + x), gxI = __ldg(g.geo + 3 * S + x);
+                gf.f[0][0] = gxE; gf.f[0][1] = gyI; gf.f[0][2] = gzI;
+                gf.f[1][0] = gyE; gf.f[1][1] = gzI; gf.f[1][2] = gxI;
+                gf.f[2][0] = gzE; gf.f[2][1] = gxI; gf.f[2][2] = gyI;
             }
-            if (nzv == ZW) {
-#pragma unroll
-                for (int n = 0; n < 3; ++n) {
-                    VF w;
-                    if constexpr (ZW == 2) w = make_float2(outc[n][0], outc[n][1]);
-                    else w = outc[n][0];
-                    *reinterpret_cast<VF*>(Ip + n * C) = w;
-                }
-            } else {
-                for (int k = 0; k < nzv; ++k)
-#pragma unroll
-                    for (int n = 0; n < 3; ++n) Ip[n * C + k] = outc[n][k];
+            update_node<true, FEAT, GEO>(g, cu, curl, t, (long long)x * g.sx + yz, numTS, sF, TMA_TY * 32, gf);
+            Ip[0] = cu[0];
+            Ip[C] = cu[1];
+            Ip[2 * C] = cu[2];
+            if (ENERGY) {
+                kahan_add(es, ec, __fmul_rn(c0, c0));
+                kahan_add(es, ec, __fmul_rn(c1, c1));
+                kahan_add(es, ec, __fmul_rn(c2, c2));
+                kahan_add(hs, hc, __fmul_rn(cu[0], cu[0]));
+                kahan_add(hs, hc, __fmul_rn(cu[1], cu[1]));
+                kahan_add(hs, hc, __fmul_rn(cu[2], cu[2]));
             }
         }
         if (__syncthreads_or(!ok)) {
@@ -599,7 +379,7 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_curr_tma(const DevGrid g, const
         for (int q = r; q < issued; ++q) mbar_wait(&bars[q % STAGES], (uint32_t)((q / STAGES) & 1));
     }
     if (ENERGY) {
-        double esum = (double)es + (double)(-ec), hsum = (double)hs + (double)(-hc);
+        double esum = (double)es - (double)ec, hsum = (double)hs - (double)hc;
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) {
             esum += __shfl_down_sync(0xffffffffu, esum, off);

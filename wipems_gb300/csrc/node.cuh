@@ -1,0 +1,199 @@
+// Per-node fused update of one half-step, shared by the direct and the
+// TMA-pipelined kernels.
+//
+// Per-cell math restated from the reference (citations relative to it):
+//   voltage update   FDTD/engine.cpp:108-161 (SSE twin engine_sse_compressed.cpp:48-156)
+//   current update   FDTD/engine.cpp:163-210 (SSE twin engine_sse_compressed.cpp:158-263)
+//   UPML flux swap   extensions/engine_ext_upml.cpp:57-239, fused as
+//                      f  = vvp*V - vvfo*F                     (pre)
+//                      Fn = F*vv + vi*curl                     (main, V<-F)
+//                      V  = f + vvfn*Fn ; F = Fn               (post)
+//   Lorentz/Drude    extensions/engine_ext_lorentzmaterial.cpp:79-173 (pre, old V)
+//                    extensions/engine_ext_dispersive.cpp:76-132 (V -= ADE after)
+//   excitation       extensions/engine_ext_excitation.cpp:33-99 (added last)
+// Hook order per half-step follows Engine::IterateTS (engine.cpp:255-274)
+// with the priorities of engine_extension.h:21-29: ADE-pre, UPML-pre, main,
+// UPML-post, ADE-apply, excitation.  Every product and sum is rounded in the
+// reference's order (__fmul_rn/__fadd_rn, no FMA contraction), so the device
+// result is bit-identical to the FP32 CPU engine (up to the geometry factor
+// product on graded meshes, see cop.h).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "cop.h"
+
+namespace wipems {
+
+// kernel feature bits (compile time)
+constexpr int FEAT_UPML = 1;
+constexpr int FEAT_ADE = 2;
+
+// device view of one half-step's tables (float4 units, layout TAB_* in cop.h)
+struct DevHalf {
+    const void* idx;     // [Nx][Ny][Nzp] tuple index (uint16 or uint32)
+    const float4* main;
+    const float4* upml;
+    const float4* ade;
+    const float4* exc;
+};
+
+struct DevGrid {
+    int Nx, Ny, Nz;      // mesh lines
+    int Nzp;             // padded z stride (multiple of 32)
+    long long sx;        // x stride (Ny*Nzp)
+    long long comp;      // component stride (Nx*Ny*Nzp)
+    float* V;            // [3][comp]
+    float* I;            // [3][comp]
+    float* FV;           // UPML voltage flux [3][comp] or null
+    float* FI;           // UPML current flux
+    float* AV;           // ADE voltage state (order 1) [3][comp]
+    float* LV;           // Lorentz voltage state
+    float* AI;           // ADE current state
+    float* LI;
+    DevHalf e, h;
+    const float* geo;    // [4][Nx+Ny+Nz] dE, iD, dH, iM (factorized meshes) or null
+    int geo_stride;      // Nx+Ny+Nz
+    const float* sigV;   // excitation signals
+    const float* sigC;
+    int sig_len;
+    int sig_period;      // 0 = none
+    const int* d_ts;     // timestep counter (numTS)
+    double* d_eacc;      // energy accumulators {sum V^2, sum I^2}
+};
+
+template <typename IdxT>
+__device__ __forceinline__ uint32_t load_idx(const void* p, long long o) {
+    return (uint32_t)__ldg(reinterpret_cast<const IdxT*>(p) + o);
+}
+
+__device__ __forceinline__ int exc_index(int numTS, int delay, int length, int period) {
+    // engine_ext_excitation.cpp:44-53
+    int exc_pos = numTS - delay;
+    exc_pos *= (exc_pos > 0);
+    const int p = period > 0 ? period : numTS + 1;
+    exc_pos %= p;
+    exc_pos *= (exc_pos < length);
+    return exc_pos;
+}
+
+// geometry factors of one node for the three components (factorized meshes):
+// E: gE(n) = dE[n][p_n] * iD[nP][p_nP] * iD[nPP][p_nPP]; H with dH / iM.
+struct GeoF {
+    float f[3][3];
+};
+
+__device__ __forceinline__ GeoF geo_factors(const DevGrid& g, bool H, int x, int y, int z) {
+    const int S = g.geo_stride;
+    const float* a = g.geo + (H ? 2 : 0) * S;  // dE | dH
+    const float* b = g.geo + (H ? 3 : 1) * S;  // iD | iM
+    const int p[3] = {x, g.Nx + y, g.Nx + g.Ny + z};
+    GeoF r;
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+        r.f[n][0] = __ldg(a + p[n]);
+        r.f[n][1] = __ldg(b + p[(n + 1) % 3]);
+        r.f[n][2] = __ldg(b + p[(n + 2) % 3]);
+    }
+    return r;
+}
+
+// One node of one half-step.  fld[3]: the old field (V or I); curl[3]: the
+// curl of the other field; t: tuple index; o: node offset; F (UPML flux of
+// the node) is read from fsrc[n*fstride] when fsrc is set, else from global.
+template <bool H, int FEAT, bool GEO>
+__device__ __forceinline__ void update_node(const DevGrid& g, float fld[3], const float curl[3], uint32_t t,
+                                            long long o, int numTS, const float* fsrc, int fstride,
+                                            const GeoF& gf) {
+    const DevHalf& T = H ? g.h : g.e;
+    const float4 ta = __ldg(&T.main[TAB_MAIN * t]);
+    const float4 tb = __ldg(&T.main[TAB_MAIN * t + 1]);
+    const float c1[3] = {ta.x, ta.y, ta.z};
+    float c2[3] = {ta.w, tb.x, tb.y};
+    if (GEO) {
+#pragma unroll
+        for (int n = 0; n < 3; ++n) c2[n] = __fmul_rn(__fmul_rn(__fmul_rn(c2[n], gf.f[n][0]), gf.f[n][1]), gf.f[n][2]);
+    }
+    const uint32_t flags = __float_as_uint(tb.z);
+    const long long C = g.comp;
+    float* A = H ? g.AI : g.AV;
+    float* Lr = H ? g.LI : g.LV;
+    float* Fl = H ? g.FI : g.FV;
+    float ade[3] = {0.f, 0.f, 0.f};
+    if ((FEAT & FEAT_ADE) && (flags & TF_ADE)) {
+        const float4 a0 = __ldg(&T.ade[TAB_ADE * t]);
+        const float4 a1 = __ldg(&T.ade[TAB_ADE * t + 1]);
+        const float4 a2 = __ldg(&T.ade[TAB_ADE * t + 2]);
+        const float kint[3] = {a0.x, a0.y, a0.z};
+        const float kext[3] = {a0.w, a1.x, a1.y};
+        const float klor[3] = {a1.z, a1.w, a2.x};
+        if (flags & TF_LOR) {
+#pragma unroll
+            for (int n = 0; n < 3; ++n) {
+                float lor = Lr[n * C + o];
+                float a = A[n * C + o];
+                lor = __fadd_rn(lor, __fmul_rn(klor[n], a));
+                a = __fmul_rn(a, kint[n]);
+                a = __fadd_rn(a, __fmul_rn(kext[n], __fsub_rn(fld[n], lor)));
+                Lr[n * C + o] = lor;
+                A[n * C + o] = a;
+                ade[n] = a;
+            }
+        } else {
+#pragma unroll
+            for (int n = 0; n < 3; ++n) {
+                float a = A[n * C + o];
+                a = __fmul_rn(a, kint[n]);
+                a = __fadd_rn(a, __fmul_rn(kext[n], fld[n]));
+                A[n * C + o] = a;
+                ade[n] = a;
+            }
+        }
+    }
+    if ((FEAT & FEAT_UPML) && (flags & TF_UPML)) {
+        const float4 u0 = __ldg(&T.upml[TAB_UPML * t]);
+        const float4 u1 = __ldg(&T.upml[TAB_UPML * t + 1]);
+        const float4 u2 = __ldg(&T.upml[TAB_UPML * t + 2]);
+        const float kp[3] = {u0.x, u0.y, u0.z};
+        const float kfo[3] = {u0.w, u1.x, u1.y};
+        const float kfn[3] = {u1.z, u1.w, u2.x};
+#pragma unroll
+        for (int n = 0; n < 3; ++n) {
+            const float F = fsrc ? fsrc[n * fstride] : Fl[n * C + o];
+            const float f = __fsub_rn(__fmul_rn(kp[n], fld[n]), __fmul_rn(kfo[n], F));
+            const float Fn = __fadd_rn(__fmul_rn(F, c1[n]), __fmul_rn(c2[n], curl[n]));
+            Fl[n * C + o] = Fn;
+            fld[n] = __fadd_rn(f, __fmul_rn(kfn[n], Fn));
+        }
+    } else {
+#pragma unroll
+        for (int n = 0; n < 3; ++n) fld[n] = __fadd_rn(__fmul_rn(fld[n], c1[n]), __fmul_rn(c2[n], curl[n]));
+    }
+    if ((FEAT & FEAT_ADE) && (flags & TF_ADE)) {
+#pragma unroll
+        for (int n = 0; n < 3; ++n) fld[n] = __fsub_rn(fld[n], ade[n]);
+    }
+    if (flags & TF_EXC) {
+        const float4 e0 = __ldg(&T.exc[TAB_EXC * t]);
+        const float4 e1 = __ldg(&T.exc[TAB_EXC * t + 1]);
+        const float amp[3] = {e0.x, e0.y, e0.z};
+        const int dly[3] = {__float_as_int(e1.x), __float_as_int(e1.y), __float_as_int(e1.z)};
+        const float* sig = H ? g.sigC : g.sigV;
+#pragma unroll
+        for (int n = 0; n < 3; ++n)
+            if (dly[n] >= 0) {
+                const int k = exc_index(numTS, dly[n], g.sig_len, g.sig_period);
+                fld[n] = __fadd_rn(fld[n], __fmul_rn(amp[n], sig[k]));
+            }
+    }
+}
+
+__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
+    const float y = __fsub_rn(x, c);
+    const float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+}
+
+}  // namespace wipems

@@ -1394,6 +1394,8 @@ int fdtd_operator_describe(fdtd_operator_t op, fdtd_op_desc* d) {
     d->signal_volt = op->sig_volt.data();
     d->signal_curr = op->sig_curr.data();
     d->signal_period_ts = 0;
+    for (int n = 0; n < 3; ++n) d->lines[n] = op->lines[n].data();
+    d->unit = op->unit;
     return FDTD_OK;
 }
 

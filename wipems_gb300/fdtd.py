@@ -218,14 +218,18 @@ class CompressedOperator:
     uint16/uint32 tuple index + coefficient tables in (pinned) host memory.
     Runs without a GPU."""
 
-    def __init__(self, op: Operator):
+    MODES = {"auto": 0, "exact": 1, "factorized": 2}
+
+    def __init__(self, op: Operator, mode: str = "auto"):
         h = C.c_void_p()
-        check(lib().fdtd_compress(C.byref(op.desc), C.byref(h)), "fdtd_compress")
+        check(lib().fdtd_compress_ex(C.byref(op.desc), self.MODES[mode], C.byref(h)), "fdtd_compress")
         self._h = h
         self.op = op
         info = _abi.FdtdCopInfo()
         check(lib().fdtd_cop_get_info(h, C.byref(info)), "fdtd_cop_get_info")
-        self.info = {k: (list(getattr(info, k)) if k == "num_lines" else getattr(info, k)) for k, _ in info._fields_}
+        self.info = {k: (list(getattr(info, k)) if k in ("num_lines", "trim_e") else getattr(info, k))
+                     for k, _ in info._fields_}
+        self.factorized = bool(self.info["geometry_factored"])
 
     def __del__(self):
         if getattr(self, "_h", None):
@@ -253,7 +257,7 @@ class Engine:
 
     def __init__(self, op, device: int = 0, max_timesteps: int = 0, probe_interval: int | None = None,
                  use_graphs: bool = True, energy_on_probe: bool = True, tile_y: int = 0, x_chunk: int = 0,
-                 probes: bool = True, kernel: str = "tma", stages: int = 0, z_per_thread: int = 0):
+                 probes: bool = True, kernel: str = "tma", stages: int = 0):
         cop = op if isinstance(op, CompressedOperator) else None
         if cop is not None:
             op = cop.op
@@ -270,7 +274,6 @@ class Engine:
             raise ValueError("kernel must be 'tma' or 'direct'")
         o.kernel = 0 if kernel == "tma" else 1
         o.stages = int(stages)
-        o.z_per_thread = int(z_per_thread)
         h = C.c_void_p()
         if cop is not None:
             check(lib().fdtd_engine_create_compressed(cop._h, C.byref(o), C.byref(h)), "fdtd_engine_create_compressed")
