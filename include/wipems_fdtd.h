@@ -359,6 +359,28 @@ int fdtd_engine_profile_kernels(fdtd_engine_t eng, uint32_t n_steps,
  * on the engine stream (ms) and the number of kernel launches it issued. */
 int fdtd_engine_last_timing(fdtd_engine_t eng, double* ms, uint64_t* launches);
 
+/* ---------------------------------------------------- allocation-free path */
+
+/* Energy eps0*sum(V^2) + mu0*sum(I^2) over x < Nx-1, y < Ny-1, z < Nz-1 of
+ * caller-owned device fields -- the quantity fdtd_engine_energy returns --
+ * for callers that must not allocate device memory (a fixed memory budget,
+ * a real-time loop that may not touch the allocator, an embedding
+ * application whose allocator is off limits).  No counterpart in the
+ * reference: it has no device code.
+ *   volt, curr   device arrays [3][Nx][Ny][z_pitch] (z fastest)
+ *   num_lines    {Nx, Ny, Nz};  z_pitch >= Nz
+ *   stream       cudaStream_t to launch on (NULL = default stream)
+ *   energy       device pointer receiving one double
+ * The per-plane partial sums live in a static device array of 4096 planes
+ * (64 KB, held by every GPU that loads the library until exit); Nx-1 above
+ * 4096 is rejected with FDTD_ERR_ARG.  Calls no cudaMalloc / cudaFree.  The
+ * first call on a device looks the array up with cudaGetSymbolAddress, so
+ * make that first call before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU race. */
+int fdtd_field_energy_static(const float* volt, const float* curr,
+                             const uint32_t num_lines[3], uint32_t z_pitch,
+                             void* stream, double* energy);
+
 #ifdef __cplusplus
 }
 #endif

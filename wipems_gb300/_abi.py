@@ -127,6 +127,7 @@ SIGNATURES = [
     ("fdtd_engine_get_stats", C.c_int, [_P, C.POINTER(FdtdEngineStats)]),
     ("fdtd_engine_last_timing", C.c_int, [_P, PD, C.POINTER(C.c_uint64)]),
     ("fdtd_engine_profile_kernels", C.c_int, [_P, u32, PD, PD]),
+    ("fdtd_field_energy_static", C.c_int, [_P, _P, PU32, u32, _P, _P]),
 ]
 
 
