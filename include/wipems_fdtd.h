@@ -359,6 +359,42 @@ int fdtd_engine_profile_kernels(fdtd_engine_t eng, uint32_t n_steps,
  * on the engine stream (ms) and the number of kernel launches it issued. */
 int fdtd_engine_last_timing(fdtd_engine_t eng, double* ms, uint64_t* launches);
 
+/* ----------------------------------------------------------------- batches */
+
+/* Batched mode (no counterpart in the reference, which runs one simulation
+ * per process): the jobs -- engines created as above, on one device, with
+ * the TMA kernels -- advance together with one persistent kernel per
+ * half-step and kernel variant over a flattened (job, tile) work list, each
+ * job sampling its probes / energy at its own interval, the step sequence
+ * replayed from a CUDA graph.  The engines stay owned by the caller and must
+ * outlive the batch; per-job calls (read_samples, get_fields, reset) work
+ * between batch iterations. */
+typedef struct fdtd_batch_s* fdtd_batch_t;
+
+typedef struct {
+    int x_chunk;        /* x planes per work item (0 = 8) */
+    int stages;         /* TMA ring depth 3..8 (0 = 3) */
+    int blocks_per_sm;  /* cap on resident blocks per SM (0 = occupancy) */
+    int graph_steps;    /* timesteps per captured graph (0 = 8, 1 = none) */
+} fdtd_batch_opts;
+
+typedef struct {
+    uint32_t num_jobs, num_groups;
+    uint64_t total_nodes;
+    uint64_t work_items;
+    uint32_t persistent_blocks;
+    uint64_t device_bytes;
+    double   last_ms;
+    uint64_t last_launches;
+} fdtd_batch_stats;
+
+int fdtd_batch_create(const fdtd_engine_t* engines, uint32_t n,
+                      const fdtd_batch_opts* opts, fdtd_batch_t* out);
+/* Advances every job by n_steps (each job's numTS moves by n_steps). */
+int fdtd_batch_iterate(fdtd_batch_t batch, uint32_t n_steps);
+int fdtd_batch_info(fdtd_batch_t batch, fdtd_batch_stats* stats);
+int fdtd_batch_destroy(fdtd_batch_t batch);
+
 /* ---------------------------------------------------- allocation-free path */
 
 /* Energy eps0*sum(V^2) + mu0*sum(I^2) over x < Nx-1, y < Ny-1, z < Nz-1 of

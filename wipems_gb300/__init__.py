@@ -5,8 +5,8 @@ on-device probes runs in hand-written sm_103a CUDA kernels
 (csrc/kernels.cuh), behind the C ABI of include/wipems_fdtd.h.  The host
 operator build (csrc/operator.cpp) restates openEMS's Operator.
 """
-from .fdtd import (BC_PEC, BC_PMC, BC_PML, C0, EPS0, MUE0, CompressedOperator, Engine, Operator, Samples, Scene,
-                   run_fdtd)
+from .fdtd import (BC_PEC, BC_PMC, BC_PML, C0, EPS0, MUE0, Batch, CompressedOperator, Engine, Operator, Samples,
+                   Scene, run_fdtd)
 
-__all__ = ["Scene", "Operator", "CompressedOperator", "Engine", "Samples", "run_fdtd", "BC_PEC", "BC_PMC", "BC_PML", "EPS0", "MUE0",
+__all__ = ["Scene", "Operator", "CompressedOperator", "Batch", "Engine", "Samples", "run_fdtd", "BC_PEC", "BC_PMC", "BC_PML", "EPS0", "MUE0",
            "C0"]

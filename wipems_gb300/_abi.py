@@ -75,6 +75,16 @@ class FdtdCopInfo(C.Structure):
                 ("pinned", C.c_int)]
 
 
+class FdtdBatchOpts(C.Structure):
+    _fields_ = [("x_chunk", C.c_int), ("stages", C.c_int), ("blocks_per_sm", C.c_int), ("graph_steps", C.c_int)]
+
+
+class FdtdBatchStats(C.Structure):
+    _fields_ = [("num_jobs", u32), ("num_groups", u32), ("total_nodes", C.c_uint64), ("work_items", C.c_uint64),
+                ("persistent_blocks", u32), ("device_bytes", C.c_uint64), ("last_ms", C.c_double),
+                ("last_launches", C.c_uint64)]
+
+
 class FdtdError(RuntimeError):
     def __init__(self, code: int, where: str, msg: str):
         super().__init__(f"{where} failed ({code}): {msg}")
@@ -128,6 +138,10 @@ SIGNATURES = [
     ("fdtd_engine_last_timing", C.c_int, [_P, PD, C.POINTER(C.c_uint64)]),
     ("fdtd_engine_profile_kernels", C.c_int, [_P, u32, PD, PD]),
     ("fdtd_field_energy_static", C.c_int, [_P, _P, PU32, u32, _P, _P]),
+    ("fdtd_batch_create", C.c_int, [C.POINTER(_P), u32, C.POINTER(FdtdBatchOpts), C.POINTER(_P)]),
+    ("fdtd_batch_iterate", C.c_int, [_P, u32]),
+    ("fdtd_batch_info", C.c_int, [_P, C.POINTER(FdtdBatchStats)]),
+    ("fdtd_batch_destroy", C.c_int, [_P]),
 ]
 
 

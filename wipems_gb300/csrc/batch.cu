@@ -1,0 +1,432 @@
+// Batched mode: many independent simulations of uneven grid sizes advance
+// together, one persistent kernel per half-step (per kernel variant) over a
+// flattened (job, tile, x-chunk) work list, with every job's probes and
+// energy sampled on the device at its own probe interval.  The timestep
+// sequence [voltage kernels, current kernels, sampler] is captured into a
+// CUDA graph and replayed.
+//
+// A job is an ordinary engine (fdtd_engine_create*): the batch only refers
+// to its device arrays, so per-job calls (read_samples, get_fields, reset)
+// keep working between batch iterations.  Jobs of different kernel variants
+// (uint16 / uint32 tuple index, UPML / ADE features, factorized geometry)
+// form separate groups, each with its own persistent kernels.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "engine_state.h"
+
+namespace wipems {
+namespace {
+
+// per-job state of the batched sampler
+struct AdvJob {
+    int* d_ts;
+    ProbeSet ps;
+    DevGrid g;
+    int interval;
+    int energy_valid;
+};
+
+// Block j advances job j's numTS by one and records a sample row when the
+// new timestep is a multiple of the job's probe interval (the decision is
+// taken on the device, so the step sequence can be replayed as a graph).
+__global__ void k_batch_advance(const AdvJob* __restrict__ jobs, double eps0, double mue0) {
+    const AdvJob& J = jobs[blockIdx.x];
+    __shared__ int s_sample;
+    if (threadIdx.x == 0) {
+        const int ts = *J.d_ts + 1;
+        s_sample = (J.interval > 0 && (ts % J.interval) == 0) ? 1 : 0;
+    }
+    __syncthreads();
+    advance_sample(J.d_ts, 1, s_sample, J.ps, J.g, J.energy_valid, eps0, mue0);
+}
+
+struct Group {
+    bool e16 = true, h16 = true, geo = false;
+    int feat = 0;
+    std::vector<int> jobs;
+    DevBuf<WorkItem> itE, itH;
+    int nE = 0, nH = 0, gridE = 0, gridH = 0;
+    size_t smemE = 0, smemH = 0;
+};
+
+template <typename IdxT, int FEAT, bool GEO>
+void volt_batch_launch(const Group& G, const BatchJob* jobs, int XC, int S, cudaStream_t st) {
+    k_volt_batch<IdxT, FEAT, GEO><<<G.gridE, dim3(32, TMA_TY), G.smemE, st>>>(jobs, G.itE.p, G.nE, XC, S);
+}
+template <typename IdxT, int FEAT, bool GEO>
+void curr_batch_launch(const Group& G, const BatchJob* jobs, int XC, int S, cudaStream_t st) {
+    k_curr_batch<IdxT, FEAT, GEO><<<G.gridH, dim3(32, TMA_TY), G.smemH, st>>>(jobs, G.itH.p, G.nH, XC, S);
+}
+
+template <typename IdxT, bool GEO>
+void volt_feat(const Group& G, const BatchJob* jobs, int XC, int S, cudaStream_t st) {
+    switch (G.feat) {
+        case 0: volt_batch_launch<IdxT, 0, GEO>(G, jobs, XC, S, st); break;
+        case 1: volt_batch_launch<IdxT, 1, GEO>(G, jobs, XC, S, st); break;
+        case 2: volt_batch_launch<IdxT, 2, GEO>(G, jobs, XC, S, st); break;
+        default: volt_batch_launch<IdxT, 3, GEO>(G, jobs, XC, S, st); break;
+    }
+}
+template <typename IdxT, bool GEO>
+void curr_feat(const Group& G, const BatchJob* jobs, int XC, int S, cudaStream_t st) {
+    switch (G.feat) {
+        case 0: curr_batch_launch<IdxT, 0, GEO>(G, jobs, XC, S, st); break;
+        case 1: curr_batch_launch<IdxT, 1, GEO>(G, jobs, XC, S, st); break;
+        case 2: curr_batch_launch<IdxT, 2, GEO>(G, jobs, XC, S, st); break;
+        default: curr_batch_launch<IdxT, 3, GEO>(G, jobs, XC, S, st); break;
+    }
+}
+
+void launch_group_volt(const Group& G, const BatchJob* jobs, int XC, int S, cudaStream_t st) {
+    if (G.e16) {
+        if (G.geo) volt_feat<uint16_t, true>(G, jobs, XC, S, st);
+        else volt_feat<uint16_t, false>(G, jobs, XC, S, st);
+    } else {
+        if (G.geo) volt_feat<uint32_t, true>(G, jobs, XC, S, st);
+        else volt_feat<uint32_t, false>(G, jobs, XC, S, st);
+    }
+}
+void launch_group_curr(const Group& G, const BatchJob* jobs, int XC, int S, cudaStream_t st) {
+    if (G.h16) {
+        if (G.geo) curr_feat<uint16_t, true>(G, jobs, XC, S, st);
+        else curr_feat<uint16_t, false>(G, jobs, XC, S, st);
+    } else {
+        if (G.geo) curr_feat<uint32_t, true>(G, jobs, XC, S, st);
+        else curr_feat<uint32_t, false>(G, jobs, XC, S, st);
+    }
+}
+
+// occupancy of one batched kernel variant (blocks per SM)
+template <typename IdxT, int FEAT, bool GEO>
+int occ_one(bool volt, size_t smem) {
+    int n = 0;
+    if (volt)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_volt_batch<IdxT, FEAT, GEO>, 32 * TMA_TY, smem);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_curr_batch<IdxT, FEAT, GEO>, 32 * TMA_TY, smem);
+    return n;
+}
+template <typename IdxT, bool GEO>
+int occ_feat(int feat, bool volt, size_t smem) {
+    switch (feat) {
+        case 0: return occ_one<IdxT, 0, GEO>(volt, smem);
+        case 1: return occ_one<IdxT, 1, GEO>(volt, smem);
+        case 2: return occ_one<IdxT, 2, GEO>(volt, smem);
+        default: return occ_one<IdxT, 3, GEO>(volt, smem);
+    }
+}
+int occupancy(const Group& G, bool volt, size_t smem) {
+    const bool i16 = volt ? G.e16 : G.h16;
+    if (i16) return G.geo ? occ_feat<uint16_t, true>(G.feat, volt, smem) : occ_feat<uint16_t, false>(G.feat, volt, smem);
+    return G.geo ? occ_feat<uint32_t, true>(G.feat, volt, smem) : occ_feat<uint32_t, false>(G.feat, volt, smem);
+}
+
+template <typename IdxT, int FEAT, bool GEO>
+cudaError_t batch_smem_attr_one(int bytes) {
+    const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    cudaError_t r1 = cudaFuncSetAttribute(k_volt_batch<IdxT, FEAT, GEO>, a, bytes);
+    cudaError_t r2 = cudaFuncSetAttribute(k_curr_batch<IdxT, FEAT, GEO>, a, bytes);
+    return r1 != cudaSuccess ? r1 : r2;
+}
+
+int batch_smem_attrs(int bytes) {
+    cudaError_t r = cudaSuccess, t;
+#define WIPEMS_BATTR(I, F)                                                     \
+    if ((t = batch_smem_attr_one<I, F, false>(bytes)) != cudaSuccess) r = t;   \
+    if ((t = batch_smem_attr_one<I, F, true>(bytes)) != cudaSuccess) r = t;
+    WIPEMS_BATTR(uint16_t, 0) WIPEMS_BATTR(uint16_t, 1) WIPEMS_BATTR(uint16_t, 2) WIPEMS_BATTR(uint16_t, 3)
+    WIPEMS_BATTR(uint32_t, 0) WIPEMS_BATTR(uint32_t, 1) WIPEMS_BATTR(uint32_t, 2) WIPEMS_BATTR(uint32_t, 3)
+#undef WIPEMS_BATTR
+    if (r != cudaSuccess) {
+        set_error(std::string("cudaFuncSetAttribute (batch): ") + cudaGetErrorString(r));
+        return FDTD_ERR_CUDA;
+    }
+    return FDTD_OK;
+}
+
+size_t stage_smem(bool i16, bool upml, int S) {
+    if (i16) return upml ? StageLayout<uint16_t, true>::smem(S) : StageLayout<uint16_t, false>::smem(S);
+    return upml ? StageLayout<uint32_t, true>::smem(S) : StageLayout<uint32_t, false>::smem(S);
+}
+
+}  // namespace
+}  // namespace wipems
+
+using namespace wipems;
+
+struct fdtd_batch_s {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<fdtd_engine_s*> jobs;
+    std::vector<Group> groups;
+    DevBuf<BatchJob> d_jobs;
+    DevBuf<TmaMaps> d_maps;
+    DevBuf<AdvJob> d_adv;
+    int XC = 8, stages = 3, blocks_per_sm = 0;
+    uint32_t graph_steps = 8;
+    cudaGraphExec_t graph = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double last_ms = 0;
+    uint64_t last_launches = 0;
+    uint64_t device_bytes = 0;
+    uint64_t total_nodes = 0;
+    ~fdtd_batch_s() {
+        if (graph) cudaGraphExecDestroy(graph);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace wipems {
+namespace {
+
+int batch_step(fdtd_batch_s* b) {
+    for (const Group& G : b->groups) launch_group_volt(G, b->d_jobs.p, b->XC, b->stages, b->stream);
+    for (const Group& G : b->groups) launch_group_curr(G, b->d_jobs.p, b->XC, b->stages, b->stream);
+    k_batch_advance<<<(unsigned)b->jobs.size(), 256, 0, b->stream>>>(b->d_adv.p, kEps0, kMue0);
+    b->last_launches += 2 * b->groups.size() + 1;
+    const cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) {
+        set_error(std::string("batch kernel launch: ") + cudaGetErrorString(err));
+        return FDTD_ERR_CUDA;
+    }
+    return FDTD_OK;
+}
+
+int batch_graph(fdtd_batch_s* b) {
+    if (b->graph) return FDTD_OK;
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = FDTD_OK;
+    const uint64_t saved = b->last_launches;
+    for (uint32_t k = 0; k < b->graph_steps && rc == FDTD_OK; ++k) rc = batch_step(b);
+    b->last_launches = saved;
+    const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (ce != cudaSuccess) {
+        set_error(std::string("cudaStreamEndCapture (batch): ") + cudaGetErrorString(ce));
+        return FDTD_ERR_CUDA;
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+        b->graph = nullptr;
+        set_error(std::string("cudaGraphInstantiate (batch): ") + cudaGetErrorString(ie));
+        return FDTD_ERR_CUDA;
+    }
+    return FDTD_OK;
+}
+
+int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts* o, fdtd_batch_s* b) {
+    if (n == 0) {
+        set_error("fdtd_batch_create: no jobs");
+        return FDTD_ERR_ARG;
+    }
+    b->device = engines[0]->device;
+    b->XC = (o && o->x_chunk > 0) ? o->x_chunk : 8;
+    b->stages = (o && o->stages > 0) ? o->stages : 3;
+    b->blocks_per_sm = (o && o->blocks_per_sm > 0) ? o->blocks_per_sm : 0;
+    b->graph_steps = (o && o->graph_steps > 0) ? (uint32_t)o->graph_steps : 8;
+    if (b->stages < 3 || b->stages > TMA_MAX_STAGES) {
+        set_error("fdtd_batch_create: stages must be 3..8");
+        return FDTD_ERR_ARG;
+    }
+    CK(cudaSetDevice(b->device));
+    CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&b->ev0));
+    CK(cudaEventCreate(&b->ev1));
+    int rc;
+    std::map<std::tuple<int, int, int, int>, int> gidx;
+    for (uint32_t j = 0; j < n; ++j) {
+        fdtd_engine_s* e = engines[j];
+        if (!e) {
+            set_error("fdtd_batch_create: null engine");
+            return FDTD_ERR_ARG;
+        }
+        if (e->device != b->device) {
+            set_error("fdtd_batch_create: all jobs must live on one device");
+            return FDTD_ERR_ARG;
+        }
+        if (!e->use_tma) {
+            set_error("fdtd_batch_create: jobs must use the TMA kernels");
+            return FDTD_ERR_ARG;
+        }
+        for (uint32_t k = 0; k < j; ++k)
+            if (engines[k] == e) {
+                set_error("fdtd_batch_create: a job appears twice");
+                return FDTD_ERR_ARG;
+            }
+        if ((rc = engine_start(e))) return rc;
+        CK(cudaStreamSynchronize(e->stream));
+        b->jobs.push_back(e);
+        b->total_nodes += (uint64_t)e->N[0] * e->N[1] * e->N[2];
+        auto key = std::make_tuple((int)e->E.idx16, (int)e->H.idx16, (int)e->geo_on, e->feat);
+        auto it = gidx.find(key);
+        if (it == gidx.end()) {
+            Group G;
+            G.e16 = e->E.idx16;
+            G.h16 = e->H.idx16;
+            G.geo = e->geo_on;
+            G.feat = e->feat;
+            b->groups.push_back(std::move(G));
+            it = gidx.emplace(key, (int)b->groups.size() - 1).first;
+        }
+        b->groups[it->second].jobs.push_back((int)j);
+    }
+    // descriptors
+    std::vector<TmaMaps> hmaps(n);
+    for (uint32_t j = 0; j < n; ++j) hmaps[j] = b->jobs[j]->maps;
+    if ((rc = b->d_maps.alloc(n, b->device_bytes)) || (rc = b->d_jobs.alloc(n, b->device_bytes)) ||
+        (rc = b->d_adv.alloc(n, b->device_bytes)))
+        return rc;
+    std::vector<BatchJob> hj(n);
+    std::vector<AdvJob> ha(n);
+    for (uint32_t j = 0; j < n; ++j) {
+        fdtd_engine_s* e = b->jobs[j];
+        std::memset(&hj[j], 0, sizeof(BatchJob));
+        hj[j].g = e->g;
+        hj[j].ti = e->ti;
+        hj[j].maps = b->d_maps.p + j;
+        hj[j].interval = (int)e->interval;
+        ha[j].d_ts = e->d_ts.p;
+        ha[j].ps = e->ps;
+        ha[j].g = e->g;
+        ha[j].interval = (int)e->interval;
+        ha[j].energy_valid = e->energy_on_probe ? 1 : 0;
+    }
+    CK(cudaMemcpyAsync(b->d_maps.p, hmaps.data(), n * sizeof(TmaMaps), cudaMemcpyHostToDevice, b->stream));
+    CK(cudaMemcpyAsync(b->d_jobs.p, hj.data(), n * sizeof(BatchJob), cudaMemcpyHostToDevice, b->stream));
+    CK(cudaMemcpyAsync(b->d_adv.p, ha.data(), n * sizeof(AdvJob), cudaMemcpyHostToDevice, b->stream));
+    // work lists and persistent grid sizes
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
+    const size_t maxsm = stage_smem(false, true, b->stages);
+    if (maxsm > 48 * 1024 && (rc = batch_smem_attrs((int)maxsm))) return rc;
+    for (Group& G : b->groups) {
+        std::vector<WorkItem> wE, wH;
+        for (int j : G.jobs) {
+            const fdtd_engine_s* e = b->jobs[j];
+            const int bxE = (e->ti.ne[2] + 31) / 32, byE = (e->ti.ne[1] + TMA_TY - 1) / TMA_TY,
+                      bzE = (e->ti.ne[0] + b->XC - 1) / b->XC;
+            for (int z = 0; z < bzE; ++z)
+                for (int y = 0; y < byE; ++y)
+                    for (int x = 0; x < bxE; ++x) wE.push_back(WorkItem{j, x, y, z});
+            const int bxH = ((int)e->N[2] - 1 + 31) / 32, byH = ((int)e->N[1] - 1 + TMA_TY - 1) / TMA_TY,
+                      bzH = ((int)e->N[0] - 1 + b->XC - 1) / b->XC;
+            for (int z = 0; z < bzH; ++z)
+                for (int y = 0; y < byH; ++y)
+                    for (int x = 0; x < bxH; ++x) wH.push_back(WorkItem{j, x, y, z});
+        }
+        G.nE = (int)wE.size();
+        G.nH = (int)wH.size();
+        if ((rc = G.itE.alloc(wE.size(), b->device_bytes)) || (rc = G.itH.alloc(wH.size(), b->device_bytes))) return rc;
+        CK(cudaMemcpyAsync(G.itE.p, wE.data(), wE.size() * sizeof(WorkItem), cudaMemcpyHostToDevice, b->stream));
+        CK(cudaMemcpyAsync(G.itH.p, wH.data(), wH.size() * sizeof(WorkItem), cudaMemcpyHostToDevice, b->stream));
+        const bool up = (G.feat & FEAT_UPML) != 0;
+        G.smemE = stage_smem(G.e16, up, b->stages);
+        G.smemH = stage_smem(G.h16, up, b->stages);
+        int oE = occupancy(G, true, G.smemE), oH = occupancy(G, false, G.smemH);
+        if (b->blocks_per_sm > 0) {
+            oE = std::min(oE, b->blocks_per_sm);
+            oH = std::min(oH, b->blocks_per_sm);
+        }
+        G.gridE = std::max(1, std::min(G.nE, std::max(1, oE) * sms));
+        G.gridH = std::max(1, std::min(G.nH, std::max(1, oH) * sms));
+    }
+    CK(cudaStreamSynchronize(b->stream));
+    return FDTD_OK;
+}
+
+}  // namespace
+}  // namespace wipems
+
+extern "C" {
+
+int fdtd_batch_create(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts* opts, fdtd_batch_t* out) {
+    if (!engines || !out) {
+        set_error("fdtd_batch_create: null argument");
+        return FDTD_ERR_ARG;
+    }
+    fdtd_batch_s* b = new (std::nothrow) fdtd_batch_s();
+    if (!b) return FDTD_ERR_NOMEM;
+    int rc;
+    try {
+        rc = build_batch(engines, n, opts, b);
+    } catch (const std::bad_alloc&) {
+        set_error("fdtd_batch_create: host allocation failed");
+        rc = FDTD_ERR_NOMEM;
+    }
+    if (rc) {
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return FDTD_OK;
+}
+
+int fdtd_batch_destroy(fdtd_batch_t b) {
+    if (!b) return FDTD_OK;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    delete b;
+    return FDTD_OK;
+}
+
+int fdtd_batch_iterate(fdtd_batch_t b, uint32_t n) {
+    if (!b) return FDTD_ERR_ARG;
+    CK(cudaSetDevice(b->device));
+    b->last_launches = 0;
+    int rc;
+    if (b->graph_steps > 1 && n >= b->graph_steps && (rc = batch_graph(b))) return rc;
+    CK(cudaEventRecord(b->ev0, b->stream));
+    uint32_t left = n;
+    while (left > 0) {
+        if (b->graph && left >= b->graph_steps) {
+            CK(cudaGraphLaunch(b->graph, b->stream));
+            b->last_launches += (2 * b->groups.size() + 1) * b->graph_steps;
+            left -= b->graph_steps;
+            continue;
+        }
+        if ((rc = batch_step(b))) return rc;
+        left -= 1;
+    }
+    CK(cudaEventRecord(b->ev1, b->stream));
+    CK(cudaEventSynchronize(b->ev1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    b->last_ms = ms;
+    for (fdtd_engine_s* e : b->jobs) {
+        e->ts += n;
+        if ((rc = engine_check_errors(e))) return rc;
+    }
+    return FDTD_OK;
+}
+
+int fdtd_batch_info(fdtd_batch_t b, fdtd_batch_stats* st) {
+    if (!b || !st) return FDTD_ERR_ARG;
+    std::memset(st, 0, sizeof(*st));
+    st->num_jobs = (uint32_t)b->jobs.size();
+    st->num_groups = (uint32_t)b->groups.size();
+    st->total_nodes = b->total_nodes;
+    for (const Group& G : b->groups) {
+        st->work_items += (uint64_t)G.nE + G.nH;
+        st->persistent_blocks = std::max<uint32_t>(st->persistent_blocks, (uint32_t)std::max(G.gridE, G.gridH));
+    }
+    st->device_bytes = b->device_bytes;
+    st->last_ms = b->last_ms;
+    st->last_launches = b->last_launches;
+    return FDTD_OK;
+}
+
+}  // extern "C"

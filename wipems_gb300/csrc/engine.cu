@@ -18,113 +18,8 @@
 #include <string>
 #include <vector>
 
-#include "cop.h"
-#include "fdtd_host.h"
-#include "kernels.cuh"
-#include "kernels_tma.cuh"
 
-namespace wipems {
-namespace {
-
-#define CK(call)                                                           \
-    do {                                                                   \
-        cudaError_t e_ = (call);                                           \
-        if (e_ != cudaSuccess) {                                           \
-            set_error(std::string(#call) + ": " + cudaGetErrorString(e_)); \
-            return FDTD_ERR_CUDA;                                          \
-        }                                                                  \
-    } while (0)
-
-template <class T>
-struct DevBuf {
-    T* p = nullptr;
-    size_t n = 0;
-    ~DevBuf() {
-        if (p) cudaFree(p);
-    }
-    int alloc(size_t count, uint64_t& total) {
-        n = count;
-        if (count == 0) return FDTD_OK;
-        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
-        if (e != cudaSuccess) {
-            p = nullptr;
-            set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
-            return FDTD_ERR_NOMEM;
-        }
-        total += count * sizeof(T);
-        return FDTD_OK;
-    }
-};
-
-struct DevHalfBufs {
-    DevBuf<uint8_t> idx;
-    DevBuf<float> main, upml, ade, exc;
-    bool idx16 = true;
-};
-
-}  // namespace
-}  // namespace wipems
-
-using namespace wipems;
-
-struct fdtd_engine_s {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    uint32_t N[3];
-    int Nzp = 0;
-    long long comp = 0;
-    double dT = 0;
-    DevGrid g{};
-    DevBuf<float> V, I, FV, FI, AV, LV, AI, LI;
-    DevHalfBufs E, H;
-    DevBuf<float> geo;
-    DevBuf<float> sigV, sigC;
-    DevBuf<int> d_ts;
-    DevBuf<double> d_eacc;
-    DevBuf<double> d_energy_tmp;
-    // probes
-    std::vector<ProbeEntry> h_entries;
-    std::vector<int> h_first{0};
-    std::vector<double> h_weight;
-    DevBuf<ProbeEntry> d_entries;
-    DevBuf<int> d_first;
-    DevBuf<double> d_weight;
-    DevBuf<double> ring;
-    DevBuf<int> d_nsamp;
-    DevBuf<int> d_err;
-    ProbeSet ps{};
-    bool probes_uploaded = false;
-    uint32_t interval = 0;
-    bool energy_on_probe = true;
-    bool use_graphs = true;
-    uint32_t cap = 0;
-    // state
-    uint32_t ts = 0;
-    bool started = false;
-    bool need_initial_sample = true;
-    int feat = 0;
-    bool geo_on = false;
-    int TY = 8;
-    int XC = 8;
-    bool use_tma = true;
-    int stages = 3;
-    TmaMaps maps{};
-    TileInfo ti{};
-    size_t smem_direct = 0;
-    uint32_t num_tuples_e = 0, num_tuples_h = 0, upml_nodes = 0, ade_nodes = 0;
-    uint64_t device_bytes = 0;
-    cudaGraphExec_t chunk = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    double last_ms = 0;
-    uint64_t last_launches = 0;
-
-    ~fdtd_engine_s() {
-        if (chunk) cudaGraphExecDestroy(chunk);
-        if (ev0) cudaEventDestroy(ev0);
-        if (ev1) cudaEventDestroy(ev1);
-        if (stream) cudaStreamDestroy(stream);
-    }
-};
+#include "engine_state.h"
 
 namespace wipems {
 namespace {
@@ -643,6 +538,10 @@ int probe_entries(const fdtd_engine_s* e, const fdtd_probe_desc* p, std::vector<
 }
 
 }  // namespace
+
+int engine_start(fdtd_engine_s* e) { return start(e); }
+int engine_check_errors(fdtd_engine_s* e) { return check_error_word(e); }
+
 }  // namespace wipems
 
 // ===================================================================== C ABI

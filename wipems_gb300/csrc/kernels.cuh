@@ -215,8 +215,8 @@ struct ProbeSet {
 // Advances numTS by adv (Engine::IterateTS ++numTS) and, when sample is set,
 // records one probe/energy sample row (ProcessIntegral::Process): the probe
 // sums (ProcessVoltage / ProcessCurrent) as warp reductions in double.
-__global__ void k_advance_sample(int* d_ts, int adv, int sample, ProbeSet ps, const DevGrid g, int energy_valid,
-                                 double eps0, double mue0) {
+__device__ __forceinline__ void advance_sample(int* d_ts, int adv, int sample, const ProbeSet& ps, const DevGrid& g,
+                                               int energy_valid, double eps0, double mue0) {
     __shared__ int s_ts, s_row;
     if (threadIdx.x == 0) {
         int ts = *d_ts + adv;
@@ -264,8 +264,13 @@ __global__ void k_advance_sample(int* d_ts, int adv, int sample, ProbeSet ps, co
     }
 }
 
+static __global__ void k_advance_sample(int* d_ts, int adv, int sample, ProbeSet ps, const DevGrid g, int energy_valid,
+                                        double eps0, double mue0) {
+    advance_sample(d_ts, adv, sample, ps, g, energy_valid, eps0, mue0);
+}
+
 // Full-grid energy (CalcFastEnergy) on demand.
-__global__ void k_energy(const DevGrid g, double* out) {
+static __global__ void k_energy(const DevGrid g, double* out) {
     double es = 0.0, hs = 0.0;
     const long long nyz = (long long)(g.Ny - 1) * (g.Nz - 1);
     const long long total = (long long)(g.Nx - 1) * nyz;

@@ -130,35 +130,32 @@ __device__ __forceinline__ bool tile_has_upml(const TileInfo& ti, int x, int y0,
 }
 
 // ------------------------------------------------------------- E half-step
+// One tile of the voltage update: the 32 x TY tile (bx, by) over the
+// x-chunk bz.  ring counts the planes this block has pushed through its
+// mbarrier ring so far (the ring persists across the tiles of a persistent
+// block).  Returns false if a bounded wait gave up.
 template <typename IdxT, int FEAT, bool GEO>
-__global__ void __launch_bounds__(TMA_TY * 32) k_volt_tma(const DevGrid g, const __grid_constant__ TmaMaps m,
-                                                          const TileInfo ti, int ts_off, int XC, int STAGES) {
+__device__ __forceinline__ bool volt_tile(const DevGrid& g, const TmaMaps& m, const TileInfo& ti, int bx, int by,
+                                          int bz, int XC, int STAGES, float* smem, uint64_t* bars, uint32_t& ring,
+                                          int numTS) {
     constexpr bool UPML = (FEAT & FEAT_UPML) != 0;
     using L = StageLayout<IdxT, UPML>;
     constexpr int HW = L::HW;
-    extern __shared__ __align__(128) float smem_raw[];
-    float* smem = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * STAGES);
     const int tz = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * 32 + tz;
-    const int z0 = blockIdx.x * 32, y0 = blockIdx.y * TMA_TY;
+    const int z0 = bx * 32, y0 = by * TMA_TY;
     const int z = z0 + tz, y = y0 + ty;
-    const int x0 = blockIdx.z * XC;
+    const int x0 = bz * XC;
     const int x1 = min(x0 + XC, ti.ne[0]);
     const int nplanes = x1 - x0;
     const bool valid = (y < ti.ne[1]) && (z < ti.ne[2]);
-    const int numTS = *g.d_ts + ts_off;
     const long long C = g.comp;
     const int zl = min(z0 + 31, g.Nz - 1), yl = min(y0 + TMA_TY - 1, g.Ny - 1);
+    const uint32_t base = ring;
 
-    if (tid == 0) {
-        for (int s = 0; s < STAGES; ++s) mbar_init(&bars[s], 1);
-        fence_barrier_init();
-    }
-    __syncthreads();
-
-    auto issue = [&](int r) {  // thread 0: plane x0+r into stage r % STAGES
-        const int s = r % STAGES;
+    auto issue = [&](int r) {  // thread 0: plane x0+r into the ring
+        const uint32_t q = base + (uint32_t)r;
+        const int s = (int)(q % (uint32_t)STAGES);
         const int x = x0 + r;
         float* st = smem + (size_t)s * L::STAGE;
         const bool up = UPML && tile_has_upml(ti, x, y0, yl, z0, zl);
@@ -172,6 +169,7 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_volt_tma(const DevGrid g, const
 
     int issued = 0;
     if (tid == 0) {
+        fence_proxy_async();
         for (; issued < min(STAGES - 1, nplanes); ++issued) issue(issued);
     }
     float p1 = 0.f, p2 = 0.f;  // I1, I2 at x-1
@@ -199,8 +197,9 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_volt_tma(const DevGrid g, const
             issue(issued);
             ++issued;
         }
-        const int s = r % STAGES;
-        const bool ok = mbar_wait(&bars[s], (uint32_t)((r / STAGES) & 1));
+        const uint32_t q = base + (uint32_t)r;
+        const int s = (int)(q % (uint32_t)STAGES);
+        const bool ok = mbar_wait(&bars[s], (q / (uint32_t)STAGES) & 1u);
         const int x = x0 + r;
         const float* st = smem + (size_t)s * L::STAGE;
         float c1 = 0.f, c2 = 0.f;
@@ -247,44 +246,44 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_volt_tma(const DevGrid g, const
             break;
         }
     }
+    ring = base + (uint32_t)nplanes;
     if (aborted && tid == 0) {
         atomicOr(ti.d_err, 4);
         // wait (bounded) for the copies this block still has in flight
-        for (int q = r; q < issued; ++q) mbar_wait(&bars[q % STAGES], (uint32_t)((q / STAGES) & 1));
+        for (int k = r; k < issued; ++k) {
+            const uint32_t q = base + (uint32_t)k;
+            mbar_wait(&bars[q % (uint32_t)STAGES], (q / (uint32_t)STAGES) & 1u);
+        }
     }
+    return !aborted;
 }
 
 // ------------------------------------------------------------- H half-step
-template <typename IdxT, int FEAT, bool GEO, bool ENERGY>
-__global__ void __launch_bounds__(TMA_TY * 32) k_curr_tma(const DevGrid g, const __grid_constant__ TmaMaps m,
-                                                          const TileInfo ti, int ts_off, int XC, int STAGES) {
+// One tile of the current update (see volt_tile).  es/ec/hs/hc: the
+// thread's Kahan sums of V^2 and I^2, accumulated when energy is set.
+template <typename IdxT, int FEAT, bool GEO>
+__device__ __forceinline__ bool curr_tile(const DevGrid& g, const TmaMaps& m, const TileInfo& ti, int bx, int by,
+                                          int bz, int XC, int STAGES, float* smem, uint64_t* bars, uint32_t& ring,
+                                          int numTS, bool energy, float& es, float& ec, float& hs, float& hc) {
     constexpr bool UPML = (FEAT & FEAT_UPML) != 0;
     using L = StageLayout<IdxT, UPML>;
     constexpr int HW = L::HW;
-    extern __shared__ __align__(128) float smem_raw[];
-    float* smem = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * STAGES);
     const int tz = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * 32 + tz;
-    const int z0 = blockIdx.x * 32, y0 = blockIdx.y * TMA_TY;
+    const int z0 = bx * 32, y0 = by * TMA_TY;
     const int z = z0 + tz, y = y0 + ty;
-    const int x0 = blockIdx.z * XC;
+    const int x0 = bz * XC;
     const int x1 = min(x0 + XC, g.Nx - 1);
     const int nplanes = x1 - x0;      // planes updated
     const int nload = nplanes + 1;    // plane x1 is read as the x+1 neighbour
     const bool active = (z < g.Nz - 1) && (y < g.Ny - 1);
-    const int numTS = *g.d_ts + ts_off;
     const long long C = g.comp;
     const int zl = min(z0 + 31, g.Nz - 1), yl = min(y0 + TMA_TY - 1, g.Ny - 1);
-
-    if (tid == 0) {
-        for (int s = 0; s < STAGES; ++s) mbar_init(&bars[s], 1);
-        fence_barrier_init();
-    }
-    __syncthreads();
+    const uint32_t base = ring;
 
     auto issue = [&](int r) {
-        const int s = r % STAGES;
+        const uint32_t q = base + (uint32_t)r;
+        const int s = (int)(q % (uint32_t)STAGES);
         const int x = x0 + r;
         float* st = smem + (size_t)s * L::STAGE;
         const bool upd = r < nplanes;  // plane x1 only contributes V
@@ -302,9 +301,9 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_curr_tma(const DevGrid g, const
 
     int issued = 0;
     if (nplanes > 0 && tid == 0) {
+        fence_proxy_async();
         for (; issued < min(STAGES - 1, nload); ++issued) issue(issued);
     }
-    float es = 0.f, ec = 0.f, hs = 0.f, hc = 0.f;  // Kahan sums of V^2 and I^2
     const long long yz = (long long)y * g.Nzp + z;
     float gyE = 0.f, gyI = 0.f, gzE = 0.f, gzI = 0.f;  // dH / iM parts
     if (GEO && active) {
@@ -323,10 +322,11 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_curr_tma(const DevGrid g, const
             issue(issued);
             ++issued;
         }
-        const int s = r % STAGES;
-        const int sn = (r + 1) % STAGES;
-        bool ok = mbar_wait(&bars[s], (uint32_t)((r / STAGES) & 1));
-        ok = ok && mbar_wait(&bars[sn], (uint32_t)(((r + 1) / STAGES) & 1));
+        const uint32_t q = base + (uint32_t)r;
+        const int s = (int)(q % (uint32_t)STAGES);
+        const int sn = (int)((q + 1) % (uint32_t)STAGES);
+        bool ok = mbar_wait(&bars[s], (q / (uint32_t)STAGES) & 1u);
+        ok = ok && mbar_wait(&bars[sn], ((q + 1) / (uint32_t)STAGES) & 1u);
         const int x = x0 + r;
         if (ok && active) {
             const float* st = smem + (size_t)s * L::STAGE;
@@ -360,7 +360,7 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_curr_tma(const DevGrid g, const
             Ip[0] = cu[0];
             Ip[C] = cu[1];
             Ip[2 * C] = cu[2];
-            if (ENERGY) {
+            if (energy) {
                 kahan_add(es, ec, __fmul_rn(c0, c0));
                 kahan_add(es, ec, __fmul_rn(c1, c1));
                 kahan_add(es, ec, __fmul_rn(c2, c2));
@@ -374,21 +374,131 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_curr_tma(const DevGrid g, const
             break;
         }
     }
+    ring = base + (uint32_t)(nplanes > 0 ? nload : 0);
     if (aborted && tid == 0) {
         atomicOr(ti.d_err, 4);
-        for (int q = r; q < issued; ++q) mbar_wait(&bars[q % STAGES], (uint32_t)((q / STAGES) & 1));
+        for (int k = r; k < issued; ++k) {
+            const uint32_t q = base + (uint32_t)k;
+            mbar_wait(&bars[q % (uint32_t)STAGES], (q / (uint32_t)STAGES) & 1u);
+        }
     }
-    if (ENERGY) {
-        double esum = (double)es - (double)ec, hsum = (double)hs - (double)hc;
+    return !aborted;
+}
+
+// warp-reduce the Kahan sums and add them to the job's energy accumulators
+__device__ __forceinline__ void flush_energy(double* eacc, float es, float ec, float hs, float hc) {
+    double esum = (double)es - (double)ec, hsum = (double)hs - (double)hc;
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            esum += __shfl_down_sync(0xffffffffu, esum, off);
-            hsum += __shfl_down_sync(0xffffffffu, hsum, off);
-        }
-        if (tz == 0 && (esum != 0.0 || hsum != 0.0)) {
-            atomicAdd(&g.d_eacc[0], esum);
-            atomicAdd(&g.d_eacc[1], hsum);
-        }
+    for (int off = 16; off > 0; off >>= 1) {
+        esum += __shfl_down_sync(0xffffffffu, esum, off);
+        hsum += __shfl_down_sync(0xffffffffu, hsum, off);
+    }
+    if ((threadIdx.x & 31) == 0 && (esum != 0.0 || hsum != 0.0)) {
+        atomicAdd(&eacc[0], esum);
+        atomicAdd(&eacc[1], hsum);
+    }
+}
+
+__device__ __forceinline__ float* aligned_smem(float* raw) {
+    return reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(raw) + 127) & ~(uintptr_t)127);
+}
+
+__device__ __forceinline__ void init_ring(uint64_t* bars, int STAGES) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        for (int s = 0; s < STAGES; ++s) mbar_init(&bars[s], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------- single job
+template <typename IdxT, int FEAT, bool GEO>
+__global__ void __launch_bounds__(TMA_TY * 32) k_volt_tma(const DevGrid g, const __grid_constant__ TmaMaps m,
+                                                          const TileInfo ti, int ts_off, int XC, int STAGES) {
+    using L = StageLayout<IdxT, (FEAT & FEAT_UPML) != 0>;
+    extern __shared__ __align__(128) float smem_raw[];
+    float* smem = aligned_smem(smem_raw);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * STAGES);
+    init_ring(bars, STAGES);
+    uint32_t ring = 0;
+    volt_tile<IdxT, FEAT, GEO>(g, m, ti, blockIdx.x, blockIdx.y, blockIdx.z, XC, STAGES, smem, bars, ring,
+                               *g.d_ts + ts_off);
+}
+
+template <typename IdxT, int FEAT, bool GEO, bool ENERGY>
+__global__ void __launch_bounds__(TMA_TY * 32) k_curr_tma(const DevGrid g, const __grid_constant__ TmaMaps m,
+                                                          const TileInfo ti, int ts_off, int XC, int STAGES) {
+    using L = StageLayout<IdxT, (FEAT & FEAT_UPML) != 0>;
+    extern __shared__ __align__(128) float smem_raw[];
+    float* smem = aligned_smem(smem_raw);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * STAGES);
+    init_ring(bars, STAGES);
+    uint32_t ring = 0;
+    float es = 0.f, ec = 0.f, hs = 0.f, hc = 0.f;
+    curr_tile<IdxT, FEAT, GEO>(g, m, ti, blockIdx.x, blockIdx.y, blockIdx.z, XC, STAGES, smem, bars, ring,
+                               *g.d_ts + ts_off, ENERGY, es, ec, hs, hc);
+    if (ENERGY) flush_energy(g.d_eacc, es, ec, hs, hc);
+}
+
+// ---------------------------------------------------------- batched jobs
+// One job of a batch: its grid, UPML geometry, tensor maps (in global
+// memory) and probe interval (0 = no sampling).
+struct BatchJob {
+    DevGrid g;
+    TileInfo ti;
+    const TmaMaps* maps;
+    int interval;
+    int pad[3];
+};
+
+// Work item of a persistent batched kernel: job, tile (bx, by), x-chunk bz.
+struct WorkItem {
+    int job, bx, by, bz;
+};
+
+// Persistent voltage half-step over the work items of many jobs: block b
+// takes items b, b + gridDim.x, ...  Every job's numTS is read from its own
+// counter, so jobs need not be in step.
+template <typename IdxT, int FEAT, bool GEO>
+__global__ void __launch_bounds__(TMA_TY * 32) k_volt_batch(const BatchJob* __restrict__ jobs,
+                                                            const WorkItem* __restrict__ items, int nitems, int XC,
+                                                            int STAGES) {
+    using L = StageLayout<IdxT, (FEAT & FEAT_UPML) != 0>;
+    extern __shared__ __align__(128) float smem_raw[];
+    float* smem = aligned_smem(smem_raw);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * STAGES);
+    init_ring(bars, STAGES);
+    uint32_t ring = 0;
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const WorkItem w = items[it];
+        const BatchJob& J = jobs[w.job];
+        if (!volt_tile<IdxT, FEAT, GEO>(J.g, *J.maps, J.ti, w.bx, w.by, w.bz, XC, STAGES, smem, bars, ring,
+                                        *J.g.d_ts))
+            break;
+    }
+}
+
+template <typename IdxT, int FEAT, bool GEO>
+__global__ void __launch_bounds__(TMA_TY * 32) k_curr_batch(const BatchJob* __restrict__ jobs,
+                                                            const WorkItem* __restrict__ items, int nitems, int XC,
+                                                            int STAGES) {
+    using L = StageLayout<IdxT, (FEAT & FEAT_UPML) != 0>;
+    extern __shared__ __align__(128) float smem_raw[];
+    float* smem = aligned_smem(smem_raw);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * STAGES);
+    init_ring(bars, STAGES);
+    uint32_t ring = 0;
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const WorkItem w = items[it];
+        const BatchJob& J = jobs[w.job];
+        // energy on the job's sample steps (the sample after this step)
+        const int numTS = *J.g.d_ts;
+        const bool energy = J.interval > 0 && ((numTS + 1) % J.interval) == 0;
+        float es = 0.f, ec = 0.f, hs = 0.f, hc = 0.f;
+        const bool ok = curr_tile<IdxT, FEAT, GEO>(J.g, *J.maps, J.ti, w.bx, w.by, w.bz, XC, STAGES, smem, bars,
+                                                   ring, numTS, energy, es, ec, hs, hc);
+        if (energy) flush_energy(J.g.d_eacc, es, ec, hs, hc);
+        if (!ok) break;
     }
 }
 

@@ -385,6 +385,39 @@ class Engine:
         return ms.value, n.value
 
 
+class Batch:
+    """Batched mode: the given engines advance together, one persistent
+    kernel per half-step and kernel variant (see fdtd_batch_create).  The
+    engines must outlive the batch."""
+
+    def __init__(self, engines, x_chunk: int = 0, stages: int = 0, blocks_per_sm: int = 0, graph_steps: int = 0):
+        self.engines = list(engines)
+        arr = (C.c_void_p * len(self.engines))(*[e._h.value for e in self.engines])
+        o = _abi.FdtdBatchOpts(int(x_chunk), int(stages), int(blocks_per_sm), int(graph_steps))
+        h = C.c_void_p()
+        check(lib().fdtd_batch_create(arr, len(self.engines), C.byref(o), C.byref(h)), "fdtd_batch_create")
+        self._h = h
+
+    def iterate(self, n: int):
+        check(lib().fdtd_batch_iterate(self._h, int(n)), "fdtd_batch_iterate")
+
+    def stats(self) -> dict:
+        s = _abi.FdtdBatchStats()
+        check(lib().fdtd_batch_info(self._h, C.byref(s)), "fdtd_batch_info")
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fdtd_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def run_fdtd(engine: Engine, nr_ts: int, end_crit: float = 1e-6) -> dict:
     """openEMS::RunFDTD's loop: iterate in probe-interval chunks until NrTS
     or until the energy has decayed below end_crit relative to its maximum
