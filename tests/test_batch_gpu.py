@@ -1,6 +1,10 @@
 """Batched mode: jobs of different sizes and kernel variants advanced by the
 persistent batched kernels must produce exactly what each job produces when
-run alone (same per-node arithmetic; only the energy sums' order differs)."""
+run alone: fields and probe values bit for bit (same per-node arithmetic).
+The energy is a float-Kahan-per-thread, double-across-threads sum whose
+grouping follows the tile shape, so it agrees to 1e-6 relative (it only
+feeds the -40 dB end criterion).
+"""
 import numpy as np
 import pytest
 
@@ -27,7 +31,7 @@ def _check_same(solo, batched):
     assert np.array_equal(ss.ts, sb.ts)
     assert np.array_equal(ss.values, sb.values)
     ok = ss.energy > 0
-    assert np.allclose(sb.energy[ok], ss.energy[ok], rtol=1e-9, atol=0)
+    assert np.allclose(sb.energy[ok], ss.energy[ok], rtol=1e-6, atol=0)
 
 
 @pytest.mark.parametrize("graph_steps", [8, 1])

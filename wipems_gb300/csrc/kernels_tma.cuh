@@ -103,6 +103,16 @@ __device__ __forceinline__ void tma_3d(void* dst, const CUtensorMap* map, uint64
         : "memory");
 }
 
+// Tensor maps that live in global memory (the batched kernels' per-job maps,
+// written by host copies) are read through the tensormap proxy: an acquire
+// fence on each 128-byte map orders those writes before the TMA reads them.
+__device__ __forceinline__ void tensormap_acquire(const TmaMaps* m) {
+    const char* p = reinterpret_cast<const char*>(m);
+#pragma unroll
+    for (int k = 0; k < (int)(sizeof(TmaMaps) / 128); ++k)
+        asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"(p + 128 * k) : "memory");
+}
+
 // stage layout (floats, every buffer 128-byte aligned)
 template <typename IdxT, bool UPML>
 struct StageLayout {
@@ -469,9 +479,14 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_volt_batch(const BatchJob* __re
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * STAGES);
     init_ring(bars, STAGES);
     uint32_t ring = 0;
+    int last_job = -1;
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const WorkItem w = items[it];
         const BatchJob& J = jobs[w.job];
+        if (w.job != last_job) {
+            if (threadIdx.x == 0 && threadIdx.y == 0) tensormap_acquire(J.maps);
+            last_job = w.job;
+        }
         if (!volt_tile<IdxT, FEAT, GEO>(J.g, *J.maps, J.ti, w.bx, w.by, w.bz, XC, STAGES, smem, bars, ring,
                                         *J.g.d_ts))
             break;
@@ -488,9 +503,14 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_curr_batch(const BatchJob* __re
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * STAGES);
     init_ring(bars, STAGES);
     uint32_t ring = 0;
+    int last_job = -1;
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const WorkItem w = items[it];
         const BatchJob& J = jobs[w.job];
+        if (w.job != last_job) {
+            if (threadIdx.x == 0 && threadIdx.y == 0) tensormap_acquire(J.maps);
+            last_job = w.job;
+        }
         // energy on the job's sample steps (the sample after this step)
         const int numTS = *J.g.d_ts;
         const bool energy = J.interval > 0 && ((numTS + 1) % J.interval) == 0;
