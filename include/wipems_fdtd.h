@@ -282,6 +282,12 @@ typedef struct {
     int      kernel;          /* 0 = TMA-pipelined kernels (default),
                                  1 = direct-load kernels */
     int      stages;          /* TMA ring depth in x-planes, 3..8 (0 = 3) */
+    double   end_crit;        /* > 0: the job stops on the device at the first
+                                 sample whose energy is <= end_crit x the
+                                 largest sampled energy, or at max_timesteps
+                                 (openEMS::RunFDTD's end criterion,
+                                 openems.cpp:1285-1314); needs probe_interval
+                                 and energy_on_probe.  0 = off */
 } fdtd_engine_opts;
 
 /* Operator::CreateEngine for the CUDA engine: compresses the coefficient
@@ -312,6 +318,9 @@ int fdtd_engine_add_probe(fdtd_engine_t eng, const fdtd_probe_desc* p,
 /* Engine::IterateTS (engine.cpp:255-274). */
 int fdtd_engine_iterate(fdtd_engine_t eng, uint32_t n_steps);
 /* Engine::GetNumberOfTimesteps. */
+/* 1 once the engine's end criterion (opts.end_crit) stopped it, as of the
+ * last iterate; numTS then stays at the stopping timestep. */
+int fdtd_engine_done(fdtd_engine_t eng, int* done);
 int fdtd_engine_num_timesteps(fdtd_engine_t eng, uint32_t* ts);
 
 /* Number of recorded samples and the per-sample record layout:
@@ -376,10 +385,14 @@ typedef struct {
     int stages;         /* TMA ring depth 3..8 (0 = 3) */
     int blocks_per_sm;  /* cap on resident blocks per SM (0 = occupancy) */
     int graph_steps;    /* timesteps per captured graph (0 = 8, 1 = none) */
+    int bin_mib;        /* L2 bins: jobs are packed into bins of at most this
+                           many MiB of device state; each bin runs graph_steps
+                           steps in a row so its data is re-read from L2
+                           (0 = one bin with every job) */
 } fdtd_batch_opts;
 
 typedef struct {
-    uint32_t num_jobs, num_groups;
+    uint32_t num_jobs, num_groups, num_bins;
     uint64_t total_nodes;
     uint64_t work_items;
     uint32_t persistent_blocks;

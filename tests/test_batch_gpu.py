@@ -8,7 +8,7 @@ feeds the -40 dB end criterion).
 import numpy as np
 import pytest
 
-from wipems_gb300 import Batch, CompressedOperator, Engine, Operator, scenes
+from wipems_gb300 import Batch, CompressedOperator, Engine, Operator, run_fdtd, scenes
 
 pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("libs")]
 
@@ -34,8 +34,8 @@ def _check_same(solo, batched):
     assert np.allclose(sb.energy[ok], ss.energy[ok], rtol=1e-6, atol=0)
 
 
-@pytest.mark.parametrize("graph_steps", [8, 1])
-def test_batch_equals_solo_runs(graph_steps):
+@pytest.mark.parametrize("graph_steps,bin_mib", [(8, 0), (1, 0), (8, 1)])
+def test_batch_equals_solo_runs(graph_steps, bin_mib):
     nsteps = 130
     ops = _ops(400)
     cops = [CompressedOperator(op) for op in ops]
@@ -43,9 +43,10 @@ def test_batch_equals_solo_runs(graph_steps):
     for e in solo:
         e.iterate(nsteps)
     jobs = [Engine(c) for c in cops]
-    b = Batch(jobs, graph_steps=graph_steps)
+    b = Batch(jobs, graph_steps=graph_steps, bin_mib=bin_mib)
     st = b.stats()
     assert st["num_jobs"] == len(jobs) and st["num_groups"] >= 3
+    assert (st["num_bins"] > 1) == (bin_mib > 0)
     b.iterate(nsteps - 37)
     b.iterate(37)
     for s, j in zip(solo, jobs):
@@ -65,4 +66,47 @@ def test_batch_jobs_at_different_timesteps():
     b = Batch(jobs, x_chunk=4, stages=4)
     b.iterate(60)
     for s, j in zip(solo, jobs):
+        _check_same(s, j)
+
+
+END_KINDS = ["upml", "drude", "graded", "lorentz"]   # the last one never decays to 1e-3 in 800 steps
+
+
+def test_device_end_criterion_matches_host_loop():
+    """The on-device end criterion stops a job at the same timestep as
+    RunFDTD's host loop (run_fdtd), with identical samples and fields; later
+    iterate calls leave a stopped job untouched."""
+    nr_ts, crit = 800, 1e-3
+    stops = []
+    for k in END_KINDS:
+        op = Operator(scenes.mini(k, seed=3, nr_ts=nr_ts))
+        host = Engine(op)
+        r = run_fdtd(host, nr_ts, crit)
+        dev = Engine(op, end_crit=crit)
+        for n in (100, 300, 400):
+            dev.iterate(n)
+        assert dev.num_timesteps == r["timesteps"]
+        assert dev.done
+        _check_same(host, dev)
+        V0, _ = dev.fields()
+        dev.iterate(50)
+        assert dev.num_timesteps == r["timesteps"]
+        assert np.array_equal(dev.fields()[0], V0)
+        stops.append(r["timesteps"])
+    assert min(stops) < nr_ts and max(stops) == nr_ts
+
+
+def test_batch_end_criterion_same_as_alone():
+    """Jobs that stop on their own end criterion inside a batch (L2 bins,
+    graphs) stop at the same step with the same results as alone."""
+    nr_ts, crit = 800, 1e-3
+    cops = [CompressedOperator(Operator(scenes.mini(k, seed=3, nr_ts=nr_ts))) for k in END_KINDS]
+    solo = [Engine(c, end_crit=crit) for c in cops]
+    for e in solo:
+        e.iterate(nr_ts)
+    jobs = [Engine(c, end_crit=crit) for c in cops]
+    b = Batch(jobs, graph_steps=16, bin_mib=1)
+    b.iterate(nr_ts + 64)
+    for s, j in zip(solo, jobs):
+        assert j.num_timesteps == s.num_timesteps and j.done == s.done
         _check_same(s, j)

@@ -59,7 +59,7 @@ class FdtdProbeDesc(C.Structure):
 class FdtdEngineOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("max_timesteps", u32), ("probe_interval", u32),
                 ("use_graphs", C.c_int), ("energy_on_probe", C.c_int), ("tile_y", C.c_int),
-                ("x_chunk", C.c_int), ("kernel", C.c_int), ("stages", C.c_int)]
+                ("x_chunk", C.c_int), ("kernel", C.c_int), ("stages", C.c_int), ("end_crit", C.c_double)]
 
 
 class FdtdEngineStats(C.Structure):
@@ -76,11 +76,12 @@ class FdtdCopInfo(C.Structure):
 
 
 class FdtdBatchOpts(C.Structure):
-    _fields_ = [("x_chunk", C.c_int), ("stages", C.c_int), ("blocks_per_sm", C.c_int), ("graph_steps", C.c_int)]
+    _fields_ = [("x_chunk", C.c_int), ("stages", C.c_int), ("blocks_per_sm", C.c_int), ("graph_steps", C.c_int),
+                ("bin_mib", C.c_int)]
 
 
 class FdtdBatchStats(C.Structure):
-    _fields_ = [("num_jobs", u32), ("num_groups", u32), ("total_nodes", C.c_uint64), ("work_items", C.c_uint64),
+    _fields_ = [("num_jobs", u32), ("num_groups", u32), ("num_bins", u32), ("total_nodes", C.c_uint64), ("work_items", C.c_uint64),
                 ("persistent_blocks", u32), ("device_bytes", C.c_uint64), ("last_ms", C.c_double),
                 ("last_launches", C.c_uint64)]
 
@@ -127,6 +128,7 @@ SIGNATURES = [
     ("fdtd_engine_destroy", C.c_int, [_P]),
     ("fdtd_engine_add_probe", C.c_int, [_P, C.POINTER(FdtdProbeDesc), PU32]),
     ("fdtd_engine_iterate", C.c_int, [_P, u32]),
+    ("fdtd_engine_done", C.c_int, [_P, C.POINTER(C.c_int)]),
     ("fdtd_engine_num_timesteps", C.c_int, [_P, PU32]),
     ("fdtd_engine_num_samples", C.c_int, [_P, PU32]),
     ("fdtd_engine_read_samples", C.c_int, [_P, u32, u32, PU32, PD, PD]),

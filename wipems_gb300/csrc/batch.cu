@@ -31,6 +31,8 @@ struct AdvJob {
     DevGrid g;
     int interval;
     int energy_valid;
+    const int* ctl;  // the job's control words (numTS, samples, errors, done)
+    int* out;        // the batch's copy of them, read back after each iterate
 };
 
 // Block j advances job j's numTS by one and records a sample row when the
@@ -45,9 +47,12 @@ __global__ void k_batch_advance(const AdvJob* __restrict__ jobs, double eps0, do
     }
     __syncthreads();
     advance_sample(J.d_ts, 1, s_sample, J.ps, J.g, J.energy_valid, eps0, mue0);
+    __syncthreads();
+    if (threadIdx.x < 4) J.out[threadIdx.x] = J.ctl[threadIdx.x];
 }
 
 struct Group {
+    int bin = 0;
     bool e16 = true, h16 = true, geo = false;
     int feat = 0;
     std::vector<int> jobs;
@@ -169,6 +174,16 @@ struct fdtd_batch_s {
     DevBuf<BatchJob> d_jobs;
     DevBuf<TmaMaps> d_maps;
     DevBuf<AdvJob> d_adv;
+    DevBuf<int> d_status;      // [jobs][4] control words of every job
+    std::vector<int> h_status;
+    // L2 bins: jobs whose footprints together fit a bin run graph_steps
+    // steps in a row while their data stays in L2, then the next bin runs
+    struct Bin {
+        std::vector<int> groups;
+        int first = 0, count = 0;  // job range (jobs are stored bin by bin)
+    };
+    std::vector<Bin> bins;
+    uint64_t bin_bytes = 0;
     int XC = 8, stages = 3, blocks_per_sm = 0;
     uint32_t graph_steps = 8;
     cudaGraphExec_t graph = nullptr;
@@ -188,11 +203,13 @@ struct fdtd_batch_s {
 namespace wipems {
 namespace {
 
-int batch_step(fdtd_batch_s* b) {
-    for (const Group& G : b->groups) launch_group_volt(G, b->d_jobs.p, b->XC, b->stages, b->stream);
-    for (const Group& G : b->groups) launch_group_curr(G, b->d_jobs.p, b->XC, b->stages, b->stream);
-    k_batch_advance<<<(unsigned)b->jobs.size(), 256, 0, b->stream>>>(b->d_adv.p, kEps0, kMue0);
-    b->last_launches += 2 * b->groups.size() + 1;
+// one timestep of the jobs of bin k
+int bin_step(fdtd_batch_s* b, size_t k) {
+    const fdtd_batch_s::Bin& B = b->bins[k];
+    for (int gi : B.groups) launch_group_volt(b->groups[gi], b->d_jobs.p, b->XC, b->stages, b->stream);
+    for (int gi : B.groups) launch_group_curr(b->groups[gi], b->d_jobs.p, b->XC, b->stages, b->stream);
+    k_batch_advance<<<(unsigned)B.count, 256, 0, b->stream>>>(b->d_adv.p + B.first, kEps0, kMue0);
+    b->last_launches += 2 * B.groups.size() + 1;
     const cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) {
         set_error(std::string("batch kernel launch: ") + cudaGetErrorString(err));
@@ -207,7 +224,8 @@ int batch_graph(fdtd_batch_s* b) {
     CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     int rc = FDTD_OK;
     const uint64_t saved = b->last_launches;
-    for (uint32_t k = 0; k < b->graph_steps && rc == FDTD_OK; ++k) rc = batch_step(b);
+    for (size_t bi = 0; bi < b->bins.size() && rc == FDTD_OK; ++bi)
+        for (uint32_t k = 0; k < b->graph_steps && rc == FDTD_OK; ++k) rc = bin_step(b, bi);
     b->last_launches = saved;
     const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
     if (rc) {
@@ -233,11 +251,12 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
         set_error("fdtd_batch_create: no jobs");
         return FDTD_ERR_ARG;
     }
-    b->device = engines[0]->device;
+    b->device = engines[0] ? engines[0]->device : 0;
     b->XC = (o && o->x_chunk > 0) ? o->x_chunk : 8;
     b->stages = (o && o->stages > 0) ? o->stages : 3;
     b->blocks_per_sm = (o && o->blocks_per_sm > 0) ? o->blocks_per_sm : 0;
     b->graph_steps = (o && o->graph_steps > 0) ? (uint32_t)o->graph_steps : 8;
+    b->bin_bytes = (o && o->bin_mib > 0) ? (uint64_t)o->bin_mib << 20 : 0;
     if (b->stages < 3 || b->stages > TMA_MAX_STAGES) {
         set_error("fdtd_batch_create: stages must be 3..8");
         return FDTD_ERR_ARG;
@@ -247,7 +266,6 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
     CK(cudaEventCreate(&b->ev0));
     CK(cudaEventCreate(&b->ev1));
     int rc;
-    std::map<std::tuple<int, int, int, int>, int> gidx;
     for (uint32_t j = 0; j < n; ++j) {
         fdtd_engine_s* e = engines[j];
         if (!e) {
@@ -269,27 +287,66 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
             }
         if ((rc = engine_start(e))) return rc;
         CK(cudaStreamSynchronize(e->stream));
-        b->jobs.push_back(e);
-        b->total_nodes += (uint64_t)e->N[0] * e->N[1] * e->N[2];
-        auto key = std::make_tuple((int)e->E.idx16, (int)e->H.idx16, (int)e->geo_on, e->feat);
-        auto it = gidx.find(key);
-        if (it == gidx.end()) {
-            Group G;
-            G.e16 = e->E.idx16;
-            G.h16 = e->H.idx16;
-            G.geo = e->geo_on;
-            G.feat = e->feat;
-            b->groups.push_back(std::move(G));
-            it = gidx.emplace(key, (int)b->groups.size() - 1).first;
+    }
+    // L2 bins: first fit by decreasing footprint (one bin when binning is off)
+    std::vector<std::vector<fdtd_engine_s*>> binned;
+    {
+        std::vector<fdtd_engine_s*> byfoot(engines, engines + n);
+        std::vector<uint64_t> load;
+        if (b->bin_bytes)
+            std::stable_sort(byfoot.begin(), byfoot.end(),
+                             [](const fdtd_engine_s* a, const fdtd_engine_s* c) { return a->device_bytes > c->device_bytes; });
+        else
+            binned.emplace_back();
+        for (fdtd_engine_s* e : byfoot) {
+            if (!b->bin_bytes) {
+                binned[0].push_back(e);
+                continue;
+            }
+            size_t k = 0;
+            while (k < binned.size() && load[k] + e->device_bytes > b->bin_bytes) ++k;
+            if (k == binned.size()) {
+                binned.emplace_back();
+                load.push_back(0);
+            }
+            binned[k].push_back(e);
+            load[k] += e->device_bytes;
         }
-        b->groups[it->second].jobs.push_back((int)j);
+    }
+    // jobs stored bin by bin; groups per (bin, kernel variant)
+    for (size_t bi = 0; bi < binned.size(); ++bi) {
+        fdtd_batch_s::Bin B;
+        B.first = (int)b->jobs.size();
+        B.count = (int)binned[bi].size();
+        std::map<std::tuple<int, int, int, int>, int> gidx;
+        for (fdtd_engine_s* e : binned[bi]) {
+            const int j = (int)b->jobs.size();
+            b->jobs.push_back(e);
+            b->total_nodes += (uint64_t)e->N[0] * e->N[1] * e->N[2];
+            auto key = std::make_tuple((int)e->E.idx16, (int)e->H.idx16, (int)e->geo_on, e->feat);
+            auto it = gidx.find(key);
+            if (it == gidx.end()) {
+                Group G;
+                G.bin = (int)bi;
+                G.e16 = e->E.idx16;
+                G.h16 = e->H.idx16;
+                G.geo = e->geo_on;
+                G.feat = e->feat;
+                b->groups.push_back(std::move(G));
+                it = gidx.emplace(key, (int)b->groups.size() - 1).first;
+                B.groups.push_back(it->second);
+            }
+            b->groups[it->second].jobs.push_back(j);
+        }
+        b->bins.push_back(std::move(B));
     }
     // descriptors
     std::vector<TmaMaps> hmaps(n);
     for (uint32_t j = 0; j < n; ++j) hmaps[j] = b->jobs[j]->maps;
     if ((rc = b->d_maps.alloc(n, b->device_bytes)) || (rc = b->d_jobs.alloc(n, b->device_bytes)) ||
-        (rc = b->d_adv.alloc(n, b->device_bytes)))
+        (rc = b->d_adv.alloc(n, b->device_bytes)) || (rc = b->d_status.alloc(4 * (size_t)n, b->device_bytes)))
         return rc;
+    b->h_status.assign(4 * (size_t)n, 0);
     std::vector<BatchJob> hj(n);
     std::vector<AdvJob> ha(n);
     for (uint32_t j = 0; j < n; ++j) {
@@ -299,11 +356,16 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
         hj[j].ti = e->ti;
         hj[j].maps = b->d_maps.p + j;
         hj[j].interval = (int)e->interval;
-        ha[j].d_ts = e->d_ts.p;
+        std::memset(&ha[j], 0, sizeof(AdvJob));
+        ha[j].d_ts = e->p_ts();
         ha[j].ps = e->ps;
         ha[j].g = e->g;
         ha[j].interval = (int)e->interval;
         ha[j].energy_valid = e->energy_on_probe ? 1 : 0;
+        ha[j].ctl = e->ctl.p;
+        ha[j].out = b->d_status.p + 4 * (size_t)j;
+        CK(cudaMemcpyAsync(b->d_status.p + 4 * (size_t)j, e->ctl.p, 4 * sizeof(int), cudaMemcpyDeviceToDevice,
+                           b->stream));
     }
     CK(cudaMemcpyAsync(b->d_maps.p, hmaps.data(), n * sizeof(TmaMaps), cudaMemcpyHostToDevice, b->stream));
     CK(cudaMemcpyAsync(b->d_jobs.p, hj.data(), n * sizeof(BatchJob), cudaMemcpyHostToDevice, b->stream));
@@ -385,6 +447,7 @@ int fdtd_batch_destroy(fdtd_batch_t b) {
 
 int fdtd_batch_iterate(fdtd_batch_t b, uint32_t n) {
     if (!b) return FDTD_ERR_ARG;
+    if (n == 0) return FDTD_OK;
     CK(cudaSetDevice(b->device));
     b->last_launches = 0;
     int rc;
@@ -394,11 +457,12 @@ int fdtd_batch_iterate(fdtd_batch_t b, uint32_t n) {
     while (left > 0) {
         if (b->graph && left >= b->graph_steps) {
             CK(cudaGraphLaunch(b->graph, b->stream));
-            b->last_launches += (2 * b->groups.size() + 1) * b->graph_steps;
+            b->last_launches += (2 * b->groups.size() + b->bins.size()) * b->graph_steps;
             left -= b->graph_steps;
             continue;
         }
-        if ((rc = batch_step(b))) return rc;
+        for (size_t bi = 0; bi < b->bins.size(); ++bi)
+            if ((rc = bin_step(b, bi))) return rc;
         left -= 1;
     }
     CK(cudaEventRecord(b->ev1, b->stream));
@@ -406,11 +470,19 @@ int fdtd_batch_iterate(fdtd_batch_t b, uint32_t n) {
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
     b->last_ms = ms;
-    for (fdtd_engine_s* e : b->jobs) {
-        e->ts += n;
-        if ((rc = engine_check_errors(e))) return rc;
+    // every job's control words in one copy: numTS, done, error word
+    const size_t nj = b->jobs.size();
+    CK(cudaMemcpyAsync(b->h_status.data(), b->d_status.p, nj * 4 * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    int first_rc = FDTD_OK;
+    for (size_t j = 0; j < nj; ++j) {
+        fdtd_engine_s* e = b->jobs[j];
+        const int* c = &b->h_status[4 * j];
+        e->ts = (uint32_t)c[0];
+        e->done = c[3] != 0;
+        if (c[2] && first_rc == FDTD_OK) first_rc = engine_decode_error(c[2]);
     }
-    return FDTD_OK;
+    return first_rc;
 }
 
 int fdtd_batch_info(fdtd_batch_t b, fdtd_batch_stats* st) {
@@ -418,6 +490,7 @@ int fdtd_batch_info(fdtd_batch_t b, fdtd_batch_stats* st) {
     std::memset(st, 0, sizeof(*st));
     st->num_jobs = (uint32_t)b->jobs.size();
     st->num_groups = (uint32_t)b->groups.size();
+    st->num_bins = (uint32_t)b->bins.size();
     st->total_nodes = b->total_nodes;
     for (const Group& G : b->groups) {
         st->work_items += (uint64_t)G.nE + G.nH;

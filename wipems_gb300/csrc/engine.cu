@@ -120,7 +120,7 @@ int launch_step(fdtd_engine_s* e, int ts_off, bool energy) {
 }
 
 int launch_advance(fdtd_engine_s* e, int adv, bool sample, bool energy_valid) {
-    k_advance_sample<<<1, 256, 0, e->stream>>>(e->d_ts.p, adv, sample ? 1 : 0, e->ps, e->g, energy_valid ? 1 : 0,
+    k_advance_sample<<<1, 256, 0, e->stream>>>(e->p_ts(), adv, sample ? 1 : 0, e->ps, e->g, energy_valid ? 1 : 0,
                                                 kEps0, kMue0);
     e->last_launches += 1;
     return check_launch();
@@ -150,8 +150,11 @@ int upload_probes(fdtd_engine_s* e) {
     e->ps.row_doubles = row;
     e->ps.ring = e->ring.p;
     e->ps.cap = (int)e->cap;
-    e->ps.d_nsamp = e->d_nsamp.p;
-    e->ps.d_err = e->d_err.p;
+    e->ps.d_nsamp = e->p_nsamp();
+    e->ps.d_err = e->p_err();
+    e->ps.d_done = e->p_done();
+    e->ps.end_crit = e->end_crit;
+    e->ps.stop_ts = e->end_crit > 0 ? (int)e->stop_ts : 0;
     e->probes_uploaded = true;
     return FDTD_OK;
 }
@@ -201,10 +204,7 @@ int start(fdtd_engine_s* e) {
     return FDTD_OK;
 }
 
-int check_error_word(fdtd_engine_s* e) {
-    int err = 0;
-    CK(cudaMemcpyAsync(&err, e->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
-    CK(cudaStreamSynchronize(e->stream));
+int decode_error(int err) {
     if (err & 4) {
         set_error("a bounded device wait gave up: a TMA copy did not complete in time");
         return FDTD_ERR_TIMEOUT;
@@ -220,6 +220,16 @@ int check_error_word(fdtd_engine_s* e) {
     return FDTD_OK;
 }
 
+// Reads the control words back: numTS (which stops advancing once a device
+// end criterion is met) and the error word.
+int check_error_word(fdtd_engine_s* e) {
+    int ctl[4] = {0, 0, 0, 0};
+    CK(cudaMemcpyAsync(ctl, e->ctl.p, sizeof(ctl), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    e->ts = (uint32_t)ctl[0];
+    e->done = ctl[3] != 0;
+    return decode_error(ctl[2]);
+}
 // --------------------------------------------------------------- TMA maps
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -324,11 +334,10 @@ int reset_state(fdtd_engine_s* e) {
     const size_t F = 3 * (size_t)e->comp * sizeof(float);
     for (DevBuf<float>* b : {&e->V, &e->I, &e->FV, &e->FI, &e->AV, &e->LV, &e->AI, &e->LI})
         if (b->p) CK(cudaMemsetAsync(b->p, 0, F, s));
-    CK(cudaMemsetAsync(e->d_ts.p, 0, sizeof(int), s));
-    CK(cudaMemsetAsync(e->d_eacc.p, 0, 2 * sizeof(double), s));
-    CK(cudaMemsetAsync(e->d_nsamp.p, 0, sizeof(int), s));
-    CK(cudaMemsetAsync(e->d_err.p, 0, sizeof(int), s));
+    CK(cudaMemsetAsync(e->ctl.p, 0, 4 * sizeof(int), s));
+    CK(cudaMemsetAsync(e->d_eacc.p, 0, 4 * sizeof(double), s));
     e->ts = 0;
+    e->done = false;
     e->need_initial_sample = true;
     return FDTD_OK;
 }
@@ -382,6 +391,12 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     }
     const uint32_t maxts = (opts && opts->max_timesteps) ? opts->max_timesteps : 100000;
     e->cap = (e->interval ? maxts / e->interval : 0) + 2;
+    e->end_crit = opts ? opts->end_crit : 0.0;
+    e->stop_ts = maxts;
+    if (e->end_crit < 0 || (e->end_crit > 0 && (!e->interval || !e->energy_on_probe))) {
+        set_error("end_crit needs probe_interval > 0 and energy_on_probe (the energy is checked on sample steps)");
+        return FDTD_ERR_ARG;
+    }
     e->num_tuples_e = c->E.num_tuples;
     e->num_tuples_h = c->H.num_tuples;
     e->upml_nodes = c->upml_nodes;
@@ -405,8 +420,7 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     if ((rc = e->sigV.alloc(std::max<uint32_t>(1, c->sig_len), tot)) ||
         (rc = e->sigC.alloc(std::max<uint32_t>(1, c->sig_len), tot)))
         return rc;
-    if ((rc = e->d_ts.alloc(1, tot)) || (rc = e->d_eacc.alloc(2, tot)) || (rc = e->d_energy_tmp.alloc(2, tot)) ||
-        (rc = e->d_nsamp.alloc(1, tot)) || (rc = e->d_err.alloc(1, tot)))
+    if ((rc = e->ctl.alloc(4, tot)) || (rc = e->d_eacc.alloc(4, tot)) || (rc = e->d_energy_tmp.alloc(2, tot)))
         return rc;
     DevGrid& g = e->g;
     if ((rc = upload_half(e, c->E, e->E, g.e)) || (rc = upload_half(e, c->H, e->H, g.h))) return rc;
@@ -442,7 +456,8 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     g.sigC = e->sigC.p;
     g.sig_len = (int)c->sig_len;
     g.sig_period = (int)c->sig_period;
-    g.d_ts = e->d_ts.p;
+    g.d_ts = e->p_ts();
+    g.d_done = e->p_done();
     g.d_eacc = e->d_eacc.p;
     e->smem_direct = 2 * 3 * (size_t)(e->TY + 1) * 33 * sizeof(float);
     for (int a = 0; a < 3; ++a) {
@@ -450,7 +465,7 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
         e->ti.hi[a] = c->inner_hi[a];
         e->ti.ne[a] = (int)e->N[a] - (c->trim_e[a] ? 1 : 0);
     }
-    e->ti.d_err = e->d_err.p;
+    e->ti.d_err = e->p_err();
     if (e->use_tma) {
         if ((rc = make_maps(e))) return rc;
         const size_t need = (e->feat & FEAT_UPML) ? StageLayout<uint32_t, true>::smem(e->stages)
@@ -541,6 +556,7 @@ int probe_entries(const fdtd_engine_s* e, const fdtd_probe_desc* p, std::vector<
 
 int engine_start(fdtd_engine_s* e) { return start(e); }
 int engine_check_errors(fdtd_engine_s* e) { return check_error_word(e); }
+int engine_decode_error(int err) { return decode_error(err); }
 
 }  // namespace wipems
 
@@ -645,6 +661,12 @@ int fdtd_engine_iterate(fdtd_engine_t e, uint32_t n) {
     return check_error_word(e);
 }
 
+int fdtd_engine_done(fdtd_engine_t e, int* done) {
+    if (!e || !done) return FDTD_ERR_ARG;
+    *done = e->done ? 1 : 0;
+    return FDTD_OK;
+}
+
 int fdtd_engine_num_timesteps(fdtd_engine_t e, uint32_t* ts) {
     if (!e || !ts) return FDTD_ERR_ARG;
     *ts = e->ts;
@@ -659,7 +681,7 @@ int fdtd_engine_num_samples(fdtd_engine_t e, uint32_t* n) {
     }
     CK(cudaSetDevice(e->device));
     int v = 0;
-    CK(cudaMemcpyAsync(&v, e->d_nsamp.p, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaMemcpyAsync(&v, e->p_nsamp(), sizeof(int), cudaMemcpyDeviceToHost, e->stream));
     CK(cudaStreamSynchronize(e->stream));
     *n = (uint32_t)v;
     return FDTD_OK;

@@ -67,8 +67,14 @@ struct fdtd_engine_s {
     DevHalfBufs E, H;
     DevBuf<float> geo;
     DevBuf<float> sigV, sigC;
-    DevBuf<int> d_ts;
-    DevBuf<double> d_eacc;
+    // control words, one allocation so a single copy reads them all:
+    // [0] numTS, [1] samples recorded, [2] error word, [3] done flag
+    DevBuf<int> ctl;
+    int* p_ts() const { return ctl.p; }
+    int* p_nsamp() const { return ctl.p + 1; }
+    int* p_err() const { return ctl.p + 2; }
+    int* p_done() const { return ctl.p + 3; }
+    DevBuf<double> d_eacc;  // {sum V^2, sum I^2, running energy maximum}
     DevBuf<double> d_energy_tmp;
     // probes
     std::vector<ProbeEntry> h_entries;
@@ -78,13 +84,14 @@ struct fdtd_engine_s {
     DevBuf<int> d_first;
     DevBuf<double> d_weight;
     DevBuf<double> ring;
-    DevBuf<int> d_nsamp;
-    DevBuf<int> d_err;
     ProbeSet ps{};
     bool probes_uploaded = false;
     uint32_t interval = 0;
     bool energy_on_probe = true;
     bool use_graphs = true;
+    double end_crit = 0;     // > 0: stop on the device (energy decay or stop_ts)
+    uint32_t stop_ts = 0;
+    bool done = false;       // as of the last control-word read
     uint32_t cap = 0;
     // state
     uint32_t ts = 0;
@@ -118,5 +125,6 @@ struct fdtd_engine_s {
 namespace wipems {
 // engine.cu helpers used by the batched path
 int engine_start(fdtd_engine_s* e);        // upload probes, graph, ts = 0 sample
-int engine_check_errors(fdtd_engine_s* e); // read and decode the error word
+int engine_check_errors(fdtd_engine_s* e); // read the control words, decode errors
+int engine_decode_error(int err);          // error word -> status code + message
 }  // namespace wipems

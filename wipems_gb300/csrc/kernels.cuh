@@ -17,6 +17,7 @@ namespace wipems {
 // y-1 halo, column 0 the z-1 halo.
 template <typename IdxT, int FEAT, bool GEO>
 __global__ void __launch_bounds__(256) k_volt(const DevGrid g, int ts_off, int XC) {
+    if (*g.d_done) return;
     extern __shared__ float smem[];
     const int TY = blockDim.y;
     const int tz = threadIdx.x, ty = threadIdx.y;
@@ -95,6 +96,7 @@ __global__ void __launch_bounds__(256) k_volt(const DevGrid g, int ts_off, int X
 // the z+1 halo).
 template <typename IdxT, int FEAT, bool GEO, bool ENERGY>
 __global__ void __launch_bounds__(256) k_curr(const DevGrid g, int ts_off, int XC) {
+    if (*g.d_done) return;
     extern __shared__ float smem[];
     const int TY = blockDim.y;
     const int tz = threadIdx.x, ty = threadIdx.y;
@@ -210,19 +212,32 @@ struct ProbeSet {
     int cap;
     int* d_nsamp;               // samples written
     int* d_err;                 // error word (ring overflow, non-finite)
+    int* d_done;                // end criterion met (0 / 1)
+    double end_crit;            // > 0: stop once energy <= end_crit * max energy
+    int stop_ts;                // > 0 (with end_crit): stop at this numTS
 };
 
 // Advances numTS by adv (Engine::IterateTS ++numTS) and, when sample is set,
 // records one probe/energy sample row (ProcessIntegral::Process): the probe
 // sums (ProcessVoltage / ProcessCurrent) as warp reductions in double.
+// With an end criterion the job stops here, on the device, the way
+// openEMS::RunFDTD's loop ends (openems.cpp:1285-1314): at the first sample
+// whose energy is <= end_crit times the largest energy seen so far, or at
+// stop_ts timesteps; a stopped job's kernels and samplers do nothing.
 __device__ __forceinline__ void advance_sample(int* d_ts, int adv, int sample, const ProbeSet& ps, const DevGrid& g,
                                                int energy_valid, double eps0, double mue0) {
-    __shared__ int s_ts, s_row;
+    __shared__ int s_ts, s_row, s_done;
+    if (threadIdx.x == 0) {
+        s_row = -1;
+        s_done = *ps.d_done;
+    }
+    __syncthreads();
+    if (s_done) return;
     if (threadIdx.x == 0) {
         int ts = *d_ts + adv;
         if (adv) *d_ts = ts;
         s_ts = ts;
-        s_row = -1;
+        if (ps.end_crit > 0.0 && ps.stop_ts > 0 && ts >= ps.stop_ts) *ps.d_done = 1;
         if (sample) {
             int row = *ps.d_nsamp;
             if (row < ps.cap) {
@@ -256,6 +271,11 @@ __device__ __forceinline__ void advance_sample(int* d_ts, int adv, int sample, c
             double e = eps0 * g.d_eacc[0] + mue0 * g.d_eacc[1];
             if (!isfinite(e)) atomicOr(ps.d_err, 2);
             rec[1] = e;
+            if (ps.end_crit > 0.0) {
+                const double m = fmax(g.d_eacc[2], e);
+                g.d_eacc[2] = m;
+                if (m > 0.0 && e / m <= ps.end_crit) *ps.d_done = 1;
+            }
         } else {
             rec[1] = -1.0;
         }

@@ -429,6 +429,7 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_volt_tma(const DevGrid g, const
     extern __shared__ __align__(128) float smem_raw[];
     float* smem = aligned_smem(smem_raw);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * STAGES);
+    if (*g.d_done) return;
     init_ring(bars, STAGES);
     uint32_t ring = 0;
     volt_tile<IdxT, FEAT, GEO>(g, m, ti, blockIdx.x, blockIdx.y, blockIdx.z, XC, STAGES, smem, bars, ring,
@@ -442,6 +443,7 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_curr_tma(const DevGrid g, const
     extern __shared__ __align__(128) float smem_raw[];
     float* smem = aligned_smem(smem_raw);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * STAGES);
+    if (*g.d_done) return;
     init_ring(bars, STAGES);
     uint32_t ring = 0;
     float es = 0.f, ec = 0.f, hs = 0.f, hc = 0.f;
@@ -483,6 +485,7 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_volt_batch(const BatchJob* __re
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const WorkItem w = items[it];
         const BatchJob& J = jobs[w.job];
+        if (*J.g.d_done) continue;  // the job met its end criterion
         if (w.job != last_job) {
             if (threadIdx.x == 0 && threadIdx.y == 0) tensormap_acquire(J.maps);
             last_job = w.job;
@@ -507,6 +510,7 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_curr_batch(const BatchJob* __re
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const WorkItem w = items[it];
         const BatchJob& J = jobs[w.job];
+        if (*J.g.d_done) continue;
         if (w.job != last_job) {
             if (threadIdx.x == 0 && threadIdx.y == 0) tensormap_acquire(J.maps);
             last_job = w.job;

@@ -60,7 +60,8 @@ struct DevGrid {
     int sig_len;
     int sig_period;      // 0 = none
     const int* d_ts;     // timestep counter (numTS)
-    double* d_eacc;      // energy accumulators {sum V^2, sum I^2}
+    const int* d_done;   // set once the job met its end criterion: kernels skip
+    double* d_eacc;      // {sum V^2, sum I^2, running energy maximum}
 };
 
 template <typename IdxT>

@@ -257,7 +257,7 @@ class Engine:
 
     def __init__(self, op, device: int = 0, max_timesteps: int = 0, probe_interval: int | None = None,
                  use_graphs: bool = True, energy_on_probe: bool = True, tile_y: int = 0, x_chunk: int = 0,
-                 probes: bool = True, kernel: str = "tma", stages: int = 0):
+                 probes: bool = True, kernel: str = "tma", stages: int = 0, end_crit: float = 0.0):
         cop = op if isinstance(op, CompressedOperator) else None
         if cop is not None:
             op = cop.op
@@ -274,6 +274,7 @@ class Engine:
             raise ValueError("kernel must be 'tma' or 'direct'")
         o.kernel = 0 if kernel == "tma" else 1
         o.stages = int(stages)
+        o.end_crit = float(end_crit)
         h = C.c_void_p()
         if cop is not None:
             check(lib().fdtd_engine_create_compressed(cop._h, C.byref(o), C.byref(h)), "fdtd_engine_create_compressed")
@@ -304,6 +305,13 @@ class Engine:
 
     def iterate(self, n: int):
         check(lib().fdtd_engine_iterate(self._h, int(n)), "fdtd_engine_iterate")
+
+    @property
+    def done(self) -> bool:
+        """True once the device end criterion (end_crit) stopped the job."""
+        v = C.c_int()
+        check(lib().fdtd_engine_done(self._h, C.byref(v)), "fdtd_engine_done")
+        return bool(v.value)
 
     @property
     def num_timesteps(self) -> int:
@@ -390,10 +398,11 @@ class Batch:
     kernel per half-step and kernel variant (see fdtd_batch_create).  The
     engines must outlive the batch."""
 
-    def __init__(self, engines, x_chunk: int = 0, stages: int = 0, blocks_per_sm: int = 0, graph_steps: int = 0):
+    def __init__(self, engines, x_chunk: int = 0, stages: int = 0, blocks_per_sm: int = 0, graph_steps: int = 0,
+                 bin_mib: int = 0):
         self.engines = list(engines)
         arr = (C.c_void_p * len(self.engines))(*[e._h.value for e in self.engines])
-        o = _abi.FdtdBatchOpts(int(x_chunk), int(stages), int(blocks_per_sm), int(graph_steps))
+        o = _abi.FdtdBatchOpts(int(x_chunk), int(stages), int(blocks_per_sm), int(graph_steps), int(bin_mib))
         h = C.c_void_p()
         check(lib().fdtd_batch_create(arr, len(self.engines), C.byref(o), C.byref(h)), "fdtd_batch_create")
         self._h = h
