@@ -408,6 +408,85 @@ int fdtd_batch_iterate(fdtd_batch_t batch, uint32_t n_steps);
 int fdtd_batch_info(fdtd_batch_t batch, fdtd_batch_stats* stats);
 int fdtd_batch_destroy(fdtd_batch_t batch);
 
+/* ------------------------------------------------------------------ server */
+
+/* Continuous-batching job server (no counterpart in the reference, which
+ * runs one simulation per openEMS process).  Scenes are submitted at any
+ * time; host worker threads build and compress their operators while the
+ * GPU runs; one GPU thread retires jobs whose device end criterion fired,
+ * admits built jobs while their device footprint fits the HBM budget, and
+ * advances all resident jobs together in batched rounds (fdtd_batch_*).
+ * A job stops at the same timestep, with the same samples and fields, as
+ * it would alone.  All functions are thread-safe. */
+typedef struct fdtd_server_s* fdtd_server_t;
+
+enum {
+    FDTD_JOB_QUEUED = 0,    /* waiting for a build worker */
+    FDTD_JOB_BUILDING = 1,  /* operator build + compression on the host */
+    FDTD_JOB_READY = 2,     /* built, waiting for device memory / a slot */
+    FDTD_JOB_RUNNING = 3,   /* resident in HBM, advancing in the batch */
+    FDTD_JOB_DONE = 4,      /* results on the host */
+    FDTD_JOB_FAILED = 5
+};
+
+typedef struct {
+    int      device;
+    uint64_t hbm_budget;          /* bytes resident jobs may hold (0 = 90 % of free) */
+    uint32_t max_active;          /* cap on resident jobs (0 = 256) */
+    uint32_t round_steps;         /* timesteps per scheduling round (0 = 128) */
+    int      build_workers;       /* concurrent operator builds (0 = auto) */
+    int      build_threads_per_job; /* threads per operator build (0 = auto) */
+    fdtd_batch_opts batch;        /* tiling of the batched kernels */
+} fdtd_server_opts;
+
+typedef struct {
+    double   end_crit;        /* energy decay stop, e.g. 1e-4 = -40 dB (0 = off) */
+    uint32_t max_timesteps;   /* timestep cap (0 = the scene's NrTS) */
+    uint32_t probe_interval;  /* 0 = the operator's Nyquist-derived interval */
+    int      keep_fields;     /* copy the final fields to the host at retirement */
+} fdtd_job_opts;
+
+typedef struct {
+    int      state;           /* FDTD_JOB_* */
+    int      error;           /* status code of a failed job (message via fdtd_last_error) */
+    uint32_t timesteps;       /* numTS at retirement */
+    uint32_t num_samples, num_probes, probe_interval;
+    uint64_t nodes;           /* lines product */
+    uint32_t num_lines[3];
+    double   dT;              /* timestep (s) */
+    uint64_t footprint;       /* device bytes reserved while resident */
+    double   t_submit, t_built, t_admit, t_done;  /* s since fdtd_server_create */
+} fdtd_job_status;
+
+typedef struct {
+    uint64_t jobs_submitted, jobs_admitted, jobs_done, jobs_failed;
+    uint64_t rounds, rebuilds, kernel_launches;
+    double   node_steps;      /* sum over finished jobs of nodes x timesteps */
+    double   gpu_ms;          /* device time of all rounds (CUDA events) */
+    uint64_t budget_bytes, used_bytes, peak_bytes;
+    uint32_t active_jobs;
+    int      last_error;
+    double   elapsed_s;
+} fdtd_server_stats;
+
+int fdtd_server_create(const fdtd_server_opts* opts, fdtd_server_t* out);
+/* Takes ownership of scene (do not destroy it afterwards). */
+int fdtd_server_submit(fdtd_server_t srv, fdtd_scene_t scene, const fdtd_job_opts* opts,
+                       uint64_t* job_id);
+int fdtd_server_job_status(fdtd_server_t srv, uint64_t job_id, fdtd_job_status* st);
+/* Blocks until the job (job_id = 0: every submitted job) is done or failed;
+ * timeout_s <= 0 waits without limit. */
+int fdtd_server_wait(fdtd_server_t srv, uint64_t job_id, double timeout_s);
+/* Samples of a finished job: num_samples rows (see fdtd_job_status). */
+int fdtd_server_read_samples(fdtd_server_t srv, uint64_t job_id, uint32_t* ts, double* vals,
+                             double* energy);
+int fdtd_server_get_fields(fdtd_server_t srv, uint64_t job_id, float* volt, float* curr);
+/* Drops a finished job's host results. */
+int fdtd_server_release(fdtd_server_t srv, uint64_t job_id);
+int fdtd_server_get_stats(fdtd_server_t srv, fdtd_server_stats* st);
+/* Stops the threads; queued and running jobs are abandoned. */
+int fdtd_server_destroy(fdtd_server_t srv);
+
 /* ---------------------------------------------------- allocation-free path */
 
 /* Energy eps0*sum(V^2) + mu0*sum(I^2) over x < Nx-1, y < Ny-1, z < Nz-1 of

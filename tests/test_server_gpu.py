@@ -1,0 +1,89 @@
+"""Continuous-batching server: every job's result (stopping timestep,
+probe samples, final fields) is the same as when the job runs alone on the
+plain engine with the same end criterion, whatever else shares the GPU."""
+import numpy as np
+import pytest
+
+from wipems_gb300 import Engine, Operator, Server, scenes
+
+pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("libs")]
+
+KINDS = ["upml", "drude", "lorentz", "graded", "mixed", "pec"]
+NR_TS, CRIT = 700, 1e-3
+
+
+def _alone(kind, seed):
+    op = Operator(scenes.mini(kind, seed=seed, nr_ts=NR_TS))
+    e = Engine(op, end_crit=CRIT)
+    e.iterate(NR_TS)
+    return e
+
+
+def _same(e, srv, jid):
+    st = srv.status(jid)
+    assert st["state"] == "done", st
+    assert st["timesteps"] == e.num_timesteps
+    a, b = e.samples(), srv.samples(jid)
+    assert np.array_equal(a.ts, b.ts)
+    assert np.array_equal(a.values, b.values)
+    ok = a.energy > 0
+    assert np.allclose(b.energy[ok], a.energy[ok], rtol=1e-6, atol=0)
+    Va, Ia = e.fields()
+    Vb, Ib = srv.fields(jid)
+    assert np.array_equal(Va.view(np.uint32), Vb.view(np.uint32))
+    assert np.array_equal(Ia.view(np.uint32), Ib.view(np.uint32))
+
+
+@pytest.mark.parametrize("round_steps,bin_mib", [(64, 0), (37, 1)])
+def test_server_results_same_as_alone(round_steps, bin_mib):
+    srv = Server(round_steps=round_steps, bin_mib=bin_mib, build_workers=2)
+    ids = {}
+    for seed in (3, 4):
+        for k in KINDS:
+            ids[(k, seed)] = srv.submit(scenes.mini(k, seed=seed, nr_ts=NR_TS), end_crit=CRIT, keep_fields=True)
+    srv.wait(0, timeout=600)
+    st = srv.stats()
+    assert st["jobs_done"] == len(ids) and st["jobs_failed"] == 0
+    for (k, seed), jid in ids.items():
+        _same(_alone(k, seed), srv, jid)
+    srv.close()
+
+
+def test_server_admission_by_footprint():
+    """A budget that holds about two jobs at a time: every job still runs,
+    the resident footprint never exceeds the budget, and results match."""
+    probe = Server(max_active=1)
+    j = probe.submit(scenes.mini("upml", seed=3, nr_ts=NR_TS), end_crit=CRIT)
+    probe.wait(j, timeout=300)
+    foot = probe.status(j)["footprint"]
+    probe.close()
+    budget = int(2.5 * foot)
+    srv = Server(hbm_budget=budget, round_steps=50)
+    ids = [srv.submit(scenes.mini("upml", seed=s, nr_ts=NR_TS), end_crit=CRIT, keep_fields=True) for s in range(3, 9)]
+    srv.wait(0, timeout=600)
+    st = srv.stats()
+    assert st["jobs_done"] == len(ids)
+    assert st["peak_bytes"] <= budget
+    assert st["rebuilds"] >= 3            # jobs entered as earlier ones retired
+    t_admit = sorted(srv.status(i)["t_admit"] for i in ids)
+    t_done = sorted(srv.status(i)["t_done"] for i in ids)
+    assert t_admit[-1] >= t_done[0]       # the last admissions waited for retirements
+    for s, jid in zip(range(3, 9), ids):
+        _same(_alone("upml", s), srv, jid)
+    srv.close()
+
+
+def test_server_rejects_oversized_job_and_keeps_serving():
+    """A job whose footprint exceeds the whole budget fails cleanly; the
+    server keeps serving jobs that fit."""
+    srv = Server(hbm_budget=8 << 20)
+    big = srv.submit(scenes.mini("upml", seed=3, nr_ts=NR_TS), end_crit=CRIT)
+    srv.wait(big, timeout=300)
+    st = srv.status(big)
+    assert st["state"] == "failed" and "budget" in st["message"]
+    srv.close()
+    srv = Server(hbm_budget=1 << 30)
+    ok = srv.submit(scenes.mini("pec", seed=3, nr_ts=200), end_crit=CRIT)
+    srv.wait(ok, timeout=300)
+    assert srv.status(ok)["state"] == "done"
+    srv.close()

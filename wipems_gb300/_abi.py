@@ -80,6 +80,30 @@ class FdtdBatchOpts(C.Structure):
                 ("bin_mib", C.c_int)]
 
 
+class FdtdServerOpts(C.Structure):
+    _fields_ = [("device", C.c_int), ("hbm_budget", C.c_uint64), ("max_active", u32), ("round_steps", u32),
+                ("build_workers", C.c_int), ("build_threads_per_job", C.c_int), ("batch", FdtdBatchOpts)]
+
+
+class FdtdJobOpts(C.Structure):
+    _fields_ = [("end_crit", C.c_double), ("max_timesteps", u32), ("probe_interval", u32), ("keep_fields", C.c_int)]
+
+
+class FdtdJobStatus(C.Structure):
+    _fields_ = [("state", C.c_int), ("error", C.c_int), ("timesteps", u32), ("num_samples", u32),
+                ("num_probes", u32), ("probe_interval", u32), ("nodes", C.c_uint64), ("num_lines", u32 * 3),
+                ("dT", C.c_double), ("footprint", C.c_uint64), ("t_submit", C.c_double), ("t_built", C.c_double),
+                ("t_admit", C.c_double), ("t_done", C.c_double)]
+
+
+class FdtdServerStats(C.Structure):
+    _fields_ = [("jobs_submitted", C.c_uint64), ("jobs_admitted", C.c_uint64), ("jobs_done", C.c_uint64),
+                ("jobs_failed", C.c_uint64), ("rounds", C.c_uint64), ("rebuilds", C.c_uint64),
+                ("kernel_launches", C.c_uint64), ("node_steps", C.c_double), ("gpu_ms", C.c_double),
+                ("budget_bytes", C.c_uint64), ("used_bytes", C.c_uint64), ("peak_bytes", C.c_uint64),
+                ("active_jobs", u32), ("last_error", C.c_int), ("elapsed_s", C.c_double)]
+
+
 class FdtdBatchStats(C.Structure):
     _fields_ = [("num_jobs", u32), ("num_groups", u32), ("num_bins", u32), ("total_nodes", C.c_uint64), ("work_items", C.c_uint64),
                 ("persistent_blocks", u32), ("device_bytes", C.c_uint64), ("last_ms", C.c_double),
@@ -144,6 +168,15 @@ SIGNATURES = [
     ("fdtd_batch_iterate", C.c_int, [_P, u32]),
     ("fdtd_batch_info", C.c_int, [_P, C.POINTER(FdtdBatchStats)]),
     ("fdtd_batch_destroy", C.c_int, [_P]),
+    ("fdtd_server_create", C.c_int, [C.POINTER(FdtdServerOpts), C.POINTER(_P)]),
+    ("fdtd_server_submit", C.c_int, [_P, _P, C.POINTER(FdtdJobOpts), C.POINTER(C.c_uint64)]),
+    ("fdtd_server_job_status", C.c_int, [_P, C.c_uint64, C.POINTER(FdtdJobStatus)]),
+    ("fdtd_server_wait", C.c_int, [_P, C.c_uint64, C.c_double]),
+    ("fdtd_server_read_samples", C.c_int, [_P, C.c_uint64, PU32, PD, PD]),
+    ("fdtd_server_get_fields", C.c_int, [_P, C.c_uint64, PF, PF]),
+    ("fdtd_server_release", C.c_int, [_P, C.c_uint64]),
+    ("fdtd_server_get_stats", C.c_int, [_P, C.POINTER(FdtdServerStats)]),
+    ("fdtd_server_destroy", C.c_int, [_P]),
 ]
 
 

@@ -116,4 +116,5 @@ struct fdtd_operator_s {
 
 namespace wipems {
 void set_error(const std::string& msg);
+const std::string& last_error();  // this thread's last error message
 }

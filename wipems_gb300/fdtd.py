@@ -427,6 +427,98 @@ class Batch:
             pass
 
 
+JOB_STATES = ("queued", "building", "ready", "running", "done", "failed")
+
+
+class Server:
+    """Continuous-batching job server (fdtd_server_*): submit scenes at any
+    time; operators are built on host worker threads, jobs are admitted by
+    device footprint, advanced together in batched rounds and retired on
+    their own end criterion."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0, max_active: int = 0, round_steps: int = 0,
+                 build_workers: int = 0, build_threads_per_job: int = 0, x_chunk: int = 0, stages: int = 0,
+                 blocks_per_sm: int = 0, graph_steps: int = 0, bin_mib: int = 0):
+        o = _abi.FdtdServerOpts()
+        o.device = device
+        o.hbm_budget = int(hbm_budget)
+        o.max_active = int(max_active)
+        o.round_steps = int(round_steps)
+        o.build_workers = int(build_workers)
+        o.build_threads_per_job = int(build_threads_per_job)
+        o.batch = _abi.FdtdBatchOpts(int(x_chunk), int(stages), int(blocks_per_sm), int(graph_steps), int(bin_mib))
+        h = C.c_void_p()
+        check(lib().fdtd_server_create(C.byref(o), C.byref(h)), "fdtd_server_create")
+        self._h = h
+        self._probe_types: dict[int, list] = {}
+
+    def submit(self, scene: Scene, end_crit: float = 0.0, max_timesteps: int = 0, probe_interval: int = 0,
+               keep_fields: bool = False) -> int:
+        """Queues the scene (the server takes it over: the Scene object is
+        spent afterwards) and returns the job id."""
+        o = _abi.FdtdJobOpts(float(end_crit), int(max_timesteps), int(probe_interval), int(keep_fields))
+        jid = C.c_uint64()
+        check(lib().fdtd_server_submit(self._h, scene._h, C.byref(o), C.byref(jid)), "fdtd_server_submit")
+        scene._h = None
+        self._probe_types[jid.value] = [p["type"] for p in scene.probes]
+        return jid.value
+
+    def status(self, job: int) -> dict:
+        st = _abi.FdtdJobStatus()
+        check(lib().fdtd_server_job_status(self._h, int(job), C.byref(st)), "fdtd_server_job_status")
+        d = {k: getattr(st, k) for k, _ in st._fields_}
+        d["num_lines"] = tuple(st.num_lines)
+        d["state"] = JOB_STATES[st.state]
+        if st.state == 5:
+            d["message"] = _abi.last_error()
+        return d
+
+    def wait(self, job: int = 0, timeout: float = 0.0):
+        """Blocks until the job (0: every submitted job) has finished."""
+        check(lib().fdtd_server_wait(self._h, int(job), float(timeout)), "fdtd_server_wait")
+
+    def samples(self, job: int) -> Samples:
+        st = self.status(job)
+        n, npr = st["num_samples"], st["num_probes"]
+        ts = np.zeros(n, np.uint32)
+        vals = np.zeros((n, max(npr, 1)), np.float64)
+        en = np.zeros(n, np.float64)
+        check(lib().fdtd_server_read_samples(self._h, int(job), ts.ctypes.data_as(_abi.PU32),
+                                             vals.ctypes.data_as(_abi.PD), en.ctypes.data_as(_abi.PD)),
+              "fdtd_server_read_samples")
+        types = self._probe_types.get(job, [0] * npr)
+        return Samples(ts=ts.astype(np.int64), values=vals[:, :npr], energy=en, dT=st["dT"],
+                       probe_types=list(types))
+
+    def fields(self, job: int):
+        shape = (3,) + self.status(job)["num_lines"]
+        V = np.empty(shape, np.float32)
+        I = np.empty(shape, np.float32)
+        check(lib().fdtd_server_get_fields(self._h, int(job), V.ctypes.data_as(_abi.PF), I.ctypes.data_as(_abi.PF)),
+              "fdtd_server_get_fields")
+        return V, I
+
+    def release(self, job: int):
+        check(lib().fdtd_server_release(self._h, int(job)), "fdtd_server_release")
+        self._probe_types.pop(job, None)
+
+    def stats(self) -> dict:
+        st = _abi.FdtdServerStats()
+        check(lib().fdtd_server_get_stats(self._h, C.byref(st)), "fdtd_server_get_stats")
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fdtd_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def run_fdtd(engine: Engine, nr_ts: int, end_crit: float = 1e-6) -> dict:
     """openEMS::RunFDTD's loop: iterate in probe-interval chunks until NrTS
     or until the energy has decayed below end_crit relative to its maximum
