@@ -230,6 +230,27 @@ struct BoxIndex {
             default: return l[i] - g.raw_delta(a, (int)i - 1) * 0.25;
         }
     }
+    // index range [lo, hi] of axis a in which some box matches some sample
+    // kind (lookup returns -1 outside it); false when there is none
+    bool span(int a, uint32_t& lo, uint32_t& hi) const {
+        bool any = false;
+        lo = 0;
+        hi = 0;
+        if (prim.empty()) return false;
+        for (int k = 0; k < SK_COUNT; ++k) {
+            const std::vector<uint64_t>& m = masks[a][k];
+            const size_t n = m.size() / (size_t)W;
+            for (size_t i = 0; i < n; ++i) {
+                bool hit = false;
+                for (int w = 0; w < W; ++w) hit |= m[i * W + w] != 0;
+                if (!hit) continue;
+                if (!any || i < lo) lo = (uint32_t)i;
+                if (!any || i > hi) hi = (uint32_t)i;
+                any = true;
+            }
+        }
+        return any;
+    }
     // winner for (kind,index) per axis; -1 = none
     int lookup(const int kind[3], const uint32_t idx[3]) const {
         if (prim.empty()) return -1;
@@ -468,10 +489,12 @@ struct Builder {
         parallel_for(N[0], threads, [&](uint32_t x, int t) {
             uint32_t pos[3] = {x, 0, 0};
             double dT_loc = best[t];
+            // (the minimum does not depend on the visiting order; z innermost
+            // follows the memory layout)
             for (int n = 0; n < 3; ++n) {
                 int nP = (n + 1) % 3, nPP = (n + 2) % 3;
-                for (pos[2] = 0; pos[2] < N[2]; ++pos[2])
-                    for (pos[1] = 0; pos[1] < N[1]; ++pos[1]) {
+                for (pos[1] = 0; pos[1] < N[1]; ++pos[1])
+                    for (pos[2] = 0; pos[2] < N[2]; ++pos[2]) {
                         int s0[3] = {0, 0, 0};
                         int sP1[3] = {0, 0, 0}; sP1[nP] = 1;
                         int sPP1[3] = {0, 0, 0}; sPP1[nPP] = 1;
@@ -795,11 +818,17 @@ static int build_operator(const fdtd_scene_s& S, int threads, fdtd_operator_s& o
     const double dT = B.dT;
 
     // ---- extension 1: excitation (operator_ext_excitation.cpp:101-285)
-    {
+    // (only the index box in which some excitation primitive can match is
+    // visited, in the reference's z, y, x order: the lookups outside it
+    // return no primitive)
+    uint32_t elo[3], ehi[3];
+    const bool any_exc = B.exc_idx.span(0, elo[0], ehi[0]) && B.exc_idx.span(1, elo[1], ehi[1]) &&
+                         B.exc_idx.span(2, elo[2], ehi[2]);
+    if (any_exc) {
         uint32_t pos[3];
-        for (pos[2] = 0; pos[2] < N[2]; ++pos[2])
-            for (pos[1] = 0; pos[1] < N[1]; ++pos[1])
-                for (pos[0] = 0; pos[0] < N[0]; ++pos[0]) {
+        for (pos[2] = elo[2]; pos[2] <= ehi[2]; ++pos[2])
+            for (pos[1] = elo[1]; pos[1] <= ehi[1]; ++pos[1])
+                for (pos[0] = elo[0]; pos[0] <= ehi[0]; ++pos[0]) {
                     double c[3];
                     for (int n = 0; n < 3; ++n) {
                         if (!g.yee_coords(n, pos, c, false)) continue;
@@ -857,12 +886,12 @@ static int build_operator(const fdtd_scene_s& S, int threads, fdtd_operator_s& o
         for (int n = 0; n < 3; ++n) { slab.start[n] = u.start[n]; slab.num_lines[n] = u.nl[n]; }
         slab.vv.assign(3 * nloc, 0.f); slab.vvfo.assign(3 * nloc, 0.f); slab.vvfn.assign(3 * nloc, 0.f);
         slab.ii.assign(3 * nloc, 0.f); slab.iifo.assign(3 * nloc, 0.f); slab.iifn.assign(3 * nloc, 0.f);
-        parallel_for(u.nl[0], threads, [&](uint32_t lx, int) {
-            uint32_t loc[3] = {lx, 0, 0};
+        parallel_for(u.nl[0] * u.nl[1], threads, [&](uint32_t lxy, int) {
+            uint32_t loc[3] = {lxy / u.nl[1], lxy % u.nl[1], 0};
             uint32_t pos[3];
             double kv[3] = {0, 0, 0}, ki[3] = {0, 0, 0}, eff[4];
             pos[0] = loc[0] + u.start[0];
-            for (loc[1] = 0; loc[1] < u.nl[1]; ++loc[1]) {
+            {
                 pos[1] = loc[1] + u.start[1];
                 for (loc[2] = 0; loc[2] < u.nl[2]; ++loc[2]) {
                     pos[2] = loc[2] + u.start[2];
