@@ -9,7 +9,8 @@
 // to its device arrays, so per-job calls (read_samples, get_fields, reset)
 // keep working between batch iterations.  Jobs of different kernel variants
 // (uint16 / uint32 tuple index, UPML / ADE features, factorized geometry)
-// form separate groups, each with its own persistent kernels.
+// form separate groups, each with its own persistent kernels; the groups of
+// one half-step run concurrently.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -40,13 +41,9 @@ struct AdvJob {
 // taken on the device, so the step sequence can be replayed as a graph).
 __global__ void k_batch_advance(const AdvJob* __restrict__ jobs, double eps0, double mue0) {
     const AdvJob& J = jobs[blockIdx.x];
-    __shared__ int s_sample;
-    if (threadIdx.x == 0) {
-        const int ts = *J.d_ts + 1;
-        s_sample = (J.interval > 0 && (ts % J.interval) == 0) ? 1 : 0;
-    }
-    __syncthreads();
-    advance_sample(J.d_ts, 1, s_sample, J.ps, J.g, J.energy_valid, eps0, mue0);
+    const int ts = *J.d_ts + 1;
+    const int sample = (J.interval > 0 && (ts % J.interval) == 0) ? 1 : 0;
+    advance_sample(J.d_ts, 1, sample, J.ps, J.g, J.energy_valid, eps0, mue0, threadIdx.x, blockDim.x);
     __syncthreads();
     if (threadIdx.x < 4) J.out[threadIdx.x] = J.ctl[threadIdx.x];
 }
@@ -203,13 +200,17 @@ struct fdtd_batch_s {
 namespace wipems {
 namespace {
 
-// one timestep of the jobs of bin k
+// one timestep of the jobs of bin k: the voltage kernels of the bin's
+// groups, their current kernels, then the bin's samplers.  (Running the
+// groups of a half-step concurrently on side streams was measured slower:
+// each persistent grid already fills the GPU.)
 int bin_step(fdtd_batch_s* b, size_t k) {
     const fdtd_batch_s::Bin& B = b->bins[k];
+    const size_t ng = B.groups.size();
     for (int gi : B.groups) launch_group_volt(b->groups[gi], b->d_jobs.p, b->XC, b->stages, b->stream);
     for (int gi : B.groups) launch_group_curr(b->groups[gi], b->d_jobs.p, b->XC, b->stages, b->stream);
     k_batch_advance<<<(unsigned)B.count, 256, 0, b->stream>>>(b->d_adv.p + B.first, kEps0, kMue0);
-    b->last_launches += 2 * B.groups.size() + 1;
+    b->last_launches += 2 * ng + 1;
     const cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) {
         set_error(std::string("batch kernel launch: ") + cudaGetErrorString(err));

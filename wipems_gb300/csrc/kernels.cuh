@@ -224,16 +224,18 @@ struct ProbeSet {
 // openEMS::RunFDTD's loop ends (openems.cpp:1285-1314): at the first sample
 // whose energy is <= end_crit times the largest energy seen so far, or at
 // stop_ts timesteps; a stopped job's kernels and samplers do nothing.
+// tid / nthr: the calling thread's linear index in the block and the
+// block's thread count (a multiple of 32); every thread of the block calls.
 __device__ __forceinline__ void advance_sample(int* d_ts, int adv, int sample, const ProbeSet& ps, const DevGrid& g,
-                                               int energy_valid, double eps0, double mue0) {
+                                               int energy_valid, double eps0, double mue0, int tid, int nthr) {
     __shared__ int s_ts, s_row, s_done;
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
         s_row = -1;
         s_done = *ps.d_done;
     }
     __syncthreads();
     if (s_done) return;
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
         int ts = *d_ts + adv;
         if (adv) *d_ts = ts;
         s_ts = ts;
@@ -251,8 +253,8 @@ __device__ __forceinline__ void advance_sample(int* d_ts, int adv, int sample, c
     __syncthreads();
     if (!sample || s_row < 0) return;
     double* rec = ps.ring + (long long)s_row * ps.row_doubles;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int nwarps = blockDim.x >> 5;
+    const int warp = tid >> 5, lane = tid & 31;
+    const int nwarps = nthr >> 5;
     for (int p = warp; p < ps.nprobe; p += nwarps) {
         double acc = 0.0;
         for (int e = ps.first[p] + lane; e < ps.first[p + 1]; e += 32) {
@@ -265,7 +267,7 @@ __device__ __forceinline__ void advance_sample(int* d_ts, int adv, int sample, c
         for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
         if (lane == 0) rec[2 + p] = acc * ps.weight[p];
     }
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
         rec[0] = (double)s_ts;
         if (energy_valid) {
             double e = eps0 * g.d_eacc[0] + mue0 * g.d_eacc[1];
@@ -286,7 +288,7 @@ __device__ __forceinline__ void advance_sample(int* d_ts, int adv, int sample, c
 
 static __global__ void k_advance_sample(int* d_ts, int adv, int sample, ProbeSet ps, const DevGrid g, int energy_valid,
                                         double eps0, double mue0) {
-    advance_sample(d_ts, adv, sample, ps, g, energy_valid, eps0, mue0);
+    advance_sample(d_ts, adv, sample, ps, g, energy_valid, eps0, mue0, threadIdx.x, blockDim.x);
 }
 
 // Full-grid energy (CalcFastEnergy) on demand.

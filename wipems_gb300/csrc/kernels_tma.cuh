@@ -29,9 +29,18 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include "kernels.cuh"
 #include "node.cuh"
 
 namespace wipems {
+
+// minimum resident blocks per SM the batched kernels are compiled for
+// (caps their registers at 64: the per-job descriptor fields they read from
+// global memory cost registers that the single-job kernels take from
+// constant memory)
+#ifndef WIPEMS_BATCH_MIN_BLOCKS
+#define WIPEMS_BATCH_MIN_BLOCKS 4
+#endif
 
 constexpr int TMA_MAX_STAGES = 8;
 constexpr int TMA_TY = 8;
@@ -472,7 +481,7 @@ struct WorkItem {
 // takes items b, b + gridDim.x, ...  Every job's numTS is read from its own
 // counter, so jobs need not be in step.
 template <typename IdxT, int FEAT, bool GEO>
-__global__ void __launch_bounds__(TMA_TY * 32) k_volt_batch(const BatchJob* __restrict__ jobs,
+__global__ void __launch_bounds__(TMA_TY * 32, WIPEMS_BATCH_MIN_BLOCKS) k_volt_batch(const BatchJob* __restrict__ jobs,
                                                             const WorkItem* __restrict__ items, int nitems, int XC,
                                                             int STAGES) {
     using L = StageLayout<IdxT, (FEAT & FEAT_UPML) != 0>;
@@ -497,7 +506,7 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_volt_batch(const BatchJob* __re
 }
 
 template <typename IdxT, int FEAT, bool GEO>
-__global__ void __launch_bounds__(TMA_TY * 32) k_curr_batch(const BatchJob* __restrict__ jobs,
+__global__ void __launch_bounds__(TMA_TY * 32, WIPEMS_BATCH_MIN_BLOCKS) k_curr_batch(const BatchJob* __restrict__ jobs,
                                                             const WorkItem* __restrict__ items, int nitems, int XC,
                                                             int STAGES) {
     using L = StageLayout<IdxT, (FEAT & FEAT_UPML) != 0>;
