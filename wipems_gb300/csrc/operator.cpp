@@ -60,7 +60,24 @@ struct Geo {
         if (pos < N[n] - 1) return 0.5 * (l[pos] + l[pos + 1]);
         return l[pos] + 0.5 * (l[pos] - l[pos - 1]);
     }
-    double disc_delta(int n, uint32_t pos, bool dual) const {  // GetDiscDelta
+    // GetDiscDelta per axis and mesh, evaluated once (cache()) and then read
+    std::vector<double> dd[3][2];
+    void cache() {
+        for (int n = 0; n < 3; ++n)
+            for (int d = 0; d < 2; ++d) {
+                dd[n][d].clear();
+                std::vector<double> v(N[n]);
+                for (uint32_t i = 0; i < N[n]; ++i) v[i] = disc_delta_eval(n, i, d != 0);
+                dd[n][d] = std::move(v);
+            }
+    }
+    double disc_delta(int n, uint32_t pos, bool dual) const {
+        if (pos >= N[n]) return 0.0;
+        const std::vector<double>& c = dd[n][dual ? 1 : 0];
+        if (!c.empty()) return c[pos];
+        return disc_delta_eval(n, pos, dual);
+    }
+    double disc_delta_eval(int n, uint32_t pos, bool dual) const {  // GetDiscDelta
         if (pos >= N[n]) return 0.0;
         double delta = 0;
         if (!dual) {
@@ -308,6 +325,7 @@ struct Builder {
         g.L = s.lines;
         for (int n = 0; n < 3; ++n) g.N[n] = N[n];
         g.unit = s.unit;
+        g.cache();
         NN = (size_t)N[0] * N[1] * N[2];
         for (int i = 0; i < 6; ++i) {
             BC[i] = s.bc[i];
@@ -319,24 +337,18 @@ struct Builder {
     }
     size_t at(int n, const uint32_t* p) const { return at(n, p[0], p[1], p[2]); }
 
-    // Operator::GetMaterial with the kinds of the three sample coordinates.
-    double material(int type, const int kind[3], const uint32_t idx[3]) const {
+    // Operator::GetMaterial with the kinds of the three sample coordinates:
+    // the winning primitive's (eps, kappa, mue, sigma), or the background's.
+    struct Mat {
+        double eps, kappa, mue, sigma;
+    };
+    Mat material(const int kind[3], const uint32_t idx[3]) const {
         int w = mat_idx.lookup(kind, idx);
         if (w >= 0) {
             const Prim& p = S.prims[w];
-            switch (type) {
-                case 0: return p.eps;
-                case 1: return p.kappa;
-                case 2: return p.mue;
-                default: return p.sigma;
-            }
+            return Mat{p.eps, p.kappa, p.mue, p.sigma};
         }
-        switch (type) {
-            case 0: return S.bg_eps;
-            case 1: return S.bg_kappa;
-            case 2: return S.bg_mue;
-            default: return S.bg_sigma;
-        }
+        return Mat{S.bg_eps, S.bg_kappa, S.bg_mue, S.bg_sigma};
     }
 
     // Operator::AverageMatQuarterCell (operator.cpp:1406-1518)
@@ -349,34 +361,39 @@ struct Builder {
         double area = 0;
         int kind[3];
         uint32_t idx[3] = {pos[0], pos[1], pos[2]};
+        Mat m;
 
         // shift up-right
         kind[n] = SK_HALF; kind[nP] = SK_QP; kind[nPP] = SK_QP;
         A_n = g.node_area_i(ny, loc_pos, true);
-        EffMat[0] = material(0, kind, idx) * A_n;
-        EffMat[1] = material(1, kind, idx) * A_n;
+        m = material(kind, idx);
+        EffMat[0] = m.eps * A_n;
+        EffMat[1] = m.kappa * A_n;
         area += A_n;
         // shift up-left
         kind[nP] = SK_QM; kind[nPP] = SK_QP;
         --loc_pos[nP];
         A_n = g.node_area_i(ny, loc_pos, true);
-        EffMat[0] += material(0, kind, idx) * A_n;
-        EffMat[1] += material(1, kind, idx) * A_n;
+        m = material(kind, idx);
+        EffMat[0] += m.eps * A_n;
+        EffMat[1] += m.kappa * A_n;
         area += A_n;
         // shift down-right
         kind[nP] = SK_QP; kind[nPP] = SK_QM;
         ++loc_pos[nP];
         --loc_pos[nPP];
         A_n = g.node_area_i(ny, loc_pos, true);
-        EffMat[0] += material(0, kind, idx) * A_n;
-        EffMat[1] += material(1, kind, idx) * A_n;
+        m = material(kind, idx);
+        EffMat[0] += m.eps * A_n;
+        EffMat[1] += m.kappa * A_n;
         area += A_n;
         // shift down-left
         kind[nP] = SK_QM; kind[nPP] = SK_QM;
         --loc_pos[nP];
         A_n = g.node_area_i(ny, loc_pos, true);
-        EffMat[0] += material(0, kind, idx) * A_n;
-        EffMat[1] += material(1, kind, idx) * A_n;
+        m = material(kind, idx);
+        EffMat[0] += m.eps * A_n;
+        EffMat[1] += m.kappa * A_n;
         area += A_n;
 
         EffMat[0] *= kEps0 / area;
@@ -391,8 +408,9 @@ struct Builder {
         kind[n] = SK_QM; kind[nP] = SK_HALF; kind[nPP] = SK_HALF;
         --loc_pos[n];
         double delta_ny = g.node_width_i(n, loc_pos, true);
-        EffMat[2] = delta_ny / material(2, kind, idx);
-        double sigma = material(3, kind, idx);
+        m = material(kind, idx);
+        EffMat[2] = delta_ny / m.mue;
+        double sigma = m.sigma;
         if (sigma)
             EffMat[3] = delta_ny / sigma;
         else
@@ -402,8 +420,9 @@ struct Builder {
         kind[n] = SK_QP;
         ++loc_pos[n];
         delta_ny = g.node_width_i(n, loc_pos, true);
-        EffMat[2] += delta_ny / material(2, kind, idx);
-        sigma = material(3, kind, idx);
+        m = material(kind, idx);
+        EffMat[2] += delta_ny / m.mue;
+        sigma = m.sigma;
         if (sigma)
             EffMat[3] += delta_ny / sigma;
         else
@@ -502,10 +521,17 @@ struct Builder {
                         int sPPm[3] = {0, 0, 0}; sPPm[nPP] = -1;
                         int sPmPPm[3] = {0, 0, 0}; sPmPPm[nP] = -1; sPmPPm[nPP] = -1;
                         int sN1[3] = {0, 0, 0}; sN1[n] = 1;
-                        size_t ip = shifted(0, pos, s0) - 0;  // linear offset within a component
-                        auto C = [&](int c, const int* s) { return EC_C[(size_t)c * NN + (shifted(0, pos, s))]; };
-                        auto Lf = [&](int c, const int* s) { return EC_L[(size_t)c * NN + (shifted(0, pos, s))]; };
-                        (void)ip;
+                        // interior nodes: every +-1 shift stays on the grid, no reflection
+                        const bool inner = pos[0] > 0 && pos[1] > 0 && pos[2] > 0 && pos[0] + 1 < N[0] &&
+                                           pos[1] + 1 < N[1] && pos[2] + 1 < N[2];
+                        const size_t base = at(0, pos);
+                        auto off = [&](const int* s) -> size_t {
+                            if (inner)
+                                return base + (size_t)((long long)s[0] * N[1] * N[2] + (long long)s[1] * N[2] + s[2]);
+                            return shifted(0, pos, s);
+                        };
+                        auto C = [&](int c, const int* s) { return EC_C[(size_t)c * NN + off(s)]; };
+                        auto Lf = [&](int c, const int* s) { return EC_L[(size_t)c * NN + off(s)]; };
                         float one = 1;
                         double wqp = one / (Lf(nPP, s0) * C(n, sP1)) + one / (Lf(nPP, s0) * C(n, s0));
                         wqp += one / (Lf(nP, s0) * C(n, sPP1)) + one / (Lf(nP, s0) * C(n, s0));
