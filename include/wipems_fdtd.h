@@ -278,9 +278,19 @@ typedef struct {
     int      use_graphs;      /* capture chunks of interval steps */
     int      energy_on_probe; /* fuse the energy reduction into sample steps */
     int      tile_y;          /* kernel tile rows (0 = autotuned default) */
-    int      x_chunk;         /* x planes per block (0 = 8) */
-    int      kernel;          /* 0 = TMA-pipelined kernels (default),
-                                 1 = direct-load kernels */
+    int      x_chunk;         /* x planes per block (0 = chosen from the grid
+                                 size by a wave model: 1, 2, 4, 8 or 16) */
+    int      kernel;          /* 0 = default: the TMA-pipelined two-pass
+                                     kernels (3),
+                                 1 = direct-load kernels,
+                                 2 = fused single-pass TMA kernel (E and H of
+                                     a timestep in one x-march, double-
+                                     buffered fields; not with Lorentz/Drude
+                                     nodes or factorized geometry; fewer DRAM
+                                     bytes but fewer resident blocks: measured
+                                     slower than 3 on GB300 once the x-chunk
+                                     is tuned),
+                                 3 = TMA-pipelined two-pass kernels */
     int      stages;          /* TMA ring depth in x-planes, 3..8 (0 = 3) */
     double   end_crit;        /* > 0: the job stops on the device at the first
                                  sample whose energy is <= end_crit x the
@@ -353,6 +363,8 @@ typedef struct {
     uint32_t padded_nz;       /* z row stride on the device */
     uint64_t device_bytes;    /* device memory held by the engine */
     uint32_t tile_y, x_chunk; /* kernel tiling in use */
+    uint32_t kernel;          /* kernel family in use: 1, 2 or 3 as in
+                                 fdtd_engine_opts.kernel */
 } fdtd_engine_stats;
 
 int fdtd_engine_get_stats(fdtd_engine_t eng, fdtd_engine_stats* st);
@@ -381,7 +393,8 @@ int fdtd_engine_last_timing(fdtd_engine_t eng, double* ms, uint64_t* launches);
 typedef struct fdtd_batch_s* fdtd_batch_t;
 
 typedef struct {
-    int x_chunk;        /* x planes per work item (0 = 8) */
+    int x_chunk;        /* x planes per work item (0 = chosen from the
+                           batch's size by a wave model) */
     int stages;         /* TMA ring depth 3..8 (0 = 3) */
     int blocks_per_sm;  /* cap on resident blocks per SM (0 = occupancy) */
     int graph_steps;    /* timesteps per captured graph (0 = 8, 1 = none) */
@@ -399,6 +412,7 @@ typedef struct {
     uint64_t device_bytes;
     double   last_ms;
     uint64_t last_launches;
+    uint32_t x_chunk;   /* x planes per work item in use */
 } fdtd_batch_stats;
 
 int fdtd_batch_create(const fdtd_engine_t* engines, uint32_t n,

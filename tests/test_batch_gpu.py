@@ -42,7 +42,7 @@ def test_batch_equals_solo_runs(graph_steps, bin_mib):
     solo = [Engine(c) for c in cops]
     for e in solo:
         e.iterate(nsteps)
-    jobs = [Engine(c) for c in cops]
+    jobs = [Engine(c, kernel="tma") for c in cops]
     b = Batch(jobs, graph_steps=graph_steps, bin_mib=bin_mib)
     st = b.stats()
     assert st["num_jobs"] == len(jobs) and st["num_groups"] >= 3
@@ -58,7 +58,7 @@ def test_batch_jobs_at_different_timesteps():
     ops = _ops(300)[:4]
     cops = [CompressedOperator(op) for op in ops]
     solo = [Engine(c) for c in cops]
-    jobs = [Engine(c) for c in cops]
+    jobs = [Engine(c, kernel="tma") for c in cops]
     jobs[1].iterate(17)          # job 1 runs ahead on its own first
     solo[1].iterate(17 + 60)
     for k in (0, 2, 3):
@@ -104,7 +104,7 @@ def test_batch_end_criterion_same_as_alone():
     solo = [Engine(c, end_crit=crit) for c in cops]
     for e in solo:
         e.iterate(nr_ts)
-    jobs = [Engine(c, end_crit=crit) for c in cops]
+    jobs = [Engine(c, end_crit=crit, kernel="tma") for c in cops]
     b = Batch(jobs, graph_steps=16, bin_mib=1)
     b.iterate(nr_ts + 64)
     for s, j in zip(solo, jobs):

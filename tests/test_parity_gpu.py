@@ -143,6 +143,27 @@ def test_l256_full_size_first_steps_bitwise():
     compare(op, eng, ref)
 
 
+def test_d192_full_size_first_steps():
+    """D192 (graded mesh, UPML, Drude + Lorentz bricks) at full size: the
+    default (factorized-geometry) engine within the probe / field tolerance,
+    the exact-table engine (uint32 index) bit-identical to the oracle."""
+    op = Operator(scenes.d192(nr_ts=3000))
+    n = 40
+    ref = oracle.run(op.desc, op.probes, n, op.probe_interval, engine=oracle.SSE_COMPRESSED_MT,
+                     threads=os.cpu_count())
+    cop = CompressedOperator(op)
+    assert cop.info["geometry_factored"] == 1 and cop.info["num_ade_nodes"] > 0
+    eng = Engine(cop)
+    eng.iterate(n)
+    compare(op, eng, ref, bitwise=False)
+    eng.close()
+    exact = CompressedOperator(op, mode="exact")
+    assert exact.info["index_bytes_e"] == 4
+    eng = Engine(exact)
+    eng.iterate(n)
+    compare(op, eng, ref)
+
+
 def test_cavity_resonances_on_gpu():
     sc = scenes.cavity(nr_ts=20000)
     op = Operator(sc)
@@ -166,3 +187,68 @@ def test_field_access_and_energy():
     Vr, Ir = ref["volt"][:, :-1, :-1, :-1].astype(np.float64), ref["curr"][:, :-1, :-1, :-1].astype(np.float64)
     e_ref = eps0 * np.sum(Vr * Vr) + mue0 * np.sum(Ir * Ir)
     assert abs(eng.energy() / e_ref - 1) < 1e-6
+
+
+# ---------------------------------------------------------------- fused kernel
+@pytest.mark.parametrize("kind", ["pec", "upml"])
+def test_fused_kernel_matches_oracle(kind):
+    """The single-pass kernel (double-buffered fields, redundant halo E) is
+    bit-identical to the reference stepping, across odd tile edges."""
+    op = Operator(scenes.mini(kind, nr_ts=400))
+    n = 301
+    ref = oracle.run(op.desc, op.probes, n, op.probe_interval, engine=oracle.BASIC)
+    eng = Engine(op, kernel="fused")
+    assert eng.stats()["kernel"] == 2
+    eng.iterate(137)
+    eng.iterate(n - 137)
+    compare(op, eng, ref)
+
+
+def test_fused_kernel_tilings_and_graphs_invisible():
+    op = Operator(scenes.mini("upml", seed=2, nr_ts=400))
+    ref = oracle.run(op.desc, op.probes, 120, op.probe_interval, engine=oracle.BASIC)
+    for kw in (dict(x_chunk=1), dict(x_chunk=3, stages=4), dict(x_chunk=16, use_graphs=False), dict(stages=5)):
+        eng = Engine(op, kernel="fused", **kw)
+        eng.iterate(57)
+        eng.iterate(63)
+        compare(op, eng, ref)
+        eng.close()
+
+
+def test_fused_kernel_graded_exact_and_p64():
+    """32-bit indices (graded mesh, exact table) and a grid whose last lines
+    fall on tile edges (P64: 64 cells, the last y row and z column are
+    owned by the tiles below them)."""
+    op = Operator(scenes.mini("graded", nr_ts=400))
+    cop = CompressedOperator(op, mode="exact")
+    ref = oracle.run(op.desc, op.probes, 200, op.probe_interval, engine=oracle.BASIC)
+    eng = Engine(cop, kernel="fused")
+    eng.iterate(200)
+    compare(op, eng, ref)
+    op = Operator(scenes.p64(nr_ts=2000))
+    ref = oracle.run(op.desc, op.probes, 700, op.probe_interval, engine=oracle.SSE_COMPRESSED_MT,
+                     threads=os.cpu_count())
+    eng = Engine(op, kernel="fused")
+    eng.iterate(700)
+    compare(op, eng, ref)
+    V, I = eng.fields()
+    assert eng.get_volt(2, 32, 31, 30) == V[2, 32, 31, 30]
+    assert eng.get_curr(0, 63, 63, 63) == I[0, 63, 63, 63]
+
+
+def test_fused_kernel_l256_first_steps_bitwise():
+    op = Operator(scenes.l256(nr_ts=1000))
+    n = 18
+    ref = oracle.run(op.desc, op.probes, n, op.probe_interval, engine=oracle.SSE_COMPRESSED_MT,
+                     threads=os.cpu_count())
+    eng = Engine(op, kernel="fused")
+    eng.iterate(n)
+    compare(op, eng, ref)
+
+
+def test_fused_kernel_refuses_ade():
+    from wipems_gb300._abi import FdtdError
+    op = Operator(scenes.mini("drude", nr_ts=100))
+    with pytest.raises(FdtdError) as ei:
+        Engine(op, kernel="fused")
+    assert ei.value.code == -5

@@ -65,7 +65,7 @@ class FdtdEngineOpts(C.Structure):
 class FdtdEngineStats(C.Structure):
     _fields_ = [("num_tuples", u32), ("index_bytes", u32), ("num_upml_nodes", u32),
                 ("num_ade_nodes", u32), ("padded_nz", u32), ("device_bytes", C.c_uint64),
-                ("tile_y", u32), ("x_chunk", u32)]
+                ("tile_y", u32), ("x_chunk", u32), ("kernel", u32)]
 
 
 class FdtdCopInfo(C.Structure):
@@ -107,7 +107,7 @@ class FdtdServerStats(C.Structure):
 class FdtdBatchStats(C.Structure):
     _fields_ = [("num_jobs", u32), ("num_groups", u32), ("num_bins", u32), ("total_nodes", C.c_uint64), ("work_items", C.c_uint64),
                 ("persistent_blocks", u32), ("device_bytes", C.c_uint64), ("last_ms", C.c_double),
-                ("last_launches", C.c_uint64)]
+                ("last_launches", C.c_uint64), ("x_chunk", u32)]
 
 
 class FdtdError(RuntimeError):

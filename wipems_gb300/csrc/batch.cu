@@ -253,7 +253,7 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
         return FDTD_ERR_ARG;
     }
     b->device = engines[0] ? engines[0]->device : 0;
-    b->XC = (o && o->x_chunk > 0) ? o->x_chunk : 8;
+    b->XC = (o && o->x_chunk > 0) ? o->x_chunk : 0;  // 0: chosen below from the batch's size
     b->stages = (o && o->stages > 0) ? o->stages : 3;
     b->blocks_per_sm = (o && o->blocks_per_sm > 0) ? o->blocks_per_sm : 0;
     b->graph_steps = (o && o->graph_steps > 0) ? (uint32_t)o->graph_steps : 8;
@@ -277,8 +277,8 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
             set_error("fdtd_batch_create: all jobs must live on one device");
             return FDTD_ERR_ARG;
         }
-        if (!e->use_tma) {
-            set_error("fdtd_batch_create: jobs must use the TMA kernels");
+        if (!e->use_tma || e->fused) {
+            set_error("fdtd_batch_create: jobs must use the two-pass TMA kernels");
             return FDTD_ERR_ARG;
         }
         for (uint32_t k = 0; k < j; ++k)
@@ -374,6 +374,11 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
     // work lists and persistent grid sizes
     int sms = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
+    if (b->XC == 0) {
+        std::vector<const uint32_t*> lines;
+        for (const fdtd_engine_s* e : b->jobs) lines.push_back(e->N);
+        b->XC = auto_x_chunk(lines, (uint64_t)WIPEMS_BATCH_MIN_BLOCKS * (uint64_t)sms);
+    }
     const size_t maxsm = stage_smem(false, true, b->stages);
     if (maxsm > 48 * 1024 && (rc = batch_smem_attrs((int)maxsm))) return rc;
     for (Group& G : b->groups) {
@@ -500,6 +505,7 @@ int fdtd_batch_info(fdtd_batch_t b, fdtd_batch_stats* st) {
     st->device_bytes = b->device_bytes;
     st->last_ms = b->last_ms;
     st->last_launches = b->last_launches;
+    st->x_chunk = (uint32_t)b->XC;
     return FDTD_OK;
 }
 

@@ -103,6 +103,33 @@ void launch_curr(fdtd_engine_s* e, int ts_off, bool energy) {
     }
 }
 
+template <typename IE, typename IH, int FEAT, bool EN>
+void launch_fused_t(fdtd_engine_s* e, int ts_off) {
+    const size_t sm = FusedLayout<IE, IH, (FEAT & FEAT_UPML) != 0>::smem(e->stages);
+    dim3 grid((e->N[2] - 1 + 31) / 32, (e->N[1] - 1 + FU_TY - 1) / FU_TY, (e->N[0] - 1 + e->XC - 1) / e->XC);
+    k_step_fused<IE, IH, FEAT, EN><<<grid, dim3(32, FU_WARPS), sm, e->stream>>>(e->g, e->fmaps, e->ti, ts_off, e->XC,
+                                                                             e->stages);
+}
+template <typename IE, typename IH, bool EN>
+void launch_fused_f(fdtd_engine_s* e, int ts_off) {
+    if (e->feat & FEAT_UPML) launch_fused_t<IE, IH, FEAT_UPML, EN>(e, ts_off);
+    else launch_fused_t<IE, IH, 0, EN>(e, ts_off);
+}
+template <bool EN>
+void launch_fused_e(fdtd_engine_s* e, int ts_off) {
+    if (e->E.idx16) {
+        if (e->H.idx16) launch_fused_f<uint16_t, uint16_t, EN>(e, ts_off);
+        else launch_fused_f<uint16_t, uint32_t, EN>(e, ts_off);
+    } else {
+        if (e->H.idx16) launch_fused_f<uint32_t, uint16_t, EN>(e, ts_off);
+        else launch_fused_f<uint32_t, uint32_t, EN>(e, ts_off);
+    }
+}
+void launch_fused(fdtd_engine_s* e, int ts_off, bool energy) {
+    if (energy) launch_fused_e<true>(e, ts_off);
+    else launch_fused_e<false>(e, ts_off);
+}
+
 int check_launch() {
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) {
@@ -113,6 +140,11 @@ int check_launch() {
 }
 
 int launch_step(fdtd_engine_s* e, int ts_off, bool energy) {
+    if (e->fused) {
+        launch_fused(e, ts_off, energy);
+        e->last_launches += 1;
+        return check_launch();
+    }
     launch_volt(e, ts_off);
     launch_curr(e, ts_off, energy);
     e->last_launches += 2;
@@ -264,7 +296,8 @@ int field_map(CUtensorMap* m, float* base, const fdtd_engine_s* e, uint32_t box_
     return FDTD_OK;
 }
 
-int index_map(CUtensorMap* m, void* base, const fdtd_engine_s* e, bool idx16) {
+int index_map(CUtensorMap* m, void* base, const fdtd_engine_s* e, bool idx16, uint32_t box_z = 32,
+              uint32_t box_y = TMA_TY) {
     PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
     if (!enc) {
         set_error("cuTensorMapEncodeTiled is not available from the driver");
@@ -273,13 +306,58 @@ int index_map(CUtensorMap* m, void* base, const fdtd_engine_s* e, bool idx16) {
     const cuuint64_t ib = idx16 ? 2 : 4;
     cuuint64_t dims[3] = {e->N[2], e->N[1], e->N[0]};
     cuuint64_t strides[2] = {(cuuint64_t)e->Nzp * ib, (cuuint64_t)e->N[1] * e->Nzp * ib};
-    cuuint32_t box[3] = {32, TMA_TY, 1};
+    cuuint32_t box[3] = {box_z, box_y, 1};
     cuuint32_t es[3] = {1, 1, 1};
     CUresult r = enc(m, idx16 ? CU_TENSOR_MAP_DATA_TYPE_UINT16 : CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, base, dims, strides,
                      box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         set_error("cuTensorMapEncodeTiled (index) failed: " + std::to_string((int)r));
+        return FDTD_ERR_CUDA;
+    }
+    return FDTD_OK;
+}
+
+// tensor maps of the fused kernel (boxes: see kernels_fused.cuh)
+int make_fused_maps(fdtd_engine_s* e) {
+    int rc;
+    FusedMaps& m = e->fmaps;
+    float* Vb[2] = {e->V.p, e->V2.p};
+    float* Ib[2] = {e->I.p, e->I2.p};
+    float* Fb[2] = {e->FV.p, e->FV2.p};
+    for (int p = 0; p < 2; ++p) {
+        if ((rc = field_map(&m.I_halo[p], Ib[p], e, FU_IW, FU_IH)) ||
+            (rc = field_map(&m.V_ext[p], Vb[p], e, FU_VW, FU_EH)))
+            return rc;
+        if (Fb[p] && (rc = field_map(&m.FV_ext[p], Fb[p], e, FU_VW, FU_EH))) return rc;
+    }
+    if (e->FI.p && (rc = field_map(&m.FI_own, e->FI.p, e, 32, FU_TY))) return rc;
+    if ((rc = index_map(&m.idxE_ext, e->E.idx.p, e, e->E.idx16, FU_XW, FU_EH)) ||
+        (rc = index_map(&m.idxH_own, e->H.idx.p, e, e->H.idx16, 32, FU_TY)))
+        return rc;
+    return FDTD_OK;
+}
+
+template <typename IE, typename IH>
+cudaError_t fused_attr_one(int bytes) {
+    const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    cudaError_t r[4] = {cudaFuncSetAttribute(k_step_fused<IE, IH, 0, false>, a, bytes),
+                        cudaFuncSetAttribute(k_step_fused<IE, IH, 0, true>, a, bytes),
+                        cudaFuncSetAttribute(k_step_fused<IE, IH, FEAT_UPML, false>, a, bytes),
+                        cudaFuncSetAttribute(k_step_fused<IE, IH, FEAT_UPML, true>, a, bytes)};
+    for (cudaError_t x : r)
+        if (x != cudaSuccess) return x;
+    return cudaSuccess;
+}
+
+int set_fused_attrs(int bytes) {
+    cudaError_t r = cudaSuccess, t;
+    if ((t = fused_attr_one<uint16_t, uint16_t>(bytes)) != cudaSuccess) r = t;
+    if ((t = fused_attr_one<uint16_t, uint32_t>(bytes)) != cudaSuccess) r = t;
+    if ((t = fused_attr_one<uint32_t, uint16_t>(bytes)) != cudaSuccess) r = t;
+    if ((t = fused_attr_one<uint32_t, uint32_t>(bytes)) != cudaSuccess) r = t;
+    if (r != cudaSuccess) {
+        set_error(std::string("cudaFuncSetAttribute(MaxDynamicSharedMemorySize, fused): ") + cudaGetErrorString(r));
         return FDTD_ERR_CUDA;
     }
     return FDTD_OK;
@@ -332,7 +410,7 @@ int set_smem_attrs(int bytes) {
 int reset_state(fdtd_engine_s* e) {
     cudaStream_t s = e->stream;
     const size_t F = 3 * (size_t)e->comp * sizeof(float);
-    for (DevBuf<float>* b : {&e->V, &e->I, &e->FV, &e->FI, &e->AV, &e->LV, &e->AI, &e->LI})
+    for (DevBuf<float>* b : {&e->V, &e->I, &e->FV, &e->FI, &e->AV, &e->LV, &e->AI, &e->LI, &e->V2, &e->I2, &e->FV2})
         if (b->p) CK(cudaMemsetAsync(b->p, 0, F, s));
     CK(cudaMemsetAsync(e->ctl.p, 0, 4 * sizeof(int), s));
     CK(cudaMemsetAsync(e->d_eacc.p, 0, 4 * sizeof(double), s));
@@ -379,11 +457,17 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
         set_error("tile_y must be 1..8");
         return FDTD_ERR_ARG;
     }
-    e->XC = (opts && opts->x_chunk > 0) ? opts->x_chunk : 8;
+    e->XC = (opts && opts->x_chunk > 0) ? opts->x_chunk : 0;  // 0: auto_x_chunk below
     e->interval = opts ? opts->probe_interval : 0;
     e->energy_on_probe = opts ? opts->energy_on_probe != 0 : true;
     e->use_graphs = opts ? opts->use_graphs != 0 : true;
-    e->use_tma = !(opts && opts->kernel == 1);
+    const int kern = opts ? opts->kernel : 0;
+    if (kern < 0 || kern > 3) {
+        set_error("kernel must be 0 (auto), 1 (direct), 2 (fused) or 3 (two-pass TMA)");
+        return FDTD_ERR_ARG;
+    }
+    e->use_tma = kern != 1;
+    e->fused = kern == 2;
     e->stages = (opts && opts->stages > 0) ? opts->stages : 3;
     if (e->stages < 3 || e->stages > TMA_MAX_STAGES) {
         set_error("stages must be 3..8");
@@ -402,17 +486,29 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     e->upml_nodes = c->upml_nodes;
     e->ade_nodes = c->ade_nodes;
     e->Nzp = c->Nzp;
+    if (e->XC == 0) {
+        int sms = 0;
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->device));
+        e->XC = auto_x_chunk({e->N}, 5ull * (uint64_t)sms);  // about 5 resident blocks per SM
+    }
     e->comp = c->comp;
     e->geo_on = c->geo;
     const bool any_upml = c->E.any_upml || c->H.any_upml;
     const bool any_ade = c->E.any_ade || c->H.any_ade;
     e->feat = (any_upml ? FEAT_UPML : 0) | (any_ade ? FEAT_ADE : 0);
+    if (e->fused && (any_ade || c->geo)) {
+        set_error("the fused single-pass kernel does not cover Lorentz/Drude nodes or factorized geometry "
+                  "(use the two-pass TMA kernels)");
+        return FDTD_ERR_UNSUPPORTED;
+    }
 
     int rc;
     uint64_t& tot = e->device_bytes;
     const size_t F = 3 * (size_t)e->comp;
     if ((rc = e->V.alloc(F, tot)) || (rc = e->I.alloc(F, tot))) return rc;
     if (any_upml && ((rc = e->FV.alloc(F, tot)) || (rc = e->FI.alloc(F, tot)))) return rc;
+    if (e->fused && ((rc = e->V2.alloc(F, tot)) || (rc = e->I2.alloc(F, tot)))) return rc;
+    if (e->fused && any_upml && (rc = e->FV2.alloc(F, tot))) return rc;
     if (c->E.any_ade && (rc = e->AV.alloc(F, tot))) return rc;
     if (c->E.any_lor && (rc = e->LV.alloc(F, tot))) return rc;
     if (c->H.any_ade && (rc = e->AI.alloc(F, tot))) return rc;
@@ -444,6 +540,9 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     g.comp = e->comp;
     g.V = e->V.p;
     g.I = e->I.p;
+    g.V2 = e->V2.p;
+    g.I2 = e->I2.p;
+    g.FV2 = e->FV2.p;
     g.FV = e->FV.p;
     g.FI = e->FI.p;
     g.AV = e->AV.p;
@@ -466,7 +565,11 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
         e->ti.ne[a] = (int)e->N[a] - (c->trim_e[a] ? 1 : 0);
     }
     e->ti.d_err = e->p_err();
-    if (e->use_tma) {
+    if (e->fused) {
+        if ((rc = make_fused_maps(e))) return rc;
+        const size_t need = FusedLayout<uint32_t, uint32_t, true>::smem(e->stages);
+        if (need > 48 * 1024 && (rc = set_fused_attrs((int)need))) return rc;
+    } else if (e->use_tma) {
         if ((rc = make_maps(e))) return rc;
         const size_t need = (e->feat & FEAT_UPML) ? StageLayout<uint32_t, true>::smem(e->stages)
                                                   : StageLayout<uint32_t, false>::smem(e->stages);
@@ -718,7 +821,10 @@ int fdtd_engine_energy(fdtd_engine_t e, double* energy) {
     if (!e || !energy) return FDTD_ERR_ARG;
     CK(cudaSetDevice(e->device));
     CK(cudaMemsetAsync(e->d_energy_tmp.p, 0, 2 * sizeof(double), e->stream));
-    k_energy<<<4 * 152, 256, 0, e->stream>>>(e->g, e->d_energy_tmp.p);
+    DevGrid g = e->g;
+    g.V = e->cur_V();
+    g.I = e->cur_I();
+    k_energy<<<4 * 152, 256, 0, e->stream>>>(g, e->d_energy_tmp.p);
     CK(cudaGetLastError());
     double h[2];
     CK(cudaMemcpyAsync(h, e->d_energy_tmp.p, sizeof(h), cudaMemcpyDeviceToHost, e->stream));
@@ -734,7 +840,7 @@ int fdtd_engine_get_fields(fdtd_engine_t e, float* volt, float* curr) {
     for (int which = 0; which < 2; ++which) {
         float* dst = which ? curr : volt;
         if (!dst) continue;
-        const float* src = which ? e->I.p : e->V.p;
+        const float* src = which ? e->cur_I() : e->cur_V();
         // rows of Nz floats out of rows of Nzp floats
         CK(cudaMemcpy2DAsync(dst, Nz * sizeof(float), src, e->Nzp * sizeof(float), Nz * sizeof(float),
                              (size_t)3 * Nx * Ny, cudaMemcpyDeviceToHost, e->stream));
@@ -756,10 +862,10 @@ static int get_one(fdtd_engine_t e, const float* base, uint32_t n, uint32_t x, u
 }
 
 int fdtd_engine_get_volt(fdtd_engine_t e, uint32_t n, uint32_t x, uint32_t y, uint32_t z, float* v) {
-    return get_one(e, e ? e->V.p : nullptr, n, x, y, z, v);
+    return get_one(e, e ? e->cur_V() : nullptr, n, x, y, z, v);
 }
 int fdtd_engine_get_curr(fdtd_engine_t e, uint32_t n, uint32_t x, uint32_t y, uint32_t z, float* v) {
-    return get_one(e, e ? e->I.p : nullptr, n, x, y, z, v);
+    return get_one(e, e ? e->cur_I() : nullptr, n, x, y, z, v);
 }
 
 int fdtd_engine_profile_kernels(fdtd_engine_t e, uint32_t n_steps, double* ms_volt, double* ms_curr) {
@@ -772,9 +878,14 @@ int fdtd_engine_profile_kernels(fdtd_engine_t e, uint32_t n_steps, double* ms_vo
     for (uint32_t k = 0; k < n_steps; ++k) {
         const bool sample = e->interval && ((e->ts + 1) % e->interval) == 0;
         CK(cudaEventRecord(ev[3 * k], e->stream));
-        launch_volt(e, 0);
-        CK(cudaEventRecord(ev[3 * k + 1], e->stream));
-        launch_curr(e, 0, sample && e->energy_on_probe);
+        if (e->fused) {  // one kernel per step: reported as the "volt" time
+            launch_fused(e, 0, sample && e->energy_on_probe);
+            CK(cudaEventRecord(ev[3 * k + 1], e->stream));
+        } else {
+            launch_volt(e, 0);
+            CK(cudaEventRecord(ev[3 * k + 1], e->stream));
+            launch_curr(e, 0, sample && e->energy_on_probe);
+        }
         CK(cudaEventRecord(ev[3 * k + 2], e->stream));
         if ((rc = check_launch())) return rc;
         if ((rc = launch_advance(e, 1, sample, e->energy_on_probe))) return rc;
@@ -806,6 +917,7 @@ int fdtd_engine_get_stats(fdtd_engine_t e, fdtd_engine_stats* st) {
     st->device_bytes = e->device_bytes;
     st->tile_y = (uint32_t)(e->use_tma ? TMA_TY : e->TY);
     st->x_chunk = (uint32_t)e->XC;
+    st->kernel = e->fused ? 2u : (e->use_tma ? 3u : 1u);
     return FDTD_OK;
 }
 

@@ -11,6 +11,7 @@
 #include "cop.h"
 #include "fdtd_host.h"
 #include "kernels.cuh"
+#include "kernels_fused.cuh"
 #include "kernels_tma.cuh"
 
 namespace wipems {
@@ -64,6 +65,7 @@ struct fdtd_engine_s {
     double dT = 0;
     DevGrid g{};
     DevBuf<float> V, I, FV, FI, AV, LV, AI, LI;
+    DevBuf<float> V2, I2, FV2;  // second field / voltage-flux buffers (fused kernel)
     DevHalfBufs E, H;
     DevBuf<float> geo;
     DevBuf<float> sigV, sigC;
@@ -102,6 +104,11 @@ struct fdtd_engine_s {
     int TY = 8;
     int XC = 8;
     bool use_tma = true;
+    bool fused = false;      // single-pass kernel, double-buffered fields
+    FusedMaps fmaps{};
+    // field buffers holding the fields at the current numTS
+    float* cur_V() const { return (fused && (ts & 1)) ? V2.p : V.p; }
+    float* cur_I() const { return (fused && (ts & 1)) ? I2.p : I.p; }
     int stages = 3;
     TmaMaps maps{};
     TileInfo ti{};
@@ -123,6 +130,29 @@ struct fdtd_engine_s {
 
 
 namespace wipems {
+// x-chunk (planes per block: 1, 2, 4, 8 or 16) from a wave model of the
+// current-kernel grid: a block costs about (2 + x_chunk) plane times (the
+// ring prologue, then one plane each), blocks run in waves of `resident`,
+// so the step costs ceil(blocks / resident) * (2 + x_chunk); a chunk that
+// leaves SMs idle in the only wave is skipped, ties go to the longer chunk
+// (fewer halo-plane re-reads).  lines: the jobs' (Nx, Ny, Nz) triples.
+inline int auto_x_chunk(const std::vector<const uint32_t*>& lines, uint64_t resident) {
+    int best = 1;
+    uint64_t best_cost = ~0ull;
+    for (int xc = 16; xc >= 1; xc /= 2) {
+        uint64_t items = 0;
+        for (const uint32_t* N : lines)
+            items += (uint64_t)((N[2] - 1 + 31) / 32) * ((N[1] - 1 + TMA_TY - 1) / TMA_TY) * ((N[0] - 1 + xc - 1) / xc);
+        if (items < resident && xc > 1) continue;
+        const uint64_t cost = (items + resident - 1) / resident * (uint64_t)(2 + xc);
+        if (cost < best_cost) {
+            best_cost = cost;
+            best = xc;
+        }
+    }
+    return best;
+}
+
 // engine.cu helpers used by the batched path
 int engine_start(fdtd_engine_s* e);        // upload probes, graph, ts = 0 sample
 int engine_check_errors(fdtd_engine_s* e); // read the control words, decode errors

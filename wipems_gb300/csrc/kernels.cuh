@@ -259,7 +259,8 @@ __device__ __forceinline__ void advance_sample(int* d_ts, int adv, int sample, c
         double acc = 0.0;
         for (int e = ps.first[p] + lane; e < ps.first[p + 1]; e += 32) {
             const ProbeEntry pe = ps.entries[e];
-            const float* f = pe.field ? g.I : g.V;
+            const bool odd = g.V2 && (s_ts & 1);  // fused kernel: the buffer of numTS
+            const float* f = pe.field ? (odd ? g.I2 : g.I) : (odd ? g.V2 : g.V);
             const float val = f[(long long)pe.comp * g.comp + pe.off];
             acc += pe.sign > 0 ? (double)val : -(double)val;
         }

@@ -48,6 +48,9 @@ struct DevGrid {
     float* I;            // [3][comp]
     float* FV;           // UPML voltage flux [3][comp] or null
     float* FI;           // UPML current flux
+    float* V2;           // fused single-pass kernel: second field buffers
+    float* I2;           // (fields at numTS live in V/I when numTS is even,
+    float* FV2;          // in V2/I2 when odd); null otherwise
     float* AV;           // ADE voltage state (order 1) [3][comp]
     float* LV;           // Lorentz voltage state
     float* AI;           // ADE current state
@@ -103,10 +106,12 @@ __device__ __forceinline__ GeoF geo_factors(const DevGrid& g, bool H, int x, int
 // One node of one half-step.  fld[3]: the old field (V or I); curl[3]: the
 // curl of the other field; t: tuple index; o: node offset; F (UPML flux of
 // the node) is read from fsrc[n*fstride] when fsrc is set, else from global.
+// The new flux goes to fout (default: the engine's flux array, in place),
+// and only when fwrite is set.
 template <bool H, int FEAT, bool GEO>
 __device__ __forceinline__ void update_node(const DevGrid& g, float fld[3], const float curl[3], uint32_t t,
                                             long long o, int numTS, const float* fsrc, int fstride,
-                                            const GeoF& gf) {
+                                            const GeoF& gf, float* fout = nullptr, bool fwrite = true) {
     const DevHalf& T = H ? g.h : g.e;
     const float4 ta = __ldg(&T.main[TAB_MAIN * t]);
     const float4 tb = __ldg(&T.main[TAB_MAIN * t + 1]);
@@ -120,7 +125,7 @@ __device__ __forceinline__ void update_node(const DevGrid& g, float fld[3], cons
     const long long C = g.comp;
     float* A = H ? g.AI : g.AV;
     float* Lr = H ? g.LI : g.LV;
-    float* Fl = H ? g.FI : g.FV;
+    float* Fl = fout ? fout : (H ? g.FI : g.FV);
     float ade[3] = {0.f, 0.f, 0.f};
     if ((FEAT & FEAT_ADE) && (flags & TF_ADE)) {
         const float4 a0 = __ldg(&T.ade[TAB_ADE * t]);
@@ -164,7 +169,7 @@ __device__ __forceinline__ void update_node(const DevGrid& g, float fld[3], cons
             const float F = fsrc ? fsrc[n * fstride] : Fl[n * C + o];
             const float f = __fsub_rn(__fmul_rn(kp[n], fld[n]), __fmul_rn(kfo[n], F));
             const float Fn = __fadd_rn(__fmul_rn(F, c1[n]), __fmul_rn(c2[n], curl[n]));
-            Fl[n * C + o] = Fn;
+            if (fwrite) Fl[n * C + o] = Fn;
             fld[n] = __fadd_rn(f, __fmul_rn(kfn[n], Fn));
         }
     } else {

@@ -243,6 +243,7 @@ int admit(fdtd_server_s* s, Job* j) {
     o.max_timesteps = j->max_ts;
     o.probe_interval = j->interval;
     o.use_graphs = 0;  // the batch replays its own graphs
+    o.kernel = 3;      // batched jobs run the two-pass kernels
     o.energy_on_probe = 1;
     o.end_crit = j->opts.end_crit;
     fdtd_engine_t e = nullptr;

@@ -257,7 +257,7 @@ class Engine:
 
     def __init__(self, op, device: int = 0, max_timesteps: int = 0, probe_interval: int | None = None,
                  use_graphs: bool = True, energy_on_probe: bool = True, tile_y: int = 0, x_chunk: int = 0,
-                 probes: bool = True, kernel: str = "tma", stages: int = 0, end_crit: float = 0.0):
+                 probes: bool = True, kernel: str = "auto", stages: int = 0, end_crit: float = 0.0):
         cop = op if isinstance(op, CompressedOperator) else None
         if cop is not None:
             op = cop.op
@@ -270,9 +270,10 @@ class Engine:
         o.energy_on_probe = int(energy_on_probe)
         o.tile_y = int(tile_y)
         o.x_chunk = int(x_chunk)
-        if kernel not in ("tma", "direct"):
-            raise ValueError("kernel must be 'tma' or 'direct'")
-        o.kernel = 0 if kernel == "tma" else 1
+        kinds = {"auto": 0, "direct": 1, "fused": 2, "tma": 3}
+        if kernel not in kinds:
+            raise ValueError("kernel must be 'auto', 'tma', 'direct' or 'fused'")
+        o.kernel = kinds[kernel]
         o.stages = int(stages)
         o.end_crit = float(end_crit)
         h = C.c_void_p()

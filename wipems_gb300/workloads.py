@@ -1,0 +1,165 @@
+"""Measurement drivers for the workloads beside the L256 headline of
+bench.py: the P64 and D192 single jobs, the B96 batched sweep and the S
+serving stream.  Each prints one JSON object.
+
+    python -m wipems_gb300.workloads p64|d192|b96|serve [options]
+
+Timings are CUDA-event device times unless named wall (host clock around a
+whole stream, including operator builds).  Mcell-updates/s uses the node
+count (lines product), the reference's convention (openems.cpp:1303-1305).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+
+def single(kind: str, steps: int = 0, device: int = 0) -> dict:
+    """One job on the plain engine (CUDA graphs, TMA kernels, autotuned)."""
+    from . import CompressedOperator, Engine, Operator, autotune, scenes
+    sc = {"p64": scenes.p64, "d192": scenes.d192}[kind]()
+    t0 = time.perf_counter()
+    op = Operator(sc)
+    cop = CompressedOperator(op)
+    setup = time.perf_counter() - t0
+    best, _ = autotune.tune(cop, stages=(3, 4), steps=40, device=device)
+    nts = steps or sc.nr_ts
+    eng = Engine(cop, device=device, max_timesteps=nts + 100, stages=best["stages"], x_chunk=best["x_chunk"],
+                 kernel=best["kernel"])
+    eng.iterate(min(nts, 50))     # warm-up (graph instantiation)
+    eng.reset()
+    eng.iterate(nts)
+    ms, launches = eng.last_timing()
+    mv, mc = eng.profile_kernels(20)
+    n = op.num_nodes
+    info = cop.info
+    return dict(workload=kind, nodes=n, timesteps=nts, device_ms=ms, mcells=n * nts / (ms / 1e3) / 1e6,
+                kernel=best["kernel"],
+                ms_volt=mv, ms_curr=mc, launches=launches, setup_s=round(setup, 3), tiling=best,
+                tuples_e=info["num_tuples_e"], tuples_h=info["num_tuples_h"],
+                geometry_factored=info["geometry_factored"], upml_nodes=info["num_upml_nodes"],
+                ade_nodes=info["num_ade_nodes"])
+
+
+def b96(n_jobs: int = 96, timesteps: int = 1500, device: int = 0) -> dict:
+    """B96: the seeded 96-job sweep, plain engine job by job vs one batch
+    (autotuned x_chunk / graph length)."""
+    from . import Batch, CompressedOperator, Engine, Operator, autotune, scenes
+    t0 = time.perf_counter()
+    cops, nodes = [], []
+    for s in range(n_jobs):
+        op = Operator(scenes.b96_job(s, nr_ts=timesteps))
+        cops.append(CompressedOperator(op))
+        nodes.append(op.num_nodes)
+    setup = time.perf_counter() - t0
+    work = sum(nodes) * timesteps
+    plain_ms = 0.0
+    for c in cops:
+        e = Engine(c, device=device, max_timesteps=timesteps)
+        e.iterate(timesteps)
+        plain_ms += e.last_timing()[0]
+        e.close()
+    best, table = autotune.tune_batch(cops, device=device)
+    engines = [Engine(c, device=device, max_timesteps=timesteps, kernel="tma") for c in cops]
+    b = Batch(engines, x_chunk=best["x_chunk"], graph_steps=best["graph_steps"])
+    b.iterate(timesteps)
+    st = b.stats()
+    b.close()
+    for e in engines:
+        e.close()
+    plain = work / (plain_ms / 1e3) / 1e6
+    batched = work / (st["last_ms"] / 1e3) / 1e6
+    return dict(workload="b96", jobs=n_jobs, timesteps=timesteps, nodes=sum(nodes), setup_s=round(setup, 2),
+                plain_ms=plain_ms, plain_mcells=plain, batched_ms=st["last_ms"], batched_mcells=batched,
+                speedup=batched / plain, tiling=best, groups=st["num_groups"], work_items=st["work_items"],
+                persistent_blocks=st["persistent_blocks"], launches=st["last_launches"])
+
+
+def serve(n_jobs: int = 48, mean_gap: float = 0.02, end_crit: float = 1e-4, seed: int = 777, device: int = 0,
+          round_steps: int = 128, modes=("served", "plain")) -> dict:
+    """S: a seeded Poisson stream of serve_job requests (operator build
+    included), through the continuous-batching server and one at a time
+    through the plain engine.  Both stop every job at -40 dB energy or its
+    NrTS; the stopping timesteps are compared."""
+    from . import CompressedOperator, Engine, Operator, Server, scenes
+    rng = np.random.default_rng(seed)
+    arr = np.cumsum(rng.exponential(mean_gap, n_jobs))
+    arr -= arr[0]
+    out = dict(workload="serve", jobs=n_jobs, mean_gap_s=mean_gap, end_crit=end_crit, seed=seed)
+
+    def pct(a, q):
+        return float(np.percentile(np.asarray(a), q))
+
+    ts_served = ts_plain = None
+    if "served" in modes:
+        srv = Server(device=device, round_steps=round_steps)
+        t0 = time.perf_counter()
+        ids = []
+        for k in range(n_jobs):
+            dt = arr[k] - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            ids.append(srv.submit(scenes.serve_job(k), end_crit=end_crit))
+        srv.wait(0)
+        st = [srv.status(i) for i in ids]
+        ss = srv.stats()
+        srv.close()
+        lat = [x["t_done"] - x["t_submit"] for x in st]
+        mk = max(x["t_done"] for x in st) - min(x["t_submit"] for x in st)
+        work = sum(x["nodes"] * x["timesteps"] for x in st)
+        ts_served = [x["timesteps"] for x in st]
+        out["served"] = dict(wall_s=mk, mcells=work / mk / 1e6, jobs_per_s=n_jobs / mk, p50_s=pct(lat, 50),
+                             p99_s=pct(lat, 99), gpu_ms=ss["gpu_ms"], gpu_mcells=work / (ss["gpu_ms"] / 1e3) / 1e6,
+                             rounds=ss["rounds"], rebuilds=ss["rebuilds"], peak_gb=ss["peak_bytes"] / 1e9,
+                             failed=ss["jobs_failed"], node_steps=work)
+    if "plain" in modes:
+        t0 = time.perf_counter()
+        lat, ts_plain, work, gpu_ms = [], [], 0, 0.0
+        for k in range(n_jobs):
+            dt = arr[k] - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            sc = scenes.serve_job(k)
+            op = Operator(sc)
+            e = Engine(CompressedOperator(op), device=device, end_crit=end_crit)
+            while not e.done and e.num_timesteps < sc.nr_ts:
+                e.iterate(min(1024, sc.nr_ts - e.num_timesteps))
+                gpu_ms += e.last_timing()[0]
+            e.samples()
+            ts_plain.append(e.num_timesteps)
+            work += op.num_nodes * e.num_timesteps
+            e.close()
+            lat.append(time.perf_counter() - t0 - arr[k])
+        mk = time.perf_counter() - t0
+        out["plain"] = dict(wall_s=mk, mcells=work / mk / 1e6, jobs_per_s=n_jobs / mk, p50_s=pct(lat, 50),
+                            p99_s=pct(lat, 99), gpu_ms=gpu_ms, gpu_mcells=work / (gpu_ms / 1e3) / 1e6,
+                            node_steps=work)
+    if ts_served is not None and ts_plain is not None:
+        out["same_stop_timesteps"] = ts_served == ts_plain
+        out["speedup"] = out["served"]["mcells"] / out["plain"]["mcells"]
+        out["gpu_speedup"] = out["served"]["gpu_mcells"] / out["plain"]["gpu_mcells"]
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("workload", choices=["p64", "d192", "b96", "serve"])
+    ap.add_argument("--jobs", type=int, default=0)
+    ap.add_argument("--timesteps", type=int, default=0)
+    ap.add_argument("--gap", type=float, default=0.02)
+    ap.add_argument("--device", type=int, default=0)
+    args = ap.parse_args()
+    if args.workload in ("p64", "d192"):
+        r = single(args.workload, args.timesteps, args.device)
+    elif args.workload == "b96":
+        r = b96(args.jobs or 96, args.timesteps or 1500, args.device)
+    else:
+        r = serve(args.jobs or 48, args.gap, device=args.device)
+    print(json.dumps(r), flush=True)
+
+
+if __name__ == "__main__":
+    main()
