@@ -204,7 +204,7 @@ def run_gpu(args, rank, world, local_rank):
     # kernel tiling from the project's autotuner (setup, not timed)
     from wipems_gb300 import autotune
     t_tune = time.perf_counter()
-    best, _ = autotune.tune(cop, stages=(3, 4), xchunks=(4, 8, 16), steps=40, device=local_rank)
+    best, _ = autotune.tune(cop, stages=(3, 4), xchunks=(4, 8, 16), steps=100, device=local_rank)
     setup["autotune_s"] = round(time.perf_counter() - t_tune, 2)
     setup["tiling"] = {"stages": best["stages"], "x_chunk": best["x_chunk"], "tile": "32z x 8y"}
     tiling = dict(stages=best["stages"], x_chunk=best["x_chunk"], kernel=best["kernel"])

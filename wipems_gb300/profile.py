@@ -1,7 +1,7 @@
 """Profiling driver: builds one workload and runs a few timesteps, so that an
 external profiler (ncu) can capture the half-step kernels.
 
-    python -m wipems_gb300.profile --workload l256 --steps 8 [--no-graphs]
+    python -m wipems_gb300.profile --workload l256|p64|d192|l160|b96 --steps 8 [--graphs]
 
 Kernels are launched individually (no CUDA graph) unless --graphs is given,
 so a launch list shows every E / H kernel separately.
@@ -14,13 +14,28 @@ import time
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="l256", choices=["l256", "p64", "d192", "l160"])
+    ap.add_argument("--workload", default="l256", choices=["l256", "p64", "d192", "l160", "b96"])
+    ap.add_argument("--jobs", type=int, default=24, help="b96: number of sweep jobs (seeds 0..jobs-1)")
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--graphs", action="store_true")
     ap.add_argument("--tile-y", type=int, default=0)
     ap.add_argument("--x-chunk", type=int, default=0)
     args = ap.parse_args()
-    from . import CompressedOperator, Engine, Operator, scenes
+    from . import Batch, CompressedOperator, Engine, Operator, scenes
+    if args.workload == "b96":  # batched mode, one step per launch sequence (no graph)
+        t0 = time.perf_counter()
+        cops = [CompressedOperator(Operator(scenes.b96_job(s))) for s in range(args.jobs)]
+        engines = [Engine(c, kernel="tma") for c in cops]
+        b = Batch(engines, x_chunk=args.x_chunk, graph_steps=1)
+        t1 = time.perf_counter()
+        b.iterate(args.steps)
+        st = b.stats()
+        n = st["total_nodes"]
+        print(f"b96[{args.jobs}]: nodes={n} setup={t1 - t0:.2f}s steps={args.steps} device_ms={st['last_ms']:.3f} "
+              f"launches={st['last_launches']} Mcell-updates/s={n * args.steps / (st['last_ms'] / 1e3) / 1e6:.1f} "
+              f"stats={st}")
+        b.close()
+        return
     if args.workload == "l256":
         sc = scenes.l256()
     elif args.workload == "l160":
