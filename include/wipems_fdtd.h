@@ -328,6 +328,16 @@ int fdtd_engine_add_probe(fdtd_engine_t eng, const fdtd_probe_desc* p,
 /* Engine::IterateTS (engine.cpp:255-274). */
 int fdtd_engine_iterate(fdtd_engine_t eng, uint32_t n_steps);
 /* Engine::GetNumberOfTimesteps. */
+/* fdtd_engine_iterate in two halves: _async queues the timesteps on the
+ * engine's own stream and returns; _wait blocks until they are done and
+ * reports their errors (numTS, done and samples are current after it).
+ * Engines on different streams then run concurrently on the GPU; no other
+ * call may touch the engine between the two. */
+int fdtd_engine_iterate_async(fdtd_engine_t eng, uint32_t n_steps);
+int fdtd_engine_wait(fdtd_engine_t eng);
+/* *ready = 1 when no asynchronous iterate is outstanding or it has finished
+ * on the device (fdtd_engine_wait then returns at once). */
+int fdtd_engine_query(fdtd_engine_t eng, int* ready);
 /* 1 once the engine's end criterion (opts.end_crit) stopped it, as of the
  * last iterate; numTS then stays at the stopping timestep. */
 int fdtd_engine_done(fdtd_engine_t eng, int* done);
@@ -450,6 +460,12 @@ typedef struct {
     uint32_t round_steps;         /* timesteps per scheduling round (0 = 128) */
     int      build_workers;       /* concurrent operator builds (0 = auto) */
     int      build_threads_per_job; /* threads per operator build (0 = auto) */
+    uint32_t batch_min_jobs;      /* with at least this many resident jobs,
+                                     advance them as one persistent batch
+                                     (fdtd_batch_*); otherwise (and with 0,
+                                     the default) every job advances through
+                                     its own engine, concurrently on its own
+                                     stream */
     fdtd_batch_opts batch;        /* tiling of the batched kernels */
 } fdtd_server_opts;
 
@@ -476,7 +492,9 @@ typedef struct {
     uint64_t jobs_submitted, jobs_admitted, jobs_done, jobs_failed;
     uint64_t rounds, rebuilds, kernel_launches;
     double   node_steps;      /* sum over finished jobs of nodes x timesteps */
-    double   gpu_ms;          /* device time of all rounds (CUDA events) */
+    double   gpu_ms;          /* time with GPU work in flight: batch rounds by
+                                 CUDA events, concurrent engines by the host
+                                 clock while any has steps queued */
     uint64_t budget_bytes, used_bytes, peak_bytes;
     uint32_t active_jobs;
     int      last_error;

@@ -34,9 +34,11 @@ def _same(e, srv, jid):
     assert np.array_equal(Ia.view(np.uint32), Ib.view(np.uint32))
 
 
-@pytest.mark.parametrize("round_steps,bin_mib", [(64, 0), (37, 1)])
-def test_server_results_same_as_alone(round_steps, bin_mib):
-    srv = Server(round_steps=round_steps, bin_mib=bin_mib, build_workers=2)
+@pytest.mark.parametrize("round_steps,bin_mib,batch_min", [(64, 0, 0), (37, 1, 1), (50, 0, 3)])
+def test_server_results_same_as_alone(round_steps, bin_mib, batch_min):
+    """Concurrent engines (the default), persistent-batch rounds with L2
+    bins, and a mix of both modes all give each job its solo result."""
+    srv = Server(round_steps=round_steps, bin_mib=bin_mib, build_workers=2, batch_min_jobs=batch_min)
     ids = {}
     for seed in (3, 4):
         for k in KINDS:
@@ -58,7 +60,7 @@ def test_server_admission_by_footprint():
     foot = probe.status(j)["footprint"]
     probe.close()
     budget = int(2.5 * foot)
-    srv = Server(hbm_budget=budget, round_steps=50)
+    srv = Server(hbm_budget=budget, round_steps=50, batch_min_jobs=1)  # resident jobs run as a batch
     ids = [srv.submit(scenes.mini("upml", seed=s, nr_ts=NR_TS), end_crit=CRIT, keep_fields=True) for s in range(3, 9)]
     srv.wait(0, timeout=600)
     st = srv.stats()

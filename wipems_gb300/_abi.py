@@ -82,7 +82,8 @@ class FdtdBatchOpts(C.Structure):
 
 class FdtdServerOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("hbm_budget", C.c_uint64), ("max_active", u32), ("round_steps", u32),
-                ("build_workers", C.c_int), ("build_threads_per_job", C.c_int), ("batch", FdtdBatchOpts)]
+                ("build_workers", C.c_int), ("build_threads_per_job", C.c_int), ("batch_min_jobs", u32),
+                ("batch", FdtdBatchOpts)]
 
 
 class FdtdJobOpts(C.Structure):
@@ -152,6 +153,9 @@ SIGNATURES = [
     ("fdtd_engine_destroy", C.c_int, [_P]),
     ("fdtd_engine_add_probe", C.c_int, [_P, C.POINTER(FdtdProbeDesc), PU32]),
     ("fdtd_engine_iterate", C.c_int, [_P, u32]),
+    ("fdtd_engine_iterate_async", C.c_int, [_P, u32]),
+    ("fdtd_engine_wait", C.c_int, [_P]),
+    ("fdtd_engine_query", C.c_int, [_P, C.POINTER(C.c_int)]),
     ("fdtd_engine_done", C.c_int, [_P, C.POINTER(C.c_int)]),
     ("fdtd_engine_num_timesteps", C.c_int, [_P, PU32]),
     ("fdtd_engine_num_samples", C.c_int, [_P, PU32]),

@@ -735,7 +735,33 @@ int fdtd_engine_add_probe(fdtd_engine_t e, const fdtd_probe_desc* p, uint32_t* s
 }
 
 int fdtd_engine_iterate(fdtd_engine_t e, uint32_t n) {
+    const int rc = fdtd_engine_iterate_async(e, n);
+    if (rc) return rc;
+    return fdtd_engine_wait(e);
+}
+
+int fdtd_engine_wait(fdtd_engine_t e) {
     if (!e) return FDTD_ERR_ARG;
+    if (!e->pending) return FDTD_OK;
+    CK(cudaSetDevice(e->device));
+    e->pending = false;
+    CK(cudaEventSynchronize(e->ev1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+    e->last_ms = ms;
+    return check_error_word(e);
+}
+
+int fdtd_engine_iterate_async(fdtd_engine_t e, uint32_t n) {
+    if (!e) return FDTD_ERR_ARG;
+    if (e->pending) {
+        set_error("fdtd_engine_iterate_async: the previous asynchronous iterate was not waited for");
+        return FDTD_ERR_STATE;
+    }
+    if (e->end_crit > 0) {  // a stopped job stays stopped; never step past the timestep cap
+        if (e->done || e->ts >= e->stop_ts) n = 0;
+        else n = std::min(n, e->stop_ts - e->ts);
+    }
     CK(cudaSetDevice(e->device));
     e->last_launches = 0;
     int rc;
@@ -757,11 +783,28 @@ int fdtd_engine_iterate(fdtd_engine_t e, uint32_t n) {
         left -= 1;
     }
     CK(cudaEventRecord(e->ev1, e->stream));
-    CK(cudaEventSynchronize(e->ev1));
-    float ms = 0;
-    CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
-    e->last_ms = ms;
-    return check_error_word(e);
+    e->pending = true;
+    return FDTD_OK;
+}
+
+int fdtd_engine_query(fdtd_engine_t e, int* ready) {
+    if (!e || !ready) return FDTD_ERR_ARG;
+    if (!e->pending) {
+        *ready = 1;
+        return FDTD_OK;
+    }
+    CK(cudaSetDevice(e->device));
+    const cudaError_t q = cudaEventQuery(e->ev1);
+    if (q == cudaErrorNotReady) {
+        *ready = 0;
+        return FDTD_OK;
+    }
+    if (q != cudaSuccess) {
+        set_error(std::string("fdtd_engine_query: ") + cudaGetErrorString(q));
+        return FDTD_ERR_CUDA;
+    }
+    *ready = 1;
+    return FDTD_OK;
 }
 
 int fdtd_engine_done(fdtd_engine_t e, int* done) {

@@ -91,6 +91,7 @@ struct fdtd_engine_s {
     uint32_t interval = 0;
     bool energy_on_probe = true;
     bool use_graphs = true;
+    bool pending = false;    // an asynchronous iterate was launched, not yet waited for
     double end_crit = 0;     // > 0: stop on the device (energy decay or stop_ts)
     uint32_t stop_ts = 0;
     bool done = false;       // as of the last control-word read

@@ -12,10 +12,14 @@
 //   admit   built jobs in arrival order while their device footprint fits
 //           the HBM budget and the active-job cap (first fit: a large job
 //           that does not fit yet does not block smaller ones behind it);
-//   batch   on any change of the active set, a new batch over the active
-//           engines (fdtd_batch_create) replaces the old one;
-//   step    fdtd_batch_iterate(round_steps): one persistent kernel per
-//           half-step and kernel variant over every active job's tiles.
+//   batch   (batch mode) on any change of the active set, a new batch over
+//           the active engines (fdtd_batch_create) replaces the old one;
+//   step    every idle resident job gets its next round_steps queued on
+//           its own stream (fdtd_engine_iterate_async), so the GPU overlaps
+//           all of them and a job that finishes is picked up, retired and
+//           replaced without waiting for the others; or, with
+//           batch_min_jobs set and at least that many jobs resident, one
+//           persistent batch round (fdtd_batch_iterate) over all of them.
 //
 // Jobs stop on the device at exactly the timestep they would stop at when
 // run alone (the kernels of a stopped job do nothing for the rest of the
@@ -242,7 +246,7 @@ int admit(fdtd_server_s* s, Job* j) {
     o.device = s->opts.device;
     o.max_timesteps = j->max_ts;
     o.probe_interval = j->interval;
-    o.use_graphs = 0;  // the batch replays its own graphs
+    o.use_graphs = 1;  // interval graphs for rounds a job runs on its own
     o.kernel = 3;      // batched jobs run the two-pass kernels
     o.energy_on_probe = 1;
     o.end_crit = j->opts.end_crit;
@@ -270,13 +274,71 @@ int admit(fdtd_server_s* s, Job* j) {
     return FDTD_OK;
 }
 
+// One persistent-batch round over all resident jobs (batch mode).
+void batch_round(fdtd_server_s* s, bool changed) {
+    if (changed || !s->batch) {
+        if (s->batch) fdtd_batch_destroy(s->batch);
+        s->batch = nullptr;
+        std::vector<fdtd_engine_t> es;
+        for (Job* j : s->active) es.push_back(j->eng);
+        const int rc = fdtd_batch_create(es.data(), (uint32_t)es.size(), &s->opts.batch, &s->batch);
+        std::lock_guard<std::mutex> lock(s->mu);
+        s->st.rebuilds++;
+        if (rc) {
+            s->batch = nullptr;
+            s->st.last_error = rc;
+        }
+    }
+    int rc = s->batch ? fdtd_batch_iterate(s->batch, s->opts.round_steps) : FDTD_ERR_STATE;
+    if (s->batch) {
+        fdtd_batch_stats bs{};
+        fdtd_batch_info(s->batch, &bs);
+        std::lock_guard<std::mutex> lock(s->mu);
+        s->st.rounds++;
+        s->st.gpu_ms += bs.last_ms;
+        s->st.kernel_launches += bs.last_launches;
+    }
+    if (rc) {
+        // find the failing jobs: each engine decodes its own error word
+        const std::string msg = last_error();
+        std::vector<Job*> ok;
+        for (Job* j : s->active) {
+            const int jr = s->batch ? fdtd_engine_iterate(j->eng, 0) : rc;
+            if (jr) retire(s, j, jr, s->batch ? last_error() : msg);
+            else ok.push_back(j);
+        }
+        if (ok.size() == s->active.size()) {  // not attributable to a job: fail them all
+            for (Job* j : ok) retire(s, j, rc, msg);
+            ok.clear();
+        }
+        s->active.swap(ok);
+        if (s->batch) fdtd_batch_destroy(s->batch);
+        s->batch = nullptr;
+    }
+}
+
 void gpu_loop(fdtd_server_s* s) {
     cudaSetDevice(s->opts.device);
+    Clock::time_point busy_since{};
+    bool busy = false;
     for (;;) {
         bool changed = false;
-        // retire
+        // collect finished work, retire jobs whose end criterion fired
         std::vector<Job*> keep;
+        bool any_pending = false;
         for (Job* j : s->active) {
+            int ready = 1;
+            if (fdtd_engine_query(j->eng, &ready) == FDTD_OK && !ready) {
+                keep.push_back(j);
+                any_pending = true;
+                continue;
+            }
+            const int rc = fdtd_engine_wait(j->eng);
+            if (rc) {
+                retire(s, j, rc, last_error());
+                changed = true;
+                continue;
+            }
             int done = 0;
             fdtd_engine_done(j->eng, &done);
             if (done) {
@@ -291,6 +353,10 @@ void gpu_loop(fdtd_server_s* s) {
         std::vector<Job*> take;
         {
             std::unique_lock<std::mutex> lock(s->mu);
+            if (busy && !any_pending) {  // time with concurrent-engine work in flight
+                s->st.gpu_ms += std::chrono::duration<double, std::milli>(Clock::now() - busy_since).count();
+                busy = false;
+            }
             if (s->active.empty() && s->ready.empty()) {
                 if (s->batch) {
                     lock.unlock();
@@ -299,6 +365,11 @@ void gpu_loop(fdtd_server_s* s) {
                     lock.lock();
                 }
                 s->cv_gpu.wait(lock, [&] { return s->stop || !s->ready.empty(); });
+            } else if (any_pending && !changed && s->ready.empty()) {
+                // every resident job is busy: sleep until a new job is built
+                // or a short poll interval has passed
+                s->cv_gpu.wait_for(lock, std::chrono::microseconds(50),
+                                   [&] { return s->stop || !s->ready.empty(); });
             }
             if (s->stop) break;
             std::vector<Job*> rest;
@@ -325,50 +396,69 @@ void gpu_loop(fdtd_server_s* s) {
             s->st.active_jobs = (uint32_t)s->active.size();
         }
         if (s->active.empty()) continue;
-        if (changed || !s->batch) {
-            if (s->batch) fdtd_batch_destroy(s->batch);
-            s->batch = nullptr;
-            std::vector<fdtd_engine_t> es;
-            for (Job* j : s->active) es.push_back(j->eng);
-            const int rc = fdtd_batch_create(es.data(), (uint32_t)es.size(), &s->opts.batch, &s->batch);
-            std::lock_guard<std::mutex> lock(s->mu);
-            s->st.rebuilds++;
-            if (rc) {
-                s->batch = nullptr;
-                s->st.last_error = rc;
-            }
-        }
-        int rc = s->batch ? fdtd_batch_iterate(s->batch, s->opts.round_steps) : FDTD_ERR_STATE;
-        if (s->batch) {
-            fdtd_batch_stats bs{};
-            fdtd_batch_info(s->batch, &bs);
-            std::lock_guard<std::mutex> lock(s->mu);
-            s->st.rounds++;
-            s->st.gpu_ms += bs.last_ms;
-            s->st.kernel_launches += bs.last_launches;
-        }
-        if (rc) {
-            // find the failing jobs: each engine decodes its own error word
-            const std::string msg = last_error();
-            std::vector<Job*> ok;
+        const bool batch_mode = s->opts.batch_min_jobs > 0 && s->active.size() >= s->opts.batch_min_jobs;
+        if (batch_mode) {
+            // a batch needs every engine idle
+            bool idle = true;
             for (Job* j : s->active) {
-                const int jr = s->batch ? fdtd_engine_iterate(j->eng, 0) : rc;
-                if (jr) retire(s, j, jr, s->batch ? last_error() : msg);
-                else ok.push_back(j);
+                int ready = 1;
+                if (fdtd_engine_query(j->eng, &ready) == FDTD_OK && !ready) idle = false;
             }
-            if (ok.size() == s->active.size()) {  // not attributable to a job: fail them all
-                for (Job* j : ok) retire(s, j, rc, msg);
-                ok.clear();
-            }
-            s->active.swap(ok);
-            if (s->batch) fdtd_batch_destroy(s->batch);
+            if (!idle) continue;  // collected on the next pass
+            batch_round(s, changed);
+            continue;
+        }
+        // concurrent engines: every idle job gets its next round_steps
+        // queued on its own stream at once; finished jobs are picked up on
+        // the next pass, so short and long jobs never wait for each other
+        if (s->batch) {
+            fdtd_batch_destroy(s->batch);
             s->batch = nullptr;
+        }
+        std::vector<Job*> ok;
+        uint64_t launches = 0;
+        bool launched = false;
+        for (Job* j : s->active) {
+            int ready = 1;
+            if (fdtd_engine_query(j->eng, &ready) == FDTD_OK && !ready) {
+                ok.push_back(j);
+                continue;
+            }
+            int rc = fdtd_engine_wait(j->eng);  // collects steps that finished since the pass above
+            int done = 0;
+            if (!rc) fdtd_engine_done(j->eng, &done);
+            if (!rc && done) {
+                retire(s, j, FDTD_OK, "");
+                continue;
+            }
+            if (!rc) rc = fdtd_engine_iterate_async(j->eng, s->opts.round_steps);
+            if (rc) {
+                retire(s, j, rc, last_error());
+                continue;
+            }
+            double ms = 0;
+            uint64_t l = 0;
+            fdtd_engine_last_timing(j->eng, &ms, &l);
+            launches += l;
+            launched = true;
+            ok.push_back(j);
+        }
+        s->active.swap(ok);
+        std::lock_guard<std::mutex> lock(s->mu);
+        if (launched) {
+            s->st.rounds++;
+            s->st.kernel_launches += launches;
+            if (!busy) {
+                busy = true;
+                busy_since = Clock::now();
+            }
         }
     }
     // shutdown: free what is still resident
     if (s->batch) fdtd_batch_destroy(s->batch);
     s->batch = nullptr;
     for (Job* j : s->active) {
+        fdtd_engine_wait(j->eng);
         fdtd_engine_destroy(j->eng);
         j->eng = nullptr;
     }

@@ -307,6 +307,13 @@ class Engine:
     def iterate(self, n: int):
         check(lib().fdtd_engine_iterate(self._h, int(n)), "fdtd_engine_iterate")
 
+    def iterate_async(self, n: int):
+        """Queues n timesteps on the engine's stream and returns (wait())."""
+        check(lib().fdtd_engine_iterate_async(self._h, int(n)), "fdtd_engine_iterate_async")
+
+    def wait(self):
+        check(lib().fdtd_engine_wait(self._h), "fdtd_engine_wait")
+
     @property
     def done(self) -> bool:
         """True once the device end criterion (end_crit) stopped the job."""
@@ -439,7 +446,7 @@ class Server:
 
     def __init__(self, device: int = 0, hbm_budget: int = 0, max_active: int = 0, round_steps: int = 0,
                  build_workers: int = 0, build_threads_per_job: int = 0, x_chunk: int = 0, stages: int = 0,
-                 blocks_per_sm: int = 0, graph_steps: int = 0, bin_mib: int = 0):
+                 blocks_per_sm: int = 0, graph_steps: int = 0, bin_mib: int = 0, batch_min_jobs: int = 0):
         o = _abi.FdtdServerOpts()
         o.device = device
         o.hbm_budget = int(hbm_budget)
@@ -447,6 +454,7 @@ class Server:
         o.round_steps = int(round_steps)
         o.build_workers = int(build_workers)
         o.build_threads_per_job = int(build_threads_per_job)
+        o.batch_min_jobs = int(batch_min_jobs)
         o.batch = _abi.FdtdBatchOpts(int(x_chunk), int(stages), int(blocks_per_sm), int(graph_steps), int(bin_mib))
         h = C.c_void_p()
         check(lib().fdtd_server_create(C.byref(o), C.byref(h)), "fdtd_server_create")

@@ -70,16 +70,30 @@ def b96(n_jobs: int = 96, timesteps: int = 1500, device: int = 0) -> dict:
     b.close()
     for e in engines:
         e.close()
+    # the same jobs as concurrent plain engines (one stream each)
+    engines = [Engine(c, device=device, max_timesteps=timesteps) for c in cops]
+    for e in engines:
+        e.iterate(0)  # uploads done, first sample taken
+    t0 = time.perf_counter()
+    for e in engines:
+        e.iterate_async(timesteps)
+    for e in engines:
+        e.wait()
+    conc_s = time.perf_counter() - t0
+    for e in engines:
+        e.close()
     plain = work / (plain_ms / 1e3) / 1e6
     batched = work / (st["last_ms"] / 1e3) / 1e6
     return dict(workload="b96", jobs=n_jobs, timesteps=timesteps, nodes=sum(nodes), setup_s=round(setup, 2),
                 plain_ms=plain_ms, plain_mcells=plain, batched_ms=st["last_ms"], batched_mcells=batched,
-                speedup=batched / plain, tiling=best, groups=st["num_groups"], work_items=st["work_items"],
+                speedup=batched / plain, concurrent_wall_s=conc_s, concurrent_mcells=work / conc_s / 1e6,
+                tiling=best, groups=st["num_groups"], work_items=st["work_items"],
                 persistent_blocks=st["persistent_blocks"], launches=st["last_launches"])
 
 
 def serve(n_jobs: int = 48, mean_gap: float = 0.02, end_crit: float = 1e-4, seed: int = 777, device: int = 0,
-          round_steps: int = 128, modes=("served", "plain")) -> dict:
+          round_steps: int = 128, modes=("served", "plain"), batch_min_jobs: int = 0,
+          build_workers: int = 0) -> dict:
     """S: a seeded Poisson stream of serve_job requests (operator build
     included), through the continuous-batching server and one at a time
     through the plain engine.  Both stop every job at -40 dB energy or its
@@ -88,14 +102,16 @@ def serve(n_jobs: int = 48, mean_gap: float = 0.02, end_crit: float = 1e-4, seed
     rng = np.random.default_rng(seed)
     arr = np.cumsum(rng.exponential(mean_gap, n_jobs))
     arr -= arr[0]
-    out = dict(workload="serve", jobs=n_jobs, mean_gap_s=mean_gap, end_crit=end_crit, seed=seed)
+    out = dict(workload="serve", jobs=n_jobs, mean_gap_s=mean_gap, end_crit=end_crit, seed=seed,
+               round_steps=round_steps, batch_min_jobs=batch_min_jobs)
 
     def pct(a, q):
         return float(np.percentile(np.asarray(a), q))
 
     ts_served = ts_plain = None
     if "served" in modes:
-        srv = Server(device=device, round_steps=round_steps)
+        srv = Server(device=device, round_steps=round_steps, batch_min_jobs=batch_min_jobs,
+                     build_workers=build_workers)
         t0 = time.perf_counter()
         ids = []
         for k in range(n_jobs):
@@ -151,13 +167,19 @@ def main():
     ap.add_argument("--timesteps", type=int, default=0)
     ap.add_argument("--gap", type=float, default=0.02)
     ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--batch-min", type=int, default=0,
+                    help="serve: run the persistent batch with at least this many resident jobs (0 = never)")
+    ap.add_argument("--served-only", action="store_true")
+    ap.add_argument("--workers", type=int, default=0, help="serve: host build workers (0 = the server's default)")
     args = ap.parse_args()
     if args.workload in ("p64", "d192"):
         r = single(args.workload, args.timesteps, args.device)
     elif args.workload == "b96":
         r = b96(args.jobs or 96, args.timesteps or 1500, args.device)
     else:
-        r = serve(args.jobs or 48, args.gap, device=args.device)
+        r = serve(args.jobs or 48, args.gap, device=args.device, batch_min_jobs=args.batch_min,
+                  build_workers=args.workers,
+                  modes=("served",) if args.served_only else ("served", "plain"))
     print(json.dumps(r), flush=True)
 
 
