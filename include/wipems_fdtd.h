@@ -126,6 +126,28 @@ int fdtd_scene_add_probe(fdtd_scene_t s, int type,
                          const double start[3], const double stop[3],
                          double weight, int norm_dir);
 
+/* openEMS XML input (openEMS::ParseFDTDSetup, openems.cpp:756-936, and the
+ * CSXCAD <ContinuousStructure> it embeds), the subset this engine covers:
+ * <FDTD NumberOfTimesteps endCriteria OverSampling> with a Gaussian
+ * <Excitation Type="0"> and <BoundaryCond> (PEC / PMC / PML_n or codes);
+ * <RectilinearGrid DeltaUnit> with X/Y/ZLines; <BackgroundMaterial>; the
+ * properties Material, Metal, LumpedElement (R, C, caps), Excitation,
+ * ProbeBox (voltage / current) and LorentzMaterial (order 1), each with
+ * <Box Priority><P1/><P2/></Box> primitives.  Other content that changes
+ * the simulation is refused with FDTD_ERR_UNSUPPORTED naming it; field
+ * dumps and field probes are skipped (counted in `skipped`). */
+typedef struct {
+    uint32_t nr_ts;           /* NumberOfTimesteps */
+    double   end_crit;        /* endCriteria (0 in the file -> 1e-6) */
+    uint32_t oversampling;    /* OverSampling (0 = default) */
+    int      excite_type;     /* <Excitation Type> */
+    double   f0, fc;          /* Gaussian pulse */
+    uint32_t num_properties, num_boxes, num_probes, skipped;
+} fdtd_xml_info;
+
+int fdtd_scene_load_xml(const char* xml_text, fdtd_scene_t* out, fdtd_xml_info* info);
+int fdtd_scene_load_xml_file(const char* path, fdtd_scene_t* out, fdtd_xml_info* info);
+
 /* ---------------------------------------------------------------- operator */
 
 typedef struct fdtd_operator_s* fdtd_operator_t;

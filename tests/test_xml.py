@@ -1,0 +1,102 @@
+"""openEMS XML input: a document in the front ends' format builds the same
+operator as the same scene made through the scene API, and content outside
+the covered subset is refused by name."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from wipems_gb300 import BC_PEC, BC_PMC, BC_PML, CompressedOperator, Operator, Scene
+from wipems_gb300._abi import FdtdError
+
+GOLDEN = Path(__file__).parent / "golden"
+
+
+def _lines():
+    x = np.arange(0, 12.01, 0.5)
+    y = np.array([0, 1, 2, 3] + list(np.arange(3.5, 11.6, 0.5)) + [12, 13, 14, 15, 16], float)
+    z = np.arange(0, 8.01, 0.5)
+    return x, y, z
+
+
+def _api_scene():
+    s = Scene(*_lines(), 1e-3)
+    s.set_boundary([BC_PML, BC_PML, BC_PML, BC_PML, BC_PEC, BC_PMC], [8, 8, 8, 6, 0, 0])
+    s.set_gauss_excite(10e9, 5e9, 600)
+    s.set_oversampling(4)
+    s.add_material([2, 3.5, 1], [9.5, 12, 6], eps_r=3.66, kappa=0.01, priority=10)
+    s.add_metal([3, 4, 6], [8, 11, 6], priority=20)
+    s.add_lumped([6, 7.5, 1], [6.5, 8, 6], 2, R=50.0, caps=True, priority=5)
+    s.add_excitation([6, 7.5, 1], [6.5, 8, 6], [0, 0, -1], exc_type=0, priority=5)
+    s.add_probe([6.25, 7.75, 1], [6.25, 7.75, 6], 0, weight=-1.0)
+    s.add_probe([6, 7.5, 3.5], [6.5, 8, 3.5], 1, weight=1.0, norm_dir=2)
+    return s
+
+
+def _same_operator(a: Operator, b: Operator):
+    assert a.num_lines == b.num_lines
+    assert a.dT == b.dT and a.probe_interval == b.probe_interval
+    for x, y in zip(a.coefficients(), b.coefficients()):
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+    assert len(a.probes) == len(b.probes)
+    for p, q in zip(a.probes, b.probes):
+        assert bytes(p) == bytes(q)
+    ea, eb = a.excitation(), b.excitation()
+    for k in ea:
+        assert np.array_equal(np.asarray(ea[k]), np.asarray(eb[k])), k
+    for x, y in zip(a.signals(), b.signals()):
+        assert np.array_equal(x, y)
+    ca, cb = CompressedOperator(a, mode="exact"), CompressedOperator(b, mode="exact")
+    assert ca.info["num_tuples_e"] == cb.info["num_tuples_e"] and ca.info["num_upml_nodes"] == cb.info["num_upml_nodes"]
+    for x, y in zip(ca.expand(), cb.expand()):  # applied coefficients and per-node UPML / ADE / excitation flags
+        assert np.array_equal(x, y)
+
+
+def test_xml_document_builds_the_api_operator():
+    sx = Scene.from_xml(str(GOLDEN / "port_box.xml"))
+    info = sx.xml_info
+    assert info["nr_ts"] == 600 and info["end_crit"] == 1e-5 and info["excite_type"] == 0
+    assert info["num_probes"] == 2 and info["skipped"] == 1  # the field dump
+    _same_operator(Operator(sx), Operator(_api_scene()))
+
+
+def test_xml_text_and_lorentz_material():
+    text = (GOLDEN / "port_box.xml").read_text()
+    text = text.replace(
+        '<Metal ID="1" Name="plate">',
+        '<LorentzMaterial ID="7" Name="drude" Order="1"><Primitives><Box Priority="15">'
+        '<P1 X="4" Y="5" Z="2"/><P2 X="7" Y="9" Z="4"/></Box></Primitives>'
+        '<Property Epsilon="2" EpsilonPlasmaFrequency="5e9" EpsilonRelaxTime="1e-9" '
+        'EpsilonLorPoleFrequency="0"/></LorentzMaterial>\n      <Metal ID="1" Name="plate">')
+    sx = Scene.from_xml(text)
+    s = _api_scene()
+    s.add_lorentz([4, 5, 2], [7, 9, 4], eps_r=2.0, plasma_f=[5e9], relax_t=[1e-9], pole_f=[0.0], priority=15)
+    _same_operator(Operator(sx), Operator(s))
+
+
+@pytest.mark.parametrize("edit,needle", [
+    (('<Box Priority="20">', '<Cylinder Priority="20" Radius="1">'), "Cylinder"),
+    (('ymin="3"', 'ymin="MUR"'), "Mur"),
+    (('<Excitation Type="0" f0="1e+10"', '<Excitation Type="1" f0="1e+10"'), "excitation Type 1"),
+    (('Epsilon="3.66"', 'Epsilon="3.66,3.66,4"'), "anisotropic"),
+    (('<Weight Epsilon="1"', '<Weight Epsilon="2*x"'), "weighting"),
+    (('<Metal ID="1" Name="plate">', '<ConductingSheet ID="1" Name="plate">'), "ConductingSheet"),
+])
+def test_xml_refuses_uncovered_content(edit, needle):
+    text = (GOLDEN / "port_box.xml").read_text().replace(*edit)
+    if needle == "Cylinder":
+        text = text.replace('</Box>\n        </Primitives>\n      </Metal>', '</Cylinder>\n        </Primitives>\n      </Metal>')
+    if needle == "ConductingSheet":
+        text = text.replace("</Metal>", "</ConductingSheet>")
+    with pytest.raises(FdtdError) as ei:
+        Scene.from_xml(text)
+    assert ei.value.code == -5, str(ei.value)
+    assert needle.lower() in str(ei.value).lower()
+
+
+def test_xml_malformed_documents():
+    for text in ("<openEMS><FDTD></openEMS>", "<notopenEMS/>", "<openEMS><FDTD/></openEMS>",
+                 "<openEMS><FDTD a=1/></openEMS>"):
+        with pytest.raises(FdtdError) as ei:
+            Scene.from_xml(text)
+        assert ei.value.code == -1

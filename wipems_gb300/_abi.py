@@ -80,6 +80,12 @@ class FdtdBatchOpts(C.Structure):
                 ("bin_mib", C.c_int)]
 
 
+class FdtdXmlInfo(C.Structure):
+    _fields_ = [("nr_ts", u32), ("end_crit", C.c_double), ("oversampling", u32), ("excite_type", C.c_int),
+                ("f0", C.c_double), ("fc", C.c_double), ("num_properties", u32), ("num_boxes", u32),
+                ("num_probes", u32), ("skipped", u32)]
+
+
 class FdtdServerOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("hbm_budget", C.c_uint64), ("max_active", u32), ("round_steps", u32),
                 ("build_workers", C.c_int), ("build_threads_per_job", C.c_int), ("batch_min_jobs", u32),
@@ -168,6 +174,8 @@ SIGNATURES = [
     ("fdtd_engine_last_timing", C.c_int, [_P, PD, C.POINTER(C.c_uint64)]),
     ("fdtd_engine_profile_kernels", C.c_int, [_P, u32, PD, PD]),
     ("fdtd_field_energy_static", C.c_int, [_P, _P, PU32, u32, _P, _P]),
+    ("fdtd_scene_load_xml", C.c_int, [C.c_char_p, C.POINTER(_P), C.POINTER(FdtdXmlInfo)]),
+    ("fdtd_scene_load_xml_file", C.c_int, [C.c_char_p, C.POINTER(_P), C.POINTER(FdtdXmlInfo)]),
     ("fdtd_batch_create", C.c_int, [C.POINTER(_P), u32, C.POINTER(FdtdBatchOpts), C.POINTER(_P)]),
     ("fdtd_batch_iterate", C.c_int, [_P, u32]),
     ("fdtd_batch_info", C.c_int, [_P, C.POINTER(FdtdBatchStats)]),

@@ -23,7 +23,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread", "-I/usr/local/cuda/include"]
 
 CU_SOURCES = ["engine.cu", "energy_static.cu", "batch.cu"]
-CXX_SOURCES = ["operator.cpp", "compress.cpp", "server.cpp"]
+CXX_SOURCES = ["operator.cpp", "compress.cpp", "server.cpp", "xml_scene.cpp"]
 
 
 def _nvcc() -> str:

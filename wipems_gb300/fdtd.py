@@ -50,6 +50,28 @@ class Scene:
         self.probes: list[dict] = []
         self.meta: dict = {}
 
+    @classmethod
+    def from_xml(cls, xml: str) -> "Scene":
+        """A scene from an openEMS XML document (the text, or a path to the
+        file): the subset fdtd_scene_load_xml covers.  The run settings are
+        in .xml_info (nr_ts, end_crit, ...)."""
+        h = C.c_void_p()
+        inf = _abi.FdtdXmlInfo()
+        if "<" in xml:
+            check(lib().fdtd_scene_load_xml(xml.encode(), C.byref(h), C.byref(inf)), "fdtd_scene_load_xml")
+        else:
+            check(lib().fdtd_scene_load_xml_file(str(xml).encode(), C.byref(h), C.byref(inf)),
+                  "fdtd_scene_load_xml_file")
+        s = cls.__new__(cls)
+        s._h = h
+        s._lines = None
+        s.unit = None
+        s.nr_ts = int(inf.nr_ts)
+        s.probes = []
+        s.meta = {}
+        s.xml_info = {k: getattr(inf, k) for k, _ in inf._fields_}
+        return s
+
     @property
     def lines(self):
         return self._lines
