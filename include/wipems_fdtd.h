@@ -360,6 +360,19 @@ int fdtd_engine_wait(fdtd_engine_t eng);
 /* *ready = 1 when no asynchronous iterate is outstanding or it has finished
  * on the device (fdtd_engine_wait then returns at once). */
 int fdtd_engine_query(fdtd_engine_t eng, int* ready);
+/* Frequency-domain probe accumulation on the device (ProcessIntegral::
+ * Process, processintegral.cpp:154-168): on every timestep that is a
+ * multiple of fd_interval (ts = 0 included), every probe's integral v
+ * (weighted) is added as v * exp(-2 pi i f t) * 2 dT fd_interval for each
+ * frequency f, t = numTS * dT (current probes: (numTS + 0.5) * dT).  The
+ * reference's interval is Processing::AddFrequency's (processing.cpp:150-
+ * 170): the operator's Nyquist number, lowered to CalcNyquistNum(f, dT) of
+ * any higher frequency.  Set before the first iterate; not available in
+ * batches.  read_fd returns [probe][frequency][re, im] and the number of
+ * accumulated samples. */
+int fdtd_engine_set_fd(fdtd_engine_t eng, const double* freqs, uint32_t nfreq,
+                       uint32_t fd_interval);
+int fdtd_engine_read_fd(fdtd_engine_t eng, double* re_im, uint32_t* samples);
 /* 1 once the engine's end criterion (opts.end_crit) stopped it, as of the
  * last iterate; numTS then stays at the stopping timestep. */
 int fdtd_engine_done(fdtd_engine_t eng, int* done);

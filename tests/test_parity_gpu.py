@@ -29,6 +29,8 @@ def compare(op, eng, ref, bitwise=True):
     assert np.array_equal(s.ts, ref["ts"]), (s.ts[:5], ref["ts"][:5])
     for p in range(s.values.shape[1]):
         assert rel_l2(s.values[:, p], ref["values"][:, p]) <= PROBE_TOL, p
+    if bitwise:  # the probe sums run in the reference's order and precision
+        assert np.array_equal(s.values, ref["values"])
     e_ok = ref["energy"] > 0
     if e_ok.any():
         assert np.max(np.abs(s.energy[e_ok] / ref["energy"][e_ok] - 1)) < 1e-6

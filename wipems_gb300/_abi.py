@@ -162,6 +162,8 @@ SIGNATURES = [
     ("fdtd_engine_iterate_async", C.c_int, [_P, u32]),
     ("fdtd_engine_wait", C.c_int, [_P]),
     ("fdtd_engine_query", C.c_int, [_P, C.POINTER(C.c_int)]),
+    ("fdtd_engine_set_fd", C.c_int, [_P, PD, u32, u32]),
+    ("fdtd_engine_read_fd", C.c_int, [_P, PD, PU32]),
     ("fdtd_engine_done", C.c_int, [_P, C.POINTER(C.c_int)]),
     ("fdtd_engine_num_timesteps", C.c_int, [_P, PU32]),
     ("fdtd_engine_num_samples", C.c_int, [_P, PU32]),

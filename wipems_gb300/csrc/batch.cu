@@ -281,6 +281,10 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
             set_error("fdtd_batch_create: jobs must use the two-pass TMA kernels");
             return FDTD_ERR_ARG;
         }
+        if (e->fd_interval) {
+            set_error("fdtd_batch_create: frequency-domain accumulation is not provided in batches");
+            return FDTD_ERR_UNSUPPORTED;
+        }
         for (uint32_t k = 0; k < j; ++k)
             if (engines[k] == e) {
                 set_error("fdtd_batch_create: a job appears twice");

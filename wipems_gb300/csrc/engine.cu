@@ -158,6 +158,15 @@ int launch_advance(fdtd_engine_s* e, int adv, bool sample, bool energy_valid) {
     return check_launch();
 }
 
+// frequency-domain accumulation at numTS = ts (after the step that reached it)
+int launch_fd(fdtd_engine_s* e, uint32_t ts) {
+    if (!e->fd_interval || e->h_freq.empty() || e->ps.nprobe == 0) return FDTD_OK;
+    const size_t sm = std::max<size_t>(8, (size_t)e->ps.nprobe * sizeof(double));
+    k_fd_accumulate<<<1, 256, sm, e->stream>>>(e->p_ts(), (int)ts, e->ps, e->g, e->fd);
+    e->last_launches += 1;
+    return check_launch();
+}
+
 // ------------------------------------------------------------------ probes
 int upload_probes(fdtd_engine_s* e) {
     if (e->probes_uploaded) return FDTD_OK;
@@ -187,6 +196,23 @@ int upload_probes(fdtd_engine_s* e) {
     e->ps.d_done = e->p_done();
     e->ps.end_crit = e->end_crit;
     e->ps.stop_ts = e->end_crit > 0 ? (int)e->stop_ts : 0;
+    if (e->fd_interval && !e->h_freq.empty() && np) {
+        const size_t nf = e->h_freq.size();
+        if ((rc = e->d_freq.alloc(nf, e->device_bytes)) || (rc = e->d_fd.alloc(2 * np * nf, e->device_bytes)) ||
+            (rc = e->d_fd_dual.alloc(np, e->device_bytes)) || (rc = e->d_fd_count.alloc(1, e->device_bytes)))
+            return rc;
+        CK(cudaMemcpyAsync(e->d_freq.p, e->h_freq.data(), nf * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+        CK(cudaMemcpyAsync(e->d_fd_dual.p, e->h_dual.data(), np * sizeof(int), cudaMemcpyHostToDevice, e->stream));
+        CK(cudaMemsetAsync(e->d_fd.p, 0, 2 * np * nf * sizeof(double), e->stream));
+        CK(cudaMemsetAsync(e->d_fd_count.p, 0, sizeof(int), e->stream));
+        e->fd.nfreq = (int)nf;
+        e->fd.freq = e->d_freq.p;
+        e->fd.acc = e->d_fd.p;
+        e->fd.dual = e->d_fd_dual.p;
+        e->fd.dT = e->dT;
+        e->fd.scale = 2.0 * e->dT * (double)e->fd_interval;
+        e->fd.count = e->d_fd_count.p;
+    }
     e->probes_uploaded = true;
     return FDTD_OK;
 }
@@ -232,6 +258,7 @@ int start(fdtd_engine_s* e) {
         if (e->interval) {  // sample at ts = 0 (RunFDTD's PA->Process() before the loop)
             if ((rc = launch_advance(e, 0, true, e->energy_on_probe))) return rc;
         }
+        if ((rc = launch_fd(e, 0))) return rc;  // 0 % FD_interval == 0
     }
     return FDTD_OK;
 }
@@ -413,6 +440,8 @@ int reset_state(fdtd_engine_s* e) {
     for (DevBuf<float>* b : {&e->V, &e->I, &e->FV, &e->FI, &e->AV, &e->LV, &e->AI, &e->LI, &e->V2, &e->I2, &e->FV2})
         if (b->p) CK(cudaMemsetAsync(b->p, 0, F, s));
     CK(cudaMemsetAsync(e->ctl.p, 0, 4 * sizeof(int), s));
+    if (e->d_fd.p) CK(cudaMemsetAsync(e->d_fd.p, 0, e->d_fd.n * sizeof(double), s));
+    if (e->d_fd_count.p) CK(cudaMemsetAsync(e->d_fd_count.p, 0, sizeof(int), s));
     CK(cudaMemsetAsync(e->d_eacc.p, 0, 4 * sizeof(double), s));
     e->ts = 0;
     e->done = false;
@@ -730,6 +759,7 @@ int fdtd_engine_add_probe(fdtd_engine_t e, const fdtd_probe_desc* p, uint32_t* s
     e->h_entries.insert(e->h_entries.end(), ent.begin(), ent.end());
     e->h_first.push_back((int)e->h_entries.size());
     e->h_weight.push_back(p->weight);
+    e->h_dual.push_back(p->type == 1 ? 1 : 0);
     if (slot) *slot = (uint32_t)(e->h_weight.size() - 1);
     return FDTD_OK;
 }
@@ -767,13 +797,19 @@ int fdtd_engine_iterate_async(fdtd_engine_t e, uint32_t n) {
     int rc;
     CK(cudaEventRecord(e->ev0, e->stream));
     if ((rc = start(e))) return rc;
+    const bool fd_on = e->fd_interval && !e->h_freq.empty() && e->ps.nprobe;
     uint32_t left = n;
     while (left > 0) {
-        if (e->interval && e->use_graphs && e->chunk && (e->ts % e->interval) == 0 && left >= e->interval) {
+        // steps to the next frequency-domain step (a chunk graph may end on
+        // it, not pass it)
+        const uint32_t to_fd = fd_on ? e->fd_interval - (e->ts % e->fd_interval) : ~0u;
+        if (e->interval && e->use_graphs && e->chunk && (e->ts % e->interval) == 0 && left >= e->interval &&
+            to_fd >= e->interval) {
             CK(cudaGraphLaunch(e->chunk, e->stream));
-            e->last_launches += 2 * (uint64_t)e->interval + 1;
+            e->last_launches += (e->fused ? 1 : 2) * (uint64_t)e->interval + 1;
             e->ts += e->interval;
             left -= e->interval;
+            if (to_fd == e->interval && (rc = launch_fd(e, e->ts))) return rc;
             continue;
         }
         const bool sample = e->interval && ((e->ts + 1) % e->interval) == 0;
@@ -781,9 +817,43 @@ int fdtd_engine_iterate_async(fdtd_engine_t e, uint32_t n) {
         if ((rc = launch_advance(e, 1, sample, e->energy_on_probe))) return rc;
         e->ts += 1;
         left -= 1;
+        if (fd_on && (e->ts % e->fd_interval) == 0 && (rc = launch_fd(e, e->ts))) return rc;
     }
     CK(cudaEventRecord(e->ev1, e->stream));
     e->pending = true;
+    return FDTD_OK;
+}
+
+int fdtd_engine_set_fd(fdtd_engine_t e, const double* freqs, uint32_t nfreq, uint32_t fd_interval) {
+    if (!e || (nfreq && !freqs)) return FDTD_ERR_ARG;
+    if (e->started) {
+        set_error("fdtd_engine_set_fd: frequencies must be set before the first iterate");
+        return FDTD_ERR_STATE;
+    }
+    if (nfreq && fd_interval == 0) {
+        set_error("fdtd_engine_set_fd: fd_interval must be > 0");
+        return FDTD_ERR_ARG;
+    }
+    e->h_freq.assign(freqs, freqs + nfreq);
+    e->fd_interval = nfreq ? fd_interval : 0;
+    return FDTD_OK;
+}
+
+int fdtd_engine_read_fd(fdtd_engine_t e, double* re_im, uint32_t* samples) {
+    if (!e) return FDTD_ERR_ARG;
+    if (e->pending) {
+        set_error("fdtd_engine_read_fd: wait for the asynchronous iterate first");
+        return FDTD_ERR_STATE;
+    }
+    CK(cudaSetDevice(e->device));
+    int cnt = 0;
+    if (e->d_fd.p) {
+        if (re_im)
+            CK(cudaMemcpyAsync(re_im, e->d_fd.p, e->d_fd.n * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaMemcpyAsync(&cnt, e->d_fd_count.p, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+    }
+    if (samples) *samples = (uint32_t)cnt;
     return FDTD_OK;
 }
 

@@ -82,6 +82,13 @@ struct fdtd_engine_s {
     std::vector<ProbeEntry> h_entries;
     std::vector<int> h_first{0};
     std::vector<double> h_weight;
+    std::vector<int> h_dual;           // per probe: 1 = current probe (dual time)
+    // frequency-domain accumulation (0 frequencies = off)
+    std::vector<double> h_freq;
+    uint32_t fd_interval = 0;
+    DevBuf<double> d_freq, d_fd;
+    DevBuf<int> d_fd_dual, d_fd_count;
+    FdSet fd{};
     DevBuf<ProbeEntry> d_entries;
     DevBuf<int> d_first;
     DevBuf<double> d_weight;

@@ -217,6 +217,81 @@ struct ProbeSet {
     int stop_ts;                // > 0 (with end_crit): stop at this numTS
 };
 
+// Integral of probe p over the fields of numTS ts, by one warp: the lanes
+// load 32 entries at a time and the sum runs over them in entry order --
+// the reference's own order and precision: ProcessVoltage's line sum in
+// double (engine_interface_fdtd.cpp:200-226), ProcessCurrent's loop sum in
+// float (processcurrent.cpp:93-168) -- so the samples are bit-identical to
+// the reference's.  Every lane returns the sum.
+__device__ __forceinline__ double probe_sum(const ProbeSet& ps, const DevGrid& g, int p, int ts, int lane) {
+    const int first = ps.first[p], last = ps.first[p + 1];
+    if (first >= last) return 0.0;
+    const bool odd = g.V2 && (ts & 1);  // fused kernel: the buffer of numTS
+    const bool current = ps.entries[first].field != 0;
+    double accd = 0.0;
+    float accf = 0.f;
+    for (int base = first; base < last; base += 32) {
+        float v = 0.f;
+        int sg = 1;
+        if (base + lane < last) {
+            const ProbeEntry pe = ps.entries[base + lane];
+            const float* f = pe.field ? (odd ? g.I2 : g.I) : (odd ? g.V2 : g.V);
+            v = f[(long long)pe.comp * g.comp + pe.off];
+            sg = pe.sign;
+        }
+        const int cnt = min(32, last - base);
+        for (int k = 0; k < cnt; ++k) {
+            const float vk = __shfl_sync(0xffffffffu, v, k);
+            const int sk = __shfl_sync(0xffffffffu, sg, k);
+            if (current) accf = sk > 0 ? __fadd_rn(accf, vk) : __fsub_rn(accf, vk);
+            else accd = sk > 0 ? __dadd_rn(accd, (double)vk) : __dsub_rn(accd, (double)vk);
+        }
+    }
+    return current ? (double)accf : accd;
+}
+
+// Frequency-domain probe accumulation (ProcessIntegral::Process,
+// processintegral.cpp:154-168): on every FD step, for each probe p and
+// frequency f,  F[p][f] += v_p * weight_p * exp(-2 pi i f t_p) * scale  with
+// t_p = (numTS + 0.5 for current probes) * dT and scale = 2 dT FD_interval.
+struct FdSet {
+    int nfreq;
+    const double* freq;  // [nfreq] Hz
+    double* acc;         // [nprobe][nfreq][2] re, im
+    const int* dual;     // [nprobe] 1: sampled at the dual time (current probe)
+    double dT;
+    double scale;
+    int* count;          // FD samples accumulated
+};
+
+// One block; dynamic shared memory: nprobe doubles.  expect_ts: the numTS
+// the host launched this for (a job that stopped on its end criterion
+// earlier has a smaller numTS and is left alone).
+static __global__ void k_fd_accumulate(const int* d_ts, int expect_ts, ProbeSet ps, const DevGrid g, FdSet fd) {
+    extern __shared__ double s_val[];
+    __shared__ int s_go;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    if (tid == 0) s_go = (*d_ts == expect_ts);
+    __syncthreads();
+    if (!s_go) return;
+    for (int p = warp; p < ps.nprobe; p += nwarps) {
+        const double acc = probe_sum(ps, g, p, expect_ts, lane);
+        if (lane == 0) s_val[p] = acc * ps.weight[p];
+    }
+    __syncthreads();
+    const int n = ps.nprobe * fd.nfreq;
+    for (int k = tid; k < n; k += blockDim.x) {
+        const int p = k / fd.nfreq, f = k - p * fd.nfreq;
+        const double t = ((double)expect_ts + 0.5 * (double)fd.dual[p]) * fd.dT;
+        double sn, cs;
+        sincospi(2.0 * fd.freq[f] * t, &sn, &cs);  // exp(-2 pi i f t) = cs - i sn
+        const double v = s_val[p] * fd.scale;
+        fd.acc[2 * k] += v * cs;
+        fd.acc[2 * k + 1] -= v * sn;
+    }
+    if (tid == 0) *fd.count += 1;
+}
+
 // Advances numTS by adv (Engine::IterateTS ++numTS) and, when sample is set,
 // records one probe/energy sample row (ProcessIntegral::Process): the probe
 // sums (ProcessVoltage / ProcessCurrent) as warp reductions in double.
@@ -256,16 +331,7 @@ __device__ __forceinline__ void advance_sample(int* d_ts, int adv, int sample, c
     const int warp = tid >> 5, lane = tid & 31;
     const int nwarps = nthr >> 5;
     for (int p = warp; p < ps.nprobe; p += nwarps) {
-        double acc = 0.0;
-        for (int e = ps.first[p] + lane; e < ps.first[p + 1]; e += 32) {
-            const ProbeEntry pe = ps.entries[e];
-            const bool odd = g.V2 && (s_ts & 1);  // fused kernel: the buffer of numTS
-            const float* f = pe.field ? (odd ? g.I2 : g.I) : (odd ? g.V2 : g.V);
-            const float val = f[(long long)pe.comp * g.comp + pe.off];
-            acc += pe.sign > 0 ? (double)val : -(double)val;
-        }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+        const double acc = probe_sum(ps, g, p, s_ts, lane);
         if (lane == 0) rec[2 + p] = acc * ps.weight[p];
     }
     if (tid == 0) {

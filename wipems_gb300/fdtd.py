@@ -329,6 +329,39 @@ class Engine:
     def iterate(self, n: int):
         check(lib().fdtd_engine_iterate(self._h, int(n)), "fdtd_engine_iterate")
 
+    def set_frequencies(self, freqs, fd_interval: int | None = None):
+        """Frequency-domain probe accumulation on the device at the given
+        frequencies (Hz).  The default interval follows the reference's
+        Processing::AddFrequency (processing.cpp:150-170): the operator's
+        Nyquist number, lowered for frequencies above the excited band;
+        frequencies too high for the timestep are dropped, as there."""
+        dT = self.op.dT
+        kept = []
+        interval = int(self.op.nyquist)
+        for f in freqs:
+            nyq = int(np.floor(1.0 / f / 2.0 / dT)) if f > 0 else 2 ** 32 - 1  # CalcNyquistNum (tools/useful.cpp:30-36)
+            if nyq == 0:
+                continue
+            interval = min(interval, nyq) if interval else nyq
+            kept.append(float(f))
+        if fd_interval is not None:
+            interval = int(fd_interval)
+        arr = np.asarray(kept, np.float64)
+        check(lib().fdtd_engine_set_fd(self._h, arr.ctypes.data_as(_abi.PD), len(kept), int(interval)),
+              "fdtd_engine_set_fd")
+        self.fd_freqs = arr
+        self.fd_interval = interval
+        return arr
+
+    def fd_results(self):
+        """(values [probe][frequency] complex, samples accumulated)."""
+        nf = len(getattr(self, "fd_freqs", []))
+        npr = len(self.probe_types)
+        buf = np.zeros((npr, nf, 2), np.float64)
+        cnt = C.c_uint32()
+        check(lib().fdtd_engine_read_fd(self._h, buf.ctypes.data_as(_abi.PD), C.byref(cnt)), "fdtd_engine_read_fd")
+        return buf[..., 0] + 1j * buf[..., 1], cnt.value
+
     def iterate_async(self, n: int):
         """Queues n timesteps on the engine's stream and returns (wait())."""
         check(lib().fdtd_engine_iterate_async(self._h, int(n)), "fdtd_engine_iterate_async")
