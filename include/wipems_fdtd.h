@@ -60,7 +60,7 @@ typedef struct fdtd_scene_s* fdtd_scene_t;
 /* Boundary condition codes, as openEMS::m_BC_type (openems.cpp:850-880). */
 #define FDTD_BC_PEC 0
 #define FDTD_BC_PMC 1
-#define FDTD_BC_MUR 2   /* rejected: Mur ABC is not provided */
+#define FDTD_BC_MUR 2   /* first-order Mur absorbing boundary */
 #define FDTD_BC_PML 3
 
 /* Mesh lines in drawing units (strictly increasing), unit = metres per
@@ -79,6 +79,10 @@ int fdtd_scene_set_background(fdtd_scene_t s, double eps_r, double mue_r,
  * openEMS::SetupBoundaryConditions (openems.cpp:380-406). */
 int fdtd_scene_set_boundary(fdtd_scene_t s, const int bc[6],
                             const uint32_t pml_size[6]);
+/* Mur phase velocity per face (m/s; 0 = the speed of light in the
+ * boundary material), <BoundaryCond MUR_PhaseVelocity[_xmin..]>
+ * (openems.cpp:882-890). */
+int fdtd_scene_set_mur_velocity(fdtd_scene_t s, const double v_phase[6]);
 /* Gaussian pulse excitation signal, Excitation::SetupGaussianPulse
  * (excitation.cpp:55-62).  nr_ts = NumberOfTimesteps (signal length cap). */
 int fdtd_scene_set_gauss_excite(fdtd_scene_t s, double f0, double fc,
@@ -129,7 +133,8 @@ int fdtd_scene_add_probe(fdtd_scene_t s, int type,
 /* openEMS XML input (openEMS::ParseFDTDSetup, openems.cpp:756-936, and the
  * CSXCAD <ContinuousStructure> it embeds), the subset this engine covers:
  * <FDTD NumberOfTimesteps endCriteria OverSampling> with a Gaussian
- * <Excitation Type="0"> and <BoundaryCond> (PEC / PMC / PML_n or codes);
+ * <Excitation Type="0"> and <BoundaryCond> (PEC / PMC / MUR / PML_n or
+ * codes, MUR_PhaseVelocity);
  * <RectilinearGrid DeltaUnit> with X/Y/ZLines; <BackgroundMaterial>; the
  * properties Material, Metal, LumpedElement (R, C, caps), Excitation,
  * ProbeBox (voltage / current) and LorentzMaterial (order 1), each with
@@ -201,6 +206,21 @@ typedef struct {
     const float* i_int; const float* i_ext; const float* i_lor;
 } fdtd_ade_desc;
 
+/* One Mur boundary face (Operator_Ext_Mur_ABC, operator_ext_mur_abc.cpp:
+ * 88-205): the tangential voltages (components (ny+1)%3 and (ny+2)%3) on
+ * line `line` of axis ny follow V = V'_shift - c V_line + c V_shift (old
+ * values primed) from the neighbouring line `shift`, coefficients
+ * c = (c0 dT - d) / (c0 dT + d) per (nP, nPP) position; active from
+ * numTS >= start_ts. */
+typedef struct {
+    int      ny, top;
+    uint32_t line, shift;
+    uint32_t n_p, n_pp;        /* lines along (ny+1)%3 and (ny+2)%3 */
+    const float* coef_p;       /* [n_p][n_pp] */
+    const float* coef_pp;
+    uint32_t start_ts;
+} fdtd_mur_desc;
+
 /* Everything Engine_CUDA needs from an Operator after CalcECOperator. */
 typedef struct {
     uint32_t num_lines[3];
@@ -231,6 +251,9 @@ typedef struct {
      * meshes with the factorized geometry. */
     const double* lines[3];
     double unit;
+    /* Mur faces (Operator_Ext_Mur_ABC), in the order of the faces */
+    uint32_t num_mur;
+    const fdtd_mur_desc* mur;
 } fdtd_op_desc;
 
 /* Fills desc with pointers into op's host arrays (valid while op lives). */

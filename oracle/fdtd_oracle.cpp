@@ -67,6 +67,8 @@ struct BasicEngine {
     std::vector<std::vector<float>> vflux, cflux;
     // ADE state per order
     std::vector<std::vector<float>> vADE, vLor, cADE, cLor;
+    // Mur ABC buffers per face (m_volt_nyP / m_volt_nyPP)
+    std::vector<std::vector<float>> murP, murPP;
 
     explicit BasicEngine(const fdtd_op_desc* d) : op(d) {
         for (int n = 0; n < 3; ++n) N[n] = d->num_lines[n];
@@ -78,6 +80,10 @@ struct BasicEngine {
             size_t nloc = 3 * (size_t)u.num_lines[0] * u.num_lines[1] * u.num_lines[2];
             vflux.emplace_back(nloc, 0.f);
             cflux.emplace_back(nloc, 0.f);
+        }
+        for (uint32_t f = 0; f < d->num_mur; ++f) {
+            murP.emplace_back((size_t)d->mur[f].n_p * d->mur[f].n_pp, 0.f);
+            murPP.emplace_back((size_t)d->mur[f].n_p * d->mur[f].n_pp, 0.f);
         }
         for (uint32_t o = 0; o < d->num_ade_orders; ++o) {
             size_t c = 3 * (size_t)d->ade[o].count;
@@ -175,6 +181,43 @@ struct BasicEngine {
                 }
     }
 
+    // ---- Mur ABC (engine_ext_mur_abc.cpp:84-164), V(n, x, y, z) -> float&.
+    // stage 0: DoPreVoltageUpdates (faces in insertion order), 1:
+    // DoPostVoltageUpdates, 2: Apply2Voltages (both in reverse insertion
+    // order: the sorted extension list holds equal priorities reversed).
+    template <class Acc>
+    void mur(int stage, unsigned ts, Acc&& Vf) {
+        const uint32_t nf = op->num_mur;
+        for (uint32_t k = 0; k < nf; ++k) {
+            const uint32_t f = stage == 0 ? k : nf - 1 - k;
+            const fdtd_mur_desc& m = op->mur[f];
+            if (ts < m.start_ts) continue;  // IsActive
+            const int ny = m.ny, nP = (ny + 1) % 3, nPP = (ny + 2) % 3;
+            uint32_t pos[3], sh[3];
+            pos[ny] = m.line;
+            sh[ny] = m.shift;
+            for (uint32_t i = 0; i < m.n_p; ++i) {
+                pos[nP] = sh[nP] = i;
+                for (uint32_t j = 0; j < m.n_pp; ++j) {
+                    pos[nPP] = sh[nPP] = j;
+                    const size_t k2 = (size_t)i * m.n_pp + j;
+                    float& bp = murP[f][k2];
+                    float& bpp = murPP[f][k2];
+                    if (stage == 0) {
+                        bp = Vf(nP, sh[0], sh[1], sh[2]) - m.coef_p[k2] * Vf(nP, pos[0], pos[1], pos[2]);
+                        bpp = Vf(nPP, sh[0], sh[1], sh[2]) - m.coef_pp[k2] * Vf(nPP, pos[0], pos[1], pos[2]);
+                    } else if (stage == 1) {
+                        bp += m.coef_p[k2] * Vf(nP, sh[0], sh[1], sh[2]);
+                        bpp += m.coef_pp[k2] * Vf(nPP, sh[0], sh[1], sh[2]);
+                    } else {
+                        Vf(nP, pos[0], pos[1], pos[2]) = bp;
+                        Vf(nPP, pos[0], pos[1], pos[2]) = bpp;
+                    }
+                }
+            }
+        }
+    }
+
     // ---- Lorentz / Drude (engine_ext_lorentzmaterial.cpp:79-173)
     template <bool VOLT>
     void ade_pre() {
@@ -245,17 +288,23 @@ struct BasicEngine {
     }
 
     // Engine::IterateTS with the extension list sorted by priority:
-    // [UPML slabs (1e6, reverse insertion), Lorentz (0), Excitation (-1000)].
+    // [UPML slabs (1e6, reverse insertion), Lorentz (0), Mur faces (0,
+    // reverse insertion: Lorentz is added after the boundaries,
+    // openems.cpp:1051-1092), Excitation (-1000)].
     // Pre hooks run in reverse list order, post / apply hooks in list order.
     void iterate(unsigned iterTS) {
         const uint32_t nu = op->num_upml;
+        auto Vf = [this](int n, uint32_t x, uint32_t y, uint32_t z) -> float& { return V(n, x, y, z); };
         for (unsigned it = 0; it < iterTS; ++it) {
-            // DoPreVoltageUpdates: excitation (none), Lorentz, UPML slabs
+            // DoPreVoltageUpdates: excitation (none), Mur faces, Lorentz, UPML slabs
+            mur(0, numTS, Vf);
             ade_pre<true>();
             for (uint32_t s = 0; s < nu; ++s) upml<true, true>(s);
             update_voltages(0, N[0]);
             for (uint32_t s = nu; s-- > 0;) upml<true, false>(s);
+            mur(1, numTS, Vf);
             ade_apply<true>();
+            mur(2, numTS, Vf);
             excite<true>();
 
             ade_pre<false>();
@@ -652,6 +701,9 @@ void sse_mt_iterate(SSEEngine& S, BasicEngine& B, unsigned iterTS, unsigned nthr
         for (unsigned it = 0; it < iterTS; ++it) {
             unsigned ts = S.numTS + it;
             // DoPreVoltageUpdates: reverse priority order, barrier after each ext
+            auto Vs = [&S](int n, uint32_t x, uint32_t y, uint32_t z) -> float& { return S.Vs(n, x, y, z); };
+            if (tid == 0 && B.op->num_mur) B.mur(0, ts, Vs);
+            bar.wait();
             if (tid == 0) H.ade_pre<true>();
             bar.wait();
             for (uint32_t s = 0; s < nu; ++s) {
@@ -664,7 +716,11 @@ void sse_mt_iterate(SSEEngine& S, BasicEngine& B, unsigned iterTS, unsigned nthr
                 H.upml<true, false>(s, u_start[s][tid], u_num[s][tid]);
                 bar.wait();
             }
+            if (tid == 0 && B.op->num_mur) B.mur(1, ts, Vs);
+            bar.wait();
             if (tid == 0) H.ade_apply<true>();
+            bar.wait();
+            if (tid == 0 && B.op->num_mur) B.mur(2, ts, Vs);
             bar.wait();
             if (tid == 0) H.excite<true>(ts);
             bar.wait();

@@ -22,7 +22,7 @@ pytestmark = pytest.mark.usefixtures("libs")
 GOLDEN = Path(__file__).resolve().parent / "golden"
 
 
-@pytest.mark.parametrize("kind", ["pec", "upml", "drude", "lorentz", "mixed"])
+@pytest.mark.parametrize("kind", ["pec", "upml", "drude", "lorentz", "mixed", "mur"])
 def test_basic_and_sse_compressed_engines_agree_bitwise(kind):
     op = Operator(scenes.mini(kind, nr_ts=200))
     a = oracle.run(op.desc, op.probes, 150, op.probe_interval, engine=oracle.BASIC)
@@ -55,3 +55,25 @@ def test_golden_fixtures(name):
     assert np.array_equal(r["energy"], data["energy"])
     crc = int(np.bitwise_xor.reduce(r["volt"].view(np.uint32).ravel()))
     assert crc == meta["volt_xor"]
+
+
+def test_mur_boundaries_absorb():
+    """Mur faces (engine_ext_mur_abc.cpp) let the port's pulse leave: the
+    energy falls far below what remains in the same box closed by PEC walls
+    (where only the port's 50 ohm load takes energy out)."""
+    from wipems_gb300 import Operator, scenes
+    from wipems_gb300.fdtd import BC_PEC
+    op = Operator(scenes.mini("mur", nr_ts=900))
+    assert op.desc.num_mur == 5
+    m = op.desc.mur[0]
+    # vacuum at the face, uniform 0.5 mm mesh: c = (c0 dT - d) / (c0 dT + d)
+    c0t = 299792458.0 * op.dT
+    assert abs(m.coef_p[0] - (c0t - 0.5e-3) / (c0t + 0.5e-3)) < 1e-7
+    r = oracle.run(op.desc, op.probes, 900, op.probe_interval, engine=oracle.BASIC, fields=False)
+    e = r["energy"]
+    assert e[-1] < 1e-3 * e.max()
+    sc = scenes.mini("mur", nr_ts=900)
+    sc.set_boundary([BC_PEC] * 6, [0] * 6)
+    op2 = Operator(sc)
+    r2 = oracle.run(op2.desc, op2.probes, 900, op2.probe_interval, engine=oracle.BASIC, fields=False)
+    assert e[-1] / e.max() < 0.01 * r2["energy"][-1] / r2["energy"].max()

@@ -44,7 +44,7 @@ def compare(op, eng, ref, bitwise=True):
 
 
 @pytest.mark.parametrize("kernel", ["tma", "direct"])
-@pytest.mark.parametrize("kind", ["pec", "upml", "graded", "drude", "lorentz", "mixed"])
+@pytest.mark.parametrize("kind", ["pec", "upml", "graded", "drude", "lorentz", "mixed", "mur"])
 def test_mini_scenes_match_oracle(kind, kernel):
     """Uniform meshes: bit-identical.  Graded meshes (automatic factorized
     geometry): within the probe / field tolerance of the oracle on the
@@ -254,3 +254,33 @@ def test_fused_kernel_refuses_ade():
     with pytest.raises(FdtdError) as ei:
         Engine(op, kernel="fused")
     assert ei.value.code == -5
+
+
+def test_mur_chunking_graphs_and_excitation_on_the_face():
+    """Mur faces through graph chunks and single steps, and a face that
+    carries an excitation (active only after the pulse, start_ts), match
+    the reference stepping bit for bit."""
+    op = Operator(scenes.mini("mur", seed=1, nr_ts=700))
+    ref = oracle.run(op.desc, op.probes, 333, op.probe_interval, engine=oracle.BASIC)
+    for kw in (dict(), dict(use_graphs=False, x_chunk=3)):
+        eng = Engine(op, **kw)
+        eng.iterate(100)
+        eng.iterate(233)
+        compare(op, eng, ref)
+    from wipems_gb300 import Scene
+    from wipems_gb300.fdtd import BC_MUR, BC_PEC
+    from wipems_gb300.scenes import uniform_lines
+    L = [uniform_lines(c, 0.5) for c in (24, 20, 30)]
+    s = Scene(*L, 1e-3)
+    s.set_boundary([BC_MUR, BC_MUR, BC_MUR, BC_MUR, BC_PEC, BC_MUR], [0] * 6)
+    s.set_gauss_excite(10e9, 10e9, 600)
+    # a soft Ez source on the xmin face (x = 0): that face starts after the pulse
+    s.add_excitation([L[0][0], L[1][8], L[2][12]], [L[0][0], L[1][12], L[2][18]], [0, 0, 1], priority=5)
+    s.add_probe([L[0][6], L[1][10], L[2][10]], [L[0][6], L[1][10], L[2][20]], 0)
+    op = Operator(s)
+    assert op.desc.mur[0].start_ts > 0
+    n = op.desc.mur[0].start_ts + 60
+    ref = oracle.run(op.desc, op.probes, n, op.probe_interval, engine=oracle.BASIC)
+    eng = Engine(op)
+    eng.iterate(n)
+    compare(op, eng, ref)

@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 from wipems_gb300 import BC_PEC, BC_PMC, BC_PML, CompressedOperator, Operator, Scene
+from wipems_gb300.fdtd import BC_MUR
 from wipems_gb300._abi import FdtdError
 
 GOLDEN = Path(__file__).parent / "golden"
@@ -76,7 +77,6 @@ def test_xml_text_and_lorentz_material():
 
 @pytest.mark.parametrize("edit,needle", [
     (('<Box Priority="20">', '<Cylinder Priority="20" Radius="1">'), "Cylinder"),
-    (('ymin="3"', 'ymin="MUR"'), "Mur"),
     (('<Excitation Type="0" f0="1e+10"', '<Excitation Type="1" f0="1e+10"'), "excitation Type 1"),
     (('Epsilon="3.66"', 'Epsilon="3.66,3.66,4"'), "anisotropic"),
     (('<Weight Epsilon="1"', '<Weight Epsilon="2*x"'), "weighting"),
@@ -100,3 +100,22 @@ def test_xml_malformed_documents():
         with pytest.raises(FdtdError) as ei:
             Scene.from_xml(text)
         assert ei.value.code == -1
+
+
+def test_xml_mur_boundaries():
+    text = (GOLDEN / "port_box.xml").read_text().replace(
+        'zmax="PMC"', 'zmax="MUR" MUR_PhaseVelocity="2.5e8" MUR_PhaseVelocity_zmax="2e8"')
+    sx = Scene.from_xml(text)
+    s = _api_scene()
+    s.set_boundary([BC_PML, BC_PML, BC_PML, BC_PML, BC_PEC, BC_MUR], [8, 8, 8, 6, 0, 0])
+    s.set_mur_velocity([2.5e8] * 5 + [2e8])
+    a, b = Operator(sx), Operator(s)
+    _same_operator(a, b)
+    assert a.desc.num_mur == b.desc.num_mur == 1
+    m = a.desc.mur[0]
+    n = m.n_p * m.n_pp
+    ca = np.ctypeslib.as_array(m.coef_p, shape=(n,))
+    cb = np.ctypeslib.as_array(b.desc.mur[0].coef_p, shape=(n,))
+    assert np.array_equal(ca, cb)
+    c0t = 2e8 * a.dT  # phase velocity given: c = (v dT - d) / (v dT + d), d = 0.5 mm
+    assert np.allclose(ca, np.float32((c0t - 0.5e-3) / (c0t + 0.5e-3)))

@@ -37,6 +37,11 @@ class FdtdAdeDesc(C.Structure):
                 ("v_int", PF), ("v_ext", PF), ("v_lor", PF), ("i_int", PF), ("i_ext", PF), ("i_lor", PF)]
 
 
+class FdtdMurDesc(C.Structure):
+    _fields_ = [("ny", C.c_int), ("top", C.c_int), ("line", u32), ("shift", u32), ("n_p", u32), ("n_pp", u32),
+                ("coef_p", PF), ("coef_pp", PF), ("start_ts", u32)]
+
+
 class FdtdOpDesc(C.Structure):
     _fields_ = [("num_lines", u32 * 3), ("dT", C.c_double),
                 ("vv", PF), ("vi", PF), ("ii", PF), ("iv", PF),
@@ -47,7 +52,8 @@ class FdtdOpDesc(C.Structure):
                 ("curr_count", u32), ("curr_index", PU32 * 3), ("curr_dir", PU16), ("curr_amp", PF),
                 ("curr_delay", PU32),
                 ("signal_length", u32), ("signal_volt", PF), ("signal_curr", PF), ("signal_period_ts", u32),
-                ("lines", C.POINTER(C.c_double) * 3), ("unit", C.c_double)]
+                ("lines", C.POINTER(C.c_double) * 3), ("unit", C.c_double),
+                ("num_mur", u32), ("mur", C.POINTER(FdtdMurDesc))]
 
 
 class FdtdProbeDesc(C.Structure):
@@ -134,6 +140,7 @@ SIGNATURES = [
     ("fdtd_scene_destroy", C.c_int, [_P]),
     ("fdtd_scene_set_background", C.c_int, [_P, C.c_double, C.c_double, C.c_double, C.c_double]),
     ("fdtd_scene_set_boundary", C.c_int, [_P, C.POINTER(C.c_int), PU32]),
+    ("fdtd_scene_set_mur_velocity", C.c_int, [_P, C.POINTER(C.c_double)]),
     ("fdtd_scene_set_gauss_excite", C.c_int, [_P, C.c_double, C.c_double, u32]),
     ("fdtd_scene_set_oversampling", C.c_int, [_P, u32]),
     ("fdtd_scene_add_material", C.c_int, [_P, C.c_int, PD, PD, C.c_double, C.c_double, C.c_double, C.c_double]),

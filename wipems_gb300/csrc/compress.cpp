@@ -464,6 +464,47 @@ int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
         c->sigV.assign(d->signal_volt, d->signal_volt + d->signal_length);
         c->sigC.assign(d->signal_curr, d->signal_curr + d->signal_length);
     }
+    // Mur faces.  The engine applies a face after the node updates of its
+    // voltage step, so a face must not meet what the reference applies
+    // between its post-update and apply hooks (Lorentz/Drude on the face or
+    // its neighbour line, an excitation on the neighbour line); an
+    // excitation on the face line itself is added after the face is set,
+    // as the reference does.
+    for (uint32_t f = 0; f < d->num_mur; ++f) {
+        const fdtd_mur_desc& m = d->mur[f];
+        if (m.ny < 0 || m.ny > 2 || m.line >= c->N[m.ny] || m.shift >= c->N[m.ny] ||
+            m.n_p != c->N[(m.ny + 1) % 3] || m.n_pp != c->N[(m.ny + 2) % 3]) {
+            set_error("Mur face descriptor does not match the grid");
+            return FDTD_ERR_ARG;
+        }
+        for (uint32_t o = 0; o < d->num_ade_orders; ++o)
+            for (uint32_t i = 0; i < d->ade[o].count; ++i) {
+                const uint32_t q = d->ade[o].pos[m.ny][i];
+                if (q == m.line || q == m.shift) {
+                    set_error("a Lorentz/Drude material touches a Mur boundary (or the line next to it): not provided");
+                    return FDTD_ERR_UNSUPPORTED;
+                }
+            }
+        for (uint32_t i = 0; i < d->volt_count; ++i)
+            if (d->volt_index[m.ny][i] == m.shift && d->volt_dir[i] != m.ny) {
+                set_error("an excitation on the line next to a Mur boundary is not provided");
+                return FDTD_ERR_UNSUPPORTED;
+            }
+        MurFace M;
+        M.ny = m.ny;
+        M.top = m.top;
+        M.line = m.line;
+        M.shift = m.shift;
+        M.n[0] = m.n_p;
+        M.n[1] = m.n_pp;
+        M.cp.assign(m.coef_p, m.coef_p + (size_t)m.n_p * m.n_pp);
+        M.cpp.assign(m.coef_pp, m.coef_pp + (size_t)m.n_p * m.n_pp);
+        M.start_ts = m.start_ts;
+        c->mur.push_back(std::move(M));
+        // the voltage kernel must keep zeroing a Mur face's line every step:
+        // neighbouring faces read it between the update and the apply
+        if (m.line == c->N[m.ny] - 1) c->trim_e[m.ny] = false;
+    }
     return FDTD_OK;
 }
 

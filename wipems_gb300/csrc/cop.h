@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "../../include/wipems_fdtd.h"
+#include "fdtd_host.h"
 
 namespace wipems {
 
@@ -75,6 +76,7 @@ struct fdtd_cop_s {
     int inner_lo[3] = {0, 0, 0}, inner_hi[3] = {0, 0, 0};  // nodes outside may be UPML
     bool trim_e[3] = {false, false, false};  // last line inert for the voltage update
     std::vector<float> sigV, sigC;
+    std::vector<wipems::MurFace> mur;  // Mur ABC faces (copied from the operator)
     uint32_t sig_len = 0, sig_period = 0;
     ~fdtd_cop_s();
 };

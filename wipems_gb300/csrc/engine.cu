@@ -139,7 +139,22 @@ int check_launch() {
     return FDTD_OK;
 }
 
+void launch_mur(fdtd_engine_s* e, int ts_off, int stage) {
+    const unsigned blocks = std::min<unsigned>((e->mur.total + 255) / 256, 1024u);
+    k_mur<<<blocks, 256, 0, e->stream>>>(e->g, e->mur, ts_off, stage);
+    e->last_launches += 1;
+}
+
 int launch_step(fdtd_engine_s* e, int ts_off, bool energy) {
+    if (e->mur.nface) {  // Mur faces: pre-update, voltage kernel, post-update, apply
+        launch_mur(e, ts_off, 0);
+        launch_volt(e, ts_off);
+        launch_mur(e, ts_off, 1);
+        launch_mur(e, ts_off, 2);
+        launch_curr(e, ts_off, energy);
+        e->last_launches += 2;
+        return check_launch();
+    }
     if (e->fused) {
         launch_fused(e, ts_off, energy);
         e->last_launches += 1;
@@ -441,6 +456,7 @@ int reset_state(fdtd_engine_s* e) {
         if (b->p) CK(cudaMemsetAsync(b->p, 0, F, s));
     CK(cudaMemsetAsync(e->ctl.p, 0, 4 * sizeof(int), s));
     if (e->d_fd.p) CK(cudaMemsetAsync(e->d_fd.p, 0, e->d_fd.n * sizeof(double), s));
+    if (e->mur_buf.p) CK(cudaMemsetAsync(e->mur_buf.p, 0, e->mur_buf.n * sizeof(float), s));
     if (e->d_fd_count.p) CK(cudaMemsetAsync(e->d_fd_count.p, 0, sizeof(int), s));
     CK(cudaMemsetAsync(e->d_eacc.p, 0, 4 * sizeof(double), s));
     e->ts = 0;
@@ -560,6 +576,40 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     } else {
         CK(cudaMemsetAsync(e->sigV.p, 0, sizeof(float), e->stream));
         CK(cudaMemsetAsync(e->sigC.p, 0, sizeof(float), e->stream));
+    }
+    if (!c->mur.empty()) {
+        if (e->fused) {
+            set_error("the fused single-pass kernel does not cover Mur boundaries (use the two-pass kernels)");
+            return FDTD_ERR_UNSUPPORTED;
+        }
+        size_t tot_n = 0;
+        for (const MurFace& M : c->mur) tot_n += (size_t)M.n[0] * M.n[1];
+        if ((rc = e->mur_coef.alloc(2 * tot_n, tot)) || (rc = e->mur_buf.alloc(2 * tot_n, tot))) return rc;
+        CK(cudaMemsetAsync(e->mur_buf.p, 0, 2 * tot_n * sizeof(float), e->stream));
+        std::vector<float> hc(2 * tot_n);
+        size_t off = 0;
+        e->mur.nface = 0;
+        for (const MurFace& M : c->mur) {
+            const size_t n = (size_t)M.n[0] * M.n[1];
+            std::copy(M.cp.begin(), M.cp.end(), hc.begin() + 2 * off);
+            std::copy(M.cpp.begin(), M.cpp.end(), hc.begin() + 2 * off + n);
+            MurDev& F = e->mur.f[e->mur.nface++];
+            F.ny = M.ny;
+            F.line = (int)M.line;
+            F.shift = (int)M.shift;
+            F.n0 = (int)M.n[0];
+            F.n1 = (int)M.n[1];
+            F.start_ts = (int)M.start_ts;
+            F.cp = e->mur_coef.p + 2 * off;
+            F.cpp = e->mur_coef.p + 2 * off + n;
+            F.bp = e->mur_buf.p + 2 * off;
+            F.bpp = e->mur_buf.p + 2 * off + n;
+            F.offset = (uint32_t)off;
+            off += n;
+        }
+        e->mur.total = (uint32_t)tot_n;
+        e->mur.idx16 = c->E.idx16 ? 1 : 0;
+        CK(cudaMemcpyAsync(e->mur_coef.p, hc.data(), hc.size() * sizeof(float), cudaMemcpyHostToDevice, e->stream));
     }
     g.Nx = (int)e->N[0];
     g.Ny = (int)e->N[1];
@@ -995,7 +1045,12 @@ int fdtd_engine_profile_kernels(fdtd_engine_t e, uint32_t n_steps, double* ms_vo
             launch_fused(e, 0, sample && e->energy_on_probe);
             CK(cudaEventRecord(ev[3 * k + 1], e->stream));
         } else {
+            if (e->mur.nface) launch_mur(e, 0, 0);
             launch_volt(e, 0);
+            if (e->mur.nface) {
+                launch_mur(e, 0, 1);
+                launch_mur(e, 0, 2);
+            }
             CK(cudaEventRecord(ev[3 * k + 1], e->stream));
             launch_curr(e, 0, sample && e->energy_on_probe);
         }

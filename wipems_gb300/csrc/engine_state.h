@@ -89,6 +89,9 @@ struct fdtd_engine_s {
     DevBuf<double> d_freq, d_fd;
     DevBuf<int> d_fd_dual, d_fd_count;
     FdSet fd{};
+    // Mur ABC faces
+    DevBuf<float> mur_coef, mur_buf;
+    MurSet mur{};
     DevBuf<ProbeEntry> d_entries;
     DevBuf<int> d_first;
     DevBuf<double> d_weight;

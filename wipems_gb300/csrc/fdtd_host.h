@@ -61,6 +61,7 @@ struct fdtd_scene_s {
     double bg_eps = 1, bg_mue = 1, bg_kappa = 0, bg_sigma = 0;
     int bc[6] = {0, 0, 0, 0, 0, 0};
     uint32_t pml_size[6] = {0, 0, 0, 0, 0, 0};
+    double mur_vph[6] = {0, 0, 0, 0, 0, 0};
     double f0 = 0, fc = 0;
     bool have_excite = false;
     uint32_t nr_ts = 0;
@@ -82,6 +83,14 @@ struct AdeOrder {
     std::vector<uint32_t> pos[3];
     bool volt_on = false, curr_on = false, volt_lor_on = false, curr_lor_on = false;
     std::vector<float> v_int, v_ext, v_lor, i_int, i_ext, i_lor;  // [3][count]
+};
+
+struct MurFace {
+    int ny = 0, top = 0;
+    uint32_t line = 0, shift = 0;
+    uint32_t n[2] = {0, 0};
+    std::vector<float> cp, cpp;  // [n[0]][n[1]]
+    uint32_t start_ts = 0;
 };
 
 struct ExcList {
@@ -112,6 +121,8 @@ struct fdtd_operator_s {
     // descriptor scratch kept alive for fdtd_operator_describe
     std::vector<fdtd_upml_desc> upml_desc;
     std::vector<fdtd_ade_desc> ade_desc;
+    std::vector<wipems::MurFace> mur;
+    std::vector<fdtd_mur_desc> mur_desc;
 };
 
 namespace wipems {

@@ -358,6 +358,93 @@ static __global__ void k_advance_sample(int* d_ts, int adv, int sample, ProbeSet
     advance_sample(d_ts, adv, sample, ps, g, energy_valid, eps0, mue0, threadIdx.x, blockDim.x);
 }
 
+// ------------------------------------------------------------- Mur ABC
+// Engine_Ext_Mur_ABC (engine_ext_mur_abc.cpp:84-164) on the device, three
+// passes around the voltage kernel: stage 0 (before it, old V):
+// b = V(shift) - c V(line); stage 1 (after it): b += c V(shift); stage 2:
+// V(line) = b, then the line node's own excitation, if any (the reference
+// adds excitations after every other voltage hook).  Faces are in face
+// order (xmin .. zmax); where two faces share a node component the one
+// earlier in that order writes it, as the reference applies them in
+// reverse insertion order.  A face acts from numTS >= start_ts on.
+struct MurDev {
+    int ny, line, shift, n0, n1, start_ts;
+    const float* cp;
+    const float* cpp;
+    float* bp;
+    float* bpp;
+    uint32_t offset;  // first flattened index of this face in the launch
+};
+struct MurSet {
+    int nface;
+    int idx16;        // E tuple index width (for the excitation lookup)
+    uint32_t total;
+    MurDev f[6];
+};
+
+static __global__ void k_mur(const DevGrid g, MurSet ms, int ts_off, int stage) {
+    if (*g.d_done) return;
+    const int numTS = *g.d_ts + ts_off;
+    const long long C = g.comp;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < ms.total; k += gridDim.x * blockDim.x) {
+        int fi = 0;
+        while (fi + 1 < ms.nface && k >= ms.f[fi + 1].offset) ++fi;
+        const MurDev& F = ms.f[fi];
+        if (numTS < F.start_ts) continue;
+        const uint32_t loc = k - F.offset;
+        const int i = (int)(loc / (uint32_t)F.n1), j = (int)(loc - (uint32_t)i * (uint32_t)F.n1);
+        const int ny = F.ny, nP = (ny + 1) % 3, nPP = (ny + 2) % 3;
+        int pos[3], sh[3];
+        pos[ny] = F.line;
+        sh[ny] = F.shift;
+        pos[nP] = sh[nP] = i;
+        pos[nPP] = sh[nPP] = j;
+        const long long ol = (long long)pos[0] * g.sx + (long long)pos[1] * g.Nzp + pos[2];
+        const long long os = (long long)sh[0] * g.sx + (long long)sh[1] * g.Nzp + sh[2];
+        float* V = g.V;
+        if (stage == 0) {
+            F.bp[loc] = __fsub_rn(V[nP * C + os], __fmul_rn(F.cp[loc], V[nP * C + ol]));
+            F.bpp[loc] = __fsub_rn(V[nPP * C + os], __fmul_rn(F.cpp[loc], V[nPP * C + ol]));
+        } else if (stage == 1) {
+            F.bp[loc] = __fadd_rn(F.bp[loc], __fmul_rn(F.cp[loc], V[nP * C + os]));
+            F.bpp[loc] = __fadd_rn(F.bpp[loc], __fmul_rn(F.cpp[loc], V[nPP * C + os]));
+        } else {
+            const int comps[2] = {nP, nPP};
+            const float vals[2] = {F.bp[loc], F.bpp[loc]};
+            uint32_t t = 0;
+            uint32_t flags = 0;
+            bool have_t = false;
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const int c = comps[q];
+                bool mine = true;  // an earlier active face sharing this component writes it
+                for (int e = 0; e < fi; ++e) {
+                    const MurDev& G = ms.f[e];
+                    if (numTS >= G.start_ts && pos[G.ny] == G.line && c != G.ny) mine = false;
+                }
+                if (!mine) continue;
+                float v = vals[q];
+                if (!have_t) {
+                    t = ms.idx16 ? load_idx<uint16_t>(g.e.idx, ol) : load_idx<uint32_t>(g.e.idx, ol);
+                    flags = __float_as_uint(__ldg(&g.e.main[TAB_MAIN * t + 1]).z);
+                    have_t = true;
+                }
+                if (flags & TF_EXC) {
+                    const float4 e0 = __ldg(&g.e.exc[TAB_EXC * t]);
+                    const float4 e1 = __ldg(&g.e.exc[TAB_EXC * t + 1]);
+                    const float amp[3] = {e0.x, e0.y, e0.z};
+                    const int dly[3] = {__float_as_int(e1.x), __float_as_int(e1.y), __float_as_int(e1.z)};
+                    if (dly[c] >= 0) {
+                        const int kx = exc_index(numTS, dly[c], g.sig_len, g.sig_period);
+                        v = __fadd_rn(v, __fmul_rn(amp[c], g.sigV[kx]));
+                    }
+                }
+                V[c * C + ol] = v;
+            }
+        }
+    }
+}
+
 // Full-grid energy (CalcFastEnergy) on demand.
 static __global__ void k_energy(const DevGrid g, double* out) {
     double es = 0.0, hs = 0.0;

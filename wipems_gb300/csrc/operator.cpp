@@ -205,7 +205,10 @@ struct Geo {
 //   HALF  l[i] + raw(i)*0.5            (quarter-cell averaging)
 //   QP    l[i] + raw(i)*0.25
 //   QM    l[i] - raw(i-1)*0.25
-enum SampleKind { SK_LINE = 0, SK_DUAL = 1, SK_HALF = 2, SK_QP = 3, SK_QM = 4, SK_COUNT = 5 };
+//   MURLO / MURHI  l[i] +- |edge length| / 2  (Mur face material probe,
+//                  operator_ext_mur_abc.cpp:132-136; used at the first /
+//                  last line)
+enum SampleKind { SK_LINE = 0, SK_DUAL = 1, SK_HALF = 2, SK_QP = 3, SK_QM = 4, SK_MURLO = 5, SK_MURHI = 6, SK_COUNT = 7 };
 
 struct BoxIndex {
     std::vector<int> prim;  // bit -> prim index (priority descending, stable)
@@ -244,6 +247,11 @@ struct BoxIndex {
             case SK_DUAL: return g.line(a, i, true);
             case SK_HALF: return l[i] + g.raw_delta(a, (int)i) * 0.5;
             case SK_QP: return l[i] + g.raw_delta(a, (int)i) * 0.25;
+            case SK_MURLO:
+            case SK_MURHI: {
+                const double d = std::fabs(g.disc_delta(a, i, false) * g.unit);
+                return kind == SK_MURLO ? g.line(a, i, false) + d / 2 / g.unit : g.line(a, i, false) - d / 2 / g.unit;
+            }
             default: return l[i] - g.raw_delta(a, (int)i - 1) * 0.25;
         }
     }
@@ -1099,6 +1107,53 @@ static int build_operator(const fdtd_scene_s& S, int threads, fdtd_operator_s& o
     }
     op.probe_interval = std::max<uint32_t>(1, op.nyquist / std::max<uint32_t>(1, S.oversampling));
 
+    // ---- Mur ABC faces (Operator_Ext_Mur_ABC::SetDirection / BuildExtension,
+    // operator_ext_mur_abc.cpp:88-195), in face order; the start timestep of
+    // a face with an excitation on it follows Engine_Ext_Mur_ABC's
+    // constructor (engine_ext_mur_abc.cpp:40-60)
+    for (int f = 0; f < 6; ++f) {
+        if (S.bc[f] != FDTD_BC_MUR) continue;
+        MurFace M;
+        M.ny = f / 2;
+        M.top = f % 2;
+        const int ny = M.ny, nP = (ny + 1) % 3, nPP = (ny + 2) % 3;
+        if (N[ny] < 2) continue;
+        M.line = M.top ? N[ny] - 1 : 0;
+        M.shift = M.top ? N[ny] - 2 : 1;
+        M.n[0] = N[nP];
+        M.n[1] = N[nPP];
+        M.cp.assign((size_t)M.n[0] * M.n[1], 0.f);
+        M.cpp.assign((size_t)M.n[0] * M.n[1], 0.f);
+        uint32_t pos[3] = {0, 0, 0};
+        pos[ny] = M.line;
+        const double delta = std::fabs(g.edge_length(ny, pos, false));
+        int kind[3];
+        kind[ny] = M.top ? SK_MURHI : SK_MURLO;
+        kind[nP] = SK_LINE;
+        kind[nPP] = SK_LINE;
+        const double vph = S.mur_vph[f];
+        for (pos[nP] = 0; pos[nP] < N[nP]; ++pos[nP])
+            for (pos[nPP] = 0; pos[nPP] < N[nPP]; ++pos[nPP]) {
+                const size_t k = (size_t)pos[nP] * M.n[1] + pos[nPP];
+                const int w = B.mat_idx.lookup(kind, pos);
+                double c0t;
+                if (w >= 0) {
+                    const Prim& p = S.prims[w];
+                    c0t = vph > 0.0 ? vph * dT : kC0 * dT / std::sqrt(p.eps * p.mue);
+                } else {
+                    c0t = vph > 0.0 ? vph * dT : kC0 / std::sqrt(S.bg_eps * S.bg_mue) * dT;
+                }
+                M.cp[k] = (float)((c0t - delta) / (c0t + delta));
+                M.cpp[k] = M.cp[k];
+            }
+        int maxDelay = -1;
+        for (size_t n = 0; n < op.volt_exc.amp.size(); ++n)
+            if ((op.volt_exc.dir[n] == nP || op.volt_exc.dir[n] == nPP) && op.volt_exc.index[ny][n] == M.line)
+                maxDelay = std::max(maxDelay, (int)op.volt_exc.delay[n]);
+        M.start_ts = maxDelay >= 0 ? (uint32_t)maxDelay + op.signal_length + 10 : 0;
+        op.mur.push_back(std::move(M));
+    }
+
     // ---- probes (openems.cpp:480-560 SetupProcessing)
     for (const Prim& p : S.prims) {
         if (p.kind != PK_PROBE) continue;
@@ -1217,16 +1272,24 @@ int fdtd_scene_set_background(fdtd_scene_t s, double eps_r, double mue_r, double
 int fdtd_scene_set_boundary(fdtd_scene_t s, const int bc[6], const uint32_t pml_size[6]) {
     if (!s || !bc) return FDTD_ERR_ARG;
     for (int i = 0; i < 6; ++i) {
-        if (bc[i] == FDTD_BC_MUR) {
-            set_error("fdtd_scene_set_boundary: Mur ABC is not provided by this engine");
-            return FDTD_ERR_UNSUPPORTED;
-        }
         if (bc[i] < -1 || bc[i] > 3) {
             set_error("fdtd_scene_set_boundary: unknown boundary code");
             return FDTD_ERR_ARG;
         }
         s->bc[i] = bc[i];
         s->pml_size[i] = (bc[i] == FDTD_BC_PML && pml_size) ? pml_size[i] : 0;
+    }
+    return FDTD_OK;
+}
+
+int fdtd_scene_set_mur_velocity(fdtd_scene_t s, const double v_phase[6]) {
+    if (!s || !v_phase) return FDTD_ERR_ARG;
+    for (int i = 0; i < 6; ++i) {
+        if (!(v_phase[i] >= 0)) {
+            set_error("fdtd_scene_set_mur_velocity: phase velocities must be >= 0");
+            return FDTD_ERR_ARG;
+        }
+        s->mur_vph[i] = v_phase[i];
     }
     return FDTD_OK;
 }
@@ -1445,6 +1508,22 @@ int fdtd_operator_describe(fdtd_operator_t op, fdtd_op_desc* d) {
     d->curr_dir = op->curr_exc.dir.data();
     d->curr_amp = op->curr_exc.amp.data();
     d->curr_delay = op->curr_exc.delay.data();
+    op->mur_desc.resize(op->mur.size());
+    for (size_t k = 0; k < op->mur.size(); ++k) {
+        const MurFace& M = op->mur[k];
+        fdtd_mur_desc& m = op->mur_desc[k];
+        m.ny = M.ny;
+        m.top = M.top;
+        m.line = M.line;
+        m.shift = M.shift;
+        m.n_p = M.n[0];
+        m.n_pp = M.n[1];
+        m.coef_p = M.cp.data();
+        m.coef_pp = M.cpp.data();
+        m.start_ts = M.start_ts;
+    }
+    d->num_mur = (uint32_t)op->mur.size();
+    d->mur = op->mur_desc.empty() ? nullptr : op->mur_desc.data();
     d->signal_length = op->signal_length;
     d->signal_volt = op->sig_volt.data();
     d->signal_curr = op->sig_curr.data();

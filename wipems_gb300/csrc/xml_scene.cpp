@@ -10,12 +10,12 @@
 //
 // Covered: <FDTD NumberOfTimesteps endCriteria OverSampling>, its Gaussian
 // <Excitation Type="0" f0 fc> and <BoundaryCond> (numeric codes or
-// PEC / PMC / PML_n); the <RectilinearGrid DeltaUnit> with its X/Y/ZLines,
+// PEC / PMC / MUR / PML_n, MUR_PhaseVelocity[_face]); the <RectilinearGrid DeltaUnit> with its X/Y/ZLines,
 // <BackgroundMaterial>, and the properties Material, Metal, LumpedElement,
 // Excitation, ProbeBox (voltage and current) and LorentzMaterial (order 1),
 // each with <Box> primitives (Priority, P1, P2).  Anything else that would
-// change the simulation (other primitives, excitation signals, boundary
-// types, anisotropic or weighted materials, cylindrical coordinates) is
+// change the simulation (other primitives, excitation signals, anisotropic
+// or weighted materials, cylindrical coordinates) is
 // refused with FDTD_ERR_UNSUPPORTED and a message naming it; purely visual
 // elements (colours) are ignored.
 #include <algorithm>
@@ -358,7 +358,17 @@ int fdtd_scene_load_xml(const char* text, fdtd_scene_t* out, fdtd_xml_info* info
             bc[n] = 3;
             pml[n] = (uint32_t)std::atoi(v->c_str() + 4);
         }  // else: the reference warns and keeps PEC
-        if (bc[n] == 2) L.bad(FDTD_ERR_UNSUPPORTED, "Mur absorbing boundary (" + std::string(bnames[n]) + ")");
+    }
+    // Mur phase velocities (openems.cpp:882-890)
+    double vph[6] = {0, 0, 0, 0, 0, 0};
+    if (bcn) {
+        double v;
+        L.num(*bcn, "MUR_PhaseVelocity", v, 0);
+        for (int n = 0; n < 6; ++n) vph[n] = v;
+        for (int n = 0; n < 6; ++n) {
+            const std::string k = std::string("MUR_PhaseVelocity_") + bnames[n];
+            if (bcn->attr(k.c_str())) L.num(*bcn, k.c_str(), vph[n], 0);
+        }
     }
     // ---- <ContinuousStructure>: grid
     const XNode* grid = csx->child("RectilinearGrid");
@@ -403,6 +413,7 @@ int fdtd_scene_load_xml(const char* text, fdtd_scene_t* out, fdtd_xml_info* info
         if ((rc = fdtd_scene_set_background(sc, e, m, k, s))) return fail(rc, "background material");
     }
     if ((rc = fdtd_scene_set_boundary(sc, bc, pml))) return fail(rc, "boundary conditions");
+    if ((rc = fdtd_scene_set_mur_velocity(sc, vph))) return fail(rc, "Mur phase velocity");
     if (inf.excite_type == 0 && (rc = fdtd_scene_set_gauss_excite(sc, f0, fc, inf.nr_ts)))
         return fail(rc, "Gaussian excitation");
     if (inf.oversampling && (rc = fdtd_scene_set_oversampling(sc, inf.oversampling))) return fail(rc, "OverSampling");

@@ -92,6 +92,10 @@ class Scene:
         s = (C.c_uint32 * 6)(*pml_size)
         check(lib().fdtd_scene_set_boundary(self._h, b, s), "set_boundary")
 
+    def set_mur_velocity(self, v_phase):
+        """Mur phase velocity per face (m/s, 0 = from the boundary material)."""
+        check(lib().fdtd_scene_set_mur_velocity(self._h, (C.c_double * 6)(*v_phase)), "set_mur_velocity")
+
     def set_gauss_excite(self, f0: float, fc: float, nr_ts: int):
         self.nr_ts = int(nr_ts)
         check(lib().fdtd_scene_set_gauss_excite(self._h, f0, fc, int(nr_ts)), "set_gauss_excite")

@@ -19,7 +19,7 @@ import math
 
 import numpy as np
 
-from .fdtd import BC_PEC, BC_PML, Scene
+from .fdtd import BC_MUR, BC_PEC, BC_PML, Scene
 
 
 def uniform_lines(cells: int, delta: float) -> np.ndarray:
@@ -230,6 +230,10 @@ def mini(kind: str, seed: int = 0, nr_ts: int = 400) -> Scene:
         return port_scene([21, 17, 37], 1.0, 0, 3, seed, 5e9, 5e9, nr_ts, edge_range=(2, 6))
     if kind == "upml":
         return port_scene([33, 29, 41], 0.5, 6, 5, seed, 10e9, 10e9, nr_ts, edge_range=(2, 8))
+    if kind == "mur":  # Mur on five faces, PEC below, dielectric bricks, lumped port
+        s = port_scene([31, 27, 39], 0.5, 0, 4, seed, 10e9, 10e9, nr_ts, edge_range=(2, 8))
+        s.set_boundary([BC_MUR, BC_MUR, BC_MUR, BC_MUR, BC_PEC, BC_MUR], [0] * 6)
+        return s
     if kind == "graded":
         rng = np.random.default_rng(seed)
         lines = [graded_lines(c, rng) for c in (30, 26, 35)]
