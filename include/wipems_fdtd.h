@@ -396,6 +396,17 @@ int fdtd_engine_query(fdtd_engine_t eng, int* ready);
 int fdtd_engine_set_fd(fdtd_engine_t eng, const double* freqs, uint32_t nfreq,
                        uint32_t fd_interval);
 int fdtd_engine_read_fd(fdtd_engine_t eng, double* re_im, uint32_t* samples);
+/* Checkpoint / resume (no counterpart in the reference, which has no
+ * restart): every piece of the engine's device state -- fields, UPML flux,
+ * Lorentz/Drude and Mur state, numTS, energy accumulators, the recorded
+ * samples and frequency-domain sums -- as one host blob.  checkpoint with
+ * buf = NULL only reports the size.  restore loads a blob into an engine
+ * made from the same operator with the same options (before or after its
+ * first iterate); stepping on from there gives the same results, bit for
+ * bit, as stepping on from the checkpointed engine.  A server can use it to
+ * take a job off the GPU and put it back later. */
+int fdtd_engine_checkpoint(fdtd_engine_t eng, void* buf, uint64_t cap, uint64_t* size);
+int fdtd_engine_restore(fdtd_engine_t eng, const void* buf, uint64_t size);
 /* 1 once the engine's end criterion (opts.end_crit) stopped it, as of the
  * last iterate; numTS then stays at the stopping timestep. */
 int fdtd_engine_done(fdtd_engine_t eng, int* done);

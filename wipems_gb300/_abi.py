@@ -170,6 +170,8 @@ SIGNATURES = [
     ("fdtd_engine_wait", C.c_int, [_P]),
     ("fdtd_engine_query", C.c_int, [_P, C.POINTER(C.c_int)]),
     ("fdtd_engine_set_fd", C.c_int, [_P, PD, u32, u32]),
+    ("fdtd_engine_checkpoint", C.c_int, [_P, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
+    ("fdtd_engine_restore", C.c_int, [_P, _P, C.c_uint64]),
     ("fdtd_engine_read_fd", C.c_int, [_P, PD, PU32]),
     ("fdtd_engine_done", C.c_int, [_P, C.POINTER(C.c_int)]),
     ("fdtd_engine_num_timesteps", C.c_int, [_P, PU32]),

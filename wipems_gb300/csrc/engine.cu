@@ -907,6 +907,148 @@ int fdtd_engine_read_fd(fdtd_engine_t e, double* re_im, uint32_t* samples) {
     return FDTD_OK;
 }
 
+// ------------------------------------------------------------ checkpoints
+// Blob: a header, then every piece of device state as (element count, raw
+// bytes) in a fixed order; restore checks each count against the engine.
+namespace {
+struct CkptHeader {
+    char magic[8];
+    uint32_t version;
+    uint32_t N[3];
+    int32_t Nzp;
+    uint32_t nprobe, row_doubles, nfreq, nmur;
+    uint32_t ts, done, nsamp;
+    int32_t fused;
+};
+
+struct CkptPart {
+    void* p;
+    size_t bytes;
+};
+
+std::vector<CkptPart> ckpt_parts(fdtd_engine_s* e, uint32_t nsamp) {
+    std::vector<CkptPart> v;
+    auto add = [&](void* p, size_t bytes) { v.push_back(CkptPart{p, p ? bytes : 0}); };
+    const size_t F = 3 * (size_t)e->comp * sizeof(float);
+    add(e->ctl.p, 4 * sizeof(int));
+    add(e->d_eacc.p, 4 * sizeof(double));
+    for (DevBuf<float>* b : {&e->V, &e->I, &e->FV, &e->FI, &e->AV, &e->LV, &e->AI, &e->LI, &e->V2, &e->I2, &e->FV2})
+        add(b->p, F);
+    add(e->ring.p, (size_t)nsamp * e->ps.row_doubles * sizeof(double));
+    add(e->d_fd.p, e->d_fd.n * sizeof(double));
+    add(e->d_fd_count.p, sizeof(int));
+    add(e->mur_buf.p, e->mur_buf.n * sizeof(float));
+    return v;
+}
+
+void ckpt_header(const fdtd_engine_s* e, uint32_t nsamp, CkptHeader& h) {
+    std::memset(&h, 0, sizeof(h));
+    std::memcpy(h.magic, "WFDTDCK1", 8);
+    h.version = 1;
+    for (int a = 0; a < 3; ++a) h.N[a] = e->N[a];
+    h.Nzp = e->Nzp;
+    h.nprobe = (uint32_t)e->ps.nprobe;
+    h.row_doubles = (uint32_t)e->ps.row_doubles;
+    h.nfreq = (uint32_t)e->h_freq.size();
+    h.nmur = (uint32_t)e->mur.nface;
+    h.ts = e->ts;
+    h.done = e->done ? 1u : 0u;
+    h.nsamp = nsamp;
+    h.fused = e->fused ? 1 : 0;
+}
+}  // namespace
+
+int fdtd_engine_checkpoint(fdtd_engine_t e, void* buf, uint64_t cap, uint64_t* size) {
+    if (!e || !size) return FDTD_ERR_ARG;
+    if (e->pending) {
+        set_error("fdtd_engine_checkpoint: wait for the asynchronous iterate first");
+        return FDTD_ERR_STATE;
+    }
+    CK(cudaSetDevice(e->device));
+    int rc;
+    if ((rc = start(e))) return rc;  // a checkpoint of a fresh engine holds its ts = 0 sample
+    int ctl[4] = {0, 0, 0, 0};
+    CK(cudaMemcpyAsync(ctl, e->ctl.p, sizeof(ctl), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    const uint32_t nsamp = (uint32_t)ctl[1];
+    const std::vector<CkptPart> parts = ckpt_parts(e, nsamp);
+    uint64_t need = sizeof(CkptHeader);
+    for (const CkptPart& q : parts) need += sizeof(uint64_t) + q.bytes;
+    *size = need;
+    if (!buf) return FDTD_OK;  // size query
+    if (cap < need) {
+        set_error("fdtd_engine_checkpoint: buffer too small");
+        return FDTD_ERR_ARG;
+    }
+    CkptHeader h;
+    ckpt_header(e, nsamp, h);
+    char* o = static_cast<char*>(buf);
+    std::memcpy(o, &h, sizeof(h));
+    o += sizeof(h);
+    for (const CkptPart& q : parts) {
+        const uint64_t b = q.bytes;
+        std::memcpy(o, &b, sizeof(b));
+        o += sizeof(b);
+        if (b) CK(cudaMemcpyAsync(o, q.p, b, cudaMemcpyDeviceToHost, e->stream));
+        o += b;
+    }
+    CK(cudaStreamSynchronize(e->stream));
+    return FDTD_OK;
+}
+
+int fdtd_engine_restore(fdtd_engine_t e, const void* buf, uint64_t size) {
+    if (!e || !buf) return FDTD_ERR_ARG;
+    if (e->pending) {
+        set_error("fdtd_engine_restore: wait for the asynchronous iterate first");
+        return FDTD_ERR_STATE;
+    }
+    if (size < sizeof(CkptHeader)) {
+        set_error("fdtd_engine_restore: blob too small");
+        return FDTD_ERR_ARG;
+    }
+    CkptHeader h;
+    std::memcpy(&h, buf, sizeof(h));
+    CkptHeader mine;
+    if (!e->started) e->need_initial_sample = false;  // the blob holds the samples
+    CK(cudaSetDevice(e->device));
+    int rc;
+    if ((rc = start(e))) return rc;
+    ckpt_header(e, h.nsamp, mine);
+    if (std::memcmp(h.magic, mine.magic, 8) != 0 || h.version != mine.version || h.N[0] != mine.N[0] ||
+        h.N[1] != mine.N[1] || h.N[2] != mine.N[2] || h.Nzp != mine.Nzp || h.nprobe != mine.nprobe ||
+        h.row_doubles != mine.row_doubles || h.nfreq != mine.nfreq || h.nmur != mine.nmur || h.fused != mine.fused) {
+        set_error("fdtd_engine_restore: the checkpoint belongs to a different engine configuration");
+        return FDTD_ERR_ARG;
+    }
+    if (h.nsamp > (uint32_t)e->ps.cap) {
+        set_error("fdtd_engine_restore: the checkpoint holds more samples than this engine's ring");
+        return FDTD_ERR_ARG;
+    }
+    const std::vector<CkptPart> parts = ckpt_parts(e, h.nsamp);
+    const char* o = static_cast<const char*>(buf) + sizeof(h);
+    const char* end = static_cast<const char*>(buf) + size;
+    for (const CkptPart& q : parts) {
+        uint64_t b = 0;
+        if (o + sizeof(b) > end) {
+            set_error("fdtd_engine_restore: blob truncated");
+            return FDTD_ERR_ARG;
+        }
+        std::memcpy(&b, o, sizeof(b));
+        o += sizeof(b);
+        if (b != q.bytes || o + b > end) {
+            set_error("fdtd_engine_restore: a state array does not match this engine");
+            return FDTD_ERR_ARG;
+        }
+        if (b) CK(cudaMemcpyAsync(q.p, o, b, cudaMemcpyHostToDevice, e->stream));
+        o += b;
+    }
+    CK(cudaStreamSynchronize(e->stream));
+    e->ts = h.ts;
+    e->done = h.done != 0;
+    e->need_initial_sample = false;
+    return FDTD_OK;
+}
+
 int fdtd_engine_query(fdtd_engine_t e, int* ready) {
     if (!e || !ready) return FDTD_ERR_ARG;
     if (!e->pending) {

@@ -366,6 +366,18 @@ class Engine:
         check(lib().fdtd_engine_read_fd(self._h, buf.ctypes.data_as(_abi.PD), C.byref(cnt)), "fdtd_engine_read_fd")
         return buf[..., 0] + 1j * buf[..., 1], cnt.value
 
+    def checkpoint(self) -> bytes:
+        """All device state of the engine as bytes (fdtd_engine_checkpoint)."""
+        size = C.c_uint64()
+        check(lib().fdtd_engine_checkpoint(self._h, None, 0, C.byref(size)), "fdtd_engine_checkpoint")
+        buf = C.create_string_buffer(size.value)
+        check(lib().fdtd_engine_checkpoint(self._h, buf, size.value, C.byref(size)), "fdtd_engine_checkpoint")
+        return buf.raw[:size.value]
+
+    def restore(self, blob: bytes):
+        """Loads a checkpoint of an engine made from the same operator."""
+        check(lib().fdtd_engine_restore(self._h, blob, len(blob)), "fdtd_engine_restore")
+
     def iterate_async(self, n: int):
         """Queues n timesteps on the engine's stream and returns (wait())."""
         check(lib().fdtd_engine_iterate_async(self._h, int(n)), "fdtd_engine_iterate_async")
