@@ -104,6 +104,21 @@ int fdtd_scene_add_metal(fdtd_scene_t s, int priority,
 int fdtd_scene_add_lumped(fdtd_scene_t s, int priority,
                           const double start[3], const double stop[3],
                           int direction, double R, double C, int caps);
+/* Lumped RLC element (CSPropLumpedElement with an inductance or the series
+ * type; Operator_Ext_LumpedRLC, operator_ext_lumpedRLC.cpp:112-486, and
+ * Engine_Ext_LumpedRLC, engine_ext_lumpedRLC.cpp:83-145).  type:
+ * FDTD_LE_PARALLEL (R || L || C; with L not given this is the element of
+ * fdtd_scene_add_lumped), FDTD_LE_SERIES (R - L - C in series) or
+ * FDTD_LE_INVALID (ignored, as the reference ignores it).  R, L, C < 0 mean
+ * "not given".  The Gaussian's f0 + fc is the highest frequency used to
+ * bound the edge's parasitic capacitance. */
+#define FDTD_LE_INVALID (-1)
+#define FDTD_LE_PARALLEL 0
+#define FDTD_LE_SERIES 1
+int fdtd_scene_add_lumped_rlc(fdtd_scene_t s, int priority,
+                              const double start[3], const double stop[3],
+                              int direction, int type, double R, double L,
+                              double C, int caps);
 /* Excitation box: exc_type 0 soft-E, 1 hard-E, 2 soft-H, 3 hard-H;
  * vec = weighted excitation per direction; delay in seconds
  * (operator_ext_excitation.cpp:134-220). */
@@ -221,6 +236,21 @@ typedef struct {
     uint32_t start_ts;
 } fdtd_mur_desc;
 
+/* Lumped RLC edges (Operator_Ext_LumpedRLC, operator_ext_lumpedRLC.h:59-79):
+ * per edge its node position and direction and the ADE coefficients.  Per
+ * timestep, after the other post-update hooks:
+ *   Il += i2v ilv Vd[n-1]                          (parallel inductor)
+ *   Vd  = vvd (V - Il + vv2 Vd[n-2] + vj1 J[n-1] + vj2 J[n-2]);  V = Vd
+ *   J   = ib0 (Vd - Vd[n-2]) - b1 ib0 J[n-1] - b2 ib0 J[n-2]      */
+typedef struct {
+    uint32_t count;
+    const uint32_t* pos[3];
+    const int* dir;
+    const float* ilv; const float* i2v;
+    const float* vv2; const float* vj1; const float* vj2; const float* vvd;
+    const float* ib0; const float* b1; const float* b2;
+} fdtd_rlc_desc;
+
 /* Everything Engine_CUDA needs from an Operator after CalcECOperator. */
 typedef struct {
     uint32_t num_lines[3];
@@ -254,6 +284,8 @@ typedef struct {
     /* Mur faces (Operator_Ext_Mur_ABC), in the order of the faces */
     uint32_t num_mur;
     const fdtd_mur_desc* mur;
+    /* lumped RLC edges (NULL or count 0 = none) */
+    const fdtd_rlc_desc* rlc;
 } fdtd_op_desc;
 
 /* Fills desc with pointers into op's host arrays (valid while op lives). */

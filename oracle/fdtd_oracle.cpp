@@ -13,6 +13,8 @@
 //   Engine_Ext_LorentzMaterial pre-updates      extensions/engine_ext_lorentzmaterial.cpp:79-173
 //   Engine_Ext_Dispersive::Apply2*              extensions/engine_ext_dispersive.cpp:76-132
 //   Engine_Ext_Excitation::Apply2*              extensions/engine_ext_excitation.cpp:33-99
+//   Engine_Ext_Mur_ABC pre/post/apply           extensions/engine_ext_mur_abc.cpp:84-164
+//   Engine_Ext_LumpedRLC pre/apply              extensions/engine_ext_lumpedRLC.cpp:83-145
 //   Engine_Interface_FDTD::CalcVoltageIntegral  FDTD/engine_interface_fdtd.cpp:200-226
 //   ProcessCurrent::CalcIntegral (float acc.)   Common/processcurrent.cpp:93-168
 //   Engine_Interface_FDTD::CalcFastEnergy       FDTD/engine_interface_fdtd.cpp:292-337
@@ -69,6 +71,8 @@ struct BasicEngine {
     std::vector<std::vector<float>> vADE, vLor, cADE, cLor;
     // Mur ABC buffers per face (m_volt_nyP / m_volt_nyPP)
     std::vector<std::vector<float>> murP, murPP;
+    // lumped RLC state (v_Il, v_Vdn[3], v_Jn[3]), rotated like the reference's pointers
+    std::vector<float> rlcIl, rlcVd[3], rlcJ[3];
 
     explicit BasicEngine(const fdtd_op_desc* d) : op(d) {
         for (int n = 0; n < 3; ++n) N[n] = d->num_lines[n];
@@ -84,6 +88,13 @@ struct BasicEngine {
         for (uint32_t f = 0; f < d->num_mur; ++f) {
             murP.emplace_back((size_t)d->mur[f].n_p * d->mur[f].n_pp, 0.f);
             murPP.emplace_back((size_t)d->mur[f].n_p * d->mur[f].n_pp, 0.f);
+        }
+        if (d->rlc && d->rlc->count) {
+            rlcIl.assign(d->rlc->count, 0.f);
+            for (int k = 0; k < 3; ++k) {
+                rlcVd[k].assign(d->rlc->count, 0.f);
+                rlcJ[k].assign(d->rlc->count, 0.f);
+            }
         }
         for (uint32_t o = 0; o < d->num_ade_orders; ++o) {
             size_t c = 3 * (size_t)d->ade[o].count;
@@ -218,6 +229,30 @@ struct BasicEngine {
         }
     }
 
+    // ---- lumped RLC (engine_ext_lumpedRLC.cpp:83-145)
+    void rlc_pre() {  // DoPreVoltageUpdates: rotate Vd, parallel inductor current
+        if (!op->rlc || !op->rlc->count) return;
+        const fdtd_rlc_desc& r = *op->rlc;
+        std::swap(rlcVd[2], rlcVd[1]);  // Vd[2] <- Vd[1], Vd[1] <- Vd[0], Vd[0] <- old Vd[2]
+        std::swap(rlcVd[1], rlcVd[0]);
+        for (uint32_t k = 0; k < r.count; ++k) rlcIl[k] += r.i2v[k] * r.ilv[k] * rlcVd[1][k];
+    }
+    template <class Acc>
+    void rlc_apply(Acc&& Vf) {  // Apply2Voltages
+        if (!op->rlc || !op->rlc->count) return;
+        const fdtd_rlc_desc& r = *op->rlc;
+        std::swap(rlcJ[2], rlcJ[1]);
+        std::swap(rlcJ[1], rlcJ[0]);
+        for (uint32_t k = 0; k < r.count; ++k) rlcVd[0][k] = Vf(r.dir[k], r.pos[0][k], r.pos[1][k], r.pos[2][k]);
+        for (uint32_t k = 0; k < r.count; ++k) {
+            rlcVd[0][k] = r.vvd[k] * (rlcVd[0][k] - rlcIl[k] + r.vv2[k] * rlcVd[2][k] + r.vj1[k] * rlcJ[1][k] +
+                                      r.vj2[k] * rlcJ[2][k]);
+            rlcJ[0][k] = r.ib0[k] * (rlcVd[0][k] - rlcVd[2][k]) - (r.b1[k] * r.ib0[k]) * rlcJ[1][k] -
+                         (r.b2[k] * r.ib0[k]) * rlcJ[2][k];
+        }
+        for (uint32_t k = 0; k < r.count; ++k) Vf(r.dir[k], r.pos[0][k], r.pos[1][k], r.pos[2][k]) = rlcVd[0][k];
+    }
+
     // ---- Lorentz / Drude (engine_ext_lorentzmaterial.cpp:79-173)
     template <bool VOLT>
     void ade_pre() {
@@ -288,21 +323,23 @@ struct BasicEngine {
     }
 
     // Engine::IterateTS with the extension list sorted by priority:
-    // [UPML slabs (1e6, reverse insertion), Lorentz (0), Mur faces (0,
-    // reverse insertion: Lorentz is added after the boundaries,
-    // openems.cpp:1051-1092), Excitation (-1000)].
+    // [UPML slabs (1e6, reverse insertion), lumped RLC, Lorentz, Mur faces
+    // (all 0, reverse insertion: the boundaries are added first, then
+    // Lorentz, then RLC, openems.cpp:1051-1096), Excitation (-1000)].
     // Pre hooks run in reverse list order, post / apply hooks in list order.
     void iterate(unsigned iterTS) {
         const uint32_t nu = op->num_upml;
         auto Vf = [this](int n, uint32_t x, uint32_t y, uint32_t z) -> float& { return V(n, x, y, z); };
         for (unsigned it = 0; it < iterTS; ++it) {
-            // DoPreVoltageUpdates: excitation (none), Mur faces, Lorentz, UPML slabs
+            // DoPreVoltageUpdates: excitation (none), Mur faces, Lorentz, RLC, UPML slabs
             mur(0, numTS, Vf);
             ade_pre<true>();
+            rlc_pre();
             for (uint32_t s = 0; s < nu; ++s) upml<true, true>(s);
             update_voltages(0, N[0]);
             for (uint32_t s = nu; s-- > 0;) upml<true, false>(s);
             mur(1, numTS, Vf);
+            rlc_apply(Vf);
             ade_apply<true>();
             mur(2, numTS, Vf);
             excite<true>();
@@ -706,6 +743,8 @@ void sse_mt_iterate(SSEEngine& S, BasicEngine& B, unsigned iterTS, unsigned nthr
             bar.wait();
             if (tid == 0) H.ade_pre<true>();
             bar.wait();
+            if (tid == 0) B.rlc_pre();
+            bar.wait();
             for (uint32_t s = 0; s < nu; ++s) {
                 H.upml<true, true>(s, u_start[s][tid], u_num[s][tid]);
                 bar.wait();
@@ -717,6 +756,8 @@ void sse_mt_iterate(SSEEngine& S, BasicEngine& B, unsigned iterTS, unsigned nthr
                 bar.wait();
             }
             if (tid == 0 && B.op->num_mur) B.mur(1, ts, Vs);
+            bar.wait();
+            if (tid == 0) B.rlc_apply(Vs);
             bar.wait();
             if (tid == 0) H.ade_apply<true>();
             bar.wait();

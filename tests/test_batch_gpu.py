@@ -110,3 +110,12 @@ def test_batch_end_criterion_same_as_alone():
     for s, j in zip(solo, jobs):
         assert j.num_timesteps == s.num_timesteps and j.done == s.done
         _check_same(s, j)
+
+
+@pytest.mark.parametrize("kind,what", [("mur", "Mur"), ("rlc", "lumped RLC")])
+def test_batch_refuses_unbatched_extensions(kind, what):
+    from wipems_gb300._abi import FdtdError
+    plain = Engine(Operator(scenes.mini("upml", seed=3, nr_ts=100)))
+    other = Engine(Operator(scenes.mini(kind, seed=3, nr_ts=100)))
+    with pytest.raises(FdtdError, match=what):
+        Batch([plain, other])

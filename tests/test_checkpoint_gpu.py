@@ -17,7 +17,8 @@ def _engine(op, **kw):
     return e
 
 
-@pytest.mark.parametrize("kind,kw", [("upml", {}), ("drude", {}), ("mur", {}), ("pec", dict(kernel="fused")),
+@pytest.mark.parametrize("kind,kw", [("upml", {}), ("drude", {}), ("mur", {}), ("rlc_mur", {}),
+                                     ("pec", dict(kernel="fused")),
                                      ("lorentz", dict(use_graphs=False, kernel="direct"))])
 def test_resume_is_bit_identical(kind, kw):
     op = Operator(scenes.mini(kind, seed=2, nr_ts=800))

@@ -22,7 +22,7 @@ pytestmark = pytest.mark.usefixtures("libs")
 GOLDEN = Path(__file__).resolve().parent / "golden"
 
 
-@pytest.mark.parametrize("kind", ["pec", "upml", "drude", "lorentz", "mixed", "mur"])
+@pytest.mark.parametrize("kind", ["pec", "upml", "drude", "lorentz", "mixed", "mur", "rlc", "rlc_mur"])
 def test_basic_and_sse_compressed_engines_agree_bitwise(kind):
     op = Operator(scenes.mini(kind, nr_ts=200))
     a = oracle.run(op.desc, op.probes, 150, op.probe_interval, engine=oracle.BASIC)

@@ -44,7 +44,7 @@ def compare(op, eng, ref, bitwise=True):
 
 
 @pytest.mark.parametrize("kernel", ["tma", "direct"])
-@pytest.mark.parametrize("kind", ["pec", "upml", "graded", "drude", "lorentz", "mixed", "mur"])
+@pytest.mark.parametrize("kind", ["pec", "upml", "graded", "drude", "lorentz", "mixed", "mur", "rlc", "rlc_mur"])
 def test_mini_scenes_match_oracle(kind, kernel):
     """Uniform meshes: bit-identical.  Graded meshes (automatic factorized
     geometry): within the probe / field tolerance of the oracle on the
@@ -284,3 +284,21 @@ def test_mur_chunking_graphs_and_excitation_on_the_face():
     eng = Engine(op)
     eng.iterate(n)
     compare(op, eng, ref)
+
+
+def test_rlc_through_graph_chunks_and_single_steps():
+    """The lumped RLC pass keeps its Vd / J history in a ring indexed by the
+    timestep, so CUDA-graph chunks, single steps and the direct kernels all
+    reproduce the reference's pointer rotation bit for bit; the fused
+    single-pass kernel refuses RLC elements."""
+    op = Operator(scenes.mini("rlc_mur", seed=1, nr_ts=700))
+    ref = oracle.run(op.desc, op.probes, 333, op.probe_interval, engine=oracle.BASIC)
+    for kw, chunks in ((dict(), [100, 233]), (dict(use_graphs=False, x_chunk=3), [1, 2, 330]),
+                       (dict(kernel="direct"), [333])):
+        eng = Engine(op, **kw)
+        for c in chunks:
+            eng.iterate(c)
+        compare(op, eng, ref)
+    from wipems_gb300._abi import FdtdError
+    with pytest.raises(FdtdError, match="lumped RLC"):
+        Engine(Operator(scenes.mini("rlc", nr_ts=100)), kernel="fused")

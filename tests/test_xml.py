@@ -119,3 +119,26 @@ def test_xml_mur_boundaries():
     assert np.array_equal(ca, cb)
     c0t = 2e8 * a.dT  # phase velocity given: c = (v dT - d) / (v dT + d), d = 0.5 mm
     assert np.allclose(ca, np.float32((c0t - 0.5e-3) / (c0t + 0.5e-3)))
+
+
+@pytest.mark.parametrize("letype,extra,n_rlc", [("1", 'L="2e-9" C="1e-12"', 4), ("0", 'L="2e-9"', 4),
+                                                ("-1", 'L="2e-9"', 0)])
+def test_xml_lumped_rlc(letype, extra, n_rlc):
+    """<LumpedElement LEtype> with an inductance or the series type goes to
+    the lumped RLC extension; an invalid type is ignored, as the reference
+    ignores it (neither Calc_LumpedElements nor the RLC extension takes it)."""
+    text = (GOLDEN / "port_box.xml").read_text().replace(
+        "</Properties>",
+        f'<LumpedElement ID="9" Name="rlc" Direction="0" Caps="0" R="25" {extra} LEtype="{letype}">'
+        '<Primitives><Box Priority="7"><P1 X="3" Y="2" Z="3"/><P2 X="4" Y="3" Z="3"/></Box></Primitives>'
+        "</LumpedElement></Properties>", 1)
+    a = Operator(Scene.from_xml(text))
+    s = _api_scene()
+    L = 2e-9
+    C = 1e-12 if letype == "1" else -1.0
+    s.add_lumped_rlc([3, 2, 3], [4, 3, 3], 0, R=25.0, L=L, Cap=C, caps=False, priority=7, le_type=int(letype))
+    b = Operator(s)
+    _same_operator(a, b)
+    na = a.desc.rlc.contents.count if a.desc.rlc else 0
+    nb = b.desc.rlc.contents.count if b.desc.rlc else 0
+    assert na == nb == n_rlc

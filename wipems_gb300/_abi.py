@@ -42,6 +42,12 @@ class FdtdMurDesc(C.Structure):
                 ("coef_p", PF), ("coef_pp", PF), ("start_ts", u32)]
 
 
+class FdtdRlcDesc(C.Structure):
+    _fields_ = [("count", u32), ("pos", PU32 * 3), ("dir", C.POINTER(C.c_int)),
+                ("ilv", PF), ("i2v", PF), ("vv2", PF), ("vj1", PF), ("vj2", PF), ("vvd", PF),
+                ("ib0", PF), ("b1", PF), ("b2", PF)]
+
+
 class FdtdOpDesc(C.Structure):
     _fields_ = [("num_lines", u32 * 3), ("dT", C.c_double),
                 ("vv", PF), ("vi", PF), ("ii", PF), ("iv", PF),
@@ -53,7 +59,8 @@ class FdtdOpDesc(C.Structure):
                 ("curr_delay", PU32),
                 ("signal_length", u32), ("signal_volt", PF), ("signal_curr", PF), ("signal_period_ts", u32),
                 ("lines", C.POINTER(C.c_double) * 3), ("unit", C.c_double),
-                ("num_mur", u32), ("mur", C.POINTER(FdtdMurDesc))]
+                ("num_mur", u32), ("mur", C.POINTER(FdtdMurDesc)),
+                ("rlc", C.POINTER(FdtdRlcDesc))]
 
 
 class FdtdProbeDesc(C.Structure):
@@ -146,6 +153,8 @@ SIGNATURES = [
     ("fdtd_scene_add_material", C.c_int, [_P, C.c_int, PD, PD, C.c_double, C.c_double, C.c_double, C.c_double]),
     ("fdtd_scene_add_metal", C.c_int, [_P, C.c_int, PD, PD]),
     ("fdtd_scene_add_lumped", C.c_int, [_P, C.c_int, PD, PD, C.c_int, C.c_double, C.c_double, C.c_int]),
+    ("fdtd_scene_add_lumped_rlc", C.c_int, [_P, C.c_int, PD, PD, C.c_int, C.c_int, C.c_double, C.c_double,
+                                            C.c_double, C.c_int]),
     ("fdtd_scene_add_excitation", C.c_int, [_P, C.c_int, PD, PD, C.c_int, PD, C.c_double]),
     ("fdtd_scene_add_lorentz", C.c_int, [_P, C.c_int, PD, PD, C.c_double, C.c_double, C.c_double, C.c_double,
                                          C.c_int, PD, PD, PD]),

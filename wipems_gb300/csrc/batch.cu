@@ -285,6 +285,10 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
             set_error("fdtd_batch_create: Mur boundaries are not provided in batches");
             return FDTD_ERR_UNSUPPORTED;
         }
+        if (e->rlc.count) {
+            set_error("fdtd_batch_create: lumped RLC elements are not provided in batches");
+            return FDTD_ERR_UNSUPPORTED;
+        }
         if (e->fd_interval) {
             set_error("fdtd_batch_create: frequency-domain accumulation is not provided in batches");
             return FDTD_ERR_UNSUPPORTED;

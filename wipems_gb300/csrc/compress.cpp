@@ -505,6 +505,62 @@ int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
         // neighbouring faces read it between the update and the apply
         if (m.line == c->N[m.ny] - 1) c->trim_e[m.ny] = false;
     }
+    // Lumped RLC edges.  The engine applies them in a pass after the
+    // voltage kernel (and the Mur post-update); the reference applies them
+    // before the Lorentz/Drude apply and the excitation, which the voltage
+    // kernel has already done -- so an RLC edge must not carry either.
+    if (d->rlc && d->rlc->count) {
+        const fdtd_rlc_desc& r = *d->rlc;
+        std::vector<uint64_t> keys(r.count);
+        for (uint32_t k = 0; k < r.count; ++k) {
+            const int n = r.dir[k];
+            if (n < 0 || n > 2 || r.pos[0][k] >= c->N[0] || r.pos[1][k] >= c->N[1] || r.pos[2][k] >= c->N[2]) {
+                set_error("lumped RLC edge outside the grid");
+                return FDTD_ERR_ARG;
+            }
+            keys[k] = (((uint64_t)r.pos[0][k] * c->N[1] + r.pos[1][k]) * c->N[2] + r.pos[2][k]) * 3 + n;
+        }
+        std::vector<uint64_t> sorted = keys;
+        std::sort(sorted.begin(), sorted.end());
+        if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end()) {
+            set_error("two lumped RLC elements share an edge: not provided");
+            return FDTD_ERR_UNSUPPORTED;
+        }
+        auto has = [&](uint32_t x, uint32_t y, uint32_t z, int n) {
+            const uint64_t key = (((uint64_t)x * c->N[1] + y) * c->N[2] + z) * 3 + n;
+            return std::binary_search(sorted.begin(), sorted.end(), key);
+        };
+        for (uint32_t o = 0; o < d->num_ade_orders; ++o) {
+            const fdtd_ade_desc& a = d->ade[o];
+            if (!a.volt_on) continue;
+            for (uint32_t i = 0; i < a.count; ++i)
+                for (int n = 0; n < 3; ++n)
+                    if (has(a.pos[0][i], a.pos[1][i], a.pos[2][i], n)) {
+                        set_error("a lumped RLC element inside a Lorentz/Drude material: not provided");
+                        return FDTD_ERR_UNSUPPORTED;
+                    }
+        }
+        for (uint32_t i = 0; i < d->volt_count; ++i)
+            if (has(d->volt_index[0][i], d->volt_index[1][i], d->volt_index[2][i], d->volt_dir[i])) {
+                set_error("a voltage excitation on a lumped RLC edge: not provided");
+                return FDTD_ERR_UNSUPPORTED;
+            }
+        RlcList& q = c->rlc;
+        for (int a = 0; a < 3; ++a) q.pos[a].assign(r.pos[a], r.pos[a] + r.count);
+        q.dir.assign(r.dir, r.dir + r.count);
+        q.ilv.assign(r.ilv, r.ilv + r.count);
+        q.i2v.assign(r.i2v, r.i2v + r.count);
+        q.vv2.assign(r.vv2, r.vv2 + r.count);
+        q.vj1.assign(r.vj1, r.vj1 + r.count);
+        q.vj2.assign(r.vj2, r.vj2 + r.count);
+        q.vvd.assign(r.vvd, r.vvd + r.count);
+        q.ib0.assign(r.ib0, r.ib0 + r.count);
+        q.b1.assign(r.b1, r.b1 + r.count);
+        q.b2.assign(r.b2, r.b2 + r.count);
+        for (uint32_t k = 0; k < r.count; ++k)
+            for (int a = 0; a < 3; ++a)
+                if (r.pos[a][k] == c->N[a] - 1) c->trim_e[a] = false;
+    }
     return FDTD_OK;
 }
 

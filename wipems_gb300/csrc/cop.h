@@ -77,6 +77,7 @@ struct fdtd_cop_s {
     bool trim_e[3] = {false, false, false};  // last line inert for the voltage update
     std::vector<float> sigV, sigC;
     std::vector<wipems::MurFace> mur;  // Mur ABC faces (copied from the operator)
+    wipems::RlcList rlc;               // lumped RLC edges (copied from the operator)
     uint32_t sig_len = 0, sig_period = 0;
     ~fdtd_cop_s();
 };

@@ -145,12 +145,26 @@ void launch_mur(fdtd_engine_s* e, int ts_off, int stage) {
     e->last_launches += 1;
 }
 
+void launch_rlc(fdtd_engine_s* e, int ts_off) {
+    const unsigned blocks = std::min<unsigned>((e->rlc.count + 127) / 128, 1024u);
+    k_rlc<<<blocks, 128, 0, e->stream>>>(e->g, e->rlc, ts_off);
+    e->last_launches += 1;
+}
+
+// The voltage half-step with the passes that surround it: Mur pre-update,
+// the voltage kernel, Mur post-update, lumped RLC, Mur apply (the
+// reference's hook order for these extensions).
+void launch_volt_hooks(fdtd_engine_s* e, int ts_off) {
+    if (e->mur.nface) launch_mur(e, ts_off, 0);
+    launch_volt(e, ts_off);
+    if (e->mur.nface) launch_mur(e, ts_off, 1);
+    if (e->rlc.count) launch_rlc(e, ts_off);
+    if (e->mur.nface) launch_mur(e, ts_off, 2);
+}
+
 int launch_step(fdtd_engine_s* e, int ts_off, bool energy) {
-    if (e->mur.nface) {  // Mur faces: pre-update, voltage kernel, post-update, apply
-        launch_mur(e, ts_off, 0);
-        launch_volt(e, ts_off);
-        launch_mur(e, ts_off, 1);
-        launch_mur(e, ts_off, 2);
+    if (e->mur.nface || e->rlc.count) {
+        launch_volt_hooks(e, ts_off);
         launch_curr(e, ts_off, energy);
         e->last_launches += 2;
         return check_launch();
@@ -457,6 +471,7 @@ int reset_state(fdtd_engine_s* e) {
     CK(cudaMemsetAsync(e->ctl.p, 0, 4 * sizeof(int), s));
     if (e->d_fd.p) CK(cudaMemsetAsync(e->d_fd.p, 0, e->d_fd.n * sizeof(double), s));
     if (e->mur_buf.p) CK(cudaMemsetAsync(e->mur_buf.p, 0, e->mur_buf.n * sizeof(float), s));
+    if (e->rlc_state.p) CK(cudaMemsetAsync(e->rlc_state.p, 0, e->rlc_state.n * sizeof(float), s));
     if (e->d_fd_count.p) CK(cudaMemsetAsync(e->d_fd_count.p, 0, sizeof(int), s));
     CK(cudaMemsetAsync(e->d_eacc.p, 0, 4 * sizeof(double), s));
     e->ts = 0;
@@ -610,6 +625,32 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
         e->mur.total = (uint32_t)tot_n;
         e->mur.idx16 = c->E.idx16 ? 1 : 0;
         CK(cudaMemcpyAsync(e->mur_coef.p, hc.data(), hc.size() * sizeof(float), cudaMemcpyHostToDevice, e->stream));
+    }
+    if (c->rlc.size()) {
+        if (e->fused) {
+            set_error("the fused single-pass kernel does not cover lumped RLC elements (use the two-pass kernels)");
+            return FDTD_ERR_UNSUPPORTED;
+        }
+        const size_t n = c->rlc.size();
+        if ((rc = e->rlc_coef.alloc(9 * n, tot)) || (rc = e->rlc_state.alloc(7 * n, tot)) ||
+            (rc = e->rlc_off.alloc(n, tot)))
+            return rc;
+        std::vector<float> hc(9 * n);
+        std::vector<long long> ho(n);
+        const RlcList& r = c->rlc;
+        const std::vector<float>* cols[9] = {&r.ilv, &r.i2v, &r.vv2, &r.vj1, &r.vj2, &r.vvd, &r.ib0, &r.b1, &r.b2};
+        for (int q = 0; q < 9; ++q) std::copy(cols[q]->begin(), cols[q]->end(), hc.begin() + q * n);
+        for (size_t k = 0; k < n; ++k)
+            ho[k] = (long long)r.dir[k] * e->comp + ((long long)r.pos[0][k] * e->N[1] + r.pos[1][k]) * e->Nzp +
+                    r.pos[2][k];
+        CK(cudaMemcpyAsync(e->rlc_coef.p, hc.data(), hc.size() * sizeof(float), cudaMemcpyHostToDevice, e->stream));
+        CK(cudaMemcpyAsync(e->rlc_off.p, ho.data(), n * sizeof(long long), cudaMemcpyHostToDevice, e->stream));
+        CK(cudaMemsetAsync(e->rlc_state.p, 0, 7 * n * sizeof(float), e->stream));
+        CK(cudaStreamSynchronize(e->stream));  // the host staging vectors end here
+        e->rlc.count = (uint32_t)n;
+        e->rlc.off = e->rlc_off.p;
+        e->rlc.coef = e->rlc_coef.p;
+        e->rlc.state = e->rlc_state.p;
     }
     g.Nx = (int)e->N[0];
     g.Ny = (int)e->N[1];
@@ -919,6 +960,7 @@ struct CkptHeader {
     uint32_t nprobe, row_doubles, nfreq, nmur;
     uint32_t ts, done, nsamp;
     int32_t fused;
+    uint32_t nrlc;
 };
 
 struct CkptPart {
@@ -938,13 +980,14 @@ std::vector<CkptPart> ckpt_parts(fdtd_engine_s* e, uint32_t nsamp) {
     add(e->d_fd.p, e->d_fd.n * sizeof(double));
     add(e->d_fd_count.p, sizeof(int));
     add(e->mur_buf.p, e->mur_buf.n * sizeof(float));
+    add(e->rlc_state.p, e->rlc_state.n * sizeof(float));
     return v;
 }
 
 void ckpt_header(const fdtd_engine_s* e, uint32_t nsamp, CkptHeader& h) {
     std::memset(&h, 0, sizeof(h));
     std::memcpy(h.magic, "WFDTDCK1", 8);
-    h.version = 1;
+    h.version = 2;
     for (int a = 0; a < 3; ++a) h.N[a] = e->N[a];
     h.Nzp = e->Nzp;
     h.nprobe = (uint32_t)e->ps.nprobe;
@@ -955,6 +998,7 @@ void ckpt_header(const fdtd_engine_s* e, uint32_t nsamp, CkptHeader& h) {
     h.done = e->done ? 1u : 0u;
     h.nsamp = nsamp;
     h.fused = e->fused ? 1 : 0;
+    h.nrlc = e->rlc.count;
 }
 }  // namespace
 
@@ -1016,7 +1060,8 @@ int fdtd_engine_restore(fdtd_engine_t e, const void* buf, uint64_t size) {
     ckpt_header(e, h.nsamp, mine);
     if (std::memcmp(h.magic, mine.magic, 8) != 0 || h.version != mine.version || h.N[0] != mine.N[0] ||
         h.N[1] != mine.N[1] || h.N[2] != mine.N[2] || h.Nzp != mine.Nzp || h.nprobe != mine.nprobe ||
-        h.row_doubles != mine.row_doubles || h.nfreq != mine.nfreq || h.nmur != mine.nmur || h.fused != mine.fused) {
+        h.row_doubles != mine.row_doubles || h.nfreq != mine.nfreq || h.nmur != mine.nmur || h.fused != mine.fused ||
+        h.nrlc != mine.nrlc) {
         set_error("fdtd_engine_restore: the checkpoint belongs to a different engine configuration");
         return FDTD_ERR_ARG;
     }
@@ -1187,12 +1232,7 @@ int fdtd_engine_profile_kernels(fdtd_engine_t e, uint32_t n_steps, double* ms_vo
             launch_fused(e, 0, sample && e->energy_on_probe);
             CK(cudaEventRecord(ev[3 * k + 1], e->stream));
         } else {
-            if (e->mur.nface) launch_mur(e, 0, 0);
-            launch_volt(e, 0);
-            if (e->mur.nface) {
-                launch_mur(e, 0, 1);
-                launch_mur(e, 0, 2);
-            }
+            launch_volt_hooks(e, 0);
             CK(cudaEventRecord(ev[3 * k + 1], e->stream));
             launch_curr(e, 0, sample && e->energy_on_probe);
         }

@@ -92,6 +92,10 @@ struct fdtd_engine_s {
     // Mur ABC faces
     DevBuf<float> mur_coef, mur_buf;
     MurSet mur{};
+    // lumped RLC edges
+    DevBuf<float> rlc_coef, rlc_state;
+    DevBuf<long long> rlc_off;
+    RlcSet rlc{};
     DevBuf<ProbeEntry> d_entries;
     DevBuf<int> d_first;
     DevBuf<double> d_weight;

@@ -41,7 +41,8 @@ struct Prim {
     double eps_lor_pole_f[kMaxDispOrder] = {0, 0, 0, 0};
     // lumped element
     int ny = 2;
-    double R = -1, C = -1;
+    double R = -1, C = -1, L = -1;
+    int le_type = 0;  // FDTD_LE_PARALLEL / SERIES / INVALID
     bool caps = false;
     // excitation
     int exc_type = 0;
@@ -93,6 +94,14 @@ struct MurFace {
     uint32_t start_ts = 0;
 };
 
+// Operator_Ext_LumpedRLC's arrays (operator_ext_lumpedRLC.h:59-79)
+struct RlcList {
+    std::vector<uint32_t> pos[3];
+    std::vector<int> dir;
+    std::vector<float> ilv, i2v, vv2, vj1, vj2, vvd, ib0, b1, b2;
+    size_t size() const { return dir.size(); }
+};
+
 struct ExcList {
     std::vector<uint32_t> index[3];
     std::vector<uint16_t> dir;
@@ -123,6 +132,8 @@ struct fdtd_operator_s {
     std::vector<fdtd_ade_desc> ade_desc;
     std::vector<wipems::MurFace> mur;
     std::vector<fdtd_mur_desc> mur_desc;
+    wipems::RlcList rlc;
+    fdtd_rlc_desc rlc_desc{};
 };
 
 namespace wipems {

@@ -445,6 +445,53 @@ static __global__ void k_mur(const DevGrid g, MurSet ms, int ts_off, int stage) 
     }
 }
 
+// ------------------------------------------------------------- lumped RLC
+// Engine_Ext_LumpedRLC (engine_ext_lumpedRLC.cpp:83-145) on the device: one
+// pass after the voltage kernel (and after the Mur post-update, before the
+// Mur apply), one thread per RLC edge.  The reference rotates its Vd[0..2]
+// and J[0..2] buffers every step; here the history is a ring indexed by
+// numTS: slot numTS % 3 is [n], (numTS + 2) % 3 is [n-1], (numTS + 1) % 3
+// is [n-2].  The pre-update (parallel inductor current) touches only the
+// element's own state, so it runs in the same pass.  Float products and
+// sums in the reference's order.
+struct RlcSet {
+    uint32_t count;
+    const long long* off;  // dir * comp + x * sx + y * Nzp + z
+    const float* coef;     // [9][count]: ilv, i2v, vv2, vj1, vj2, vvd, ib0, b1, b2
+    float* state;          // [7][count]: Il, Vd[3 slots], J[3 slots]
+};
+
+static __global__ void k_rlc(const DevGrid g, RlcSet rs, int ts_off) {
+    if (*g.d_done) return;
+    const int numTS = *g.d_ts + ts_off;
+    const uint32_t n = rs.count;
+    const uint32_t s0 = (uint32_t)(numTS % 3), s1 = (uint32_t)((numTS + 2) % 3), s2 = (uint32_t)((numTS + 1) % 3);
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const float* c = rs.coef + k;
+        const float ilv = c[0], i2v = c[n], vv2 = c[2 * n], vj1 = c[3 * n], vj2 = c[4 * n], vvd = c[5 * n],
+                    ib0 = c[6 * n], b1 = c[7 * n], b2 = c[8 * n];
+        float* Il = rs.state + k;
+        float* Vd = rs.state + n + k;
+        float* J = rs.state + 4 * n + k;
+        // DoPreVoltageUpdates: Il += i2v * ilv * Vd[n-1]
+        const float il = __fadd_rn(Il[0], __fmul_rn(__fmul_rn(i2v, ilv), Vd[s1 * n]));
+        Il[0] = il;
+        const float vd2 = Vd[s2 * n], j1 = J[s1 * n], j2 = J[s2 * n];
+        // Apply2Voltages
+        float t = __fsub_rn(g.V[rs.off[k]], il);
+        t = __fadd_rn(t, __fmul_rn(vv2, vd2));
+        t = __fadd_rn(t, __fmul_rn(vj1, j1));
+        t = __fadd_rn(t, __fmul_rn(vj2, j2));
+        const float vd = __fmul_rn(vvd, t);
+        float jn = __fmul_rn(ib0, __fsub_rn(vd, vd2));
+        jn = __fsub_rn(jn, __fmul_rn(__fmul_rn(b1, ib0), j1));
+        jn = __fsub_rn(jn, __fmul_rn(__fmul_rn(b2, ib0), j2));
+        Vd[s0 * n] = vd;
+        J[s0 * n] = jn;
+        g.V[rs.off[k]] = vd;
+    }
+}
+
 // Full-grid energy (CalcFastEnergy) on demand.
 static __global__ void k_energy(const DevGrid g, double* out) {
     double es = 0.0, hs = 0.0;

@@ -663,6 +663,9 @@ struct Builder {
     bool calc_lumped() {  // Operator::Calc_LumpedElements (operator.cpp:1535-1712)
         for (const Prim& p : S.prims) {
             if (p.kind != PK_LUMPED) continue;
+            // only parallel R/C elements (IsLEparRC, operator.cpp:1714-1724);
+            // the rest belong to the lumped RLC extension
+            if (!(p.le_type == FDTD_LE_PARALLEL && !(p.L > 0))) continue;
             double C = p.C;
             if (C <= 0) C = NAN;
             double R = p.R;
@@ -715,6 +718,113 @@ struct Builder {
             }
         }
         return true;
+    }
+
+    // Operator_Ext_LumpedRLC::BuildExtension (operator_ext_lumpedRLC.cpp:
+    // 112-486): parallel R||L||C and series R-L-C elements.  Each box is
+    // split into Ncells_0 edges in series along its direction and
+    // Ncells_1 x Ncells_2 in parallel across it; the element's R, L, C are
+    // scaled accordingly.  The edge's own capacitance carries C (parallel)
+    // or stays the parasitic capacitance, raised where it would short the
+    // element below fmax (series, and parallel without C); G is replaced;
+    // vv/vi (and ii/iv) of the edge are recomputed from EC_C/EC_G/EC_L/EC_R.
+    // The double coefficients are stored as float, as the reference copies
+    // its double vectors into FDTD_FLOAT arrays.
+    void calc_rlc(double fmax, RlcList& out) {
+        constexpr double kZFact = 20.0;  // LUMPED_RLC_Z_FACT (operator_ext_lumpedRLC.h:29)
+        for (const Prim& p : S.prims) {
+            if (p.kind != PK_LUMPED) continue;
+            const int type = p.le_type;
+            double C = p.C;
+            if (C < 0) C = NAN;
+            double R = p.R;
+            if (R < 0) R = NAN;
+            double L = p.L;
+            if (L < 0) L = NAN;
+            // IsLElumpedRLC (operator_ext_lumpedRLC.cpp:502-513)
+            if (!((type == FDTD_LE_PARALLEL && L > 0.0) || type == FDTD_LE_SERIES)) continue;
+            const int dir = p.ny;
+            if (dir < 0 || dir > 2) continue;
+            const int d1 = (dir + 1) % 3, d2 = (dir + 2) % 3;
+            uint32_t uiStart[3], uiStop[3];
+            const int dim = g.snap_box(p.start, p.stop, uiStart, uiStop, false, 0, nullptr, nullptr);
+            if (dim <= 0) continue;
+            if (uiStart[dir] == uiStop[dir]) continue;
+            const unsigned Ncells_0 = uiStop[dir] - uiStart[dir];
+            const unsigned Ncells_1 = uiStop[d1] - uiStart[d1] + 1;
+            const unsigned Ncells_2 = uiStop[d2] - uiStart[d2] + 1;
+            const unsigned Npar = Ncells_1 * Ncells_2;
+            const double dL = L * Npar / Ncells_0;
+            const double dR = R * Npar / Ncells_0;
+            double dG = (1 / R) * Ncells_0 / Npar;
+            double dC = C * Ncells_0 / Npar;  // mutable across the box's edges, as in the reference
+            const double ib0 = 2.0 * dT * dC / (4.0 * dL * dC + 2.0 * dT * dR * dC + dT * dT);
+            const double b1 = (dT * dT - 4.0 * dL * dC) / (dT * dC);
+            const double b2 = (4.0 * dL * dC - 2.0 * dT * dR * dC + dT * dT) / (2.0 * dT * dC);
+            if (type == FDTD_LE_PARALLEL && R == 0.0) dG = 0.0;
+            uint32_t pos[3];
+            for (pos[dir] = uiStart[dir]; pos[dir] < uiStop[dir]; ++pos[dir])
+                for (pos[d1] = uiStart[d1]; pos[d1] <= uiStop[d1]; ++pos[d1])
+                    for (pos[d2] = uiStart[d2]; pos[d2] <= uiStop[d2]; ++pos[d2]) {
+                        const size_t i = at(dir, pos);
+                        double Zmin, Zcd_min;
+                        if (type == FDTD_LE_PARALLEL) {
+                            if (dC > 0)
+                                EC_C[i] = (float)dC;
+                            else
+                                dC = EC_C[i];
+                            out.i2v.push_back((float)((dT / dC) / (1.0 + dT * dG / (2.0 * dC))));
+                            if (R >= 0) EC_G[i] = (float)dG;
+                            out.ilv.push_back(L > 0 ? (float)(dT / dL) : 0.f);
+                            if (dC == 0) {
+                                double Cd = EC_C[i];
+                                Zmin = std::max(dR, 2 * kPi * fmax * dL);
+                                Zcd_min = 1.0 / (2.0 * kPi * fmax * Cd);
+                                if (Zcd_min < kZFact * Zmin) {
+                                    Cd = 1.0 / (2 * kPi * fmax * Zmin * kZFact);
+                                    EC_C[i] = (float)Cd;
+                                }
+                            }
+                            out.vv2.push_back(0.f);
+                            out.vj1.push_back(0.f);
+                            out.vj2.push_back(0.f);
+                            out.vvd.push_back(1.f);
+                            out.ib0.push_back(0.f);
+                            out.b1.push_back(0.f);
+                            out.b2.push_back(0.f);
+                        } else {
+                            EC_G[i] = 0.f;
+                            float Cd = EC_C[i];  // FDTD_FLOAT in the reference
+                            Zmin = std::sqrt(std::pow(dR, 2) + std::pow(2 * kPi * fmax * dL - 1.0 / (dC * 2 * kPi * fmax), 2));
+                            Zcd_min = 1.0 / (2.0 * kPi * fmax * Cd);
+                            if (Zcd_min < kZFact * Zmin) {
+                                Cd = (float)(1.0 / (2 * kPi * fmax * Zmin * kZFact));
+                                EC_C[i] = Cd;
+                            }
+                            out.ilv.push_back(0.f);
+                            out.i2v.push_back(0.f);
+                            out.vv2.push_back((float)(0.5 * dT * ib0 / Cd));
+                            out.vj1.push_back((float)(0.5 * dT * (b1 * ib0 - 1.0) / Cd));
+                            out.vj2.push_back((float)(0.5 * dT * b2 * ib0 / Cd));
+                            out.vvd.push_back((float)(1.0 / (1.0 + 0.5 * dT * ib0 / Cd)));
+                            out.ib0.push_back((float)ib0);
+                            out.b1.push_back((float)b1);
+                            out.b2.push_back((float)b2);
+                        }
+                        ec_operator_pos(dir, pos);
+                        out.dir.push_back(dir);
+                        for (int a = 0; a < 3; ++a) out.pos[a].push_back(pos[a]);
+                    }
+            if (p.caps) {  // metal caps at both ends, as Calc_LumpedElements builds them
+                for (pos[d1] = uiStart[d1]; pos[d1] <= uiStop[d1]; ++pos[d1])
+                    for (pos[d2] = uiStart[d2]; pos[d2] <= uiStop[d2]; ++pos[d2])
+                        for (uint32_t end : {uiStart[dir], uiStop[dir]}) {
+                            pos[dir] = end;
+                            if (pos[d1] < uiStop[d1]) { vv[at(d1, pos)] = 0; vi[at(d1, pos)] = 0; }
+                            if (pos[d2] < uiStop[d2]) { vv[at(d2, pos)] = 0; vi[at(d2, pos)] = 0; }
+                        }
+            }
+        }
     }
 };
 
@@ -1073,6 +1183,10 @@ static int build_operator(const fdtd_scene_s& S, int threads, fdtd_operator_s& o
         }
     }
 
+    // ---- extension 9: lumped RLC elements (added last, openems.cpp:1095-1096);
+    // fmax = GetCenterFreq() + GetCutOffFreq() of the Gaussian
+    B.calc_rlc(S.f0 + S.fc, op.rlc);
+
     // ---- excitation signal (Excitation::CalcGaussianPulsExcitation)
     if (S.have_excite) {
         double f0 = S.f0, fc = S.fc;
@@ -1361,6 +1475,23 @@ int fdtd_scene_add_lumped(fdtd_scene_t s, int prio, const double start[3], const
     return FDTD_OK;
 }
 
+int fdtd_scene_add_lumped_rlc(fdtd_scene_t s, int prio, const double start[3], const double stop[3], int dir,
+                              int type, double R, double L, double C, int caps) {
+    if (!s || !check_box(start, stop) || dir < 0 || dir > 2 || type < FDTD_LE_INVALID || type > FDTD_LE_SERIES) {
+        set_error("fdtd_scene_add_lumped_rlc: invalid box, direction or type");
+        return FDTD_ERR_ARG;
+    }
+    Prim p = make_box(PK_LUMPED, prio, start, stop);
+    p.ny = dir;
+    p.le_type = type;
+    p.R = R;
+    p.L = L;
+    p.C = C;
+    p.caps = caps != 0;
+    s->prims.push_back(p);
+    return FDTD_OK;
+}
+
 int fdtd_scene_add_excitation(fdtd_scene_t s, int prio, const double start[3], const double stop[3],
                               int exc_type, const double vec[3], double delay) {
     if (!s || !check_box(start, stop) || !vec || exc_type < 0 || exc_type > 3 || delay < 0) {
@@ -1524,6 +1655,17 @@ int fdtd_operator_describe(fdtd_operator_t op, fdtd_op_desc* d) {
     }
     d->num_mur = (uint32_t)op->mur.size();
     d->mur = op->mur_desc.empty() ? nullptr : op->mur_desc.data();
+    {
+        const RlcList& r = op->rlc;
+        fdtd_rlc_desc& q = op->rlc_desc;
+        q.count = (uint32_t)r.size();
+        for (int n = 0; n < 3; ++n) q.pos[n] = r.pos[n].data();
+        q.dir = r.dir.data();
+        q.ilv = r.ilv.data(); q.i2v = r.i2v.data();
+        q.vv2 = r.vv2.data(); q.vj1 = r.vj1.data(); q.vj2 = r.vj2.data(); q.vvd = r.vvd.data();
+        q.ib0 = r.ib0.data(); q.b1 = r.b1.data(); q.b2 = r.b2.data();
+        d->rlc = q.count ? &op->rlc_desc : nullptr;
+    }
     d->signal_length = op->signal_length;
     d->signal_volt = op->sig_volt.data();
     d->signal_curr = op->sig_curr.data();

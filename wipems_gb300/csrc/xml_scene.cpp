@@ -491,15 +491,15 @@ int fdtd_scene_load_xml(const char* text, fdtd_scene_t* out, fdtd_xml_info* info
             L.num(p, "C", C, NAN);
             L.num(p, "L", Lh, NAN);
             L.num(p, "Caps", caps, 1);
-            if (!std::isnan(Lh) && Lh > 0) L.bad(FDTD_ERR_UNSUPPORTED, "inductive lumped element '" + pname + "'");
-            if (p.attr("LEtype")) {
-                L.num(p, "LEtype", d, -1);
-                if (d != -1 && d != 0) L.bad(FDTD_ERR_UNSUPPORTED, "series lumped element '" + pname + "'");
-            }
+            double type;
+            L.num(p, "LEtype", type, FDTD_LE_PARALLEL);  // -1 invalid, 0 parallel, 1 series
+            if (type != FDTD_LE_INVALID && type != FDTD_LE_PARALLEL && type != FDTD_LE_SERIES)
+                L.bad(FDTD_ERR_ARG, "<LumpedElement LEtype> of '" + pname + "'");
             if (L.code) return fail(L.code, L.err);
             for (const Box& b : boxes) {
-                if ((rc = fdtd_scene_add_lumped(sc, b.priority, b.a, b.b, (int)dir, std::isnan(R) ? -1.0 : R,
-                                                std::isnan(C) ? -1.0 : C, caps != 0)))
+                if ((rc = fdtd_scene_add_lumped_rlc(sc, b.priority, b.a, b.b, (int)dir, (int)type,
+                                                    std::isnan(R) ? -1.0 : R, std::isnan(Lh) ? -1.0 : Lh,
+                                                    std::isnan(C) ? -1.0 : C, caps != 0)))
                     return fail(rc, "lumped element '" + pname + "'");
                 ++inf.num_boxes;
             }

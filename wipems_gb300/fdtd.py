@@ -114,6 +114,17 @@ class Scene:
         check(lib().fdtd_scene_add_lumped(self._h, int(priority), _d3(start), _d3(stop), int(direction), float(R),
                                           float(Cap), int(bool(caps))), "add_lumped")
 
+    def add_lumped_rlc(self, start, stop, direction, R=-1.0, L=-1.0, Cap=-1.0, series=False, caps=True, priority=0,
+                       le_type=None):
+        """Lumped element with an inductance and/or the series type
+        (CSPropLumpedElement; Operator_Ext_LumpedRLC): parallel R || L || C
+        or, with series=True, R - L - C in series.  Values < 0 are "not
+        given".  le_type overrides series with the raw LEtype (-1 invalid:
+        the element is ignored, as the reference ignores it)."""
+        t = (1 if series else 0) if le_type is None else int(le_type)
+        check(lib().fdtd_scene_add_lumped_rlc(self._h, int(priority), _d3(start), _d3(stop), int(direction), t,
+                                              float(R), float(L), float(Cap), int(bool(caps))), "add_lumped_rlc")
+
     def add_excitation(self, start, stop, vec, exc_type=0, delay=0.0, priority=0):
         check(lib().fdtd_scene_add_excitation(self._h, int(priority), _d3(start), _d3(stop), int(exc_type),
                                               _d3(vec), float(delay)), "add_excitation")

@@ -89,6 +89,30 @@ def port_scene(cells, delta, pml, n_bricks, seed, f0, fc, nr_ts, eps_max=12.0, k
     return s
 
 
+def rlc_probe(series: bool, R: float, L: float, Cap: float, nr_ts: int = 8000, cells: int = 24,
+              f0: float = 2e9, fc: float = 2e9) -> Scene:
+    """One lumped RLC edge (1 mm, z-directed) in a UPML-bounded vacuum box,
+    with a voltage probe along the edge and a current loop around it, driven
+    by a soft z excitation four cells away.  The loop current is the edge's
+    total current (element plus edge capacitance), so V/I is the element's
+    impedance in parallel with the edge capacitance."""
+    lines = [uniform_lines(cells, 1.0) for _ in range(3)]
+    s = Scene(*lines, 1e-3)
+    s.set_boundary([BC_PML] * 6, [6] * 6)
+    s.set_gauss_excite(f0, fc, nr_ts)
+    c = cells // 2
+    a = [lines[0][c], lines[1][c], lines[2][c]]
+    b = [lines[0][c], lines[1][c], lines[2][c + 1]]
+    s.add_lumped_rlc(a, b, 2, R=R, L=L, Cap=Cap, series=series, caps=False, priority=10)
+    s.add_excitation([lines[0][c - 4], lines[1][c], lines[2][c]], [lines[0][c - 4], lines[1][c], lines[2][c + 1]],
+                     [0.0, 0.0, 1.0], priority=10)
+    s.add_probe(a, b, 0, name="v")
+    half = 0.5 * (lines[2][c] + lines[2][c + 1])
+    s.add_probe([lines[0][c] - 0.5, lines[1][c] - 0.5, half], [lines[0][c] + 0.5, lines[1][c] + 0.5, half], 1,
+                norm_dir=2, name="i")
+    return s
+
+
 def l256(nr_ts: int = 1000, seed: int = 256, cells: int = 256, n_bricks: int = 40) -> Scene:
     """256^3 cells at 0.5 mm, UPML-8, 40 bricks (edge 8-64 cells, eps_r
     U[1,12], kappa log-U[1e-4,1] S/m), 50 ohm z port with a Gaussian pulse."""
@@ -233,6 +257,26 @@ def mini(kind: str, seed: int = 0, nr_ts: int = 400) -> Scene:
     if kind == "mur":  # Mur on five faces, PEC below, dielectric bricks, lumped port
         s = port_scene([31, 27, 39], 0.5, 0, 4, seed, 10e9, 10e9, nr_ts, edge_range=(2, 8))
         s.set_boundary([BC_MUR, BC_MUR, BC_MUR, BC_MUR, BC_PEC, BC_MUR], [0] * 6)
+        return s
+    if kind in ("rlc", "rlc_mur"):  # series and parallel lumped RLC elements beside the port
+        cells = [33, 29, 41]
+        s = port_scene(cells, 0.5, 6 if kind == "rlc" else 0, 3, seed, 10e9, 10e9, nr_ts, edge_range=(2, 8))
+        lines = [uniform_lines(n, 0.5) for n in cells]
+        c = [n // 2 for n in cells]
+        # series R-L-C along z over three cells, one edge wide
+        s.add_lumped_rlc([lines[0][c[0] - 4], lines[1][c[1]], lines[2][c[2] - 2]],
+                         [lines[0][c[0] - 4], lines[1][c[1]], lines[2][c[2] + 1]], 2,
+                         R=20.0, L=1e-9, Cap=0.5e-12, series=True, caps=False, priority=900)
+        # parallel R || L || C along x over two cells, two lines across, with caps
+        s.add_lumped_rlc([lines[0][c[0] + 3], lines[1][c[1] - 1], lines[2][c[2]]],
+                         [lines[0][c[0] + 5], lines[1][c[1]], lines[2][c[2]]], 0,
+                         R=200.0, L=3e-9, Cap=0.2e-12, caps=True, priority=900)
+        if kind == "rlc_mur":
+            s.set_boundary([BC_MUR, BC_MUR, BC_MUR, BC_MUR, BC_PEC, BC_MUR], [0] * 6)
+            # a series element on the xmin Mur face line (the face's apply overwrites it)
+            s.add_lumped_rlc([lines[0][0], lines[1][c[1] + 3], lines[2][c[2] - 2]],
+                             [lines[0][0], lines[1][c[1] + 3], lines[2][c[2]]], 2,
+                             R=50.0, L=2e-9, Cap=1e-12, series=True, caps=False, priority=900)
         return s
     if kind == "graded":
         rng = np.random.default_rng(seed)

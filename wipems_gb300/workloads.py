@@ -44,6 +44,56 @@ def single(kind: str, steps: int = 0, device: int = 0) -> dict:
                 ade_nodes=info["num_ade_nodes"])
 
 
+def extensions(steps: int = 1000, device: int = 0) -> list:
+    """The cost of the extensions around the hot path on the L256 grid
+    (256^3 cells, 40 bricks, 50 ohm port), one tiling for all variants:
+    UPML-8 (the headline), PEC walls, Mur on all faces, UPML-8 with 64
+    frequency-domain probe frequencies, UPML-8 with four lumped RLC
+    elements (two series, two parallel) beside the port."""
+    from . import CompressedOperator, Engine, Operator, autotune, scenes
+    from .fdtd import BC_MUR, BC_PEC
+
+    def variant(name):
+        sc = scenes.l256(nr_ts=steps)
+        if name == "pec":
+            sc.set_boundary([BC_PEC] * 6, [0] * 6)
+        elif name == "mur":
+            sc.set_boundary([BC_MUR] * 6, [0] * 6)
+        elif name == "rlc":
+            L = scenes.uniform_lines(256, 0.5)
+            c = 128
+            for k, series in enumerate((True, True, False, False)):
+                x = L[c - 6 + 4 * k]
+                sc.add_lumped_rlc([x, L[c + 5], L[c - 2]], [x, L[c + 5], L[c + 2]], 2, R=25.0 + 10 * k,
+                                  L=2e-9, Cap=0.5e-12, series=series, caps=False, priority=900)
+        return sc
+
+    out = []
+    best = None
+    for name in ("upml", "pec", "mur", "fd", "rlc"):
+        op = Operator(variant(name))
+        cop = CompressedOperator(op)
+        if best is None:
+            best, _ = autotune.tune(cop, stages=(3, 4), steps=40, device=device)
+        eng = Engine(cop, device=device, max_timesteps=steps + 100, stages=best["stages"], x_chunk=best["x_chunk"],
+                     kernel=best["kernel"])
+        if name == "fd":
+            eng.set_frequencies(np.linspace(1e9, 20e9, 64))
+        eng.iterate(50)  # warm-up (graph instantiation)
+        eng.reset()
+        eng.iterate(steps)
+        ms, launches = eng.last_timing()
+        n = op.num_nodes
+        out.append(dict(workload="l256_" + name, nodes=n, timesteps=steps, device_ms=round(ms, 3),
+                        mcells=round(n * steps / (ms / 1e3) / 1e6, 1), launches=launches,
+                        us_per_step=round(ms * 1e3 / steps, 2), tiling=best))
+        del eng, cop, op
+    base = out[0]["us_per_step"]
+    for r in out:
+        r["vs_upml"] = round(r["us_per_step"] / base, 4)
+    return out
+
+
 def b96(n_jobs: int = 96, timesteps: int = 1500, device: int = 0) -> dict:
     """B96: the seeded 96-job sweep, plain engine job by job vs one batch
     (autotuned x_chunk / graph length)."""
@@ -162,7 +212,7 @@ def serve(n_jobs: int = 48, mean_gap: float = 0.02, end_crit: float = 1e-4, seed
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("workload", choices=["p64", "d192", "b96", "serve"])
+    ap.add_argument("workload", choices=["p64", "d192", "b96", "serve", "ext"])
     ap.add_argument("--jobs", type=int, default=0)
     ap.add_argument("--timesteps", type=int, default=0)
     ap.add_argument("--gap", type=float, default=0.02)
@@ -176,6 +226,8 @@ def main():
         r = single(args.workload, args.timesteps, args.device)
     elif args.workload == "b96":
         r = b96(args.jobs or 96, args.timesteps or 1500, args.device)
+    elif args.workload == "ext":
+        r = extensions(args.timesteps or 1000, args.device)
     else:
         r = serve(args.jobs or 48, args.gap, device=args.device, batch_min_jobs=args.batch_min,
                   build_workers=args.workers,
