@@ -153,7 +153,11 @@ int batch_smem_attrs(int bytes) {
     return FDTD_OK;
 }
 
-size_t stage_smem(bool i16, bool upml, int S) {
+size_t stage_smem(bool i16, bool upml, bool ade, int S) {
+    if (ade) {  // voltage kernels of groups with Lorentz/Drude nodes stage their states too
+        if (i16) return upml ? StageLayout<uint16_t, true, true>::smem(S) : StageLayout<uint16_t, false, true>::smem(S);
+        return upml ? StageLayout<uint32_t, true, true>::smem(S) : StageLayout<uint32_t, false, true>::smem(S);
+    }
     if (i16) return upml ? StageLayout<uint16_t, true>::smem(S) : StageLayout<uint16_t, false>::smem(S);
     return upml ? StageLayout<uint32_t, true>::smem(S) : StageLayout<uint32_t, false>::smem(S);
 }
@@ -391,7 +395,7 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
         for (const fdtd_engine_s* e : b->jobs) lines.push_back(e->N);
         b->XC = auto_x_chunk(lines, (uint64_t)WIPEMS_BATCH_MIN_BLOCKS * (uint64_t)sms);
     }
-    const size_t maxsm = stage_smem(false, true, b->stages);
+    const size_t maxsm = stage_smem(false, true, true, b->stages);
     if (maxsm > 48 * 1024 && (rc = batch_smem_attrs((int)maxsm))) return rc;
     for (Group& G : b->groups) {
         std::vector<WorkItem> wE, wH;
@@ -414,8 +418,8 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
         CK(cudaMemcpyAsync(G.itE.p, wE.data(), wE.size() * sizeof(WorkItem), cudaMemcpyHostToDevice, b->stream));
         CK(cudaMemcpyAsync(G.itH.p, wH.data(), wH.size() * sizeof(WorkItem), cudaMemcpyHostToDevice, b->stream));
         const bool up = (G.feat & FEAT_UPML) != 0;
-        G.smemE = stage_smem(G.e16, up, b->stages);
-        G.smemH = stage_smem(G.h16, up, b->stages);
+        G.smemE = stage_smem(G.e16, up, (G.feat & FEAT_ADE) != 0, b->stages);
+        G.smemH = stage_smem(G.h16, up, false, b->stages);
         int oE = occupancy(G, true, G.smemE), oH = occupancy(G, false, G.smemH);
         if (b->blocks_per_sm > 0) {
             oE = std::min(oE, b->blocks_per_sm);

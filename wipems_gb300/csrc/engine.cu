@@ -29,7 +29,7 @@ template <typename IdxT, int FEAT, bool GEO>
 void launch_volt_t(fdtd_engine_s* e, int ts_off) {
     if (e->use_tma) {
         constexpr bool UP = (FEAT & FEAT_UPML) != 0;
-        const size_t sm = StageLayout<IdxT, UP>::smem(e->stages);
+        const size_t sm = StageLayout<IdxT, UP, (FEAT & FEAT_ADE) != 0>::smem(e->stages);
         dim3 grid((e->ti.ne[2] + 31) / 32, (e->ti.ne[1] + TMA_TY - 1) / TMA_TY, (e->ti.ne[0] + e->XC - 1) / e->XC);
         k_volt_tma<IdxT, FEAT, GEO><<<grid, dim3(32, TMA_TY), sm, e->stream>>>(e->g, e->maps, e->ti, ts_off, e->XC,
                                                                                e->stages);
@@ -431,6 +431,8 @@ int make_maps(fdtd_engine_s* e) {
     if (e->FV.p && ((rc = field_map(&e->maps.FV_own, e->FV.p, e, 32, TMA_TY)) ||
                     (rc = field_map(&e->maps.FI_own, e->FI.p, e, 32, TMA_TY))))
         return rc;
+    if (e->AV.p && (rc = field_map(&e->maps.AV_own, e->AV.p, e, 32, TMA_TY))) return rc;
+    if (e->LV.p && (rc = field_map(&e->maps.LV_own, e->LV.p, e, 32, TMA_TY))) return rc;
     return FDTD_OK;
 }
 
@@ -667,6 +669,31 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     g.FI = e->FI.p;
     g.AV = e->AV.p;
     g.LV = e->LV.p;
+    if (c->E.any_ade) {  // which voltage-kernel tile planes hold Lorentz/Drude nodes
+        const int ZT = ((int)e->N[2] + 31) / 32, YT = ((int)e->N[1] + TMA_TY - 1) / TMA_TY;
+        std::vector<uint8_t> tf(c->E.num_tuples);
+        for (uint32_t k = 0; k < c->E.num_tuples; ++k) {
+            uint32_t f;
+            std::memcpy(&f, &c->E.main[(size_t)k * TAB_MAIN * 4 + 6], 4);
+            tf[k] = (uint8_t)(((f & TF_ADE) ? 1u : 0u) | ((f & TF_LOR) ? 2u : 0u));
+        }
+        std::vector<uint8_t> h((size_t)e->N[0] * YT * ZT, 0);
+        for (uint32_t x = 0; x < e->N[0]; ++x)
+            for (uint32_t y = 0; y < e->N[1]; ++y) {
+                const size_t row = ((size_t)x * e->N[1] + y) * (size_t)e->Nzp;
+                uint8_t* hf = &h[((size_t)x * YT + y / TMA_TY) * ZT];
+                for (uint32_t z = 0; z < e->N[2]; ++z) {
+                    const uint32_t t = c->E.idx16 ? reinterpret_cast<const uint16_t*>(c->E.idx)[row + z]
+                                                  : reinterpret_cast<const uint32_t*>(c->E.idx)[row + z];
+                    hf[z / 32] |= tf[t];
+                }
+            }
+        if ((rc = e->ade_tile.alloc(h.size(), tot))) return rc;
+        CK(cudaMemcpy(e->ade_tile.p, h.data(), h.size(), cudaMemcpyHostToDevice));
+        g.ade_tile = e->ade_tile.p;
+    } else {
+        g.ade_tile = nullptr;
+    }
     g.AI = e->AI.p;
     g.LI = e->LI.p;
     g.geo = e->geo.p;
@@ -691,8 +718,8 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
         if (need > 48 * 1024 && (rc = set_fused_attrs((int)need))) return rc;
     } else if (e->use_tma) {
         if ((rc = make_maps(e))) return rc;
-        const size_t need = (e->feat & FEAT_UPML) ? StageLayout<uint32_t, true>::smem(e->stages)
-                                                  : StageLayout<uint32_t, false>::smem(e->stages);
+        const size_t need = (e->feat & FEAT_UPML) ? StageLayout<uint32_t, true, true>::smem(e->stages)
+                                                  : StageLayout<uint32_t, false, true>::smem(e->stages);
         if (need > 48 * 1024 && (rc = set_smem_attrs((int)need))) return rc;
     }
     return reset_state(e);

@@ -65,6 +65,7 @@ struct fdtd_engine_s {
     double dT = 0;
     DevGrid g{};
     DevBuf<float> V, I, FV, FI, AV, LV, AI, LI;
+    DevBuf<uint8_t> ade_tile;  // per voltage-kernel tile plane: Lorentz/Drude flags (DevGrid::ade_tile)
     DevBuf<float> V2, I2, FV2;  // second field / voltage-flux buffers (fused kernel)
     DevHalfBufs E, H;
     DevBuf<float> geo;

@@ -15,6 +15,8 @@
 //             V own box  {32, TY, 1, 3}   at (z0, y0, x)
 //             E index    {32, TY, 1}      at (z0, y0, x)
 //             V-flux box {32, TY, 1, 3}   (UPML tiles only)
+//             Lorentz/Drude state boxes {32, TY, 1, 3} (tile planes that
+//             hold such nodes, from a per-tile-plane flag array)
 //   H kernel: V halo box {36, TY+1, 1, 3} at (z0, y0, x)      (z+1, y+1 halo)
 //             I own box  {32, TY, 1, 3}, H index box, I-flux box
 // The innermost start coordinate is always a multiple of 4 floats (16 B);
@@ -47,7 +49,7 @@ constexpr int TMA_TY = 8;
 constexpr unsigned long long TMA_WAIT_CYCLES = 4000000000ull;  // ~2 s at 2 GHz
 
 struct TmaMaps {
-    CUtensorMap I_halo, I_own, V_halo, V_own, FV_own, FI_own, idxE, idxH;
+    CUtensorMap I_halo, I_own, V_halo, V_own, FV_own, FI_own, idxE, idxH, AV_own, LV_own;
 };
 
 // geometry of the UPML slabs: a node is in a slab iff one coordinate is
@@ -122,8 +124,9 @@ __device__ __forceinline__ void tensormap_acquire(const TmaMaps* m) {
         asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"(p + 128 * k) : "memory");
 }
 
-// stage layout (floats, every buffer 128-byte aligned)
-template <typename IdxT, bool UPML>
+// stage layout (floats, every buffer 128-byte aligned); ADE adds the two
+// Lorentz/Drude state boxes (voltage kernel only)
+template <typename IdxT, bool UPML, bool ADE = false>
 struct StageLayout {
     static constexpr int HW = 36;                               // halo box row width
     static constexpr int HALO = 3 * (TMA_TY + 1) * HW;          // halo box, 3 components
@@ -132,7 +135,9 @@ struct StageLayout {
     static constexpr int IDX = TMA_TY * 32 * (int)sizeof(IdxT) / 4;
     static constexpr int IDX_A = (IDX + 31) / 32 * 32;
     static constexpr int FLUX = UPML ? OWN : 0;
-    static constexpr int STAGE = HALO_A + OWN + IDX_A + FLUX;    // floats
+    static constexpr int OFF_FLUX = HALO_A + OWN + IDX_A;
+    static constexpr int OFF_ADE = OFF_FLUX + FLUX;              // ADE state, then Lorentz state
+    static constexpr int STAGE = OFF_ADE + (ADE ? 2 * OWN : 0);  // floats
     static constexpr int HALO_BYTES = HALO * 4;
     static constexpr int OWN_BYTES = OWN * 4;
     static constexpr int IDX_BYTES = TMA_TY * 32 * (int)sizeof(IdxT);
@@ -153,12 +158,20 @@ __device__ __forceinline__ bool tile_has_upml(const TileInfo& ti, int x, int y0,
 // x-chunk bz.  ring counts the planes this block has pushed through its
 // mbarrier ring so far (the ring persists across the tiles of a persistent
 // block).  Returns false if a bounded wait gave up.
+// per (x, y-tile, z-tile) Lorentz/Drude flags of the voltage kernel's tiles:
+// bit 0 = an ADE node, bit 1 = a Lorentz node in that tile plane
+__device__ __forceinline__ uint32_t ade_tile_flags(const DevGrid& g, int x, int bx, int by) {
+    const int ZT = (g.Nz + 31) / 32, YT = (g.Ny + TMA_TY - 1) / TMA_TY;
+    return g.ade_tile ? (uint32_t)__ldg(g.ade_tile + ((long long)x * YT + by) * ZT + bx) : 0u;
+}
+
 template <typename IdxT, int FEAT, bool GEO>
 __device__ __forceinline__ bool volt_tile(const DevGrid& g, const TmaMaps& m, const TileInfo& ti, int bx, int by,
                                           int bz, int XC, int STAGES, float* smem, uint64_t* bars, uint32_t& ring,
                                           int numTS) {
     constexpr bool UPML = (FEAT & FEAT_UPML) != 0;
-    using L = StageLayout<IdxT, UPML>;
+    constexpr bool ADE = (FEAT & FEAT_ADE) != 0;
+    using L = StageLayout<IdxT, UPML, ADE>;
     constexpr int HW = L::HW;
     const int tz = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * 32 + tz;
@@ -178,12 +191,16 @@ __device__ __forceinline__ bool volt_tile(const DevGrid& g, const TmaMaps& m, co
         const int x = x0 + r;
         float* st = smem + (size_t)s * L::STAGE;
         const bool up = UPML && tile_has_upml(ti, x, y0, yl, z0, zl);
-        const uint32_t bytes = L::HALO_BYTES + L::OWN_BYTES + L::IDX_BYTES + (up ? L::OWN_BYTES : 0);
+        const uint32_t af = ADE ? ade_tile_flags(g, x, bx, by) : 0u;
+        const uint32_t bytes = L::HALO_BYTES + L::OWN_BYTES + L::IDX_BYTES + (up ? L::OWN_BYTES : 0) +
+                               ((af & 1u) ? L::OWN_BYTES : 0) + ((af & 2u) ? L::OWN_BYTES : 0);
         mbar_expect_tx(&bars[s], bytes);
         tma_4d(st, &m.I_halo, &bars[s], z0 - 4, y0 - 1, x, 0);
         tma_4d(st + L::HALO_A, &m.V_own, &bars[s], z0, y0, x, 0);
         tma_3d(st + L::HALO_A + L::OWN, &m.idxE, &bars[s], z0, y0, x);
-        if (up) tma_4d(st + L::HALO_A + L::OWN + L::IDX_A, &m.FV_own, &bars[s], z0, y0, x, 0);
+        if (up) tma_4d(st + L::OFF_FLUX, &m.FV_own, &bars[s], z0, y0, x, 0);
+        if (af & 1u) tma_4d(st + L::OFF_ADE, &m.AV_own, &bars[s], z0, y0, x, 0);
+        if (af & 2u) tma_4d(st + L::OFF_ADE + L::OWN, &m.LV_own, &bars[s], z0, y0, x, 0);
     };
 
     int issued = 0;
@@ -244,7 +261,10 @@ __device__ __forceinline__ bool volt_tile(const DevGrid& g, const TmaMaps& m, co
             const float* sV = st + L::HALO_A;
             const uint32_t t = (uint32_t)reinterpret_cast<const IdxT*>(st + L::HALO_A + L::OWN)[oi];
             const bool up = UPML && tile_has_upml(ti, x, y0, yl, z0, zl);
-            const float* sF = up ? st + L::HALO_A + L::OWN + L::IDX_A + oi : nullptr;
+            const float* sF = up ? st + L::OFF_FLUX + oi : nullptr;
+            const uint32_t af = ADE ? ade_tile_flags(g, x, bx, by) : 0u;
+            const float* sA = (af & 1u) ? st + L::OFF_ADE + oi : nullptr;
+            const float* sL = (af & 2u) ? st + L::OFF_ADE + L::OWN + oi : nullptr;
             float v[3] = {sV[oi], sV[TMA_TY * 32 + oi], sV[2 * TMA_TY * 32 + oi]};
             GeoF gf;
             if (GEO) {
@@ -253,7 +273,8 @@ __device__ __forceinline__ bool volt_tile(const DevGrid& g, const TmaMaps& m, co
                 gf.f[1][0] = gyE; gf.f[1][1] = gzI; gf.f[1][2] = gxI;
                 gf.f[2][0] = gzE; gf.f[2][1] = gxI; gf.f[2][2] = gyI;
             }
-            update_node<false, FEAT, GEO>(g, v, curl, t, (long long)x * g.sx + yz, numTS, sF, TMA_TY * 32, gf);
+            update_node<false, FEAT, GEO>(g, v, curl, t, (long long)x * g.sx + yz, numTS, sF, TMA_TY * 32, gf,
+                                          nullptr, true, sA, sL);
             Vp[0] = v[0];
             Vp[C] = v[1];
             Vp[2 * C] = v[2];
@@ -315,7 +336,7 @@ __device__ __forceinline__ bool curr_tile(const DevGrid& g, const TmaMaps& m, co
             tma_4d(st + L::HALO_A, &m.I_own, &bars[s], z0, y0, x, 0);
             tma_3d(st + L::HALO_A + L::OWN, &m.idxH, &bars[s], z0, y0, x);
         }
-        if (up) tma_4d(st + L::HALO_A + L::OWN + L::IDX_A, &m.FI_own, &bars[s], z0, y0, x, 0);
+        if (up) tma_4d(st + L::OFF_FLUX, &m.FI_own, &bars[s], z0, y0, x, 0);
     };
 
     int issued = 0;
@@ -365,7 +386,7 @@ __device__ __forceinline__ bool curr_tile(const DevGrid& g, const TmaMaps& m, co
             const float* sI = st + L::HALO_A;
             const uint32_t t = (uint32_t)reinterpret_cast<const IdxT*>(st + L::HALO_A + L::OWN)[oi];
             const bool up = UPML && tile_has_upml(ti, x, y0, yl, z0, zl);
-            const float* sF = up ? st + L::HALO_A + L::OWN + L::IDX_A + oi : nullptr;
+            const float* sF = up ? st + L::OFF_FLUX + oi : nullptr;
             float cu[3] = {sI[oi], sI[TMA_TY * 32 + oi], sI[2 * TMA_TY * 32 + oi]};
             GeoF gf;
             if (GEO) {
@@ -434,7 +455,7 @@ __device__ __forceinline__ void init_ring(uint64_t* bars, int STAGES) {
 template <typename IdxT, int FEAT, bool GEO>
 __global__ void __launch_bounds__(TMA_TY * 32) k_volt_tma(const DevGrid g, const __grid_constant__ TmaMaps m,
                                                           const TileInfo ti, int ts_off, int XC, int STAGES) {
-    using L = StageLayout<IdxT, (FEAT & FEAT_UPML) != 0>;
+    using L = StageLayout<IdxT, (FEAT & FEAT_UPML) != 0, (FEAT & FEAT_ADE) != 0>;
     extern __shared__ __align__(128) float smem_raw[];
     float* smem = aligned_smem(smem_raw);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * STAGES);
@@ -484,7 +505,7 @@ template <typename IdxT, int FEAT, bool GEO>
 __global__ void __launch_bounds__(TMA_TY * 32, WIPEMS_BATCH_MIN_BLOCKS) k_volt_batch(const BatchJob* __restrict__ jobs,
                                                             const WorkItem* __restrict__ items, int nitems, int XC,
                                                             int STAGES) {
-    using L = StageLayout<IdxT, (FEAT & FEAT_UPML) != 0>;
+    using L = StageLayout<IdxT, (FEAT & FEAT_UPML) != 0, (FEAT & FEAT_ADE) != 0>;
     extern __shared__ __align__(128) float smem_raw[];
     float* smem = aligned_smem(smem_raw);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * STAGES);

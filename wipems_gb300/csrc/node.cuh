@@ -55,6 +55,10 @@ struct DevGrid {
     float* LV;           // Lorentz voltage state
     float* AI;           // ADE current state
     float* LI;
+    // per (x, 8-row y tile, 32-node z tile) of the voltage kernel: bit 0 =
+    // a Lorentz/Drude node, bit 1 = a Lorentz node in that tile plane
+    // (the TMA kernels stage the states of those tile planes); null = none
+    const uint8_t* ade_tile;
     DevHalf e, h;
     const float* geo;    // [4][Nx+Ny+Nz] dE, iD, dH, iM (factorized meshes) or null
     int geo_stride;      // Nx+Ny+Nz
@@ -107,11 +111,14 @@ __device__ __forceinline__ GeoF geo_factors(const DevGrid& g, bool H, int x, int
 // curl of the other field; t: tuple index; o: node offset; F (UPML flux of
 // the node) is read from fsrc[n*fstride] when fsrc is set, else from global.
 // The new flux goes to fout (default: the engine's flux array, in place),
-// and only when fwrite is set.
+// and only when fwrite is set.  The Lorentz/Drude states are read from
+// asrc / lsrc[n*fstride] when set (staged copies), else from global; the
+// new states always go to global.
 template <bool H, int FEAT, bool GEO>
 __device__ __forceinline__ void update_node(const DevGrid& g, float fld[3], const float curl[3], uint32_t t,
                                             long long o, int numTS, const float* fsrc, int fstride,
-                                            const GeoF& gf, float* fout = nullptr, bool fwrite = true) {
+                                            const GeoF& gf, float* fout = nullptr, bool fwrite = true,
+                                            const float* asrc = nullptr, const float* lsrc = nullptr) {
     const DevHalf& T = H ? g.h : g.e;
     const float4 ta = __ldg(&T.main[TAB_MAIN * t]);
     const float4 tb = __ldg(&T.main[TAB_MAIN * t + 1]);
@@ -137,8 +144,8 @@ __device__ __forceinline__ void update_node(const DevGrid& g, float fld[3], cons
         if (flags & TF_LOR) {
 #pragma unroll
             for (int n = 0; n < 3; ++n) {
-                float lor = Lr[n * C + o];
-                float a = A[n * C + o];
+                float lor = lsrc ? lsrc[n * fstride] : Lr[n * C + o];
+                float a = asrc ? asrc[n * fstride] : A[n * C + o];
                 lor = __fadd_rn(lor, __fmul_rn(klor[n], a));
                 a = __fmul_rn(a, kint[n]);
                 a = __fadd_rn(a, __fmul_rn(kext[n], __fsub_rn(fld[n], lor)));
@@ -149,7 +156,7 @@ __device__ __forceinline__ void update_node(const DevGrid& g, float fld[3], cons
         } else {
 #pragma unroll
             for (int n = 0; n < 3; ++n) {
-                float a = A[n * C + o];
+                float a = asrc ? asrc[n * fstride] : A[n * C + o];
                 a = __fmul_rn(a, kint[n]);
                 a = __fadd_rn(a, __fmul_rn(kext[n], fld[n]));
                 A[n * C + o] = a;
