@@ -528,6 +528,9 @@ typedef struct {
 
 int fdtd_batch_create(const fdtd_engine_t* engines, uint32_t n,
                       const fdtd_batch_opts* opts, fdtd_batch_t* out);
+/* *ok = 1 when fdtd_batch_create would take the engine (two-pass TMA
+ * kernels; no Mur face, lumped RLC edge or frequency-domain accumulation). */
+int fdtd_batch_accepts(fdtd_engine_t eng, int* ok);
 /* Advances every job by n_steps (each job's numTS moves by n_steps). */
 int fdtd_batch_iterate(fdtd_batch_t batch, uint32_t n_steps);
 int fdtd_batch_info(fdtd_batch_t batch, fdtd_batch_stats* stats);

@@ -89,3 +89,20 @@ def test_server_rejects_oversized_job_and_keeps_serving():
     srv.wait(ok, timeout=300)
     assert srv.status(ok)["state"] == "done"
     srv.close()
+
+
+def test_batch_mode_runs_unbatchable_jobs_beside_the_batch():
+    """With batch rounds on, jobs the persistent batch cannot take (Mur
+    faces, lumped RLC edges) run as concurrent engines next to it; every job
+    still gets its solo result."""
+    srv = Server(round_steps=40, build_workers=2, batch_min_jobs=2)
+    kinds = [("upml", 3), ("mur", 3), ("pec", 4), ("rlc", 3), ("drude", 4), ("rlc_mur", 5)]
+    ids = {(k, s): srv.submit(scenes.mini(k, seed=s, nr_ts=NR_TS), end_crit=CRIT, keep_fields=True)
+           for k, s in kinds}
+    srv.wait(0, timeout=600)
+    st = srv.stats()
+    assert st["jobs_done"] == len(ids) and st["jobs_failed"] == 0, st
+    assert st["rebuilds"] >= 1
+    for (k, s), jid in ids.items():
+        _same(_alone(k, s), srv, jid)
+    srv.close()

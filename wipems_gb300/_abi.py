@@ -197,6 +197,7 @@ SIGNATURES = [
     ("fdtd_scene_load_xml", C.c_int, [C.c_char_p, C.POINTER(_P), C.POINTER(FdtdXmlInfo)]),
     ("fdtd_scene_load_xml_file", C.c_int, [C.c_char_p, C.POINTER(_P), C.POINTER(FdtdXmlInfo)]),
     ("fdtd_batch_create", C.c_int, [C.POINTER(_P), u32, C.POINTER(FdtdBatchOpts), C.POINTER(_P)]),
+    ("fdtd_batch_accepts", C.c_int, [_P, C.POINTER(C.c_int)]),
     ("fdtd_batch_iterate", C.c_int, [_P, u32]),
     ("fdtd_batch_info", C.c_int, [_P, C.POINTER(FdtdBatchStats)]),
     ("fdtd_batch_destroy", C.c_int, [_P]),

@@ -153,6 +153,27 @@ int batch_smem_attrs(int bytes) {
     return FDTD_OK;
 }
 
+// Why an engine cannot join a batch (0 = it can; the message is set).
+int batch_refusal(const fdtd_engine_s* e) {
+    if (!e->use_tma || e->fused) {
+        set_error("fdtd_batch_create: jobs must use the two-pass TMA kernels");
+        return FDTD_ERR_ARG;
+    }
+    if (e->mur.nface) {
+        set_error("fdtd_batch_create: Mur boundaries are not provided in batches");
+        return FDTD_ERR_UNSUPPORTED;
+    }
+    if (e->rlc.count) {
+        set_error("fdtd_batch_create: lumped RLC elements are not provided in batches");
+        return FDTD_ERR_UNSUPPORTED;
+    }
+    if (e->fd_interval) {
+        set_error("fdtd_batch_create: frequency-domain accumulation is not provided in batches");
+        return FDTD_ERR_UNSUPPORTED;
+    }
+    return FDTD_OK;
+}
+
 size_t stage_smem(bool i16, bool upml, bool ade, int S) {
     if (ade) {  // voltage kernels of groups with Lorentz/Drude nodes stage their states too
         if (i16) return upml ? StageLayout<uint16_t, true, true>::smem(S) : StageLayout<uint16_t, false, true>::smem(S);
@@ -281,22 +302,7 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
             set_error("fdtd_batch_create: all jobs must live on one device");
             return FDTD_ERR_ARG;
         }
-        if (!e->use_tma || e->fused) {
-            set_error("fdtd_batch_create: jobs must use the two-pass TMA kernels");
-            return FDTD_ERR_ARG;
-        }
-        if (e->mur.nface) {
-            set_error("fdtd_batch_create: Mur boundaries are not provided in batches");
-            return FDTD_ERR_UNSUPPORTED;
-        }
-        if (e->rlc.count) {
-            set_error("fdtd_batch_create: lumped RLC elements are not provided in batches");
-            return FDTD_ERR_UNSUPPORTED;
-        }
-        if (e->fd_interval) {
-            set_error("fdtd_batch_create: frequency-domain accumulation is not provided in batches");
-            return FDTD_ERR_UNSUPPORTED;
-        }
+        if ((rc = batch_refusal(e))) return rc;
         for (uint32_t k = 0; k < j; ++k)
             if (engines[k] == e) {
                 set_error("fdtd_batch_create: a job appears twice");
@@ -456,6 +462,14 @@ int fdtd_batch_create(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch
         return rc;
     }
     *out = b;
+    return FDTD_OK;
+}
+
+int fdtd_batch_accepts(fdtd_engine_t e, int* ok) {
+    if (!e || !ok) return FDTD_ERR_ARG;
+    const std::string keep = last_error();  // a query leaves the thread's last message alone
+    *ok = batch_refusal(e) == FDTD_OK ? 1 : 0;
+    set_error(keep);
     return FDTD_OK;
 }
 

@@ -100,6 +100,7 @@ struct fdtd_server_s {
     // GPU-thread state
     std::vector<Job*> active;
     fdtd_batch_t batch = nullptr;
+    std::vector<Job*> batch_jobs;  // the jobs the current batch was built over
     uint64_t used = 0;
     // statistics (under mu)
     fdtd_server_stats st{};
@@ -274,19 +275,27 @@ int admit(fdtd_server_s* s, Job* j) {
     return FDTD_OK;
 }
 
-// One persistent-batch round over all resident jobs (batch mode).
-void batch_round(fdtd_server_s* s, bool changed) {
-    if (changed || !s->batch) {
-        if (s->batch) fdtd_batch_destroy(s->batch);
-        s->batch = nullptr;
+void drop_batch(fdtd_server_s* s) {
+    if (s->batch) fdtd_batch_destroy(s->batch);
+    s->batch = nullptr;
+    s->batch_jobs.clear();
+}
+
+// One persistent-batch round over `jobs` (batch mode); the batch is rebuilt
+// when its membership changed.  Returns the jobs that are still running.
+std::vector<Job*> batch_round(fdtd_server_s* s, const std::vector<Job*>& jobs) {
+    if (!s->batch || jobs != s->batch_jobs) {
+        drop_batch(s);
         std::vector<fdtd_engine_t> es;
-        for (Job* j : s->active) es.push_back(j->eng);
+        for (Job* j : jobs) es.push_back(j->eng);
         const int rc = fdtd_batch_create(es.data(), (uint32_t)es.size(), &s->opts.batch, &s->batch);
         std::lock_guard<std::mutex> lock(s->mu);
         s->st.rebuilds++;
         if (rc) {
             s->batch = nullptr;
             s->st.last_error = rc;
+        } else {
+            s->batch_jobs = jobs;
         }
     }
     int rc = s->batch ? fdtd_batch_iterate(s->batch, s->opts.round_steps) : FDTD_ERR_STATE;
@@ -298,23 +307,21 @@ void batch_round(fdtd_server_s* s, bool changed) {
         s->st.gpu_ms += bs.last_ms;
         s->st.kernel_launches += bs.last_launches;
     }
-    if (rc) {
-        // find the failing jobs: each engine decodes its own error word
-        const std::string msg = last_error();
-        std::vector<Job*> ok;
-        for (Job* j : s->active) {
-            const int jr = s->batch ? fdtd_engine_iterate(j->eng, 0) : rc;
-            if (jr) retire(s, j, jr, s->batch ? last_error() : msg);
-            else ok.push_back(j);
-        }
-        if (ok.size() == s->active.size()) {  // not attributable to a job: fail them all
-            for (Job* j : ok) retire(s, j, rc, msg);
-            ok.clear();
-        }
-        s->active.swap(ok);
-        if (s->batch) fdtd_batch_destroy(s->batch);
-        s->batch = nullptr;
+    if (!rc) return jobs;
+    // find the failing jobs: each engine decodes its own error word
+    const std::string msg = last_error();
+    std::vector<Job*> ok;
+    for (Job* j : jobs) {
+        const int jr = s->batch ? fdtd_engine_iterate(j->eng, 0) : rc;
+        if (jr) retire(s, j, jr, s->batch ? last_error() : msg);
+        else ok.push_back(j);
     }
+    if (ok.size() == jobs.size()) {  // not attributable to a job: fail them all
+        for (Job* j : ok) retire(s, j, rc, msg);
+        ok.clear();
+    }
+    drop_batch(s);
+    return ok;
 }
 
 void gpu_loop(fdtd_server_s* s) {
@@ -360,8 +367,7 @@ void gpu_loop(fdtd_server_s* s) {
             if (s->active.empty() && s->ready.empty()) {
                 if (s->batch) {
                     lock.unlock();
-                    fdtd_batch_destroy(s->batch);
-                    s->batch = nullptr;
+                    drop_batch(s);
                     lock.lock();
                 }
                 s->cv_gpu.wait(lock, [&] { return s->stop || !s->ready.empty(); });
@@ -396,29 +402,33 @@ void gpu_loop(fdtd_server_s* s) {
             s->st.active_jobs = (uint32_t)s->active.size();
         }
         if (s->active.empty()) continue;
-        const bool batch_mode = s->opts.batch_min_jobs > 0 && s->active.size() >= s->opts.batch_min_jobs;
-        if (batch_mode) {
-            // a batch needs every engine idle
-            bool idle = true;
+        // batch mode: the jobs a batch can take run as one persistent batch
+        // once there are batch_min_jobs of them; the others (Mur, lumped
+        // RLC) run as concurrent engines beside it
+        std::vector<Job*> bjobs, solo;
+        if (s->opts.batch_min_jobs > 0) {
             for (Job* j : s->active) {
-                int ready = 1;
-                if (fdtd_engine_query(j->eng, &ready) == FDTD_OK && !ready) idle = false;
+                int ok = 0;
+                fdtd_batch_accepts(j->eng, &ok);
+                (ok ? bjobs : solo).push_back(j);
             }
-            if (!idle) continue;  // collected on the next pass
-            batch_round(s, changed);
-            continue;
+            if (bjobs.size() < s->opts.batch_min_jobs) {
+                solo = s->active;
+                bjobs.clear();
+            }
+        } else {
+            solo = s->active;
         }
+        if (bjobs.empty() && s->batch) drop_batch(s);
         // concurrent engines: every idle job gets its next round_steps
         // queued on its own stream at once; finished jobs are picked up on
         // the next pass, so short and long jobs never wait for each other
-        if (s->batch) {
-            fdtd_batch_destroy(s->batch);
-            s->batch = nullptr;
-        }
+        // (queued before a batch round, which runs synchronously, so the two
+        // overlap on the device)
         std::vector<Job*> ok;
         uint64_t launches = 0;
         bool launched = false;
-        for (Job* j : s->active) {
+        for (Job* j : solo) {
             int ready = 1;
             if (fdtd_engine_query(j->eng, &ready) == FDTD_OK && !ready) {
                 ok.push_back(j);
@@ -443,6 +453,15 @@ void gpu_loop(fdtd_server_s* s) {
             launched = true;
             ok.push_back(j);
         }
+        if (!bjobs.empty()) {
+            bool idle = true;  // a batch needs every one of its engines idle
+            for (Job* j : bjobs) {
+                int ready = 1;
+                if (fdtd_engine_query(j->eng, &ready) == FDTD_OK && !ready) idle = false;
+            }
+            const std::vector<Job*> left = idle ? batch_round(s, bjobs) : bjobs;  // else collected next pass
+            ok.insert(ok.end(), left.begin(), left.end());
+        }
         s->active.swap(ok);
         std::lock_guard<std::mutex> lock(s->mu);
         if (launched) {
@@ -455,8 +474,7 @@ void gpu_loop(fdtd_server_s* s) {
         }
     }
     // shutdown: free what is still resident
-    if (s->batch) fdtd_batch_destroy(s->batch);
-    s->batch = nullptr;
+    drop_batch(s);
     for (Job* j : s->active) {
         fdtd_engine_wait(j->eng);
         fdtd_engine_destroy(j->eng);
