@@ -428,6 +428,28 @@ int fdtd_engine_query(fdtd_engine_t eng, int* ready);
 int fdtd_engine_set_fd(fdtd_engine_t eng, const double* freqs, uint32_t nfreq,
                        uint32_t fd_interval);
 int fdtd_engine_read_fd(fdtd_engine_t eng, double* re_im, uint32_t* samples);
+/* Field dump from the device (ProcessFieldsTD / ProcessFields::CalcField,
+ * Common/processfields_td.cpp:49-91, processfields.cpp:280-330, with the
+ * interpolation of Engine_Interface_FDTD, engine_interface_fdtd.cpp:60-200):
+ * E (V/m) or H (A/m) at the engine's current timestep on the mesh lines
+ * start + i * step of a box (ProcessFields::CalcMeshPos with sub-sampling),
+ * out[3][num0][num1][num2] as float.  out = NULL: only num[] is filled.
+ * The file format (VTK / HDF5) is the caller's: wipems_gb300/dumps.py
+ * writes legacy VTK rectilinear grids. */
+#define FDTD_DUMP_E 0
+#define FDTD_DUMP_H 1
+#define FDTD_INTERP_NONE 0
+#define FDTD_INTERP_NODE 1
+#define FDTD_INTERP_CELL 2
+typedef struct {
+    int      field;               /* FDTD_DUMP_E or FDTD_DUMP_H */
+    int      interp;              /* FDTD_INTERP_* */
+    uint32_t start[3], stop[3];   /* mesh-line indices (either order) */
+    uint32_t step[3];             /* sub-sampling per axis (0 = every line) */
+} fdtd_dump_box;
+int fdtd_engine_dump_field(fdtd_engine_t eng, const fdtd_dump_box* box,
+                           float* out, uint64_t cap, uint32_t num[3]);
+
 /* Checkpoint / resume (no counterpart in the reference, which has no
  * restart): every piece of the engine's device state -- fields, UPML flux,
  * Lorentz/Drude and Mur state, numTS, energy accumulators, the recorded

@@ -88,3 +88,101 @@ def cavity_check(t_list, val_list, meta) -> dict:
         te_outside=check_frequency(f, uy, o2, o1, max_amp, "outside"),
         tm_outside=check_frequency(f, uz, o2t, o1t, max_amp, "outside"),
     )
+
+
+def edge_lengths(lines, unit, dual):
+    """Operator::GetEdgeLength along one axis (GetDiscDelta * grid delta)."""
+    l = np.asarray(lines, np.float64)
+    n = len(l)
+    dl = np.empty(n)
+    if not dual:
+        dl[:-1] = l[1:] - l[:-1]
+        dl[-1] = l[-1] - l[-2]
+    else:
+        d = np.empty(n)  # dual lines
+        d[:-1] = 0.5 * (l[:-1] + l[1:])
+        d[-1] = l[-1] + 0.5 * (l[-1] - l[-2])
+        dl[1:] = d[1:] - d[:-1]
+        dl[0] = l[1] - l[0]
+    return dl * unit
+
+
+def dump_reference(V, I, lines, unit, field, interp, start, stop, step):
+    """Engine_Interface_FDTD::GetRawInterpolated(Dual)Field at the dump lines
+    (engine_interface_fdtd.cpp:60-200), point by point in the reference's
+    order, double arithmetic, stored as float (processfields.cpp:280-330)."""
+    N = V.shape[1:]
+    Lm = [edge_lengths(lines[a], unit, False) for a in range(3)]
+    Ld = [edge_lengths(lines[a], unit, True) for a in range(3)]
+    idx = [list(range(min(start[a], stop[a]), max(start[a], stop[a]) + 1, max(1, step[a]))) for a in range(3)]
+    out = np.zeros((3, len(idx[0]), len(idx[1]), len(idx[2])), np.float32)
+
+    def rawE(n, p):
+        d = Lm[n][p[n]]
+        return float(V[n][p[0], p[1], p[2]]) / d if d != 0 else 0.0
+
+    def rawH(n, p):
+        d = Ld[n][p[n]]
+        return float(I[n][p[0], p[1], p[2]]) / d if d != 0 else 0.0
+
+    for i, x in enumerate(idx[0]):
+        for j, y in enumerate(idx[1]):
+            for k, z in enumerate(idx[2]):
+                p = [x, y, z]
+                top = any(p[a] == N[a] - 1 for a in range(3))
+                for n in range(3):
+                    nP, nPP = (n + 1) % 3, (n + 2) % 3
+                    q = list(p)
+                    if field == "E":
+                        if interp == "none":
+                            o = rawE(n, p)
+                        elif interp == "node":
+                            if p[n] == N[n] - 1:
+                                q[n] -= 1
+                                o = rawE(n, q)
+                            elif Lm[n][p[n]] == 0:
+                                o = 0.0
+                            elif p[n] == 0:
+                                o = rawE(n, p)
+                            else:
+                                delta = Lm[n][p[n]]
+                                q[n] -= 1
+                                rel = delta / (delta + Lm[n][q[n]])
+                                o = rawE(n, p) * (1.0 - rel) + rawE(n, q) * rel
+                        else:
+                            if top:
+                                o = 0.0
+                            else:
+                                o = rawE(n, q)
+                                q[nP] += 1
+                                o += rawE(n, q)
+                                q[nPP] += 1
+                                o += rawE(n, q)
+                                q[nP] -= 1
+                                o += rawE(n, q)
+                                o /= 4
+                    else:
+                        if interp == "none":
+                            o = rawH(n, p)
+                        elif interp == "node":
+                            if top or p[nP] == 0 or p[nPP] == 0:
+                                o = 0.0
+                            else:
+                                o = rawH(n, q)
+                                q[nP] -= 1
+                                o += rawH(n, q)
+                                q[nPP] -= 1
+                                o += rawH(n, q)
+                                q[nP] += 1
+                                o += rawH(n, q)
+                                o /= 4
+                        else:
+                            if p[n] >= N[n] - 1:
+                                o = 0.0
+                            else:
+                                delta = Ld[n][p[n]]
+                                q[n] += 1
+                                rel = delta / (delta + Ld[n][q[n]])
+                                o = rawH(n, p) * (1.0 - rel) + rawH(n, q) * rel
+                    out[n, i, j, k] = o
+    return out

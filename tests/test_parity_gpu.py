@@ -1,6 +1,6 @@
 """GPU parity: the CUDA engine (through the C ABI) against the oracle.
 
-Bar (BASELINE the benchmark spec): probe series within 1e-5 relative L2, final
+Bar: probe series within 1e-5 relative L2, final
 fields within 1e-4 relative max-norm.  The kernels keep the reference's
 FP32 operation order, so fields are in fact required to be bit-identical;
 probe sums differ only by reduction order (device warp sums in double vs the

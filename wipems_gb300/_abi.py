@@ -63,6 +63,10 @@ class FdtdOpDesc(C.Structure):
                 ("rlc", C.POINTER(FdtdRlcDesc))]
 
 
+class FdtdDumpBox(C.Structure):
+    _fields_ = [("field", C.c_int), ("interp", C.c_int), ("start", u32 * 3), ("stop", u32 * 3), ("step", u32 * 3)]
+
+
 class FdtdProbeDesc(C.Structure):
     _fields_ = [("type", C.c_int), ("start", u32 * 3), ("stop", u32 * 3),
                 ("start_inside", C.c_int * 3), ("stop_inside", C.c_int * 3),
@@ -198,6 +202,7 @@ SIGNATURES = [
     ("fdtd_scene_load_xml_file", C.c_int, [C.c_char_p, C.POINTER(_P), C.POINTER(FdtdXmlInfo)]),
     ("fdtd_batch_create", C.c_int, [C.POINTER(_P), u32, C.POINTER(FdtdBatchOpts), C.POINTER(_P)]),
     ("fdtd_batch_accepts", C.c_int, [_P, C.POINTER(C.c_int)]),
+    ("fdtd_engine_dump_field", C.c_int, [_P, C.POINTER(FdtdDumpBox), PF, C.c_uint64, PU32]),
     ("fdtd_batch_iterate", C.c_int, [_P, u32]),
     ("fdtd_batch_info", C.c_int, [_P, C.POINTER(FdtdBatchStats)]),
     ("fdtd_batch_destroy", C.c_int, [_P]),

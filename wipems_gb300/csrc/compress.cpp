@@ -307,6 +307,18 @@ int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
             off += N;
         }
     }
+    if (have_lines) {  // Operator::GetEdgeLength per axis, main and dual, for field dumps
+        const size_t tot = (size_t)Nx + Ny + Nz;
+        c->edges.assign(2 * tot, 0.0);
+        size_t off = 0;
+        for (int a = 0; a < 3; ++a) {
+            for (uint32_t i = 0; i < P.N[a]; ++i) {
+                c->edges[off + i] = edge_len(d->lines[a], P.N[a], i, false, d->unit);
+                c->edges[tot + off + i] = edge_len(d->lines[a], P.N[a], i, true, d->unit);
+            }
+            off += P.N[a];
+        }
+    }
     int rc = prepare(d, P);
     if (rc) return rc;
 

@@ -78,6 +78,8 @@ struct fdtd_cop_s {
     std::vector<float> sigV, sigC;
     std::vector<wipems::MurFace> mur;  // Mur ABC faces (copied from the operator)
     wipems::RlcList rlc;               // lumped RLC edges (copied from the operator)
+    std::vector<double> edges;         // [2][Nx+Ny+Nz]: main / dual edge lengths in m (field dumps);
+                                       // empty when the description has no mesh lines
     uint32_t sig_len = 0, sig_period = 0;
     ~fdtd_cop_s();
 };

@@ -669,6 +669,10 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     g.FI = e->FI.p;
     g.AV = e->AV.p;
     g.LV = e->LV.p;
+    if (!c->edges.empty()) {
+        if ((rc = e->edges.alloc(c->edges.size(), tot))) return rc;
+        CK(cudaMemcpy(e->edges.p, c->edges.data(), c->edges.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
     if (c->E.any_ade) {  // which voltage-kernel tile planes hold Lorentz/Drude nodes
         const int ZT = ((int)e->N[2] + 31) / 32, YT = ((int)e->N[1] + TMA_TY - 1) / TMA_TY;
         std::vector<uint8_t> tf(c->E.num_tuples);
@@ -1222,6 +1226,61 @@ int fdtd_engine_get_fields(fdtd_engine_t e, float* volt, float* curr) {
         CK(cudaMemcpy2DAsync(dst, Nz * sizeof(float), src, e->Nzp * sizeof(float), Nz * sizeof(float),
                              (size_t)3 * Nx * Ny, cudaMemcpyDeviceToHost, e->stream));
     }
+    CK(cudaStreamSynchronize(e->stream));
+    return FDTD_OK;
+}
+
+int fdtd_engine_dump_field(fdtd_engine_t e, const fdtd_dump_box* b, float* out, uint64_t cap, uint32_t num[3]) {
+    if (!e || !b || !num) return FDTD_ERR_ARG;
+    if (b->field < 0 || b->field > 1 || b->interp < 0 || b->interp > 2) {
+        set_error("fdtd_engine_dump_field: field must be 0 (E) or 1 (H), interp 0 (none), 1 (node) or 2 (cell)");
+        return FDTD_ERR_ARG;
+    }
+    DumpBox d{};
+    d.field = b->field;
+    d.interp = b->interp;
+    uint64_t total = 1;
+    for (int a = 0; a < 3; ++a) {
+        const uint32_t lo = std::min(b->start[a], b->stop[a]), hi = std::max(b->start[a], b->stop[a]);
+        if (hi >= e->N[a]) {
+            set_error("fdtd_engine_dump_field: box outside the grid");
+            return FDTD_ERR_ARG;
+        }
+        const uint32_t step = b->step[a] ? b->step[a] : 1;
+        num[a] = (hi - lo) / step + 1;  // ProcessFields::CalcMeshPos, SUBSAMPLE
+        d.start[a] = (int)lo;
+        d.step[a] = (int)step;
+        d.num[a] = (int)num[a];
+        total *= num[a];
+    }
+    if (!out) return FDTD_OK;  // size query
+    if (cap < 3 * total) {
+        set_error("fdtd_engine_dump_field: output buffer too small");
+        return FDTD_ERR_ARG;
+    }
+    if (!e->edges.p) {
+        set_error("fdtd_engine_dump_field: the operator description had no mesh lines (edge lengths unknown)");
+        return FDTD_ERR_STATE;
+    }
+    if (e->pending) {
+        set_error("fdtd_engine_dump_field: wait for the asynchronous iterate first");
+        return FDTD_ERR_STATE;
+    }
+    CK(cudaSetDevice(e->device));
+    int rc;
+    if ((rc = start(e))) return rc;
+    if (e->dump.n < 3 * total) {
+        if (e->dump.p) {
+            cudaFree(e->dump.p);
+            e->device_bytes -= e->dump.n * sizeof(float);
+            e->dump.p = nullptr;
+        }
+        if ((rc = e->dump.alloc(3 * total, e->device_bytes))) return rc;
+    }
+    const unsigned blocks = (unsigned)std::min<uint64_t>((total + 255) / 256, 4096);
+    k_dump_field<<<blocks, 256, 0, e->stream>>>(e->g, e->cur_V(), e->cur_I(), e->edges.p, d, e->dump.p);
+    if ((rc = check_launch())) return rc;
+    CK(cudaMemcpyAsync(out, e->dump.p, 3 * total * sizeof(float), cudaMemcpyDeviceToHost, e->stream));
     CK(cudaStreamSynchronize(e->stream));
     return FDTD_OK;
 }

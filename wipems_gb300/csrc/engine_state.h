@@ -66,6 +66,8 @@ struct fdtd_engine_s {
     DevGrid g{};
     DevBuf<float> V, I, FV, FI, AV, LV, AI, LI;
     DevBuf<uint8_t> ade_tile;  // per voltage-kernel tile plane: Lorentz/Drude flags (DevGrid::ade_tile)
+    DevBuf<double> edges;      // [2][Nx+Ny+Nz] main / dual edge lengths (field dumps; empty = no mesh lines)
+    DevBuf<float> dump;        // field-dump scratch, grown on demand
     DevBuf<float> V2, I2, FV2;  // second field / voltage-flux buffers (fused kernel)
     DevHalfBufs E, H;
     DevBuf<float> geo;

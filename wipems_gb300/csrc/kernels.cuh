@@ -492,6 +492,124 @@ static __global__ void k_rlc(const DevGrid g, RlcSet rs, int ts_off) {
     }
 }
 
+// ------------------------------------------------------------- field dumps
+// ProcessFields::CalcField (processfields.cpp:280-330) for E and H dumps on
+// the device: Engine_Interface_FDTD::GetRawInterpolatedField /
+// GetRawInterpolatedDualField (engine_interface_fdtd.cpp:60-200) with
+// GetRawField / GetRawDualField (E = V / edge length, H = I / dual edge
+// length, 0 where the length is 0), in double and in the reference's order,
+// stored as float like the reference's FDTD_FLOAT field arrays.  Output
+// [3][n0][n1][n2] at the mesh lines start + i * step.
+struct DumpBox {
+    int field;   // 0 = E, 1 = H
+    int interp;  // 0 = none, 1 = node, 2 = cell
+    int start[3], step[3], num[3];
+};
+
+static __global__ void k_dump_field(const DevGrid g, const float* __restrict__ V, const float* __restrict__ I,
+                                    const double* __restrict__ edges, DumpBox b, float* __restrict__ out) {
+    const long long total = (long long)b.num[0] * b.num[1] * b.num[2];
+    const int Nn[3] = {g.Nx, g.Ny, g.Nz};
+    const int eoff[3] = {0, g.Nx, g.Nx + g.Ny};
+    const int ntot = g.Nx + g.Ny + g.Nz;
+    auto len = [&](int n, int p, bool dual) -> double { return edges[(dual ? ntot : 0) + eoff[n] + p]; };
+    auto at = [&](int n, const int* p) -> long long {
+        return n * g.comp + (long long)p[0] * g.sx + (long long)p[1] * g.Nzp + p[2];
+    };
+    auto rawE = [&](int n, const int* p) -> double {  // GetRawField, type 0
+        const double value = V[at(n, p)];
+        const double delta = len(n, p[n], false);
+        return delta != 0.0 ? value / delta : 0.0;
+    };
+    auto rawH = [&](int n, const int* p) -> double {  // GetRawDualField, type 0
+        const double value = I[at(n, p)];
+        const double delta = len(n, p[n], true);
+        return delta != 0.0 ? value / delta : 0.0;
+    };
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < total;
+         k += (long long)gridDim.x * blockDim.x) {
+        const int l = (int)(k % b.num[2]);
+        const int j = (int)((k / b.num[2]) % b.num[1]);
+        const int i = (int)(k / ((long long)b.num[1] * b.num[2]));
+        const int pos[3] = {b.start[0] + i * b.step[0], b.start[1] + j * b.step[1], b.start[2] + l * b.step[2]};
+        int q[3] = {pos[0], pos[1], pos[2]};
+        double o[3];
+        const bool top = pos[0] == Nn[0] - 1 || pos[1] == Nn[1] - 1 || pos[2] == Nn[2] - 1;
+        for (int n = 0; n < 3; ++n) {
+            const int nP = (n + 1) % 3, nPP = (n + 2) % 3;
+            if (b.field == 0) {
+                if (b.interp == 0) {
+                    o[n] = rawE(n, pos);
+                } else if (b.interp == 1) {  // node: edge-length weighted mean of the two edges at the node
+                    if (pos[n] == Nn[n] - 1) {
+                        --q[n];
+                        o[n] = rawE(n, q);
+                        ++q[n];
+                        continue;
+                    }
+                    const double delta = len(n, q[n], false);
+                    o[n] = rawE(n, q);
+                    if (delta == 0.0) {
+                        o[n] = 0.0;
+                        continue;
+                    }
+                    if (pos[n] == 0) continue;
+                    --q[n];
+                    const double deltaDown = len(n, q[n], false);
+                    const double deltaRel = delta / (delta + deltaDown);
+                    o[n] = o[n] * (1.0 - deltaRel) + rawE(n, q) * deltaRel;
+                    ++q[n];
+                } else {  // cell: mean of the four edges around the cell centre line
+                    if (top) {
+                        o[n] = 0.0;
+                        continue;
+                    }
+                    o[n] = rawE(n, q);
+                    ++q[nP];
+                    o[n] += rawE(n, q);
+                    ++q[nPP];
+                    o[n] += rawE(n, q);
+                    --q[nP];
+                    o[n] += rawE(n, q);
+                    --q[nPP];
+                    o[n] /= 4;
+                }
+            } else {
+                if (b.interp == 0) {
+                    o[n] = rawH(n, pos);
+                } else if (b.interp == 1) {  // node: mean of the four dual edges around the node
+                    if (top || pos[nP] == 0 || pos[nPP] == 0) {
+                        o[n] = 0.0;
+                        continue;
+                    }
+                    o[n] = rawH(n, q);
+                    --q[nP];
+                    o[n] += rawH(n, q);
+                    --q[nPP];
+                    o[n] += rawH(n, q);
+                    ++q[nP];
+                    o[n] += rawH(n, q);
+                    ++q[nPP];
+                    o[n] /= 4;
+                } else {  // cell: dual-length weighted mean along n
+                    const double delta = len(n, q[n], true);
+                    o[n] = rawH(n, q);
+                    if (pos[n] >= Nn[n] - 1) {
+                        o[n] = 0.0;
+                        continue;
+                    }
+                    ++q[n];
+                    const double deltaUp = len(n, q[n], true);
+                    const double deltaRel = delta / (delta + deltaUp);
+                    o[n] = o[n] * (1.0 - deltaRel) + rawH(n, q) * deltaRel;
+                    --q[n];
+                }
+            }
+        }
+        for (int n = 0; n < 3; ++n) out[n * total + k] = (float)o[n];
+    }
+}
+
 // Full-grid energy (CalcFastEnergy) on demand.
 static __global__ void k_energy(const DevGrid g, double* out) {
     double es = 0.0, hs = 0.0;

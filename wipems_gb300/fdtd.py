@@ -35,7 +35,9 @@ def _d3(v) -> C.Array:
 
 
 class Scene:
-    """Mesh + primitives; the stand-in for CSXCAD (see DESIGN: box model)."""
+    """Mesh + primitives; the stand-in for CSXCAD: rectilinear mesh lines and
+    priority-ordered axis-aligned boxes of material, metal, lumped elements,
+    excitations and probes."""
 
     def __init__(self, lines_x, lines_y, lines_z, unit: float):
         self._lines = [np.ascontiguousarray(l, dtype=np.float64) for l in (lines_x, lines_y, lines_z)]
@@ -376,6 +378,26 @@ class Engine:
         cnt = C.c_uint32()
         check(lib().fdtd_engine_read_fd(self._h, buf.ctypes.data_as(_abi.PD), C.byref(cnt)), "fdtd_engine_read_fd")
         return buf[..., 0] + 1j * buf[..., 1], cnt.value
+
+    def dump_field(self, field: str = "E", interp: str = "node", start=(0, 0, 0), stop=None, step=(1, 1, 1)):
+        """E (V/m) or H (A/m) at the current timestep on the mesh lines
+        start + i * step (indices, both ends included) of a box, interpolated
+        as the reference's field dumps do (interp "none", "node" or "cell");
+        returns a float32 array [3][n0][n1][n2] (fdtd_engine_dump_field)."""
+        kinds = {"E": 0, "H": 1}
+        modes = {"none": 0, "node": 1, "cell": 2}
+        if field not in kinds or interp not in modes:
+            raise ValueError("field must be 'E' or 'H', interp 'none', 'node' or 'cell'")
+        if stop is None:
+            stop = tuple(n - 1 for n in self.op.num_lines)
+        b = _abi.FdtdDumpBox(kinds[field], modes[interp], (C.c_uint32 * 3)(*start), (C.c_uint32 * 3)(*stop),
+                             (C.c_uint32 * 3)(*step))
+        num = (C.c_uint32 * 3)()
+        check(lib().fdtd_engine_dump_field(self._h, C.byref(b), None, 0, num), "fdtd_engine_dump_field")
+        out = np.empty((3, num[0], num[1], num[2]), np.float32)
+        check(lib().fdtd_engine_dump_field(self._h, C.byref(b), out.ctypes.data_as(_abi.PF), out.size, num),
+              "fdtd_engine_dump_field")
+        return out
 
     def checkpoint(self) -> bytes:
         """All device state of the engine as bytes (fdtd_engine_checkpoint)."""
