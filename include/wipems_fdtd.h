@@ -154,8 +154,9 @@ int fdtd_scene_add_probe(fdtd_scene_t s, int type,
  * properties Material, Metal, LumpedElement (R, C, caps), Excitation,
  * ProbeBox (voltage / current) and LorentzMaterial (order 1), each with
  * <Box Priority><P1/><P2/></Box> primitives.  Other content that changes
- * the simulation is refused with FDTD_ERR_UNSUPPORTED naming it; field
- * dumps and field probes are skipped (counted in `skipped`). */
+ * the simulation is refused with FDTD_ERR_UNSUPPORTED naming it; E / H
+ * time-domain DumpBoxes are recorded (fdtd_scene_get_dump), other dumps and
+ * field probes are skipped (counted in `skipped`). */
 typedef struct {
     uint32_t nr_ts;           /* NumberOfTimesteps */
     double   end_crit;        /* endCriteria (0 in the file -> 1e-6) */
@@ -164,6 +165,21 @@ typedef struct {
     double   f0, fc;          /* Gaussian pulse */
     uint32_t num_properties, num_boxes, num_probes, skipped;
 } fdtd_xml_info;
+
+/* Time-domain field dumps the document asks for (<DumpBox DumpType="0|1"
+ * DumpMode FileType SubSampling> with a Box; other dump types are skipped):
+ * the box in drawing units, for the caller to snap and run with
+ * fdtd_engine_dump_field at its interval. */
+typedef struct {
+    char     name[64];
+    int      field;          /* FDTD_DUMP_E / FDTD_DUMP_H (DumpType 0 / 1) */
+    int      interp;         /* DumpMode: FDTD_INTERP_NONE / NODE / CELL */
+    int      file_type;      /* FileType: 0 VTK, 1 HDF5 */
+    double   start[3], stop[3];
+    uint32_t step[3];        /* SubSampling (1 = every line) */
+} fdtd_scene_dump;
+int fdtd_scene_num_dumps(fdtd_scene_t s, uint32_t* n);
+int fdtd_scene_get_dump(fdtd_scene_t s, uint32_t k, fdtd_scene_dump* out);
 
 int fdtd_scene_load_xml(const char* xml_text, fdtd_scene_t* out, fdtd_xml_info* info);
 int fdtd_scene_load_xml_file(const char* path, fdtd_scene_t* out, fdtd_xml_info* info);

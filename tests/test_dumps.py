@@ -49,3 +49,16 @@ def test_reference_interpolation_rules():
     h = dump_reference(V, I, lines, 1e-3, "H", "node", [0, 0, 0], [3, 3, 3], [1, 1, 1])
     assert np.all(h[:, 3, :, :] == 0) and np.all(h[2, :, 0, :] == 0)
     assert np.array_equal(edge_lengths(lines[0], 1.0, True), [1.0, 1.5, 2.5, 3.0])  # dual lines 0.5, 2, 4.5, 7.5
+
+
+def test_xml_dumpbox_becomes_a_field_dump():
+    from pathlib import Path
+    from wipems_gb300 import Scene
+    sc = Scene.from_xml(str(Path(__file__).parent / "golden" / "port_box.xml"))
+    op = Operator(sc)
+    (spec,) = sc.dumps()
+    d = FieldDump.from_spec(op, spec)
+    # the z = 3 plane of the 0.5 mm z mesh, every x and y line
+    assert d.start[2] == d.stop[2] == 6 and d.start[:2] == [0, 0] and d.stop[:2] == [24, 25]
+    assert [len(c) for c in d.coords] == [25, 26, 1]
+    assert abs(d.coords[2][0] - 3e-3) < 1e-15

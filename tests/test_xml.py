@@ -57,7 +57,11 @@ def test_xml_document_builds_the_api_operator():
     sx = Scene.from_xml(str(GOLDEN / "port_box.xml"))
     info = sx.xml_info
     assert info["nr_ts"] == 600 and info["end_crit"] == 1e-5 and info["excite_type"] == 0
-    assert info["num_probes"] == 2 and info["skipped"] == 1  # the field dump
+    assert info["num_probes"] == 2 and info["skipped"] == 0
+    # the E-field dump (DumpType 0, node interpolation) is recorded for the caller
+    d = sx.dumps()
+    assert d == [dict(name="Et", field="E", interp="node", file_type=0, start=[0.0, 0.0, 3.0],
+                      stop=[12.0, 16.0, 3.0], step=[1, 1, 1])]
     _same_operator(Operator(sx), Operator(_api_scene()))
 
 

@@ -67,6 +67,11 @@ class FdtdDumpBox(C.Structure):
     _fields_ = [("field", C.c_int), ("interp", C.c_int), ("start", u32 * 3), ("stop", u32 * 3), ("step", u32 * 3)]
 
 
+class FdtdSceneDump(C.Structure):
+    _fields_ = [("name", C.c_char * 64), ("field", C.c_int), ("interp", C.c_int), ("file_type", C.c_int),
+                ("start", C.c_double * 3), ("stop", C.c_double * 3), ("step", u32 * 3)]
+
+
 class FdtdProbeDesc(C.Structure):
     _fields_ = [("type", C.c_int), ("start", u32 * 3), ("stop", u32 * 3),
                 ("start_inside", C.c_int * 3), ("stop_inside", C.c_int * 3),
@@ -203,6 +208,8 @@ SIGNATURES = [
     ("fdtd_batch_create", C.c_int, [C.POINTER(_P), u32, C.POINTER(FdtdBatchOpts), C.POINTER(_P)]),
     ("fdtd_batch_accepts", C.c_int, [_P, C.POINTER(C.c_int)]),
     ("fdtd_engine_dump_field", C.c_int, [_P, C.POINTER(FdtdDumpBox), PF, C.c_uint64, PU32]),
+    ("fdtd_scene_num_dumps", C.c_int, [_P, PU32]),
+    ("fdtd_scene_get_dump", C.c_int, [_P, u32, C.POINTER(FdtdSceneDump)]),
     ("fdtd_batch_iterate", C.c_int, [_P, u32]),
     ("fdtd_batch_info", C.c_int, [_P, C.POINTER(FdtdBatchStats)]),
     ("fdtd_batch_destroy", C.c_int, [_P]),

@@ -56,6 +56,18 @@ struct Prim {
 
 }  // namespace wipems
 
+namespace wipems {
+// a time-domain field dump of the scene (<DumpBox>), applied by the caller
+struct DumpSpec {
+    std::string name;
+    int field = 0;   // 0 = E, 1 = H (DumpType 0 / 1)
+    int interp = 0;  // DumpMode: 0 none, 1 node, 2 cell
+    int file_type = 0;
+    double start[3] = {0, 0, 0}, stop[3] = {0, 0, 0};
+    uint32_t step[3] = {1, 1, 1};
+};
+}  // namespace wipems
+
 struct fdtd_scene_s {
     std::vector<double> lines[3];
     double unit = 1;
@@ -68,6 +80,7 @@ struct fdtd_scene_s {
     uint32_t nr_ts = 0;
     uint32_t oversampling = 4;
     std::vector<wipems::Prim> prims;
+    std::vector<wipems::DumpSpec> dumps;
 };
 
 namespace wipems {

@@ -1396,6 +1396,31 @@ int fdtd_scene_set_boundary(fdtd_scene_t s, const int bc[6], const uint32_t pml_
     return FDTD_OK;
 }
 
+int fdtd_scene_num_dumps(fdtd_scene_t s, uint32_t* n) {
+    if (!s || !n) return FDTD_ERR_ARG;
+    *n = (uint32_t)s->dumps.size();
+    return FDTD_OK;
+}
+
+int fdtd_scene_get_dump(fdtd_scene_t s, uint32_t k, fdtd_scene_dump* out) {
+    if (!s || !out || k >= s->dumps.size()) {
+        set_error("fdtd_scene_get_dump: no such dump");
+        return FDTD_ERR_ARG;
+    }
+    const DumpSpec& d = s->dumps[k];
+    std::memset(out, 0, sizeof(*out));
+    std::strncpy(out->name, d.name.c_str(), sizeof(out->name) - 1);
+    out->field = d.field;
+    out->interp = d.interp;
+    out->file_type = d.file_type;
+    for (int a = 0; a < 3; ++a) {
+        out->start[a] = d.start[a];
+        out->stop[a] = d.stop[a];
+        out->step[a] = d.step[a];
+    }
+    return FDTD_OK;
+}
+
 int fdtd_scene_set_mur_velocity(fdtd_scene_t s, const double v_phase[6]) {
     if (!s || !v_phase) return FDTD_ERR_ARG;
     for (int i = 0; i < 6; ++i) {

@@ -531,12 +531,35 @@ int fdtd_scene_load_xml(const char* text, fdtd_scene_t* out, fdtd_xml_info* info
                     return fail(rc, "probe '" + pname + "'");
                 ++inf.num_probes;
             }
-        } else if (p.name == "DumpBox" || p.name == "DebyeMaterial" || p.name == "ConductingSheet" ||
-                   p.name == "Resistance") {
-            if (p.name == "DumpBox") {
-                ++inf.skipped;  // field dumps: out of scope, no effect on the fields
+        } else if (p.name == "DumpBox") {
+            // time-domain E / H dumps are recorded for the caller (they do not
+            // change the fields); other dump types are skipped
+            double type, mode, ftype;
+            L.num(p, "DumpType", type, 0);
+            L.num(p, "DumpMode", mode, 0);
+            L.num(p, "FileType", ftype, 0);
+            std::vector<double> sub;
+            const std::string* ss = p.attr("SubSampling");
+            if (ss && (!list(*ss, sub) || sub.size() != 3)) L.bad(FDTD_ERR_ARG, "<DumpBox SubSampling> of '" + pname + "'");
+            if (L.code) return fail(L.code, L.err);
+            if ((type != 0 && type != 1) || mode < 0 || mode > 2) {
+                ++inf.skipped;
                 continue;
             }
+            for (const Box& b : boxes) {
+                DumpSpec d;
+                d.name = pname;
+                d.field = (int)type;
+                d.interp = (int)mode;
+                d.file_type = (int)ftype;
+                for (int a = 0; a < 3; ++a) {
+                    d.start[a] = b.a[a];
+                    d.stop[a] = b.b[a];
+                    d.step[a] = ss ? (uint32_t)std::max(1.0, sub[a]) : 1u;
+                }
+                sc->dumps.push_back(d);
+            }
+        } else if (p.name == "DebyeMaterial" || p.name == "ConductingSheet" || p.name == "Resistance") {
             return fail(FDTD_ERR_UNSUPPORTED, "property <" + p.name + "> ('" + pname + "')");
         } else {
             return fail(FDTD_ERR_UNSUPPORTED, "property <" + p.name + "> ('" + pname + "')");

@@ -119,6 +119,11 @@ class FieldDump:
         self.step = [max(1, int(s)) for s in step]
         self.coords = dump_coordinates(lines, unit, self.start, self.stop, self.step, self.dual)
 
+    @classmethod
+    def from_spec(cls, op, spec: dict) -> "FieldDump":
+        """A dump from Scene.dumps() (an XML <DumpBox>)."""
+        return cls(op, spec["name"], spec["field"], spec["interp"], spec["start"], spec["stop"], spec["step"])
+
     def values(self, engine):
         return engine.dump_field(self.field, self.interp, self.start, self.stop, self.step)
 

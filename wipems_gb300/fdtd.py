@@ -78,6 +78,20 @@ class Scene:
     def lines(self):
         return self._lines
 
+    def dumps(self) -> list:
+        """The time-domain E / H field dumps of the scene (XML <DumpBox>):
+        dicts of name, field ("E"/"H"), interp, file_type, start, stop (drawing
+        units) and step, for wipems_gb300.dumps.FieldDump.from_spec."""
+        n = C.c_uint32()
+        check(lib().fdtd_scene_num_dumps(self._h, C.byref(n)), "fdtd_scene_num_dumps")
+        out = []
+        for k in range(n.value):
+            d = _abi.FdtdSceneDump()
+            check(lib().fdtd_scene_get_dump(self._h, k, C.byref(d)), "fdtd_scene_get_dump")
+            out.append(dict(name=d.name.decode(), field="EH"[d.field], interp=("none", "node", "cell")[d.interp],
+                            file_type=d.file_type, start=list(d.start), stop=list(d.stop), step=list(d.step)))
+        return out
+
     def __del__(self):
         if getattr(self, "_h", None):
             try:
