@@ -501,9 +501,13 @@ int fdtd_server_create(const fdtd_server_opts* opts, fdtd_server_t* out) {
     if (o.max_active == 0) o.max_active = 256;
     if (o.round_steps == 0) o.round_steps = 128;
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    // concurrent narrow builds scale better than one wide build per job
-    if (o.build_workers <= 0) o.build_workers = (int)std::max(1u, hw / 2);
-    if (o.build_threads_per_job <= 0) o.build_threads_per_job = (int)std::max(1u, hw / (unsigned)o.build_workers);
+    // a few concurrent builds of a few threads each (measured on a 16-core
+    // host: 4 builds finish the first large jobs sooner than 8 or 16 narrow
+    // ones); one core is left to the GPU thread, which relaunches each job
+    // as soon as its round completes
+    if (o.build_workers <= 0) o.build_workers = (int)std::max(1u, hw / 4);
+    if (o.build_threads_per_job <= 0)
+        o.build_threads_per_job = (int)std::max(1u, (hw > 1 ? hw - 1 : 1) / (unsigned)o.build_workers);
     CK(cudaSetDevice(o.device));
     size_t free_b = 0, total_b = 0;
     CK(cudaMemGetInfo(&free_b, &total_b));
