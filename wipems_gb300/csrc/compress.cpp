@@ -513,9 +513,8 @@ int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
         M.cpp.assign(m.coef_pp, m.coef_pp + (size_t)m.n_p * m.n_pp);
         M.start_ts = m.start_ts;
         c->mur.push_back(std::move(M));
-        // the voltage kernel must keep zeroing a Mur face's line every step:
-        // neighbouring faces read it between the update and the apply
-        if (m.line == c->N[m.ny] - 1) c->trim_e[m.ny] = false;
+        // a top face's line may stay trimmed from the voltage kernel: the
+        // post-update reads the inert line as the zero the update leaves there
     }
     // Lumped RLC edges.  The engine applies them in a pass after the
     // voltage kernel (and the Mur post-update); the reference applies them

@@ -626,6 +626,7 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
         }
         e->mur.total = (uint32_t)tot_n;
         e->mur.idx16 = c->E.idx16 ? 1 : 0;
+        for (int a = 0; a < 3; ++a) e->mur.trim[a] = c->trim_e[a] ? 1 : 0;
         CK(cudaMemcpyAsync(e->mur_coef.p, hc.data(), hc.size() * sizeof(float), cudaMemcpyHostToDevice, e->stream));
     }
     if (c->rlc.size()) {
@@ -739,11 +740,11 @@ int probe_entries(const fdtd_engine_s* e, const fdtd_probe_desc* p, std::vector<
             return FDTD_ERR_ARG;
         }
         ProbeEntry pe;
-        pe.off = (uint32_t)((long long)x * e->g.sx + (long long)y * e->Nzp + z);
+        pe.off = (long long)x * e->g.sx + (long long)y * e->Nzp + z;
         pe.comp = (int8_t)comp;
         pe.sign = (int8_t)sign;
         pe.field = (int8_t)field;
-        pe.pad = 0;
+        std::memset(pe.pad, 0, sizeof(pe.pad));
         out.push_back(pe);
         return FDTD_OK;
     };

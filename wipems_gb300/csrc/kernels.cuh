@@ -195,11 +195,11 @@ __global__ void __launch_bounds__(256) k_curr(const DevGrid g, int ts_off, int X
 
 // ---------------------------------------------------------- probes / counter
 struct ProbeEntry {
-    uint32_t off;   // linear offset within the component (padded layout)
+    long long off;  // linear offset within the component (padded layout; grids may exceed 2^32 nodes)
     int8_t comp;    // 0..2
     int8_t sign;    // +1 / -1
     int8_t field;   // 0 = voltage, 1 = current
-    int8_t pad;
+    int8_t pad[5];
 };
 
 struct ProbeSet {
@@ -378,6 +378,7 @@ struct MurDev {
 struct MurSet {
     int nface;
     int idx16;        // E tuple index width (for the excitation lookup)
+    int trim[3];      // the last line of this axis is left out of the voltage kernel (inert)
     uint32_t total;
     MurDev f[6];
 };
@@ -406,8 +407,15 @@ static __global__ void k_mur(const DevGrid g, MurSet ms, int ts_off, int stage) 
             F.bp[loc] = __fsub_rn(V[nP * C + os], __fmul_rn(F.cp[loc], V[nP * C + ol]));
             F.bpp[loc] = __fsub_rn(V[nPP * C + os], __fmul_rn(F.cpp[loc], V[nPP * C + ol]));
         } else if (stage == 1) {
-            F.bp[loc] = __fadd_rn(F.bp[loc], __fmul_rn(F.cp[loc], V[nP * C + os]));
-            F.bpp[loc] = __fadd_rn(F.bpp[loc], __fmul_rn(F.cpp[loc], V[nPP * C + os]));
+            // on a last line the voltage kernel leaves out (all its edges inert)
+            // the update's result is zero: read that instead of the value an
+            // earlier apply left there
+            const bool inert = (ms.trim[nP] && sh[nP] == (nP == 0 ? g.Nx : nP == 1 ? g.Ny : g.Nz) - 1) ||
+                               (ms.trim[nPP] && sh[nPP] == (nPP == 0 ? g.Nx : nPP == 1 ? g.Ny : g.Nz) - 1);
+            const float vP = inert ? 0.f : V[nP * C + os];
+            const float vPP = inert ? 0.f : V[nPP * C + os];
+            F.bp[loc] = __fadd_rn(F.bp[loc], __fmul_rn(F.cp[loc], vP));
+            F.bpp[loc] = __fadd_rn(F.bpp[loc], __fmul_rn(F.cpp[loc], vPP));
         } else {
             const int comps[2] = {nP, nPP};
             const float vals[2] = {F.bp[loc], F.bpp[loc]};
