@@ -152,11 +152,11 @@ int fdtd_scene_add_probe(fdtd_scene_t s, int type,
  * codes, MUR_PhaseVelocity);
  * <RectilinearGrid DeltaUnit> with X/Y/ZLines; <BackgroundMaterial>; the
  * properties Material, Metal, LumpedElement (R, C, caps), Excitation,
- * ProbeBox (voltage / current) and LorentzMaterial (order 1), each with
+ * ProbeBox (voltage / current / E / H field) and LorentzMaterial (order 1), each with
  * <Box Priority><P1/><P2/></Box> primitives.  Other content that changes
  * the simulation is refused with FDTD_ERR_UNSUPPORTED naming it; E / H
  * time-domain DumpBoxes are recorded (fdtd_scene_get_dump), other dumps and
- * field probes are skipped (counted in `skipped`). */
+ * mode-match probes are skipped (counted in `skipped`). */
 typedef struct {
     uint32_t nr_ts;           /* NumberOfTimesteps */
     double   end_crit;        /* endCriteria (0 in the file -> 1e-6) */
@@ -308,7 +308,10 @@ typedef struct {
 int fdtd_operator_describe(fdtd_operator_t op, fdtd_op_desc* desc);
 
 /* Snapped probe of the operator (ProcessIntegral after
- * DefineStartStopCoord).  type 0 voltage, 1 current. */
+ * DefineStartStopCoord).  type 0 voltage, 1 current, 2 E-field probe, 3
+ * H-field probe (ProcessFieldProbe, Common/processfieldprobe.cpp:79-92: the
+ * field at `start` -- main mesh for E, dual mesh and dual time for H --
+ * without interpolation; three sample columns x, y, z in V/m or A/m). */
 typedef struct {
     int      type;
     uint32_t start[3], stop[3];
@@ -412,9 +415,11 @@ int fdtd_engine_reset(fdtd_engine_t eng);
 int fdtd_engine_destroy(fdtd_engine_t eng);
 
 /* Registers a probe (ProcessVoltage::CalcIntegral / ProcessCurrent::
- * CalcIntegral, processvoltage.cpp:43-47, processcurrent.cpp:93-168) to be
- * reduced on the device at every sample step.  Must precede the first
- * iterate.  Returns the probe slot in *slot. */
+ * CalcIntegral, processvoltage.cpp:43-47, processcurrent.cpp:93-168, or a
+ * field probe) to be evaluated on the device at every sample step.  Must
+ * precede the first iterate.  Returns the probe's first sample column in
+ * *slot: one column per voltage / current probe, three per field probe
+ * (field probes need the operator description's mesh lines). */
 int fdtd_engine_add_probe(fdtd_engine_t eng, const fdtd_probe_desc* p,
                           uint32_t* slot);
 
@@ -622,7 +627,7 @@ typedef struct {
     int      state;           /* FDTD_JOB_* */
     int      error;           /* status code of a failed job (message via fdtd_last_error) */
     uint32_t timesteps;       /* numTS at retirement */
-    uint32_t num_samples, num_probes, probe_interval;
+    uint32_t num_samples, num_probes, probe_interval;  /* num_probes: sample columns */
     uint64_t nodes;           /* lines product */
     uint32_t num_lines[3];
     double   dT;              /* timestep (s) */

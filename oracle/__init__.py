@@ -42,7 +42,7 @@ def run(desc, probes, n_steps: int, interval: int, engine: int = BASIC, threads:
     ProbeArr = type(probes[0]) * nprobe if nprobe else None
     parr = ProbeArr(*probes) if nprobe else None
     max_rows = (n_steps // interval + 2) if interval else 0
-    row = 2 + nprobe
+    row = 2 + sum(3 if p.type in (2, 3) else 1 for p in probes)  # three columns per field probe
     samples = np.zeros((max(max_rows, 1), row), np.float64)
     shape = (3,) + nl
     V = np.zeros(shape, np.float32) if fields else None

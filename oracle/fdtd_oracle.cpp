@@ -18,6 +18,7 @@
 //   Engine_Interface_FDTD::CalcVoltageIntegral  FDTD/engine_interface_fdtd.cpp:200-226
 //   ProcessCurrent::CalcIntegral (float acc.)   Common/processcurrent.cpp:93-168
 //   Engine_Interface_FDTD::CalcFastEnergy       FDTD/engine_interface_fdtd.cpp:292-337
+//   ProcessFieldProbe (E / H at a point)        Common/processfieldprobe.cpp:79-92
 // and, as the timed CPU baseline, the reference's default engine family:
 //   Engine_SSE_Compressed::UpdateVoltages/Currents  FDTD/engine_sse_compressed.cpp:48-263
 //     (z-interleaved f4 layout engine_sse.h:36-44, per-vector index
@@ -352,6 +353,32 @@ struct BasicEngine {
             excite<false>();
             ++numTS;
         }
+    }
+
+    // Operator::GetEdgeLength (GetDiscDelta x grid delta) from the mesh lines
+    double edge_length(int n, uint32_t pos, bool dual) const {
+        const double* l = op->lines[n];
+        if (!l) return 0.0;
+        const uint32_t Nn = N[n];
+        auto line = [&](uint32_t p, bool du) -> double {
+            if (!du) return l[p];
+            if (p < Nn - 1) return 0.5 * (l[p] + l[p + 1]);
+            return l[p] + 0.5 * (l[p] - l[p - 1]);
+        };
+        double d;
+        if (!dual)
+            d = (pos < Nn - 1) ? line(pos + 1, false) - line(pos, false) : line(pos, false) - line(pos - 1, false);
+        else
+            d = (pos > 0) ? line(pos, true) - line(pos - 1, true) : line(1, false) - line(0, false);
+        return d * op->unit;
+    }
+    // Engine_Interface_FDTD::GetRawField / GetRawDualField, type 0
+    // (engine_interface_fdtd.cpp:257-262, 128-133)
+    double raw_field(bool h, int n, const uint32_t* pos) {
+        const double value = h ? I(n, pos[0], pos[1], pos[2]) : V(n, pos[0], pos[1], pos[2]);
+        const double delta = edge_length(n, pos[n], h);
+        if (delta) return value / delta;
+        return 0.0;
     }
 
     double voltage_integral(const uint32_t* start, const uint32_t* stop) {
@@ -811,7 +838,9 @@ long oracle_run(const fdtd_op_desc* desc, const fdtd_probe_desc* probes, int n_p
     std::unique_ptr<SSEEngine> S;
     if (engine == 1) S.reset(new SSEEngine(desc));
     if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
-    const int row = 2 + n_probes;
+    int ncol = 0;  // sample columns: one per integral probe, three per field probe
+    for (int p = 0; p < n_probes; ++p) ncol += (probes[p].type == 2 || probes[p].type == 3) ? 3 : 1;
+    const int row = 2 + ncol;
     long rows = 0;
     double secs = 0;
     // field access for probes
@@ -831,11 +860,20 @@ long oracle_run(const fdtd_op_desc* desc, const fdtd_probe_desc* probes, int n_p
         double* r = samples + rows * row;
         r[0] = ts;
         r[1] = with_energy ? B.fast_energy() : -1.0;
+        int col = 2;
         for (int p = 0; p < n_probes; ++p) {
             const fdtd_probe_desc& pd = probes[p];
+            if (pd.type == 2 || pd.type == 3) {  // ProcessFieldProbe: GetEField / GetHField, no interpolation
+                for (int n = 0; n < 3; ++n) {
+                    double v = 0;
+                    if (pd.enabled) v = B.raw_field(pd.type == 3, n, pd.start);
+                    r[col++] = v * pd.weight;
+                }
+                continue;
+            }
             double v = 0;
             if (pd.enabled) v = (pd.type == 0) ? B.voltage_integral(pd.start, pd.stop) : B.current_integral(pd);
-            r[2 + p] = v * pd.weight;
+            r[col++] = v * pd.weight;
         }
         ++rows;
     };

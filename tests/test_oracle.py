@@ -77,3 +77,25 @@ def test_mur_boundaries_absorb():
     op2 = Operator(sc)
     r2 = oracle.run(op2.desc, op2.probes, 900, op2.probe_interval, engine=oracle.BASIC, fields=False)
     assert e[-1] / e.max() < 0.01 * r2["energy"][-1] / r2["energy"].max()
+
+
+def test_oracle_field_probes_are_field_over_edge_length():
+    """ProcessFieldProbe through GetRawField / GetRawDualField: the sample is
+    the field value over the (main or dual) edge length at the snapped
+    point, weighted."""
+    from helpers import edge_lengths
+    s = scenes.mini("upml", nr_ts=200)
+    s.add_probe([5.0, 6.0, 9.0], [5.0, 6.0, 9.0], 2)
+    s.add_probe([7.25, 4.25, 12.25], [7.25, 4.25, 12.25], 3, weight=3.0)
+    op = Operator(s)
+    pe, ph = op.probes[-2], op.probes[-1]
+    assert pe.enabled and ph.enabled and list(pe.start) == [10, 12, 18] and list(ph.start) == [14, 8, 24]
+    n = 4 * op.probe_interval
+    r = oracle.run(op.desc, op.probes, n, op.probe_interval, engine=oracle.BASIC)
+    assert r["values"].shape[1] == len(op.probes) - 2 + 6
+    lines = [np.ctypeslib.as_array(op.desc.lines[a], shape=(op.num_lines[a],)) for a in range(3)]
+    for c in range(3):
+        lm = edge_lengths(lines[c], op.desc.unit, False)[pe.start[c]]
+        ld = edge_lengths(lines[c], op.desc.unit, True)[ph.start[c]]
+        assert r["values"][-1, -6 + c] == float(r["volt"][c][tuple(pe.start)]) / lm
+        assert r["values"][-1, -3 + c] == float(r["curr"][c][tuple(ph.start)]) / ld * 3.0

@@ -146,3 +146,19 @@ def test_xml_lumped_rlc(letype, extra, n_rlc):
     na = a.desc.rlc.contents.count if a.desc.rlc else 0
     nb = b.desc.rlc.contents.count if b.desc.rlc else 0
     assert na == nb == n_rlc
+
+
+def test_xml_field_probes():
+    text = (GOLDEN / "port_box.xml").read_text().replace(
+        "</Properties>",
+        '<ProbeBox ID="7" Name="et" Type="2"><Primitives><Box Priority="0"><P1 X="4" Y="5" Z="2"/>'
+        '<P2 X="4" Y="5" Z="2"/></Box></Primitives></ProbeBox>'
+        '<ProbeBox ID="8" Name="ht" Type="3" Weight="2"><Primitives><Box Priority="0"><P1 X="4.25" Y="5.25" Z="2.25"/>'
+        '<P2 X="4.25" Y="5.25" Z="2.25"/></Box></Primitives></ProbeBox>'
+        '<ProbeBox ID="9" Name="mm" Type="10"><Primitives><Box Priority="0"><P1 X="4" Y="5" Z="2"/>'
+        '<P2 X="4" Y="5" Z="2"/></Box></Primitives></ProbeBox></Properties>', 1)
+    sx = Scene.from_xml(text)
+    assert sx.xml_info["num_probes"] == 4 and sx.xml_info["skipped"] == 1  # the mode-match probe
+    op = Operator(sx)
+    types = [p.type for p in op.probes]
+    assert types[-2:] == [2, 3] and op.probes[-1].weight == 2.0

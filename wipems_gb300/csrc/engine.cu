@@ -204,18 +204,22 @@ int upload_probes(fdtd_engine_s* e) {
     if ((rc = e->d_entries.alloc(std::max<size_t>(1, e->h_entries.size()), e->device_bytes))) return rc;
     if ((rc = e->d_first.alloc(np + 1, e->device_bytes))) return rc;
     if ((rc = e->d_weight.alloc(std::max<uint32_t>(1, np), e->device_bytes))) return rc;
+    if ((rc = e->d_div.alloc(std::max<uint32_t>(1, np), e->device_bytes))) return rc;
     if (!e->h_entries.empty())
         CK(cudaMemcpyAsync(e->d_entries.p, e->h_entries.data(), e->h_entries.size() * sizeof(ProbeEntry),
                            cudaMemcpyHostToDevice, e->stream));
     CK(cudaMemcpyAsync(e->d_first.p, e->h_first.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice, e->stream));
-    if (np)
+    if (np) {
         CK(cudaMemcpyAsync(e->d_weight.p, e->h_weight.data(), np * sizeof(double), cudaMemcpyHostToDevice,
                            e->stream));
+        CK(cudaMemcpyAsync(e->d_div.p, e->h_div.data(), np * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+    }
     const int row = 2 + (int)np;
     if ((rc = e->ring.alloc((size_t)e->cap * row, e->device_bytes))) return rc;
     e->ps.entries = e->d_entries.p;
     e->ps.first = e->d_first.p;
     e->ps.weight = e->d_weight.p;
+    e->ps.div = e->d_div.p;
     e->ps.nprobe = (int)np;
     e->ps.row_doubles = row;
     e->ps.ring = e->ring.p;
@@ -671,6 +675,7 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     g.AV = e->AV.p;
     g.LV = e->LV.p;
     if (!c->edges.empty()) {
+        e->h_edges = c->edges;
         if ((rc = e->edges.alloc(c->edges.size(), tot))) return rc;
         CK(cudaMemcpy(e->edges.p, c->edges.data(), c->edges.size() * sizeof(double), cudaMemcpyHostToDevice));
     }
@@ -876,12 +881,46 @@ int fdtd_engine_add_probe(fdtd_engine_t e, const fdtd_probe_desc* p, uint32_t* s
         set_error("fdtd_engine_add_probe: probes must be added before the first iterate");
         return FDTD_ERR_STATE;
     }
+    if (p->type == 2 || p->type == 3) {  // field probe: three columns, one entry each
+        const bool h = p->type == 3;
+        for (int a = 0; a < 3; ++a)
+            if (p->start[a] >= e->N[a]) {
+                set_error("fdtd_engine_add_probe: field probe outside the grid");
+                return FDTD_ERR_ARG;
+            }
+        if (p->enabled && e->h_edges.empty()) {
+            set_error("fdtd_engine_add_probe: field probes need the mesh lines in the operator description");
+            return FDTD_ERR_STATE;
+        }
+        if (slot) *slot = (uint32_t)e->h_weight.size();
+        const size_t ntot = (size_t)e->N[0] + e->N[1] + e->N[2];
+        const size_t eoff[3] = {0, e->N[0], (size_t)e->N[0] + e->N[1]};
+        for (int n = 0; n < 3; ++n) {
+            double dv = -1.0;  // disabled probe or zero edge length: the column reads 0
+            if (p->enabled) {
+                ProbeEntry pe{};
+                pe.off = (long long)p->start[0] * e->g.sx + (long long)p->start[1] * e->Nzp + p->start[2];
+                pe.comp = (int8_t)n;
+                pe.sign = 1;
+                pe.field = (int8_t)(h ? 1 : 0);
+                e->h_entries.push_back(pe);
+                const double len = e->h_edges[(h ? ntot : 0) + eoff[n] + p->start[n]];
+                if (len != 0.0) dv = len;
+            }
+            e->h_first.push_back((int)e->h_entries.size());
+            e->h_weight.push_back(p->weight);
+            e->h_div.push_back(dv);
+            e->h_dual.push_back(h ? 1 : 0);
+        }
+        return FDTD_OK;
+    }
     std::vector<ProbeEntry> ent;
     const int rc = probe_entries(e, p, ent);
     if (rc) return rc;
     e->h_entries.insert(e->h_entries.end(), ent.begin(), ent.end());
     e->h_first.push_back((int)e->h_entries.size());
     e->h_weight.push_back(p->weight);
+    e->h_div.push_back(0.0);
     e->h_dual.push_back(p->type == 1 ? 1 : 0);
     if (slot) *slot = (uint32_t)(e->h_weight.size() - 1);
     return FDTD_OK;

@@ -85,6 +85,8 @@ struct fdtd_engine_s {
     std::vector<ProbeEntry> h_entries;
     std::vector<int> h_first{0};
     std::vector<double> h_weight;
+    std::vector<double> h_div;         // per column: 0 integral, else field-probe edge length (see ProbeSet::div)
+    std::vector<double> h_edges;       // host copy of the edge lengths (field probes)
     std::vector<int> h_dual;           // per probe: 1 = current probe (dual time)
     // frequency-domain accumulation (0 frequencies = off)
     std::vector<double> h_freq;
@@ -101,7 +103,7 @@ struct fdtd_engine_s {
     RlcSet rlc{};
     DevBuf<ProbeEntry> d_entries;
     DevBuf<int> d_first;
-    DevBuf<double> d_weight;
+    DevBuf<double> d_weight, d_div;
     DevBuf<double> ring;
     ProbeSet ps{};
     bool probes_uploaded = false;

@@ -206,6 +206,8 @@ struct ProbeSet {
     const ProbeEntry* entries;  // all probes' entries, concatenated
     const int* first;           // [nprobe+1] entry ranges
     const double* weight;       // [nprobe]
+    const double* div;          // [nprobe]: 0 = an integral; > 0 = a field-probe column, value / div
+                                // (the edge length); < 0 = a field-probe column on an edge of length 0
     int nprobe;
     int row_doubles;            // doubles per record row (2 + nprobe)
     double* ring;               // [cap][row_doubles]: ts, energy, values...
@@ -250,6 +252,20 @@ __device__ __forceinline__ double probe_sum(const ProbeSet& ps, const DevGrid& g
     return current ? (double)accf : accd;
 }
 
+// Sample column p: an integral (probe_sum) or one component of a field
+// probe, GetRawField / GetRawDualField (engine_interface_fdtd.cpp:257-266
+// and 128-142): the field value in double divided by the edge length, 0 for
+// an edge of length 0.
+__device__ __forceinline__ double probe_value(const ProbeSet& ps, const DevGrid& g, int p, int ts, int lane) {
+    const double dv = ps.div[p];
+    if (dv == 0.0) return probe_sum(ps, g, p, ts, lane);
+    if (dv < 0.0) return 0.0;
+    const ProbeEntry pe = ps.entries[ps.first[p]];
+    const bool odd = g.V2 && (ts & 1);
+    const float* f = pe.field ? (odd ? g.I2 : g.I) : (odd ? g.V2 : g.V);
+    return (double)f[(long long)pe.comp * g.comp + pe.off] / dv;
+}
+
 // Frequency-domain probe accumulation (ProcessIntegral::Process,
 // processintegral.cpp:154-168): on every FD step, for each probe p and
 // frequency f,  F[p][f] += v_p * weight_p * exp(-2 pi i f t_p) * scale  with
@@ -275,7 +291,7 @@ static __global__ void k_fd_accumulate(const int* d_ts, int expect_ts, ProbeSet 
     __syncthreads();
     if (!s_go) return;
     for (int p = warp; p < ps.nprobe; p += nwarps) {
-        const double acc = probe_sum(ps, g, p, expect_ts, lane);
+        const double acc = probe_value(ps, g, p, expect_ts, lane);
         if (lane == 0) s_val[p] = acc * ps.weight[p];
     }
     __syncthreads();
@@ -331,7 +347,7 @@ __device__ __forceinline__ void advance_sample(int* d_ts, int adv, int sample, c
     const int warp = tid >> 5, lane = tid & 31;
     const int nwarps = nthr >> 5;
     for (int p = warp; p < ps.nprobe; p += nwarps) {
-        const double acc = probe_sum(ps, g, p, s_ts, lane);
+        const double acc = probe_value(ps, g, p, s_ts, lane);
         if (lane == 0) rec[2 + p] = acc * ps.weight[p];
     }
     if (tid == 0) {

@@ -1278,7 +1278,15 @@ static int build_operator(const fdtd_scene_s& S, int threads, fdtd_operator_s& o
         d.norm_dir = p.norm_dir;
         d.enabled = 1;
         bool si[3] = {false, false, false}, so[3] = {false, false, false};
-        if (p.probe_type == 0) {
+        if (p.probe_type == 2 || p.probe_type == 3) {
+            // ProcessFieldProbe: the start point snapped to the main mesh (E)
+            // or the dual mesh (H, SetDualMesh, openems.cpp:520-524)
+            d.enabled = g.snap_mesh(p.start, d.start, p.probe_type == 3, si) ? 1 : 0;
+            for (int n = 0; n < 3; ++n) {
+                d.stop[n] = d.start[n];
+                so[n] = si[n];
+            }
+        } else if (p.probe_type == 0) {
             // ProcessVoltage::DefineStartStopCoord: SnapToMesh on the main mesh
             g.snap_mesh(p.start, d.start, false, si);
             g.snap_mesh(p.stop, d.stop, false, so);
@@ -1557,8 +1565,8 @@ int fdtd_scene_add_lorentz(fdtd_scene_t s, int prio, const double start[3], cons
 
 int fdtd_scene_add_probe(fdtd_scene_t s, int type, const double start[3], const double stop[3], double weight,
                          int norm_dir) {
-    if (!s || !check_box(start, stop) || (type != 0 && type != 1) || norm_dir < -1 || norm_dir > 2) {
-        set_error("fdtd_scene_add_probe: type must be 0 (voltage) or 1 (current)");
+    if (!s || !check_box(start, stop) || type < 0 || type > 3 || norm_dir < -1 || norm_dir > 2) {
+        set_error("fdtd_scene_add_probe: type must be 0 (voltage), 1 (current), 2 (E field) or 3 (H field)");
         return FDTD_ERR_ARG;
     }
     Prim p = make_box(PK_PROBE, 0, start, stop);

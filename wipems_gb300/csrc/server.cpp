@@ -578,7 +578,9 @@ int fdtd_server_job_status(fdtd_server_t s, uint64_t id, fdtd_job_status* st) {
     st->error = j->error;
     st->timesteps = j->ts;
     st->num_samples = (uint32_t)j->s_ts.size();
-    st->num_probes = (uint32_t)j->probes.size();
+    uint32_t cols = 0;  // sample columns: one per integral probe, three per field probe
+    for (const fdtd_probe_desc& p : j->probes) cols += (p.type == 2 || p.type == 3) ? 3u : 1u;
+    st->num_probes = cols;
     st->nodes = j->nodes;
     for (int a = 0; a < 3; ++a) st->num_lines[a] = j->N[a];
     st->dT = j->dT;

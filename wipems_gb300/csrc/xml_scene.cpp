@@ -522,7 +522,7 @@ int fdtd_scene_load_xml(const char* text, fdtd_scene_t* out, fdtd_xml_info* info
             L.num(p, "Type", type, 0);
             L.num(p, "Weight", weight, 1);
             L.num(p, "NormDir", nd, -1);
-            if (type != 0 && type != 1) {  // field / other probes: not part of the integral probes
+            if (type < 0 || type > 3) {  // mode-match and other probes
                 ++inf.skipped;
                 continue;
             }

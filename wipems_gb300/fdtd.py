@@ -260,9 +260,10 @@ class Samples:
     probe_types: list = field(default_factory=list)
 
     def times(self, p: int) -> np.ndarray:
-        """Sample times of probe p: voltage probes at ts*dT, current probes on
-        the dual time (ts+0.5)*dT (openems.cpp:522-526)."""
-        dual = 0.5 if self.probe_types[p] == 1 else 0.0
+        """Sample times of column p: voltage and E-field probes at ts*dT,
+        current and H-field probes on the dual time (ts+0.5)*dT
+        (openems.cpp:520-526)."""
+        dual = 0.5 if self.probe_types[p] in (1, 3) else 0.0
         return (self.ts + dual) * self.dT
 
 
@@ -340,7 +341,7 @@ class Engine:
         if probes:
             for p in op.probes:
                 check(lib().fdtd_engine_add_probe(h, C.byref(p), None), "fdtd_engine_add_probe")
-                self.probe_types.append(p.type)
+                self.probe_types += [p.type] * (3 if p.type in (2, 3) else 1)  # one column per field component
 
     def close(self):
         if getattr(self, "_h", None):
@@ -587,7 +588,7 @@ class Server:
         jid = C.c_uint64()
         check(lib().fdtd_server_submit(self._h, scene._h, C.byref(o), C.byref(jid)), "fdtd_server_submit")
         scene._h = None
-        self._probe_types[jid.value] = [p["type"] for p in scene.probes]
+        self._probe_types[jid.value] = [p["type"] for p in scene.probes for _ in range(3 if p["type"] in (2, 3) else 1)]
         return jid.value
 
     def status(self, job: int) -> dict:
