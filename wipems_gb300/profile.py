@@ -1,7 +1,7 @@
 """Profiling driver: builds one workload and runs a few timesteps, so that an
 external profiler (ncu) can capture the half-step kernels.
 
-    python -m wipems_gb300.profile --workload l256|p64|d192|l160|b96 --steps 8 [--graphs]
+    python -m wipems_gb300.profile --workload l256|p64|d192|l160|b96|l256mur --steps 8 [--graphs]
 
 Kernels are launched individually (no CUDA graph) unless --graphs is given,
 so a launch list shows every E / H kernel separately.
@@ -14,7 +14,7 @@ import time
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="l256", choices=["l256", "p64", "d192", "l160", "b96"])
+    ap.add_argument("--workload", default="l256", choices=["l256", "p64", "d192", "l160", "b96", "l256mur"])
     ap.add_argument("--jobs", type=int, default=24, help="b96: number of sweep jobs (seeds 0..jobs-1)")
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--graphs", action="store_true")
@@ -38,6 +38,10 @@ def main():
         return
     if args.workload == "l256":
         sc = scenes.l256()
+    elif args.workload == "l256mur":  # the L256 grid closed by Mur faces instead of UPML
+        from .fdtd import BC_MUR
+        sc = scenes.l256()
+        sc.set_boundary([BC_MUR] * 6, [0] * 6)
     elif args.workload == "l160":
         sc = scenes.l256(cells=160)
     elif args.workload == "p64":
