@@ -106,3 +106,24 @@ def test_batch_mode_runs_unbatchable_jobs_beside_the_batch():
     for (k, s), jid in ids.items():
         _same(_alone(k, s), srv, jid)
     srv.close()
+
+
+def test_server_job_with_field_probes():
+    """Field probes add three sample columns; the server's samples match the
+    job run alone."""
+    s = scenes.mini("upml", seed=3, nr_ts=NR_TS)
+    s.add_probe([5.0, 6.0, 9.0], [5.0, 6.0, 9.0], 2)
+    s.add_probe([7.25, 4.25, 12.25], [7.25, 4.25, 12.25], 3)
+    srv = Server(round_steps=64)
+    jid = srv.submit(s, end_crit=CRIT, keep_fields=True)
+    srv.wait(0, timeout=300)
+    st = srv.status(jid)
+    assert st["state"] == "done" and st["num_probes"] == 2 + 6
+    s2 = scenes.mini("upml", seed=3, nr_ts=NR_TS)
+    s2.add_probe([5.0, 6.0, 9.0], [5.0, 6.0, 9.0], 2)
+    s2.add_probe([7.25, 4.25, 12.25], [7.25, 4.25, 12.25], 3)
+    e = Engine(Operator(s2), end_crit=CRIT)
+    e.iterate(NR_TS)
+    _same(e, srv, jid)
+    assert srv.samples(jid).times(4)[1] - srv.samples(jid).times(4)[0] > 0
+    srv.close()

@@ -201,10 +201,10 @@ int upload_probes(fdtd_engine_s* e) {
     if (e->probes_uploaded) return FDTD_OK;
     const uint32_t np = (uint32_t)e->h_weight.size();
     int rc;
-    if ((rc = e->d_entries.alloc(std::max<size_t>(1, e->h_entries.size()), e->device_bytes))) return rc;
-    if ((rc = e->d_first.alloc(np + 1, e->device_bytes))) return rc;
-    if ((rc = e->d_weight.alloc(std::max<uint32_t>(1, np), e->device_bytes))) return rc;
-    if ((rc = e->d_div.alloc(std::max<uint32_t>(1, np), e->device_bytes))) return rc;
+    if ((rc = e->d_entries.alloc(std::max<size_t>(1, e->h_entries.size()), e->device_bytes, e->stream))) return rc;
+    if ((rc = e->d_first.alloc(np + 1, e->device_bytes, e->stream))) return rc;
+    if ((rc = e->d_weight.alloc(std::max<uint32_t>(1, np), e->device_bytes, e->stream))) return rc;
+    if ((rc = e->d_div.alloc(std::max<uint32_t>(1, np), e->device_bytes, e->stream))) return rc;
     if (!e->h_entries.empty())
         CK(cudaMemcpyAsync(e->d_entries.p, e->h_entries.data(), e->h_entries.size() * sizeof(ProbeEntry),
                            cudaMemcpyHostToDevice, e->stream));
@@ -215,7 +215,7 @@ int upload_probes(fdtd_engine_s* e) {
         CK(cudaMemcpyAsync(e->d_div.p, e->h_div.data(), np * sizeof(double), cudaMemcpyHostToDevice, e->stream));
     }
     const int row = 2 + (int)np;
-    if ((rc = e->ring.alloc((size_t)e->cap * row, e->device_bytes))) return rc;
+    if ((rc = e->ring.alloc((size_t)e->cap * row, e->device_bytes, e->stream))) return rc;
     e->ps.entries = e->d_entries.p;
     e->ps.first = e->d_first.p;
     e->ps.weight = e->d_weight.p;
@@ -231,8 +231,9 @@ int upload_probes(fdtd_engine_s* e) {
     e->ps.stop_ts = e->end_crit > 0 ? (int)e->stop_ts : 0;
     if (e->fd_interval && !e->h_freq.empty() && np) {
         const size_t nf = e->h_freq.size();
-        if ((rc = e->d_freq.alloc(nf, e->device_bytes)) || (rc = e->d_fd.alloc(2 * np * nf, e->device_bytes)) ||
-            (rc = e->d_fd_dual.alloc(np, e->device_bytes)) || (rc = e->d_fd_count.alloc(1, e->device_bytes)))
+        uint64_t& tb = e->device_bytes;
+        if ((rc = e->d_freq.alloc(nf, tb, e->stream)) || (rc = e->d_fd.alloc(2 * np * nf, tb, e->stream)) ||
+            (rc = e->d_fd_dual.alloc(np, tb, e->stream)) || (rc = e->d_fd_count.alloc(1, tb, e->stream)))
             return rc;
         CK(cudaMemcpyAsync(e->d_freq.p, e->h_freq.data(), nf * sizeof(double), cudaMemcpyHostToDevice, e->stream));
         CK(cudaMemcpyAsync(e->d_fd_dual.p, e->h_dual.data(), np * sizeof(int), cudaMemcpyHostToDevice, e->stream));
@@ -490,9 +491,10 @@ int upload_half(fdtd_engine_s* e, const HalfTables& T, DevHalfBufs& B, DevHalf& 
     int rc;
     uint64_t& tot = e->device_bytes;
     B.idx16 = T.idx16;
-    if ((rc = B.idx.alloc(T.idx_bytes, tot)) || (rc = B.main.alloc(T.main.size(), tot)) ||
-        (rc = B.exc.alloc(std::max<size_t>(4, T.exc.size()), tot)) || (rc = B.upml.alloc(T.upml.size(), tot)) ||
-        (rc = B.ade.alloc(T.ade.size(), tot)))
+    cudaStream_t st = e->stream;
+    if ((rc = B.idx.alloc(T.idx_bytes, tot, st)) || (rc = B.main.alloc(T.main.size(), tot, st)) ||
+        (rc = B.exc.alloc(std::max<size_t>(4, T.exc.size()), tot, st)) ||
+        (rc = B.upml.alloc(T.upml.size(), tot, st)) || (rc = B.ade.alloc(T.ade.size(), tot, st)))
         return rc;
     auto h2d = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
         return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, e->stream) : cudaSuccess;
@@ -516,6 +518,13 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     e->device = opts ? opts->device : 0;
     CK(cudaSetDevice(e->device));
     CK(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+    {  // keep freed pool memory in this process for the next engine (no return to the driver)
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, e->device) == cudaSuccess) {
+            uint64_t keep = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+    }
     CK(cudaEventCreate(&e->ev0));
     CK(cudaEventCreate(&e->ev1));
     e->TY = (opts && opts->tile_y > 0) ? opts->tile_y : 8;
@@ -571,23 +580,24 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     int rc;
     uint64_t& tot = e->device_bytes;
     const size_t F = 3 * (size_t)e->comp;
-    if ((rc = e->V.alloc(F, tot)) || (rc = e->I.alloc(F, tot))) return rc;
-    if (any_upml && ((rc = e->FV.alloc(F, tot)) || (rc = e->FI.alloc(F, tot)))) return rc;
-    if (e->fused && ((rc = e->V2.alloc(F, tot)) || (rc = e->I2.alloc(F, tot)))) return rc;
-    if (e->fused && any_upml && (rc = e->FV2.alloc(F, tot))) return rc;
-    if (c->E.any_ade && (rc = e->AV.alloc(F, tot))) return rc;
-    if (c->E.any_lor && (rc = e->LV.alloc(F, tot))) return rc;
-    if (c->H.any_ade && (rc = e->AI.alloc(F, tot))) return rc;
-    if (c->H.any_lor && (rc = e->LI.alloc(F, tot))) return rc;
-    if ((rc = e->sigV.alloc(std::max<uint32_t>(1, c->sig_len), tot)) ||
-        (rc = e->sigC.alloc(std::max<uint32_t>(1, c->sig_len), tot)))
+    if ((rc = e->V.alloc(F, tot, e->stream)) || (rc = e->I.alloc(F, tot, e->stream))) return rc;
+    if (any_upml && ((rc = e->FV.alloc(F, tot, e->stream)) || (rc = e->FI.alloc(F, tot, e->stream)))) return rc;
+    if (e->fused && ((rc = e->V2.alloc(F, tot, e->stream)) || (rc = e->I2.alloc(F, tot, e->stream)))) return rc;
+    if (e->fused && any_upml && (rc = e->FV2.alloc(F, tot, e->stream))) return rc;
+    if (c->E.any_ade && (rc = e->AV.alloc(F, tot, e->stream))) return rc;
+    if (c->E.any_lor && (rc = e->LV.alloc(F, tot, e->stream))) return rc;
+    if (c->H.any_ade && (rc = e->AI.alloc(F, tot, e->stream))) return rc;
+    if (c->H.any_lor && (rc = e->LI.alloc(F, tot, e->stream))) return rc;
+    if ((rc = e->sigV.alloc(std::max<uint32_t>(1, c->sig_len), tot, e->stream)) ||
+        (rc = e->sigC.alloc(std::max<uint32_t>(1, c->sig_len), tot, e->stream)))
         return rc;
-    if ((rc = e->ctl.alloc(4, tot)) || (rc = e->d_eacc.alloc(4, tot)) || (rc = e->d_energy_tmp.alloc(2, tot)))
+    if ((rc = e->ctl.alloc(4, tot, e->stream)) || (rc = e->d_eacc.alloc(4, tot, e->stream)) ||
+        (rc = e->d_energy_tmp.alloc(2, tot, e->stream)))
         return rc;
     DevGrid& g = e->g;
     if ((rc = upload_half(e, c->E, e->E, g.e)) || (rc = upload_half(e, c->H, e->H, g.h))) return rc;
     if (c->geo) {
-        if ((rc = e->geo.alloc(c->geom.size(), tot))) return rc;
+        if ((rc = e->geo.alloc(c->geom.size(), tot, e->stream))) return rc;
         CK(cudaMemcpyAsync(e->geo.p, c->geom.data(), c->geom.size() * sizeof(float), cudaMemcpyHostToDevice,
                            e->stream));
     }
@@ -605,7 +615,8 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
         }
         size_t tot_n = 0;
         for (const MurFace& M : c->mur) tot_n += (size_t)M.n[0] * M.n[1];
-        if ((rc = e->mur_coef.alloc(2 * tot_n, tot)) || (rc = e->mur_buf.alloc(2 * tot_n, tot))) return rc;
+        if ((rc = e->mur_coef.alloc(2 * tot_n, tot, e->stream)) || (rc = e->mur_buf.alloc(2 * tot_n, tot, e->stream)))
+            return rc;
         CK(cudaMemsetAsync(e->mur_buf.p, 0, 2 * tot_n * sizeof(float), e->stream));
         std::vector<float> hc(2 * tot_n);
         size_t off = 0;
@@ -639,8 +650,8 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
             return FDTD_ERR_UNSUPPORTED;
         }
         const size_t n = c->rlc.size();
-        if ((rc = e->rlc_coef.alloc(9 * n, tot)) || (rc = e->rlc_state.alloc(7 * n, tot)) ||
-            (rc = e->rlc_off.alloc(n, tot)))
+        if ((rc = e->rlc_coef.alloc(9 * n, tot, e->stream)) || (rc = e->rlc_state.alloc(7 * n, tot, e->stream)) ||
+            (rc = e->rlc_off.alloc(n, tot, e->stream)))
             return rc;
         std::vector<float> hc(9 * n);
         std::vector<long long> ho(n);
@@ -676,7 +687,7 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     g.LV = e->LV.p;
     if (!c->edges.empty()) {
         e->h_edges = c->edges;
-        if ((rc = e->edges.alloc(c->edges.size(), tot))) return rc;
+        if ((rc = e->edges.alloc(c->edges.size(), tot, e->stream))) return rc;
         CK(cudaMemcpy(e->edges.p, c->edges.data(), c->edges.size() * sizeof(double), cudaMemcpyHostToDevice));
     }
     if (c->E.any_ade) {  // which voltage-kernel tile planes hold Lorentz/Drude nodes
@@ -698,7 +709,7 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
                     hf[z / 32] |= tf[t];
                 }
             }
-        if ((rc = e->ade_tile.alloc(h.size(), tot))) return rc;
+        if ((rc = e->ade_tile.alloc(h.size(), tot, e->stream))) return rc;
         CK(cudaMemcpy(e->ade_tile.p, h.data(), h.size(), cudaMemcpyHostToDevice));
         g.ade_tile = e->ade_tile.p;
     } else {
@@ -1311,11 +1322,10 @@ int fdtd_engine_dump_field(fdtd_engine_t e, const fdtd_dump_box* b, float* out, 
     if ((rc = start(e))) return rc;
     if (e->dump.n < 3 * total) {
         if (e->dump.p) {
-            cudaFree(e->dump.p);
             e->device_bytes -= e->dump.n * sizeof(float);
-            e->dump.p = nullptr;
+            e->dump.release();
         }
-        if ((rc = e->dump.alloc(3 * total, e->device_bytes))) return rc;
+        if ((rc = e->dump.alloc(3 * total, e->device_bytes, e->stream))) return rc;
     }
     const unsigned blocks = (unsigned)std::min<uint64_t>((total + 255) / 256, 4096);
     k_dump_field<<<blocks, 256, 0, e->stream>>>(e->g, e->cur_V(), e->cur_I(), e->edges.p, d, e->dump.p);

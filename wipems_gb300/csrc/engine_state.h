@@ -25,20 +25,33 @@ namespace wipems {
         }                                                                  \
     } while (0)
 
+// Device buffer.  With a stream the memory comes from the device's
+// stream-ordered pool (cudaMallocAsync / cudaFreeAsync on that stream):
+// unlike cudaMalloc / cudaFree, neither synchronises the device, so a
+// server can create and destroy engines while other engines' work is in
+// flight.  The stream must outlive the buffer.
 template <class T>
 struct DevBuf {
     T* p = nullptr;
     size_t n = 0;
-    ~DevBuf() {
-        if (p) cudaFree(p);
+    cudaStream_t s = nullptr;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) {
+            if (s) cudaFreeAsync(p, s);
+            else cudaFree(p);
+        }
+        p = nullptr;
     }
-    int alloc(size_t count, uint64_t& total) {
+    int alloc(size_t count, uint64_t& total, cudaStream_t stream = nullptr) {
         n = count;
+        s = stream;
         if (count == 0) return FDTD_OK;
-        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        cudaError_t e = stream ? cudaMallocAsync(&p, count * sizeof(T), stream) : cudaMalloc(&p, count * sizeof(T));
+        if (e == cudaSuccess && stream) e = cudaStreamSynchronize(stream);  // usable from any stream from here on
         if (e != cudaSuccess) {
             p = nullptr;
-            set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+            set_error(std::string(stream ? "cudaMallocAsync: " : "cudaMalloc: ") + cudaGetErrorString(e));
             return FDTD_ERR_NOMEM;
         }
         total += count * sizeof(T);
@@ -59,6 +72,14 @@ using namespace wipems;
 struct fdtd_engine_s {
     int device = 0;
     cudaStream_t stream = nullptr;
+    // destroys the stream after every member declared below (the device
+    // buffers free themselves on it first)
+    struct StreamGuard {
+        cudaStream_t* s;
+        ~StreamGuard() {
+            if (*s) cudaStreamDestroy(*s);
+        }
+    } stream_guard{&stream};
     uint32_t N[3];
     int Nzp = 0;
     long long comp = 0;
@@ -144,7 +165,6 @@ struct fdtd_engine_s {
         if (chunk) cudaGraphExecDestroy(chunk);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
-        if (stream) cudaStreamDestroy(stream);
     }
 };
 

@@ -113,6 +113,13 @@ namespace {
 
 // Device bytes an engine over this operator will allocate (the allocations
 // of fdtd_engine_create_compressed), rounded up per allocation.
+// sample columns of a job: one per integral probe, three per field probe
+size_t sample_columns(const Job* j) {
+    size_t cols = 0;
+    for (const fdtd_probe_desc& p : j->probes) cols += (p.type == 2 || p.type == 3) ? 3 : 1;
+    return cols;
+}
+
 uint64_t engine_footprint(const fdtd_cop_s* c, uint32_t interval, uint32_t max_ts, size_t nprobe) {
     auto r = [](uint64_t b) { return (b + (2u << 20) - 1) / (2u << 20) * (2u << 20); };
     const uint64_t F = 3ull * (uint64_t)c->comp * 4;
@@ -166,7 +173,7 @@ void build_one(fdtd_server_s* s, Job* j) {
     j->nodes = (uint64_t)cop->N[0] * cop->N[1] * cop->N[2];
     for (int a = 0; a < 3; ++a) j->N[a] = cop->N[a];
     j->dT = cop->dT;
-    j->footprint = engine_footprint(cop, j->interval, j->max_ts, j->probes.size());
+    j->footprint = engine_footprint(cop, j->interval, j->max_ts, sample_columns(j));
     if (j->footprint > s->budget || (j->opts.end_crit > 0 && j->interval == 0)) {
         j->state = FDTD_JOB_FAILED;
         j->error = FDTD_ERR_ARG;
@@ -208,7 +215,7 @@ void retire(fdtd_server_s* s, Job* j, int err, const std::string& msg) {
     if (rc == FDTD_OK) rc = fdtd_engine_num_timesteps(j->eng, &ts);
     if (rc == FDTD_OK) rc = fdtd_engine_num_samples(j->eng, &n);
     std::vector<uint32_t> sts(n);
-    std::vector<double> se(n), sv((size_t)n * j->probes.size());
+    std::vector<double> se(n), sv((size_t)n * sample_columns(j));
     if (rc == FDTD_OK && n) rc = fdtd_engine_read_samples(j->eng, 0, n, sts.data(), sv.data(), se.data());
     std::vector<float> V, I;
     if (rc == FDTD_OK && j->opts.keep_fields) {
@@ -578,9 +585,7 @@ int fdtd_server_job_status(fdtd_server_t s, uint64_t id, fdtd_job_status* st) {
     st->error = j->error;
     st->timesteps = j->ts;
     st->num_samples = (uint32_t)j->s_ts.size();
-    uint32_t cols = 0;  // sample columns: one per integral probe, three per field probe
-    for (const fdtd_probe_desc& p : j->probes) cols += (p.type == 2 || p.type == 3) ? 3u : 1u;
-    st->num_probes = cols;
+    st->num_probes = (uint32_t)sample_columns(j);
     st->nodes = j->nodes;
     for (int a = 0; a < 3; ++a) st->num_lines[a] = j->N[a];
     st->dT = j->dT;
@@ -632,7 +637,7 @@ int fdtd_server_read_samples(fdtd_server_t s, uint64_t id, uint32_t* ts, double*
     const size_t n = j->s_ts.size();
     if (ts) std::copy(j->s_ts.begin(), j->s_ts.end(), ts);
     if (energy) std::copy(j->s_energy.begin(), j->s_energy.end(), energy);
-    if (vals) std::copy(j->s_vals.begin(), j->s_vals.begin() + n * j->probes.size(), vals);
+    if (vals) std::copy(j->s_vals.begin(), j->s_vals.begin() + n * sample_columns(j), vals);
     return FDTD_OK;
 }
 
