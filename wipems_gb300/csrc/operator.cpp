@@ -315,6 +315,24 @@ void parallel_for(uint32_t n, int threads, F&& f) {
 
 // The full operator build state (the members of Operator used during
 // CalcECOperator).
+// Effective material of the edges inside one UPML slab, kept from the EC
+// pass for the UPML build (which needs the same AverageMatQuarterCell values:
+// eff[0], eff[1], eff[2] per edge direction), so it is evaluated once.
+struct SlabEff {
+    uint32_t start[3], nl[3];
+    std::vector<double> v;  // [3 directions][nl0][nl1][nl2][3]
+    bool holds(const uint32_t* pos) const {
+        for (int a = 0; a < 3; ++a)
+            if (pos[a] < start[a] || pos[a] >= start[a] + nl[a]) return false;
+        return true;
+    }
+    size_t at(int n, const uint32_t* pos) const {
+        const size_t nloc = (size_t)nl[0] * nl[1] * nl[2];
+        const size_t li = ((size_t)(pos[0] - start[0]) * nl[1] + (pos[1] - start[1])) * nl[2] + (pos[2] - start[2]);
+        return 3 * ((size_t)n * nloc + li);
+    }
+};
+
 struct Builder {
     const fdtd_scene_s& S;
     Geo g;
@@ -469,17 +487,25 @@ struct Builder {
         return true;
     }
 
-    bool calc_ec() {  // Operator::Calc_EC_Range over all lines
+    // Operator::Calc_EC_Range over all lines; the effective materials of
+    // edges inside the given UPML slabs are kept in them (slabs do not overlap)
+    bool calc_ec(std::vector<SlabEff>* slabs = nullptr) {
         EC_C.assign(3 * NN, 0.f);
         EC_G.assign(3 * NN, 0.f);
         EC_L.assign(3 * NN, 0.f);
         EC_R.assign(3 * NN, 0.f);
+        if (slabs)
+            for (SlabEff& se : *slabs) se.v.assign(9 * (size_t)se.nl[0] * se.nl[1] * se.nl[2], 0.0);
         std::atomic<bool> ok{true};
         parallel_for(N[0], threads, [&](uint32_t x, int) {
             uint32_t pos[3] = {x, 0, 0};
             double ec[4], eff[4];
             for (pos[1] = 0; pos[1] < N[1]; ++pos[1])
-                for (pos[2] = 0; pos[2] < N[2]; ++pos[2])
+                for (pos[2] = 0; pos[2] < N[2]; ++pos[2]) {
+                    SlabEff* keep = nullptr;
+                    if (slabs)
+                        for (SlabEff& se : *slabs)
+                            if (se.holds(pos)) keep = &se;
                     for (int n = 0; n < 3; ++n) {
                         if (!calc_ec_pos(n, pos, ec, eff)) {
                             ok = false;
@@ -490,7 +516,14 @@ struct Builder {
                         EC_G[i] = (float)ec[1];
                         EC_L[i] = (float)ec[2];
                         EC_R[i] = (float)ec[3];
+                        if (keep) {
+                            double* d = &keep->v[keep->at(n, pos)];
+                            d[0] = eff[0];
+                            d[1] = eff[1];
+                            d[2] = eff[2];
+                        }
                     }
+                }
         });
         if (!ok) set_error("an effective material parameter is NaN or Inf (AverageMatQuarterCell)");
         return ok;
@@ -927,7 +960,17 @@ static int build_operator(const fdtd_scene_s& S, int threads, fdtd_operator_s& o
     B.pec_idx.build(S.prims, is_mat_or_metal, B.g);
     B.exc_idx.build(S.prims, is_excitation, B.g);
 
-    if (!B.calc_ec()) return FDTD_ERR_ARG;
+    // the UPML slabs (operator_ext_upml.cpp:77-255) depend only on the grid and
+    // the boundary settings; their edges' effective materials come out of the
+    // EC pass
+    std::vector<UpmlBuild> ub = create_upml(B.N, S.bc, S.pml_size);
+    std::vector<SlabEff> slab_eff(ub.size());
+    for (size_t k = 0; k < ub.size(); ++k)
+        for (int a = 0; a < 3; ++a) {
+            slab_eff[k].start[a] = ub[k].start[a];
+            slab_eff[k].nl[a] = ub[k].nl[a];
+        }
+    if (!B.calc_ec(&slab_eff)) return FDTD_ERR_ARG;
 
     // CalcTimestep (Var3, the default method 3, operator.cpp:52)
     B.dT = B.calc_timestep_var3();
@@ -1021,10 +1064,31 @@ static int build_operator(const fdtd_scene_s& S, int threads, fdtd_operator_s& o
     }
 
     // ---- extensions 2..7: UPML slabs (operator_ext_upml.cpp:365-466)
-    std::vector<UpmlBuild> ub = create_upml(N, S.bc, S.pml_size);
-    // the grading of each axis depends only on (axis, line, n==ny); the
-    // evaluation below calls grading_kappa per (n, pos) as the reference does
-    for (const UpmlBuild& u : ub) {
+    // CalcGradingKappa's value on axis a depends only on (a, the line on a,
+    // whether a is the edge direction) and on the boundary settings every
+    // slab shares: tabulate it once per line with the same function, then
+    // look it up per edge
+    struct GradK {
+        double kv, ki;
+    };
+    std::vector<GradK> gtab[3][2];
+    if (!ub.empty()) {
+        for (int a = 0; a < 3; ++a)
+            for (int same = 0; same < 2; ++same) {
+                gtab[a][same].resize(N[a]);
+                parallel_for(N[a], threads, [&](uint32_t p, int) {
+                    uint32_t pos[3] = {0, 0, 0};
+                    pos[a] = p;
+                    const int ny = same ? a : (a + 1) % 3;
+                    double kv[3] = {0, 0, 0}, ki[3] = {0, 0, 0};
+                    grading_kappa(g, ub[0], ny, pos, kZ0, kv, ki);
+                    gtab[a][same][p] = GradK{kv[a], ki[a]};
+                });
+            }
+    }
+    for (size_t slab_k = 0; slab_k < ub.size(); ++slab_k) {
+        const UpmlBuild& u = ub[slab_k];
+        const SlabEff& se = slab_eff[slab_k];
         UpmlSlab slab;
         size_t nloc = (size_t)u.nl[0] * u.nl[1] * u.nl[2];
         for (int n = 0; n < 3; ++n) { slab.start[n] = u.start[n]; slab.num_lines[n] = u.nl[n]; }
@@ -1040,8 +1104,15 @@ static int build_operator(const fdtd_scene_s& S, int threads, fdtd_operator_s& o
                 for (loc[2] = 0; loc[2] < u.nl[2]; ++loc[2]) {
                     pos[2] = loc[2] + u.start[2];
                     for (int n = 0; n < 3; ++n) {
-                        B.avg_quarter_cell(n, pos, eff);
-                        grading_kappa(g, u, n, pos, kZ0, kv, ki);
+                        const double* ke = &se.v[se.at(n, pos)];  // AverageMatQuarterCell of the EC pass
+                        eff[0] = ke[0];
+                        eff[1] = ke[1];
+                        eff[2] = ke[2];
+                        for (int a = 0; a < 3; ++a) {  // grading_kappa(g, u, n, pos, kZ0, kv, ki)
+                            const GradK& gk = gtab[a][a == n ? 1 : 0][pos[a]];
+                            kv[a] = gk.kv;
+                            ki[a] = gk.ki;
+                        }
                         int nP = (n + 1) % 3, nPP = (n + 2) % 3;
                         size_t li = (size_t)n * nloc + ((size_t)loc[0] * u.nl[1] + loc[1]) * u.nl[2] + loc[2];
                         size_t gi = B.at(n, pos);
