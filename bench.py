@@ -162,6 +162,18 @@ def cpu_baseline(op, threads: int, target_s: float = 12.0):
     return mcs, n, r["seconds"]
 
 
+def max_over_ranks(vals, device):
+    """The slowest rank's figures: elementwise max over all ranks of a list
+    of floats (unchanged with one rank)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [float(v) for v in vals]
+    t = torch.tensor([float(v) for v in vals], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -234,10 +246,7 @@ def run_gpu(args, rank, world, local_rank):
     if dist:
         dist.barrier()
     dev_s = ms_total / 1e3
-    if dist:
-        t = torch.tensor([dev_s, wall], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_s, wall = float(t[0]), float(t[1])
+    dev_s, wall = max_over_ranks([dev_s, wall], "cuda")
     value = nodes * TIMESTEPS * args.steps * world / dev_s / 1e6
 
     # live per-kernel durations (events around each launch)
