@@ -20,7 +20,7 @@ INCLUDE = PKG.parent / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-fmad=false", "-Xptxas", "-v"]
-CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread", "-I/usr/local/cuda/include"]
+CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread", "-I/usr/local/cuda/include"]
 
 CU_SOURCES = ["engine.cu", "energy_static.cu", "batch.cu"]
 CXX_SOURCES = ["operator.cpp", "compress.cpp", "server.cpp", "xml_scene.cpp"]
