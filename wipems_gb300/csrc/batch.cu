@@ -60,11 +60,11 @@ struct Group {
 
 template <typename IdxT, int FEAT, bool GEO>
 void volt_batch_launch(const Group& G, const BatchJob* jobs, int XC, int S, cudaStream_t st) {
-    k_volt_batch<IdxT, FEAT, GEO><<<G.gridE, dim3(32, TMA_TY), G.smemE, st>>>(jobs, G.itE.p, G.nE, XC, S);
+    k_volt_batch<IdxT, FEAT, GEO><<<G.gridE, dim3(32, BATCH_TY), G.smemE, st>>>(jobs, G.itE.p, G.nE, XC, S);
 }
 template <typename IdxT, int FEAT, bool GEO>
 void curr_batch_launch(const Group& G, const BatchJob* jobs, int XC, int S, cudaStream_t st) {
-    k_curr_batch<IdxT, FEAT, GEO><<<G.gridH, dim3(32, TMA_TY), G.smemH, st>>>(jobs, G.itH.p, G.nH, XC, S);
+    k_curr_batch<IdxT, FEAT, GEO><<<G.gridH, dim3(32, BATCH_TY), G.smemH, st>>>(jobs, G.itH.p, G.nH, XC, S);
 }
 
 template <typename IdxT, bool GEO>
@@ -110,9 +110,9 @@ template <typename IdxT, int FEAT, bool GEO>
 int occ_one(bool volt, size_t smem) {
     int n = 0;
     if (volt)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_volt_batch<IdxT, FEAT, GEO>, 32 * TMA_TY, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_volt_batch<IdxT, FEAT, GEO>, 32 * BATCH_TY, smem);
     else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_curr_batch<IdxT, FEAT, GEO>, 32 * TMA_TY, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_curr_batch<IdxT, FEAT, GEO>, 32 * BATCH_TY, smem);
     return n;
 }
 template <typename IdxT, bool GEO>
@@ -174,13 +174,15 @@ int batch_refusal(const fdtd_engine_s* e) {
     return FDTD_OK;
 }
 
-size_t stage_smem(bool i16, bool upml, bool ade, int S) {
+size_t stage_smem(bool i16, bool upml, bool ade, int S) {  // the batched kernels' BATCH_TY-row stages
+    constexpr int T = BATCH_TY;
     if (ade) {  // voltage kernels of groups with Lorentz/Drude nodes stage their states too
-        if (i16) return upml ? StageLayout<uint16_t, true, true>::smem(S) : StageLayout<uint16_t, false, true>::smem(S);
-        return upml ? StageLayout<uint32_t, true, true>::smem(S) : StageLayout<uint32_t, false, true>::smem(S);
+        if (i16)
+            return upml ? StageLayout<uint16_t, true, true, T>::smem(S) : StageLayout<uint16_t, false, true, T>::smem(S);
+        return upml ? StageLayout<uint32_t, true, true, T>::smem(S) : StageLayout<uint32_t, false, true, T>::smem(S);
     }
-    if (i16) return upml ? StageLayout<uint16_t, true>::smem(S) : StageLayout<uint16_t, false>::smem(S);
-    return upml ? StageLayout<uint32_t, true>::smem(S) : StageLayout<uint32_t, false>::smem(S);
+    if (i16) return upml ? StageLayout<uint16_t, true, false, T>::smem(S) : StageLayout<uint16_t, false, false, T>::smem(S);
+    return upml ? StageLayout<uint32_t, true, false, T>::smem(S) : StageLayout<uint32_t, false, false, T>::smem(S);
 }
 
 }  // namespace
@@ -364,8 +366,9 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
         b->bins.push_back(std::move(B));
     }
     // descriptors
-    std::vector<TmaMaps> hmaps(n);
-    for (uint32_t j = 0; j < n; ++j) hmaps[j] = b->jobs[j]->maps;
+    std::vector<TmaMaps> hmaps(n);  // the jobs' tensor maps for the batch's BATCH_TY-row tiles
+    for (uint32_t j = 0; j < n; ++j)
+        if ((rc = engine_tma_maps(b->jobs[j], &hmaps[j], BATCH_TY))) return rc;
     if ((rc = b->d_maps.alloc(n, b->device_bytes)) || (rc = b->d_jobs.alloc(n, b->device_bytes)) ||
         (rc = b->d_adv.alloc(n, b->device_bytes)) || (rc = b->d_status.alloc(4 * (size_t)n, b->device_bytes)))
         return rc;
@@ -399,7 +402,7 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
     if (b->XC == 0) {
         std::vector<const uint32_t*> lines;
         for (const fdtd_engine_s* e : b->jobs) lines.push_back(e->N);
-        b->XC = auto_x_chunk(lines, (uint64_t)WIPEMS_BATCH_MIN_BLOCKS * (uint64_t)sms);
+        b->XC = auto_x_chunk(lines, (uint64_t)WIPEMS_BATCH_MIN_BLOCKS * (uint64_t)sms, BATCH_TY);
     }
     const size_t maxsm = stage_smem(false, true, true, b->stages);
     if (maxsm > 48 * 1024 && (rc = batch_smem_attrs((int)maxsm))) return rc;
@@ -407,12 +410,12 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
         std::vector<WorkItem> wE, wH;
         for (int j : G.jobs) {
             const fdtd_engine_s* e = b->jobs[j];
-            const int bxE = (e->ti.ne[2] + 31) / 32, byE = (e->ti.ne[1] + TMA_TY - 1) / TMA_TY,
+            const int bxE = (e->ti.ne[2] + 31) / 32, byE = (e->ti.ne[1] + BATCH_TY - 1) / BATCH_TY,
                       bzE = (e->ti.ne[0] + b->XC - 1) / b->XC;
             for (int z = 0; z < bzE; ++z)
                 for (int y = 0; y < byE; ++y)
                     for (int x = 0; x < bxE; ++x) wE.push_back(WorkItem{j, x, y, z});
-            const int bxH = ((int)e->N[2] - 1 + 31) / 32, byH = ((int)e->N[1] - 1 + TMA_TY - 1) / TMA_TY,
+            const int bxH = ((int)e->N[2] - 1 + 31) / 32, byH = ((int)e->N[1] - 1 + BATCH_TY - 1) / BATCH_TY,
                       bzH = ((int)e->N[0] - 1 + b->XC - 1) / b->XC;
             for (int z = 0; z < bzH; ++z)
                 for (int y = 0; y < byH; ++y)

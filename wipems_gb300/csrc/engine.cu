@@ -424,22 +424,23 @@ int set_fused_attrs(int bytes) {
     return FDTD_OK;
 }
 
-int make_maps(fdtd_engine_s* e) {
+// the two-pass kernels' tensor maps for tiles of `rows` y rows
+int make_tma_maps(const fdtd_engine_s* e, TmaMaps* m, uint32_t rows) {
     int rc;
-    if ((rc = field_map(&e->maps.I_halo, e->I.p, e, 36, TMA_TY + 1)) ||
-        (rc = field_map(&e->maps.I_own, e->I.p, e, 32, TMA_TY)) ||
-        (rc = field_map(&e->maps.V_halo, e->V.p, e, 36, TMA_TY + 1)) ||
-        (rc = field_map(&e->maps.V_own, e->V.p, e, 32, TMA_TY)) ||
-        (rc = index_map(&e->maps.idxE, e->E.idx.p, e, e->E.idx16)) ||
-        (rc = index_map(&e->maps.idxH, e->H.idx.p, e, e->H.idx16)))
+    if ((rc = field_map(&m->I_halo, e->I.p, e, 36, rows + 1)) || (rc = field_map(&m->I_own, e->I.p, e, 32, rows)) ||
+        (rc = field_map(&m->V_halo, e->V.p, e, 36, rows + 1)) || (rc = field_map(&m->V_own, e->V.p, e, 32, rows)) ||
+        (rc = index_map(&m->idxE, e->E.idx.p, e, e->E.idx16, 32, rows)) ||
+        (rc = index_map(&m->idxH, e->H.idx.p, e, e->H.idx16, 32, rows)))
         return rc;
-    if (e->FV.p && ((rc = field_map(&e->maps.FV_own, e->FV.p, e, 32, TMA_TY)) ||
-                    (rc = field_map(&e->maps.FI_own, e->FI.p, e, 32, TMA_TY))))
+    if (e->FV.p && ((rc = field_map(&m->FV_own, e->FV.p, e, 32, rows)) ||
+                    (rc = field_map(&m->FI_own, e->FI.p, e, 32, rows))))
         return rc;
-    if (e->AV.p && (rc = field_map(&e->maps.AV_own, e->AV.p, e, 32, TMA_TY))) return rc;
-    if (e->LV.p && (rc = field_map(&e->maps.LV_own, e->LV.p, e, 32, TMA_TY))) return rc;
+    if (e->AV.p && (rc = field_map(&m->AV_own, e->AV.p, e, 32, rows))) return rc;
+    if (e->LV.p && (rc = field_map(&m->LV_own, e->LV.p, e, 32, rows))) return rc;
     return FDTD_OK;
 }
+
+int make_maps(fdtd_engine_s* e) { return make_tma_maps(e, &e->maps, TMA_TY); }
 
 template <typename IdxT, int FEAT, bool GEO>
 cudaError_t smem_attr_one(int bytes) {
@@ -564,7 +565,8 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     if (e->XC == 0) {
         int sms = 0;
         CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->device));
-        e->XC = auto_x_chunk({e->N}, 5ull * (uint64_t)sms);  // about 5 resident blocks per SM
+        // about 1280 resident threads per SM (5 blocks of 32 x 8, 10 of 32 x 4)
+        e->XC = auto_x_chunk({e->N}, (uint64_t)(1280 / (32 * TMA_TY)) * (uint64_t)sms);
     }
     e->comp = c->comp;
     e->geo_on = c->geo;
@@ -826,6 +828,7 @@ int probe_entries(const fdtd_engine_s* e, const fdtd_probe_desc* p, std::vector<
 }  // namespace
 
 int engine_start(fdtd_engine_s* e) { return start(e); }
+int engine_tma_maps(const fdtd_engine_s* e, TmaMaps* out, uint32_t rows) { return make_tma_maps(e, out, rows); }
 int engine_check_errors(fdtd_engine_s* e) { return check_error_word(e); }
 int engine_decode_error(int err) { return decode_error(err); }
 

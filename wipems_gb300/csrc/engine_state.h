@@ -176,13 +176,13 @@ namespace wipems {
 // so the step costs ceil(blocks / resident) * (2 + x_chunk); a chunk that
 // leaves SMs idle in the only wave is skipped, ties go to the longer chunk
 // (fewer halo-plane re-reads).  lines: the jobs' (Nx, Ny, Nz) triples.
-inline int auto_x_chunk(const std::vector<const uint32_t*>& lines, uint64_t resident) {
+inline int auto_x_chunk(const std::vector<const uint32_t*>& lines, uint64_t resident, int ty = TMA_TY) {
     int best = 1;
     uint64_t best_cost = ~0ull;
     for (int xc = 16; xc >= 1; xc /= 2) {
         uint64_t items = 0;
         for (const uint32_t* N : lines)
-            items += (uint64_t)((N[2] - 1 + 31) / 32) * ((N[1] - 1 + TMA_TY - 1) / TMA_TY) * ((N[0] - 1 + xc - 1) / xc);
+            items += (uint64_t)((N[2] - 1 + 31) / 32) * ((N[1] - 1 + ty - 1) / ty) * ((N[0] - 1 + xc - 1) / xc);
         if (items < resident && xc > 1) continue;
         const uint64_t cost = (items + resident - 1) / resident * (uint64_t)(2 + xc);
         if (cost < best_cost) {
@@ -195,6 +195,7 @@ inline int auto_x_chunk(const std::vector<const uint32_t*>& lines, uint64_t resi
 
 // engine.cu helpers used by the batched path
 int engine_start(fdtd_engine_s* e);        // upload probes, graph, ts = 0 sample
+int engine_tma_maps(const fdtd_engine_s* e, TmaMaps* out, uint32_t rows);  // tensor maps for rows-high tiles
 int engine_check_errors(fdtd_engine_s* e); // read the control words, decode errors
 int engine_decode_error(int err);          // error word -> status code + message
 }  // namespace wipems

@@ -36,16 +36,22 @@
 
 namespace wipems {
 
-// minimum resident blocks per SM the batched kernels are compiled for
-// (caps their registers at 64: the per-job descriptor fields they read from
-// global memory cost registers that the single-job kernels take from
-// constant memory)
-#ifndef WIPEMS_BATCH_MIN_BLOCKS
-#define WIPEMS_BATCH_MIN_BLOCKS 4
-#endif
-
 constexpr int TMA_MAX_STAGES = 8;
-constexpr int TMA_TY = 8;
+// tile rows (y) per block.  Single jobs: 32 (z) x 4 tiles of 128 threads,
+// measured faster than 32 x 8 (L256 272.6 vs 277.8 us per step, D192 210.8
+// vs 218) and than 32 x 2 (321 us: the y halo row costs half a tile).
+// Batches: 32 x 8 -- a persistent block pays a ring prologue per work item,
+// and with half-size items the B96 batch fell from 44.7 to 33.8 G.
+constexpr int TMA_TY = 4;
+constexpr int BATCH_TY = 8;
+
+// minimum resident blocks per SM the batched kernels are compiled for:
+// 1024 threads per SM, which caps their registers at 64 (the per-job
+// descriptor fields they read from global memory cost registers that the
+// single-job kernels take from constant memory)
+#ifndef WIPEMS_BATCH_MIN_BLOCKS
+#define WIPEMS_BATCH_MIN_BLOCKS (1024 / (32 * BATCH_TY))
+#endif
 constexpr unsigned long long TMA_WAIT_CYCLES = 4000000000ull;  // ~2 s at 2 GHz
 
 struct TmaMaps {
@@ -126,13 +132,13 @@ __device__ __forceinline__ void tensormap_acquire(const TmaMaps* m) {
 
 // stage layout (floats, every buffer 128-byte aligned); ADE adds the two
 // Lorentz/Drude state boxes (voltage kernel only)
-template <typename IdxT, bool UPML, bool ADE = false>
+template <typename IdxT, bool UPML, bool ADE = false, int TY = TMA_TY>
 struct StageLayout {
     static constexpr int HW = 36;                               // halo box row width
-    static constexpr int HALO = 3 * (TMA_TY + 1) * HW;          // halo box, 3 components
+    static constexpr int HALO = 3 * (TY + 1) * HW;          // halo box, 3 components
     static constexpr int HALO_A = (HALO + 31) / 32 * 32;
-    static constexpr int OWN = 3 * TMA_TY * 32;                  // own box, 3 components
-    static constexpr int IDX = TMA_TY * 32 * (int)sizeof(IdxT) / 4;
+    static constexpr int OWN = 3 * TY * 32;                  // own box, 3 components
+    static constexpr int IDX = TY * 32 * (int)sizeof(IdxT) / 4;
     static constexpr int IDX_A = (IDX + 31) / 32 * 32;
     static constexpr int FLUX = UPML ? OWN : 0;
     static constexpr int OFF_FLUX = HALO_A + OWN + IDX_A;
@@ -140,7 +146,7 @@ struct StageLayout {
     static constexpr int STAGE = OFF_ADE + (ADE ? 2 * OWN : 0);  // floats
     static constexpr int HALO_BYTES = HALO * 4;
     static constexpr int OWN_BYTES = OWN * 4;
-    static constexpr int IDX_BYTES = TMA_TY * 32 * (int)sizeof(IdxT);
+    static constexpr int IDX_BYTES = TY * 32 * (int)sizeof(IdxT);
     // + barriers + slack to align the dynamic shared memory base to 128 bytes
     static size_t smem(int stages) { return (size_t)STAGE * 4 * stages + 8 * TMA_MAX_STAGES + 128; }
 };
@@ -160,29 +166,38 @@ __device__ __forceinline__ bool tile_has_upml(const TileInfo& ti, int x, int y0,
 // block).  Returns false if a bounded wait gave up.
 // per (x, y-tile, z-tile) Lorentz/Drude flags of the voltage kernel's tiles:
 // bit 0 = an ADE node, bit 1 = a Lorentz node in that tile plane
+// (the array has TMA_TY-row granularity; a TY-row tile ORs the rows it spans)
+template <int TY>
 __device__ __forceinline__ uint32_t ade_tile_flags(const DevGrid& g, int x, int bx, int by) {
+    if (!g.ade_tile) return 0u;
     const int ZT = (g.Nz + 31) / 32, YT = (g.Ny + TMA_TY - 1) / TMA_TY;
-    return g.ade_tile ? (uint32_t)__ldg(g.ade_tile + ((long long)x * YT + by) * ZT + bx) : 0u;
+    uint32_t f = 0u;
+#pragma unroll
+    for (int k = 0; k < TY / TMA_TY; ++k) {
+        const int r = by * (TY / TMA_TY) + k;
+        if (r < YT) f |= (uint32_t)__ldg(g.ade_tile + ((long long)x * YT + r) * ZT + bx);
+    }
+    return f;
 }
 
-template <typename IdxT, int FEAT, bool GEO>
+template <typename IdxT, int FEAT, bool GEO, int TY = TMA_TY>
 __device__ __forceinline__ bool volt_tile(const DevGrid& g, const TmaMaps& m, const TileInfo& ti, int bx, int by,
                                           int bz, int XC, int STAGES, float* smem, uint64_t* bars, uint32_t& ring,
                                           int numTS) {
     constexpr bool UPML = (FEAT & FEAT_UPML) != 0;
     constexpr bool ADE = (FEAT & FEAT_ADE) != 0;
-    using L = StageLayout<IdxT, UPML, ADE>;
+    using L = StageLayout<IdxT, UPML, ADE, TY>;
     constexpr int HW = L::HW;
     const int tz = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * 32 + tz;
-    const int z0 = bx * 32, y0 = by * TMA_TY;
+    const int z0 = bx * 32, y0 = by * TY;
     const int z = z0 + tz, y = y0 + ty;
     const int x0 = bz * XC;
     const int x1 = min(x0 + XC, ti.ne[0]);
     const int nplanes = x1 - x0;
     const bool valid = (y < ti.ne[1]) && (z < ti.ne[2]);
     const long long C = g.comp;
-    const int zl = min(z0 + 31, g.Nz - 1), yl = min(y0 + TMA_TY - 1, g.Ny - 1);
+    const int zl = min(z0 + 31, g.Nz - 1), yl = min(y0 + TY - 1, g.Ny - 1);
     const uint32_t base = ring;
 
     auto issue = [&](int r) {  // thread 0: plane x0+r into the ring
@@ -191,7 +206,7 @@ __device__ __forceinline__ bool volt_tile(const DevGrid& g, const TmaMaps& m, co
         const int x = x0 + r;
         float* st = smem + (size_t)s * L::STAGE;
         const bool up = UPML && tile_has_upml(ti, x, y0, yl, z0, zl);
-        const uint32_t af = ADE ? ade_tile_flags(g, x, bx, by) : 0u;
+        const uint32_t af = ADE ? ade_tile_flags<TY>(g, x, bx, by) : 0u;
         const uint32_t bytes = L::HALO_BYTES + L::OWN_BYTES + L::IDX_BYTES + (up ? L::OWN_BYTES : 0) +
                                ((af & 1u) ? L::OWN_BYTES : 0) + ((af & 2u) ? L::OWN_BYTES : 0);
         mbar_expect_tx(&bars[s], bytes);
@@ -242,8 +257,8 @@ __device__ __forceinline__ bool volt_tile(const DevGrid& g, const TmaMaps& m, co
         if (ok && valid) {
             const int hi = (ty + 1) * HW + 4 + tz;  // own position in the halo box
             const float* sI0 = st;
-            const float* sI1 = st + (TMA_TY + 1) * HW;
-            const float* sI2 = st + 2 * (TMA_TY + 1) * HW;
+            const float* sI1 = st + (TY + 1) * HW;
+            const float* sI2 = st + 2 * (TY + 1) * HW;
             const float c0 = sI0[hi];
             c1 = sI1[hi];
             c2 = sI2[hi];
@@ -262,10 +277,10 @@ __device__ __forceinline__ bool volt_tile(const DevGrid& g, const TmaMaps& m, co
             const uint32_t t = (uint32_t)reinterpret_cast<const IdxT*>(st + L::HALO_A + L::OWN)[oi];
             const bool up = UPML && tile_has_upml(ti, x, y0, yl, z0, zl);
             const float* sF = up ? st + L::OFF_FLUX + oi : nullptr;
-            const uint32_t af = ADE ? ade_tile_flags(g, x, bx, by) : 0u;
+            const uint32_t af = ADE ? ade_tile_flags<TY>(g, x, bx, by) : 0u;
             const float* sA = (af & 1u) ? st + L::OFF_ADE + oi : nullptr;
             const float* sL = (af & 2u) ? st + L::OFF_ADE + L::OWN + oi : nullptr;
-            float v[3] = {sV[oi], sV[TMA_TY * 32 + oi], sV[2 * TMA_TY * 32 + oi]};
+            float v[3] = {sV[oi], sV[TY * 32 + oi], sV[2 * TY * 32 + oi]};
             GeoF gf;
             if (GEO) {
                 const float gxE = __ldg(g.geo + x), gxI = __ldg(g.geo + g.geo_stride + x);
@@ -273,7 +288,7 @@ __device__ __forceinline__ bool volt_tile(const DevGrid& g, const TmaMaps& m, co
                 gf.f[1][0] = gyE; gf.f[1][1] = gzI; gf.f[1][2] = gxI;
                 gf.f[2][0] = gzE; gf.f[2][1] = gxI; gf.f[2][2] = gyI;
             }
-            update_node<false, FEAT, GEO>(g, v, curl, t, (long long)x * g.sx + yz, numTS, sF, TMA_TY * 32, gf,
+            update_node<false, FEAT, GEO>(g, v, curl, t, (long long)x * g.sx + yz, numTS, sF, TY * 32, gf,
                                           nullptr, true, sA, sL);
             Vp[0] = v[0];
             Vp[C] = v[1];
@@ -301,16 +316,16 @@ __device__ __forceinline__ bool volt_tile(const DevGrid& g, const TmaMaps& m, co
 // ------------------------------------------------------------- H half-step
 // One tile of the current update (see volt_tile).  es/ec/hs/hc: the
 // thread's Kahan sums of V^2 and I^2, accumulated when energy is set.
-template <typename IdxT, int FEAT, bool GEO>
+template <typename IdxT, int FEAT, bool GEO, int TY = TMA_TY>
 __device__ __forceinline__ bool curr_tile(const DevGrid& g, const TmaMaps& m, const TileInfo& ti, int bx, int by,
                                           int bz, int XC, int STAGES, float* smem, uint64_t* bars, uint32_t& ring,
                                           int numTS, bool energy, float& es, float& ec, float& hs, float& hc) {
     constexpr bool UPML = (FEAT & FEAT_UPML) != 0;
-    using L = StageLayout<IdxT, UPML>;
+    using L = StageLayout<IdxT, UPML, false, TY>;
     constexpr int HW = L::HW;
     const int tz = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * 32 + tz;
-    const int z0 = bx * 32, y0 = by * TMA_TY;
+    const int z0 = bx * 32, y0 = by * TY;
     const int z = z0 + tz, y = y0 + ty;
     const int x0 = bz * XC;
     const int x1 = min(x0 + XC, g.Nx - 1);
@@ -318,7 +333,7 @@ __device__ __forceinline__ bool curr_tile(const DevGrid& g, const TmaMaps& m, co
     const int nload = nplanes + 1;    // plane x1 is read as the x+1 neighbour
     const bool active = (z < g.Nz - 1) && (y < g.Ny - 1);
     const long long C = g.comp;
-    const int zl = min(z0 + 31, g.Nz - 1), yl = min(y0 + TMA_TY - 1, g.Ny - 1);
+    const int zl = min(z0 + 31, g.Nz - 1), yl = min(y0 + TY - 1, g.Ny - 1);
     const uint32_t base = ring;
 
     auto issue = [&](int r) {
@@ -372,12 +387,12 @@ __device__ __forceinline__ bool curr_tile(const DevGrid& g, const TmaMaps& m, co
             const float* st = smem + (size_t)s * L::STAGE;
             const float* stn = smem + (size_t)sn * L::STAGE;
             const float* sV0 = st;
-            const float* sV1 = st + (TMA_TY + 1) * HW;
-            const float* sV2 = st + 2 * (TMA_TY + 1) * HW;
+            const float* sV1 = st + (TY + 1) * HW;
+            const float* sV2 = st + 2 * (TY + 1) * HW;
             const int hi = ty * HW + tz;
             const float c0 = sV0[hi], c1 = sV1[hi], c2 = sV2[hi];
-            const float n1 = stn[(TMA_TY + 1) * HW + hi];
-            const float n2 = stn[2 * (TMA_TY + 1) * HW + hi];
+            const float n1 = stn[(TY + 1) * HW + hi];
+            const float n2 = stn[2 * (TY + 1) * HW + hi];
             float curl[3];
             curl[0] = __fadd_rn(__fsub_rn(__fsub_rn(c2, sV2[hi + HW]), c1), sV1[hi + 1]);
             curl[1] = __fadd_rn(__fsub_rn(__fsub_rn(c0, sV0[hi + 1]), c2), n2);
@@ -387,7 +402,7 @@ __device__ __forceinline__ bool curr_tile(const DevGrid& g, const TmaMaps& m, co
             const uint32_t t = (uint32_t)reinterpret_cast<const IdxT*>(st + L::HALO_A + L::OWN)[oi];
             const bool up = UPML && tile_has_upml(ti, x, y0, yl, z0, zl);
             const float* sF = up ? st + L::OFF_FLUX + oi : nullptr;
-            float cu[3] = {sI[oi], sI[TMA_TY * 32 + oi], sI[2 * TMA_TY * 32 + oi]};
+            float cu[3] = {sI[oi], sI[TY * 32 + oi], sI[2 * TY * 32 + oi]};
             GeoF gf;
             if (GEO) {
                 const int S = g.geo_stride;
@@ -396,7 +411,7 @@ __device__ __forceinline__ bool curr_tile(const DevGrid& g, const TmaMaps& m, co
                 gf.f[1][0] = gyE; gf.f[1][1] = gzI; gf.f[1][2] = gxI;
                 gf.f[2][0] = gzE; gf.f[2][1] = gxI; gf.f[2][2] = gyI;
             }
-            update_node<true, FEAT, GEO>(g, cu, curl, t, (long long)x * g.sx + yz, numTS, sF, TMA_TY * 32, gf);
+            update_node<true, FEAT, GEO>(g, cu, curl, t, (long long)x * g.sx + yz, numTS, sF, TY * 32, gf);
             Ip[0] = cu[0];
             Ip[C] = cu[1];
             Ip[2 * C] = cu[2];
@@ -502,10 +517,10 @@ struct WorkItem {
 // takes items b, b + gridDim.x, ...  Every job's numTS is read from its own
 // counter, so jobs need not be in step.
 template <typename IdxT, int FEAT, bool GEO>
-__global__ void __launch_bounds__(TMA_TY * 32, WIPEMS_BATCH_MIN_BLOCKS) k_volt_batch(const BatchJob* __restrict__ jobs,
+__global__ void __launch_bounds__(BATCH_TY * 32, WIPEMS_BATCH_MIN_BLOCKS) k_volt_batch(const BatchJob* __restrict__ jobs,
                                                             const WorkItem* __restrict__ items, int nitems, int XC,
                                                             int STAGES) {
-    using L = StageLayout<IdxT, (FEAT & FEAT_UPML) != 0, (FEAT & FEAT_ADE) != 0>;
+    using L = StageLayout<IdxT, (FEAT & FEAT_UPML) != 0, (FEAT & FEAT_ADE) != 0, BATCH_TY>;
     extern __shared__ __align__(128) float smem_raw[];
     float* smem = aligned_smem(smem_raw);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * STAGES);
@@ -520,17 +535,17 @@ __global__ void __launch_bounds__(TMA_TY * 32, WIPEMS_BATCH_MIN_BLOCKS) k_volt_b
             if (threadIdx.x == 0 && threadIdx.y == 0) tensormap_acquire(J.maps);
             last_job = w.job;
         }
-        if (!volt_tile<IdxT, FEAT, GEO>(J.g, *J.maps, J.ti, w.bx, w.by, w.bz, XC, STAGES, smem, bars, ring,
+        if (!volt_tile<IdxT, FEAT, GEO, BATCH_TY>(J.g, *J.maps, J.ti, w.bx, w.by, w.bz, XC, STAGES, smem, bars, ring,
                                         *J.g.d_ts))
             break;
     }
 }
 
 template <typename IdxT, int FEAT, bool GEO>
-__global__ void __launch_bounds__(TMA_TY * 32, WIPEMS_BATCH_MIN_BLOCKS) k_curr_batch(const BatchJob* __restrict__ jobs,
+__global__ void __launch_bounds__(BATCH_TY * 32, WIPEMS_BATCH_MIN_BLOCKS) k_curr_batch(const BatchJob* __restrict__ jobs,
                                                             const WorkItem* __restrict__ items, int nitems, int XC,
                                                             int STAGES) {
-    using L = StageLayout<IdxT, (FEAT & FEAT_UPML) != 0>;
+    using L = StageLayout<IdxT, (FEAT & FEAT_UPML) != 0, false, BATCH_TY>;
     extern __shared__ __align__(128) float smem_raw[];
     float* smem = aligned_smem(smem_raw);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * STAGES);
@@ -549,7 +564,7 @@ __global__ void __launch_bounds__(TMA_TY * 32, WIPEMS_BATCH_MIN_BLOCKS) k_curr_b
         const int numTS = *J.g.d_ts;
         const bool energy = J.interval > 0 && ((numTS + 1) % J.interval) == 0;
         float es = 0.f, ec = 0.f, hs = 0.f, hc = 0.f;
-        const bool ok = curr_tile<IdxT, FEAT, GEO>(J.g, *J.maps, J.ti, w.bx, w.by, w.bz, XC, STAGES, smem, bars,
+        const bool ok = curr_tile<IdxT, FEAT, GEO, BATCH_TY>(J.g, *J.maps, J.ti, w.bx, w.by, w.bz, XC, STAGES, smem, bars,
                                                    ring, numTS, energy, es, ec, hs, hc);
         if (energy) flush_energy(J.g.d_eacc, es, ec, hs, hc);
         if (!ok) break;
