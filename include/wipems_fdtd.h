@@ -614,6 +614,11 @@ typedef struct {
                                      its own engine, concurrently on its own
                                      stream */
     fdtd_batch_opts batch;        /* tiling of the batched kernels */
+    uint32_t tile_share;          /* concurrent engines: each job's x-chunk is
+                                     chosen as if it had 1/tile_share of the
+                                     SMs (jobs overlap on their streams, so
+                                     longer chunks with fewer halo planes
+                                     pay); 0 = 4, 1 = the job alone */
 } fdtd_server_opts;
 
 typedef struct {

@@ -111,7 +111,7 @@ class FdtdXmlInfo(C.Structure):
 class FdtdServerOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("hbm_budget", C.c_uint64), ("max_active", u32), ("round_steps", u32),
                 ("build_workers", C.c_int), ("build_threads_per_job", C.c_int), ("batch_min_jobs", u32),
-                ("batch", FdtdBatchOpts)]
+                ("batch", FdtdBatchOpts), ("tile_share", u32)]
 
 
 class FdtdJobOpts(C.Structure):

@@ -831,6 +831,12 @@ int engine_start(fdtd_engine_s* e) { return start(e); }
 int engine_tma_maps(const fdtd_engine_s* e, TmaMaps* out, uint32_t rows) { return make_tma_maps(e, out, rows); }
 int engine_check_errors(fdtd_engine_s* e) { return check_error_word(e); }
 int engine_decode_error(int err) { return decode_error(err); }
+int engine_auto_x_chunk(const uint32_t N[3], int device, unsigned share) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms <= 0) return 0;
+    const uint64_t resident = (uint64_t)(1280 / (32 * TMA_TY)) * (uint64_t)sms / (share > 0 ? share : 1);
+    return auto_x_chunk({N}, resident > 0 ? resident : 1);
+}
 
 }  // namespace wipems
 

@@ -152,4 +152,8 @@ struct fdtd_operator_s {
 namespace wipems {
 void set_error(const std::string& msg);
 const std::string& last_error();  // this thread's last error message
+// x planes per block for a grid of N[3] lines that gets about 1/share of the
+// SMs of `device` (the wave model of the engine's automatic choice); 0 when
+// the device cannot be queried
+int engine_auto_x_chunk(const uint32_t N[3], int device, unsigned share);
 }

@@ -258,6 +258,8 @@ int admit(fdtd_server_s* s, Job* j) {
     o.kernel = 3;      // batched jobs run the two-pass kernels
     o.energy_on_probe = 1;
     o.end_crit = j->opts.end_crit;
+    // jobs overlap on their own streams: tile each for its share of the SMs
+    if (s->opts.tile_share != 1) o.x_chunk = engine_auto_x_chunk(j->N, o.device, s->opts.tile_share);
     fdtd_engine_t e = nullptr;
     int rc = fdtd_engine_create_compressed(j->cop, &o, &e);
     for (size_t p = 0; rc == FDTD_OK && p < j->probes.size(); ++p) rc = fdtd_engine_add_probe(e, &j->probes[p], nullptr);
@@ -507,6 +509,7 @@ int fdtd_server_create(const fdtd_server_opts* opts, fdtd_server_t* out) {
     fdtd_server_opts& o = s->opts;
     if (o.max_active == 0) o.max_active = 256;
     if (o.round_steps == 0) o.round_steps = 128;
+    if (o.tile_share == 0) o.tile_share = 4;
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
     // a few concurrent builds of a few threads each (measured on a 16-core
     // host: 4 builds finish the first large jobs sooner than 8 or 16 narrow

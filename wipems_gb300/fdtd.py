@@ -565,7 +565,8 @@ class Server:
 
     def __init__(self, device: int = 0, hbm_budget: int = 0, max_active: int = 0, round_steps: int = 0,
                  build_workers: int = 0, build_threads_per_job: int = 0, x_chunk: int = 0, stages: int = 0,
-                 blocks_per_sm: int = 0, graph_steps: int = 0, bin_mib: int = 0, batch_min_jobs: int = 0):
+                 blocks_per_sm: int = 0, graph_steps: int = 0, bin_mib: int = 0, batch_min_jobs: int = 0,
+                 tile_share: int = 0):
         o = _abi.FdtdServerOpts()
         o.device = device
         o.hbm_budget = int(hbm_budget)
@@ -575,6 +576,7 @@ class Server:
         o.build_threads_per_job = int(build_threads_per_job)
         o.batch_min_jobs = int(batch_min_jobs)
         o.batch = _abi.FdtdBatchOpts(int(x_chunk), int(stages), int(blocks_per_sm), int(graph_steps), int(bin_mib))
+        o.tile_share = int(tile_share)
         h = C.c_void_p()
         check(lib().fdtd_server_create(C.byref(o), C.byref(h)), "fdtd_server_create")
         self._h = h
