@@ -294,20 +294,25 @@ bool is_material(const Prim& p) { return p.kind == PK_MATERIAL; }
 bool is_mat_or_metal(const Prim& p) { return p.kind == PK_MATERIAL || p.kind == PK_METAL; }
 bool is_excitation(const Prim& p) { return p.kind == PK_EXCITATION; }
 
+// f(i, thread) for i in [0, n); the threads take `grain` consecutive
+// indices at a time (short items: fewer shared-counter round trips, and no
+// two threads writing neighbouring items' cache lines)
 template <class F>
-void parallel_for(uint32_t n, int threads, F&& f) {
+void parallel_for(uint32_t n, int threads, F&& f, uint32_t grain = 1) {
     if (threads <= 1 || n < 2) {
         for (uint32_t i = 0; i < n; ++i) f(i, 0);
         return;
     }
+    if (grain < 1) grain = 1;
     std::atomic<uint32_t> next{0};
     std::vector<std::thread> pool;
     for (int t = 0; t < threads; ++t)
         pool.emplace_back([&, t] {
             for (;;) {
-                uint32_t i = next.fetch_add(1);
-                if (i >= n) break;
-                f(i, t);
+                const uint32_t i0 = next.fetch_add(grain);
+                if (i0 >= n) break;
+                const uint32_t i1 = std::min(n, i0 + grain);
+                for (uint32_t i = i0; i < i1; ++i) f(i, t);
             }
         });
     for (auto& th : pool) th.join();
@@ -1149,7 +1154,7 @@ static int build_operator(const fdtd_scene_s& S, int threads, fdtd_operator_s& o
                     }
                 }
             }
-        });
+        }, std::max(1u, 4096u / std::max(1u, u.nl[2])));
         op.upml.push_back(std::move(slab));
     }
 
