@@ -20,7 +20,12 @@ INCLUDE = PKG.parent / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-fmad=false", "-Xptxas", "-v"]
-CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread", "-I/usr/local/cuda/include"]
+# host code: no FMA contraction (the operator's float/double expressions are
+# rounded in the reference's order); -fno-math-errno only drops the errno
+# side effect of sqrt & co. (values unchanged), which lets loops such as the
+# timestep search vectorize
+CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-math-errno", "-pthread",
+             "-I/usr/local/cuda/include"]
 
 CU_SOURCES = ["engine.cu", "energy_static.cu", "batch.cu"]
 CXX_SOURCES = ["operator.cpp", "compress.cpp", "server.cpp", "xml_scene.cpp"]

@@ -549,61 +549,119 @@ struct Builder {
     // Operator::CalcTimestep_Var3 (operator.cpp:1897-1971).  The terms are
     // evaluated as the reference does: float products / reciprocals of the
     // float EC arrays, accumulated into doubles.
+    double node_dt_var3(int n, const uint32_t* pos) const {
+        int nP = (n + 1) % 3, nPP = (n + 2) % 3;
+        int s0[3] = {0, 0, 0};
+        int sP1[3] = {0, 0, 0}; sP1[nP] = 1;
+        int sPP1[3] = {0, 0, 0}; sPP1[nPP] = 1;
+        int sPm[3] = {0, 0, 0}; sPm[nP] = -1;
+        int sPPm[3] = {0, 0, 0}; sPPm[nPP] = -1;
+        int sPmPPm[3] = {0, 0, 0}; sPmPPm[nP] = -1; sPmPPm[nPP] = -1;
+        int sN1[3] = {0, 0, 0}; sN1[n] = 1;
+        auto C = [&](int c, const int* s) { return EC_C[(size_t)c * NN + shifted(0, pos, s)]; };
+        auto Lf = [&](int c, const int* s) { return EC_L[(size_t)c * NN + shifted(0, pos, s)]; };
+        float one = 1;
+        double wqp = one / (Lf(nPP, s0) * C(n, sP1)) + one / (Lf(nPP, s0) * C(n, s0));
+        wqp += one / (Lf(nP, s0) * C(n, sPP1)) + one / (Lf(nP, s0) * C(n, s0));
+        // ipos = Shift(nP,-1); GetShiftedPos(nP,1) == pos
+        wqp += one / (Lf(nPP, sPm) * C(n, s0)) + one / (Lf(nPP, sPm) * C(n, sPm));
+        // ipos = Shift(nPP,-1) (shift nP and nPP by -1); GetShiftedPos(nPP,1) -> nP-1 only
+        wqp += one / (Lf(nP, sPmPPm) * C(n, sPm)) + one / (Lf(nP, sPmPPm) * C(n, sPmPPm));
+
+        double wt_4[4];
+        wt_4[0] = one / (Lf(nPP, s0) * C(nP, s0));
+        wt_4[1] = one / (Lf(nPP, sPm) * C(nP, s0));
+        wt_4[2] = one / (Lf(nP, s0) * C(nPP, s0));
+        wt_4[3] = one / (Lf(nP, sPPm) * C(nPP, s0));
+        double wt1 = wt_4[0] + wt_4[1] + wt_4[2] + wt_4[3] - 2 * min4(wt_4);
+
+        wt_4[0] = one / (Lf(nPP, s0) * C(nP, sN1));
+        wt_4[1] = one / (Lf(nPP, sPm) * C(nP, sN1));
+        wt_4[2] = one / (Lf(nP, s0) * C(nPP, sN1));
+        wt_4[3] = one / (Lf(nP, sPPm) * C(nPP, sN1));
+        double wt2 = wt_4[0] + wt_4[1] + wt_4[2] + wt_4[3] - 2 * min4(wt_4);
+
+        double w_total = wqp + wt1 + wt2;
+        return 2 / std::sqrt(w_total);
+    }
+
+    // The same terms for the interior run z in [1, N2-2] of the line (x, y)
+    // (x, y interior): every shift stays on the grid, so each operand is a
+    // fixed offset from the line and the loop runs over z with plain pointer
+    // reads (the compiler vectorizes it; every operation is the scalar one,
+    // in the same order, so the values are identical).
+    void line_dt_var3(int n, uint32_t x, uint32_t y, double* out) const {
+        const int nP = (n + 1) % 3, nPP = (n + 2) % 3;
+        const long long st[3] = {(long long)N[1] * N[2], (long long)N[2], 1};
+        const float* Lb = EC_L.data() + at(0, x, y, 0);
+        const float* Cb = EC_C.data() + at(0, x, y, 0);
+        const long long cn = (long long)n * NN, cp = (long long)nP * NN, cpp = (long long)nPP * NN;
+        const float* Lpp_0 = Lb + cpp;
+        const float* Lp_0 = Lb + cp;
+        const float* Lpp_m = Lb + cpp - st[nP];
+        const float* Lp_mm = Lb + cp - st[nP] - st[nPP];
+        const float* Lp_ppm = Lb + cp - st[nPP];
+        const float* Cn_0 = Cb + cn;
+        const float* Cn_p1 = Cb + cn + st[nP];
+        const float* Cn_pp1 = Cb + cn + st[nPP];
+        const float* Cn_m = Cb + cn - st[nP];
+        const float* Cn_mm = Cb + cn - st[nP] - st[nPP];
+        const float* Cp_0 = Cb + cp;
+        const float* Cpp_0 = Cb + cpp;
+        const float* Cp_n1 = Cb + cp + st[n];
+        const float* Cpp_n1 = Cb + cpp + st[n];
+        const float one = 1;
+        const uint32_t z1 = N[2] - 1;
+        for (uint32_t z = 1; z < z1; ++z) {
+            double wqp = one / (Lpp_0[z] * Cn_p1[z]) + one / (Lpp_0[z] * Cn_0[z]);
+            wqp += one / (Lp_0[z] * Cn_pp1[z]) + one / (Lp_0[z] * Cn_0[z]);
+            wqp += one / (Lpp_m[z] * Cn_0[z]) + one / (Lpp_m[z] * Cn_m[z]);
+            wqp += one / (Lp_mm[z] * Cn_m[z]) + one / (Lp_mm[z] * Cn_mm[z]);
+            double a0 = one / (Lpp_0[z] * Cp_0[z]), a1 = one / (Lpp_m[z] * Cp_0[z]);
+            double a2 = one / (Lp_0[z] * Cpp_0[z]), a3 = one / (Lp_ppm[z] * Cpp_0[z]);
+            double m = a0;
+            m = a1 < m ? a1 : m;
+            m = a2 < m ? a2 : m;
+            m = a3 < m ? a3 : m;
+            const double wt1 = a0 + a1 + a2 + a3 - 2 * m;
+            a0 = one / (Lpp_0[z] * Cp_n1[z]);
+            a1 = one / (Lpp_m[z] * Cp_n1[z]);
+            a2 = one / (Lp_0[z] * Cpp_n1[z]);
+            a3 = one / (Lp_ppm[z] * Cpp_n1[z]);
+            m = a0;
+            m = a1 < m ? a1 : m;
+            m = a2 < m ? a2 : m;
+            m = a3 < m ? a3 : m;
+            const double wt2 = a0 + a1 + a2 + a3 - 2 * m;
+            const double w_total = wqp + wt1 + wt2;
+            out[z] = 2 / std::sqrt(w_total);
+        }
+    }
+
     double calc_timestep_var3() const {
         std::vector<double> best(std::max(threads, 1), 1e200);
         parallel_for(N[0], threads, [&](uint32_t x, int t) {
             uint32_t pos[3] = {x, 0, 0};
             double dT_loc = best[t];
-            // (the minimum does not depend on the visiting order; z innermost
-            // follows the memory layout)
-            for (int n = 0; n < 3; ++n) {
-                int nP = (n + 1) % 3, nPP = (n + 2) % 3;
-                for (pos[1] = 0; pos[1] < N[1]; ++pos[1])
-                    for (pos[2] = 0; pos[2] < N[2]; ++pos[2]) {
-                        int s0[3] = {0, 0, 0};
-                        int sP1[3] = {0, 0, 0}; sP1[nP] = 1;
-                        int sPP1[3] = {0, 0, 0}; sPP1[nPP] = 1;
-                        int sPm[3] = {0, 0, 0}; sPm[nP] = -1;
-                        int sPPm[3] = {0, 0, 0}; sPPm[nPP] = -1;
-                        int sPmPPm[3] = {0, 0, 0}; sPmPPm[nP] = -1; sPmPPm[nPP] = -1;
-                        int sN1[3] = {0, 0, 0}; sN1[n] = 1;
-                        // interior nodes: every +-1 shift stays on the grid, no reflection
-                        const bool inner = pos[0] > 0 && pos[1] > 0 && pos[2] > 0 && pos[0] + 1 < N[0] &&
-                                           pos[1] + 1 < N[1] && pos[2] + 1 < N[2];
-                        const size_t base = at(0, pos);
-                        auto off = [&](const int* s) -> size_t {
-                            if (inner)
-                                return base + (size_t)((long long)s[0] * N[1] * N[2] + (long long)s[1] * N[2] + s[2]);
-                            return shifted(0, pos, s);
-                        };
-                        auto C = [&](int c, const int* s) { return EC_C[(size_t)c * NN + off(s)]; };
-                        auto Lf = [&](int c, const int* s) { return EC_L[(size_t)c * NN + off(s)]; };
-                        float one = 1;
-                        double wqp = one / (Lf(nPP, s0) * C(n, sP1)) + one / (Lf(nPP, s0) * C(n, s0));
-                        wqp += one / (Lf(nP, s0) * C(n, sPP1)) + one / (Lf(nP, s0) * C(n, s0));
-                        // ipos = Shift(nP,-1); GetShiftedPos(nP,1) == pos
-                        wqp += one / (Lf(nPP, sPm) * C(n, s0)) + one / (Lf(nPP, sPm) * C(n, sPm));
-                        // ipos = Shift(nPP,-1) (shift nP and nPP by -1); GetShiftedPos(nPP,1) -> nP-1 only
-                        wqp += one / (Lf(nP, sPmPPm) * C(n, sPm)) + one / (Lf(nP, sPmPPm) * C(n, sPmPPm));
-
-                        double wt_4[4];
-                        wt_4[0] = one / (Lf(nPP, s0) * C(nP, s0));
-                        wt_4[1] = one / (Lf(nPP, sPm) * C(nP, s0));
-                        wt_4[2] = one / (Lf(nP, s0) * C(nPP, s0));
-                        wt_4[3] = one / (Lf(nP, sPPm) * C(nPP, s0));
-                        double wt1 = wt_4[0] + wt_4[1] + wt_4[2] + wt_4[3] - 2 * min4(wt_4);
-
-                        wt_4[0] = one / (Lf(nPP, s0) * C(nP, sN1));
-                        wt_4[1] = one / (Lf(nPP, sPm) * C(nP, sN1));
-                        wt_4[2] = one / (Lf(nP, s0) * C(nPP, sN1));
-                        wt_4[3] = one / (Lf(nP, sPPm) * C(nPP, sN1));
-                        double wt2 = wt_4[0] + wt_4[1] + wt_4[2] + wt_4[3] - 2 * min4(wt_4);
-
-                        double w_total = wqp + wt1 + wt2;
-                        double newT = 2 / std::sqrt(w_total);
-                        if ((newT < dT_loc) && (newT > 0.0)) dT_loc = newT;
+            std::vector<double> line(N[2]);
+            auto take = [&](double newT) {
+                if ((newT < dT_loc) && (newT > 0.0)) dT_loc = newT;
+            };
+            // (the minimum does not depend on the visiting order)
+            for (int n = 0; n < 3; ++n)
+                for (pos[1] = 0; pos[1] < N[1]; ++pos[1]) {
+                    const bool fast = x > 0 && x + 1 < N[0] && pos[1] > 0 && pos[1] + 1 < N[1] && N[2] > 2;
+                    if (fast) {
+                        line_dt_var3(n, x, pos[1], line.data());
+                        for (uint32_t z = 1; z + 1 < N[2]; ++z) take(line[z]);
+                        pos[2] = 0;
+                        take(node_dt_var3(n, pos));
+                        pos[2] = N[2] - 1;
+                        take(node_dt_var3(n, pos));
+                    } else {
+                        for (pos[2] = 0; pos[2] < N[2]; ++pos[2]) take(node_dt_var3(n, pos));
                     }
-            }
+                }
             best[t] = dT_loc;
         });
         double r = 1e200;
