@@ -188,3 +188,39 @@ def test_uniform_mesh_is_exact_and_fits_uint16_index():
     assert not cop.factorized
     assert cop.info["index_bytes_e"] == 2 and cop.info["index_bytes_h"] == 2
     assert cop.info["trim_e"] == [1, 1, 1]
+
+
+def _operator_bytes(op):
+    """The coefficient arrays, UPML slabs, dispersion coefficients and dT
+    of a built operator as one byte string."""
+    d = op.desc
+
+    def arr(p, n):
+        return np.ctypeslib.as_array(p, shape=(n,)).tobytes() if n else b""
+
+    parts = [np.float64(d.dT).tobytes()]
+    nn = 3 * d.num_lines[0] * d.num_lines[1] * d.num_lines[2]
+    parts += [arr(getattr(d, f), nn) for f in ("vv", "vi", "ii", "iv")]
+    for i in range(d.num_upml):
+        u = d.upml[i]
+        n = 3 * u.num_lines[0] * u.num_lines[1] * u.num_lines[2]
+        parts += [arr(getattr(u, f), n) for f in ("vv", "vvfo", "vvfn", "ii", "iifo", "iifn")]
+    for i in range(d.num_ade_orders):
+        a = d.ade[i]
+        for f, on in (("v_int", a.volt_on), ("v_ext", a.volt_on), ("v_lor", a.volt_lor_on),
+                      ("i_int", a.curr_on), ("i_ext", a.curr_on), ("i_lor", a.curr_lor_on)):
+            if on:
+                parts.append(arr(getattr(a, f), 3 * a.count))
+    return b"".join(parts)
+
+
+@pytest.mark.parametrize("make", [lambda: scenes.mini("upml", seed=2), lambda: scenes.mini("mixed", seed=1),
+                                  lambda: scenes.mini("graded", seed=5), lambda: scenes.serve_job(1)],
+                         ids=["upml", "mixed", "graded", "serve_lorentz"])
+def test_operator_independent_of_build_threads(make):
+    """The parallel build loops (EC pass, Var3 timestep search with its
+    vectorized interior lines, UPML slabs handed out in chunks of lines,
+    dispersion) give the same bytes for any thread count."""
+    ref = _operator_bytes(Operator(make(), threads=1))
+    for th in (3, 8):
+        assert _operator_bytes(Operator(make(), threads=th)) == ref

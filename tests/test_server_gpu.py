@@ -34,11 +34,14 @@ def _same(e, srv, jid):
     assert np.array_equal(Ia.view(np.uint32), Ib.view(np.uint32))
 
 
-@pytest.mark.parametrize("round_steps,bin_mib,batch_min", [(64, 0, 0), (37, 1, 1), (50, 0, 3)])
-def test_server_results_same_as_alone(round_steps, bin_mib, batch_min):
-    """Concurrent engines (the default), persistent-batch rounds with L2
-    bins, and a mix of both modes all give each job its solo result."""
-    srv = Server(round_steps=round_steps, bin_mib=bin_mib, build_workers=2, batch_min_jobs=batch_min)
+@pytest.mark.parametrize("round_steps,bin_mib,batch_min,tile_share",
+                         [(64, 0, 0, 0), (37, 1, 1, 0), (50, 0, 3, 0), (29, 0, 0, 16)])
+def test_server_results_same_as_alone(round_steps, bin_mib, batch_min, tile_share):
+    """Concurrent engines (the default, each job tiled for a share of the
+    SMs), persistent-batch rounds with L2 bins, and a mix of both modes all
+    give each job its solo result."""
+    srv = Server(round_steps=round_steps, bin_mib=bin_mib, build_workers=2, batch_min_jobs=batch_min,
+                 tile_share=tile_share)
     ids = {}
     for seed in (3, 4):
         for k in KINDS:
