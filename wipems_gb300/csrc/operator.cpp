@@ -368,128 +368,161 @@ struct Builder {
     }
     size_t at(int n, const uint32_t* p) const { return at(n, p[0], p[1], p[2]); }
 
-    // Operator::GetMaterial with the kinds of the three sample coordinates:
-    // the winning primitive's (eps, kappa, mue, sigma), or the background's.
-    struct Mat {
-        double eps, kappa, mue, sigma;
+    // Operator::AverageMatQuarterCell (operator.cpp:1406-1518) and
+    // Operator::Calc_ECPos (operator.cpp:1176-1224) for the edges in
+    // direction ny along one z-line (x, y), every z at once.
+    //
+    // GetMaterial's box lookup: the winner for a sample is the first set bit
+    // of the three per-axis masks ANDed (BoxIndex::lookup); the x and y
+    // masks of the six samples are fixed along the line, so they are ANDed
+    // once per line.  The geometry comes from per-axis tables of the same
+    // products the reference forms (GetNodeWidth / GetEdgeLength =
+    // disc delta * unit; GetNodeArea = the product of two widths, 0 when a
+    // shifted position is negative).  Every product, sum and quotient is
+    // then formed in the reference's order, so the values are identical.
+    struct EcLine {
+        // Wm[a][i]: GetNodeWidth(a, i, dual) = GetEdgeLength(a, i, main);
+        // Dm[a][i]: GetNodeWidth(a, i, main) = GetEdgeLength(a, i, dual)
+        std::vector<double> Wm[3], Dm[3];
+        // material table indexed by winner bit; the last entry is the background
+        std::vector<double> eps, kappa, mue, sigma;
     };
-    Mat material(const int kind[3], const uint32_t idx[3]) const {
-        int w = mat_idx.lookup(kind, idx);
-        if (w >= 0) {
-            const Prim& p = S.prims[w];
-            return Mat{p.eps, p.kappa, p.mue, p.sigma};
+    EcLine ec_tables() const {
+        EcLine t;
+        for (int a = 0; a < 3; ++a) {
+            t.Wm[a].resize(N[a]);
+            t.Dm[a].resize(N[a]);
+            for (uint32_t i = 0; i < N[a]; ++i) {
+                t.Wm[a][i] = g.disc_delta(a, i, false) * g.unit;
+                t.Dm[a][i] = g.disc_delta(a, i, true) * g.unit;
+            }
         }
-        return Mat{S.bg_eps, S.bg_kappa, S.bg_mue, S.bg_sigma};
+        const size_t nb = mat_idx.prim.size();
+        t.eps.resize(nb + 1); t.kappa.resize(nb + 1); t.mue.resize(nb + 1); t.sigma.resize(nb + 1);
+        for (size_t b = 0; b < nb; ++b) {
+            const Prim& p = S.prims[mat_idx.prim[b]];
+            t.eps[b] = p.eps; t.kappa[b] = p.kappa; t.mue[b] = p.mue; t.sigma[b] = p.sigma;
+        }
+        t.eps[nb] = S.bg_eps; t.kappa[nb] = S.bg_kappa; t.mue[nb] = S.bg_mue; t.sigma[nb] = S.bg_sigma;
+        return t;
     }
 
-    // Operator::AverageMatQuarterCell (operator.cpp:1406-1518)
-    bool avg_quarter_cell(int ny, const uint32_t* pos, double* EffMat) const {
-        int n = ny;
-        int nP = (n + 1) % 3;
-        int nPP = (n + 2) % 3;
-        int loc_pos[3] = {(int)pos[0], (int)pos[1], (int)pos[2]};
-        double A_n;
-        double area = 0;
-        int kind[3];
-        uint32_t idx[3] = {pos[0], pos[1], pos[2]};
-        Mat m;
-
-        // shift up-right
-        kind[n] = SK_HALF; kind[nP] = SK_QP; kind[nPP] = SK_QP;
-        A_n = g.node_area_i(ny, loc_pos, true);
-        m = material(kind, idx);
-        EffMat[0] = m.eps * A_n;
-        EffMat[1] = m.kappa * A_n;
-        area += A_n;
-        // shift up-left
-        kind[nP] = SK_QM; kind[nPP] = SK_QP;
-        --loc_pos[nP];
-        A_n = g.node_area_i(ny, loc_pos, true);
-        m = material(kind, idx);
-        EffMat[0] += m.eps * A_n;
-        EffMat[1] += m.kappa * A_n;
-        area += A_n;
-        // shift down-right
-        kind[nP] = SK_QP; kind[nPP] = SK_QM;
-        ++loc_pos[nP];
-        --loc_pos[nPP];
-        A_n = g.node_area_i(ny, loc_pos, true);
-        m = material(kind, idx);
-        EffMat[0] += m.eps * A_n;
-        EffMat[1] += m.kappa * A_n;
-        area += A_n;
-        // shift down-left
-        kind[nP] = SK_QM; kind[nPP] = SK_QM;
-        --loc_pos[nP];
-        A_n = g.node_area_i(ny, loc_pos, true);
-        m = material(kind, idx);
-        EffMat[0] += m.eps * A_n;
-        EffMat[1] += m.kappa * A_n;
-        area += A_n;
-
-        EffMat[0] *= kEps0 / area;
-        EffMat[1] /= area;
-
-        // mu, sigma averaging
-        loc_pos[0] = pos[0];
-        loc_pos[1] = pos[1];
-        loc_pos[2] = pos[2];
-        double length = 0;
-        // shift down
-        kind[n] = SK_QM; kind[nP] = SK_HALF; kind[nPP] = SK_HALF;
-        --loc_pos[n];
-        double delta_ny = g.node_width_i(n, loc_pos, true);
-        m = material(kind, idx);
-        EffMat[2] = delta_ny / m.mue;
-        double sigma = m.sigma;
-        if (sigma)
-            EffMat[3] = delta_ny / sigma;
-        else
-            EffMat[3] = 0;
-        length = delta_ny;
-        // shift up
-        kind[n] = SK_QP;
-        ++loc_pos[n];
-        delta_ny = g.node_width_i(n, loc_pos, true);
-        m = material(kind, idx);
-        EffMat[2] += delta_ny / m.mue;
-        sigma = m.sigma;
-        if (sigma)
-            EffMat[3] += delta_ny / sigma;
-        else
-            EffMat[3] = 0;
-        length += delta_ny;
-
-        EffMat[2] = length * kMue0 / EffMat[2];
-        if (EffMat[3]) EffMat[3] = length / EffMat[3];
-
-        for (int k = 0; k < 4; ++k)
-            if (std::isnan(EffMat[k]) || std::isinf(EffMat[k])) return false;
-        return true;
-    }
-
-    // Operator::Calc_ECPos (operator.cpp:1176-1224)
-    bool calc_ec_pos(int ny, const uint32_t* pos, double* EC, double* EffMat) const {
-        if (!avg_quarter_cell(ny, pos, EffMat)) return false;
-        double delta = g.edge_length(ny, pos, false);
-        double area = g.edge_area(ny, pos, false);
-        if (delta) {
-            EC[0] = EffMat[0] * area / delta;
-            EC[1] = EffMat[1] * area / delta;
-        } else {
-            EC[0] = 0;
-            EC[1] = 0;
+    // The edges (ny, x, y, z) for every z: EC[4][z] and EffMat[3][z] (eps,
+    // kappa, mue averages) into ec / eff; false when an effective material
+    // parameter is NaN or Inf.  m01: scratch of 6 * W words.
+    bool ec_line(const EcLine& t, int ny, uint32_t x, uint32_t y, double* ec, double* eff,
+                 std::vector<uint64_t>& m01) const {
+        const int n = ny, nP = (n + 1) % 3, nPP = (n + 2) % 3;
+        const int W = mat_idx.W;
+        const size_t nb = mat_idx.prim.size();
+        // sample kinds per axis of the six lookups: the four quarter cells
+        // (up-right, up-left, down-right, down-left), then the two half
+        // lines below and above the node along ny
+        int kind[6][3];
+        const int qP[4] = {SK_QP, SK_QM, SK_QP, SK_QM}, qPP[4] = {SK_QP, SK_QP, SK_QM, SK_QM};
+        for (int q = 0; q < 4; ++q) {
+            kind[q][n] = SK_HALF;
+            kind[q][nP] = qP[q];
+            kind[q][nPP] = qPP[q];
         }
-        delta = g.edge_length(ny, pos, true);
-        area = g.edge_area(ny, pos, true);
-        if (delta) {
-            EC[2] = EffMat[2] * area / delta;
-            EC[3] = EffMat[3] * area / delta;
-        } else {
-            EC[2] = 0;
-            EC[3] = 0;
+        for (int q = 4; q < 6; ++q) {
+            kind[q][n] = q == 4 ? SK_QM : SK_QP;
+            kind[q][nP] = SK_HALF;
+            kind[q][nPP] = SK_HALF;
         }
-        return true;
+        m01.resize(6 * (size_t)W);
+        if (nb)
+            for (int q = 0; q < 6; ++q) {
+                const uint64_t* a0 = &mat_idx.masks[0][kind[q][0]][(size_t)x * W];
+                const uint64_t* a1 = &mat_idx.masks[1][kind[q][1]][(size_t)y * W];
+                for (int w = 0; w < W; ++w) m01[q * W + w] = a0[w] & a1[w];
+            }
+        auto winner = [&](int q, uint32_t z) -> size_t {
+            if (!nb) return nb;
+            const uint64_t* a2 = &mat_idx.masks[2][kind[q][2]][(size_t)z * W];
+            for (int w = 0; w < W; ++w) {
+                const uint64_t m = m01[q * W + w] & a2[w];
+                if (m) return (size_t)w * 64 + (size_t)__builtin_ctzll(m);
+            }
+            return nb;
+        };
+        const uint32_t pos_xy[2] = {x, y};
+        bool ok = true;
+        for (uint32_t z = 0; z < N[2]; ++z) {
+            const uint32_t pos[3] = {pos_xy[0], pos_xy[1], z};
+            const uint32_t p = pos[nP], pp = pos[nPP], pn = pos[n];
+            // quarter-cell areas GetNodeArea(ny, loc, dual) of the four shifts
+            const double wP0 = t.Wm[nP][p], wPP0 = t.Wm[nPP][pp];
+            const double wP1 = p ? t.Wm[nP][p - 1] : 0, wPP1 = pp ? t.Wm[nPP][pp - 1] : 0;
+            const double A[4] = {wP0 * wPP0, p ? wP1 * wPP0 : 0.0, pp ? wP0 * wPP1 : 0.0,
+                                 (p && pp) ? wP1 * wPP1 : 0.0};
+            double E0, E1, area = 0;
+            {
+                size_t w = winner(0, z);
+                E0 = t.eps[w] * A[0];
+                E1 = t.kappa[w] * A[0];
+                area += A[0];
+                for (int q = 1; q < 4; ++q) {
+                    w = winner(q, z);
+                    E0 += t.eps[w] * A[q];
+                    E1 += t.kappa[w] * A[q];
+                    area += A[q];
+                }
+            }
+            E0 *= kEps0 / area;
+            E1 /= area;
+            // mu, sigma: harmonic along ny over the half lines below and above
+            double E2, E3, length;
+            {
+                double delta_ny = pn ? t.Wm[n][pn - 1] : 0;
+                size_t w = winner(4, z);
+                E2 = delta_ny / t.mue[w];
+                double sigma = t.sigma[w];
+                E3 = sigma ? delta_ny / sigma : 0;
+                length = delta_ny;
+                delta_ny = t.Wm[n][pn];
+                w = winner(5, z);
+                E2 += delta_ny / t.mue[w];
+                sigma = t.sigma[w];
+                if (sigma)
+                    E3 += delta_ny / sigma;
+                else
+                    E3 = 0;
+                length += delta_ny;
+            }
+            E2 = length * kMue0 / E2;
+            if (E3) E3 = length / E3;
+            if (std::isnan(E0) || std::isinf(E0) || std::isnan(E1) || std::isinf(E1) || std::isnan(E2) ||
+                std::isinf(E2) || std::isnan(E3) || std::isinf(E3)) {
+                ok = false;
+                break;
+            }
+            // Calc_ECPos
+            double delta = t.Wm[n][pn];
+            double ar = t.Dm[nP][p] * t.Dm[nPP][pp];
+            double* e = ec + 4 * (size_t)z;
+            if (delta) {
+                e[0] = E0 * ar / delta;
+                e[1] = E1 * ar / delta;
+            } else {
+                e[0] = 0;
+                e[1] = 0;
+            }
+            delta = t.Dm[n][pn];
+            ar = t.Wm[nP][p] * t.Wm[nPP][pp];
+            if (delta) {
+                e[2] = E2 * ar / delta;
+                e[3] = E3 * ar / delta;
+            } else {
+                e[2] = 0;
+                e[3] = 0;
+            }
+            double* f = eff + 3 * (size_t)z;
+            f[0] = E0;
+            f[1] = E1;
+            f[2] = E2;
+        }
+        return ok;
     }
 
     // Operator::Calc_EC_Range over all lines; the effective materials of
@@ -501,33 +534,36 @@ struct Builder {
         EC_R.assign(3 * NN, 0.f);
         if (slabs)
             for (SlabEff& se : *slabs) se.v.assign(9 * (size_t)se.nl[0] * se.nl[1] * se.nl[2], 0.0);
+        const EcLine t = ec_tables();
         std::atomic<bool> ok{true};
         parallel_for(N[0], threads, [&](uint32_t x, int) {
-            uint32_t pos[3] = {x, 0, 0};
-            double ec[4], eff[4];
-            for (pos[1] = 0; pos[1] < N[1]; ++pos[1])
-                for (pos[2] = 0; pos[2] < N[2]; ++pos[2]) {
-                    SlabEff* keep = nullptr;
-                    if (slabs)
-                        for (SlabEff& se : *slabs)
-                            if (se.holds(pos)) keep = &se;
-                    for (int n = 0; n < 3; ++n) {
-                        if (!calc_ec_pos(n, pos, ec, eff)) {
-                            ok = false;
-                            return;
-                        }
-                        size_t i = at(n, pos);
-                        EC_C[i] = (float)ec[0];
-                        EC_G[i] = (float)ec[1];
-                        EC_L[i] = (float)ec[2];
-                        EC_R[i] = (float)ec[3];
-                        if (keep) {
-                            double* d = &keep->v[keep->at(n, pos)];
-                            d[0] = eff[0];
-                            d[1] = eff[1];
-                            d[2] = eff[2];
-                        }
+            std::vector<double> ec(4 * (size_t)N[2]), eff(3 * (size_t)N[2]);
+            std::vector<uint64_t> m01;
+            for (uint32_t y = 0; y < N[1]; ++y)
+                for (int n = 0; n < 3; ++n) {
+                    if (!ec_line(t, n, x, y, ec.data(), eff.data(), m01)) {
+                        ok = false;
+                        return;
                     }
+                    const size_t i0 = at(n, x, y, 0);
+                    for (uint32_t z = 0; z < N[2]; ++z) {
+                        EC_C[i0 + z] = (float)ec[4 * z];
+                        EC_G[i0 + z] = (float)ec[4 * z + 1];
+                        EC_L[i0 + z] = (float)ec[4 * z + 2];
+                        EC_R[i0 + z] = (float)ec[4 * z + 3];
+                    }
+                    if (slabs)
+                        for (SlabEff& se : *slabs) {
+                            uint32_t pos[3] = {x, y, se.start[2]};
+                            if (!se.holds(pos)) continue;
+                            for (uint32_t z = se.start[2]; z < se.start[2] + se.nl[2]; ++z) {
+                                pos[2] = z;
+                                double* d = &se.v[se.at(n, pos)];
+                                d[0] = eff[3 * z];
+                                d[1] = eff[3 * z + 1];
+                                d[2] = eff[3 * z + 2];
+                            }
+                        }
                 }
         });
         if (!ok) set_error("an effective material parameter is NaN or Inf (AverageMatQuarterCell)");
