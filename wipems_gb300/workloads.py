@@ -143,7 +143,7 @@ def b96(n_jobs: int = 96, timesteps: int = 1500, device: int = 0) -> dict:
 
 def serve(n_jobs: int = 48, mean_gap: float = 0.02, end_crit: float = 1e-4, seed: int = 777, device: int = 0,
           round_steps: int = 128, modes=("served", "plain"), batch_min_jobs: int = 0,
-          build_workers: int = 0, tile_share: int = 0) -> dict:
+          build_workers: int = 0, tile_share: int = 0, max_active: int = 0) -> dict:
     """S: a seeded Poisson stream of serve_job requests (operator build
     included), through the continuous-batching server and one at a time
     through the plain engine.  Both stop every job at -40 dB energy or its
@@ -153,7 +153,7 @@ def serve(n_jobs: int = 48, mean_gap: float = 0.02, end_crit: float = 1e-4, seed
     arr = np.cumsum(rng.exponential(mean_gap, n_jobs))
     arr -= arr[0]
     out = dict(workload="serve", jobs=n_jobs, mean_gap_s=mean_gap, end_crit=end_crit, seed=seed,
-               round_steps=round_steps, batch_min_jobs=batch_min_jobs, tile_share=tile_share)
+               round_steps=round_steps, batch_min_jobs=batch_min_jobs, tile_share=tile_share, max_active=max_active)
 
     def pct(a, q):
         return float(np.percentile(np.asarray(a), q))
@@ -161,7 +161,7 @@ def serve(n_jobs: int = 48, mean_gap: float = 0.02, end_crit: float = 1e-4, seed
     ts_served = ts_plain = None
     if "served" in modes:
         srv = Server(device=device, round_steps=round_steps, batch_min_jobs=batch_min_jobs,
-                     build_workers=build_workers, tile_share=tile_share)
+                     build_workers=build_workers, tile_share=tile_share, max_active=max_active)
         t0 = time.perf_counter()
         ids = []
         for k in range(n_jobs):
@@ -222,6 +222,7 @@ def main():
     ap.add_argument("--served-only", action="store_true")
     ap.add_argument("--workers", type=int, default=0, help="serve: host build workers (0 = the server's default)")
     ap.add_argument("--round-steps", type=int, default=128, help="serve: timesteps per scheduling round")
+    ap.add_argument("--max-active", type=int, default=0, help="serve: cap on resident jobs (0 = the server's default)")
     ap.add_argument("--tile-share", type=int, default=0,
                     help="serve: tile each job for 1/N of the SMs (0 = the server's default, 1 = the job alone)")
     args = ap.parse_args()
@@ -234,6 +235,7 @@ def main():
     else:
         r = serve(args.jobs or 48, args.gap, device=args.device, batch_min_jobs=args.batch_min,
                   build_workers=args.workers, tile_share=args.tile_share, round_steps=args.round_steps,
+                  max_active=args.max_active,
                   modes=("served",) if args.served_only else ("served", "plain"))
     print(json.dumps(r), flush=True)
 
