@@ -136,30 +136,80 @@ def build_workload(threads: int = 0):
     return sc, op, cop, dict(operator_build_s=round(t1 - t0, 3), compress_s=round(t2 - t1, 3))
 
 
-def config_dict(op, cop, extra=None):
-    n = op.num_lines
-    d = {"workload": "L256: 256^3 cells (257^3 nodes), 0.5 mm uniform mesh, UPML-8 on 6 faces, 40 seeded "
-                     "dielectric bricks, 50 ohm z lumped port, Gaussian f0=fc=10 GHz; one step = one "
-                     f"{TIMESTEPS}-timestep simulation",
-         "nodes": n[0] * n[1] * n[2], "cells": (n[0] - 1) * (n[1] - 1) * (n[2] - 1), "timesteps_per_step": TIMESTEPS,
-         "upml_nodes": cop.info["num_upml_nodes"], "tuples_e": cop.info["num_tuples_e"],
-         "tuples_h": cop.info["num_tuples_h"], "index_bytes": cop.info["index_bytes_e"], "l2_policy": "inputs larger than L2 (fields+operator > 500 MB)",
+WORKLOAD = ("L256: 256^3 cells (257^3 nodes), 0.5 mm uniform mesh, UPML-8 on 6 faces, 40 seeded dielectric "
+            "bricks, 50 ohm z lumped port, Gaussian f0=fc=10 GHz; one step = one "
+            f"{TIMESTEPS}-timestep simulation")
+
+
+def config_dict(num_lines, extra=None):
+    """The workload keys both arms report (the same for the engine and the
+    reference arm)."""
+    n = num_lines
+    d = {"workload": WORKLOAD, "nodes": n[0] * n[1] * n[2], "cells": (n[0] - 1) * (n[1] - 1) * (n[2] - 1),
+         "timesteps_per_step": TIMESTEPS, "l2_policy": "inputs larger than L2 (fields+operator > 500 MB)",
          "parallelism": "replicas"}
     if extra:
         d.update(extra)
     return d
 
 
-def cpu_baseline(op, threads: int, target_s: float = 12.0):
-    """Oracle SSE-compressed MT engine on a bounded number of timesteps."""
+def oracle_operator(name: str, threads: int):
+    """A workload's operator built by the oracle from the recorded scene,
+    without the engine library (for the CPU legs)."""
     import oracle
-    # calibrate on 2 timesteps, then run about target_s of stepping
+    from wipems_gb300 import scenes
+    with scenes.spec_only():
+        sc = {"l256": lambda: scenes.l256(nr_ts=TIMESTEPS), "p64": lambda: scenes.p64(),
+              "d192": lambda: scenes.d192()}[name]()
+    return oracle.Operator(sc.spec, threads=threads)
+
+
+def _oracle_rate(op, threads: int, target_s: float, max_steps: int):
+    """Mcell-updates/s of the oracle's SSE-compressed x-slab engine on about
+    target_s of stepping (at most max_steps timesteps)."""
+    import oracle
     r = oracle.run(op.desc, [], 2, 0, engine=oracle.SSE_COMPRESSED_MT, threads=threads, energy=False, fields=False)
     per = max(r["seconds"] / 2, 1e-4)
-    n = int(max(4, min(400, target_s / per)))
+    n = int(max(4, min(max_steps, target_s / per)))
     r = oracle.run(op.desc, [], n, 0, engine=oracle.SSE_COMPRESSED_MT, threads=threads, energy=False, fields=False)
-    mcs = op.num_nodes * n / r["seconds"] / 1e6
-    return mcs, n, r["seconds"]
+    nodes = op.num_lines[0] * op.num_lines[1] * op.num_lines[2]
+    return nodes * n / r["seconds"] / 1e6, n, r["seconds"]
+
+
+def cpu_baseline(threads: int):
+    """The CPU table: the oracle's restated SSE-compressed multithreaded
+    engine (the reference's default engine family) on its own operator
+    build, on all host cores and on one, for L256 (bounded samples), P64
+    (the full 2000 timesteps) and a 300-timestep window of D192."""
+    import platform
+    out = {}
+    l256 = oracle_operator("l256", threads)
+    v, n, sec = _oracle_rate(l256, threads, 12.0, 400)
+    out["l256"] = {"value": round(v, 2), "timesteps": n, "seconds": round(sec, 2), "threads": threads}
+    v1, n1, sec1 = _oracle_rate(l256, 1, 8.0, 100)
+    out["l256_1thread"] = {"value": round(v1, 2), "timesteps": n1, "seconds": round(sec1, 2), "threads": 1}
+    del l256
+    p64 = oracle_operator("p64", threads)
+    for key, th in (("p64", threads), ("p64_1thread", 1)):
+        vv, nn, ss = _oracle_rate(p64, th, 1e9, 2000)
+        out[key] = {"value": round(vv, 2), "timesteps": nn, "seconds": round(ss, 2), "threads": th}
+    del p64
+    d192 = oracle_operator("d192", threads)
+    vv, nn, ss = _oracle_rate(d192, threads, 1e9, 300)
+    out["d192_window"] = {"value": round(vv, 2), "timesteps": nn, "seconds": round(ss, 2), "threads": threads}
+    del d192
+    cpu = platform.processor() or platform.machine()
+    try:
+        for ln in open("/proc/cpuinfo"):
+            if ln.lower().startswith(("model name", "cpu part")):
+                cpu = ln.split(":", 1)[1].strip()
+                break
+    except OSError:
+        pass
+    return {"value": round(v, 2), "unit": "Mcell-updates/s", "cores": threads, "kind": "port",
+            "sample": f"{n} timesteps of L256 ({sec:.1f} s) with the restated SSE-compressed x-slab "
+                      f"multithreaded engine on the oracle's own operator build",
+            "nproc": os.cpu_count(), "cpu": cpu, "machine": platform.machine(), "table": out}
 
 
 def max_over_ranks(vals, device):
@@ -175,11 +225,16 @@ def max_over_ranks(vals, device):
 
 
 def run_reference(args, rank, world):
+    """The reference's CPU algorithm (the oracle's restated SSE-compressed
+    x-slab multithreaded engine) on the oracle's own operator build of the
+    same L256 scene: neither the scene, nor the operator, nor the stepping
+    touches the engine library."""
     if rank != 0:
         return
-    sc, op, cop, setup = build_workload()
     threads = os.cpu_count() or 1
     import oracle
+    op = oracle_operator("l256", threads)
+    nodes = op.num_lines[0] * op.num_lines[1] * op.num_lines[2]
     per_step = max(4, args.ref_timesteps)
     for _ in range(args.warmup):
         oracle.run(op.desc, [], per_step, 0, engine=oracle.SSE_COMPRESSED_MT, threads=threads, energy=False,
@@ -189,15 +244,16 @@ def run_reference(args, rank, world):
         r = oracle.run(op.desc, [], per_step, 0, engine=oracle.SSE_COMPRESSED_MT, threads=threads, energy=False,
                        fields=False)
         tot += r["seconds"]
-    value = op.num_nodes * per_step * args.steps / tot / 1e6
+    value = nodes * per_step * args.steps / tot / 1e6
     line = {"metric": "Mcell-updates/s", "value": round(value, 2), "unit": "Mcell-updates/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(tot / args.steps * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "impl": "reference",
-            "config": config_dict(op, cop, {"cpu_timesteps_per_step": per_step}),
+            "config": config_dict(op.num_lines),
             "cpu_baseline": {"value": round(value, 2), "unit": "Mcell-updates/s", "cores": threads, "kind": "port",
                              "sample": f"{per_step} timesteps of L256 per step (restated SSE-compressed "
-                                       f"x-slab multithreaded engine)"},
+                                       f"x-slab multithreaded engine on the oracle's operator build); the rate "
+                                       f"is per timestep, so the step count does not change it"},
             "e2e": {"value": round(value, 2), "unit": "Mcell-updates/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -296,16 +352,16 @@ def run_gpu(args, rank, world, local_rank):
 
     if rank == 0:
         threads = os.cpu_count() or 1
-        cpu_v, cpu_n, cpu_s = cpu_baseline(op, threads)
+        cpu = cpu_baseline(threads)
         line = {"metric": "Mcell-updates/s", "value": round(value, 2), "unit": "Mcell-updates/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dev_s / args.steps * 1e3, 3),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic", "config": config_dict(op, cop, {**setup, "wall_s": round(wall, 3)}),
+                "data": "synthetic", "config": config_dict(op.num_lines),
+                "engine": {**setup, "wall_s": round(wall, 3), "upml_nodes": cop.info["num_upml_nodes"],
+                           "tuples_e": cop.info["num_tuples_e"], "tuples_h": cop.info["num_tuples_h"],
+                           "index_bytes": cop.info["index_bytes_e"]},
                 "roofline": roofline,
-                "cpu_baseline": {"value": round(cpu_v, 2), "unit": "Mcell-updates/s", "cores": threads,
-                                 "kind": "port",
-                                 "sample": f"{cpu_n} timesteps of L256 ({cpu_s:.1f} s) with the restated "
-                                           f"SSE-compressed x-slab multithreaded engine"},
+                "cpu_baseline": cpu,
                 "e2e": {"value": round(e2e_value, 2), "unit": "Mcell-updates/s",
                         "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h // e2e_steps),
                         "steps": e2e_steps},

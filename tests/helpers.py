@@ -186,3 +186,55 @@ def dump_reference(V, I, lines, unit, field, interp, start, stop, step):
                                 o = rawH(n, p) * (1.0 - rel) + rawH(n, q) * rel
                     out[n, i, j, k] = o
     return out
+
+
+def assert_same_operator(prod_op, ref_op):
+    """The product's operator build and the oracle's independent one agree
+    bit for bit: every coefficient array, UPML slab, ADE list, excitation
+    list and signal, Mur face, RLC list, dT, the probe interval and every
+    snapped probe."""
+    import oracle
+    a = oracle.desc_arrays(prod_op.desc)
+    b = oracle.desc_arrays(ref_op.desc)
+    assert sorted(a) == sorted(b), (sorted(set(a) ^ set(b)))
+    bad = []
+    for k in a:
+        x, y = a[k], b[k]
+        if x.shape != y.shape:
+            bad.append((k, "shape", x.shape, y.shape))
+            continue
+        if x.dtype.kind == "f":
+            w = np.uint32 if x.dtype == np.float32 else np.uint64
+            neq = x.view(w) != y.view(w)
+        else:
+            neq = x != y
+        if neq.any():
+            i = np.nonzero(neq)[0]
+            bad.append((k, int(neq.sum()), i[:4].tolist(), x[i[:2]].tolist(), y[i[:2]].tolist()))
+    assert not bad, bad
+    assert prod_op.dT == ref_op.dT
+    assert prod_op.probe_interval == ref_op.probe_interval
+    assert prod_op.nyquist == ref_op.nyquist
+    assert oracle.probe_tuples(prod_op.probes) == oracle.probe_tuples(ref_op.probes)
+
+
+def oracle_operator(prod_op, threads: int = 0):
+    """The oracle's own operator build of the scene `prod_op` was built from,
+    checked bitwise against `prod_op`.  Parity tests run the oracle on this
+    one, so no parity check rests on the product's operator build."""
+    import oracle
+    ref = oracle.Operator(prod_op.scene.spec, threads=threads)
+    assert_same_operator(prod_op, ref)
+    return ref
+
+
+def oracle_inputs(prod_op):
+    """(desc, probes) of the oracle's own operator build of prod_op's scene,
+    checked bitwise against prod_op (built once, kept alive with prod_op):
+    what the parity tests hand to oracle.run."""
+    import os
+    ref = getattr(prod_op, "_oracle_op", None)
+    if ref is None:
+        ref = oracle_operator(prod_op, threads=os.cpu_count() or 1)
+        prod_op._oracle_op = ref
+    return ref.desc, ref.probes

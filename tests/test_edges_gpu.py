@@ -10,6 +10,7 @@ import oracle
 from wipems_gb300 import Engine, Operator, Scene
 from wipems_gb300.fdtd import BC_PEC, BC_PMC
 
+from helpers import oracle_inputs
 from test_parity_gpu import compare
 
 pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("libs")]
@@ -44,7 +45,7 @@ def _thin(n, pmc_faces=(), steps=200):
 @pytest.mark.parametrize("kernel", ["tma", "direct"])
 def test_thin_and_ragged_grids_match_oracle(n, pmc, kernel):
     op = Operator(_thin(n, pmc))
-    ref = oracle.run(op.desc, op.probes, 200, op.probe_interval, engine=oracle.BASIC)
+    ref = oracle.run(*oracle_inputs(op), 200, op.probe_interval, engine=oracle.BASIC)
     eng = Engine(op, kernel=kernel)
     eng.iterate(200)
     compare(op, eng, ref)

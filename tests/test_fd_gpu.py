@@ -10,6 +10,8 @@ import oracle
 from wipems_gb300 import Engine, Operator, scenes
 from wipems_gb300.ports import lumped_port_fd, lumped_port_td
 
+from helpers import oracle_inputs
+
 pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("libs")]
 
 
@@ -25,7 +27,7 @@ def test_fd_accumulation_matches_oracle_dft(kind, graphs):
     eng.iterate(250)
     eng.iterate(n - 250)
     got, count = eng.fd_results()
-    ref = oracle.run(op.desc, op.probes, n, fdint, engine=oracle.SSE_COMPRESSED_MT, threads=os.cpu_count())
+    ref = oracle.run(*oracle_inputs(op), n, fdint, engine=oracle.SSE_COMPRESSED_MT, threads=os.cpu_count())
     assert count == len(ref["ts"]) == n // fdint + 1
     dual = np.array([0.5 if p.type == 1 else 0.0 for p in op.probes])
     t = (ref["ts"][:, None] + dual[None, :]) * op.dT                  # [sample][probe]

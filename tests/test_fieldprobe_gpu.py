@@ -11,6 +11,7 @@ import pytest
 import oracle
 from wipems_gb300 import Batch, CompressedOperator, Engine, Operator, scenes
 
+from helpers import oracle_inputs
 from test_parity_gpu import compare
 
 pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("libs")]
@@ -75,7 +76,7 @@ def test_field_probe_frequency_domain():
     fdint = eng.fd_interval
     eng.iterate(600)
     got, count = eng.fd_results()
-    ref = oracle.run(op.desc, op.probes, 600, fdint, engine=oracle.BASIC)
+    ref = oracle.run(*oracle_inputs(op), 600, fdint, engine=oracle.BASIC)
     assert count == len(ref["ts"])
     dual = np.array([0.5 if t in (1, 3) else 0.0 for t in eng.probe_types])
     t = (ref["ts"][:, None] + dual[None, :]) * op.dT

@@ -16,7 +16,7 @@ import pytest
 import oracle
 from wipems_gb300 import Operator, scenes
 
-from helpers import cavity_check
+from helpers import cavity_check, oracle_inputs
 
 pytestmark = pytest.mark.usefixtures("libs")
 GOLDEN = Path(__file__).resolve().parent / "golden"
@@ -25,8 +25,8 @@ GOLDEN = Path(__file__).resolve().parent / "golden"
 @pytest.mark.parametrize("kind", ["pec", "upml", "drude", "lorentz", "mixed", "mur", "rlc", "rlc_mur"])
 def test_basic_and_sse_compressed_engines_agree_bitwise(kind):
     op = Operator(scenes.mini(kind, nr_ts=200))
-    a = oracle.run(op.desc, op.probes, 150, op.probe_interval, engine=oracle.BASIC)
-    b = oracle.run(op.desc, op.probes, 150, op.probe_interval, engine=oracle.SSE_COMPRESSED_MT, threads=3)
+    a = oracle.run(*oracle_inputs(op), 150, op.probe_interval, engine=oracle.BASIC)
+    b = oracle.run(*oracle_inputs(op), 150, op.probe_interval, engine=oracle.SSE_COMPRESSED_MT, threads=3)
     assert np.array_equal(a["volt"].view(np.uint32), b["volt"].view(np.uint32))
     assert np.array_equal(a["curr"].view(np.uint32), b["curr"].view(np.uint32))
     assert np.array_equal(a["values"], b["values"])
@@ -36,7 +36,7 @@ def test_basic_and_sse_compressed_engines_agree_bitwise(kind):
 def test_cavity_resonances_within_reference_limits():
     sc = scenes.cavity(nr_ts=20000)
     op = Operator(sc)
-    r = oracle.run(op.desc, op.probes, 20000, 1, engine=oracle.SSE_COMPRESSED_MT, threads=8, energy=False,
+    r = oracle.run(*oracle_inputs(op), 20000, 1, engine=oracle.SSE_COMPRESSED_MT, threads=8, energy=False,
                    fields=False)
     t = r["ts"] * op.dT
     res = cavity_check([t] * 3, [r["values"][:, k] for k in range(3)], sc.meta)
@@ -50,7 +50,7 @@ def test_golden_fixtures(name):
     kind, nsteps = meta["scene"], meta["steps"]
     sc = scenes.p64(nr_ts=meta["nr_ts"]) if kind == "p64" else scenes.mini(kind, nr_ts=meta["nr_ts"])
     op = Operator(sc)
-    r = oracle.run(op.desc, op.probes, nsteps, op.probe_interval, engine=oracle.BASIC)
+    r = oracle.run(*oracle_inputs(op), nsteps, op.probe_interval, engine=oracle.BASIC)
     assert np.array_equal(r["values"], data["values"])
     assert np.array_equal(r["energy"], data["energy"])
     crc = int(np.bitwise_xor.reduce(r["volt"].view(np.uint32).ravel()))
@@ -69,13 +69,13 @@ def test_mur_boundaries_absorb():
     # vacuum at the face, uniform 0.5 mm mesh: c = (c0 dT - d) / (c0 dT + d)
     c0t = 299792458.0 * op.dT
     assert abs(m.coef_p[0] - (c0t - 0.5e-3) / (c0t + 0.5e-3)) < 1e-7
-    r = oracle.run(op.desc, op.probes, 900, op.probe_interval, engine=oracle.BASIC, fields=False)
+    r = oracle.run(*oracle_inputs(op), 900, op.probe_interval, engine=oracle.BASIC, fields=False)
     e = r["energy"]
     assert e[-1] < 1e-3 * e.max()
     sc = scenes.mini("mur", nr_ts=900)
     sc.set_boundary([BC_PEC] * 6, [0] * 6)
     op2 = Operator(sc)
-    r2 = oracle.run(op2.desc, op2.probes, 900, op2.probe_interval, engine=oracle.BASIC, fields=False)
+    r2 = oracle.run(*oracle_inputs(op2), 900, op2.probe_interval, engine=oracle.BASIC, fields=False)
     assert e[-1] / e.max() < 0.01 * r2["energy"][-1] / r2["energy"].max()
 
 
@@ -91,7 +91,7 @@ def test_oracle_field_probes_are_field_over_edge_length():
     pe, ph = op.probes[-2], op.probes[-1]
     assert pe.enabled and ph.enabled and list(pe.start) == [10, 12, 18] and list(ph.start) == [14, 8, 24]
     n = 4 * op.probe_interval
-    r = oracle.run(op.desc, op.probes, n, op.probe_interval, engine=oracle.BASIC)
+    r = oracle.run(*oracle_inputs(op), n, op.probe_interval, engine=oracle.BASIC)
     assert r["values"].shape[1] == len(op.probes) - 2 + 6
     lines = [np.ctypeslib.as_array(op.desc.lines[a], shape=(op.num_lines[a],)) for a in range(3)]
     for c in range(3):

@@ -14,7 +14,7 @@ import pytest
 import oracle
 from wipems_gb300 import CompressedOperator, Engine, Operator, scenes
 
-from helpers import cavity_check, rel_l2, rel_max
+from helpers import cavity_check, oracle_inputs, rel_l2, rel_max
 
 pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("libs")]
 
@@ -50,7 +50,7 @@ def test_mini_scenes_match_oracle(kind, kernel):
     geometry): within the probe / field tolerance of the oracle on the
     operator's own coefficients."""
     op = Operator(scenes.mini(kind, nr_ts=400))
-    ref = oracle.run(op.desc, op.probes, 400, op.probe_interval, engine=oracle.BASIC)
+    ref = oracle.run(*oracle_inputs(op), 400, op.probe_interval, engine=oracle.BASIC)
     cop = CompressedOperator(op)
     eng = Engine(cop, kernel=kernel)
     eng.iterate(400)
@@ -78,7 +78,7 @@ def test_factorized_kernels_bitwise_against_expanded_operator(kind):
 def test_exact_mode_on_graded_mesh_is_bitwise():
     op = Operator(scenes.mini("mixed", nr_ts=200))
     cop = CompressedOperator(op, mode="exact")
-    ref = oracle.run(op.desc, op.probes, 200, op.probe_interval, engine=oracle.BASIC)
+    ref = oracle.run(*oracle_inputs(op), 200, op.probe_interval, engine=oracle.BASIC)
     eng = Engine(cop)
     eng.iterate(200)
     compare(op, eng, ref, bitwise=True)
@@ -86,7 +86,7 @@ def test_exact_mode_on_graded_mesh_is_bitwise():
 
 def test_p64_full_2000_steps():
     op = Operator(scenes.p64(nr_ts=2000))
-    ref = oracle.run(op.desc, op.probes, 2000, op.probe_interval, engine=oracle.SSE_COMPRESSED_MT,
+    ref = oracle.run(*oracle_inputs(op), 2000, op.probe_interval, engine=oracle.SSE_COMPRESSED_MT,
                      threads=os.cpu_count())
     eng = Engine(op)
     eng.iterate(2000)
@@ -136,7 +136,7 @@ def test_reset_and_compressed_upload_reproduce():
 def test_l256_full_size_first_steps_bitwise():
     op = Operator(scenes.l256(nr_ts=1000))
     n = 18
-    ref = oracle.run(op.desc, op.probes, n, op.probe_interval, engine=oracle.SSE_COMPRESSED_MT,
+    ref = oracle.run(*oracle_inputs(op), n, op.probe_interval, engine=oracle.SSE_COMPRESSED_MT,
                      threads=os.cpu_count())
     eng = Engine(op)
     st = eng.stats()
@@ -151,7 +151,7 @@ def test_d192_full_size_first_steps():
     the exact-table engine (uint32 index) bit-identical to the oracle."""
     op = Operator(scenes.d192(nr_ts=3000))
     n = 40
-    ref = oracle.run(op.desc, op.probes, n, op.probe_interval, engine=oracle.SSE_COMPRESSED_MT,
+    ref = oracle.run(*oracle_inputs(op), n, op.probe_interval, engine=oracle.SSE_COMPRESSED_MT,
                      threads=os.cpu_count())
     cop = CompressedOperator(op)
     assert cop.info["geometry_factored"] == 1 and cop.info["num_ade_nodes"] > 0
@@ -184,7 +184,7 @@ def test_field_access_and_energy():
     V, I = eng.fields()
     assert eng.get_volt(2, 10, 8, 18) == V[2, 10, 8, 18]
     assert eng.get_curr(1, 5, 6, 7) == I[1, 5, 6, 7]
-    ref = oracle.run(op.desc, [], 60, 0, engine=oracle.BASIC)
+    ref = oracle.run(oracle_inputs(op)[0], [], 60, 0, engine=oracle.BASIC)
     eps0, mue0 = 8.85418781762e-12, 1.256637062e-6
     Vr, Ir = ref["volt"][:, :-1, :-1, :-1].astype(np.float64), ref["curr"][:, :-1, :-1, :-1].astype(np.float64)
     e_ref = eps0 * np.sum(Vr * Vr) + mue0 * np.sum(Ir * Ir)
@@ -198,7 +198,7 @@ def test_fused_kernel_matches_oracle(kind):
     bit-identical to the reference stepping, across odd tile edges."""
     op = Operator(scenes.mini(kind, nr_ts=400))
     n = 301
-    ref = oracle.run(op.desc, op.probes, n, op.probe_interval, engine=oracle.BASIC)
+    ref = oracle.run(*oracle_inputs(op), n, op.probe_interval, engine=oracle.BASIC)
     eng = Engine(op, kernel="fused")
     assert eng.stats()["kernel"] == 2
     eng.iterate(137)
@@ -208,7 +208,7 @@ def test_fused_kernel_matches_oracle(kind):
 
 def test_fused_kernel_tilings_and_graphs_invisible():
     op = Operator(scenes.mini("upml", seed=2, nr_ts=400))
-    ref = oracle.run(op.desc, op.probes, 120, op.probe_interval, engine=oracle.BASIC)
+    ref = oracle.run(*oracle_inputs(op), 120, op.probe_interval, engine=oracle.BASIC)
     for kw in (dict(x_chunk=1), dict(x_chunk=3, stages=4), dict(x_chunk=16, use_graphs=False), dict(stages=5)):
         eng = Engine(op, kernel="fused", **kw)
         eng.iterate(57)
@@ -223,12 +223,12 @@ def test_fused_kernel_graded_exact_and_p64():
     owned by the tiles below them)."""
     op = Operator(scenes.mini("graded", nr_ts=400))
     cop = CompressedOperator(op, mode="exact")
-    ref = oracle.run(op.desc, op.probes, 200, op.probe_interval, engine=oracle.BASIC)
+    ref = oracle.run(*oracle_inputs(op), 200, op.probe_interval, engine=oracle.BASIC)
     eng = Engine(cop, kernel="fused")
     eng.iterate(200)
     compare(op, eng, ref)
     op = Operator(scenes.p64(nr_ts=2000))
-    ref = oracle.run(op.desc, op.probes, 700, op.probe_interval, engine=oracle.SSE_COMPRESSED_MT,
+    ref = oracle.run(*oracle_inputs(op), 700, op.probe_interval, engine=oracle.SSE_COMPRESSED_MT,
                      threads=os.cpu_count())
     eng = Engine(op, kernel="fused")
     eng.iterate(700)
@@ -241,7 +241,7 @@ def test_fused_kernel_graded_exact_and_p64():
 def test_fused_kernel_l256_first_steps_bitwise():
     op = Operator(scenes.l256(nr_ts=1000))
     n = 18
-    ref = oracle.run(op.desc, op.probes, n, op.probe_interval, engine=oracle.SSE_COMPRESSED_MT,
+    ref = oracle.run(*oracle_inputs(op), n, op.probe_interval, engine=oracle.SSE_COMPRESSED_MT,
                      threads=os.cpu_count())
     eng = Engine(op, kernel="fused")
     eng.iterate(n)
@@ -261,7 +261,7 @@ def test_mur_chunking_graphs_and_excitation_on_the_face():
     carries an excitation (active only after the pulse, start_ts), match
     the reference stepping bit for bit."""
     op = Operator(scenes.mini("mur", seed=1, nr_ts=700))
-    ref = oracle.run(op.desc, op.probes, 333, op.probe_interval, engine=oracle.BASIC)
+    ref = oracle.run(*oracle_inputs(op), 333, op.probe_interval, engine=oracle.BASIC)
     for kw in (dict(), dict(use_graphs=False, x_chunk=3)):
         eng = Engine(op, **kw)
         eng.iterate(100)
@@ -280,7 +280,7 @@ def test_mur_chunking_graphs_and_excitation_on_the_face():
     op = Operator(s)
     assert op.desc.mur[0].start_ts > 0
     n = op.desc.mur[0].start_ts + 60
-    ref = oracle.run(op.desc, op.probes, n, op.probe_interval, engine=oracle.BASIC)
+    ref = oracle.run(*oracle_inputs(op), n, op.probe_interval, engine=oracle.BASIC)
     eng = Engine(op)
     eng.iterate(n)
     compare(op, eng, ref)
@@ -292,7 +292,7 @@ def test_rlc_through_graph_chunks_and_single_steps():
     reproduce the reference's pointer rotation bit for bit; the fused
     single-pass kernel refuses RLC elements."""
     op = Operator(scenes.mini("rlc_mur", seed=1, nr_ts=700))
-    ref = oracle.run(op.desc, op.probes, 333, op.probe_interval, engine=oracle.BASIC)
+    ref = oracle.run(*oracle_inputs(op), 333, op.probe_interval, engine=oracle.BASIC)
     for kw, chunks in ((dict(), [100, 233]), (dict(use_graphs=False, x_chunk=3), [1, 2, 330]),
                        (dict(kernel="direct"), [333])):
         eng = Engine(op, **kw)

@@ -22,6 +22,8 @@ from wipems_gb300._abi import FdtdError
 from wipems_gb300.fdtd import BC_PEC
 from wipems_gb300.ports import dft_time2freq
 
+from helpers import oracle_inputs
+
 pytestmark = pytest.mark.usefixtures("libs")
 
 EPS0 = 8.85418781762e-12
@@ -30,7 +32,7 @@ EPS0 = 8.85418781762e-12
 def _impedance(series, R, L, Cap, f0, fc, steps=8000):
     op = Operator(scenes.rlc_probe(series, R, L, Cap, nr_ts=steps, f0=f0, fc=fc))
     assert op.desc.rlc and op.desc.rlc.contents.count == 1
-    r = oracle.run(op.desc, op.probes, steps, 1, engine=oracle.SSE_COMPRESSED_MT, threads=8, fields=False)
+    r = oracle.run(*oracle_inputs(op), steps, 1, engine=oracle.SSE_COMPRESSED_MT, threads=8, fields=False)
     t = r["ts"] * op.dT
     dv = np.diff(r["values"][:, 0])
     di = np.diff(r["values"][:, 1])

@@ -6,7 +6,7 @@ on-device probes runs in hand-written sm_103a CUDA kernels
 operator build (csrc/operator.cpp) restates openEMS's Operator.
 """
 from .fdtd import (BC_PEC, BC_PMC, BC_PML, C0, EPS0, MUE0, Batch, CompressedOperator, Engine, Operator, Samples,
-                   Scene, Server, run_fdtd)
+                   Scene, SceneSpec, Server, run_fdtd)
 
-__all__ = ["Scene", "Operator", "CompressedOperator", "Batch", "Server", "Engine", "Samples", "run_fdtd", "BC_PEC", "BC_PMC", "BC_PML", "EPS0", "MUE0",
+__all__ = ["Scene", "SceneSpec", "Operator", "CompressedOperator", "Batch", "Server", "Engine", "Samples", "run_fdtd", "BC_PEC", "BC_PMC", "BC_PML", "EPS0", "MUE0",
            "C0"]

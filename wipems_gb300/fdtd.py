@@ -1,7 +1,8 @@
 """Host-side mirror of openEMS's Operator / Engine interface for the CUDA engine.
 
     Scene     ContinuousStructure + the <FDTD> setup (mesh, boxes, boundary
-              conditions, Gaussian excitation, probes).
+              conditions, Gaussian excitation, probes); SceneSpec is the
+              same scene as plain data, without native code.
     Operator  Operator::CalcECOperator (FDTD/operator.cpp:973-1084) with the
               excitation, UPML and Lorentz extension builds, run in C++.
     Engine    Engine_CUDA: IterateTS / GetNumberOfTimesteps / GetVolt /
@@ -34,101 +35,62 @@ def _d3(v) -> C.Array:
     return a
 
 
-class Scene:
-    """Mesh + primitives; the stand-in for CSXCAD: rectilinear mesh lines and
-    priority-ordered axis-aligned boxes of material, metal, lumped elements,
-    excitations and probes."""
+class SceneSpec:
+    """A scene as plain data: the recorder of the Scene calls (mesh lines,
+    background, boundaries, pulse, boxes) in call order, with no native
+    code.  `spec` is what an independent operator build (a checker) reads;
+    Scene adds the native scene of the engine library on top."""
 
     def __init__(self, lines_x, lines_y, lines_z, unit: float):
         self._lines = [np.ascontiguousarray(l, dtype=np.float64) for l in (lines_x, lines_y, lines_z)]
-        h = C.c_void_p()
-        L = lib()
-        ptr = [l.ctypes.data_as(C.POINTER(C.c_double)) for l in self._lines]
-        check(L.fdtd_scene_create(ptr[0], len(self._lines[0]), ptr[1], len(self._lines[1]), ptr[2],
-                                  len(self._lines[2]), float(unit), C.byref(h)), "fdtd_scene_create")
-        self._h = h
         self.unit = unit
         self.nr_ts = 0
         self.probes: list[dict] = []
         self.meta: dict = {}
-
-    @classmethod
-    def from_xml(cls, xml: str) -> "Scene":
-        """A scene from an openEMS XML document (the text, or a path to the
-        file): the subset fdtd_scene_load_xml covers.  The run settings are
-        in .xml_info (nr_ts, end_crit, ...)."""
-        h = C.c_void_p()
-        inf = _abi.FdtdXmlInfo()
-        if "<" in xml:
-            check(lib().fdtd_scene_load_xml(xml.encode(), C.byref(h), C.byref(inf)), "fdtd_scene_load_xml")
-        else:
-            check(lib().fdtd_scene_load_xml_file(str(xml).encode(), C.byref(h), C.byref(inf)),
-                  "fdtd_scene_load_xml_file")
-        s = cls.__new__(cls)
-        s._h = h
-        s._lines = None
-        s.unit = None
-        s.nr_ts = int(inf.nr_ts)
-        s.probes = []
-        s.meta = {}
-        s.xml_info = {k: getattr(inf, k) for k, _ in inf._fields_}
-        return s
+        self.spec: dict | None = dict(lines=[l.copy() for l in self._lines], unit=float(unit),
+                                      background=(1.0, 1.0, 0.0, 0.0), bc=[0] * 6, pml_size=[0] * 6,
+                                      mur_vph=[0.0] * 6, f0=0.0, fc=0.0, nr_ts=0, oversampling=4, prims=[])
 
     @property
     def lines(self):
         return self._lines
 
-    def dumps(self) -> list:
-        """The time-domain E / H field dumps of the scene (XML <DumpBox>):
-        dicts of name, field ("E"/"H"), interp, file_type, start, stop (drawing
-        units) and step, for wipems_gb300.dumps.FieldDump.from_spec."""
-        n = C.c_uint32()
-        check(lib().fdtd_scene_num_dumps(self._h, C.byref(n)), "fdtd_scene_num_dumps")
-        out = []
-        for k in range(n.value):
-            d = _abi.FdtdSceneDump()
-            check(lib().fdtd_scene_get_dump(self._h, k, C.byref(d)), "fdtd_scene_get_dump")
-            out.append(dict(name=d.name.decode(), field="EH"[d.field], interp=("none", "node", "cell")[d.interp],
-                            file_type=d.file_type, start=list(d.start), stop=list(d.stop), step=list(d.step)))
-        return out
+    def _record(self, **kv):
+        if self.spec is not None:
+            self.spec.update(kv)
 
-    def __del__(self):
-        if getattr(self, "_h", None):
-            try:
-                lib().fdtd_scene_destroy(self._h)
-            except Exception:
-                pass
-            self._h = None
+    def _prim(self, kind, priority, start, stop, **kv):
+        if self.spec is not None:
+            self.spec["prims"].append(dict(kind=kind, priority=int(priority), start=[float(v) for v in start],
+                                           stop=[float(v) for v in stop], **kv))
 
     def set_background(self, eps_r=1.0, mue_r=1.0, kappa=0.0, sigma=0.0):
-        check(lib().fdtd_scene_set_background(self._h, eps_r, mue_r, kappa, sigma), "set_background")
+        self._record(background=(float(eps_r), float(mue_r), float(kappa), float(sigma)))
 
     def set_boundary(self, bc, pml_size=(0,) * 6):
-        b = (C.c_int * 6)(*bc)
-        s = (C.c_uint32 * 6)(*pml_size)
-        check(lib().fdtd_scene_set_boundary(self._h, b, s), "set_boundary")
+        self._record(bc=[int(x) for x in bc], pml_size=[int(x) for x in pml_size])
 
     def set_mur_velocity(self, v_phase):
         """Mur phase velocity per face (m/s, 0 = from the boundary material)."""
-        check(lib().fdtd_scene_set_mur_velocity(self._h, (C.c_double * 6)(*v_phase)), "set_mur_velocity")
+        self._record(mur_vph=[float(x) for x in v_phase])
 
     def set_gauss_excite(self, f0: float, fc: float, nr_ts: int):
         self.nr_ts = int(nr_ts)
-        check(lib().fdtd_scene_set_gauss_excite(self._h, f0, fc, int(nr_ts)), "set_gauss_excite")
+        self._record(f0=float(f0), fc=float(fc), nr_ts=int(nr_ts))
 
     def set_oversampling(self, os_: int):
-        check(lib().fdtd_scene_set_oversampling(self._h, int(os_)), "set_oversampling")
+        self._record(oversampling=int(os_))
 
     def add_material(self, start, stop, eps_r=1.0, kappa=0.0, mue_r=1.0, sigma=0.0, priority=0):
-        check(lib().fdtd_scene_add_material(self._h, int(priority), _d3(start), _d3(stop), eps_r, kappa, mue_r,
-                                            sigma), "add_material")
+        self._prim("material", priority, start, stop, eps=float(eps_r), kappa=float(kappa), mue=float(mue_r),
+                   sigma=float(sigma))
 
     def add_metal(self, start, stop, priority=0):
-        check(lib().fdtd_scene_add_metal(self._h, int(priority), _d3(start), _d3(stop)), "add_metal")
+        self._prim("metal", priority, start, stop)
 
     def add_lumped(self, start, stop, direction, R=-1.0, Cap=-1.0, caps=True, priority=0):
-        check(lib().fdtd_scene_add_lumped(self._h, int(priority), _d3(start), _d3(stop), int(direction), float(R),
-                                          float(Cap), int(bool(caps))), "add_lumped")
+        self._prim("lumped", priority, start, stop, ny=int(direction), le_type=0, R=float(R), C=float(Cap), L=-1.0,
+                   caps=int(bool(caps)))
 
     def add_lumped_rlc(self, start, stop, direction, R=-1.0, L=-1.0, Cap=-1.0, series=False, caps=True, priority=0,
                        le_type=None):
@@ -138,25 +100,23 @@ class Scene:
         given".  le_type overrides series with the raw LEtype (-1 invalid:
         the element is ignored, as the reference ignores it)."""
         t = (1 if series else 0) if le_type is None else int(le_type)
-        check(lib().fdtd_scene_add_lumped_rlc(self._h, int(priority), _d3(start), _d3(stop), int(direction), t,
-                                              float(R), float(L), float(Cap), int(bool(caps))), "add_lumped_rlc")
+        self._prim("lumped", priority, start, stop, ny=int(direction), le_type=t, R=float(R), C=float(Cap),
+                   L=float(L), caps=int(bool(caps)))
 
     def add_excitation(self, start, stop, vec, exc_type=0, delay=0.0, priority=0):
-        check(lib().fdtd_scene_add_excitation(self._h, int(priority), _d3(start), _d3(stop), int(exc_type),
-                                              _d3(vec), float(delay)), "add_excitation")
+        self._prim("excitation", priority, start, stop, exc_type=int(exc_type), exc_vec=[float(v) for v in vec],
+                   delay=float(delay))
 
     def add_lorentz(self, start, stop, eps_r=1.0, kappa=0.0, mue_r=1.0, sigma=0.0, plasma_f=(), relax_t=(),
                     pole_f=(), priority=0):
         order = len(plasma_f)
-        pf = (C.c_double * max(order, 1))(*plasma_f)
-        rt = (C.c_double * max(order, 1))(*(relax_t or [0.0] * order))
-        lp = (C.c_double * max(order, 1))(*(pole_f or [0.0] * order))
-        check(lib().fdtd_scene_add_lorentz(self._h, int(priority), _d3(start), _d3(stop), eps_r, kappa, mue_r, sigma,
-                                           order, pf, rt, lp), "add_lorentz")
+        self._prim("material", priority, start, stop, eps=float(eps_r), kappa=float(kappa), mue=float(mue_r),
+                   sigma=float(sigma), disp_order=order, eps_plasma_f=[float(v) for v in plasma_f],
+                   eps_relax_t=[float(v) for v in (relax_t or [0.0] * order)],
+                   eps_pole_f=[float(v) for v in (pole_f or [0.0] * order)])
 
     def add_probe(self, start, stop, ptype: int, weight=1.0, norm_dir=-1, name=""):
-        check(lib().fdtd_scene_add_probe(self._h, int(ptype), _d3(start), _d3(stop), float(weight), int(norm_dir)),
-              "add_probe")
+        self._prim("probe", 0, start, stop, probe_type=int(ptype), weight=float(weight), norm_dir=int(norm_dir))
         self.probes.append(dict(name=name or f"probe{len(self.probes)}", type=ptype))
 
     def add_lumped_port(self, start, stop, direction, R, excite=1.0, priority=5, name="port"):
@@ -188,10 +148,170 @@ class Scene:
         self.add_probe(i_start, i_stop, 1, weight=sign, norm_dir=ny, name=name + "_it")
 
 
+class Scene(SceneSpec):
+    """Mesh + primitives; the stand-in for CSXCAD: rectilinear mesh lines and
+    priority-ordered axis-aligned boxes of material, metal, lumped elements,
+    excitations and probes, held by the engine library (fdtd_scene_*), which
+    checks every call; the calls are also recorded as plain data (`spec`)."""
+
+    def __init__(self, lines_x, lines_y, lines_z, unit: float):
+        super().__init__(lines_x, lines_y, lines_z, unit)
+        h = C.c_void_p()
+        ptr = [l.ctypes.data_as(C.POINTER(C.c_double)) for l in self._lines]
+        check(lib().fdtd_scene_create(ptr[0], len(self._lines[0]), ptr[1], len(self._lines[1]), ptr[2],
+                                      len(self._lines[2]), float(unit), C.byref(h)), "fdtd_scene_create")
+        self._h = h
+
+    @classmethod
+    def from_spec(cls, spec: "SceneSpec") -> "Scene":
+        """The native scene of a recorded one (replays its calls)."""
+        d = spec.spec
+        s = cls(*d["lines"], d["unit"])
+        s.set_background(*d["background"])
+        s.set_boundary(d["bc"], d["pml_size"])
+        if any(d["mur_vph"]):
+            s.set_mur_velocity(d["mur_vph"])
+        if d["fc"] > 0:
+            s.set_gauss_excite(d["f0"], d["fc"], d["nr_ts"])
+        if d["oversampling"] != 4:
+            s.set_oversampling(d["oversampling"])
+        for p in d["prims"]:
+            k = p["kind"]
+            a, b, pr = p["start"], p["stop"], p["priority"]
+            if k == "material" and p.get("disp_order", 0) > 0:
+                s.add_lorentz(a, b, p["eps"], p["kappa"], p["mue"], p["sigma"], p["eps_plasma_f"], p["eps_relax_t"],
+                              p["eps_pole_f"], priority=pr)
+            elif k == "material":
+                s.add_material(a, b, p["eps"], p["kappa"], p["mue"], p["sigma"], priority=pr)
+            elif k == "metal":
+                s.add_metal(a, b, priority=pr)
+            elif k == "lumped":
+                s.add_lumped_rlc(a, b, p["ny"], R=p["R"], L=p["L"], Cap=p["C"], caps=p["caps"], priority=pr,
+                                 le_type=p["le_type"])
+            elif k == "excitation":
+                s.add_excitation(a, b, p["exc_vec"], p["exc_type"], p["delay"], priority=pr)
+            elif k == "probe":
+                s.add_probe(a, b, p["probe_type"], p["weight"], p["norm_dir"])
+        s.probes = list(spec.probes)
+        s.meta = dict(spec.meta)
+        s.nr_ts = spec.nr_ts
+        return s
+
+    @classmethod
+    def from_xml(cls, xml: str) -> "Scene":
+        """A scene from an openEMS XML document (the text, or a path to the
+        file): the subset fdtd_scene_load_xml covers.  The run settings are
+        in .xml_info (nr_ts, end_crit, ...)."""
+        h = C.c_void_p()
+        inf = _abi.FdtdXmlInfo()
+        if "<" in xml:
+            check(lib().fdtd_scene_load_xml(xml.encode(), C.byref(h), C.byref(inf)), "fdtd_scene_load_xml")
+        else:
+            check(lib().fdtd_scene_load_xml_file(str(xml).encode(), C.byref(h), C.byref(inf)),
+                  "fdtd_scene_load_xml_file")
+        s = cls.__new__(cls)
+        s._h = h
+        s._lines = None
+        s.unit = None
+        s.nr_ts = int(inf.nr_ts)
+        s.probes = []
+        s.meta = {}
+        s.spec = None
+        s.xml_info = {k: getattr(inf, k) for k, _ in inf._fields_}
+        return s
+
+    def dumps(self) -> list:
+        """The time-domain E / H field dumps of the scene (XML <DumpBox>):
+        dicts of name, field ("E"/"H"), interp, file_type, start, stop (drawing
+        units) and step, for wipems_gb300.dumps.FieldDump.from_spec."""
+        n = C.c_uint32()
+        check(lib().fdtd_scene_num_dumps(self._h, C.byref(n)), "fdtd_scene_num_dumps")
+        out = []
+        for k in range(n.value):
+            d = _abi.FdtdSceneDump()
+            check(lib().fdtd_scene_get_dump(self._h, k, C.byref(d)), "fdtd_scene_get_dump")
+            out.append(dict(name=d.name.decode(), field="EH"[d.field], interp=("none", "node", "cell")[d.interp],
+                            file_type=d.file_type, start=list(d.start), stop=list(d.stop), step=list(d.step)))
+        return out
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            try:
+                lib().fdtd_scene_destroy(self._h)
+            except Exception:
+                pass
+            self._h = None
+
+    def set_background(self, eps_r=1.0, mue_r=1.0, kappa=0.0, sigma=0.0):
+        check(lib().fdtd_scene_set_background(self._h, eps_r, mue_r, kappa, sigma), "set_background")
+        super().set_background(eps_r, mue_r, kappa, sigma)
+
+    def set_boundary(self, bc, pml_size=(0,) * 6):
+        b = (C.c_int * 6)(*bc)
+        s = (C.c_uint32 * 6)(*pml_size)
+        check(lib().fdtd_scene_set_boundary(self._h, b, s), "set_boundary")
+        super().set_boundary(bc, pml_size)
+
+    def set_mur_velocity(self, v_phase):
+        check(lib().fdtd_scene_set_mur_velocity(self._h, (C.c_double * 6)(*v_phase)), "set_mur_velocity")
+        super().set_mur_velocity(v_phase)
+
+    def set_gauss_excite(self, f0: float, fc: float, nr_ts: int):
+        check(lib().fdtd_scene_set_gauss_excite(self._h, f0, fc, int(nr_ts)), "set_gauss_excite")
+        super().set_gauss_excite(f0, fc, nr_ts)
+
+    def set_oversampling(self, os_: int):
+        check(lib().fdtd_scene_set_oversampling(self._h, int(os_)), "set_oversampling")
+        super().set_oversampling(os_)
+
+    def add_material(self, start, stop, eps_r=1.0, kappa=0.0, mue_r=1.0, sigma=0.0, priority=0):
+        check(lib().fdtd_scene_add_material(self._h, int(priority), _d3(start), _d3(stop), eps_r, kappa, mue_r,
+                                            sigma), "add_material")
+        super().add_material(start, stop, eps_r, kappa, mue_r, sigma, priority)
+
+    def add_metal(self, start, stop, priority=0):
+        check(lib().fdtd_scene_add_metal(self._h, int(priority), _d3(start), _d3(stop)), "add_metal")
+        super().add_metal(start, stop, priority)
+
+    def add_lumped(self, start, stop, direction, R=-1.0, Cap=-1.0, caps=True, priority=0):
+        check(lib().fdtd_scene_add_lumped(self._h, int(priority), _d3(start), _d3(stop), int(direction), float(R),
+                                          float(Cap), int(bool(caps))), "add_lumped")
+        super().add_lumped(start, stop, direction, R, Cap, caps, priority)
+
+    def add_lumped_rlc(self, start, stop, direction, R=-1.0, L=-1.0, Cap=-1.0, series=False, caps=True, priority=0,
+                       le_type=None):
+        t = (1 if series else 0) if le_type is None else int(le_type)
+        check(lib().fdtd_scene_add_lumped_rlc(self._h, int(priority), _d3(start), _d3(stop), int(direction), t,
+                                              float(R), float(L), float(Cap), int(bool(caps))), "add_lumped_rlc")
+        super().add_lumped_rlc(start, stop, direction, R, L, Cap, series, caps, priority, le_type)
+
+    def add_excitation(self, start, stop, vec, exc_type=0, delay=0.0, priority=0):
+        check(lib().fdtd_scene_add_excitation(self._h, int(priority), _d3(start), _d3(stop), int(exc_type),
+                                              _d3(vec), float(delay)), "add_excitation")
+        super().add_excitation(start, stop, vec, exc_type, delay, priority)
+
+    def add_lorentz(self, start, stop, eps_r=1.0, kappa=0.0, mue_r=1.0, sigma=0.0, plasma_f=(), relax_t=(),
+                    pole_f=(), priority=0):
+        order = len(plasma_f)
+        pf = (C.c_double * max(order, 1))(*plasma_f)
+        rt = (C.c_double * max(order, 1))(*(relax_t or [0.0] * order))
+        lp = (C.c_double * max(order, 1))(*(pole_f or [0.0] * order))
+        check(lib().fdtd_scene_add_lorentz(self._h, int(priority), _d3(start), _d3(stop), eps_r, kappa, mue_r, sigma,
+                                           order, pf, rt, lp), "add_lorentz")
+        super().add_lorentz(start, stop, eps_r, kappa, mue_r, sigma, plasma_f, relax_t, pole_f, priority)
+
+    def add_probe(self, start, stop, ptype: int, weight=1.0, norm_dir=-1, name=""):
+        check(lib().fdtd_scene_add_probe(self._h, int(ptype), _d3(start), _d3(stop), float(weight), int(norm_dir)),
+              "add_probe")
+        super().add_probe(start, stop, ptype, weight, norm_dir, name)
+
+
 class Operator:
     """Operator::CalcECOperator + extension builds, run on the host."""
 
     def __init__(self, scene: Scene, threads: int = 0):
+        if not isinstance(scene, Scene):  # a recorded scene: make its native twin
+            scene = Scene.from_spec(scene)
         h = C.c_void_p()
         check(lib().fdtd_operator_build(scene._h, int(threads), C.byref(h)), "fdtd_operator_build")
         self._h = h

@@ -15,11 +15,32 @@ shapes, sizes and value distributions of the workload it stands for.
 """
 from __future__ import annotations
 
+import contextlib
 import math
 
 import numpy as np
 
-from .fdtd import BC_MUR, BC_PEC, BC_PML, Scene
+from .fdtd import BC_MUR, BC_PEC, BC_PML, Scene, SceneSpec
+
+_native = True
+
+
+@contextlib.contextmanager
+def spec_only():
+    """Inside this block the generators return SceneSpec objects: the same
+    scenes as plain data, built without the engine library (for a checker
+    or a CPU baseline that must not load it).  Not thread-safe."""
+    global _native
+    old = _native
+    _native = False
+    try:
+        yield
+    finally:
+        _native = old
+
+
+def _scene(lx, ly, lz, unit):
+    return (Scene if _native else SceneSpec)(lx, ly, lz, unit)
 
 
 def uniform_lines(cells: int, delta: float) -> np.ndarray:
@@ -54,7 +75,7 @@ def _pick_box(rng, lines, lo_cell, hi_cell, emin, emax):
 def p64(nr_ts: int = 2000) -> Scene:
     """Plain 64^3 PEC vacuum box with one soft Ez edge at the centre."""
     L = uniform_lines(64, 1.0)
-    s = Scene(L, L, L, 1e-3)
+    s = _scene(L, L, L, 1e-3)
     s.set_boundary([BC_PEC] * 6)
     s.set_gauss_excite(5e9, 5e9, nr_ts)
     s.add_excitation([32, 32, 32], [32, 32, 33], [0, 0, 1], exc_type=0)
@@ -69,7 +90,7 @@ def port_scene(cells, delta, pml, n_bricks, seed, f0, fc, nr_ts, eps_max=12.0, k
     rng = np.random.default_rng(seed)
     if lines is None:
         lines = [uniform_lines(c, delta) for c in cells]
-    s = Scene(*lines, 1e-3)
+    s = _scene(*lines, 1e-3)
     bc = [BC_PML if pml else BC_PEC] * 6
     s.set_boundary(bc, [pml] * 6 if pml else [0] * 6)
     s.set_gauss_excite(f0, fc, nr_ts)
@@ -97,7 +118,7 @@ def rlc_probe(series: bool, R: float, L: float, Cap: float, nr_ts: int = 8000, c
     total current (element plus edge capacitance), so V/I is the element's
     impedance in parallel with the edge capacitance."""
     lines = [uniform_lines(cells, 1.0) for _ in range(3)]
-    s = Scene(*lines, 1e-3)
+    s = _scene(*lines, 1e-3)
     s.set_boundary([BC_PML] * 6, [6] * 6)
     s.set_gauss_excite(f0, fc, nr_ts)
     c = cells // 2
@@ -126,7 +147,7 @@ def d192(nr_ts: int = 3000, seed: int = 192, cells: int = 192, pml: int = 8) -> 
     this mesh: Drude f_p = 2e15*1e-6 Hz, collision 1e13..1e14 /s * 1e-6."""
     rng = np.random.default_rng(seed)
     lines = [graded_lines(cells, rng) for _ in range(3)]
-    s = Scene(*lines, 1e-3)
+    s = _scene(*lines, 1e-3)
     s.set_boundary([BC_PML] * 6, [pml] * 6)
     s.set_gauss_excite(6e9, 6e9, nr_ts)
     lo = [pml + 1] * 3
@@ -196,7 +217,7 @@ def serve_job(seed: int, nr_ts: int = 20000) -> Scene:
         s = port_scene(cells, 0.5, 8, int(rng.integers(1, 8)), 40_000 + seed, f0, f0 / 2, nr_ts, eps_max=10.0,
                        kappa_range=None, edge_range=(4, 24), lines=lines)
     else:
-        s = Scene(*lines, 1e-3)
+        s = _scene(*lines, 1e-3)
         s.set_boundary([BC_PML] * 6, [8] * 6)
         s.set_gauss_excite(f0, f0 / 2, nr_ts)
         for b in range(int(rng.integers(1, 6))):
@@ -229,7 +250,7 @@ def cavity(nr_ts: int = 20000) -> Scene:
     mx = np.linspace(0, a, 26)
     my = np.linspace(0, b, 11)
     mz = np.linspace(0, d, 32)
-    s = Scene(mx, my, mz, 1e-3)
+    s = _scene(mx, my, mz, 1e-3)
     s.set_boundary([BC_PEC] * 6)
     f_start, f_stop = 1e9, 10e9
     s.set_gauss_excite((f_stop - f_start) / 2, (f_stop - f_start) / 2, nr_ts)
@@ -286,7 +307,7 @@ def mini(kind: str, seed: int = 0, nr_ts: int = 400) -> Scene:
         rng = np.random.default_rng(seed)
         cells = [34, 30, 38]
         lines = [graded_lines(c, rng) for c in cells] if kind == "mixed" else [uniform_lines(c, 0.5) for c in cells]
-        s = Scene(*lines, 1e-3)
+        s = _scene(*lines, 1e-3)
         s.set_boundary([BC_PML] * 6, [5] * 6)
         s.set_gauss_excite(8e9, 8e9, nr_ts)
         for b in range(4):
