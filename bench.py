@@ -19,7 +19,12 @@ are larger than the 129 MB L2, so no explicit flush is done.
     roofline  the dominant half-step kernel against the measured HBM copy
             bandwidth (MEASURED_PEAKS.json)
     cpu_baseline  the oracle's restated SSE-compressed multithreaded engine
-            (the reference's default engine family) on the host cores
+            (the reference's default engine family) on the host cores, on
+            the oracle's own operator build; a table of L256 (all cores and
+            one), P64 and a D192 window
+    batch / serve  the B96 persistent batch against job-by-job and
+            concurrent plain engines, and the serving stream against one job
+            at a time (jobs/s, p50 / p99 latency, Mcell-updates/s)
 
 --impl reference times that CPU engine alone on the same workload and metric.
 Multi-GPU (torchrun): every rank runs an independent replica of the job
@@ -200,16 +205,56 @@ def cpu_baseline(threads: int):
     del d192
     cpu = platform.processor() or platform.machine()
     try:
-        for ln in open("/proc/cpuinfo"):
-            if ln.lower().startswith(("model name", "cpu part")):
+        out_l = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out_l.splitlines():
+            if ln.lower().startswith("model name"):
                 cpu = ln.split(":", 1)[1].strip()
                 break
-    except OSError:
+    except (OSError, subprocess.SubprocessError):
         pass
     return {"value": round(v, 2), "unit": "Mcell-updates/s", "cores": threads, "kind": "port",
             "sample": f"{n} timesteps of L256 ({sec:.1f} s) with the restated SSE-compressed x-slab "
                       f"multithreaded engine on the oracle's own operator build",
             "nproc": os.cpu_count(), "cpu": cpu, "machine": platform.machine(), "table": out}
+
+
+def batch_and_serve(args, device: int) -> dict:
+    """The two patterns beside the plain engine, measured on this GPU:
+    batch -- the 96-job B96 sweep (1500 timesteps each) as one persistent
+    batch against the plain engine job by job and against the same engines
+    run concurrently on their own streams (CUDA events / wall clock);
+    serve -- a seeded Poisson stream of serving requests (operator builds
+    included) through the continuous-batching server against the same
+    stream one job at a time through the plain engine (wall clock from the
+    first submission), with p50 / p99 job latency."""
+    from wipems_gb300 import workloads
+    out = {}
+    b = workloads.b96(96, 1500, device)
+    out["batch"] = {
+        "workload": "B96: 96 seeded jobs, grid edges 48-160 cells per axis, half PEC / half UPML-8, 1-10 "
+                    "dielectric bricks, one 50 ohm port, f0 in 1-20 GHz; 1500 timesteps each",
+        "jobs": b["jobs"], "nodes": b["nodes"], "timesteps": b["timesteps"],
+        "batched_mcells": round(b["batched_mcells"], 1), "job_by_job_mcells": round(b["plain_mcells"], 1),
+        "concurrent_mcells": round(b["concurrent_mcells"], 1),
+        "ratio_vs_job_by_job": round(b["speedup"], 3),
+        "ratio_vs_concurrent": round(b["batched_mcells"] / b["concurrent_mcells"], 3),
+        "batched_ms": round(b["batched_ms"], 2), "job_by_job_ms": round(b["plain_ms"], 2),
+        "concurrent_wall_s": round(b["concurrent_wall_s"], 3), "tiling": b["tiling"],
+        "timing": "batched and job by job: CUDA events; concurrent: wall clock"}
+    sv = workloads.serve(n_jobs=args.serve_jobs, mean_gap=args.serve_gap, device=device)
+    S, P = sv["served"], sv["plain"]
+    keep = ("wall_s", "jobs_per_s", "mcells", "p50_s", "p99_s", "gpu_ms", "gpu_mcells")
+    out["serve"] = {
+        "workload": f"S: {args.serve_jobs} seeded Poisson requests (mean gap {args.serve_gap * 1e3:.0f} ms), grid "
+                    "edges log-uniform 32-256 cells, 60 % dielectric + UPML-8, 40 % Drude or Lorentz; each job "
+                    "stops at -40 dB energy or 20000 timesteps; operator builds included",
+        "jobs": sv["jobs"], "served": {k: round(S[k], 4) for k in keep},
+        "one_at_a_time": {k: round(P[k], 4) for k in keep},
+        "ratio": round(sv["speedup"], 3), "gpu_ratio": round(sv["gpu_speedup"], 3),
+        "same_stop_timesteps": sv["same_stop_timesteps"], "failed": S["failed"],
+        "timing": "wall clock over the stream (first submission to last completion); latency = completion "
+                  "minus arrival"}
+    return out
 
 
 def max_over_ranks(vals, device):
@@ -350,6 +395,9 @@ def run_gpu(args, rank, world, local_rank):
     te = time.perf_counter() - te
     e2e_value = nodes * TIMESTEPS * e2e_steps * world / te / 1e6
 
+    extra = {}
+    if rank == 0 and args.extras:
+        extra = batch_and_serve(args, local_rank)
     if rank == 0:
         threads = os.cpu_count() or 1
         cpu = cpu_baseline(threads)
@@ -365,7 +413,7 @@ def run_gpu(args, rank, world, local_rank):
                 "e2e": {"value": round(e2e_value, 2), "unit": "Mcell-updates/s",
                         "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h // e2e_steps),
                         "steps": e2e_steps},
-                "gpu_launches": int(launches), "clocks": clocks}
+                "gpu_launches": int(launches), "clocks": clocks, **extra}
         print(json.dumps(line), flush=True)
 
 
@@ -376,6 +424,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--ref-timesteps", type=int, default=20, help="CPU timesteps per reference-arm step")
+    ap.add_argument("--no-extras", dest="extras", action="store_false",
+                    help="skip the batch (B96) and serving-stream measurements")
+    ap.add_argument("--serve-jobs", type=int, default=200, help="requests in the serving stream")
+    ap.add_argument("--serve-gap", type=float, default=0.02, help="mean Poisson gap between requests (s)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

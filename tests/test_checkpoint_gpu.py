@@ -1,7 +1,6 @@
 """Checkpoint / resume: an engine restored from a checkpoint steps on to
-the same fields, probe samples and frequency-domain sums, bit for bit, as
-the engine that was checkpointed (the energy column is a double-atomic sum
-over blocks, equal to rounding)."""
+the same fields, probe samples, energies and frequency-domain sums, bit for
+bit, as the engine that was checkpointed."""
 import numpy as np
 import pytest
 
@@ -36,8 +35,7 @@ def test_resume_is_bit_identical(kind, kw):
     assert np.array_equal(Ia.view(np.uint32), Ib.view(np.uint32))
     sa, sb = a.samples(), b.samples()
     assert np.array_equal(sa.ts, sb.ts) and np.array_equal(sa.values, sb.values)
-    # energies are sums over blocks in double atomics: equal to rounding
-    np.testing.assert_allclose(sb.energy, sa.energy, rtol=1e-12, atol=0)
+    assert np.array_equal(sb.energy, sa.energy)  # fixed-order energy: the same bits
     fa, na = a.fd_results()
     fb, nb = b.fd_results()
     assert na == nb and np.array_equal(fa, fb)
@@ -58,3 +56,44 @@ def test_restore_checks_the_engine_and_keeps_a_stopped_job_stopped():
     with pytest.raises(FdtdError) as ei:
         other.restore(blob)
     assert ei.value.code == -1
+
+
+def _same_run(x, y):
+    Vx, Ix = x.fields()
+    Vy, Iy = y.fields()
+    assert np.array_equal(Vx.view(np.uint32), Vy.view(np.uint32))
+    assert np.array_equal(Ix.view(np.uint32), Iy.view(np.uint32))
+    sx, sy = x.samples(), y.samples()
+    assert np.array_equal(sx.ts, sy.ts) and np.array_equal(sx.values, sy.values)
+    assert sx.ts[0] == 0  # the ts = 0 sample of RunFDTD's first PA->Process()
+
+
+def test_rejected_restore_leaves_a_fresh_engine_untouched():
+    """A blob rejected for any reason -- another configuration, truncated,
+    trailing bytes, a corrupted part size -- changes nothing: the fresh
+    engine afterwards steps exactly like a clean one, ts = 0 sample and
+    frequency-domain sums included."""
+    op = Operator(scenes.mini("upml", seed=3, nr_ts=800))
+    a = _engine(op)
+    a.iterate(120)
+    blob = a.checkpoint()
+    pec = Operator(scenes.mini("pec", nr_ts=800))
+    import struct
+    bad_size = bytearray(blob)
+    # the blob header is 8 magic bytes and 14 uint32 words; the first part
+    # (the four int control words, 16 bytes) follows it: claim 4 bytes more
+    first_count_at = struct.calcsize("<8s14I")
+    assert struct.unpack_from("<Q", blob, first_count_at)[0] == 16
+    struct.pack_into("<Q", bad_size, first_count_at, 20)
+    for eng_op, payload in ((pec, blob), (op, blob[:-8]), (op, blob + b"\0" * 8), (op, bytes(bad_size))):
+        x = _engine(eng_op)
+        with pytest.raises(FdtdError) as ei:
+            x.restore(payload)
+        assert ei.value.code == -1
+        x.iterate(100)
+        clean = _engine(eng_op)
+        clean.iterate(100)
+        _same_run(x, clean)
+        fx, nx = x.fd_results()
+        fc, nc = clean.fd_results()
+        assert nx == nc and np.array_equal(fx, fc)

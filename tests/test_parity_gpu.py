@@ -112,7 +112,8 @@ def test_chunking_graphs_and_tiles_are_invisible():
         assert np.array_equal(I.view(np.uint32), I0.view(np.uint32)), kw
         s = e.samples()
         assert np.array_equal(s.ts, s0.ts)
-        assert np.allclose(s.values, s0.values, rtol=0, atol=0), kw
+        assert np.array_equal(s.values, s0.values), kw
+        assert np.array_equal(s.energy, s0.energy), kw  # energy summed in an order fixed by the grid
 
 
 def test_reset_and_compressed_upload_reproduce():
@@ -177,6 +178,23 @@ def test_cavity_resonances_on_gpu():
     assert all(res.values()), res
 
 
+def test_energy_on_demand_equals_the_sample_energy():
+    """fdtd_engine_energy sums the same per-node terms in the same fixed
+    order as the sample steps: right after a sample step it returns the
+    recorded energy bit for bit, for every kernel family."""
+    op = Operator(scenes.mini("mixed", nr_ts=400))
+    for kw in (dict(), dict(kernel="direct", tile_y=2, x_chunk=3), dict(x_chunk=1, stages=4)):
+        eng = Engine(op, **kw)
+        eng.iterate(5 * op.probe_interval)
+        s = eng.samples()
+        assert s.ts[-1] == eng.num_timesteps and s.energy[-1] > 0
+        assert eng.energy() == s.energy[-1], kw
+    op = Operator(scenes.mini("upml", nr_ts=400))
+    eng = Engine(op, kernel="fused")
+    eng.iterate(4 * op.probe_interval)
+    assert eng.energy() == eng.samples().energy[-1]
+
+
 def test_field_access_and_energy():
     op = Operator(scenes.mini("pec", nr_ts=100))
     eng = Engine(op)
@@ -209,11 +227,15 @@ def test_fused_kernel_matches_oracle(kind):
 def test_fused_kernel_tilings_and_graphs_invisible():
     op = Operator(scenes.mini("upml", seed=2, nr_ts=400))
     ref = oracle.run(*oracle_inputs(op), 120, op.probe_interval, engine=oracle.BASIC)
+    two_pass = Engine(op)
+    two_pass.iterate(120)
+    e0 = two_pass.samples().energy
     for kw in (dict(x_chunk=1), dict(x_chunk=3, stages=4), dict(x_chunk=16, use_graphs=False), dict(stages=5)):
         eng = Engine(op, kernel="fused", **kw)
         eng.iterate(57)
         eng.iterate(63)
         compare(op, eng, ref)
+        assert np.array_equal(eng.samples().energy, e0), kw
         eng.close()
 
 

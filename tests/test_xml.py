@@ -162,3 +162,15 @@ def test_xml_field_probes():
     op = Operator(sx)
     types = [p.type for p in op.probes]
     assert types[-2:] == [2, 3] and op.probes[-1].weight == 2.0
+
+
+@pytest.mark.parametrize("name", ["port_box.xml", "lorentz_mur.xml"])
+def test_xml_operator_matches_oracle_reader(name):
+    """The engine library's XML reader + operator build against the
+    oracle's own reader (oracle/xml_spec.py, Python's XML parser) + its
+    operator build: bit-identical operators and probes."""
+    import oracle
+    from oracle.xml_spec import xml_spec
+    from helpers import assert_same_operator
+    path = str(Path(__file__).parent / "golden" / name)
+    assert_same_operator(Operator(Scene.from_xml(path)), oracle.Operator(xml_spec(path)))

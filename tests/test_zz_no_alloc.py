@@ -23,20 +23,30 @@ def test_static_energy_matches_engine_energy(libs):
     nl = (ctypes.c_uint32 * 3)(*op.num_lines)
     out = torch.zeros(1, dtype=torch.float64, device="cuda:0")
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    for steps in (90, 60):  # two calls in a row on different field states
+    states = []
+    for steps in (90, 60):  # two field states, the second 60 steps after the first
         eng.iterate(steps)
         ref = eng.energy()
+        assert ref > 0
         V, I = eng.fields()
-        Vd = torch.from_numpy(np.ascontiguousarray(V)).to("cuda:0")
-        Id = torch.from_numpy(np.ascontiguousarray(I)).to("cuda:0")
+        states.append((ref, torch.from_numpy(np.ascontiguousarray(V)).to("cuda:0"),
+                       torch.from_numpy(np.ascontiguousarray(I)).to("cuda:0")))
+
+    def call(Vd, Id):
         out.fill_(-1.0)
         rc = L.fdtd_field_energy_static(ctypes.c_void_p(Vd.data_ptr()), ctypes.c_void_p(Id.data_ptr()), nl,
                                         op.num_lines[2], stream, ctypes.c_void_p(out.data_ptr()))
         assert rc == 0, _abi.last_error()
         torch.cuda.synchronize()
-        got = out.item()
-        assert ref > 0
+        return out.item()
+
+    call(*states[0][1:])  # the first call on the device does the set-up
+    free0, _ = torch.cuda.mem_get_info(0)
+    for ref, Vd, Id in states:  # two calls in a row
+        got = call(Vd, Id)
         assert abs(got / ref - 1) < 1e-6, (got, ref)
+    free1, _ = torch.cuda.mem_get_info(0)
+    assert free1 == free0, (free0, free1)  # the calls allocated no device memory
 
 
 def test_static_energy_rejects_oversized_grid(libs):

@@ -48,6 +48,17 @@ __global__ void k_batch_advance(const AdvJob* __restrict__ jobs, double eps0, do
     if (threadIdx.x < 4) J.out[threadIdx.x] = J.ctl[threadIdx.x];
 }
 
+// Energy plane sums (k_energy_planes) of the jobs that record a sample
+// after this step: block (x, j) sums plane x of job j (the same fixed order
+// as a job running alone, so its energies are the same bits).
+__global__ void __launch_bounds__(256) k_batch_energy_planes(const AdvJob* __restrict__ jobs) {
+    const AdvJob& J = jobs[blockIdx.y];
+    if (!J.energy_valid || J.interval <= 0 || *J.g.d_done) return;
+    if ((*J.d_ts + 1) % J.interval != 0 || (int)blockIdx.x >= J.g.Nx - 1) return;
+    const double2 r = plane_energy(J.g, (int)blockIdx.x);
+    if (threadIdx.x == 0) J.g.eplane[blockIdx.x] = r;
+}
+
 struct Group {
     int bin = 0;
     bool e16 = true, h16 = true, geo = false;
@@ -205,6 +216,7 @@ struct fdtd_batch_s {
     struct Bin {
         std::vector<int> groups;
         int first = 0, count = 0;  // job range (jobs are stored bin by bin)
+        int max_planes = 1;        // largest Nx-1 of the bin's jobs
     };
     std::vector<Bin> bins;
     uint64_t bin_bytes = 0;
@@ -236,8 +248,9 @@ int bin_step(fdtd_batch_s* b, size_t k) {
     const size_t ng = B.groups.size();
     for (int gi : B.groups) launch_group_volt(b->groups[gi], b->d_jobs.p, b->XC, b->stages, b->stream);
     for (int gi : B.groups) launch_group_curr(b->groups[gi], b->d_jobs.p, b->XC, b->stages, b->stream);
+    k_batch_energy_planes<<<dim3((unsigned)B.max_planes, (unsigned)B.count), 256, 0, b->stream>>>(b->d_adv.p + B.first);
     k_batch_advance<<<(unsigned)B.count, 256, 0, b->stream>>>(b->d_adv.p + B.first, kEps0, kMue0);
-    b->last_launches += 2 * ng + 1;
+    b->last_launches += 2 * ng + 2;
     const cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) {
         set_error(std::string("batch kernel launch: ") + cudaGetErrorString(err));
@@ -348,6 +361,7 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
             const int j = (int)b->jobs.size();
             b->jobs.push_back(e);
             b->total_nodes += (uint64_t)e->N[0] * e->N[1] * e->N[2];
+            B.max_planes = std::max(B.max_planes, (int)e->N[0] - 1);
             auto key = std::make_tuple((int)e->E.idx16, (int)e->H.idx16, (int)e->geo_on, e->feat);
             auto it = gidx.find(key);
             if (it == gidx.end()) {
@@ -382,6 +396,7 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
         hj[j].ti = e->ti;
         hj[j].maps = b->d_maps.p + j;
         hj[j].interval = (int)e->interval;
+        hj[j].energy = e->energy_on_probe ? 1 : 0;
         std::memset(&ha[j], 0, sizeof(AdvJob));
         ha[j].d_ts = e->p_ts();
         ha[j].ps = e->ps;
@@ -496,7 +511,7 @@ int fdtd_batch_iterate(fdtd_batch_t b, uint32_t n) {
     while (left > 0) {
         if (b->graph && left >= b->graph_steps) {
             CK(cudaGraphLaunch(b->graph, b->stream));
-            b->last_launches += (2 * b->groups.size() + b->bins.size()) * b->graph_steps;
+            b->last_launches += (2 * b->groups.size() + 2 * b->bins.size()) * b->graph_steps;
             left -= b->graph_steps;
             continue;
         }

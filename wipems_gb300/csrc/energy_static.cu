@@ -82,7 +82,11 @@ __global__ void k_planes_total(const double* scratch, uint32_t planes, double ep
 }
 
 // Device address of the static scratch array on the current device, looked
-// up once per device (cudaGetSymbolAddress; no allocation).
+// up once per device, on the first call made with that device current
+// (cudaGetSymbolAddress; no allocation).  The cached address belongs to
+// the device's context: after cudaDeviceReset the library's module is
+// loaded anew and the cached address is stale, so this entry point must not
+// be called again in a process that reset the device.
 int scratch_address(int dev, double** out) {
     if (dev < 0 || dev >= kMaxDevices) {
         set_error("fdtd_field_energy_static: device ordinal out of range");

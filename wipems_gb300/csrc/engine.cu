@@ -181,6 +181,10 @@ int launch_step(fdtd_engine_s* e, int ts_off, bool energy) {
 }
 
 int launch_advance(fdtd_engine_s* e, int adv, bool sample, bool energy_valid) {
+    if (sample && energy_valid && adv > 0) {  // the last current kernel wrote the energy segments
+        k_energy_planes<<<e->N[0] - 1, 256, 0, e->stream>>>(e->g);
+        e->last_launches += 1;
+    }
     k_advance_sample<<<1, 256, 0, e->stream>>>(e->p_ts(), adv, sample ? 1 : 0, e->ps, e->g, energy_valid ? 1 : 0,
                                                 kEps0, kMue0);
     e->last_launches += 1;
@@ -482,6 +486,8 @@ int reset_state(fdtd_engine_s* e) {
     if (e->rlc_state.p) CK(cudaMemsetAsync(e->rlc_state.p, 0, e->rlc_state.n * sizeof(float), s));
     if (e->d_fd_count.p) CK(cudaMemsetAsync(e->d_fd_count.p, 0, sizeof(int), s));
     CK(cudaMemsetAsync(e->d_eacc.p, 0, 4 * sizeof(double), s));
+    // the ts = 0 sample reads the plane sums of the zero fields
+    CK(cudaMemsetAsync(e->eplane.p, 0, e->eplane.n * sizeof(double2), s));
     e->ts = 0;
     e->done = false;
     e->need_initial_sample = true;
@@ -595,6 +601,11 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
         return rc;
     if ((rc = e->ctl.alloc(4, tot, e->stream)) || (rc = e->d_eacc.alloc(4, tot, e->stream)) ||
         (rc = e->d_energy_tmp.alloc(2, tot, e->stream)))
+        return rc;
+    // energy segments: one float pair per (x < Nx-1, y < Ny-1, 32-node z tile)
+    const int nzt = ((int)e->N[2] - 1 + 31) / 32;
+    if ((rc = e->eseg.alloc((size_t)(e->N[0] - 1) * (e->N[1] - 1) * (size_t)nzt, tot, e->stream)) ||
+        (rc = e->eplane.alloc(e->N[0] - 1, tot, e->stream)))
         return rc;
     DevGrid& g = e->g;
     if ((rc = upload_half(e, c->E, e->E, g.e)) || (rc = upload_half(e, c->H, e->H, g.h))) return rc;
@@ -728,6 +739,9 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     g.d_ts = e->p_ts();
     g.d_done = e->p_done();
     g.d_eacc = e->d_eacc.p;
+    g.eseg = e->eseg.p;
+    g.eplane = e->eplane.p;
+    g.nzt = ((int)e->N[2] - 1 + 31) / 32;
     e->smem_direct = 2 * 3 * (size_t)(e->TY + 1) * 33 * sizeof(float);
     for (int a = 0; a < 3; ++a) {
         e->ti.lo[a] = c->inner_lo[a];
@@ -988,7 +1002,7 @@ int fdtd_engine_iterate_async(fdtd_engine_t e, uint32_t n) {
         if (e->interval && e->use_graphs && e->chunk && (e->ts % e->interval) == 0 && left >= e->interval &&
             to_fd >= e->interval) {
             CK(cudaGraphLaunch(e->chunk, e->stream));
-            e->last_launches += (e->fused ? 1 : 2) * (uint64_t)e->interval + 1;
+            e->last_launches += (e->fused ? 1 : 2) * (uint64_t)e->interval + 1 + (e->energy_on_probe ? 1 : 0);
             e->ts += e->interval;
             left -= e->interval;
             if (to_fd == e->interval && (rc = launch_fd(e, e->ts))) return rc;
@@ -1081,8 +1095,10 @@ void ckpt_header(const fdtd_engine_s* e, uint32_t nsamp, CkptHeader& h) {
     h.version = 2;
     for (int a = 0; a < 3; ++a) h.N[a] = e->N[a];
     h.Nzp = e->Nzp;
-    h.nprobe = (uint32_t)e->ps.nprobe;
-    h.row_doubles = (uint32_t)e->ps.row_doubles;
+    // the sample row layout from the host's probe columns (known before the
+    // probes are uploaded, so a blob can be checked before anything changes)
+    h.nprobe = (uint32_t)e->h_weight.size();
+    h.row_doubles = 2 + h.nprobe;
     h.nfreq = (uint32_t)e->h_freq.size();
     h.nmur = (uint32_t)e->mur.nface;
     h.ts = e->ts;
@@ -1131,6 +1147,11 @@ int fdtd_engine_checkpoint(fdtd_engine_t e, void* buf, uint64_t cap, uint64_t* s
     return FDTD_OK;
 }
 
+// Restore validates the whole blob -- header, sample count and every part's
+// size against this engine, and the blob's length -- before it changes
+// anything: a rejected blob leaves the engine exactly as it was (a fresh
+// engine keeps its pending ts = 0 sample and FD accumulation).  Only then
+// are the parts copied to the device.
 int fdtd_engine_restore(fdtd_engine_t e, const void* buf, uint64_t size) {
     if (!e || !buf) return FDTD_ERR_ARG;
     if (e->pending) {
@@ -1144,10 +1165,6 @@ int fdtd_engine_restore(fdtd_engine_t e, const void* buf, uint64_t size) {
     CkptHeader h;
     std::memcpy(&h, buf, sizeof(h));
     CkptHeader mine;
-    if (!e->started) e->need_initial_sample = false;  // the blob holds the samples
-    CK(cudaSetDevice(e->device));
-    int rc;
-    if ((rc = start(e))) return rc;
     ckpt_header(e, h.nsamp, mine);
     if (std::memcmp(h.magic, mine.magic, 8) != 0 || h.version != mine.version || h.N[0] != mine.N[0] ||
         h.N[1] != mine.N[1] || h.N[2] != mine.N[2] || h.Nzp != mine.Nzp || h.nprobe != mine.nprobe ||
@@ -1156,25 +1173,45 @@ int fdtd_engine_restore(fdtd_engine_t e, const void* buf, uint64_t size) {
         set_error("fdtd_engine_restore: the checkpoint belongs to a different engine configuration");
         return FDTD_ERR_ARG;
     }
-    if (h.nsamp > (uint32_t)e->ps.cap) {
+    if (h.nsamp > (uint32_t)e->cap) {
         set_error("fdtd_engine_restore: the checkpoint holds more samples than this engine's ring");
         return FDTD_ERR_ARG;
     }
+    CK(cudaSetDevice(e->device));
+    int rc;
+    // the probe tables and the sample ring (idempotent; no simulation state)
+    if ((rc = upload_probes(e))) return rc;
     const std::vector<CkptPart> parts = ckpt_parts(e, h.nsamp);
-    const char* o = static_cast<const char*>(buf) + sizeof(h);
-    const char* end = static_cast<const char*>(buf) + size;
+    const char* const first = static_cast<const char*>(buf) + sizeof(h);
+    const char* const end = static_cast<const char*>(buf) + size;
+    // pass 1: every (bytes, payload) pair and the total length
+    const char* o = first;
     for (const CkptPart& q : parts) {
         uint64_t b = 0;
-        if (o + sizeof(b) > end) {
+        if ((size_t)(end - o) < sizeof(b)) {
             set_error("fdtd_engine_restore: blob truncated");
             return FDTD_ERR_ARG;
         }
         std::memcpy(&b, o, sizeof(b));
         o += sizeof(b);
-        if (b != q.bytes || o + b > end) {
+        if (b != q.bytes || (uint64_t)(end - o) < b) {
             set_error("fdtd_engine_restore: a state array does not match this engine");
             return FDTD_ERR_ARG;
         }
+        o += b;
+    }
+    if (o != end) {
+        set_error("fdtd_engine_restore: trailing bytes after the last state array");
+        return FDTD_ERR_ARG;
+    }
+    // pass 2: the blob is sound; replace the state
+    if (!e->started) e->need_initial_sample = false;  // the blob holds the samples
+    if ((rc = start(e))) return rc;
+    o = first;
+    for (const CkptPart& q : parts) {
+        uint64_t b = 0;
+        std::memcpy(&b, o, sizeof(b));
+        o += sizeof(b);
         if (b) CK(cudaMemcpyAsync(q.p, o, b, cudaMemcpyHostToDevice, e->stream));
         o += b;
     }
@@ -1260,17 +1297,24 @@ int fdtd_engine_read_samples(fdtd_engine_t e, uint32_t first, uint32_t count, ui
 
 int fdtd_engine_energy(fdtd_engine_t e, double* energy) {
     if (!e || !energy) return FDTD_ERR_ARG;
+    if (e->pending) {
+        set_error("fdtd_engine_energy: wait for the asynchronous iterate first");
+        return FDTD_ERR_STATE;
+    }
     CK(cudaSetDevice(e->device));
-    CK(cudaMemsetAsync(e->d_energy_tmp.p, 0, 2 * sizeof(double), e->stream));
     DevGrid g = e->g;
     g.V = e->cur_V();
     g.I = e->cur_I();
-    k_energy<<<4 * 152, 256, 0, e->stream>>>(g, e->d_energy_tmp.p);
+    // the segments, plane sums and total of a sample step, from the fields
+    const dim3 grid((unsigned)g.nzt, (e->N[1] - 1 + 7) / 8, e->N[0] - 1);
+    k_energy_segments<<<grid, dim3(32, 8), 0, e->stream>>>(g);
+    k_energy_planes<<<e->N[0] - 1, 256, 0, e->stream>>>(g);
+    k_energy_total<<<1, 32, 0, e->stream>>>(g, kEps0, kMue0, e->d_energy_tmp.p);
     CK(cudaGetLastError());
-    double h[2];
-    CK(cudaMemcpyAsync(h, e->d_energy_tmp.p, sizeof(h), cudaMemcpyDeviceToHost, e->stream));
+    double h = 0;
+    CK(cudaMemcpyAsync(&h, e->d_energy_tmp.p, sizeof(h), cudaMemcpyDeviceToHost, e->stream));
     CK(cudaStreamSynchronize(e->stream));
-    *energy = kEps0 * h[0] + kMue0 * h[1];
+    *energy = h;
     return FDTD_OK;
 }
 

@@ -100,8 +100,10 @@ struct fdtd_engine_s {
     int* p_nsamp() const { return ctl.p + 1; }
     int* p_err() const { return ctl.p + 2; }
     int* p_done() const { return ctl.p + 3; }
-    DevBuf<double> d_eacc;  // {sum V^2, sum I^2, running energy maximum}
+    DevBuf<double> d_eacc;  // [2]: running energy maximum (end criterion)
     DevBuf<double> d_energy_tmp;
+    DevBuf<float2> eseg;    // energy segments (DevGrid::eseg)
+    DevBuf<double2> eplane; // energy plane sums (DevGrid::eplane)
     // probes
     std::vector<ProbeEntry> h_entries;
     std::vector<int> h_first{0};

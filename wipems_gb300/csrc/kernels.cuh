@@ -112,7 +112,6 @@ __global__ void __launch_bounds__(256) k_curr(const DevGrid g, int ts_off, int X
 
     const long long yz = (long long)y * g.Nzp + z;
     const long long C = g.comp;
-    float es = 0.f, ec = 0.f, hs = 0.f, hc = 0.f;
     float c0 = 0.f, c1 = 0.f, c2 = 0.f;  // V at plane x
     if (inplane && x0 < x1) {
         long long o = (long long)x0 * g.sx + yz;
@@ -148,6 +147,7 @@ __global__ void __launch_bounds__(256) k_curr(const DevGrid g, int ts_off, int X
             s1[ty * 33 + 32] = g.V[C + oh];
         }
         __syncthreads();
+        float eh[3] = {0.f, 0.f, 0.f};  // new I of this node (energy terms)
         if (active) {
             const float v2yp = s2[si + 33];
             const float v0yp = s0[si + 33];
@@ -165,31 +165,16 @@ __global__ void __launch_bounds__(256) k_curr(const DevGrid g, int ts_off, int X
             g.I[o] = cu[0];
             g.I[C + o] = cu[1];
             g.I[2 * C + o] = cu[2];
-            if (ENERGY) {
-                // Engine_Interface_FDTD::CalcFastEnergy terms (float products)
-                kahan_add(es, ec, __fmul_rn(c0, c0));
-                kahan_add(es, ec, __fmul_rn(c1, c1));
-                kahan_add(es, ec, __fmul_rn(c2, c2));
-                kahan_add(hs, hc, __fmul_rn(cu[0], cu[0]));
-                kahan_add(hs, hc, __fmul_rn(cu[1], cu[1]));
-                kahan_add(hs, hc, __fmul_rn(cu[2], cu[2]));
-            }
+            eh[0] = cu[0];
+            eh[1] = cu[1];
+            eh[2] = cu[2];
         }
+        if (ENERGY)  // Engine_Interface_FDTD::CalcFastEnergy terms of segment (x, y, blockIdx.x)
+            energy_segment(g, x, y, blockIdx.x, active, y < g.Ny - 1 && (int)blockIdx.x * 32 < g.Nz - 1, c0, c1, c2,
+                           eh[0], eh[1], eh[2]);
         c0 = n0;
         c1 = n1;
         c2 = n2;
-    }
-    if (ENERGY) {
-        double esum = (double)es - (double)ec, hsum = (double)hs - (double)hc;
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            esum += __shfl_down_sync(0xffffffffu, esum, off);
-            hsum += __shfl_down_sync(0xffffffffu, hsum, off);
-        }
-        if (tz == 0 && (esum != 0.0 || hsum != 0.0)) {
-            atomicAdd(&g.d_eacc[0], esum);
-            atomicAdd(&g.d_eacc[1], hsum);
-        }
     }
 }
 
@@ -353,7 +338,14 @@ __device__ __forceinline__ void advance_sample(int* d_ts, int adv, int sample, c
     if (tid == 0) {
         rec[0] = (double)s_ts;
         if (energy_valid) {
-            double e = eps0 * g.d_eacc[0] + mue0 * g.d_eacc[1];
+            // the plane sums in x order (fixed by the grid)
+            double a = 0.0, b = 0.0;
+            for (int x = 0; x < g.Nx - 1; ++x) {
+                const double2 p = g.eplane[x];
+                a += p.x;
+                b += p.y;
+            }
+            double e = eps0 * a + mue0 * b;
             if (!isfinite(e)) atomicOr(ps.d_err, 2);
             rec[1] = e;
             if (ps.end_crit > 0.0) {
@@ -364,9 +356,46 @@ __device__ __forceinline__ void advance_sample(int* d_ts, int adv, int sample, c
         } else {
             rec[1] = -1.0;
         }
-        g.d_eacc[0] = 0.0;
-        g.d_eacc[1] = 0.0;
     }
+}
+
+// Sum of the energy segments of plane x in a fixed order (256 threads: each
+// sums a strided share in double, then a fixed shuffle / shared-memory
+// tree); thread 0 returns the pair.
+__device__ __forceinline__ double2 plane_energy(const DevGrid& g, int x) {
+    __shared__ double sa[8], sb[8];
+    const long long n = (long long)(g.Ny - 1) * g.nzt;
+    const float2* seg = g.eseg + (long long)x * n;
+    double a = 0.0, b = 0.0;
+    for (long long i = threadIdx.x; i < n; i += 256) {
+        const float2 v = seg[i];
+        a += (double)v.x;
+        b += (double)v.y;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, off);
+        b += __shfl_down_sync(0xffffffffu, b, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        sa[threadIdx.x >> 5] = a;
+        sb[threadIdx.x >> 5] = b;
+    }
+    __syncthreads();
+    double2 r = make_double2(0.0, 0.0);
+    if (threadIdx.x == 0) {
+        for (int w = 0; w < 8; ++w) {
+            r.x += sa[w];
+            r.y += sb[w];
+        }
+    }
+    return r;
+}
+
+// one block (256 threads) per x plane: eplane[x] from the plane's segments
+static __global__ void __launch_bounds__(256) k_energy_planes(const DevGrid g) {
+    const double2 r = plane_energy(g, blockIdx.x);
+    if (threadIdx.x == 0) g.eplane[blockIdx.x] = r;
 }
 
 static __global__ void k_advance_sample(int* d_ts, int adv, int sample, ProbeSet ps, const DevGrid g, int energy_valid,
@@ -634,35 +663,37 @@ static __global__ void k_dump_field(const DevGrid g, const float* __restrict__ V
     }
 }
 
-// Full-grid energy (CalcFastEnergy) on demand.
-static __global__ void k_energy(const DevGrid g, double* out) {
-    double es = 0.0, hs = 0.0;
-    const long long nyz = (long long)(g.Ny - 1) * (g.Nz - 1);
-    const long long total = (long long)(g.Nx - 1) * nyz;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
-         i += (long long)gridDim.x * blockDim.x) {
-        const int x = (int)(i / nyz);
-        const long long r = i - (long long)x * nyz;
-        const int y = (int)(r / (g.Nz - 1));
-        const int z = (int)(r - (long long)y * (g.Nz - 1));
+// Full-grid energy (CalcFastEnergy) on demand: the segments from the fields
+// with the same per-node terms and the same warp tree as the current
+// kernels, so that (with k_energy_planes and k_energy_total) the result is
+// bit-identical to the energy a sample step records for the same fields.
+// Blocks of (32 z, 8 y) at one x plane (blockIdx.z).
+static __global__ void k_energy_segments(const DevGrid g) {
+    const int x = blockIdx.z, y = blockIdx.y * 8 + threadIdx.y, zt = blockIdx.x;
+    const int z = zt * 32 + threadIdx.x;
+    const bool act = (y < g.Ny - 1) && (z < g.Nz - 1);
+    float v[3] = {0.f, 0.f, 0.f}, c[3] = {0.f, 0.f, 0.f};
+    if (act) {
         const long long o = (long long)x * g.sx + (long long)y * g.Nzp + z;
 #pragma unroll
         for (int n = 0; n < 3; ++n) {
-            const float v = g.V[n * g.comp + o];
-            const float c = g.I[n * g.comp + o];
-            es += (double)__fmul_rn(v, v);
-            hs += (double)__fmul_rn(c, c);
+            v[n] = g.V[n * g.comp + o];
+            c[n] = g.I[n * g.comp + o];
         }
     }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        es += __shfl_down_sync(0xffffffffu, es, off);
-        hs += __shfl_down_sync(0xffffffffu, hs, off);
+    energy_segment(g, x, y, zt, act, y < g.Ny - 1, v[0], v[1], v[2], c[0], c[1], c[2]);
+}
+
+// eps0 * sum E + mue0 * sum H over the planes in x order (one thread)
+static __global__ void k_energy_total(const DevGrid g, double eps0, double mue0, double* out) {
+    if (threadIdx.x != 0) return;
+    double a = 0.0, b = 0.0;
+    for (int x = 0; x < g.Nx - 1; ++x) {
+        const double2 p = g.eplane[x];
+        a += p.x;
+        b += p.y;
     }
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(&out[0], es);
-        atomicAdd(&out[1], hs);
-    }
+    out[0] = eps0 * a + mue0 * b;
 }
 
 }  // namespace wipems

@@ -183,7 +183,6 @@ __global__ void __launch_bounds__(FU_WARPS * 32) k_step_fused(const DevGrid g, c
         fence_proxy_async();
         for (; issued < min(STAGES, nload); ++issued) issue(issued);
     }
-    float es = 0.f, ec = 0.f, hs = 0.f, hc = 0.f;
     bool aborted = false;
     int waited = 0;  // ring planes whose copies this thread saw complete, in order
     // prologue: E at plane x0 (ring planes 0 and 1)
@@ -215,6 +214,7 @@ __global__ void __launch_bounds__(FU_WARPS * 32) k_step_fused(const DevGrid g, c
             break;
         }
         // H at plane x (ring plane r+1)
+        float ev[3] = {0.f, 0.f, 0.f}, eh[3] = {0.f, 0.f, 0.f};  // energy terms of this node
         if (hact) {
             const float* st = stage(r + 1);
             const int vi = ty * FU_VW + tz;
@@ -234,15 +234,12 @@ __global__ void __launch_bounds__(FU_WARPS * 32) k_step_fused(const DevGrid g, c
             In[o] = cu[0];
             In[C + o] = cu[1];
             In[2 * C + o] = cu[2];
-            if (ENERGY) {
-                kahan_add(es, ec, __fmul_rn(c0, c0));
-                kahan_add(es, ec, __fmul_rn(c1, c1));
-                kahan_add(es, ec, __fmul_rn(c2, c2));
-                kahan_add(hs, hc, __fmul_rn(cu[0], cu[0]));
-                kahan_add(hs, hc, __fmul_rn(cu[1], cu[1]));
-                kahan_add(hs, hc, __fmul_rn(cu[2], cu[2]));
-            }
+            ev[0] = c0; ev[1] = c1; ev[2] = c2;
+            eh[0] = cu[0]; eh[1] = cu[1]; eh[2] = cu[2];
         }
+        if (ENERGY)  // segment (x, y, blockIdx.x); the halo warp (ty == FU_TY) owns none
+            energy_segment(g, x, y, blockIdx.x, hact, ty < FU_TY && y < g.Ny - 1 && z0 < g.Nz - 1, ev[0], ev[1],
+                           ev[2], eh[0], eh[1], eh[2]);
         __syncthreads();  // ring plane r+1 and new-V plane x are free
         if (tid == 0 && issued < nload) {
             fence_proxy_async();
@@ -254,7 +251,6 @@ __global__ void __launch_bounds__(FU_WARPS * 32) k_step_fused(const DevGrid g, c
         atomicOr(ti.d_err, 4);
         for (int q = waited; q < issued; ++q) wait(q);  // bounded: copies still in flight
     }
-    if (ENERGY) flush_energy(g.d_eacc, es, ec, hs, hc);
 }
 
 }  // namespace wipems

@@ -23,7 +23,7 @@
 // out-of-range parts of a box (z<0, y<0, beyond the grid) read zeros.
 //
 // Every wait on an mbarrier is bounded by a clock budget; on expiry the block
-// raises bit 4 of the engine's error word, stops computing (the whole block
+// sets value 4 (bit 2) of the engine's error word, stops computing (the whole block
 // leaves the plane loop together via __syncthreads_or), waits -- again with
 // a budget -- for the copies it has in flight, and returns.
 #pragma once
@@ -319,7 +319,7 @@ __device__ __forceinline__ bool volt_tile(const DevGrid& g, const TmaMaps& m, co
 template <typename IdxT, int FEAT, bool GEO, int TY = TMA_TY>
 __device__ __forceinline__ bool curr_tile(const DevGrid& g, const TmaMaps& m, const TileInfo& ti, int bx, int by,
                                           int bz, int XC, int STAGES, float* smem, uint64_t* bars, uint32_t& ring,
-                                          int numTS, bool energy, float& es, float& ec, float& hs, float& hc) {
+                                          int numTS, bool energy) {
     constexpr bool UPML = (FEAT & FEAT_UPML) != 0;
     using L = StageLayout<IdxT, UPML, false, TY>;
     constexpr int HW = L::HW;
@@ -383,6 +383,7 @@ __device__ __forceinline__ bool curr_tile(const DevGrid& g, const TmaMaps& m, co
         bool ok = mbar_wait(&bars[s], (q / (uint32_t)STAGES) & 1u);
         ok = ok && mbar_wait(&bars[sn], ((q + 1) / (uint32_t)STAGES) & 1u);
         const int x = x0 + r;
+        float ev[3] = {0.f, 0.f, 0.f}, eh[3] = {0.f, 0.f, 0.f};  // energy terms of this node
         if (ok && active) {
             const float* st = smem + (size_t)s * L::STAGE;
             const float* stn = smem + (size_t)sn * L::STAGE;
@@ -415,15 +416,12 @@ __device__ __forceinline__ bool curr_tile(const DevGrid& g, const TmaMaps& m, co
             Ip[0] = cu[0];
             Ip[C] = cu[1];
             Ip[2 * C] = cu[2];
-            if (energy) {
-                kahan_add(es, ec, __fmul_rn(c0, c0));
-                kahan_add(es, ec, __fmul_rn(c1, c1));
-                kahan_add(es, ec, __fmul_rn(c2, c2));
-                kahan_add(hs, hc, __fmul_rn(cu[0], cu[0]));
-                kahan_add(hs, hc, __fmul_rn(cu[1], cu[1]));
-                kahan_add(hs, hc, __fmul_rn(cu[2], cu[2]));
-            }
+            ev[0] = c0; ev[1] = c1; ev[2] = c2;
+            eh[0] = cu[0]; eh[1] = cu[1]; eh[2] = cu[2];
         }
+        if (energy)  // Engine_Interface_FDTD::CalcFastEnergy terms of segment (x, y, bx)
+            energy_segment(g, x, y, bx, ok && active, ok && y < g.Ny - 1 && z0 < g.Nz - 1, ev[0], ev[1], ev[2],
+                           eh[0], eh[1], eh[2]);
         if (__syncthreads_or(!ok)) {
             aborted = true;
             break;
@@ -438,20 +436,6 @@ __device__ __forceinline__ bool curr_tile(const DevGrid& g, const TmaMaps& m, co
         }
     }
     return !aborted;
-}
-
-// warp-reduce the Kahan sums and add them to the job's energy accumulators
-__device__ __forceinline__ void flush_energy(double* eacc, float es, float ec, float hs, float hc) {
-    double esum = (double)es - (double)ec, hsum = (double)hs - (double)hc;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        esum += __shfl_down_sync(0xffffffffu, esum, off);
-        hsum += __shfl_down_sync(0xffffffffu, hsum, off);
-    }
-    if ((threadIdx.x & 31) == 0 && (esum != 0.0 || hsum != 0.0)) {
-        atomicAdd(&eacc[0], esum);
-        atomicAdd(&eacc[1], hsum);
-    }
 }
 
 __device__ __forceinline__ float* aligned_smem(float* raw) {
@@ -491,10 +475,8 @@ __global__ void __launch_bounds__(TMA_TY * 32) k_curr_tma(const DevGrid g, const
     if (*g.d_done) return;
     init_ring(bars, STAGES);
     uint32_t ring = 0;
-    float es = 0.f, ec = 0.f, hs = 0.f, hc = 0.f;
     curr_tile<IdxT, FEAT, GEO>(g, m, ti, blockIdx.x, blockIdx.y, blockIdx.z, XC, STAGES, smem, bars, ring,
-                               *g.d_ts + ts_off, ENERGY, es, ec, hs, hc);
-    if (ENERGY) flush_energy(g.d_eacc, es, ec, hs, hc);
+                               *g.d_ts + ts_off, ENERGY);
 }
 
 // ---------------------------------------------------------- batched jobs
@@ -505,7 +487,8 @@ struct BatchJob {
     TileInfo ti;
     const TmaMaps* maps;
     int interval;
-    int pad[3];
+    int energy;  // the job records energies on its sample steps
+    int pad[2];
 };
 
 // Work item of a persistent batched kernel: job, tile (bx, by), x-chunk bz.
@@ -562,11 +545,9 @@ __global__ void __launch_bounds__(BATCH_TY * 32, WIPEMS_BATCH_MIN_BLOCKS) k_curr
         }
         // energy on the job's sample steps (the sample after this step)
         const int numTS = *J.g.d_ts;
-        const bool energy = J.interval > 0 && ((numTS + 1) % J.interval) == 0;
-        float es = 0.f, ec = 0.f, hs = 0.f, hc = 0.f;
+        const bool energy = J.interval > 0 && J.energy && ((numTS + 1) % J.interval) == 0;
         const bool ok = curr_tile<IdxT, FEAT, GEO, BATCH_TY>(J.g, *J.maps, J.ti, w.bx, w.by, w.bz, XC, STAGES, smem, bars,
-                                                   ring, numTS, energy, es, ec, hs, hc);
-        if (energy) flush_energy(J.g.d_eacc, es, ec, hs, hc);
+                                                   ring, numTS, energy);
         if (!ok) break;
     }
 }

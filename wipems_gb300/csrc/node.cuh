@@ -68,8 +68,37 @@ struct DevGrid {
     int sig_period;      // 0 = none
     const int* d_ts;     // timestep counter (numTS)
     const int* d_done;   // set once the job met its end criterion: kernels skip
-    double* d_eacc;      // {sum V^2, sum I^2, running energy maximum}
+    double* d_eacc;      // [2]: running energy maximum (end criterion)
+    // energy on sample steps, in an order fixed by the grid alone: one
+    // (sum V^2, sum I^2) float pair per segment (x < Nx-1, y < Ny-1, 32-node
+    // z tile zt < nzt) written by the warp that updates it, then one double
+    // pair per x plane (k_energy_planes), summed in x order by the sampler
+    float2* eseg;        // [(Nx-1)*(Ny-1)*nzt]
+    double2* eplane;     // [Nx-1]
+    int nzt;             // ceil((Nz-1)/32)
 };
+
+// One energy segment: the 32 z-lanes of a warp at plane x, row y, z tile zt.
+// Each lane squares its V and I components (float products, summed in
+// component order), a fixed shuffle tree adds the 32 lanes, and lane 0
+// stores the pair.  Every lane of the warp calls this (act = the lane's node
+// counts: z < Nz-1 and the update ran); `owner` = the segment exists
+// (y < Ny-1, zt < nzt) and this warp is the one that writes it.
+__device__ __forceinline__ void energy_segment(const DevGrid& g, int x, int y, int zt, bool act, bool owner,
+                                               float v0, float v1, float v2, float i0, float i1, float i2) {
+    float pe = 0.f, ph = 0.f;
+    if (act) {
+        pe = __fadd_rn(__fadd_rn(__fmul_rn(v0, v0), __fmul_rn(v1, v1)), __fmul_rn(v2, v2));
+        ph = __fadd_rn(__fadd_rn(__fmul_rn(i0, i0), __fmul_rn(i1, i1)), __fmul_rn(i2, i2));
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        pe = __fadd_rn(pe, __shfl_down_sync(0xffffffffu, pe, off));
+        ph = __fadd_rn(ph, __shfl_down_sync(0xffffffffu, ph, off));
+    }
+    if (owner && (threadIdx.x & 31) == 0)
+        g.eseg[((long long)x * (g.Ny - 1) + y) * g.nzt + zt] = make_float2(pe, ph);
+}
 
 template <typename IdxT>
 __device__ __forceinline__ uint32_t load_idx(const void* p, long long o) {
@@ -200,13 +229,6 @@ __device__ __forceinline__ void update_node(const DevGrid& g, float fld[3], cons
                 fld[n] = __fadd_rn(fld[n], __fmul_rn(amp[n], sig[k]));
             }
     }
-}
-
-__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
-    const float y = __fsub_rn(x, c);
-    const float t = __fadd_rn(s, y);
-    c = __fsub_rn(__fsub_rn(t, s), y);
-    s = t;
 }
 
 }  // namespace wipems
