@@ -319,10 +319,11 @@ def run_gpu(args, rank, world, local_rank):
     t_tune = time.perf_counter()
     best, _ = autotune.tune(cop, stages=(3, 4), xchunks=(4, 8, 16), steps=100, device=local_rank)
     setup["autotune_s"] = round(time.perf_counter() - t_tune, 2)
-    tiling = dict(stages=best["stages"], x_chunk=best["x_chunk"], kernel=best["kernel"])
+    tiling = dict(stages=best["stages"], x_chunk=best["x_chunk"], kernel=best["kernel"], tile_y=best["tile_y"])
     eng = Engine(cop, device=local_rank, max_timesteps=TIMESTEPS, **tiling)
-    setup["tiling"] = {"stages": best["stages"], "x_chunk": best["x_chunk"],
-                       "tile": f"32z x {eng.stats()['tile_y']}y", "kernel": best["kernel"]}
+    setup["tiling"] = {"stages": best["stages"], "x_chunk": best["x_chunk"], "tile_y": eng.stats()["tile_y"],
+                       "tile": f"32z x {eng.stats()['tile_y']}y", "kernel": best["kernel"],
+                       "searched": "tile_y 4/8, stages 3/4, x_chunk 4/8/16 (CUDA events, graph chunks)"}
     # warm-up
     for _ in range(args.warmup):
         eng.reset()

@@ -364,6 +364,13 @@ int fdtd_cop_get_info(fdtd_cop_t cop, fdtd_cop_info* info);
  * per-node E/H flag words (any pointer may be NULL).  Test use. */
 int fdtd_cop_expand(fdtd_cop_t cop, float* vv, float* vi, float* ii, float* iv,
                     uint32_t* flags_e, uint32_t* flags_h);
+/* The extension coefficients of one half (0 = E, 1 = H) as the kernels apply
+ * them, per node: ade = [9][Nx][Ny][Nz] (int[3], ext[3], lor[3] of the
+ * Lorentz/Drude ADE: v_int / v_ext / v_lor or i_*), upml = [9][Nx][Ny][Nz]
+ * (vvp|iip[3], vvfo|iifo[3], vvfn|iifn[3]); zero where a node has none.
+ * Either pointer may be NULL.  With fdtd_cop_expand this rebuilds the whole
+ * operator the engine steps on (test and inspection use). */
+int fdtd_cop_expand_ext(fdtd_cop_t cop, int half, float* ade, float* upml);
 
 /* ------------------------------------------------------------------ engine */
 

@@ -57,18 +57,58 @@ def test_mini_scenes_match_oracle(kind, kernel):
     compare(op, eng, ref, bitwise=not cop.factorized)
 
 
+def expanded_desc(op, cop):
+    """A copy of op's engine description carrying the coefficients the
+    compressed operator's kernels apply (fdtd_cop_expand / _ext: the
+    factorized vi / iv, and the UPML and ADE terms after the merging of
+    rounding variants), with the arrays kept alive on the returned object."""
+    import ctypes
+    from wipems_gb300 import _abi
+    PF = ctypes.POINTER(ctypes.c_float)
+    keep = [np.ascontiguousarray(a) for a in cop.expand()[:4]]
+    d = type(op.desc).from_buffer_copy(op.desc)
+    d.vv, d.vi, d.ii, d.iv = (a.ctypes.data_as(PF) for a in keep)
+    N = op.num_lines
+    ext = [cop.expand_ext(h) for h in (0, 1)]
+    slabs = (_abi.FdtdUpmlDesc * max(1, op.desc.num_upml))()
+    for s in range(op.desc.num_upml):
+        u = op.desc.upml[s]
+        slabs[s] = u
+        st, nl = list(u.start), list(u.num_lines)
+        sl = tuple(slice(st[a], st[a] + nl[a]) for a in range(3))
+        for h, names in ((0, ("vv", "vvfo", "vvfn")), (1, ("ii", "iifo", "iifn"))):
+            for k, name in enumerate(names):
+                arr = np.ascontiguousarray(ext[h][1][3 * k:3 * k + 3][(slice(None),) + sl])
+                keep.append(arr)
+                setattr(slabs[s], name, arr.ctypes.data_as(PF))
+    d.upml = ctypes.cast(slabs, ctypes.POINTER(_abi.FdtdUpmlDesc))
+    ades = (_abi.FdtdAdeDesc * max(1, op.desc.num_ade_orders))()
+    for o in range(op.desc.num_ade_orders):
+        a = op.desc.ade[o]
+        ades[o] = a
+        c = a.count
+        pos = [np.ctypeslib.as_array(a.pos[k], shape=(c,)) for k in range(3)] if c else [np.zeros(0, int)] * 3
+        for h, names in ((0, ("v_int", "v_ext", "v_lor")), (1, ("i_int", "i_ext", "i_lor"))):
+            for k, name in enumerate(names):
+                if not getattr(a, name):
+                    continue
+                arr = np.ascontiguousarray(ext[h][0][3 * k:3 * k + 3][:, pos[0], pos[1], pos[2]].astype(np.float32))
+                keep.append(arr)
+                setattr(ades[o], name, arr.ctypes.data_as(PF))
+    d.ade = ctypes.cast(ades, ctypes.POINTER(_abi.FdtdAdeDesc))
+    keep += [slabs, ades]
+    return d, keep
+
+
 @pytest.mark.parametrize("kind", ["graded", "mixed"])
 def test_factorized_kernels_bitwise_against_expanded_operator(kind):
     """The factorized kernels apply exactly the coefficients fdtd_cop_expand
-    reports: run the oracle on those and require bit-identical fields."""
+    and fdtd_cop_expand_ext report: run the oracle on those and require
+    bit-identical fields."""
     op = Operator(scenes.mini(kind, nr_ts=300))
     cop = CompressedOperator(op)
     assert cop.factorized
-    vv, vi, ii, iv = [np.ascontiguousarray(a) for a in cop.expand()[:4]]
-    d = type(op.desc).from_buffer_copy(op.desc)
-    import ctypes
-    PF = ctypes.POINTER(ctypes.c_float)
-    d.vv, d.vi, d.ii, d.iv = (a.ctypes.data_as(PF) for a in (vv, vi, ii, iv))
+    d, keep = expanded_desc(op, cop)
     ref = oracle.run(d, op.probes, 300, op.probe_interval, engine=oracle.BASIC)
     eng = Engine(cop)
     eng.iterate(300)
@@ -103,6 +143,7 @@ def test_chunking_graphs_and_tiles_are_invisible():
                        (dict(tile_y=4, x_chunk=5, kernel="direct"), [300]),
                        (dict(tile_y=1, x_chunk=64, kernel="direct"), [100, 200]),
                        (dict(x_chunk=3), [300]), (dict(x_chunk=64), [300]),
+                       (dict(tile_y=8, x_chunk=3), [300]), (dict(tile_y=8, stages=4, x_chunk=16), [150, 150]),
                        (dict(kernel="direct", use_graphs=True), [300])]:
         e = Engine(op, **kw)
         for c in chunks:
@@ -114,6 +155,22 @@ def test_chunking_graphs_and_tiles_are_invisible():
         assert np.array_equal(s.ts, s0.ts)
         assert np.array_equal(s.values, s0.values), kw
         assert np.array_equal(s.energy, s0.energy), kw  # energy summed in an order fixed by the grid
+
+
+def test_tma_tile_heights():
+    """The two-pass TMA kernels run 4- or 8-row tiles (the autotuner picks);
+    other heights are refused; 8-row tiles are bit-identical to the oracle
+    on a graded exact-table grid with Lorentz/Drude nodes and UPML."""
+    from wipems_gb300._abi import FdtdError
+    op = Operator(scenes.mini("mixed", nr_ts=300))
+    with pytest.raises(FdtdError):
+        Engine(op, tile_y=2)
+    cop = CompressedOperator(op, mode="exact")
+    ref = oracle.run(*oracle_inputs(op), 300, op.probe_interval, engine=oracle.BASIC)
+    eng = Engine(cop, tile_y=8)
+    assert eng.stats()["tile_y"] == 8
+    eng.iterate(300)
+    compare(op, eng, ref)
 
 
 def test_reset_and_compressed_upload_reproduce():

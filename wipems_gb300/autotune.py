@@ -1,6 +1,9 @@
-"""Autotuner for the half-step kernels: picks the TMA ring depth (stages) and
-the x-chunk (planes per block) of a workload by timing each candidate with
-CUDA events on the engine stream (Engine.profile_kernels).
+"""Autotuner for the half-step kernels.  Single jobs: the tile height (4- or
+8-row tiles of 32 z-nodes), the TMA ring depth (stages) and the x-chunk
+(planes per block); batches: the x-chunk, the CUDA-graph length and the
+resident blocks per SM of the persistent kernels (how many work items each
+SM holds at once).  Every candidate is timed the way the engine runs it,
+with CUDA events on the engine's stream.
 
     python -m wipems_gb300.autotune --workload l256
 
@@ -16,6 +19,7 @@ from pathlib import Path
 
 DEFAULT_STAGES = (3, 4)
 DEFAULT_XCHUNK = (1, 2, 4, 8, 16)
+DEFAULT_TILE_Y = (4, 8)
 
 
 def _cache_path() -> Path:
@@ -31,54 +35,65 @@ def signature(cop) -> str:
 
 
 def tune(cop, stages=DEFAULT_STAGES, xchunks=DEFAULT_XCHUNK, steps: int = 30, device: int = 0, verbose=False,
-         kernels=("tma",)):
-    """Times every (kernel, stages, x_chunk) combination the way the engine
-    runs -- CUDA-graph chunks of one probe interval, device time from CUDA
-    events over `steps` timesteps -- and returns (best, table), best
+         kernels=("tma",), tile_ys=DEFAULT_TILE_Y):
+    """Times every (kernel, tile_y, stages, x_chunk) combination the way the
+    engine runs -- CUDA-graph chunks of one probe interval, device time from
+    CUDA events over `steps` timesteps -- and returns (best, table), best
     minimising the time per timestep.  kernels may add "fused" (the
-    single-pass kernel, where the grid allows it)."""
+    single-pass kernel, where the grid allows it; its tile is fixed)."""
     from ._abi import FdtdError
     from .fdtd import Engine
     table = []
     for k in kernels:
-        for s in stages:
-            for xc in xchunks:
-                try:
-                    eng = Engine(cop, device=device, stages=s, x_chunk=xc, max_timesteps=2 * steps + 64, kernel=k)
-                except FdtdError:
-                    break  # kernel not applicable to this grid
-                eng.iterate(min(steps, 16))  # warm-up, graph instantiation
-                eng.reset()
-                eng.iterate(steps)
-                ms, _ = eng.last_timing()
-                eng.close()
-                table.append(dict(kernel=k, stages=s, x_chunk=xc, ms_step=ms / steps))
-                if verbose:
-                    print(f"kernel={k:5s} stages={s} x_chunk={xc:3d}  {ms / steps * 1e3:8.1f} us/step", flush=True)
+        for ty in (tile_ys if k == "tma" else (0,)):
+            for s in stages:
+                for xc in xchunks:
+                    try:
+                        eng = Engine(cop, device=device, stages=s, x_chunk=xc, max_timesteps=2 * steps + 64,
+                                     kernel=k, tile_y=ty)
+                    except FdtdError:
+                        break  # kernel not applicable to this grid
+                    eng.iterate(min(steps, 16))  # warm-up, graph instantiation
+                    eng.reset()
+                    eng.iterate(steps)
+                    ms, _ = eng.last_timing()
+                    tile = eng.stats()["tile_y"]
+                    eng.close()
+                    table.append(dict(kernel=k, tile_y=tile, stages=s, x_chunk=xc, ms_step=ms / steps))
+                    if verbose:
+                        print(f"kernel={k:5s} tile_y={tile} stages={s} x_chunk={xc:3d}  {ms / steps * 1e3:8.1f} us/step",
+                              flush=True)
     best = min(table, key=lambda r: r["ms_step"])
     return best, table
 
 
-def tune_batch(cops, xchunks=(8, 16), graph_steps=(8, 32), steps: int = 64, device: int = 0, verbose=False):
+def tune_batch(cops, xchunks=(8, 16), graph_steps=(8, 32), blocks_per_sm=(0, 3, 2), steps: int = 64, device: int = 0,
+               verbose=False):
     """Batched mode: times the persistent kernels of the whole job set for
-    every (x_chunk, graph_steps) pair over `steps` timesteps (fresh engines
-    per candidate, device time from CUDA events); returns (best, table)."""
+    every (x_chunk, graph_steps, blocks_per_sm) combination over `steps`
+    timesteps (fresh engines per candidate, device time from CUDA events);
+    blocks_per_sm caps the resident blocks each SM runs (0 = as many as fit)
+    -- the jobs-per-SM schedule of the work list.  Returns (best, table)."""
     from .fdtd import Batch, Engine
     table = []
-    for xc in xchunks:
-        for gs in graph_steps:
-            engines = [Engine(c, device=device, max_timesteps=steps + 4 * gs, kernel="tma") for c in cops]
-            b = Batch(engines, x_chunk=xc, graph_steps=gs)
-            b.iterate(gs)  # warm-up, graph instantiation
-            n = max(gs, steps // gs * gs)
-            b.iterate(n)
-            ms = b.stats()["last_ms"] / n
-            b.close()
-            for e in engines:
-                e.close()
-            table.append(dict(x_chunk=xc, graph_steps=gs, ms_per_step=ms))
-            if verbose:
-                print(f"x_chunk={xc:3d} graph_steps={gs:3d}  {ms * 1e3:8.1f} us/step", flush=True)
+    for bps in blocks_per_sm:
+        for xc in xchunks:
+            for gs in graph_steps:
+                engines = [Engine(c, device=device, max_timesteps=steps + 4 * gs, kernel="tma") for c in cops]
+                b = Batch(engines, x_chunk=xc, graph_steps=gs, blocks_per_sm=bps)
+                b.iterate(gs)  # warm-up, graph instantiation
+                n = max(gs, steps // gs * gs)
+                b.iterate(n)
+                st = b.stats()
+                ms = st["last_ms"] / n
+                b.close()
+                for e in engines:
+                    e.close()
+                table.append(dict(x_chunk=xc, graph_steps=gs, blocks_per_sm=bps, tile_y=8,
+                                  persistent_blocks=st["persistent_blocks"], ms_per_step=ms))
+                if verbose:
+                    print(f"blocks_per_sm={bps} x_chunk={xc:3d} graph_steps={gs:3d}  {ms * 1e3:8.1f} us/step",
+                          flush=True)
     best = min(table, key=lambda r: r["ms_per_step"])
     return best, table
 

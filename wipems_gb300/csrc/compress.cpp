@@ -217,6 +217,105 @@ void make_tuple(const Plan& P, int half, uint32_t x, uint32_t y, uint32_t z, siz
         }
 }
 
+// ---- factorized mode: snapping of rounding variants ------------------------
+// On a graded mesh the factorized VI = vi / g, and the ADE and UPML terms,
+// come out of the operator's float arithmetic with last-bit variants that
+// differ from node to node (the geometric factors cancel in exact
+// arithmetic, not in the rounded one).  Within each coefficient kind the
+// variants are mapped onto the most frequent value at most kSnapUlps float
+// steps away, so tuples that differ only by such variants merge (D192: about
+// 300 K voltage tuples -> a table that fits the uint16 index).  Zero and
+// non-finite values are never moved; the map depends on the operator alone
+// (node counts, values), not on threads or order.
+constexpr int64_t kSnapUlps = 1;
+
+inline int64_t float_order(float f) {  // adjacent floats differ by 1
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return (u >> 31) ? -(int64_t)(u & 0x7fffffffu) : (int64_t)u;
+}
+
+// the coefficient kind of every snapped slot of a tuple: VI|IV, the three
+// ADE kinds and the three UPML kinds (vv|ii stay exact)
+constexpr int kSnapKinds = 7;
+template <class F>
+void for_snap_slots(HalfTuple& t, F&& f) {
+    for (int n = 0; n < 3; ++n) f(0, t.c[3 + n]);
+    if (t.flags & TF_ADE)
+        for (int k = 0; k < 9; ++k) f(1 + k / 3, t.a[k]);
+    if (t.flags & TF_UPML)
+        for (int k = 0; k < 9; ++k) f(4 + k / 3, t.u[k]);
+}
+
+// Snaps the tuples (weighted by the nodes using them), merges the tuples
+// that became equal; returns old tuple id -> new tuple id.
+std::vector<uint32_t> snap_tuples(std::vector<HalfTuple>& tuples, const std::vector<uint64_t>& uses) {
+    std::unordered_map<uint32_t, uint64_t> hist[kSnapKinds];
+    for (size_t k = 0; k < tuples.size(); ++k) {
+        HalfTuple t = tuples[k];
+        for_snap_slots(t, [&](int kind, float& v) {
+            if (v == 0.f || !std::isfinite(v)) return;
+            uint32_t b;
+            std::memcpy(&b, &v, 4);
+            hist[kind][b] += uses[k];
+        });
+    }
+    std::unordered_map<uint32_t, uint32_t> to[kSnapKinds];
+    for (int kind = 0; kind < kSnapKinds; ++kind) {
+        struct V {
+            int64_t ord;
+            uint32_t bits;
+            uint64_t cnt;
+        };
+        std::vector<V> vals;
+        vals.reserve(hist[kind].size());
+        for (const auto& kv : hist[kind]) {
+            float f;
+            std::memcpy(&f, &kv.first, 4);
+            vals.push_back(V{float_order(f), kv.first, kv.second});
+        }
+        std::sort(vals.begin(), vals.end(), [](const V& a, const V& b) { return a.ord < b.ord; });
+        std::vector<size_t> order(vals.size());
+        for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+        std::sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+            return vals[a].cnt != vals[b].cnt ? vals[a].cnt > vals[b].cnt : vals[a].ord < vals[b].ord;
+        });
+        std::vector<int64_t> rep(vals.size(), -1);
+        for (size_t i : order) {
+            if (rep[i] >= 0) continue;
+            rep[i] = (int64_t)i;
+            for (size_t j = i; j-- > 0 && vals[i].ord - vals[j].ord <= kSnapUlps;)
+                if (rep[j] < 0) rep[j] = (int64_t)i;
+            for (size_t j = i + 1; j < vals.size() && vals[j].ord - vals[i].ord <= kSnapUlps; ++j)
+                if (rep[j] < 0) rep[j] = (int64_t)i;
+        }
+        for (size_t i = 0; i < vals.size(); ++i) to[kind][vals[i].bits] = vals[(size_t)rep[i]].bits;
+    }
+    TupleMap merged;
+    std::vector<HalfTuple> out;
+    std::vector<uint32_t> newid(tuples.size());
+    for (size_t k = 0; k < tuples.size(); ++k) {
+        HalfTuple t = tuples[k];
+        for_snap_slots(t, [&](int kind, float& v) {
+            if (v == 0.f || !std::isfinite(v)) return;
+            uint32_t b;
+            std::memcpy(&b, &v, 4);
+            const uint32_t r = to[kind].at(b);
+            std::memcpy(&v, &r, 4);
+        });
+        auto it = merged.find(t);
+        if (it == merged.end()) {
+            newid[k] = (uint32_t)out.size();
+            merged.emplace(t, newid[k]);
+            out.push_back(t);
+        } else {
+            newid[k] = it->second;
+        }
+    }
+    tuples.swap(out);
+    return newid;
+}
+
 void pack(const std::vector<HalfTuple>& tuples, HalfTables& T) {
     const size_t n = tuples.size();
     T.num_tuples = (uint32_t)n;
@@ -405,6 +504,14 @@ int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
                 }
             }
             std::vector<HalfTuple>().swap(pt[h][x]);
+        }
+        if (P.geo) {  // factorized mode: merge the tuples that differ by rounding variants only
+            std::vector<uint64_t> uses(tuples.size(), 0);
+            for (uint32_t x = 0; x < Nx; ++x)
+                for (uint32_t lid : pl[h][x]) uses[remap[x][lid]]++;
+            const std::vector<uint32_t> newid = snap_tuples(tuples, uses);
+            for (uint32_t x = 0; x < Nx; ++x)
+                for (uint32_t& id : remap[x]) id = newid[id];
         }
         HalfTables& T = h ? c->H : c->E;
         T.idx16 = tuples.size() <= 65536;
@@ -671,6 +778,28 @@ int fdtd_cop_expand(fdtd_cop_t c, float* vv, float* vi, float* ii, float* iv, ui
                     }
                     uint32_t* f = h ? flags_h : flags_e;
                     if (f) std::memcpy(&f[gi], &m[6], 4);
+                }
+            }
+    return FDTD_OK;
+}
+
+int fdtd_cop_expand_ext(fdtd_cop_t c, int half, float* ade, float* upml) {
+    if (!c || half < 0 || half > 1) return FDTD_ERR_ARG;
+    const HalfTables& T = half ? c->H : c->E;
+    const uint32_t Nx = c->N[0], Ny = c->N[1], Nz = c->N[2];
+    const size_t NN = (size_t)Nx * Ny * Nz;
+    for (uint32_t x = 0; x < Nx; ++x)
+        for (uint32_t y = 0; y < Ny; ++y)
+            for (uint32_t z = 0; z < Nz; ++z) {
+                const size_t pi = ((size_t)x * Ny + y) * c->Nzp + z;
+                const size_t gi = ((size_t)x * Ny + y) * Nz + z;
+                const uint32_t t = T.idx16 ? reinterpret_cast<const uint16_t*>(T.idx)[pi]
+                                           : reinterpret_cast<const uint32_t*>(T.idx)[pi];
+                uint32_t flags;
+                std::memcpy(&flags, &T.main[(size_t)t * TAB_MAIN * 4 + 6], 4);
+                for (int k = 0; k < 9; ++k) {
+                    if (ade) ade[k * NN + gi] = (flags & TF_ADE) ? T.ade[(size_t)t * TAB_ADE * 4 + k] : 0.f;
+                    if (upml) upml[k * NN + gi] = (flags & TF_UPML) ? T.upml[(size_t)t * TAB_UPML * 4 + k] : 0.f;
                 }
             }
     return FDTD_OK;

@@ -18,7 +18,10 @@
 //   gH(n, pos) = dH[n][p_n] * iM[nP][p_nP] * iM[nPP][p_nPP]
 // built from per-axis line arrays (main edge length dE, 1/dual length iD,
 // dual edge length dH, 1/main length iM), and the kernels multiply it back.
-// That reproduces vi within a few float ulps rather than bit-exactly.
+// That reproduces vi within a few float ulps rather than bit-exactly.  In
+// that mode the last-bit rounding variants of each coefficient kind are also
+// merged onto their most frequent neighbour (at most one float step away),
+// so that tuples differing only by such variants share one entry.
 #pragma once
 
 #include <cstdint>

@@ -25,14 +25,29 @@ namespace wipems {
 namespace {
 
 // ------------------------------------------------------------ kernel launch
+template <typename IdxT, int FEAT, bool GEO, int TY>
+void launch_volt_tma(fdtd_engine_s* e, int ts_off) {
+    constexpr bool UP = (FEAT & FEAT_UPML) != 0;
+    const size_t sm = StageLayout<IdxT, UP, (FEAT & FEAT_ADE) != 0, TY>::smem(e->stages);
+    dim3 grid((e->ti.ne[2] + 31) / 32, (e->ti.ne[1] + TY - 1) / TY, (e->ti.ne[0] + e->XC - 1) / e->XC);
+    k_volt_tma<IdxT, FEAT, GEO, TY><<<grid, dim3(32, TY), sm, e->stream>>>(e->g, e->maps, e->ti, ts_off, e->XC,
+                                                                           e->stages);
+}
+
+template <typename IdxT, int FEAT, bool GEO, bool EN, int TY>
+void launch_curr_tma(fdtd_engine_s* e, int ts_off) {
+    constexpr bool UP = (FEAT & FEAT_UPML) != 0;
+    const size_t sm = StageLayout<IdxT, UP, false, TY>::smem(e->stages);
+    dim3 grid((e->N[2] - 1 + 31) / 32, (e->N[1] - 1 + TY - 1) / TY, (e->N[0] - 1 + e->XC - 1) / e->XC);
+    k_curr_tma<IdxT, FEAT, GEO, EN, TY><<<grid, dim3(32, TY), sm, e->stream>>>(e->g, e->maps, e->ti, ts_off, e->XC,
+                                                                               e->stages);
+}
+
 template <typename IdxT, int FEAT, bool GEO>
 void launch_volt_t(fdtd_engine_s* e, int ts_off) {
     if (e->use_tma) {
-        constexpr bool UP = (FEAT & FEAT_UPML) != 0;
-        const size_t sm = StageLayout<IdxT, UP, (FEAT & FEAT_ADE) != 0>::smem(e->stages);
-        dim3 grid((e->ti.ne[2] + 31) / 32, (e->ti.ne[1] + TMA_TY - 1) / TMA_TY, (e->ti.ne[0] + e->XC - 1) / e->XC);
-        k_volt_tma<IdxT, FEAT, GEO><<<grid, dim3(32, TMA_TY), sm, e->stream>>>(e->g, e->maps, e->ti, ts_off, e->XC,
-                                                                               e->stages);
+        if (e->tma_ty == 8) launch_volt_tma<IdxT, FEAT, GEO, 8>(e, ts_off);
+        else launch_volt_tma<IdxT, FEAT, GEO, TMA_TY>(e, ts_off);
     } else {
         dim3 grid((e->N[2] + 31) / 32, (e->N[1] + e->TY - 1) / e->TY, (e->N[0] + e->XC - 1) / e->XC);
         k_volt<IdxT, FEAT, GEO><<<grid, dim3(32, e->TY), e->smem_direct, e->stream>>>(e->g, ts_off, e->XC);
@@ -42,11 +57,8 @@ void launch_volt_t(fdtd_engine_s* e, int ts_off) {
 template <typename IdxT, int FEAT, bool GEO, bool EN>
 void launch_curr_t(fdtd_engine_s* e, int ts_off) {
     if (e->use_tma) {
-        constexpr bool UP = (FEAT & FEAT_UPML) != 0;
-        const size_t sm = StageLayout<IdxT, UP>::smem(e->stages);
-        dim3 grid((e->N[2] - 1 + 31) / 32, (e->N[1] - 1 + TMA_TY - 1) / TMA_TY, (e->N[0] - 1 + e->XC - 1) / e->XC);
-        k_curr_tma<IdxT, FEAT, GEO, EN><<<grid, dim3(32, TMA_TY), sm, e->stream>>>(e->g, e->maps, e->ti, ts_off,
-                                                                                   e->XC, e->stages);
+        if (e->tma_ty == 8) launch_curr_tma<IdxT, FEAT, GEO, EN, 8>(e, ts_off);
+        else launch_curr_tma<IdxT, FEAT, GEO, EN, TMA_TY>(e, ts_off);
     } else {
         dim3 grid((e->N[2] + 31) / 32, (e->N[1] + e->TY - 1) / e->TY, (e->N[0] - 1 + e->XC - 1) / e->XC);
         k_curr<IdxT, FEAT, GEO, EN><<<grid, dim3(32, e->TY), e->smem_direct, e->stream>>>(e->g, ts_off, e->XC);
@@ -444,14 +456,17 @@ int make_tma_maps(const fdtd_engine_s* e, TmaMaps* m, uint32_t rows) {
     return FDTD_OK;
 }
 
-int make_maps(fdtd_engine_s* e) { return make_tma_maps(e, &e->maps, TMA_TY); }
+int make_maps(fdtd_engine_s* e) { return make_tma_maps(e, &e->maps, (uint32_t)e->tma_ty); }
 
 template <typename IdxT, int FEAT, bool GEO>
 cudaError_t smem_attr_one(int bytes) {
     const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    cudaError_t r[3] = {cudaFuncSetAttribute(k_volt_tma<IdxT, FEAT, GEO>, a, bytes),
-                        cudaFuncSetAttribute(k_curr_tma<IdxT, FEAT, GEO, true>, a, bytes),
-                        cudaFuncSetAttribute(k_curr_tma<IdxT, FEAT, GEO, false>, a, bytes)};
+    cudaError_t r[6] = {cudaFuncSetAttribute(k_volt_tma<IdxT, FEAT, GEO, TMA_TY>, a, bytes),
+                        cudaFuncSetAttribute(k_curr_tma<IdxT, FEAT, GEO, true, TMA_TY>, a, bytes),
+                        cudaFuncSetAttribute(k_curr_tma<IdxT, FEAT, GEO, false, TMA_TY>, a, bytes),
+                        cudaFuncSetAttribute(k_volt_tma<IdxT, FEAT, GEO, 8>, a, bytes),
+                        cudaFuncSetAttribute(k_curr_tma<IdxT, FEAT, GEO, true, 8>, a, bytes),
+                        cudaFuncSetAttribute(k_curr_tma<IdxT, FEAT, GEO, false, 8>, a, bytes)};
     for (cudaError_t x : r)
         if (x != cudaSuccess) return x;
     return cudaSuccess;
@@ -550,6 +565,12 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     }
     e->use_tma = kern != 1;
     e->fused = kern == 2;
+    // the two-pass TMA kernels come in 4- and 8-row tiles (4 by default)
+    e->tma_ty = (opts && opts->tile_y > 0) ? opts->tile_y : TMA_TY;
+    if (e->use_tma && !e->fused && e->tma_ty != 4 && e->tma_ty != 8) {
+        set_error("the TMA kernels take tile_y 4 or 8 (0 = 4)");
+        return FDTD_ERR_ARG;
+    }
     e->stages = (opts && opts->stages > 0) ? opts->stages : 3;
     if (e->stages < 3 || e->stages > TMA_MAX_STAGES) {
         set_error("stages must be 3..8");
@@ -572,7 +593,7 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
         int sms = 0;
         CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->device));
         // about 1280 resident threads per SM (5 blocks of 32 x 8, 10 of 32 x 4)
-        e->XC = auto_x_chunk({e->N}, (uint64_t)(1280 / (32 * TMA_TY)) * (uint64_t)sms);
+        e->XC = auto_x_chunk({e->N}, (uint64_t)(1280 / (32 * e->tma_ty)) * (uint64_t)sms);
     }
     e->comp = c->comp;
     e->geo_on = c->geo;
@@ -755,8 +776,11 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
         if (need > 48 * 1024 && (rc = set_fused_attrs((int)need))) return rc;
     } else if (e->use_tma) {
         if ((rc = make_maps(e))) return rc;
-        const size_t need = (e->feat & FEAT_UPML) ? StageLayout<uint32_t, true, true>::smem(e->stages)
-                                                  : StageLayout<uint32_t, false, true>::smem(e->stages);
+        const size_t need = e->tma_ty == 8
+                                ? ((e->feat & FEAT_UPML) ? StageLayout<uint32_t, true, true, 8>::smem(e->stages)
+                                                         : StageLayout<uint32_t, false, true, 8>::smem(e->stages))
+                                : ((e->feat & FEAT_UPML) ? StageLayout<uint32_t, true, true>::smem(e->stages)
+                                                         : StageLayout<uint32_t, false, true>::smem(e->stages));
         if (need > 48 * 1024 && (rc = set_smem_attrs((int)need))) return rc;
     }
     return reset_state(e);
@@ -1454,7 +1478,7 @@ int fdtd_engine_get_stats(fdtd_engine_t e, fdtd_engine_stats* st) {
     st->num_ade_nodes = e->ade_nodes;
     st->padded_nz = (uint32_t)e->Nzp;
     st->device_bytes = e->device_bytes;
-    st->tile_y = (uint32_t)(e->use_tma ? TMA_TY : e->TY);
+    st->tile_y = (uint32_t)(e->fused ? FU_TY : (e->use_tma ? e->tma_ty : e->TY));
     st->x_chunk = (uint32_t)e->XC;
     st->kernel = e->fused ? 2u : (e->use_tma ? 3u : 1u);
     return FDTD_OK;

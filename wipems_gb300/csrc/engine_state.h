@@ -144,7 +144,8 @@ struct fdtd_engine_s {
     bool need_initial_sample = true;
     int feat = 0;
     bool geo_on = false;
-    int TY = 8;
+    int TY = 8;       // direct kernels: tile rows
+    int tma_ty = 4;   // two-pass TMA kernels: tile rows (4 or 8)
     int XC = 8;
     bool use_tma = true;
     bool fused = false;      // single-pass kernel, double-buffered fields

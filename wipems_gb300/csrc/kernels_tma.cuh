@@ -451,32 +451,33 @@ __device__ __forceinline__ void init_ring(uint64_t* bars, int STAGES) {
 }
 
 // ---------------------------------------------------------- single job
-template <typename IdxT, int FEAT, bool GEO>
-__global__ void __launch_bounds__(TMA_TY * 32) k_volt_tma(const DevGrid g, const __grid_constant__ TmaMaps m,
-                                                          const TileInfo ti, int ts_off, int XC, int STAGES) {
-    using L = StageLayout<IdxT, (FEAT & FEAT_UPML) != 0, (FEAT & FEAT_ADE) != 0>;
+// TY: tile rows (4 or 8; the tensor maps' box height matches)
+template <typename IdxT, int FEAT, bool GEO, int TY>
+__global__ void __launch_bounds__(TY * 32) k_volt_tma(const DevGrid g, const __grid_constant__ TmaMaps m,
+                                                      const TileInfo ti, int ts_off, int XC, int STAGES) {
+    using L = StageLayout<IdxT, (FEAT & FEAT_UPML) != 0, (FEAT & FEAT_ADE) != 0, TY>;
     extern __shared__ __align__(128) float smem_raw[];
     float* smem = aligned_smem(smem_raw);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * STAGES);
     if (*g.d_done) return;
     init_ring(bars, STAGES);
     uint32_t ring = 0;
-    volt_tile<IdxT, FEAT, GEO>(g, m, ti, blockIdx.x, blockIdx.y, blockIdx.z, XC, STAGES, smem, bars, ring,
-                               *g.d_ts + ts_off);
+    volt_tile<IdxT, FEAT, GEO, TY>(g, m, ti, blockIdx.x, blockIdx.y, blockIdx.z, XC, STAGES, smem, bars, ring,
+                                   *g.d_ts + ts_off);
 }
 
-template <typename IdxT, int FEAT, bool GEO, bool ENERGY>
-__global__ void __launch_bounds__(TMA_TY * 32) k_curr_tma(const DevGrid g, const __grid_constant__ TmaMaps m,
-                                                          const TileInfo ti, int ts_off, int XC, int STAGES) {
-    using L = StageLayout<IdxT, (FEAT & FEAT_UPML) != 0>;
+template <typename IdxT, int FEAT, bool GEO, bool ENERGY, int TY>
+__global__ void __launch_bounds__(TY * 32) k_curr_tma(const DevGrid g, const __grid_constant__ TmaMaps m,
+                                                      const TileInfo ti, int ts_off, int XC, int STAGES) {
+    using L = StageLayout<IdxT, (FEAT & FEAT_UPML) != 0, false, TY>;
     extern __shared__ __align__(128) float smem_raw[];
     float* smem = aligned_smem(smem_raw);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * STAGES);
     if (*g.d_done) return;
     init_ring(bars, STAGES);
     uint32_t ring = 0;
-    curr_tile<IdxT, FEAT, GEO>(g, m, ti, blockIdx.x, blockIdx.y, blockIdx.z, XC, STAGES, smem, bars, ring,
-                               *g.d_ts + ts_off, ENERGY);
+    curr_tile<IdxT, FEAT, GEO, TY>(g, m, ti, blockIdx.x, blockIdx.y, blockIdx.z, XC, STAGES, smem, bars, ring,
+                                   *g.d_ts + ts_off, ENERGY);
 }
 
 // ---------------------------------------------------------- batched jobs

@@ -424,6 +424,17 @@ class CompressedOperator:
                                     fh.ctypes.data_as(_abi.PU32)), "fdtd_cop_expand")
         return out + [fe, fh]
 
+    def expand_ext(self, half: int):
+        """The ADE and UPML coefficients of one half (0 = E, 1 = H) as the
+        kernels apply them: two [9][Nx][Ny][Nz] arrays (int/ext/lor, and
+        vvp/vvfo/vvfn or the current-side terms), zero where a node has none."""
+        shape = (9,) + self.op.num_lines
+        ade = np.empty(shape, np.float32)
+        upml = np.empty(shape, np.float32)
+        check(lib().fdtd_cop_expand_ext(self._h, int(half), ade.ctypes.data_as(_abi.PF), upml.ctypes.data_as(_abi.PF)),
+              "fdtd_cop_expand_ext")
+        return ade, upml
+
 
 class Engine:
     """Engine_CUDA on one GPU.  op is an Operator (compressed here) or a

@@ -28,7 +28,7 @@ def single(kind: str, steps: int = 0, device: int = 0) -> dict:
     best, _ = autotune.tune(cop, stages=(3, 4), steps=40, device=device)
     nts = steps or sc.nr_ts
     eng = Engine(cop, device=device, max_timesteps=nts + 100, stages=best["stages"], x_chunk=best["x_chunk"],
-                 kernel=best["kernel"])
+                 kernel=best["kernel"], tile_y=best["tile_y"])
     eng.iterate(min(nts, 50))     # warm-up (graph instantiation)
     eng.reset()
     eng.iterate(nts)
@@ -76,7 +76,7 @@ def extensions(steps: int = 1000, device: int = 0) -> list:
         if best is None:
             best, _ = autotune.tune(cop, stages=(3, 4), steps=40, device=device)
         eng = Engine(cop, device=device, max_timesteps=steps + 100, stages=best["stages"], x_chunk=best["x_chunk"],
-                     kernel=best["kernel"])
+                     kernel=best["kernel"], tile_y=best["tile_y"])
         if name == "fd":
             eng.set_frequencies(np.linspace(1e9, 20e9, 64))
         eng.iterate(50)  # warm-up (graph instantiation)
@@ -114,7 +114,7 @@ def b96(n_jobs: int = 96, timesteps: int = 1500, device: int = 0) -> dict:
         e.close()
     best, table = autotune.tune_batch(cops, device=device)
     engines = [Engine(c, device=device, max_timesteps=timesteps, kernel="tma") for c in cops]
-    b = Batch(engines, x_chunk=best["x_chunk"], graph_steps=best["graph_steps"])
+    b = Batch(engines, x_chunk=best["x_chunk"], graph_steps=best["graph_steps"], blocks_per_sm=best["blocks_per_sm"])
     b.iterate(timesteps)
     st = b.stats()
     b.close()
