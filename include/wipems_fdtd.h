@@ -515,6 +515,19 @@ int fdtd_engine_get_volt(fdtd_engine_t eng, uint32_t n, uint32_t x,
                          uint32_t y, uint32_t z, float* v);
 int fdtd_engine_get_curr(fdtd_engine_t eng, uint32_t n, uint32_t x,
                          uint32_t y, uint32_t z, float* v);
+/* Engine::SetVolt / SetCurr (engine.h:58-61): one field value. */
+int fdtd_engine_set_volt(fdtd_engine_t eng, uint32_t n, uint32_t x,
+                         uint32_t y, uint32_t z, float v);
+int fdtd_engine_set_curr(fdtd_engine_t eng, uint32_t n, uint32_t x,
+                         uint32_t y, uint32_t z, float v);
+/* One probe integral of the current fields, unweighted, in the reference's
+ * order and precision: a voltage line integral (type 0,
+ * Engine_Interface_FDTD::CalcVoltageIntegral, engine_interface_fdtd.cpp:
+ * 200-226) or a current loop (type 1, ProcessCurrent::CalcIntegral,
+ * processcurrent.cpp:93-168).  For an openEMS processing that evaluates
+ * integrals on its own schedule (Engine_Interface_CUDA). */
+int fdtd_engine_probe_now(fdtd_engine_t eng, const fdtd_probe_desc* p,
+                          double* value);
 
 typedef struct {
     uint32_t num_tuples;      /* unique coefficient tuples after compression */

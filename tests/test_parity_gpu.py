@@ -381,3 +381,23 @@ def test_rlc_through_graph_chunks_and_single_steps():
     from wipems_gb300._abi import FdtdError
     with pytest.raises(FdtdError, match="lumped RLC"):
         Engine(Operator(scenes.mini("rlc", nr_ts=100)), kernel="fused")
+
+
+def test_probe_now_and_field_writes():
+    """fdtd_engine_probe_now evaluates a voltage / current integral on the
+    current fields in the sampler's order and precision (the engine
+    interface of an openEMS processing that samples on its own schedule):
+    times the probe's weight it equals the sample recorded at that
+    timestep, bit for bit.  SetVolt / SetCurr write one value."""
+    op = Operator(scenes.mini("upml", nr_ts=300))
+    eng = Engine(op)
+    eng.iterate(4 * op.probe_interval)
+    s = eng.samples()
+    assert s.ts[-1] == eng.num_timesteps
+    for k, p in enumerate(op.probes):
+        assert eng.probe_now(p) * p.weight == s.values[-1, k], k
+    v = eng.get_volt(2, 5, 6, 7)
+    eng.set_volt(2, 5, 6, 7, v + 1.5)
+    assert eng.get_volt(2, 5, 6, 7) == np.float32(v + 1.5)
+    eng.set_curr(0, 3, 4, 5, -2.25)
+    assert eng.get_curr(0, 3, 4, 5) == -2.25

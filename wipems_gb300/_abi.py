@@ -200,6 +200,9 @@ SIGNATURES = [
     ("fdtd_engine_get_fields", C.c_int, [_P, PF, PF]),
     ("fdtd_engine_get_volt", C.c_int, [_P, u32, u32, u32, u32, PF]),
     ("fdtd_engine_get_curr", C.c_int, [_P, u32, u32, u32, u32, PF]),
+    ("fdtd_engine_set_volt", C.c_int, [_P, u32, u32, u32, u32, C.c_float]),
+    ("fdtd_engine_set_curr", C.c_int, [_P, u32, u32, u32, u32, C.c_float]),
+    ("fdtd_engine_probe_now", C.c_int, [_P, C.POINTER(FdtdProbeDesc), C.POINTER(C.c_double)]),
     ("fdtd_engine_get_stats", C.c_int, [_P, C.POINTER(FdtdEngineStats)]),
     ("fdtd_engine_last_timing", C.c_int, [_P, PD, C.POINTER(C.c_uint64)]),
     ("fdtd_engine_profile_kernels", C.c_int, [_P, u32, PD, PD]),

@@ -1431,6 +1431,72 @@ int fdtd_engine_get_curr(fdtd_engine_t e, uint32_t n, uint32_t x, uint32_t y, ui
     return get_one(e, e ? e->cur_I() : nullptr, n, x, y, z, v);
 }
 
+static int set_one(fdtd_engine_t e, float* base, uint32_t n, uint32_t x, uint32_t y, uint32_t z, float v) {
+    if (!e || n > 2 || x >= e->N[0] || y >= e->N[1] || z >= e->N[2]) {
+        set_error("field access out of range");
+        return FDTD_ERR_ARG;
+    }
+    if (e->pending) {
+        set_error("field write: wait for the asynchronous iterate first");
+        return FDTD_ERR_STATE;
+    }
+    CK(cudaSetDevice(e->device));
+    const long long off = n * e->comp + (long long)x * e->g.sx + (long long)y * e->Nzp + z;
+    CK(cudaMemcpyAsync(base + off, &v, sizeof(float), cudaMemcpyHostToDevice, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return FDTD_OK;
+}
+int fdtd_engine_set_volt(fdtd_engine_t e, uint32_t n, uint32_t x, uint32_t y, uint32_t z, float v) {
+    return set_one(e, e ? e->cur_V() : nullptr, n, x, y, z, v);
+}
+int fdtd_engine_set_curr(fdtd_engine_t e, uint32_t n, uint32_t x, uint32_t y, uint32_t z, float v) {
+    return set_one(e, e ? e->cur_I() : nullptr, n, x, y, z, v);
+}
+
+int fdtd_engine_probe_now(fdtd_engine_t e, const fdtd_probe_desc* p, double* value) {
+    if (!e || !p || !value || (p->type != 0 && p->type != 1)) {
+        set_error("fdtd_engine_probe_now: a voltage (0) or current (1) probe is needed");
+        return FDTD_ERR_ARG;
+    }
+    if (e->pending) {
+        set_error("fdtd_engine_probe_now: wait for the asynchronous iterate first");
+        return FDTD_ERR_STATE;
+    }
+    std::vector<ProbeEntry> ent;
+    int rc = probe_entries(e, p, ent);
+    if (rc) return rc;
+    *value = 0.0;
+    if (ent.empty()) return FDTD_OK;
+    CK(cudaSetDevice(e->device));
+    uint64_t& tb = e->device_bytes;
+    if (e->now_entries.n < ent.size()) {
+        e->now_entries.release();
+        if ((rc = e->now_entries.alloc(ent.size(), tb, e->stream))) return rc;
+    }
+    if (!e->now_misc.p && (rc = e->now_misc.alloc(4, tb, e->stream))) return rc;
+    // now_misc: [0] the sum, [1] div = 0 (an integral), [2..3] first = {0, count} as ints
+    double misc[4] = {0.0, 0.0, 0.0, 0.0};
+    int first[2] = {0, (int)ent.size()};
+    std::memcpy(&misc[2], first, sizeof(first));
+    CK(cudaMemcpyAsync(e->now_entries.p, ent.data(), ent.size() * sizeof(ProbeEntry), cudaMemcpyHostToDevice,
+                       e->stream));
+    CK(cudaMemcpyAsync(e->now_misc.p, misc, sizeof(misc), cudaMemcpyHostToDevice, e->stream));
+    ProbeSet ps{};
+    ps.entries = e->now_entries.p;
+    ps.first = reinterpret_cast<const int*>(e->now_misc.p + 2);
+    ps.div = e->now_misc.p + 1;
+    ps.nprobe = 1;
+    DevGrid g = e->g;
+    g.V = e->cur_V();
+    g.I = e->cur_I();
+    g.V2 = nullptr;  // the current buffers are named directly
+    k_probe_now<<<1, 32, 0, e->stream>>>(ps, g, e->now_misc.p);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(value, e->now_misc.p, sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return FDTD_OK;
+}
+
 int fdtd_engine_profile_kernels(fdtd_engine_t e, uint32_t n_steps, double* ms_volt, double* ms_curr) {
     if (!e || n_steps == 0) return FDTD_ERR_ARG;
     CK(cudaSetDevice(e->device));

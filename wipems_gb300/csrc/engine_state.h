@@ -102,6 +102,8 @@ struct fdtd_engine_s {
     int* p_done() const { return ctl.p + 3; }
     DevBuf<double> d_eacc;  // [2]: running energy maximum (end criterion)
     DevBuf<double> d_energy_tmp;
+    DevBuf<ProbeEntry> now_entries;  // fdtd_engine_probe_now scratch, grown on demand
+    DevBuf<double> now_misc;
     DevBuf<float2> eseg;    // energy segments (DevGrid::eseg)
     DevBuf<double2> eplane; // energy plane sums (DevGrid::eplane)
     // probes

@@ -392,6 +392,12 @@ __device__ __forceinline__ double2 plane_energy(const DevGrid& g, int x) {
     return r;
 }
 
+// one probe integral of the current fields (one warp), written to out[0]
+static __global__ void k_probe_now(ProbeSet ps, const DevGrid g, double* out) {
+    const double v = probe_value(ps, g, 0, 0, threadIdx.x & 31);
+    if (threadIdx.x == 0) out[0] = v;
+}
+
 // one block (256 threads) per x plane: eplane[x] from the plane's segments
 static __global__ void __launch_bounds__(256) k_energy_planes(const DevGrid g) {
     const double2 r = plane_energy(g, blockIdx.x);

@@ -610,6 +610,19 @@ class Engine:
         check(lib().fdtd_engine_get_volt(self._h, n, x, y, z, C.byref(v)), "get_volt")
         return v.value
 
+    def set_volt(self, n, x, y, z, value: float):
+        check(lib().fdtd_engine_set_volt(self._h, n, x, y, z, float(value)), "fdtd_engine_set_volt")
+
+    def set_curr(self, n, x, y, z, value: float):
+        check(lib().fdtd_engine_set_curr(self._h, n, x, y, z, float(value)), "fdtd_engine_set_curr")
+
+    def probe_now(self, probe) -> float:
+        """The unweighted integral of a voltage / current probe descriptor on
+        the current fields (fdtd_engine_probe_now)."""
+        v = C.c_double()
+        check(lib().fdtd_engine_probe_now(self._h, C.byref(probe), C.byref(v)), "fdtd_engine_probe_now")
+        return v.value
+
     def get_curr(self, n, x, y, z) -> float:
         v = C.c_float()
         check(lib().fdtd_engine_get_curr(self._h, n, x, y, z, C.byref(v)), "get_curr")
