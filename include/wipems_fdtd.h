@@ -87,6 +87,18 @@ int fdtd_scene_set_mur_velocity(fdtd_scene_t s, const double v_phase[6]);
  * (excitation.cpp:55-62).  nr_ts = NumberOfTimesteps (signal length cap). */
 int fdtd_scene_set_gauss_excite(fdtd_scene_t s, double f0, double fc,
                                 uint32_t nr_ts);
+/* Sinusoidal excitation of frequency f0, Excitation::SetupSinusoidal /
+ * CalcSinusExcitation (excitation.cpp:65-71, 273-295): two periods of
+ * sin(2 pi f0 t) (0 at t = 0), repeated with the period; the operator
+ * shortens dT so that 1/f0 is a whole number of timesteps
+ * (Operator::CalcECOperator, operator.cpp:1001-1007).  nr_ts > 0. */
+int fdtd_scene_set_sinus_excite(fdtd_scene_t s, double f0, uint32_t nr_ts);
+/* Dirac pulse (1 at timestep 1 only) and step (1 from timestep 0 on),
+ * Excitation::SetupDiracPulse / SetupStepExcite and their Calc functions
+ * (excitation.cpp:73-85, 179-218); both sample the probes every timestep
+ * (Nyquist number 1).  f_max = <FDTD f_max>. */
+int fdtd_scene_set_dirac_excite(fdtd_scene_t s, double f_max, uint32_t nr_ts);
+int fdtd_scene_set_step_excite(fdtd_scene_t s, double f_max, uint32_t nr_ts);
 /* <FDTD OverSampling=...> (openems.cpp:830-832, default 4). */
 int fdtd_scene_set_oversampling(fdtd_scene_t s, uint32_t oversampling);
 
@@ -137,6 +149,22 @@ int fdtd_scene_add_lorentz(fdtd_scene_t s, int priority,
                            const double* eps_plasma_f,
                            const double* eps_relax_t,
                            const double* eps_lor_pole_f);
+/* Drude / Lorentz material with both the electric and the magnetic
+ * families of CSPropLorentzMaterial: per order o < order, eps_* act on the
+ * E edges (from EC_C, the E-side ADE) and mue_plasma_f[o] (Hz),
+ * mue_relax_t[o] (s), mue_lor_pole_f[o] (Hz, 0 = Drude) on the H edges
+ * (from EC_L, the H-side ADE), operator_ext_lorentzmaterial.cpp:210-276.
+ * Any of the six arrays may be NULL (all zeros: that family is off). */
+int fdtd_scene_add_lorentz_material(fdtd_scene_t s, int priority,
+                                    const double start[3], const double stop[3],
+                                    double eps_r, double kappa, double mue_r,
+                                    double sigma, int order,
+                                    const double* eps_plasma_f,
+                                    const double* eps_relax_t,
+                                    const double* eps_lor_pole_f,
+                                    const double* mue_plasma_f,
+                                    const double* mue_relax_t,
+                                    const double* mue_lor_pole_f);
 /* Probe box: type 0 voltage (line integral, ProcessVoltage), type 1 current
  * (loop around a surface, ProcessCurrent); weight multiplies the integral;
  * norm_dir = normal direction of a current probe or -1.

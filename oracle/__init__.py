@@ -91,6 +91,8 @@ def _scene_struct(spec: dict):
         sc.pml_size[k] = spec["pml_size"][k]
         sc.mur_vph[k] = spec["mur_vph"][k]
     sc.f0, sc.fc = spec["f0"], spec["fc"]
+    sc.excite_type = spec.get("excite_type", 0)
+    sc.f_max = spec.get("f_max", 0.0)
     sc.nr_ts = spec["nr_ts"]
     sc.oversampling = spec["oversampling"]
     prims = (abi.OraclePrim * max(1, len(spec["prims"])))()
@@ -201,6 +203,7 @@ def desc_arrays(desc) -> dict:
     L = int(desc.signal_length)
     out["signal_volt"] = _arr(desc.signal_volt, L, np.float32)
     out["signal_curr"] = _arr(desc.signal_curr, L, np.float32)
+    out["signal_period_ts"] = np.array([desc.signal_period_ts])
     for f in range(desc.num_mur):
         m = desc.mur[f]
         out[f"mur{f}.geom"] = np.array([m.ny, m.top, m.line, m.shift, m.n_p, m.n_pp, m.start_ts])

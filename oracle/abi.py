@@ -32,7 +32,8 @@ class OracleScene(C.Structure):
                 ("bg_eps", C.c_double), ("bg_mue", C.c_double), ("bg_kappa", C.c_double), ("bg_sigma", C.c_double),
                 ("bc", C.c_int * 6), ("pml_size", u32 * 6), ("mur_vph", C.c_double * 6),
                 ("f0", C.c_double), ("fc", C.c_double), ("nr_ts", u32), ("oversampling", u32),
-                ("num_prims", u32), ("prims", C.POINTER(OraclePrim))]
+                ("num_prims", u32), ("prims", C.POINTER(OraclePrim)), ("excite_type", C.c_int),
+                ("f_max", C.c_double)]
 
 
 class OracleOpInfo(C.Structure):

@@ -32,6 +32,9 @@
 //   Operator_Ext_LorentzMaterial::BuildExtension  extensions/operator_ext_lorentzmaterial.cpp:117-414
 //   Operator_Ext_LumpedRLC::BuildExtension   extensions/operator_ext_lumpedRLC.cpp:112-486
 //   Excitation::CalcGaussianPulsExcitation   FDTD/excitation.cpp:151-177
+//   Excitation::CalcSinusExcitation, CalcDiracPulsExcitation,
+//   CalcStepExcitation                       FDTD/excitation.cpp:179-218, 273-295
+//   periodic-signal timestep                 FDTD/operator.cpp:999-1007
 //   CalcNyquistNum                       tools/useful.cpp:30-36
 //   probe snapping: openEMS::SetupProcessing openems.cpp:470-540,
 //     Processing::DefineStartStopCoord Common/processing.cpp:180-189,
@@ -95,6 +98,8 @@ typedef struct {
     uint32_t oversampling;
     uint32_t num_prims;
     const oracle_prim* prims;
+    int excite_type;  // Excitation::ExciteTypes: 0 Gaussian, 1 sinusoid, 2 Dirac, 3 step
+    double f_max;
 } oracle_scene;
 
 typedef struct {
@@ -232,6 +237,8 @@ struct oracle_operator_s {
     uint32_t pml[6];
     double mur_vph[6];
     double f0, fc;
+    int excite_type = 0;
+    double signal_period = 0;  // Excitation::m_SignalPeriod
     uint32_t nr_ts, oversampling;
     int threads;
     Csx csx;
@@ -245,7 +252,7 @@ struct oracle_operator_s {
     std::vector<float> v_amp, c_amp;
     std::vector<uint32_t> v_delay, c_delay;
     std::vector<float> sig_v, sig_c;
-    uint32_t length = 0, nyquist = 0, max_exc_ts = 0, probe_interval = 1;
+    uint32_t length = 0, nyquist = 0, max_exc_ts = 0, probe_interval = 1, period_ts = 0;
     std::vector<MurO> mur;
     std::vector<UpmlSlabO> upml;
     std::vector<AdeO> ade;
@@ -1281,9 +1288,15 @@ struct oracle_operator_s {
         cvt(vvd, r_vvd); cvt(ib0v, r_ib0); cvt(b1v, r_b1); cvt(b2v, r_b2);
     }
 
-    // Excitation::CalcGaussianPulsExcitation (excitation.cpp:151-177) and
     // CalcNyquistNum (tools/useful.cpp:30-36)
-    void BuildSignal() {
+    uint32_t CalcNyquistNum(double fmax) const {
+        if (fmax == 0) return UINT_MAX;
+        if (dT == 0) return 1;
+        double T0 = 1 / fmax;
+        return (uint32_t)std::floor(T0 / 2 / dT);
+    }
+    // Excitation::CalcGaussianPulsExcitation (excitation.cpp:151-177)
+    void CalcGaussianPulsExcitation() {
         length = (uint32_t)std::ceil(2.0 * 9.0 / (2.0 * kPI * fc) / dT);
         if (length > nr_ts) length = nr_ts;
         sig_v.resize(length);
@@ -1296,13 +1309,38 @@ struct oracle_operator_s {
             sig_c[n] = (float)(std::cos(2.0 * kPI * f0 * (t - 9.0 / (2.0 * kPI * fc))) *
                                std::exp(-1 * std::pow(2.0 * kPI * fc * t / 3.0 - 3, 2)));
         }
-        double fmax = f0 + fc;
-        if (fmax == 0)
-            nyquist = UINT_MAX;
-        else {
-            double T0 = 1 / fmax;
-            nyquist = (uint32_t)std::floor(T0 / 2 / dT);
+        nyquist = CalcNyquistNum(f0 + fc);
+    }
+    // Excitation::CalcSinusExcitation (excitation.cpp:273-295)
+    void CalcSinusExcitation() {
+        length = (uint32_t)std::round(2.0 / f0 / dT);
+        sig_v.resize(length);
+        sig_c.resize(length);
+        if (length) sig_v[0] = 0.0f, sig_c[0] = 0.0f;
+        for (uint32_t n = 1; n < length; ++n) {
+            double t = n * dT;
+            sig_v[n] = (float)std::sin(2.0 * kPI * f0 * t);
+            t += 0.5 * dT;
+            sig_c[n] = (float)std::sin(2.0 * kPI * f0 * t);
         }
+        nyquist = CalcNyquistNum(f0);
+    }
+    // Excitation::CalcDiracPulsExcitation / CalcStepExcitation (excitation.cpp:179-218)
+    void CalcUnitExcitation(bool step) {
+        length = 2;
+        sig_v = {step ? 1.0f : 0.0f, 1.0f};
+        sig_c = {step ? 1.0f : 0.0f, 1.0f};
+        nyquist = 1;
+    }
+    // Excitation::buildExcitationSignal (excitation.cpp:96-134)
+    void BuildSignal() {
+        switch (excite_type) {
+            case 0: CalcGaussianPulsExcitation(); break;
+            case 1: CalcSinusExcitation(); break;
+            default: CalcUnitExcitation(excite_type == 3); break;
+        }
+        // Engine_Ext_Excitation's period (engine_ext_excitation.cpp:44-46)
+        period_ts = signal_period > 0 ? (uint32_t)int(signal_period / dT) : 0;
         // Excitation::GetMaxExcitationTimestep (excitation.cpp:136-149)
         float maxAmp = 0;
         max_exc_ts = 0;
@@ -1385,6 +1423,13 @@ struct oracle_operator_s {
         Calc_EC();
         dT = CalcTimestep_Var3();
         if (!(dT > 0) || dT >= 1e200) return -1;
+        // m_TimeStepFactor 1; a periodic signal fits a whole number of
+        // timesteps into its period (operator.cpp:999-1007)
+        if (signal_period > 0) {
+            unsigned int TS = (unsigned int)std::ceil(signal_period / dT);
+            double new_dT = signal_period / TS;
+            dT = new_dT;
+        }
         vv.assign(3 * NN, 0.f);
         vi.assign(3 * NN, 0.f);
         ii.assign(3 * NN, 0.f);
@@ -1464,8 +1509,13 @@ int oracle_operator_build(const oracle_scene* S, int threads, oracle_operator_s*
         op->pml[k] = S->bc[k] == 3 ? S->pml_size[k] : 0;
         op->mur_vph[k] = S->mur_vph[k];
     }
-    op->f0 = S->f0;
-    op->fc = S->fc;
+    // openEMS::Parse_XML_FDTDSetup / Excitation::Setup* (openems.cpp:900-927,
+    // excitation.cpp:56-85): the Dirac and step leave m_f0 / m_fc unset in
+    // the reference; 0 here
+    op->excite_type = S->excite_type;
+    op->f0 = S->excite_type <= 1 ? S->f0 : 0.0;
+    op->fc = S->excite_type == 0 ? S->fc : 0.0;
+    op->signal_period = S->excite_type == 1 ? 1 / S->f0 : 0.0;
     op->nr_ts = S->nr_ts;
     op->oversampling = S->oversampling ? S->oversampling : 4;
     op->threads = threads > 0 ? threads : (int)std::max(1u, std::thread::hardware_concurrency());
@@ -1576,7 +1626,7 @@ int oracle_operator_describe(oracle_operator_s* op, fdtd_op_desc* d) {
     d->signal_length = op->length;
     d->signal_volt = op->sig_v.data();
     d->signal_curr = op->sig_c.data();
-    d->signal_period_ts = 0;
+    d->signal_period_ts = op->period_ts;
     for (int n = 0; n < 3; ++n) d->lines[n] = op->lines[n].data();
     d->unit = op->unit;
     return 0;

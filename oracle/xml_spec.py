@@ -9,12 +9,13 @@ reader, independent of the engine library's, restating:
     openEMS::Parse_XML_FDTDSetup     openems.cpp:796-936 (NumberOfTimesteps,
         endCriteria, OverSampling only when > 1, BoundaryCond codes or
         PEC / PMC / MUR / PML_n names, MUR_PhaseVelocity[_face], the
-        Gaussian <Excitation Type="0" f0 fc>)
+        <Excitation> of Type 0 (Gaussian: f0 fc), 1 (sinusoid: f0), 2 / 3
+        (Dirac / step: <FDTD f_max>))
     default PML size 8               openems.cpp:101
     CSXCAD ContinuousStructure::ReadFromXML, for rectilinear grids
         (DeltaUnit, X/Y/ZLines as sorted unique number lists), the
         background material and the properties Material, LorentzMaterial
-        (one order), Metal, LumpedElement (Direction, R, C, L, Caps, LEtype),
+        (one order, electric and magnetic families), Metal, LumpedElement (Direction, R, C, L, Caps, LEtype),
         Excitation (Type, Excite, Delay) and ProbeBox (Type, Weight,
         NormDir), each with <Box Priority><P1/><P2/></Box> primitives.
 
@@ -74,9 +75,12 @@ def xml_spec(path_or_text: str) -> dict:
         if fdtd.get(k) is not None:
             raise ValueError(f"<FDTD {k}>")
     exc = fdtd.find("Excitation")
-    if exc is None or int(_num(exc, "Type", -1)) != 0:
-        raise ValueError("only the Gaussian pulse excitation (Type 0)")
-    f0, fc = _num(exc, "f0", 0.0), _num(exc, "fc", 0.0)
+    etype = -1 if exc is None else int(_num(exc, "Type", -1))
+    if etype not in (0, 1, 2, 3):
+        raise ValueError("only the Gaussian (0), sinusoid (1), Dirac (2) and step (3) excitations")
+    f0 = _num(exc, "f0", 0.0) if etype <= 1 else 0.0
+    fc = _num(exc, "fc", 0.0) if etype == 0 else 0.0
+    f_max = _num(fdtd, "f_max", 0.0) if etype >= 2 else 0.0
     bcn = fdtd.find("BoundaryCond")
     if bcn is None:
         raise ValueError("<BoundaryCond> missing")
@@ -146,11 +150,12 @@ def xml_spec(path_or_text: str) -> dict:
             if p.tag == "LorentzMaterial":
                 if int(_num(p, "Order", 1)) > 1:
                     raise ValueError("dispersion order > 1")
-                if _iso(prop, "MuePlasmaFrequency", 0.0) != 0:
-                    raise ValueError("magnetic dispersion")
                 mat.update(disp_order=1, eps_plasma_f=[_iso(prop, "EpsilonPlasmaFrequency", 0.0)],
                            eps_relax_t=[_iso(prop, "EpsilonRelaxTime", 0.0)],
-                           eps_pole_f=[_iso(prop, "EpsilonLorPoleFrequency", 0.0)])
+                           eps_pole_f=[_iso(prop, "EpsilonLorPoleFrequency", 0.0)],
+                           mue_plasma_f=[_iso(prop, "MuePlasmaFrequency", 0.0)],
+                           mue_relax_t=[_iso(prop, "MueRelaxTime", 0.0)],
+                           mue_pole_f=[_iso(prop, "MueLorPoleFrequency", 0.0)])
             for pr, a, b in boxes:
                 prims.append(dict(kind="material", priority=pr, start=a, stop=b, **mat))
         elif p.tag == "Metal":
@@ -180,4 +185,4 @@ def xml_spec(path_or_text: str) -> dict:
         else:
             raise ValueError(f"property <{p.tag}>")
     return dict(lines=lines, unit=unit, background=background, bc=bc, pml_size=pml, mur_vph=vph, f0=f0, fc=fc,
-                nr_ts=nr_ts, oversampling=oversampling, prims=prims)
+                nr_ts=nr_ts, oversampling=oversampling, prims=prims, excite_type=etype, f_max=f_max)

@@ -238,3 +238,16 @@ def oracle_inputs(prod_op):
         ref = oracle_operator(prod_op, threads=os.cpu_count() or 1)
         prod_op._oracle_op = ref
     return ref.desc, ref.probes
+
+
+def with_signal(scene, excite_type: int, f: float = 0.0):
+    """The scene with its Gaussian pulse replaced by another signal of the
+    reference: 1 sinusoid of frequency f, 2 Dirac pulse, 3 step (f = f_max)."""
+    import copy
+    from wipems_gb300 import Scene, SceneSpec
+    src = copy.deepcopy(scene.spec)
+    sp = SceneSpec(*src["lines"], src["unit"])
+    src.update(excite_type=int(excite_type), f0=float(f) if excite_type == 1 else 0.0, fc=0.0,
+               f_max=float(f) if excite_type >= 2 else 0.0)
+    sp.spec = src
+    return Scene.from_spec(sp)

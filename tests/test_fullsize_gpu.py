@@ -56,6 +56,20 @@ def test_d192_full_3000_timesteps():
     compare(op, eng, ref, bitwise=False)
 
 
+def test_drude_metamaterial_plane_wave_full_6000_timesteps_bitwise():
+    """The double-negative Drude slab plane wave (E and H ADE both on,
+    PMC / PEC / Mur walls, a whole-plane soft E excitation), 6000
+    timesteps: the pulse crosses the slab and leaves through the Mur face;
+    bit-identical, on both kernel families."""
+    op = Operator(scenes.drude_metamaterial(nr_ts=6000))
+    ref = _oracle(op, 6000)
+    for kernel in ("tma", "direct"):
+        eng = Engine(op, kernel=kernel)
+        eng.iterate(6000)
+        compare(op, eng, ref)
+        eng.close()
+
+
 def test_b96_jobs_full_1500_timesteps_in_one_batch():
     """Four B96 jobs (two PEC, two UPML-8, uneven non-cubic grids) advanced
     together by the persistent batched kernels for the full 1500 timesteps:
@@ -119,7 +133,7 @@ def test_serve_jobs_full_length_match_oracle():
     srv.close()
 
 
-@pytest.mark.parametrize("name", ["port_box.xml", "lorentz_mur.xml"])
+@pytest.mark.parametrize("name", ["port_box.xml", "lorentz_mur.xml", "drude_mtm.xml"])
 def test_xml_scene_full_length_matches_oracle(name):
     """openEMS XML input: the engine library's reader + operator on the GPU
     against the oracle's own XML reader + operator + stepping, over the

@@ -71,6 +71,7 @@ class BridgedOperator:
         self._h = self._L.bridge_build(C.addressof(op.desc))
         self.desc = _abi.FdtdOpDesc.from_address(self._L.bridge_desc(self._h))
         self.num_lines, self.probes, self.probe_interval, self.scene = op.num_lines, op.probes, op.probe_interval, op.scene
+        self.dT = op.dT
 
     def __del__(self):
         if getattr(self, "_h", None):
@@ -78,7 +79,7 @@ class BridgedOperator:
             self._h = None
 
 
-CASES = ["upml", "graded", "drude", "lorentz", "mixed", "mur", "rlc", "rlc_mur"]
+CASES = ["upml", "graded", "drude", "lorentz", "mixed", "mur", "rlc", "rlc_mur", "magnetic"]
 
 
 @pytest.mark.parametrize("kind", CASES)
@@ -92,7 +93,7 @@ def test_bridge_rebuilds_the_description_bitwise(kind):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kind", ["upml", "mixed", "rlc_mur"])
+@pytest.mark.parametrize("kind", ["upml", "mixed", "rlc_mur", "magnetic"])
 def test_engine_from_the_bridged_description_matches_oracle(kind):
     from test_parity_gpu import compare
     op = Operator(scenes.mini(kind, nr_ts=300))

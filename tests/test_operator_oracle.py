@@ -7,14 +7,15 @@ Calc_LumpedElements, the excitation, Mur, UPML, Lorentz/Drude and lumped RLC
 BuildExtension in openEMS's extension order, probe snapping).  Bar: bitwise
 on every array, on the mini scenes of every feature, P64, the cavity, L256,
 D192, B96 jobs (PEC and UPML) and serving jobs of each kind (dielectric,
-Drude, Lorentz)."""
+Drude, Lorentz), and the magnetic (mue) family of the Lorentz material on
+its own and beside the electric one."""
 import numpy as np
 import pytest
 
 import oracle
 from wipems_gb300 import Operator, scenes
 
-from helpers import assert_same_operator
+from helpers import assert_same_operator, with_signal
 
 pytestmark = pytest.mark.usefixtures("libs")
 
@@ -23,14 +24,16 @@ def both(scene):
     return Operator(scene), oracle.Operator(scene.spec)
 
 
-@pytest.mark.parametrize("kind", ["pec", "upml", "graded", "drude", "lorentz", "mixed", "mur", "rlc", "rlc_mur"])
+@pytest.mark.parametrize("kind", ["pec", "upml", "graded", "drude", "lorentz", "mixed", "mur", "rlc", "rlc_mur",
+                                  "magnetic", "magnetic_graded"])
 def test_mini_scene_operators_identical(kind):
     assert_same_operator(*both(scenes.mini(kind)))
 
 
-@pytest.mark.parametrize("name", ["p64", "cavity", "rlc_series", "rlc_parallel"])
+@pytest.mark.parametrize("name", ["p64", "cavity", "rlc_series", "rlc_parallel", "drude_metamaterial"])
 def test_small_scene_operators_identical(name):
     s = {"p64": lambda: scenes.p64(),
+         "drude_metamaterial": lambda: scenes.drude_metamaterial(),
          "cavity": lambda: scenes.cavity(),
          "rlc_series": lambda: scenes.rlc_probe(True, R=50.0, L=1e-9, Cap=1e-12),
          "rlc_parallel": lambda: scenes.rlc_probe(False, R=50.0, L=1e-9, Cap=1e-12)}[name]()
@@ -62,6 +65,59 @@ def test_headline_operators_identical(name):
         assert O.desc.num_ade_orders == 1 and O.desc.ade[0].count > 100_000
     else:
         assert O.desc.num_upml == 6
+
+
+def test_magnetic_dispersion_builds_the_current_side_terms():
+    """The mue family drives the H-side ADE: the double-negative Drude
+    plane-wave scene turns both halves on (Drude: no Lorentz pole terms), the
+    magnetic Lorentz pole of the mini scene turns on the H-side pole term,
+    and the reference's coefficients come out: i_int = (2 C_D - dT G_D) /
+    (2 C_D + dT G_D) with C_D = 1 / (w_p^2 EC_L) and G_D = C_D / tau
+    (operator_ext_lorentzmaterial.cpp:248-276, 300-330), so i_int depends
+    only on w_p, tau and dT."""
+    s = scenes.drude_metamaterial()
+    O = oracle.Operator(s.spec)
+    a = O.desc.ade[0]
+    assert a.volt_on and a.curr_on and not a.volt_lor_on and not a.curr_lor_on
+    c = a.count
+    i_int = np.ctypeslib.as_array(a.i_int, shape=(3 * c,))
+    i_ext = np.ctypeslib.as_array(a.i_ext, shape=(3 * c,))
+    on = i_ext != 0
+    assert on.sum() > c  # the two H components across the channel, in the slab
+    dT, tau = O.dT, s.meta["relax_t"]
+    # C_D cancels: (2 - dT/tau) / (2 + dT/tau), rounded once to float
+    want = np.float32((2.0 - dT / tau) / (2.0 + dT / tau))
+    assert np.max(np.abs(i_int[on] - want)) <= 2 * np.spacing(want)
+    m = oracle.Operator(scenes.mini("magnetic").spec)
+    assert m.desc.ade[0].curr_lor_on and m.desc.ade[0].volt_lor_on
+
+
+@pytest.mark.parametrize("kind", ["upml", "rlc_mur"])
+@pytest.mark.parametrize("etype,f", [(1, 6e9), (1, 13.7e9), (2, 2e10), (3, 0.0)])
+def test_excitation_signal_operators_identical(kind, etype, f):
+    """Sinusoid, Dirac pulse and step (excitation.cpp:179-218, 273-295) in
+    place of the Gaussian: identical operators, including the sinusoid's
+    shortened timestep (operator.cpp:1001-1007), its two-period signal and
+    the engine's period (engine_ext_excitation.cpp:45-46), the RLC elements
+    built with fMax = f0 and the Mur faces' start timestep."""
+    s = with_signal(scenes.mini(kind, nr_ts=400), etype, f)
+    P, O = both(s)
+    assert_same_operator(P, O)
+    d = O.desc
+    sig = np.ctypeslib.as_array(d.signal_volt, shape=(d.signal_length,))
+    gauss = oracle.Operator(scenes.mini(kind, nr_ts=400).spec)
+    if etype == 1:
+        T = 1 / f
+        assert O.dT <= gauss.dT and O.dT > gauss.dT * 0.9
+        ts = round(T / O.dT)
+        assert abs(T / O.dT - ts) < 1e-9 and d.signal_period_ts in (ts - 1, ts)
+        assert d.signal_length == round(2 * T / O.dT) and sig[0] == 0
+        assert np.max(np.abs(sig)) > 0.99
+        assert O.nyquist == int(np.floor(T / 2 / O.dT))
+    else:
+        assert O.dT == gauss.dT and d.signal_period_ts == 0
+        assert sig.tolist() == ([0.0, 1.0] if etype == 2 else [1.0, 1.0])
+        assert O.nyquist == 1 and O.probe_interval == 1
 
 
 def test_comparison_sees_a_planted_mistake():

@@ -14,7 +14,7 @@ import pytest
 import oracle
 from wipems_gb300 import CompressedOperator, Engine, Operator, scenes
 
-from helpers import cavity_check, oracle_inputs, rel_l2, rel_max
+from helpers import cavity_check, oracle_inputs, rel_l2, rel_max, with_signal
 
 pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("libs")]
 
@@ -44,7 +44,8 @@ def compare(op, eng, ref, bitwise=True):
 
 
 @pytest.mark.parametrize("kernel", ["tma", "direct"])
-@pytest.mark.parametrize("kind", ["pec", "upml", "graded", "drude", "lorentz", "mixed", "mur", "rlc", "rlc_mur"])
+@pytest.mark.parametrize("kind", ["pec", "upml", "graded", "drude", "lorentz", "mixed", "mur", "rlc", "rlc_mur",
+                                  "magnetic", "magnetic_graded"])
 def test_mini_scenes_match_oracle(kind, kernel):
     """Uniform meshes: bit-identical.  Graded meshes (automatic factorized
     geometry): within the probe / field tolerance of the oracle on the
@@ -55,6 +56,18 @@ def test_mini_scenes_match_oracle(kind, kernel):
     eng = Engine(cop, kernel=kernel)
     eng.iterate(400)
     compare(op, eng, ref, bitwise=not cop.factorized)
+
+
+@pytest.mark.parametrize("kind", ["upml", "rlc_mur"])
+@pytest.mark.parametrize("etype,f", [(1, 6e9), (2, 2e10), (3, 0.0)])
+def test_excitation_signals_match_oracle(kind, etype, f):
+    """Sinusoid (periodic: the signal index wraps with the period), Dirac
+    pulse and step through the graph-chunked TMA engine: bit-identical."""
+    op = Operator(with_signal(scenes.mini(kind, nr_ts=700), etype, f))
+    ref = oracle.run(*oracle_inputs(op), 700, op.probe_interval, engine=oracle.BASIC)
+    eng = Engine(CompressedOperator(op), kernel="tma")
+    eng.iterate(700)
+    compare(op, eng, ref)
 
 
 def expanded_desc(op, cop):
@@ -100,7 +113,7 @@ def expanded_desc(op, cop):
     return d, keep
 
 
-@pytest.mark.parametrize("kind", ["graded", "mixed"])
+@pytest.mark.parametrize("kind", ["graded", "mixed", "magnetic_graded"])
 def test_factorized_kernels_bitwise_against_expanded_operator(kind):
     """The factorized kernels apply exactly the coefficients fdtd_cop_expand
     and fdtd_cop_expand_ext report: run the oracle on those and require

@@ -79,9 +79,28 @@ def test_xml_text_and_lorentz_material():
     _same_operator(Operator(sx), Operator(s))
 
 
+def test_xml_magnetic_lorentz_material():
+    """MuePlasmaFrequency / MueRelaxTime / MueLorPoleFrequency read into
+    the magnetic family of the API's Lorentz material."""
+    text = (GOLDEN / "port_box.xml").read_text()
+    text = text.replace(
+        '<Metal ID="1" Name="plate">',
+        '<LorentzMaterial ID="7" Name="dng" Order="1"><Primitives><Box Priority="15">'
+        '<P1 X="4" Y="5" Z="2"/><P2 X="7" Y="9" Z="4"/></Box></Primitives>'
+        '<Property Epsilon="2" Mue="1.5" EpsilonPlasmaFrequency="5e9" EpsilonRelaxTime="1e-9" '
+        'MuePlasmaFrequency="6e9" MueRelaxTime="2e-9" MueLorPoleFrequency="3e9"/></LorentzMaterial>\n'
+        '      <Metal ID="1" Name="plate">')
+    sx = Scene.from_xml(text)
+    s = _api_scene()
+    s.add_lorentz([4, 5, 2], [7, 9, 4], eps_r=2.0, mue_r=1.5, plasma_f=[5e9], relax_t=[1e-9], priority=15,
+                  mue_plasma_f=[6e9], mue_relax_t=[2e-9], mue_pole_f=[3e9])
+    _same_operator(Operator(sx), Operator(s))
+    assert Operator(sx).desc.ade[0].curr_lor_on
+
+
 @pytest.mark.parametrize("edit,needle", [
     (('<Box Priority="20">', '<Cylinder Priority="20" Radius="1">'), "Cylinder"),
-    (('<Excitation Type="0" f0="1e+10"', '<Excitation Type="1" f0="1e+10"'), "excitation Type 1"),
+    (('<Excitation Type="0" f0="1e+10"', '<Excitation Type="10" f0="1e+10"'), "excitation Type 10"),
     (('Epsilon="3.66"', 'Epsilon="3.66,3.66,4"'), "anisotropic"),
     (('<Weight Epsilon="1"', '<Weight Epsilon="2*x"'), "weighting"),
     (('<Metal ID="1" Name="plate">', '<ConductingSheet ID="1" Name="plate">'), "ConductingSheet"),
@@ -164,7 +183,28 @@ def test_xml_field_probes():
     assert types[-2:] == [2, 3] and op.probes[-1].weight == 2.0
 
 
-@pytest.mark.parametrize("name", ["port_box.xml", "lorentz_mur.xml"])
+@pytest.mark.parametrize("etype", [1, 2, 3])
+def test_xml_excitation_signals(etype):
+    """<Excitation Type="1" f0> (sinusoid), Type 2 / 3 (Dirac / step, with
+    <FDTD f_max>): the engine library's reader equals the API scene and the
+    oracle's reader + operator."""
+    import oracle
+    from oracle.xml_spec import xml_spec
+    from helpers import assert_same_operator
+    text = (GOLDEN / "port_box.xml").read_text().replace(
+        '<Excitation Type="0" f0="1e+10" fc="5e+09"/>', f'<Excitation Type="{etype}" f0="7e+09" fc="5e+09"/>')
+    sx = Scene.from_xml(text)
+    assert sx.xml_info["excite_type"] == etype
+    s = _api_scene()
+    if etype == 1:
+        s.set_sinus_excite(7e9, 600)
+    else:
+        (s.set_dirac_excite if etype == 2 else s.set_step_excite)(1.5e10, 600)
+    _same_operator(Operator(sx), Operator(s))
+    assert_same_operator(Operator(sx), oracle.Operator(xml_spec(text)))
+
+
+@pytest.mark.parametrize("name", ["port_box.xml", "lorentz_mur.xml", "drude_mtm.xml"])
 def test_xml_operator_matches_oracle_reader(name):
     """The engine library's XML reader + operator build against the
     oracle's own reader (oracle/xml_spec.py, Python's XML parser) + its

@@ -158,6 +158,9 @@ SIGNATURES = [
     ("fdtd_scene_set_boundary", C.c_int, [_P, C.POINTER(C.c_int), PU32]),
     ("fdtd_scene_set_mur_velocity", C.c_int, [_P, C.POINTER(C.c_double)]),
     ("fdtd_scene_set_gauss_excite", C.c_int, [_P, C.c_double, C.c_double, u32]),
+    ("fdtd_scene_set_sinus_excite", C.c_int, [_P, C.c_double, u32]),
+    ("fdtd_scene_set_dirac_excite", C.c_int, [_P, C.c_double, u32]),
+    ("fdtd_scene_set_step_excite", C.c_int, [_P, C.c_double, u32]),
     ("fdtd_scene_set_oversampling", C.c_int, [_P, u32]),
     ("fdtd_scene_add_material", C.c_int, [_P, C.c_int, PD, PD, C.c_double, C.c_double, C.c_double, C.c_double]),
     ("fdtd_scene_add_metal", C.c_int, [_P, C.c_int, PD, PD]),
@@ -167,6 +170,8 @@ SIGNATURES = [
     ("fdtd_scene_add_excitation", C.c_int, [_P, C.c_int, PD, PD, C.c_int, PD, C.c_double]),
     ("fdtd_scene_add_lorentz", C.c_int, [_P, C.c_int, PD, PD, C.c_double, C.c_double, C.c_double, C.c_double,
                                          C.c_int, PD, PD, PD]),
+    ("fdtd_scene_add_lorentz_material", C.c_int, [_P, C.c_int, PD, PD, C.c_double, C.c_double, C.c_double,
+                                                  C.c_double, C.c_int, PD, PD, PD, PD, PD, PD]),
     ("fdtd_scene_add_probe", C.c_int, [_P, C.c_int, PD, PD, C.c_double, C.c_int]),
     ("fdtd_operator_build", C.c_int, [_P, C.c_int, C.POINTER(_P)]),
     ("fdtd_operator_destroy", C.c_int, [_P]),

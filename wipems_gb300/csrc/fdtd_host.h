@@ -39,6 +39,9 @@ struct Prim {
     double eps_plasma_f[kMaxDispOrder] = {0, 0, 0, 0};
     double eps_relax_t[kMaxDispOrder] = {0, 0, 0, 0};
     double eps_lor_pole_f[kMaxDispOrder] = {0, 0, 0, 0};
+    double mue_plasma_f[kMaxDispOrder] = {0, 0, 0, 0};
+    double mue_relax_t[kMaxDispOrder] = {0, 0, 0, 0};
+    double mue_lor_pole_f[kMaxDispOrder] = {0, 0, 0, 0};
     // lumped element
     int ny = 2;
     double R = -1, C = -1, L = -1;
@@ -76,6 +79,11 @@ struct fdtd_scene_s {
     uint32_t pml_size[6] = {0, 0, 0, 0, 0, 0};
     double mur_vph[6] = {0, 0, 0, 0, 0, 0};
     double f0 = 0, fc = 0;
+    // Excitation::ExciteTypes (excitation.h:28): 0 Gaussian pulse,
+    // 1 sinusoid, 2 Dirac pulse, 3 step; f_max is the Dirac / step's
+    // <FDTD f_max> (recorded, it changes nothing on this path)
+    int excite_type = 0;
+    double f_max = 0;
     bool have_excite = false;
     uint32_t nr_ts = 0;
     uint32_t oversampling = 4;
@@ -136,6 +144,7 @@ struct fdtd_operator_s {
     wipems::ExcList volt_exc, curr_exc;
     std::vector<float> sig_volt, sig_curr;
     uint32_t signal_length = 0;
+    uint32_t signal_period_ts = 0;  // 0: not periodic
     uint32_t nyquist = 0;
     uint32_t probe_interval = 1;
     uint32_t max_excite_ts = 0;

@@ -1077,7 +1077,14 @@ static int build_operator(const fdtd_scene_s& S, int threads, fdtd_operator_s& o
         set_error("timestep is zero: no valid edge found by CalcTimestep_Var3");
         return FDTD_ERR_ARG;
     }
-    // m_TimeStepFactor = 1; Gaussian pulse has no signal period
+    // m_TimeStepFactor = 1.  A periodic signal (the sinusoid) shortens dT
+    // so that its period is a whole number of timesteps
+    // (Operator::CalcECOperator, operator.cpp:1001-1007)
+    if (S.have_excite && S.excite_type == 1) {
+        const double period = 1 / S.f0;
+        const unsigned int TS = (unsigned int)std::ceil(period / B.dT);
+        B.dT = period / TS;
+    }
 
     B.vv.assign(3 * B.NN, 0.f);
     B.vi.assign(3 * B.NN, 0.f);
@@ -1298,9 +1305,32 @@ static int build_operator(const fdtd_scene_s& S, int threads, fdtd_operator_s& o
                                 }
                             }
                         }
+                        // magnetic side: the same model on the dual edges, from
+                        // the mue parameters and EC_L (lorentzmaterial.cpp:248-276)
                         for (int n = 0; n < 3; ++n) {
                             C_D[n] = 0; G_D[n] = 0; L_L[n] = 0;
-                            // magnetic dispersion (mue plasma frequency) is not part of the box model
+                            if (!g.yee_coords(n, pos, c, true)) continue;
+                            if (B.iv[B.at(n, pos)] == 0) continue;
+                            int kind[3] = {SK_DUAL, SK_DUAL, SK_DUAL};
+                            kind[n] = SK_LINE;
+                            int w = B.pec_idx.lookup(kind, pos);
+                            if (w < 0) continue;
+                            const Prim& p = S.prims[w];
+                            if (!(p.kind == PK_MATERIAL && p.lorentz)) continue;
+                            double ecl = B.EC_L[(size_t)n * B.NN + index];
+                            double w_plasma = (o < p.disp_order ? p.mue_plasma_f[o] : 0) * 2 * kPi;
+                            if ((w_plasma > 0) && (ecl > 0)) {
+                                b_pos_on = true;
+                                A.curr_on = true;
+                                C_D[n] = 1 / (w_plasma * w_plasma * ecl);
+                            }
+                            double t_relax = (o < p.disp_order ? p.mue_relax_t[o] : 0);
+                            if ((t_relax > 0) && A.curr_on) G_D[n] = C_D[n] / t_relax;
+                            double w_lor = (o < p.disp_order ? p.mue_lor_pole_f[o] : 0) * 2 * kPi;
+                            if ((w_lor > 0) && (C_D[n] > 0)) {
+                                A.curr_lor_on = true;
+                                L_L[n] = 1 / (w_lor * w_lor * C_D[n]);
+                            }
                         }
                         if (b_pos_on) {
                             for (int n = 0; n < 3; ++n) {
@@ -1354,11 +1384,21 @@ static int build_operator(const fdtd_scene_s& S, int threads, fdtd_operator_s& o
     }
 
     // ---- extension 9: lumped RLC elements (added last, openems.cpp:1095-1096);
-    // fmax = GetCenterFreq() + GetCutOffFreq() of the Gaussian
+    // fMax = GetCenterFreq() + GetCutOffFreq() (operator_ext_lumpedRLC.cpp:116-118):
+    // f0 + fc of the Gaussian, f0 of the sinusoid.  The reference leaves
+    // m_f0 / m_fc unset for the Dirac and step signals (and m_fc for the
+    // sinusoid); they count as 0 here
     B.calc_rlc(S.f0 + S.fc, op.rlc);
 
-    // ---- excitation signal (Excitation::CalcGaussianPulsExcitation)
-    if (S.have_excite) {
+    // ---- excitation signal: Excitation::buildExcitationSignal
+    // (excitation.cpp:96-134) and CalcNyquistNum (tools/useful.cpp:30-36)
+    op.signal_period_ts = 0;
+    auto nyquist_num = [&](double fmax) -> uint32_t {
+        if (fmax == 0) return UINT32_MAX;
+        return (uint32_t)std::floor(1 / fmax / 2 / dT);
+    };
+    if (S.have_excite && S.excite_type == 0) {
+        // CalcGaussianPulsExcitation (excitation.cpp:151-177)
         double f0 = S.f0, fc = S.fc;
         uint32_t Length = (uint32_t)std::ceil(2.0 * 9.0 / (2.0 * kPi * fc) / dT);
         if (S.nr_ts > 0 && Length > S.nr_ts) Length = S.nr_ts;
@@ -1372,22 +1412,45 @@ static int build_operator(const fdtd_scene_s& S, int threads, fdtd_operator_s& o
             op.sig_curr[n] = (float)(std::cos(2.0 * kPi * f0 * (t - 9.0 / (2.0 * kPi * fc))) *
                                      std::exp(-1 * std::pow(2.0 * kPi * fc * t / 3.0 - 3, 2)));
         }
-        op.signal_length = Length;
-        // CalcNyquistNum(f0+fc, dT) (tools/useful.cpp:30-36)
-        double fmax = f0 + fc;
-        op.nyquist = (fmax == 0) ? UINT32_MAX : (uint32_t)std::floor(1 / fmax / 2 / dT);
-        // GetMaxExcitationTimestep (excitation.cpp:137-149)
+        op.nyquist = nyquist_num(f0 + fc);
+    } else if (S.have_excite && S.excite_type == 1) {
+        // CalcSinusExcitation (excitation.cpp:273-295): two periods
+        const double f0 = S.f0;
+        const uint32_t Length = (uint32_t)std::round(2.0 / f0 / dT);
+        op.sig_volt.assign(Length, 0.f);
+        op.sig_curr.assign(Length, 0.f);
+        for (uint32_t n = 1; n < Length; ++n) {
+            double t = n * dT;
+            op.sig_volt[n] = (float)std::sin(2.0 * kPi * f0 * t);
+            t += 0.5 * dT;
+            op.sig_curr[n] = (float)std::sin(2.0 * kPi * f0 * t);
+        }
+        op.nyquist = nyquist_num(f0);
+        // the engine's period p = int(GetSignalPeriod() / dT)
+        // (engine_ext_excitation.cpp:45-46)
+        op.signal_period_ts = (uint32_t)(int)((1 / f0) / dT);
+    } else if (S.have_excite) {
+        // CalcDiracPulsExcitation / CalcStepExcitation (excitation.cpp:179-218)
+        const float first = S.excite_type == 3 ? 1.f : 0.f;
+        op.sig_volt = {first, 1.f};
+        op.sig_curr = {first, 1.f};
+        op.nyquist = 1;
+    } else {
+        op.sig_volt.clear();
+        op.sig_curr.clear();
+        op.nyquist = 1;
+    }
+    op.signal_length = (uint32_t)op.sig_volt.size();
+    {
+        // GetMaxExcitationTimestep (excitation.cpp:136-149)
         float maxAmp = 0;
         uint32_t maxStep = 0;
-        for (uint32_t n = 0; n < Length; ++n)
+        for (uint32_t n = 0; n < op.signal_length; ++n)
             if (std::fabs(op.sig_volt[n]) > maxAmp) {
                 maxAmp = std::fabs(op.sig_volt[n]);
                 maxStep = n;
             }
         op.max_excite_ts = maxStep;
-    } else {
-        op.signal_length = 0;
-        op.nyquist = 1;
     }
     op.probe_interval = std::max<uint32_t>(1, op.nyquist / std::max<uint32_t>(1, S.oversampling));
 
@@ -1619,8 +1682,44 @@ int fdtd_scene_set_gauss_excite(fdtd_scene_t s, double f0, double fc, uint32_t n
     s->f0 = f0;
     s->fc = fc;
     s->nr_ts = nr_ts;
+    s->excite_type = 0;
     s->have_excite = true;
     return FDTD_OK;
+}
+
+int fdtd_scene_set_sinus_excite(fdtd_scene_t s, double f0, uint32_t nr_ts) {
+    if (!s || !(f0 > 0) || nr_ts == 0) {
+        set_error("fdtd_scene_set_sinus_excite: need f0 > 0 and nr_ts > 0");
+        return FDTD_ERR_ARG;
+    }
+    s->f0 = f0;
+    s->fc = 0;
+    s->nr_ts = nr_ts;
+    s->excite_type = 1;
+    s->have_excite = true;
+    return FDTD_OK;
+}
+
+static int set_unit_excite(fdtd_scene_t s, int type, double f_max, uint32_t nr_ts, const char* name) {
+    if (!s || f_max < 0) {
+        set_error(std::string(name) + ": need f_max >= 0");
+        return FDTD_ERR_ARG;
+    }
+    s->f0 = 0;
+    s->fc = 0;
+    s->f_max = f_max;
+    s->nr_ts = nr_ts;
+    s->excite_type = type;
+    s->have_excite = true;
+    return FDTD_OK;
+}
+
+int fdtd_scene_set_dirac_excite(fdtd_scene_t s, double f_max, uint32_t nr_ts) {
+    return set_unit_excite(s, 2, f_max, nr_ts, "fdtd_scene_set_dirac_excite");
+}
+
+int fdtd_scene_set_step_excite(fdtd_scene_t s, double f_max, uint32_t nr_ts) {
+    return set_unit_excite(s, 3, f_max, nr_ts, "fdtd_scene_set_step_excite");
 }
 
 int fdtd_scene_set_oversampling(fdtd_scene_t s, uint32_t os) {
@@ -1709,12 +1808,13 @@ int fdtd_scene_add_excitation(fdtd_scene_t s, int prio, const double start[3], c
     return FDTD_OK;
 }
 
-int fdtd_scene_add_lorentz(fdtd_scene_t s, int prio, const double start[3], const double stop[3], double eps_r,
-                           double kappa, double mue_r, double sigma, int order, const double* plasma_f,
-                           const double* relax_t, const double* pole_f) {
-    if (!s || !check_box(start, stop) || order < 1 || order > kMaxDispOrder || !plasma_f || !(eps_r > 0) ||
-        !(mue_r > 0)) {
-        set_error("fdtd_scene_add_lorentz: invalid arguments (order 1..4)");
+int fdtd_scene_add_lorentz_material(fdtd_scene_t s, int prio, const double start[3], const double stop[3],
+                                    double eps_r, double kappa, double mue_r, double sigma, int order,
+                                    const double* eps_plasma_f, const double* eps_relax_t,
+                                    const double* eps_lor_pole_f, const double* mue_plasma_f,
+                                    const double* mue_relax_t, const double* mue_lor_pole_f) {
+    if (!s || !check_box(start, stop) || order < 1 || order > kMaxDispOrder || !(eps_r > 0) || !(mue_r > 0)) {
+        set_error("fdtd_scene_add_lorentz_material: invalid arguments (order 1..4)");
         return FDTD_ERR_ARG;
     }
     Prim p = make_box(PK_MATERIAL, prio, start, stop);
@@ -1725,12 +1825,26 @@ int fdtd_scene_add_lorentz(fdtd_scene_t s, int prio, const double start[3], cons
     p.lorentz = true;
     p.disp_order = order;
     for (int o = 0; o < order; ++o) {
-        p.eps_plasma_f[o] = plasma_f[o];
-        p.eps_relax_t[o] = relax_t ? relax_t[o] : 0;
-        p.eps_lor_pole_f[o] = pole_f ? pole_f[o] : 0;
+        p.eps_plasma_f[o] = eps_plasma_f ? eps_plasma_f[o] : 0;
+        p.eps_relax_t[o] = eps_relax_t ? eps_relax_t[o] : 0;
+        p.eps_lor_pole_f[o] = eps_lor_pole_f ? eps_lor_pole_f[o] : 0;
+        p.mue_plasma_f[o] = mue_plasma_f ? mue_plasma_f[o] : 0;
+        p.mue_relax_t[o] = mue_relax_t ? mue_relax_t[o] : 0;
+        p.mue_lor_pole_f[o] = mue_lor_pole_f ? mue_lor_pole_f[o] : 0;
     }
     s->prims.push_back(p);
     return FDTD_OK;
+}
+
+int fdtd_scene_add_lorentz(fdtd_scene_t s, int prio, const double start[3], const double stop[3], double eps_r,
+                           double kappa, double mue_r, double sigma, int order, const double* plasma_f,
+                           const double* relax_t, const double* pole_f) {
+    if (!plasma_f) {
+        set_error("fdtd_scene_add_lorentz: invalid arguments (order 1..4)");
+        return FDTD_ERR_ARG;
+    }
+    return fdtd_scene_add_lorentz_material(s, prio, start, stop, eps_r, kappa, mue_r, sigma, order, plasma_f,
+                                           relax_t, pole_f, nullptr, nullptr, nullptr);
 }
 
 int fdtd_scene_add_probe(fdtd_scene_t s, int type, const double start[3], const double stop[3], double weight,
@@ -1872,7 +1986,7 @@ int fdtd_operator_describe(fdtd_operator_t op, fdtd_op_desc* d) {
     d->signal_length = op->signal_length;
     d->signal_volt = op->sig_volt.data();
     d->signal_curr = op->sig_curr.data();
-    d->signal_period_ts = 0;
+    d->signal_period_ts = op->signal_period_ts;
     for (int n = 0; n < 3; ++n) d->lines[n] = op->lines[n].data();
     d->unit = op->unit;
     return FDTD_OK;

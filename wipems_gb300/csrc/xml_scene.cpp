@@ -8,11 +8,13 @@
 // matlab/python front ends write that document (matlab/WriteOpenEMS.m,
 // InitFDTD.m, SetGaussExcite.m, SetBoundaryCond.m).
 //
-// Covered: <FDTD NumberOfTimesteps endCriteria OverSampling>, its Gaussian
-// <Excitation Type="0" f0 fc> and <BoundaryCond> (numeric codes or
+// Covered: <FDTD NumberOfTimesteps endCriteria OverSampling f_max>, its
+// <Excitation> of Type 0 (Gaussian, f0 fc), 1 (sinusoid, f0), 2 (Dirac) or
+// 3 (step), and <BoundaryCond> (numeric codes or
 // PEC / PMC / MUR / PML_n, MUR_PhaseVelocity[_face]); the <RectilinearGrid DeltaUnit> with its X/Y/ZLines,
 // <BackgroundMaterial>, and the properties Material, Metal, LumpedElement,
-// Excitation, ProbeBox (voltage and current) and LorentzMaterial (order 1),
+// Excitation, ProbeBox (voltage and current) and LorentzMaterial (order 1,
+// electric and magnetic families),
 // each with <Box> primitives (Priority, P1, P2).  Anything else that would
 // change the simulation (other primitives, excitation signals, anisotropic
 // or weighted materials, cylindrical coordinates) is
@@ -326,13 +328,19 @@ int fdtd_scene_load_xml(const char* text, fdtd_scene_t* out, fdtd_xml_info* info
         if (fdtd->attr(k)) L.bad(FDTD_ERR_UNSUPPORTED, std::string("<FDTD ") + k + ">");
     const XNode* exc = fdtd->child("Excitation");
     if (!exc) L.bad(FDTD_ERR_ARG, "<FDTD> has no <Excitation> (openems.cpp:892-896)");
-    double f0 = 0, fc = 0;
+    // the signal (openems.cpp:898-926): Type 0 Gaussian (f0, fc), 1 sinusoid
+    // (f0), 2 Dirac and 3 step (<FDTD f_max>); 10 (a custom function of t)
+    // is not covered
+    double f0 = 0, fc = 0, f_max = 0;
     if (exc) {
         L.num(*exc, "Type", d, -1);
         inf.excite_type = (int)d;
-        if ((int)d != 0) L.bad(FDTD_ERR_UNSUPPORTED, "excitation Type " + std::to_string((int)d) + " (only the Gaussian pulse, Type 0)");
-        L.num(*exc, "f0", f0, 0);
-        L.num(*exc, "fc", fc, 0);
+        if ((int)d < 0 || (int)d > 3)
+            L.bad(FDTD_ERR_UNSUPPORTED, "excitation Type " + std::to_string((int)d) +
+                                            " (Gaussian 0, sinusoid 1, Dirac 2 and step 3 are covered)");
+        if ((int)d <= 1) L.num(*exc, "f0", f0, 0);
+        if ((int)d == 0) L.num(*exc, "fc", fc, 0);
+        if ((int)d >= 2) L.num(*fdtd, "f_max", f_max, 0);
     }
     inf.f0 = f0;
     inf.fc = fc;
@@ -416,6 +424,12 @@ int fdtd_scene_load_xml(const char* text, fdtd_scene_t* out, fdtd_xml_info* info
     if ((rc = fdtd_scene_set_mur_velocity(sc, vph))) return fail(rc, "Mur phase velocity");
     if (inf.excite_type == 0 && (rc = fdtd_scene_set_gauss_excite(sc, f0, fc, inf.nr_ts)))
         return fail(rc, "Gaussian excitation");
+    if (inf.excite_type == 1 && (rc = fdtd_scene_set_sinus_excite(sc, f0, inf.nr_ts)))
+        return fail(rc, "sinusoidal excitation");
+    if (inf.excite_type == 2 && (rc = fdtd_scene_set_dirac_excite(sc, f_max, inf.nr_ts)))
+        return fail(rc, "Dirac excitation");
+    if (inf.excite_type == 3 && (rc = fdtd_scene_set_step_excite(sc, f_max, inf.nr_ts)))
+        return fail(rc, "step excitation");
     if (inf.oversampling && (rc = fdtd_scene_set_oversampling(sc, inf.oversampling))) return fail(rc, "OverSampling");
     // ---- properties
     const XNode* props = csx->child("Properties");
@@ -461,21 +475,23 @@ int fdtd_scene_load_xml(const char* text, fdtd_scene_t* out, fdtd_xml_info* info
             L.iso(prop, "Mue", m, 1);
             L.iso(prop, "Kappa", k, 0);
             L.iso(prop, "Sigma", s, 0);
-            double pf = 0, rt = 0, lf = 0;
+            double pf = 0, rt = 0, lf = 0, mpf = 0, mrt = 0, mlf = 0;
             if (p.name == "LorentzMaterial") {
                 L.num(p, "Order", d, 1);
                 if (d > 1) L.bad(FDTD_ERR_UNSUPPORTED, "dispersion Order " + std::to_string((int)d) + " of '" + pname + "'");
                 L.iso(prop, "EpsilonPlasmaFrequency", pf, 0);
                 L.iso(prop, "EpsilonRelaxTime", rt, 0);
                 L.iso(prop, "EpsilonLorPoleFrequency", lf, 0);
-                double mp = 0;
-                L.iso(prop, "MuePlasmaFrequency", mp, 0);
-                if (mp != 0) L.bad(FDTD_ERR_UNSUPPORTED, "magnetic dispersion of '" + pname + "'");
+                L.iso(prop, "MuePlasmaFrequency", mpf, 0);
+                L.iso(prop, "MueRelaxTime", mrt, 0);
+                L.iso(prop, "MueLorPoleFrequency", mlf, 0);
             }
             if (L.code) return fail(L.code, L.err);
             for (const Box& b : boxes) {
-                rc = p.name == "Material" ? fdtd_scene_add_material(sc, b.priority, b.a, b.b, e, k, m, s)
-                                          : fdtd_scene_add_lorentz(sc, b.priority, b.a, b.b, e, k, m, s, 1, &pf, &rt, &lf);
+                rc = p.name == "Material"
+                         ? fdtd_scene_add_material(sc, b.priority, b.a, b.b, e, k, m, s)
+                         : fdtd_scene_add_lorentz_material(sc, b.priority, b.a, b.b, e, k, m, s, 1, &pf, &rt, &lf,
+                                                           &mpf, &mrt, &mlf);
                 if (rc) return fail(rc, "property '" + pname + "'");
                 ++inf.num_boxes;
             }

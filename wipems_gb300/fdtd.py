@@ -1,7 +1,7 @@
 """Host-side mirror of openEMS's Operator / Engine interface for the CUDA engine.
 
     Scene     ContinuousStructure + the <FDTD> setup (mesh, boxes, boundary
-              conditions, Gaussian excitation, probes); SceneSpec is the
+              conditions, excitation signal, probes); SceneSpec is the
               same scene as plain data, without native code.
     Operator  Operator::CalcECOperator (FDTD/operator.cpp:973-1084) with the
               excitation, UPML and Lorentz extension builds, run in C++.
@@ -35,6 +35,22 @@ def _d3(v) -> C.Array:
     return a
 
 
+def _lorentz_families(*fams):
+    """The six per-order lists of a Lorentz material (eps plasma, relax,
+    pole; mue plasma, relax, pole), each padded with zeros to the
+    dispersion order = the longer plasma-frequency list."""
+    order = max(len(fams[0]), len(fams[3]))
+    if not 1 <= order <= 4:
+        raise ValueError("add_lorentz: 1..4 plasma frequencies per family")
+    out = []
+    for f in fams:
+        f = [float(v) for v in f]
+        if len(f) > order:
+            raise ValueError("add_lorentz: more values than dispersion orders")
+        out.append(f + [0.0] * (order - len(f)))
+    return out
+
+
 class SceneSpec:
     """A scene as plain data: the recorder of the Scene calls (mesh lines,
     background, boundaries, pulse, boxes) in call order, with no native
@@ -49,7 +65,8 @@ class SceneSpec:
         self.meta: dict = {}
         self.spec: dict | None = dict(lines=[l.copy() for l in self._lines], unit=float(unit),
                                       background=(1.0, 1.0, 0.0, 0.0), bc=[0] * 6, pml_size=[0] * 6,
-                                      mur_vph=[0.0] * 6, f0=0.0, fc=0.0, nr_ts=0, oversampling=4, prims=[])
+                                      mur_vph=[0.0] * 6, f0=0.0, fc=0.0, nr_ts=0, oversampling=4, prims=[],
+                                      excite_type=0, f_max=0.0)
 
     @property
     def lines(self):
@@ -76,7 +93,23 @@ class SceneSpec:
 
     def set_gauss_excite(self, f0: float, fc: float, nr_ts: int):
         self.nr_ts = int(nr_ts)
-        self._record(f0=float(f0), fc=float(fc), nr_ts=int(nr_ts))
+        self._record(f0=float(f0), fc=float(fc), nr_ts=int(nr_ts), excite_type=0, f_max=0.0)
+
+    def set_sinus_excite(self, f0: float, nr_ts: int):
+        """Sinusoid of frequency f0 (openEMS SetSinusExcite); the operator
+        shortens dT so that 1/f0 is a whole number of timesteps."""
+        self.nr_ts = int(nr_ts)
+        self._record(f0=float(f0), fc=0.0, nr_ts=int(nr_ts), excite_type=1, f_max=0.0)
+
+    def set_dirac_excite(self, f_max: float, nr_ts: int):
+        """Dirac pulse: 1 at timestep 1 (openEMS SetDiracExcite)."""
+        self.nr_ts = int(nr_ts)
+        self._record(f0=0.0, fc=0.0, nr_ts=int(nr_ts), excite_type=2, f_max=float(f_max))
+
+    def set_step_excite(self, f_max: float, nr_ts: int):
+        """Step: 1 from timestep 0 on (openEMS SetStepExcite)."""
+        self.nr_ts = int(nr_ts)
+        self._record(f0=0.0, fc=0.0, nr_ts=int(nr_ts), excite_type=3, f_max=float(f_max))
 
     def set_oversampling(self, os_: int):
         self._record(oversampling=int(os_))
@@ -108,12 +141,16 @@ class SceneSpec:
                    delay=float(delay))
 
     def add_lorentz(self, start, stop, eps_r=1.0, kappa=0.0, mue_r=1.0, sigma=0.0, plasma_f=(), relax_t=(),
-                    pole_f=(), priority=0):
-        order = len(plasma_f)
+                    pole_f=(), priority=0, mue_plasma_f=(), mue_relax_t=(), mue_pole_f=()):
+        """CSPropLorentzMaterial box: plasma_f / relax_t / pole_f are the
+        electric family (EpsilonPlasmaFrequency, EpsilonRelaxTime,
+        EpsilonLorPoleFrequency), mue_* the magnetic one (MuePlasmaFrequency,
+        MueRelaxTime, MueLorPoleFrequency), one value per dispersion order;
+        a pole frequency of 0 is a Drude pole."""
+        fam = _lorentz_families(plasma_f, relax_t, pole_f, mue_plasma_f, mue_relax_t, mue_pole_f)
         self._prim("material", priority, start, stop, eps=float(eps_r), kappa=float(kappa), mue=float(mue_r),
-                   sigma=float(sigma), disp_order=order, eps_plasma_f=[float(v) for v in plasma_f],
-                   eps_relax_t=[float(v) for v in (relax_t or [0.0] * order)],
-                   eps_pole_f=[float(v) for v in (pole_f or [0.0] * order)])
+                   sigma=float(sigma), disp_order=len(fam[0]), eps_plasma_f=fam[0], eps_relax_t=fam[1],
+                   eps_pole_f=fam[2], mue_plasma_f=fam[3], mue_relax_t=fam[4], mue_pole_f=fam[5])
 
     def add_probe(self, start, stop, ptype: int, weight=1.0, norm_dir=-1, name=""):
         self._prim("probe", 0, start, stop, probe_type=int(ptype), weight=float(weight), norm_dir=int(norm_dir))
@@ -171,7 +208,12 @@ class Scene(SceneSpec):
         s.set_boundary(d["bc"], d["pml_size"])
         if any(d["mur_vph"]):
             s.set_mur_velocity(d["mur_vph"])
-        if d["fc"] > 0:
+        et = d.get("excite_type", 0)
+        if et == 1:
+            s.set_sinus_excite(d["f0"], d["nr_ts"])
+        elif et in (2, 3):
+            (s.set_dirac_excite if et == 2 else s.set_step_excite)(d["f_max"], d["nr_ts"])
+        elif d["fc"] > 0:
             s.set_gauss_excite(d["f0"], d["fc"], d["nr_ts"])
         if d["oversampling"] != 4:
             s.set_oversampling(d["oversampling"])
@@ -180,7 +222,8 @@ class Scene(SceneSpec):
             a, b, pr = p["start"], p["stop"], p["priority"]
             if k == "material" and p.get("disp_order", 0) > 0:
                 s.add_lorentz(a, b, p["eps"], p["kappa"], p["mue"], p["sigma"], p["eps_plasma_f"], p["eps_relax_t"],
-                              p["eps_pole_f"], priority=pr)
+                              p["eps_pole_f"], priority=pr, mue_plasma_f=p.get("mue_plasma_f", ()),
+                              mue_relax_t=p.get("mue_relax_t", ()), mue_pole_f=p.get("mue_pole_f", ()))
             elif k == "material":
                 s.add_material(a, b, p["eps"], p["kappa"], p["mue"], p["sigma"], priority=pr)
             elif k == "metal":
@@ -260,6 +303,18 @@ class Scene(SceneSpec):
         check(lib().fdtd_scene_set_gauss_excite(self._h, f0, fc, int(nr_ts)), "set_gauss_excite")
         super().set_gauss_excite(f0, fc, nr_ts)
 
+    def set_sinus_excite(self, f0: float, nr_ts: int):
+        check(lib().fdtd_scene_set_sinus_excite(self._h, f0, int(nr_ts)), "set_sinus_excite")
+        super().set_sinus_excite(f0, nr_ts)
+
+    def set_dirac_excite(self, f_max: float, nr_ts: int):
+        check(lib().fdtd_scene_set_dirac_excite(self._h, f_max, int(nr_ts)), "set_dirac_excite")
+        super().set_dirac_excite(f_max, nr_ts)
+
+    def set_step_excite(self, f_max: float, nr_ts: int):
+        check(lib().fdtd_scene_set_step_excite(self._h, f_max, int(nr_ts)), "set_step_excite")
+        super().set_step_excite(f_max, nr_ts)
+
     def set_oversampling(self, os_: int):
         check(lib().fdtd_scene_set_oversampling(self._h, int(os_)), "set_oversampling")
         super().set_oversampling(os_)
@@ -291,14 +346,14 @@ class Scene(SceneSpec):
         super().add_excitation(start, stop, vec, exc_type, delay, priority)
 
     def add_lorentz(self, start, stop, eps_r=1.0, kappa=0.0, mue_r=1.0, sigma=0.0, plasma_f=(), relax_t=(),
-                    pole_f=(), priority=0):
-        order = len(plasma_f)
-        pf = (C.c_double * max(order, 1))(*plasma_f)
-        rt = (C.c_double * max(order, 1))(*(relax_t or [0.0] * order))
-        lp = (C.c_double * max(order, 1))(*(pole_f or [0.0] * order))
-        check(lib().fdtd_scene_add_lorentz(self._h, int(priority), _d3(start), _d3(stop), eps_r, kappa, mue_r, sigma,
-                                           order, pf, rt, lp), "add_lorentz")
-        super().add_lorentz(start, stop, eps_r, kappa, mue_r, sigma, plasma_f, relax_t, pole_f, priority)
+                    pole_f=(), priority=0, mue_plasma_f=(), mue_relax_t=(), mue_pole_f=()):
+        fam = _lorentz_families(plasma_f, relax_t, pole_f, mue_plasma_f, mue_relax_t, mue_pole_f)
+        order = len(fam[0])
+        arr = [(C.c_double * max(order, 1))(*f) for f in fam]
+        check(lib().fdtd_scene_add_lorentz_material(self._h, int(priority), _d3(start), _d3(stop), eps_r, kappa,
+                                                    mue_r, sigma, order, *arr), "add_lorentz")
+        super().add_lorentz(start, stop, eps_r, kappa, mue_r, sigma, plasma_f, relax_t, pole_f, priority,
+                            mue_plasma_f, mue_relax_t, mue_pole_f)
 
     def add_probe(self, start, stop, ptype: int, weight=1.0, norm_dir=-1, name=""):
         check(lib().fdtd_scene_add_probe(self._h, int(ptype), _d3(start), _d3(stop), float(weight), int(norm_dir)),

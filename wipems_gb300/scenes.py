@@ -12,6 +12,8 @@ shapes, sizes and value distributions of the workload it stands for.
     serve_job one job of the serving stream (edges log-uniform 32-256)
     cavity    the PEC cavity of the reference's resonance test
               (TESTSUITE/combinedtests/cavity.m:37-82)
+    drude_metamaterial  the double-negative Drude slab plane wave of the
+              reference's example (Metamaterial_PlaneWave_Drude.m)
 """
 from __future__ import annotations
 
@@ -20,7 +22,7 @@ import math
 
 import numpy as np
 
-from .fdtd import BC_MUR, BC_PEC, BC_PML, Scene, SceneSpec
+from .fdtd import BC_MUR, BC_PEC, BC_PMC, BC_PML, Scene, SceneSpec
 
 _native = True
 
@@ -325,4 +327,68 @@ def mini(kind: str, seed: int = 0, nr_ts: int = 400) -> Scene:
         stop = [lines[0][c[0] + 1], lines[1][c[1] + 1], lines[2][c[2] + 2]]
         s.add_lumped_port(start, stop, 2, 50.0, excite=1.0, priority=1000)
         return s
+    if kind in ("magnetic", "magnetic_graded"):
+        # the magnetic (mue) family of the Lorentz material, alone and with
+        # the electric one: a double-negative Drude box, a magnetic Lorentz
+        # pole, an electric Lorentz pole with a magnetic Drude term, and a
+        # magnetic-only Drude box
+        rng = np.random.default_rng(seed)
+        cells = [34, 30, 38]
+        graded = kind == "magnetic_graded"
+        lines = [graded_lines(c, rng) for c in cells] if graded else [uniform_lines(c, 0.5) for c in cells]
+        s = _scene(*lines, 1e-3)
+        s.set_boundary([BC_PML] * 6, [5] * 6)
+        s.set_gauss_excite(8e9, 8e9, nr_ts)
+        for b in range(4):
+            start, stop = _pick_box(rng, lines, [6] * 3, [c - 6 for c in cells], 3, 10)
+            fp = rng.uniform(3e9, 9e9)
+            tau = 1.0 / rng.uniform(1e8, 1e9)
+            if b == 0:
+                s.add_lorentz(start, stop, plasma_f=[fp], relax_t=[tau], mue_plasma_f=[fp], mue_relax_t=[tau],
+                              priority=10 + b)
+            elif b == 1:
+                fL = rng.uniform(4e9, 12e9)
+                s.add_lorentz(start, stop, mue_r=rng.uniform(1, 3), mue_plasma_f=[fL * math.sqrt(rng.uniform(1, 4))],
+                              mue_relax_t=[1e-9], mue_pole_f=[fL], priority=10 + b)
+            elif b == 2:
+                fL = rng.uniform(4e9, 12e9)
+                s.add_lorentz(start, stop, eps_r=rng.uniform(2, 4), plasma_f=[fL * math.sqrt(rng.uniform(1, 4))],
+                              relax_t=[1e-9], pole_f=[fL], mue_plasma_f=[fp], mue_relax_t=[tau], priority=10 + b)
+            else:
+                s.add_lorentz(start, stop, mue_plasma_f=[fp], mue_relax_t=[tau], priority=10 + b)
+        c = [n // 2 for n in cells]
+        start = [lines[0][c[0]], lines[1][c[1]], lines[2][c[2] - 2]]
+        stop = [lines[0][c[0] + 1], lines[1][c[1] + 1], lines[2][c[2] + 2]]
+        s.add_lumped_port(start, stop, 2, 50.0, excite=1.0, priority=1000)
+        h = [lines[0][c[0] - 3], lines[1][c[1] + 2], lines[2][c[2]]]
+        s.add_probe(h, h, 3, name="H")
+        return s
     raise ValueError(kind)
+
+
+def drude_metamaterial(nr_ts: int = 6000, length_mm: float = 500.0) -> Scene:
+    """A quasi-2D plane wave through a double-negative Drude slab: the
+    configuration of the reference's example
+    (matlab/examples/other/Metamaterial_PlaneWave_Drude.m:21-80): a 10 x 1.5
+    x length mm channel at 0.5 mm, PMC on x, PEC on y, Mur on z, a Gaussian
+    of f0 = 0 and fc = 10 GHz with oversampling 10, E_y excited on the third
+    z line, and a slab over the middle half of z whose eps and mue both
+    follow a Drude model of plasma frequency 5 GHz and relaxation time 5 ns.
+    Voltage probes (E_y across the channel) before, in and behind the slab."""
+    res = 0.5
+    mx = np.arange(-5.0, 5.0 + res / 2, res)
+    my = np.arange(-0.75, 0.75 + res / 2, res)
+    mz = np.arange(-length_mm / 2, length_mm / 2 + res / 2, res)
+    s = _scene(mx, my, mz, 1e-3)
+    s.set_boundary([BC_PMC, BC_PMC, BC_PEC, BC_PEC, BC_MUR, BC_MUR], [0] * 6)
+    s.set_gauss_excite(0.0, 10e9, nr_ts)
+    s.set_oversampling(10)
+    s.add_excitation([mx[0], my[0], mz[2]], [mx[-1], my[-1], mz[2]], [0, 1, 0], priority=0)
+    f0, tau = 5e9, 5e-9
+    s.add_lorentz([mx[0], my[0], -length_mm / 4], [mx[-1], my[-1], length_mm / 4], eps_r=1.0, mue_r=1.0,
+                  plasma_f=[f0], relax_t=[tau], mue_plasma_f=[f0], mue_relax_t=[tau], priority=10)
+    for name, zc in (("before", -length_mm * 0.375), ("inside", 0.0), ("behind", length_mm * 0.375)):
+        k = int(np.argmin(np.abs(mz - zc)))
+        s.add_probe([0.0, my[0], mz[k]], [0.0, my[-1], mz[k]], 0, name=name)
+    s.meta = dict(f0=f0, relax_t=tau)
+    return s
