@@ -399,6 +399,10 @@ int fdtd_cop_expand(fdtd_cop_t cop, float* vv, float* vi, float* ii, float* iv,
  * Either pointer may be NULL.  With fdtd_cop_expand this rebuilds the whole
  * operator the engine steps on (test and inspection use). */
 int fdtd_cop_expand_ext(fdtd_cop_t cop, int half, float* ade, float* upml);
+/* The Lorentz/Drude ADE terms of one dispersion order (0..3) of one half as
+ * the kernels apply them, ade = [9][Nx][Ny][Nz] as in fdtd_cop_expand_ext
+ * (order 0 is the same array). */
+int fdtd_cop_expand_ade(fdtd_cop_t cop, int half, int order, float* ade);
 
 /* ------------------------------------------------------------------ engine */
 

@@ -16,7 +16,7 @@ def _engine(op, **kw):
     return e
 
 
-@pytest.mark.parametrize("kind,kw", [("upml", {}), ("drude", {}), ("mur", {}), ("rlc_mur", {}),
+@pytest.mark.parametrize("kind,kw", [("upml", {}), ("drude", {}), ("mur", {}), ("rlc_mur", {}), ("multipole", {}),
                                      ("pec", dict(kernel="fused")),
                                      ("lorentz", dict(use_graphs=False, kernel="direct"))])
 def test_resume_is_bit_identical(kind, kw):

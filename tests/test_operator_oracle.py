@@ -25,7 +25,7 @@ def both(scene):
 
 
 @pytest.mark.parametrize("kind", ["pec", "upml", "graded", "drude", "lorentz", "mixed", "mur", "rlc", "rlc_mur",
-                                  "magnetic", "magnetic_graded"])
+                                  "magnetic", "magnetic_graded", "multipole", "multipole_graded"])
 def test_mini_scene_operators_identical(kind):
     assert_same_operator(*both(scenes.mini(kind)))
 

@@ -184,6 +184,7 @@ SIGNATURES = [
     ("fdtd_cop_get_info", C.c_int, [_P, C.POINTER(FdtdCopInfo)]),
     ("fdtd_cop_expand", C.c_int, [_P, PF, PF, PF, PF, PU32, PU32]),
     ("fdtd_cop_expand_ext", C.c_int, [_P, C.c_int, PF, PF]),
+    ("fdtd_cop_expand_ade", C.c_int, [_P, C.c_int, C.c_int, PF]),
     ("fdtd_engine_create", C.c_int, [C.POINTER(FdtdOpDesc), C.POINTER(FdtdEngineOpts), C.POINTER(_P)]),
     ("fdtd_engine_create_compressed", C.c_int, [_P, C.POINTER(FdtdEngineOpts), C.POINTER(_P)]),
     ("fdtd_engine_reset", C.c_int, [_P]),

@@ -27,7 +27,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-math-errno", "-pthread",
              "-I/usr/local/cuda/include"]
 
-CU_SOURCES = ["engine.cu", "energy_static.cu", "batch.cu"]
+CU_SOURCES = ["engine.cu", "engine_adex.cu", "energy_static.cu", "batch.cu"]
 CXX_SOURCES = ["operator.cpp", "compress.cpp", "server.cpp", "xml_scene.cpp"]
 
 

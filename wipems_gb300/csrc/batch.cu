@@ -182,6 +182,10 @@ int batch_refusal(const fdtd_engine_s* e) {
         set_error("fdtd_batch_create: frequency-domain accumulation is not provided in batches");
         return FDTD_ERR_UNSUPPORTED;
     }
+    if (e->feat & FEAT_ADEX) {
+        set_error("fdtd_batch_create: Lorentz/Drude dispersion of order > 1 is not provided in batches");
+        return FDTD_ERR_UNSUPPORTED;
+    }
     return FDTD_OK;
 }
 

@@ -31,20 +31,25 @@ fdtd_cop_s::~fdtd_cop_s() {
 namespace wipems {
 namespace {
 
+// tuples are hashed and compared over their first `bytes` bytes: the base
+// 128 bytes, or the whole tuple when the operator has dispersion orders > 1
+// (the rest is zero otherwise)
 struct TupleHash {
+    size_t bytes = kTupleBaseBytes;
     size_t operator()(const HalfTuple& t) const {
         const uint64_t* p = reinterpret_cast<const uint64_t*>(&t);
         uint64_t h = 1469598103934665603ull;
-        for (size_t i = 0; i < sizeof(HalfTuple) / 8; ++i) h ^= p[i] + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2);
+        for (size_t i = 0; i < bytes / 8; ++i) h ^= p[i] + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2);
         return (size_t)h;
     }
 };
 struct TupleEq {
-    bool operator()(const HalfTuple& a, const HalfTuple& b) const {
-        return std::memcmp(&a, &b, sizeof(HalfTuple)) == 0;
-    }
+    size_t bytes = kTupleBaseBytes;
+    bool operator()(const HalfTuple& a, const HalfTuple& b) const { return std::memcmp(&a, &b, bytes) == 0; }
 };
 using TupleMap = std::unordered_map<HalfTuple, uint32_t, TupleHash, TupleEq>;
+
+TupleMap make_map(size_t bytes) { return TupleMap(64, TupleHash{bytes}, TupleEq{bytes}); }
 
 // Operator::GetEdgeLength (main / dual) from the mesh lines, operator.cpp:136-185
 double edge_len(const double* l, uint32_t N, uint32_t pos, bool dual, double unit) {
@@ -79,7 +84,9 @@ struct Plan {
     bool geo;
     const float* gf[4][3];  // dE, iD, dH, iM per axis (float arrays in cop->geom)
     std::vector<int8_t> slab;
-    std::vector<int32_t> ade;
+    std::vector<int32_t> ade;                 // order 0: node -> position in the order's list
+    std::vector<int32_t> adex[kExtraOrders];  // orders 1..3
+    size_t key_bytes = kTupleBaseBytes;
     std::unordered_map<uint64_t, uint32_t> vexc, cexc;
 };
 
@@ -110,21 +117,24 @@ int prepare(const fdtd_op_desc* d, Plan& P) {
                     }
         }
     }
-    if (d->num_ade_orders > 1) {
-        set_error("dispersion order > 1 is not provided by the fused kernels");
+    if (d->num_ade_orders > (uint32_t)kMaxDispOrder) {
+        set_error("dispersion order > 4 is not provided");
         return FDTD_ERR_UNSUPPORTED;
     }
-    if (d->num_ade_orders == 1) {
-        const fdtd_ade_desc& A = d->ade[0];
-        P.ade.assign(P.NN, -1);
+    for (uint32_t o = 0; o < d->num_ade_orders; ++o) {
+        const fdtd_ade_desc& A = d->ade[o];
+        std::vector<int32_t>& m = o == 0 ? P.ade : P.adex[o - 1];
+        if (!A.volt_on && !A.curr_on) continue;  // the order's hooks are off (engine_ext_lorentzmaterial.cpp:83,132)
+        m.assign(P.NN, -1);
         for (uint32_t i = 0; i < A.count; ++i) {
             uint32_t x = A.pos[0][i], y = A.pos[1][i], z = A.pos[2][i];
             if (x >= Nx || y >= Ny || z >= Nz) {
                 set_error("ADE position outside the grid");
                 return FDTD_ERR_ARG;
             }
-            P.ade[((size_t)x * Ny + y) * Nz + z] = (int32_t)i;
+            m[((size_t)x * Ny + y) * Nz + z] = (int32_t)i;
         }
+        if (o > 0) P.key_bytes = sizeof(HalfTuple);
     }
     for (int half = 0; half < 2; ++half) {
         const uint32_t cnt = half ? d->curr_count : d->volt_count;
@@ -153,7 +163,7 @@ int prepare(const fdtd_op_desc* d, Plan& P) {
 // Builds the E (half = 0) or H (half = 1) tuple of a node.
 void make_tuple(const Plan& P, int half, uint32_t x, uint32_t y, uint32_t z, size_t gi, HalfTuple& t) {
     const fdtd_op_desc* d = P.d;
-    std::memset(&t, 0, sizeof(t));
+    std::memset(&t, 0, P.key_bytes);
     const float* c1 = half ? d->ii : d->vv;
     const float* c2 = half ? d->iv : d->vi;
     const uint32_t pos[3] = {x, y, z};
@@ -186,24 +196,31 @@ void make_tuple(const Plan& P, int half, uint32_t x, uint32_t y, uint32_t z, siz
         }
         t.flags |= TF_UPML;
     }
-    if (!P.ade.empty() && P.ade[gi] >= 0) {
-        const fdtd_ade_desc& A = d->ade[0];
-        const uint32_t i = (uint32_t)P.ade[gi];
+    // ADE terms of each order whose list holds the node and whose hooks run
+    // for this half (m_volt_ADE_On / m_curr_ADE_On of the order)
+    for (uint32_t o = 0; o < d->num_ade_orders; ++o) {
+        const std::vector<int32_t>& m = o == 0 ? P.ade : P.adex[o - 1];
+        if (m.empty() || m[gi] < 0) continue;
+        const fdtd_ade_desc& A = d->ade[o];
+        const uint32_t i = (uint32_t)m[gi];
         const bool on = half ? A.curr_on : A.volt_on;
-        if (on) {
-            const float* ai = half ? A.i_int : A.v_int;
-            const float* ae = half ? A.i_ext : A.v_ext;
-            const float* al = half ? A.i_lor : A.v_lor;
-            const bool lor_on = half ? A.curr_lor_on : A.volt_lor_on;
-            bool lor = false;
-            for (int n = 0; n < 3; ++n) {
-                t.a[n] = ai[n * A.count + i];
-                t.a[3 + n] = ae[n * A.count + i];
-                t.a[6 + n] = (lor_on && al) ? al[n * A.count + i] : 0.f;
-                if (t.a[6 + n] != 0.f) lor = true;
-            }
-            t.flags |= TF_ADE | (lor ? TF_LOR : 0u);
+        if (!on) continue;
+        const float* ai = half ? A.i_int : A.v_int;
+        const float* ae = half ? A.i_ext : A.v_ext;
+        const float* al = half ? A.i_lor : A.v_lor;
+        const bool lor_on = half ? A.curr_lor_on : A.volt_lor_on;
+        float* dst = o == 0 ? t.a : t.ax[o - 1];
+        bool lor = false;
+        for (int n = 0; n < 3; ++n) {
+            dst[n] = ai[n * A.count + i];
+            dst[3 + n] = ae[n * A.count + i];
+            dst[6 + n] = (lor_on && al) ? al[n * A.count + i] : 0.f;
+            if (dst[6 + n] != 0.f) lor = true;
         }
+        if (o == 0)
+            t.flags |= TF_ADE | (lor ? TF_LOR : 0u);
+        else
+            t.flags |= (TF_ADEX << (o - 1)) | (lor ? (TF_LORX << (o - 1)) : 0u);
     }
     const auto& m = half ? P.cexc : P.vexc;
     if (!m.empty())
@@ -243,13 +260,17 @@ void for_snap_slots(HalfTuple& t, F&& f) {
     for (int n = 0; n < 3; ++n) f(0, t.c[3 + n]);
     if (t.flags & TF_ADE)
         for (int k = 0; k < 9; ++k) f(1 + k / 3, t.a[k]);
+    for (int o = 0; o < kExtraOrders; ++o)
+        if (t.flags & (TF_ADEX << o))
+            for (int k = 0; k < 9; ++k) f(1 + k / 3, t.ax[o][k]);
     if (t.flags & TF_UPML)
         for (int k = 0; k < 9; ++k) f(4 + k / 3, t.u[k]);
 }
 
 // Snaps the tuples (weighted by the nodes using them), merges the tuples
 // that became equal; returns old tuple id -> new tuple id.
-std::vector<uint32_t> snap_tuples(std::vector<HalfTuple>& tuples, const std::vector<uint64_t>& uses) {
+std::vector<uint32_t> snap_tuples(std::vector<HalfTuple>& tuples, const std::vector<uint64_t>& uses,
+                                  size_t key_bytes) {
     std::unordered_map<uint32_t, uint64_t> hist[kSnapKinds];
     for (size_t k = 0; k < tuples.size(); ++k) {
         HalfTuple t = tuples[k];
@@ -291,7 +312,7 @@ std::vector<uint32_t> snap_tuples(std::vector<HalfTuple>& tuples, const std::vec
         }
         for (size_t i = 0; i < vals.size(); ++i) to[kind][vals[i].bits] = vals[(size_t)rep[i]].bits;
     }
-    TupleMap merged;
+    TupleMap merged = make_map(key_bytes);
     std::vector<HalfTuple> out;
     std::vector<uint32_t> newid(tuples.size());
     for (size_t k = 0; k < tuples.size(); ++k) {
@@ -326,9 +347,18 @@ void pack(const std::vector<HalfTuple>& tuples, HalfTables& T) {
         T.any_ade |= (t.flags & TF_ADE) != 0;
         T.any_lor |= (t.flags & TF_LOR) != 0;
         T.any_exc |= (t.flags & TF_EXC) != 0;
+        for (int o = 0; o < kExtraOrders; ++o)
+            if (t.flags & (TF_ADEX << o)) T.adex_orders = std::max(T.adex_orders, o + 1);
+        T.any_lorx |= (t.flags & (7u * TF_LORX)) != 0;
     }
     if (T.any_upml) T.upml.assign(n * TAB_UPML * 4, 0.f);
     if (T.any_ade) T.ade.assign(n * TAB_ADE * 4, 0.f);
+    if (T.adex_orders) {
+        T.adex.assign((size_t)T.adex_orders * n * TAB_ADE * 4, 0.f);
+        for (int o = 0; o < T.adex_orders; ++o)
+            for (size_t k = 0; k < n; ++k)
+                std::memcpy(&T.adex[((size_t)o * n + k) * TAB_ADE * 4], tuples[k].ax[o], sizeof(tuples[k].ax[o]));
+    }
     for (size_t k = 0; k < n; ++k) {
         const HalfTuple& t = tuples[k];
         float* m = &T.main[k * TAB_MAIN * 4];
@@ -431,7 +461,7 @@ int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
     std::vector<uint32_t> cnt_u(Nx, 0), cnt_a(Nx, 0);
     auto worker = [&](uint32_t x) {
         for (int h = 0; h < 2; ++h) {
-            TupleMap local;
+            TupleMap local = make_map(P.key_bytes);
             std::vector<HalfTuple>& tv = pt[h][x];
             std::vector<uint32_t>& lv = pl[h][x];
             lv.resize((size_t)Ny * Nz);
@@ -443,10 +473,12 @@ int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
                     make_tuple(P, h, x, y, z, gi, t);
                     if (h == 0) {
                         if (t.flags & TF_UPML) cnt_u[x]++;
-                        if (!P.ade.empty() && P.ade[gi] >= 0) cnt_a[x]++;
+                        bool a = !P.ade.empty() && P.ade[gi] >= 0;
+                        for (int o = 0; o < kExtraOrders; ++o) a = a || (!P.adex[o].empty() && P.adex[o][gi] >= 0);
+                        if (a) cnt_a[x]++;
                     }
                     uint32_t id;
-                    if (last_id != UINT32_MAX && std::memcmp(&t, &last, sizeof(t)) == 0) {
+                    if (last_id != UINT32_MAX && std::memcmp(&t, &last, P.key_bytes) == 0) {
                         id = last_id;
                     } else {
                         auto it = local.find(t);
@@ -487,7 +519,7 @@ int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
     node_e.resize(P.NN);
     std::vector<HalfTuple> all[2];
     for (int h = 0; h < 2; ++h) {
-        TupleMap global;
+        TupleMap global = make_map(P.key_bytes);
         std::vector<HalfTuple>& tuples = all[h];
         std::vector<std::vector<uint32_t>> remap(Nx);
         for (uint32_t x = 0; x < Nx; ++x) {
@@ -509,7 +541,7 @@ int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
             std::vector<uint64_t> uses(tuples.size(), 0);
             for (uint32_t x = 0; x < Nx; ++x)
                 for (uint32_t lid : pl[h][x]) uses[remap[x][lid]]++;
-            const std::vector<uint32_t> newid = snap_tuples(tuples, uses);
+            const std::vector<uint32_t> newid = snap_tuples(tuples, uses, P.key_bytes);
             for (uint32_t x = 0; x < Nx; ++x)
                 for (uint32_t& id : remap[x]) id = newid[id];
         }
@@ -548,7 +580,7 @@ int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
             const HalfTuple& t = all[0][k];
             bool z = true;
             for (int n = 0; n < 6; ++n) z = z && t.c[n] == 0.f;
-            if (t.flags & (TF_ADE | TF_EXC)) z = false;
+            if (t.flags & (TF_ADE | TF_ADEX_ALL | TF_EXC)) z = false;
             if (t.flags & TF_UPML)
                 for (int n = 0; n < 6; ++n) z = z && t.u[n] == 0.f;
             inert[k] = z;
@@ -735,7 +767,7 @@ int fdtd_cop_get_info(fdtd_cop_t c, fdtd_cop_info* info) {
     info->geometry_factored = c->geo ? 1 : 0;
     size_t tab = 0;
     for (const HalfTables* T : {&c->E, &c->H})
-        tab += T->idx_bytes + (T->main.size() + T->upml.size() + T->ade.size() + T->exc.size()) * sizeof(float);
+        tab += T->idx_bytes + (T->main.size() + T->upml.size() + T->ade.size() + T->exc.size() + T->adex.size()) * sizeof(float);
     info->host_bytes = tab + c->geom.size() * sizeof(float) + (c->sigV.size() + c->sigC.size()) * sizeof(float);
     info->pinned = (c->E.pinned && c->H.pinned) ? 1 : 0;
     return FDTD_OK;
@@ -779,6 +811,27 @@ int fdtd_cop_expand(fdtd_cop_t c, float* vv, float* vi, float* ii, float* iv, ui
                     uint32_t* f = h ? flags_h : flags_e;
                     if (f) std::memcpy(&f[gi], &m[6], 4);
                 }
+            }
+    return FDTD_OK;
+}
+
+int fdtd_cop_expand_ade(fdtd_cop_t c, int half, int order, float* ade) {
+    if (!c || half < 0 || half > 1 || order < 0 || order >= kMaxDispOrder || !ade) return FDTD_ERR_ARG;
+    const HalfTables& T = half ? c->H : c->E;
+    const uint32_t Nx = c->N[0], Ny = c->N[1], Nz = c->N[2];
+    const size_t NN = (size_t)Nx * Ny * Nz;
+    const uint32_t bit = order == 0 ? TF_ADE : (TF_ADEX << (order - 1));
+    const float* tab = order == 0 ? T.ade.data() : T.adex.data() + (size_t)(order - 1) * T.num_tuples * TAB_ADE * 4;
+    for (uint32_t x = 0; x < Nx; ++x)
+        for (uint32_t y = 0; y < Ny; ++y)
+            for (uint32_t z = 0; z < Nz; ++z) {
+                const size_t pi = ((size_t)x * Ny + y) * c->Nzp + z;
+                const size_t gi = ((size_t)x * Ny + y) * Nz + z;
+                const uint32_t t = T.idx16 ? reinterpret_cast<const uint16_t*>(T.idx)[pi]
+                                           : reinterpret_cast<const uint32_t*>(T.idx)[pi];
+                uint32_t flags;
+                std::memcpy(&flags, &T.main[(size_t)t * TAB_MAIN * 4 + 6], 4);
+                for (int k = 0; k < 9; ++k) ade[k * NN + gi] = (flags & bit) ? tab[(size_t)t * TAB_ADE * 4 + k] : 0.f;
             }
     return FDTD_OK;
 }

@@ -10,6 +10,10 @@
 //      v_lor)[3], voltage excitation amplitude[3] and delay[3]
 //   H: the same with ii/iv, the UPML current terms, the current ADE and
 //      current excitation.
+// Lorentz/Drude dispersion of order > 1 (several poles per material): the
+// ADE terms of orders 1..3 sit in a second table (`adex`, same tuple index,
+// one TAB_ADE block per extra order) with their own flag bits, and the
+// kernels keep their states in [order-1][3][comp] arrays.
 //
 // Graded meshes: vi and iv carry the edge's geometric factor delta/A, which
 // makes almost every node's tuple unique.  When the mesh is not uniform the
@@ -24,6 +28,7 @@
 // so that tuples differing only by such variants share one entry.
 #pragma once
 
+#include <cstddef>
 #include <cstdint>
 #include <vector>
 
@@ -37,17 +42,30 @@ constexpr uint32_t TF_UPML = 1u;
 constexpr uint32_t TF_ADE = 2u;
 constexpr uint32_t TF_LOR = 4u;
 constexpr uint32_t TF_EXC = 8u;
+// dispersion orders 1..3: ADE terms of order o at bit TF_ADEX << (o-1),
+// its Lorentz pole term at bit TF_LORX << (o-1)
+constexpr uint32_t TF_ADEX = 16u;
+constexpr uint32_t TF_LORX = 128u;
+constexpr uint32_t TF_ADEX_ALL = 7u * TF_ADEX;
+constexpr int kExtraOrders = kMaxDispOrder - 1;
 
 struct HalfTuple {
     float c[6];        // vv|ii [3], vi|iv [3] (or VI|IV in factorized mode)
     uint32_t flags;
     float u[9];        // UPML: vvp|iip [3], vvfo|iifo [3], vvfn|iifn [3]
-    float a[9];        // ADE: int [3], ext [3], lor [3]
+    float a[9];        // ADE of order 0: int [3], ext [3], lor [3]
     float x[3];        // excitation amplitude
     int32_t xd[3];     // excitation delay (-1 = none)
     uint32_t pad;
+    // ADE of orders 1..3 (zero unless the operator has them; tuples are
+    // compared and hashed over the first kTupleBaseBytes bytes only when no
+    // node has them)
+    float ax[kExtraOrders][9];
+    uint32_t pad2[5];
 };
-static_assert(sizeof(HalfTuple) == 128, "half tuple is 32 words");
+constexpr size_t kTupleBaseBytes = 128;
+static_assert(offsetof(HalfTuple, ax) == kTupleBaseBytes, "the base tuple is 32 words");
+static_assert(sizeof(HalfTuple) == 256, "the tuple with extra orders is 64 words");
 
 // device table layout of one half (float4 units per tuple)
 constexpr int TAB_MAIN = 2;  // {c0,c1,c2,c3},{c4,c5,flags,-}
@@ -59,7 +77,10 @@ struct HalfTables {
     uint32_t num_tuples = 0;
     bool idx16 = true;
     bool any_upml = false, any_ade = false, any_lor = false, any_exc = false;
+    int adex_orders = 0;                      // extra dispersion orders present (0..3)
+    bool any_lorx = false;
     std::vector<float> main, upml, ade, exc;  // float4-packed, see TAB_*
+    std::vector<float> adex;                  // [order-1][tuple][TAB_ADE] float4-packed
     uint8_t* idx = nullptr;                   // [Nx][Ny][Nzp], pinned when possible
     bool pinned = false;
     size_t idx_bytes = 0;

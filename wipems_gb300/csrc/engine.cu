@@ -20,58 +20,22 @@
 
 
 #include "engine_state.h"
+#include "launch.cuh"
 
 namespace wipems {
 namespace {
 
 // ------------------------------------------------------------ kernel launch
-template <typename IdxT, int FEAT, bool GEO, int TY>
-void launch_volt_tma(fdtd_engine_s* e, int ts_off) {
-    constexpr bool UP = (FEAT & FEAT_UPML) != 0;
-    const size_t sm = StageLayout<IdxT, UP, (FEAT & FEAT_ADE) != 0, TY>::smem(e->stages);
-    dim3 grid((e->ti.ne[2] + 31) / 32, (e->ti.ne[1] + TY - 1) / TY, (e->ti.ne[0] + e->XC - 1) / e->XC);
-    k_volt_tma<IdxT, FEAT, GEO, TY><<<grid, dim3(32, TY), sm, e->stream>>>(e->g, e->maps, e->ti, ts_off, e->XC,
-                                                                           e->stages);
-}
-
-template <typename IdxT, int FEAT, bool GEO, bool EN, int TY>
-void launch_curr_tma(fdtd_engine_s* e, int ts_off) {
-    constexpr bool UP = (FEAT & FEAT_UPML) != 0;
-    const size_t sm = StageLayout<IdxT, UP, false, TY>::smem(e->stages);
-    dim3 grid((e->N[2] - 1 + 31) / 32, (e->N[1] - 1 + TY - 1) / TY, (e->N[0] - 1 + e->XC - 1) / e->XC);
-    k_curr_tma<IdxT, FEAT, GEO, EN, TY><<<grid, dim3(32, TY), sm, e->stream>>>(e->g, e->maps, e->ti, ts_off, e->XC,
-                                                                               e->stages);
-}
-
-template <typename IdxT, int FEAT, bool GEO>
-void launch_volt_t(fdtd_engine_s* e, int ts_off) {
-    if (e->use_tma) {
-        if (e->tma_ty == 8) launch_volt_tma<IdxT, FEAT, GEO, 8>(e, ts_off);
-        else launch_volt_tma<IdxT, FEAT, GEO, TMA_TY>(e, ts_off);
-    } else {
-        dim3 grid((e->N[2] + 31) / 32, (e->N[1] + e->TY - 1) / e->TY, (e->N[0] + e->XC - 1) / e->XC);
-        k_volt<IdxT, FEAT, GEO><<<grid, dim3(32, e->TY), e->smem_direct, e->stream>>>(e->g, ts_off, e->XC);
-    }
-}
-
-template <typename IdxT, int FEAT, bool GEO, bool EN>
-void launch_curr_t(fdtd_engine_s* e, int ts_off) {
-    if (e->use_tma) {
-        if (e->tma_ty == 8) launch_curr_tma<IdxT, FEAT, GEO, EN, 8>(e, ts_off);
-        else launch_curr_tma<IdxT, FEAT, GEO, EN, TMA_TY>(e, ts_off);
-    } else {
-        dim3 grid((e->N[2] + 31) / 32, (e->N[1] + e->TY - 1) / e->TY, (e->N[0] - 1 + e->XC - 1) / e->XC);
-        k_curr<IdxT, FEAT, GEO, EN><<<grid, dim3(32, e->TY), e->smem_direct, e->stream>>>(e->g, ts_off, e->XC);
-    }
-}
-
+// (the per-variant launch templates are in launch.cuh; the variants with
+// dispersion orders 1..3 are instantiated in engine_adex.cu)
 template <typename IdxT, bool GEO>
 void launch_volt_f(fdtd_engine_s* e, int ts_off) {
     switch (e->feat) {
         case 0: launch_volt_t<IdxT, 0, GEO>(e, ts_off); break;
         case 1: launch_volt_t<IdxT, 1, GEO>(e, ts_off); break;
         case 2: launch_volt_t<IdxT, 2, GEO>(e, ts_off); break;
-        default: launch_volt_t<IdxT, 3, GEO>(e, ts_off); break;
+        case 3: launch_volt_t<IdxT, 3, GEO>(e, ts_off); break;
+        default: launch_volt_adex<IdxT, GEO>(e, ts_off); break;
     }
 }
 
@@ -81,7 +45,8 @@ void launch_curr_f(fdtd_engine_s* e, int ts_off) {
         case 0: launch_curr_t<IdxT, 0, GEO, EN>(e, ts_off); break;
         case 1: launch_curr_t<IdxT, 1, GEO, EN>(e, ts_off); break;
         case 2: launch_curr_t<IdxT, 2, GEO, EN>(e, ts_off); break;
-        default: launch_curr_t<IdxT, 3, GEO, EN>(e, ts_off); break;
+        case 3: launch_curr_t<IdxT, 3, GEO, EN>(e, ts_off); break;
+        default: launch_curr_adex<IdxT, GEO, EN>(e, ts_off); break;
     }
 }
 
@@ -458,20 +423,6 @@ int make_tma_maps(const fdtd_engine_s* e, TmaMaps* m, uint32_t rows) {
 
 int make_maps(fdtd_engine_s* e) { return make_tma_maps(e, &e->maps, (uint32_t)e->tma_ty); }
 
-template <typename IdxT, int FEAT, bool GEO>
-cudaError_t smem_attr_one(int bytes) {
-    const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    cudaError_t r[6] = {cudaFuncSetAttribute(k_volt_tma<IdxT, FEAT, GEO, TMA_TY>, a, bytes),
-                        cudaFuncSetAttribute(k_curr_tma<IdxT, FEAT, GEO, true, TMA_TY>, a, bytes),
-                        cudaFuncSetAttribute(k_curr_tma<IdxT, FEAT, GEO, false, TMA_TY>, a, bytes),
-                        cudaFuncSetAttribute(k_volt_tma<IdxT, FEAT, GEO, 8>, a, bytes),
-                        cudaFuncSetAttribute(k_curr_tma<IdxT, FEAT, GEO, true, 8>, a, bytes),
-                        cudaFuncSetAttribute(k_curr_tma<IdxT, FEAT, GEO, false, 8>, a, bytes)};
-    for (cudaError_t x : r)
-        if (x != cudaSuccess) return x;
-    return cudaSuccess;
-}
-
 int set_smem_attrs(int bytes) {
     cudaError_t r = cudaSuccess, t;
 #define WIPEMS_ATTR(I, F)                                                 \
@@ -480,6 +431,7 @@ int set_smem_attrs(int bytes) {
     WIPEMS_ATTR(uint16_t, 0) WIPEMS_ATTR(uint16_t, 1) WIPEMS_ATTR(uint16_t, 2) WIPEMS_ATTR(uint16_t, 3)
     WIPEMS_ATTR(uint32_t, 0) WIPEMS_ATTR(uint32_t, 1) WIPEMS_ATTR(uint32_t, 2) WIPEMS_ATTR(uint32_t, 3)
 #undef WIPEMS_ATTR
+    if ((t = smem_attrs_adex(bytes)) != cudaSuccess) r = t;
     if (r != cudaSuccess) {
         set_error(std::string("cudaFuncSetAttribute(MaxDynamicSharedMemorySize): ") + cudaGetErrorString(r));
         return FDTD_ERR_CUDA;
@@ -495,6 +447,8 @@ int reset_state(fdtd_engine_s* e) {
     const size_t F = 3 * (size_t)e->comp * sizeof(float);
     for (DevBuf<float>* b : {&e->V, &e->I, &e->FV, &e->FI, &e->AV, &e->LV, &e->AI, &e->LI, &e->V2, &e->I2, &e->FV2})
         if (b->p) CK(cudaMemsetAsync(b->p, 0, F, s));
+    for (DevBuf<float>* b : {&e->AVx, &e->LVx, &e->AIx, &e->LIx})
+        if (b->p) CK(cudaMemsetAsync(b->p, 0, b->n * sizeof(float), s));
     CK(cudaMemsetAsync(e->ctl.p, 0, 4 * sizeof(int), s));
     if (e->d_fd.p) CK(cudaMemsetAsync(e->d_fd.p, 0, e->d_fd.n * sizeof(double), s));
     if (e->mur_buf.p) CK(cudaMemsetAsync(e->mur_buf.p, 0, e->mur_buf.n * sizeof(float), s));
@@ -516,7 +470,8 @@ int upload_half(fdtd_engine_s* e, const HalfTables& T, DevHalfBufs& B, DevHalf& 
     cudaStream_t st = e->stream;
     if ((rc = B.idx.alloc(T.idx_bytes, tot, st)) || (rc = B.main.alloc(T.main.size(), tot, st)) ||
         (rc = B.exc.alloc(std::max<size_t>(4, T.exc.size()), tot, st)) ||
-        (rc = B.upml.alloc(T.upml.size(), tot, st)) || (rc = B.ade.alloc(T.ade.size(), tot, st)))
+        (rc = B.upml.alloc(T.upml.size(), tot, st)) || (rc = B.ade.alloc(T.ade.size(), tot, st)) ||
+        (rc = B.adex.alloc(T.adex.size(), tot, st)))
         return rc;
     auto h2d = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
         return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, e->stream) : cudaSuccess;
@@ -526,11 +481,14 @@ int upload_half(fdtd_engine_s* e, const HalfTables& T, DevHalfBufs& B, DevHalf& 
     CK(h2d(B.exc.p, T.exc.data(), T.exc.size() * sizeof(float)));
     CK(h2d(B.upml.p, T.upml.data(), T.upml.size() * sizeof(float)));
     CK(h2d(B.ade.p, T.ade.data(), T.ade.size() * sizeof(float)));
+    CK(h2d(B.adex.p, T.adex.data(), T.adex.size() * sizeof(float)));
     D.idx = B.idx.p;
     D.main = reinterpret_cast<const float4*>(B.main.p);
     D.upml = reinterpret_cast<const float4*>(B.upml.p);
     D.ade = reinterpret_cast<const float4*>(B.ade.p);
     D.exc = reinterpret_cast<const float4*>(B.exc.p);
+    D.adex = reinterpret_cast<const float4*>(B.adex.p);
+    D.ntup = (int)T.num_tuples;
     return FDTD_OK;
 }
 
@@ -598,8 +556,9 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     e->comp = c->comp;
     e->geo_on = c->geo;
     const bool any_upml = c->E.any_upml || c->H.any_upml;
-    const bool any_ade = c->E.any_ade || c->H.any_ade;
-    e->feat = (any_upml ? FEAT_UPML : 0) | (any_ade ? FEAT_ADE : 0);
+    const bool any_adex = c->E.adex_orders || c->H.adex_orders;
+    const bool any_ade = c->E.any_ade || c->H.any_ade || any_adex;
+    e->feat = (any_upml ? FEAT_UPML : 0) | (any_ade ? FEAT_ADE : 0) | (any_adex ? FEAT_ADEX : 0);
     if (e->fused && (any_ade || c->geo)) {
         set_error("the fused single-pass kernel does not cover Lorentz/Drude nodes or factorized geometry "
                   "(use the two-pass TMA kernels)");
@@ -617,6 +576,10 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     if (c->E.any_lor && (rc = e->LV.alloc(F, tot, e->stream))) return rc;
     if (c->H.any_ade && (rc = e->AI.alloc(F, tot, e->stream))) return rc;
     if (c->H.any_lor && (rc = e->LI.alloc(F, tot, e->stream))) return rc;
+    if (c->E.adex_orders && (rc = e->AVx.alloc(c->E.adex_orders * F, tot, e->stream))) return rc;
+    if (c->E.any_lorx && (rc = e->LVx.alloc(c->E.adex_orders * F, tot, e->stream))) return rc;
+    if (c->H.adex_orders && (rc = e->AIx.alloc(c->H.adex_orders * F, tot, e->stream))) return rc;
+    if (c->H.any_lorx && (rc = e->LIx.alloc(c->H.adex_orders * F, tot, e->stream))) return rc;
     if ((rc = e->sigV.alloc(std::max<uint32_t>(1, c->sig_len), tot, e->stream)) ||
         (rc = e->sigC.alloc(std::max<uint32_t>(1, c->sig_len), tot, e->stream)))
         return rc;
@@ -751,6 +714,10 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     }
     g.AI = e->AI.p;
     g.LI = e->LI.p;
+    g.AVx = e->AVx.p;
+    g.LVx = e->LVx.p;
+    g.AIx = e->AIx.p;
+    g.LIx = e->LIx.p;
     g.geo = e->geo.p;
     g.geo_stride = (int)(e->N[0] + e->N[1] + e->N[2]);
     g.sigV = e->sigV.p;
@@ -1110,6 +1077,7 @@ std::vector<CkptPart> ckpt_parts(fdtd_engine_s* e, uint32_t nsamp) {
     add(e->d_fd_count.p, sizeof(int));
     add(e->mur_buf.p, e->mur_buf.n * sizeof(float));
     add(e->rlc_state.p, e->rlc_state.n * sizeof(float));
+    for (DevBuf<float>* b : {&e->AVx, &e->LVx, &e->AIx, &e->LIx}) add(b->p, b->n * sizeof(float));
     return v;
 }
 

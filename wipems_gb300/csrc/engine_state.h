@@ -61,7 +61,7 @@ struct DevBuf {
 
 struct DevHalfBufs {
     DevBuf<uint8_t> idx;
-    DevBuf<float> main, upml, ade, exc;
+    DevBuf<float> main, upml, ade, exc, adex;
     bool idx16 = true;
 };
 
@@ -86,6 +86,7 @@ struct fdtd_engine_s {
     double dT = 0;
     DevGrid g{};
     DevBuf<float> V, I, FV, FI, AV, LV, AI, LI;
+    DevBuf<float> AVx, LVx, AIx, LIx;  // states of dispersion orders 1..3: [order-1][3][comp]
     DevBuf<uint8_t> ade_tile;  // per voltage-kernel tile plane: Lorentz/Drude flags (DevGrid::ade_tile)
     DevBuf<double> edges;      // [2][Nx+Ny+Nz] main / dual edge lengths (field dumps; empty = no mesh lines)
     DevBuf<float> dump;        // field-dump scratch, grown on demand

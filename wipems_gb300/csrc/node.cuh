@@ -29,6 +29,7 @@ namespace wipems {
 // kernel feature bits (compile time)
 constexpr int FEAT_UPML = 1;
 constexpr int FEAT_ADE = 2;
+constexpr int FEAT_ADEX = 4;  // dispersion orders 1..3 (always with FEAT_ADE)
 
 // device view of one half-step's tables (float4 units, layout TAB_* in cop.h)
 struct DevHalf {
@@ -37,6 +38,8 @@ struct DevHalf {
     const float4* upml;
     const float4* ade;
     const float4* exc;
+    const float4* adex;  // dispersion orders 1..3: [order-1][tuple][TAB_ADE] or null
+    int ntup;            // tuples in the table (the adex order stride)
 };
 
 struct DevGrid {
@@ -55,6 +58,12 @@ struct DevGrid {
     float* LV;           // Lorentz voltage state
     float* AI;           // ADE current state
     float* LI;
+    // states of dispersion orders 1..3: [order-1][3][comp] (null when the
+    // operator has order 1 only)
+    float* AVx;
+    float* LVx;
+    float* AIx;
+    float* LIx;
     // per (x, 8-row y tile, 32-node z tile) of the voltage kernel: bit 0 =
     // a Lorentz/Drude node, bit 1 = a Lorentz node in that tile plane
     // (the TMA kernels stage the states of those tile planes); null = none
@@ -193,6 +202,41 @@ __device__ __forceinline__ void update_node(const DevGrid& g, float fld[3], cons
             }
         }
     }
+    // dispersion orders 1..3 (materials with several poles): the same update
+    // of each order's states from the same old field, in order
+    // (engine_ext_lorentzmaterial.cpp:80-121 loop over o); the new states
+    // stay in global memory and are subtracted after the node update
+    if ((FEAT & FEAT_ADEX) && (flags & TF_ADEX_ALL)) {
+        float* Ax = H ? g.AIx : g.AVx;
+        float* Lx = H ? g.LIx : g.LVx;
+#pragma unroll 1
+        for (int k = 0; k < kExtraOrders; ++k) {
+            if (!(flags & (TF_ADEX << k))) continue;
+            const float4* ta = T.adex + ((long long)k * T.ntup + t) * TAB_ADE;
+            const float4 a0 = __ldg(ta);
+            const float4 a1 = __ldg(ta + 1);
+            const float4 a2 = __ldg(ta + 2);
+            const float kint[3] = {a0.x, a0.y, a0.z};
+            const float kext[3] = {a0.w, a1.x, a1.y};
+            const float klor[3] = {a1.z, a1.w, a2.x};
+            float* As = Ax + (long long)k * 3 * C;
+            const bool lor = (flags & (TF_LORX << k)) != 0;
+#pragma unroll
+            for (int n = 0; n < 3; ++n) {
+                float a = As[n * C + o];
+                float f = fld[n];
+                if (lor) {
+                    float* Ls = Lx + (long long)k * 3 * C;
+                    const float l = __fadd_rn(Ls[n * C + o], __fmul_rn(klor[n], a));
+                    Ls[n * C + o] = l;
+                    f = __fsub_rn(f, l);
+                }
+                a = __fmul_rn(a, kint[n]);
+                a = __fadd_rn(a, __fmul_rn(kext[n], f));
+                As[n * C + o] = a;
+            }
+        }
+    }
     if ((FEAT & FEAT_UPML) && (flags & TF_UPML)) {
         const float4 u0 = __ldg(&T.upml[TAB_UPML * t]);
         const float4 u1 = __ldg(&T.upml[TAB_UPML * t + 1]);
@@ -215,6 +259,16 @@ __device__ __forceinline__ void update_node(const DevGrid& g, float fld[3], cons
     if ((FEAT & FEAT_ADE) && (flags & TF_ADE)) {
 #pragma unroll
         for (int n = 0; n < 3; ++n) fld[n] = __fsub_rn(fld[n], ade[n]);
+    }
+    // V -= ADE of each further order, order by order (engine_ext_dispersive.cpp:76-132)
+    if ((FEAT & FEAT_ADEX) && (flags & TF_ADEX_ALL)) {
+        const float* Ax = H ? g.AIx : g.AVx;
+#pragma unroll 1
+        for (int k = 0; k < kExtraOrders; ++k) {
+            if (!(flags & (TF_ADEX << k))) continue;
+#pragma unroll
+            for (int n = 0; n < 3; ++n) fld[n] = __fsub_rn(fld[n], Ax[(long long)k * 3 * C + n * C + o]);
+        }
     }
     if (flags & TF_EXC) {
         const float4 e0 = __ldg(&T.exc[TAB_EXC * t]);

@@ -126,8 +126,11 @@ uint64_t engine_footprint(const fdtd_cop_s* c, uint32_t interval, uint32_t max_t
     uint64_t b = 2 * r(F);
     if (c->E.any_upml || c->H.any_upml) b += 2 * r(F);
     b += (c->E.any_ade ? r(F) : 0) + (c->E.any_lor ? r(F) : 0) + (c->H.any_ade ? r(F) : 0) + (c->H.any_lor ? r(F) : 0);
+    for (const HalfTables* T : {&c->E, &c->H})  // states of dispersion orders 1..3
+        b += (T->adex_orders ? r(T->adex_orders * F) : 0) + (T->any_lorx ? r(T->adex_orders * F) : 0);
     for (const HalfTables* T : {&c->E, &c->H})
-        b += r(T->idx_bytes) + r(4 * (T->main.size() + T->upml.size() + T->ade.size() + T->exc.size()));
+        b += r(T->idx_bytes) +
+             r(4 * (T->main.size() + T->upml.size() + T->ade.size() + T->exc.size() + T->adex.size()));
     b += r(4 * c->geom.size()) + 2 * r(4 * std::max<uint32_t>(1, c->sig_len));
     const uint64_t cap = (interval ? max_ts / interval : 0) + 2;
     b += r(cap * (2 + nprobe) * 8) + 8 * (2u << 20);

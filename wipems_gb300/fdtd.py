@@ -490,6 +490,14 @@ class CompressedOperator:
               "fdtd_cop_expand_ext")
         return ade, upml
 
+    def expand_ade(self, half: int, order: int):
+        """The Lorentz/Drude ADE terms of one dispersion order (0..3) of one
+        half as the kernels apply them: [9][Nx][Ny][Nz] (int/ext/lor)."""
+        ade = np.empty((9,) + self.op.num_lines, np.float32)
+        check(lib().fdtd_cop_expand_ade(self._h, int(half), int(order), ade.ctypes.data_as(_abi.PF)),
+              "fdtd_cop_expand_ade")
+        return ade
+
 
 class Engine:
     """Engine_CUDA on one GPU.  op is an Operator (compressed here) or a

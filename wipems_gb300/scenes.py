@@ -327,6 +327,29 @@ def mini(kind: str, seed: int = 0, nr_ts: int = 400) -> Scene:
         stop = [lines[0][c[0] + 1], lines[1][c[1] + 1], lines[2][c[2] + 2]]
         s.add_lumped_port(start, stop, 2, 50.0, excite=1.0, priority=1000)
         return s
+    if kind in ("multipole", "multipole_graded"):
+        # Lorentz/Drude materials of dispersion order 2 and 3 (several poles
+        # per material, as metal models use): a Drude pole plus two Lorentz
+        # poles, a Lorentz pole plus a Drude pole with a magnetic second
+        # order, and an order-2 material beside an order-1 one
+        rng = np.random.default_rng(seed)
+        cells = [34, 30, 38]
+        graded = kind == "multipole_graded"
+        lines = [graded_lines(c, rng) for c in cells] if graded else [uniform_lines(c, 0.5) for c in cells]
+        s = _scene(*lines, 1e-3)
+        s.set_boundary([BC_PML] * 6, [5] * 6)
+        s.set_gauss_excite(8e9, 8e9, nr_ts)
+        boxes = [_pick_box(rng, lines, [6] * 3, [c - 6 for c in cells], 3, 10) for _ in range(3)]
+        s.add_lorentz(*boxes[0], eps_r=2.0, plasma_f=[6e9, 9e9, 4e9], relax_t=[1e-9, 2e-9, 0.5e-9],
+                      pole_f=[0.0, 7e9, 11e9], priority=10)
+        s.add_lorentz(*boxes[1], eps_r=3.0, plasma_f=[5e9, 8e9], relax_t=[1e-9, 1e-9], pole_f=[6e9, 0.0],
+                      mue_plasma_f=[0.0, 4e9], mue_relax_t=[0.0, 1e-9], priority=11)
+        s.add_lorentz(*boxes[2], eps_r=1.5, plasma_f=[3e9], relax_t=[2e-9], priority=12)
+        c = [n // 2 for n in cells]
+        start = [lines[0][c[0]], lines[1][c[1]], lines[2][c[2] - 2]]
+        stop = [lines[0][c[0] + 1], lines[1][c[1] + 1], lines[2][c[2] + 2]]
+        s.add_lumped_port(start, stop, 2, 50.0, excite=1.0, priority=1000)
+        return s
     if kind in ("magnetic", "magnetic_graded"):
         # the magnetic (mue) family of the Lorentz material, alone and with
         # the electric one: a double-negative Drude box, a magnetic Lorentz
