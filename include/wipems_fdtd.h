@@ -371,6 +371,15 @@ typedef struct fdtd_cop_s* fdtd_cop_t;
 int fdtd_compress(const fdtd_op_desc* desc, fdtd_cop_t* out);
 /* mode: 0 = automatic, 1 = exact, 2 = factorized geometry */
 int fdtd_compress_ex(const fdtd_op_desc* desc, int mode, fdtd_cop_t* out);
+/* As fdtd_compress_ex, choosing the device axes: rotation r relabels the
+ * grid cyclically so that device axis a is the operator's axis (a + r) % 3
+ * (x -> y -> z -> x leaves the EC update and its FP32 operation order
+ * unchanged, so the fields are bit-identical); -1 = automatic (the rotation
+ * with the fewest padded nodes for 32-node z tiles, when it saves over 3 %).
+ * fdtd_compress / fdtd_compress_ex choose automatically.  Everything the
+ * engine takes or returns (probe boxes, field arrays, dump boxes, single
+ * field values) stays in the operator's own axes. */
+int fdtd_compress_rot(const fdtd_op_desc* desc, int mode, int rotation, fdtd_cop_t* out);
 int fdtd_cop_destroy(fdtd_cop_t cop);
 
 typedef struct {
@@ -381,9 +390,11 @@ typedef struct {
     uint32_t num_upml_nodes;
     uint32_t num_ade_nodes;
     int      geometry_factored;
-    int      trim_e[3];       /* last line of the axis is inert for E */
+    int      trim_e[3];       /* last line of the device axis is inert for E */
     uint64_t host_bytes;
     int      pinned;
+    int      rotation;        /* device axis a = operator axis (a + rotation) % 3 */
+    uint32_t device_lines[3]; /* the grid in device axes */
 } fdtd_cop_info;
 
 int fdtd_cop_get_info(fdtd_cop_t cop, fdtd_cop_info* info);
@@ -602,7 +613,9 @@ typedef struct {
     int x_chunk;        /* x planes per work item (0 = chosen from the
                            batch's size by a wave model) */
     int stages;         /* TMA ring depth 3..8 (0 = 3) */
-    int blocks_per_sm;  /* cap on resident blocks per SM (0 = occupancy) */
+    int blocks_per_sm;  /* cap on resident blocks per SM (0 = occupancy);
+                           -1 = no persistent blocks: one block per work
+                           item, scheduled by the hardware */
     int graph_steps;    /* timesteps per captured graph (0 = 8, 1 = none) */
     int bin_mib;        /* L2 bins: jobs are packed into bins of at most this
                            many MiB of device state; each bin runs graph_steps

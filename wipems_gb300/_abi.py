@@ -94,7 +94,7 @@ class FdtdCopInfo(C.Structure):
     _fields_ = [("num_lines", u32 * 3), ("num_tuples_e", u32), ("num_tuples_h", u32), ("index_bytes_e", u32),
                 ("index_bytes_h", u32), ("padded_nz", u32), ("num_upml_nodes", u32), ("num_ade_nodes", u32),
                 ("geometry_factored", C.c_int), ("trim_e", C.c_int * 3), ("host_bytes", C.c_uint64),
-                ("pinned", C.c_int)]
+                ("pinned", C.c_int), ("rotation", C.c_int), ("device_lines", u32 * 3)]
 
 
 class FdtdBatchOpts(C.Structure):
@@ -180,6 +180,7 @@ SIGNATURES = [
     ("fdtd_operator_get_probe", C.c_int, [_P, u32, C.POINTER(FdtdProbeDesc)]),
     ("fdtd_compress", C.c_int, [C.POINTER(FdtdOpDesc), C.POINTER(_P)]),
     ("fdtd_compress_ex", C.c_int, [C.POINTER(FdtdOpDesc), C.c_int, C.POINTER(_P)]),
+    ("fdtd_compress_rot", C.c_int, [C.POINTER(FdtdOpDesc), C.c_int, C.c_int, C.POINTER(_P)]),
     ("fdtd_cop_destroy", C.c_int, [_P]),
     ("fdtd_cop_get_info", C.c_int, [_P, C.POINTER(FdtdCopInfo)]),
     ("fdtd_cop_expand", C.c_int, [_P, PF, PF, PF, PF, PU32, PU32]),

@@ -31,7 +31,7 @@ def signature(cop) -> str:
     i = cop.info
     n = i["num_lines"]
     return (f"{n[0]}x{n[1]}x{n[2]}_u{int(i['num_upml_nodes'] > 0)}_a{int(i['num_ade_nodes'] > 0)}"
-            f"_i{i['index_bytes_e']}{i['index_bytes_h']}_g{i['geometry_factored']}")
+            f"_i{i['index_bytes_e']}{i['index_bytes_h']}_g{i['geometry_factored']}_r{i.get('rotation', 0)}")
 
 
 def tune(cop, stages=DEFAULT_STAGES, xchunks=DEFAULT_XCHUNK, steps: int = 30, device: int = 0, verbose=False,
@@ -67,13 +67,14 @@ def tune(cop, stages=DEFAULT_STAGES, xchunks=DEFAULT_XCHUNK, steps: int = 30, de
     return best, table
 
 
-def tune_batch(cops, xchunks=(8, 16), graph_steps=(8, 32), blocks_per_sm=(0, 3, 2), steps: int = 64, device: int = 0,
+def tune_batch(cops, xchunks=(8, 16), graph_steps=(8, 32), blocks_per_sm=(0, 3, -1), steps: int = 64, device: int = 0,
                verbose=False):
     """Batched mode: times the persistent kernels of the whole job set for
     every (x_chunk, graph_steps, blocks_per_sm) combination over `steps`
     timesteps (fresh engines per candidate, device time from CUDA events);
-    blocks_per_sm caps the resident blocks each SM runs (0 = as many as fit)
-    -- the jobs-per-SM schedule of the work list.  Returns (best, table)."""
+    blocks_per_sm caps the resident blocks each SM runs (0 = as many as fit;
+    -1 = no persistent blocks, one block per work item) -- the jobs-per-SM
+    schedule of the work list.  Returns (best, table)."""
     from .fdtd import Batch, Engine
     table = []
     for bps in blocks_per_sm:

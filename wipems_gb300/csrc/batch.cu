@@ -299,7 +299,7 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
     b->device = engines[0] ? engines[0]->device : 0;
     b->XC = (o && o->x_chunk > 0) ? o->x_chunk : 0;  // 0: chosen below from the batch's size
     b->stages = (o && o->stages > 0) ? o->stages : 3;
-    b->blocks_per_sm = (o && o->blocks_per_sm > 0) ? o->blocks_per_sm : 0;
+    b->blocks_per_sm = (o && o->blocks_per_sm != 0) ? std::max(-1, o->blocks_per_sm) : 0;
     b->graph_steps = (o && o->graph_steps > 0) ? (uint32_t)o->graph_steps : 8;
     b->bin_bytes = (o && o->bin_mib > 0) ? (uint64_t)o->bin_mib << 20 : 0;
     if (b->stages < 3 || b->stages > TMA_MAX_STAGES) {
@@ -455,6 +455,10 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
         }
         G.gridE = std::max(1, std::min(G.nE, std::max(1, oE) * sms));
         G.gridH = std::max(1, std::min(G.nH, std::max(1, oH) * sms));
+        if (b->blocks_per_sm < 0) {  // one block per work item: the hardware schedules the items
+            G.gridE = std::max(1, G.nE);
+            G.gridH = std::max(1, G.nH);
+        }
     }
     CK(cudaStreamSynchronize(b->stream));
     return FDTD_OK;

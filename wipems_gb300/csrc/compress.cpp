@@ -79,7 +79,9 @@ bool mesh_uniform(const fdtd_op_desc* d) {
 
 struct Plan {
     const fdtd_op_desc* d;
-    uint32_t N[3];
+    uint32_t N[3];  // the operator's grid (reference axes)
+    int rot = 0;    // device axis a holds reference axis (a + rot) % 3
+    uint32_t D[3];  // the device grid: D[a] = N[(a + rot) % 3]
     size_t NN;
     bool geo;
     const float* gf[4][3];  // dE, iD, dH, iM per axis (float arrays in cop->geom)
@@ -161,14 +163,20 @@ int prepare(const fdtd_op_desc* d, Plan& P) {
 }
 
 // Builds the E (half = 0) or H (half = 1) tuple of a node.
+// (x, y, z) and gi are the node in the reference's axes; slot k of every
+// per-component group holds reference component (k + rot) % 3, the device
+// component k.
 void make_tuple(const Plan& P, int half, uint32_t x, uint32_t y, uint32_t z, size_t gi, HalfTuple& t) {
     const fdtd_op_desc* d = P.d;
     std::memset(&t, 0, P.key_bytes);
     const float* c1 = half ? d->ii : d->vv;
     const float* c2 = half ? d->iv : d->vi;
     const uint32_t pos[3] = {x, y, z};
-    for (int n = 0; n < 3; ++n) {
-        t.c[n] = c1[n * P.NN + gi];
+    int src[3];  // reference component of device slot k
+    for (int k = 0; k < 3; ++k) src[k] = (k + P.rot) % 3;
+    for (int k = 0; k < 3; ++k) {
+        const int n = src[k];
+        t.c[k] = c1[n * P.NN + gi];
         float v = c2[n * P.NN + gi];
         if (P.geo && v != 0.f) {
             const int nP = (n + 1) % 3, nPP = (n + 2) % 3;
@@ -178,8 +186,8 @@ void make_tuple(const Plan& P, int half, uint32_t x, uint32_t y, uint32_t z, siz
             const double g = (double)a0[pos[n]] * (double)a1[pos[nP]] * (double)a2[pos[nPP]];
             v = (float)((double)v / g);
         }
-        t.c[3 + n] = v;
-        t.xd[n] = -1;
+        t.c[3 + k] = v;
+        t.xd[k] = -1;
     }
     if (!P.slab.empty() && P.slab[gi] >= 0) {
         const fdtd_upml_desc& u = d->upml[P.slab[gi]];
@@ -189,10 +197,11 @@ void make_tuple(const Plan& P, int half, uint32_t x, uint32_t y, uint32_t z, siz
         const float* a = half ? u.ii : u.vv;
         const float* b = half ? u.iifo : u.vvfo;
         const float* c = half ? u.iifn : u.vvfn;
-        for (int n = 0; n < 3; ++n) {
-            t.u[n] = a[n * nloc + li];
-            t.u[3 + n] = b[n * nloc + li];
-            t.u[6 + n] = c[n * nloc + li];
+        for (int k = 0; k < 3; ++k) {
+            const int n = src[k];
+            t.u[k] = a[n * nloc + li];
+            t.u[3 + k] = b[n * nloc + li];
+            t.u[6 + k] = c[n * nloc + li];
         }
         t.flags |= TF_UPML;
     }
@@ -211,11 +220,12 @@ void make_tuple(const Plan& P, int half, uint32_t x, uint32_t y, uint32_t z, siz
         const bool lor_on = half ? A.curr_lor_on : A.volt_lor_on;
         float* dst = o == 0 ? t.a : t.ax[o - 1];
         bool lor = false;
-        for (int n = 0; n < 3; ++n) {
-            dst[n] = ai[n * A.count + i];
-            dst[3 + n] = ae[n * A.count + i];
-            dst[6 + n] = (lor_on && al) ? al[n * A.count + i] : 0.f;
-            if (dst[6 + n] != 0.f) lor = true;
+        for (int k = 0; k < 3; ++k) {
+            const int n = src[k];
+            dst[k] = ai[n * A.count + i];
+            dst[3 + k] = ae[n * A.count + i];
+            dst[6 + k] = (lor_on && al) ? al[n * A.count + i] : 0.f;
+            if (dst[6 + k] != 0.f) lor = true;
         }
         if (o == 0)
             t.flags |= TF_ADE | (lor ? TF_LOR : 0u);
@@ -224,14 +234,31 @@ void make_tuple(const Plan& P, int half, uint32_t x, uint32_t y, uint32_t z, siz
     }
     const auto& m = half ? P.cexc : P.vexc;
     if (!m.empty())
-        for (int n = 0; n < 3; ++n) {
-            auto it = m.find((uint64_t)gi * 3 + n);
+        for (int k = 0; k < 3; ++k) {
+            auto it = m.find((uint64_t)gi * 3 + src[k]);
             if (it != m.end()) {
-                t.x[n] = (half ? d->curr_amp : d->volt_amp)[it->second];
-                t.xd[n] = (int32_t)(half ? d->curr_delay : d->volt_delay)[it->second];
+                t.x[k] = (half ? d->curr_amp : d->volt_amp)[it->second];
+                t.xd[k] = (int32_t)(half ? d->curr_delay : d->volt_delay)[it->second];
                 t.flags |= TF_EXC;
             }
         }
+}
+
+// The cyclic relabelling of the axes that fits the grid best to the
+// kernels' tiles (32 z-lanes by 4 rows): the EC update is the same under
+// x -> y -> z -> x (every component's update has the same operation order
+// relative to its own axis), so a rotated grid gives bit-identical fields.
+// Cost = padded node count; a rotation is taken when it saves over 3 %.
+int choose_rotation(const uint32_t N[3], int want) {
+    if (want >= 0 && want <= 2) return want;
+    auto cost = [&](int r) {
+        const uint64_t dx = N[r % 3], dy = N[(1 + r) % 3], dz = N[(2 + r) % 3];
+        return (double)dx * (double)((dy + 3) / 4 * 4) * (double)((dz + 31) / 32 * 32);
+    };
+    int best = 0;
+    for (int r = 1; r < 3; ++r)
+        if (cost(r) < cost(best)) best = r;
+    return cost(best) < 0.97 * cost(0) ? best : 0;
 }
 
 // ---- factorized mode: snapping of rounding variants ------------------------
@@ -389,14 +416,16 @@ int alloc_index(HalfTables& T, size_t bytes, bool try_pinned) {
     return FDTD_OK;
 }
 
-int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
+int compress_impl(const fdtd_op_desc* d, int mode, int want_rot, fdtd_cop_s* c) {
     for (int a = 0; a < 3; ++a) {
         if (d->num_lines[a] < 2) {
             set_error("every axis needs at least two lines");
             return FDTD_ERR_ARG;
         }
-        c->N[a] = d->num_lines[a];
+        c->N0[a] = d->num_lines[a];
     }
+    c->rot = choose_rotation(c->N0, want_rot);
+    for (int a = 0; a < 3; ++a) c->N[a] = c->N0[(a + c->rot) % 3];
     if (!d->vv || !d->vi || !d->ii || !d->iv) {
         set_error("coefficient arrays missing");
         return FDTD_ERR_ARG;
@@ -413,16 +442,24 @@ int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
     c->dT = d->dT;
     Plan P;
     P.d = d;
-    for (int a = 0; a < 3; ++a) P.N[a] = c->N[a];
-    const uint32_t Nx = P.N[0], Ny = P.N[1], Nz = P.N[2];
+    P.rot = c->rot;
+    for (int a = 0; a < 3; ++a) {
+        P.N[a] = c->N0[a];
+        P.D[a] = c->N[a];
+    }
+    const uint32_t Nx = P.N[0], Ny = P.N[1], Nz = P.N[2];        // reference axes
+    const uint32_t Dx = P.D[0], Dy = P.D[1], Dz = P.D[2];        // device axes
     P.NN = (size_t)Nx * Ny * Nz;
     P.geo = (mode == 2) || (mode == 0 && have_lines && !mesh_uniform(d));
     c->geo = P.geo;
+    // per-axis arrays are laid out in device axis order; device axis a is
+    // reference axis (a + rot) % 3
     if (P.geo) {
         const size_t tot = (size_t)Nx + Ny + Nz;
         c->geom.assign(4 * tot, 0.f);
         size_t off = 0;
-        for (int a = 0; a < 3; ++a) {
+        for (int da = 0; da < 3; ++da) {
+            const int a = (da + P.rot) % 3;
             const uint32_t N = P.N[a];
             for (uint32_t i = 0; i < N; ++i) {
                 const double m = edge_len(d->lines[a], N, i, false, d->unit);
@@ -440,7 +477,8 @@ int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
         const size_t tot = (size_t)Nx + Ny + Nz;
         c->edges.assign(2 * tot, 0.0);
         size_t off = 0;
-        for (int a = 0; a < 3; ++a) {
+        for (int da = 0; da < 3; ++da) {
+            const int a = (da + P.rot) % 3;
             for (uint32_t i = 0; i < P.N[a]; ++i) {
                 c->edges[off + i] = edge_len(d->lines[a], P.N[a], i, false, d->unit);
                 c->edges[tot + off + i] = edge_len(d->lines[a], P.N[a], i, true, d->unit);
@@ -455,22 +493,28 @@ int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
     std::vector<std::vector<HalfTuple>> pt[2];
     std::vector<std::vector<uint32_t>> pl[2];
     for (int h = 0; h < 2; ++h) {
-        pt[h].resize(Nx);
-        pl[h].resize(Nx);
+        pt[h].resize(Dx);
+        pl[h].resize(Dx);
     }
-    std::vector<uint32_t> cnt_u(Nx, 0), cnt_a(Nx, 0);
+    std::vector<uint32_t> cnt_u(Dx, 0), cnt_a(Dx, 0);
+    // device plane x, row y, lane z -> the reference node
+    const int ax = (0 + P.rot) % 3, ay = (1 + P.rot) % 3, az = (2 + P.rot) % 3;
     auto worker = [&](uint32_t x) {
         for (int h = 0; h < 2; ++h) {
             TupleMap local = make_map(P.key_bytes);
             std::vector<HalfTuple>& tv = pt[h][x];
             std::vector<uint32_t>& lv = pl[h][x];
-            lv.resize((size_t)Ny * Nz);
+            lv.resize((size_t)Dy * Dz);
             HalfTuple t, last;
             uint32_t last_id = UINT32_MAX;
-            for (uint32_t y = 0; y < Ny; ++y)
-                for (uint32_t z = 0; z < Nz; ++z) {
-                    const size_t gi = ((size_t)x * Ny + y) * Nz + z;
-                    make_tuple(P, h, x, y, z, gi, t);
+            uint32_t o[3];
+            o[ax] = x;
+            for (uint32_t y = 0; y < Dy; ++y)
+                for (uint32_t z = 0; z < Dz; ++z) {
+                    o[ay] = y;
+                    o[az] = z;
+                    const size_t gi = ((size_t)o[0] * Ny + o[1]) * Nz + o[2];
+                    make_tuple(P, h, o[0], o[1], o[2], gi, t);
                     if (h == 0) {
                         if (t.flags & TF_UPML) cnt_u[x]++;
                         bool a = !P.ade.empty() && P.ade[gi] >= 0;
@@ -492,19 +536,19 @@ int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
                         last = t;
                         last_id = id;
                     }
-                    lv[(size_t)y * Nz + z] = id;
+                    lv[(size_t)y * Dz + z] = id;
                 }
         }
     };
     {
         std::atomic<uint32_t> next{0};
         std::vector<std::thread> pool;
-        const int nt = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), (int)Nx));
+        const int nt = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), (int)Dx));
         for (int t = 0; t < nt; ++t)
             pool.emplace_back([&] {
                 for (;;) {
                     const uint32_t x = next.fetch_add(1);
-                    if (x >= Nx) break;
+                    if (x >= Dx) break;
                     worker(x);
                 }
             });
@@ -513,16 +557,16 @@ int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
     int ndev = 0;
     const bool try_pinned = cudaGetDeviceCount(&ndev) == cudaSuccess && ndev > 0;
     if (!try_pinned) cudaGetLastError();
-    c->Nzp = (int)((Nz + 31) / 32 * 32);
-    c->comp = (long long)Nx * Ny * c->Nzp;
+    c->Nzp = (int)((Dz + 31) / 32 * 32);
+    c->comp = (long long)Dx * Dy * c->Nzp;
     std::vector<uint32_t> node_e;  // E tuple per node, for the trim test
     node_e.resize(P.NN);
     std::vector<HalfTuple> all[2];
     for (int h = 0; h < 2; ++h) {
         TupleMap global = make_map(P.key_bytes);
         std::vector<HalfTuple>& tuples = all[h];
-        std::vector<std::vector<uint32_t>> remap(Nx);
-        for (uint32_t x = 0; x < Nx; ++x) {
+        std::vector<std::vector<uint32_t>> remap(Dx);
+        for (uint32_t x = 0; x < Dx; ++x) {
             remap[x].resize(pt[h][x].size());
             for (size_t k = 0; k < pt[h][x].size(); ++k) {
                 auto it = global.find(pt[h][x][k]);
@@ -539,35 +583,35 @@ int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
         }
         if (P.geo) {  // factorized mode: merge the tuples that differ by rounding variants only
             std::vector<uint64_t> uses(tuples.size(), 0);
-            for (uint32_t x = 0; x < Nx; ++x)
+            for (uint32_t x = 0; x < Dx; ++x)
                 for (uint32_t lid : pl[h][x]) uses[remap[x][lid]]++;
             const std::vector<uint32_t> newid = snap_tuples(tuples, uses, P.key_bytes);
-            for (uint32_t x = 0; x < Nx; ++x)
+            for (uint32_t x = 0; x < Dx; ++x)
                 for (uint32_t& id : remap[x]) id = newid[id];
         }
         HalfTables& T = h ? c->H : c->E;
         T.idx16 = tuples.size() <= 65536;
         const size_t ib = T.idx16 ? 2 : 4;
         if ((rc = alloc_index(T, (size_t)c->comp * ib, try_pinned))) return rc;
-        for (uint32_t x = 0; x < Nx; ++x) {
+        for (uint32_t x = 0; x < Dx; ++x) {
             const std::vector<uint32_t>& lv = pl[h][x];
-            for (uint32_t y = 0; y < Ny; ++y) {
-                const size_t src = (size_t)y * Nz;
-                const size_t dst = ((size_t)x * Ny + y) * c->Nzp;
-                for (uint32_t z = 0; z < Nz; ++z) {
+            for (uint32_t y = 0; y < Dy; ++y) {
+                const size_t src = (size_t)y * Dz;
+                const size_t dst = ((size_t)x * Dy + y) * c->Nzp;
+                for (uint32_t z = 0; z < Dz; ++z) {
                     const uint32_t id = remap[x][lv[src + z]];
                     if (T.idx16)
                         reinterpret_cast<uint16_t*>(T.idx)[dst + z] = (uint16_t)id;
                     else
                         reinterpret_cast<uint32_t*>(T.idx)[dst + z] = id;
-                    if (h == 0) node_e[((size_t)x * Ny + y) * Nz + z] = id;
+                    if (h == 0) node_e[((size_t)x * Dy + y) * Dz + z] = id;
                 }
             }
             std::vector<uint32_t>().swap(pl[h][x]);
         }
         pack(tuples, T);
     }
-    for (uint32_t x = 0; x < Nx; ++x) {
+    for (uint32_t x = 0; x < Dx; ++x) {
         c->upml_nodes += cnt_u[x];
         c->ade_nodes += cnt_a[x];
     }
@@ -589,24 +633,31 @@ int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
             bool allz = true;
             uint32_t pos[3];
             const int b = (a + 1) % 3, cc = (a + 2) % 3;
-            pos[a] = P.N[a] - 1;
-            for (pos[b] = 0; pos[b] < P.N[b] && allz; ++pos[b])
-                for (pos[cc] = 0; pos[cc] < P.N[cc] && allz; ++pos[cc])
-                    allz = inert[node_e[((size_t)pos[0] * Ny + pos[1]) * Nz + pos[2]]] != 0;
+            pos[a] = P.D[a] - 1;
+            for (pos[b] = 0; pos[b] < P.D[b] && allz; ++pos[b])
+                for (pos[cc] = 0; pos[cc] < P.D[cc] && allz; ++pos[cc])
+                    allz = inert[node_e[((size_t)pos[0] * Dy + pos[1]) * Dz + pos[2]]] != 0;
             c->trim_e[a] = allz;
         }
     }
     // inner box outside of which the UPML slabs lie (slabs touching a face)
-    for (int a = 0; a < 3; ++a) {
-        c->inner_lo[a] = 0;
-        c->inner_hi[a] = (int)c->N[a] - 1;
-    }
-    for (uint32_t k = 0; k < d->num_upml; ++k) {
-        const fdtd_upml_desc& u = d->upml[k];
+    {
+        int lo[3], hi[3];  // reference axes
         for (int a = 0; a < 3; ++a) {
-            if (u.num_lines[a] == c->N[a]) continue;
-            if (u.start[a] == 0) c->inner_lo[a] = std::max(c->inner_lo[a], (int)u.num_lines[a]);
-            if (u.start[a] + u.num_lines[a] == c->N[a]) c->inner_hi[a] = std::min(c->inner_hi[a], (int)u.start[a] - 1);
+            lo[a] = 0;
+            hi[a] = (int)P.N[a] - 1;
+        }
+        for (uint32_t k = 0; k < d->num_upml; ++k) {
+            const fdtd_upml_desc& u = d->upml[k];
+            for (int a = 0; a < 3; ++a) {
+                if (u.num_lines[a] == P.N[a]) continue;
+                if (u.start[a] == 0) lo[a] = std::max(lo[a], (int)u.num_lines[a]);
+                if (u.start[a] + u.num_lines[a] == P.N[a]) hi[a] = std::min(hi[a], (int)u.start[a] - 1);
+            }
+        }
+        for (int da = 0; da < 3; ++da) {
+            c->inner_lo[da] = lo[(da + P.rot) % 3];
+            c->inner_hi[da] = hi[(da + P.rot) % 3];
         }
     }
     c->sig_len = d->signal_length;
@@ -623,8 +674,8 @@ int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
     // as the reference does.
     for (uint32_t f = 0; f < d->num_mur; ++f) {
         const fdtd_mur_desc& m = d->mur[f];
-        if (m.ny < 0 || m.ny > 2 || m.line >= c->N[m.ny] || m.shift >= c->N[m.ny] ||
-            m.n_p != c->N[(m.ny + 1) % 3] || m.n_pp != c->N[(m.ny + 2) % 3]) {
+        if (m.ny < 0 || m.ny > 2 || m.line >= P.N[m.ny] || m.shift >= P.N[m.ny] ||
+            m.n_p != P.N[(m.ny + 1) % 3] || m.n_pp != P.N[(m.ny + 2) % 3]) {
             set_error("Mur face descriptor does not match the grid");
             return FDTD_ERR_ARG;
         }
@@ -642,7 +693,9 @@ int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
                 return FDTD_ERR_UNSUPPORTED;
             }
         MurFace M;
-        M.ny = m.ny;
+        // device axis of the face normal; its (nyP, nyPP) layout is unchanged
+        // by a cyclic relabelling
+        M.ny = (m.ny - P.rot + 3) % 3;
         M.top = m.top;
         M.line = m.line;
         M.shift = m.shift;
@@ -664,11 +717,11 @@ int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
         std::vector<uint64_t> keys(r.count);
         for (uint32_t k = 0; k < r.count; ++k) {
             const int n = r.dir[k];
-            if (n < 0 || n > 2 || r.pos[0][k] >= c->N[0] || r.pos[1][k] >= c->N[1] || r.pos[2][k] >= c->N[2]) {
+            if (n < 0 || n > 2 || r.pos[0][k] >= P.N[0] || r.pos[1][k] >= P.N[1] || r.pos[2][k] >= P.N[2]) {
                 set_error("lumped RLC edge outside the grid");
                 return FDTD_ERR_ARG;
             }
-            keys[k] = (((uint64_t)r.pos[0][k] * c->N[1] + r.pos[1][k]) * c->N[2] + r.pos[2][k]) * 3 + n;
+            keys[k] = (((uint64_t)r.pos[0][k] * P.N[1] + r.pos[1][k]) * P.N[2] + r.pos[2][k]) * 3 + n;
         }
         std::vector<uint64_t> sorted = keys;
         std::sort(sorted.begin(), sorted.end());
@@ -677,7 +730,7 @@ int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
             return FDTD_ERR_UNSUPPORTED;
         }
         auto has = [&](uint32_t x, uint32_t y, uint32_t z, int n) {
-            const uint64_t key = (((uint64_t)x * c->N[1] + y) * c->N[2] + z) * 3 + n;
+            const uint64_t key = (((uint64_t)x * P.N[1] + y) * P.N[2] + z) * 3 + n;
             return std::binary_search(sorted.begin(), sorted.end(), key);
         };
         for (uint32_t o = 0; o < d->num_ade_orders; ++o) {
@@ -695,9 +748,10 @@ int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
                 set_error("a voltage excitation on a lumped RLC edge: not provided");
                 return FDTD_ERR_UNSUPPORTED;
             }
-        RlcList& q = c->rlc;
-        for (int a = 0; a < 3; ++a) q.pos[a].assign(r.pos[a], r.pos[a] + r.count);
-        q.dir.assign(r.dir, r.dir + r.count);
+        RlcList& q = c->rlc;  // in device axes
+        for (int a = 0; a < 3; ++a) q.pos[a].assign(r.pos[(a + P.rot) % 3], r.pos[(a + P.rot) % 3] + r.count);
+        q.dir.resize(r.count);
+        for (uint32_t k = 0; k < r.count; ++k) q.dir[k] = (r.dir[k] - P.rot + 3) % 3;
         q.ilv.assign(r.ilv, r.ilv + r.count);
         q.i2v.assign(r.i2v, r.i2v + r.count);
         q.vv2.assign(r.vv2, r.vv2 + r.count);
@@ -709,7 +763,7 @@ int compress_impl(const fdtd_op_desc* d, int mode, fdtd_cop_s* c) {
         q.b2.assign(r.b2, r.b2 + r.count);
         for (uint32_t k = 0; k < r.count; ++k)
             for (int a = 0; a < 3; ++a)
-                if (r.pos[a][k] == c->N[a] - 1) c->trim_e[a] = false;
+                if (q.pos[a][k] == c->N[a] - 1) c->trim_e[a] = false;
     }
     return FDTD_OK;
 }
@@ -721,16 +775,16 @@ using namespace wipems;
 
 extern "C" {
 
-int fdtd_compress_ex(const fdtd_op_desc* desc, int mode, fdtd_cop_t* out) {
-    if (!desc || !out || mode < 0 || mode > 2) {
-        set_error("fdtd_compress_ex: invalid argument");
+int fdtd_compress_rot(const fdtd_op_desc* desc, int mode, int rotation, fdtd_cop_t* out) {
+    if (!desc || !out || mode < 0 || mode > 2 || rotation < -1 || rotation > 2) {
+        set_error("fdtd_compress: invalid argument");
         return FDTD_ERR_ARG;
     }
     fdtd_cop_s* c = new (std::nothrow) fdtd_cop_s();
     if (!c) return FDTD_ERR_NOMEM;
     int rc;
     try {
-        rc = compress_impl(desc, mode, c);
+        rc = compress_impl(desc, mode, rotation, c);
     } catch (const std::bad_alloc&) {
         set_error("fdtd_compress: host allocation failed");
         rc = FDTD_ERR_NOMEM;
@@ -741,6 +795,10 @@ int fdtd_compress_ex(const fdtd_op_desc* desc, int mode, fdtd_cop_t* out) {
     }
     *out = c;
     return FDTD_OK;
+}
+
+int fdtd_compress_ex(const fdtd_op_desc* desc, int mode, fdtd_cop_t* out) {
+    return fdtd_compress_rot(desc, mode, -1, out);
 }
 
 int fdtd_compress(const fdtd_op_desc* desc, fdtd_cop_t* out) { return fdtd_compress_ex(desc, 0, out); }
@@ -754,9 +812,11 @@ int fdtd_cop_get_info(fdtd_cop_t c, fdtd_cop_info* info) {
     if (!c || !info) return FDTD_ERR_ARG;
     std::memset(info, 0, sizeof(*info));
     for (int a = 0; a < 3; ++a) {
-        info->num_lines[a] = c->N[a];
+        info->num_lines[a] = c->N0[a];
+        info->device_lines[a] = c->N[a];
         info->trim_e[a] = c->trim_e[a] ? 1 : 0;
     }
+    info->rotation = c->rot;
     info->num_tuples_e = c->E.num_tuples;
     info->num_tuples_h = c->H.num_tuples;
     info->index_bytes_e = c->E.idx16 ? 2 : 4;
@@ -773,18 +833,27 @@ int fdtd_cop_get_info(fdtd_cop_t c, fdtd_cop_info* info) {
     return FDTD_OK;
 }
 
+// reference node (x, y, z) -> offset of its device node in the padded index
+static size_t dev_index(const fdtd_cop_s* c, const uint32_t o[3]) {
+    const int r = c->rot;
+    const uint32_t d0 = o[r % 3], d1 = o[(1 + r) % 3], d2 = o[(2 + r) % 3];
+    return ((size_t)d0 * c->N[1] + d1) * c->Nzp + d2;
+}
+
 int fdtd_cop_expand(fdtd_cop_t c, float* vv, float* vi, float* ii, float* iv, uint32_t* flags_e, uint32_t* flags_h) {
     if (!c) return FDTD_ERR_ARG;
-    const uint32_t Nx = c->N[0], Ny = c->N[1], Nz = c->N[2];
+    const uint32_t Nx = c->N0[0], Ny = c->N0[1], Nz = c->N0[2];
     const size_t NN = (size_t)Nx * Ny * Nz;
     const size_t tot = (size_t)Nx + Ny + Nz;
-    const size_t off[3] = {0, Nx, (size_t)Nx + Ny};
+    const size_t off[3] = {0, c->N[0], (size_t)c->N[0] + c->N[1]};  // device axes
     for (uint32_t x = 0; x < Nx; ++x)
         for (uint32_t y = 0; y < Ny; ++y)
             for (uint32_t z = 0; z < Nz; ++z) {
-                const size_t pi = ((size_t)x * Ny + y) * c->Nzp + z;
+                const uint32_t o[3] = {x, y, z};
+                const size_t pi = dev_index(c, o);
                 const size_t gi = ((size_t)x * Ny + y) * Nz + z;
-                const uint32_t pos[3] = {x, y, z};
+                uint32_t pos[3];  // device node
+                for (int a = 0; a < 3; ++a) pos[a] = o[(a + c->rot) % 3];
                 for (int h = 0; h < 2; ++h) {
                     const HalfTables& T = h ? c->H : c->E;
                     const uint32_t t = T.idx16 ? reinterpret_cast<const uint16_t*>(T.idx)[pi]
@@ -792,16 +861,17 @@ int fdtd_cop_expand(fdtd_cop_t c, float* vv, float* vi, float* ii, float* iv, ui
                     const float* m = &T.main[(size_t)t * TAB_MAIN * 4];
                     float* o1 = h ? ii : vv;
                     float* o2 = h ? iv : vi;
-                    for (int n = 0; n < 3; ++n) {
-                        if (o1) o1[n * NN + gi] = m[n];
-                        float v = m[3 + n];
+                    for (int k = 0; k < 3; ++k) {  // device component k
+                        const int n = (k + c->rot) % 3;
+                        if (o1) o1[n * NN + gi] = m[k];
+                        float v = m[3 + k];
                         if (c->geo) {
                             // the kernels' float product ((V * g0) * g1) * g2
-                            const int nP = (n + 1) % 3, nPP = (n + 2) % 3;
+                            const int kP = (k + 1) % 3, kPP = (k + 2) % 3;
                             const float* g = c->geom.data();
-                            const float g0 = g[(h ? 2 : 0) * tot + off[n] + pos[n]];
-                            const float g1 = g[(h ? 3 : 1) * tot + off[nP] + pos[nP]];
-                            const float g2 = g[(h ? 3 : 1) * tot + off[nPP] + pos[nPP]];
+                            const float g0 = g[(h ? 2 : 0) * tot + off[k] + pos[k]];
+                            const float g1 = g[(h ? 3 : 1) * tot + off[kP] + pos[kP]];
+                            const float g2 = g[(h ? 3 : 1) * tot + off[kPP] + pos[kPP]];
                             v = v * g0;
                             v = v * g1;
                             v = v * g2;
@@ -815,23 +885,33 @@ int fdtd_cop_expand(fdtd_cop_t c, float* vv, float* vi, float* ii, float* iv, ui
     return FDTD_OK;
 }
 
+// the 9 per-node terms of an extension group (3 kinds x 3 components) of
+// tuple t, from the device table tab, into reference layout [9][NN]
+static void put9(const fdtd_cop_s* c, const float* tab, size_t gi, size_t NN, bool on, float* out) {
+    for (int kind = 0; kind < 3; ++kind)
+        for (int k = 0; k < 3; ++k)
+            out[(size_t)(3 * kind + (k + c->rot) % 3) * NN + gi] = on ? tab[3 * kind + k] : 0.f;
+}
+
 int fdtd_cop_expand_ade(fdtd_cop_t c, int half, int order, float* ade) {
     if (!c || half < 0 || half > 1 || order < 0 || order >= kMaxDispOrder || !ade) return FDTD_ERR_ARG;
     const HalfTables& T = half ? c->H : c->E;
-    const uint32_t Nx = c->N[0], Ny = c->N[1], Nz = c->N[2];
+    const uint32_t Nx = c->N0[0], Ny = c->N0[1], Nz = c->N0[2];
     const size_t NN = (size_t)Nx * Ny * Nz;
     const uint32_t bit = order == 0 ? TF_ADE : (TF_ADEX << (order - 1));
     const float* tab = order == 0 ? T.ade.data() : T.adex.data() + (size_t)(order - 1) * T.num_tuples * TAB_ADE * 4;
     for (uint32_t x = 0; x < Nx; ++x)
         for (uint32_t y = 0; y < Ny; ++y)
             for (uint32_t z = 0; z < Nz; ++z) {
-                const size_t pi = ((size_t)x * Ny + y) * c->Nzp + z;
+                const uint32_t o[3] = {x, y, z};
+                const size_t pi = dev_index(c, o);
                 const size_t gi = ((size_t)x * Ny + y) * Nz + z;
                 const uint32_t t = T.idx16 ? reinterpret_cast<const uint16_t*>(T.idx)[pi]
                                            : reinterpret_cast<const uint32_t*>(T.idx)[pi];
                 uint32_t flags;
                 std::memcpy(&flags, &T.main[(size_t)t * TAB_MAIN * 4 + 6], 4);
-                for (int k = 0; k < 9; ++k) ade[k * NN + gi] = (flags & bit) ? tab[(size_t)t * TAB_ADE * 4 + k] : 0.f;
+                const bool on = (flags & bit) != 0;
+                put9(c, on ? tab + (size_t)t * TAB_ADE * 4 : nullptr, gi, NN, on, ade);
             }
     return FDTD_OK;
 }
@@ -839,21 +919,21 @@ int fdtd_cop_expand_ade(fdtd_cop_t c, int half, int order, float* ade) {
 int fdtd_cop_expand_ext(fdtd_cop_t c, int half, float* ade, float* upml) {
     if (!c || half < 0 || half > 1) return FDTD_ERR_ARG;
     const HalfTables& T = half ? c->H : c->E;
-    const uint32_t Nx = c->N[0], Ny = c->N[1], Nz = c->N[2];
+    const uint32_t Nx = c->N0[0], Ny = c->N0[1], Nz = c->N0[2];
     const size_t NN = (size_t)Nx * Ny * Nz;
     for (uint32_t x = 0; x < Nx; ++x)
         for (uint32_t y = 0; y < Ny; ++y)
             for (uint32_t z = 0; z < Nz; ++z) {
-                const size_t pi = ((size_t)x * Ny + y) * c->Nzp + z;
+                const uint32_t o[3] = {x, y, z};
+                const size_t pi = dev_index(c, o);
                 const size_t gi = ((size_t)x * Ny + y) * Nz + z;
                 const uint32_t t = T.idx16 ? reinterpret_cast<const uint16_t*>(T.idx)[pi]
                                            : reinterpret_cast<const uint32_t*>(T.idx)[pi];
                 uint32_t flags;
                 std::memcpy(&flags, &T.main[(size_t)t * TAB_MAIN * 4 + 6], 4);
-                for (int k = 0; k < 9; ++k) {
-                    if (ade) ade[k * NN + gi] = (flags & TF_ADE) ? T.ade[(size_t)t * TAB_ADE * 4 + k] : 0.f;
-                    if (upml) upml[k * NN + gi] = (flags & TF_UPML) ? T.upml[(size_t)t * TAB_UPML * 4 + k] : 0.f;
-                }
+                const bool a = (flags & TF_ADE) != 0, u = (flags & TF_UPML) != 0;
+                if (ade) put9(c, a ? &T.ade[(size_t)t * TAB_ADE * 4] : nullptr, gi, NN, a, ade);
+                if (upml) put9(c, u ? &T.upml[(size_t)t * TAB_UPML * 4] : nullptr, gi, NN, u, upml);
             }
     return FDTD_OK;
 }

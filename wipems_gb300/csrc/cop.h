@@ -89,7 +89,13 @@ struct HalfTables {
 }  // namespace wipems
 
 struct fdtd_cop_s {
+    // Device axes: the kernels' grid is the operator's with its axes
+    // relabelled cyclically, device axis a = reference axis (a + rot) % 3
+    // (and device component n = reference component (n + rot) % 3); every
+    // array below is in device axes.  N0 is the operator's own grid.
     uint32_t N[3] = {0, 0, 0};
+    uint32_t N0[3] = {0, 0, 0};
+    int rot = 0;
     int Nzp = 0;
     long long comp = 0;
     double dT = 0;

@@ -493,7 +493,11 @@ int upload_half(fdtd_engine_s* e, const HalfTables& T, DevHalfBufs& B, DevHalf& 
 }
 
 int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine_s* e) {
-    for (int a = 0; a < 3; ++a) e->N[a] = c->N[a];
+    for (int a = 0; a < 3; ++a) {
+        e->N[a] = c->N[a];
+        e->N0[a] = c->N0[a];
+    }
+    e->rot = c->rot;
     e->dT = c->dT;
     e->device = opts ? opts->device : 0;
     CK(cudaSetDevice(e->device));
@@ -756,15 +760,19 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
 // Probe entries for ProcessVoltage (Engine_Interface_FDTD::CalcVoltageIntegral,
 // engine_interface_fdtd.cpp:200-226) and ProcessCurrent::CalcIntegral
 // (processcurrent.cpp:93-168), as (component, node, sign) lists.
+// The entries of an integral probe, built in the operator's axes in the
+// reference's walk order and mapped to device nodes one by one (so the
+// device sums run in the reference's order whatever the device axes).
 int probe_entries(const fdtd_engine_s* e, const fdtd_probe_desc* p, std::vector<ProbeEntry>& out) {
     auto add = [&](int field, int comp, uint32_t x, uint32_t y, uint32_t z, int sign) -> int {
-        if (x >= e->N[0] || y >= e->N[1] || z >= e->N[2]) {
+        if (x >= e->N0[0] || y >= e->N0[1] || z >= e->N0[2]) {
             set_error("probe position outside the grid");
             return FDTD_ERR_ARG;
         }
         ProbeEntry pe;
-        pe.off = (long long)x * e->g.sx + (long long)y * e->Nzp + z;
-        pe.comp = (int8_t)comp;
+        const uint32_t o[3] = {x, y, z};
+        pe.off = e->dev_offset(o);
+        pe.comp = (int8_t)e->dev_comp(comp);
         pe.sign = (int8_t)sign;
         pe.field = (int8_t)field;
         std::memset(pe.pad, 0, sizeof(pe.pad));
@@ -909,7 +917,7 @@ int fdtd_engine_add_probe(fdtd_engine_t e, const fdtd_probe_desc* p, uint32_t* s
     if (p->type == 2 || p->type == 3) {  // field probe: three columns, one entry each
         const bool h = p->type == 3;
         for (int a = 0; a < 3; ++a)
-            if (p->start[a] >= e->N[a]) {
+            if (p->start[a] >= e->N0[a]) {
                 set_error("fdtd_engine_add_probe: field probe outside the grid");
                 return FDTD_ERR_ARG;
             }
@@ -919,17 +927,17 @@ int fdtd_engine_add_probe(fdtd_engine_t e, const fdtd_probe_desc* p, uint32_t* s
         }
         if (slot) *slot = (uint32_t)e->h_weight.size();
         const size_t ntot = (size_t)e->N[0] + e->N[1] + e->N[2];
-        const size_t eoff[3] = {0, e->N[0], (size_t)e->N[0] + e->N[1]};
-        for (int n = 0; n < 3; ++n) {
+        const size_t eoff[3] = {0, e->N[0], (size_t)e->N[0] + e->N[1]};  // edge arrays in device axes
+        for (int n = 0; n < 3; ++n) {  // columns in the operator's component order
             double dv = -1.0;  // disabled probe or zero edge length: the column reads 0
             if (p->enabled) {
                 ProbeEntry pe{};
-                pe.off = (long long)p->start[0] * e->g.sx + (long long)p->start[1] * e->Nzp + p->start[2];
-                pe.comp = (int8_t)n;
+                pe.off = e->dev_offset(p->start);
+                pe.comp = (int8_t)e->dev_comp(n);
                 pe.sign = 1;
                 pe.field = (int8_t)(h ? 1 : 0);
                 e->h_entries.push_back(pe);
-                const double len = e->h_edges[(h ? ntot : 0) + eoff[n] + p->start[n]];
+                const double len = e->h_edges[(h ? ntot : 0) + eoff[e->dev_comp(n)] + p->start[n]];
                 if (len != 0.0) dv = len;
             }
             e->h_first.push_back((int)e->h_entries.size());
@@ -1055,7 +1063,7 @@ struct CkptHeader {
     int32_t Nzp;
     uint32_t nprobe, row_doubles, nfreq, nmur;
     uint32_t ts, done, nsamp;
-    int32_t fused;
+    int32_t frame;  // bit 0: fused single-pass kernel; bits 1-2: the device axis rotation
     uint32_t nrlc;
 };
 
@@ -1096,7 +1104,7 @@ void ckpt_header(const fdtd_engine_s* e, uint32_t nsamp, CkptHeader& h) {
     h.ts = e->ts;
     h.done = e->done ? 1u : 0u;
     h.nsamp = nsamp;
-    h.fused = e->fused ? 1 : 0;
+    h.frame = (e->fused ? 1 : 0) | (e->rot << 1);
     h.nrlc = e->rlc.count;
 }
 }  // namespace
@@ -1160,7 +1168,7 @@ int fdtd_engine_restore(fdtd_engine_t e, const void* buf, uint64_t size) {
     ckpt_header(e, h.nsamp, mine);
     if (std::memcmp(h.magic, mine.magic, 8) != 0 || h.version != mine.version || h.N[0] != mine.N[0] ||
         h.N[1] != mine.N[1] || h.N[2] != mine.N[2] || h.Nzp != mine.Nzp || h.nprobe != mine.nprobe ||
-        h.row_doubles != mine.row_doubles || h.nfreq != mine.nfreq || h.nmur != mine.nmur || h.fused != mine.fused ||
+        h.row_doubles != mine.row_doubles || h.nfreq != mine.nfreq || h.nmur != mine.nmur || h.frame != mine.frame ||
         h.nrlc != mine.nrlc) {
         set_error("fdtd_engine_restore: the checkpoint belongs to a different engine configuration");
         return FDTD_ERR_ARG;
@@ -1314,13 +1322,31 @@ int fdtd_engine_get_fields(fdtd_engine_t e, float* volt, float* curr) {
     if (!e) return FDTD_ERR_ARG;
     CK(cudaSetDevice(e->device));
     const uint32_t Nx = e->N[0], Ny = e->N[1], Nz = e->N[2];
+    const size_t n = (size_t)3 * Nx * Ny * Nz;
+    std::vector<float> tmp(e->rot ? n : 0);
     for (int which = 0; which < 2; ++which) {
         float* dst = which ? curr : volt;
         if (!dst) continue;
         const float* src = which ? e->cur_I() : e->cur_V();
         // rows of Nz floats out of rows of Nzp floats
-        CK(cudaMemcpy2DAsync(dst, Nz * sizeof(float), src, e->Nzp * sizeof(float), Nz * sizeof(float),
-                             (size_t)3 * Nx * Ny, cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaMemcpy2DAsync(e->rot ? tmp.data() : dst, Nz * sizeof(float), src, e->Nzp * sizeof(float),
+                             Nz * sizeof(float), (size_t)3 * Nx * Ny, cudaMemcpyDeviceToHost, e->stream));
+        if (!e->rot) continue;
+        CK(cudaStreamSynchronize(e->stream));
+        // device [3][Nx][Ny][Nz] -> the operator's [3][N0x][N0y][N0z]
+        const uint32_t* M = e->N0;
+        const size_t NN = (size_t)M[0] * M[1] * M[2];
+        for (int c = 0; c < 3; ++c) {
+            const float* s = tmp.data() + (size_t)e->dev_comp(c) * Nx * Ny * Nz;
+            float* d = dst + c * NN;
+            uint32_t o[3], dv[3];
+            for (o[0] = 0; o[0] < M[0]; ++o[0])
+                for (o[1] = 0; o[1] < M[1]; ++o[1])
+                    for (o[2] = 0; o[2] < M[2]; ++o[2]) {
+                        e->dev_node(o, dv);
+                        *d++ = s[((size_t)dv[0] * Ny + dv[1]) * Nz + dv[2]];
+                    }
+        }
     }
     CK(cudaStreamSynchronize(e->stream));
     return FDTD_OK;
@@ -1332,21 +1358,22 @@ int fdtd_engine_dump_field(fdtd_engine_t e, const fdtd_dump_box* b, float* out, 
         set_error("fdtd_engine_dump_field: field must be 0 (E) or 1 (H), interp 0 (none), 1 (node) or 2 (cell)");
         return FDTD_ERR_ARG;
     }
-    DumpBox d{};
+    DumpBox d{};  // in device axes (the interpolation is written per component n, nP, nPP)
     d.field = b->field;
     d.interp = b->interp;
     uint64_t total = 1;
-    for (int a = 0; a < 3; ++a) {
+    for (int a = 0; a < 3; ++a) {  // the operator's axis a is device axis dev_comp(a)
         const uint32_t lo = std::min(b->start[a], b->stop[a]), hi = std::max(b->start[a], b->stop[a]);
-        if (hi >= e->N[a]) {
+        if (hi >= e->N0[a]) {
             set_error("fdtd_engine_dump_field: box outside the grid");
             return FDTD_ERR_ARG;
         }
         const uint32_t step = b->step[a] ? b->step[a] : 1;
         num[a] = (hi - lo) / step + 1;  // ProcessFields::CalcMeshPos, SUBSAMPLE
-        d.start[a] = (int)lo;
-        d.step[a] = (int)step;
-        d.num[a] = (int)num[a];
+        const int da = e->dev_comp(a);
+        d.start[da] = (int)lo;
+        d.step[da] = (int)step;
+        d.num[da] = (int)num[a];
         total *= num[a];
     }
     if (!out) return FDTD_OK;  // size query
@@ -1375,18 +1402,37 @@ int fdtd_engine_dump_field(fdtd_engine_t e, const fdtd_dump_box* b, float* out, 
     const unsigned blocks = (unsigned)std::min<uint64_t>((total + 255) / 256, 4096);
     k_dump_field<<<blocks, 256, 0, e->stream>>>(e->g, e->cur_V(), e->cur_I(), e->edges.p, d, e->dump.p);
     if ((rc = check_launch())) return rc;
-    CK(cudaMemcpyAsync(out, e->dump.p, 3 * total * sizeof(float), cudaMemcpyDeviceToHost, e->stream));
+    if (!e->rot) {
+        CK(cudaMemcpyAsync(out, e->dump.p, 3 * total * sizeof(float), cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+        return FDTD_OK;
+    }
+    std::vector<float> tmp(3 * total);
+    CK(cudaMemcpyAsync(tmp.data(), e->dump.p, 3 * total * sizeof(float), cudaMemcpyDeviceToHost, e->stream));
     CK(cudaStreamSynchronize(e->stream));
+    // device [3][d.num] -> the operator's [3][num]
+    for (int c = 0; c < 3; ++c) {
+        const float* s = tmp.data() + (size_t)e->dev_comp(c) * total;
+        float* o = out + (size_t)c * total;
+        uint32_t i[3], j[3];
+        for (i[0] = 0; i[0] < num[0]; ++i[0])
+            for (i[1] = 0; i[1] < num[1]; ++i[1])
+                for (i[2] = 0; i[2] < num[2]; ++i[2]) {
+                    e->dev_node(i, j);
+                    *o++ = s[((size_t)j[0] * d.num[1] + j[1]) * d.num[2] + j[2]];
+                }
+    }
     return FDTD_OK;
 }
 
 static int get_one(fdtd_engine_t e, const float* base, uint32_t n, uint32_t x, uint32_t y, uint32_t z, float* v) {
-    if (!e || !v || n > 2 || x >= e->N[0] || y >= e->N[1] || z >= e->N[2]) {
+    if (!e || !v || n > 2 || x >= e->N0[0] || y >= e->N0[1] || z >= e->N0[2]) {
         set_error("field access out of range");
         return FDTD_ERR_ARG;
     }
     CK(cudaSetDevice(e->device));
-    const long long off = n * e->comp + (long long)x * e->g.sx + (long long)y * e->Nzp + z;
+    const uint32_t o[3] = {x, y, z};
+    const long long off = e->dev_comp((int)n) * e->comp + e->dev_offset(o);
     CK(cudaMemcpyAsync(v, base + off, sizeof(float), cudaMemcpyDeviceToHost, e->stream));
     CK(cudaStreamSynchronize(e->stream));
     return FDTD_OK;
@@ -1400,7 +1446,7 @@ int fdtd_engine_get_curr(fdtd_engine_t e, uint32_t n, uint32_t x, uint32_t y, ui
 }
 
 static int set_one(fdtd_engine_t e, float* base, uint32_t n, uint32_t x, uint32_t y, uint32_t z, float v) {
-    if (!e || n > 2 || x >= e->N[0] || y >= e->N[1] || z >= e->N[2]) {
+    if (!e || n > 2 || x >= e->N0[0] || y >= e->N0[1] || z >= e->N0[2]) {
         set_error("field access out of range");
         return FDTD_ERR_ARG;
     }
@@ -1409,7 +1455,8 @@ static int set_one(fdtd_engine_t e, float* base, uint32_t n, uint32_t x, uint32_
         return FDTD_ERR_STATE;
     }
     CK(cudaSetDevice(e->device));
-    const long long off = n * e->comp + (long long)x * e->g.sx + (long long)y * e->Nzp + z;
+    const uint32_t o[3] = {x, y, z};
+    const long long off = e->dev_comp((int)n) * e->comp + e->dev_offset(o);
     CK(cudaMemcpyAsync(base + off, &v, sizeof(float), cudaMemcpyHostToDevice, e->stream));
     CK(cudaStreamSynchronize(e->stream));
     return FDTD_OK;

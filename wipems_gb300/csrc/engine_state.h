@@ -80,8 +80,20 @@ struct fdtd_engine_s {
             if (*s) cudaStreamDestroy(*s);
         }
     } stream_guard{&stream};
-    uint32_t N[3];
+    uint32_t N[3];             // device axes (see fdtd_cop_s)
+    uint32_t N0[3] = {0, 0, 0};  // the operator's axes, in which the API speaks
+    int rot = 0;               // device axis a = operator axis (a + rot) % 3
     int Nzp = 0;
+    // device node / component of a node / component in the operator's axes
+    void dev_node(const uint32_t o[3], uint32_t d[3]) const {
+        for (int a = 0; a < 3; ++a) d[a] = o[(a + rot) % 3];
+    }
+    int dev_comp(int n) const { return (n - rot + 3) % 3; }
+    long long dev_offset(const uint32_t o[3]) const {
+        uint32_t d[3];
+        dev_node(o, d);
+        return (long long)d[0] * g.sx + (long long)d[1] * Nzp + d[2];
+    }
     long long comp = 0;
     double dT = 0;
     DevGrid g{};

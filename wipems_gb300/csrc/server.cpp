@@ -68,7 +68,8 @@ struct Job {
     std::vector<fdtd_probe_desc> probes;
     uint32_t interval = 0, max_ts = 0;
     uint64_t nodes = 0, footprint = 0;
-    uint32_t N[3] = {0, 0, 0};
+    uint32_t N[3] = {0, 0, 0};   // device axes (tiling)
+    uint32_t N0[3] = {0, 0, 0};  // the operator's axes (reported)
     double dT = 0;
     fdtd_engine_t eng = nullptr;
     uint32_t ts = 0;
@@ -174,7 +175,10 @@ void build_one(fdtd_server_s* s, Job* j) {
     j->interval = j->opts.probe_interval ? j->opts.probe_interval : info.probe_interval;
     j->max_ts = j->opts.max_timesteps ? j->opts.max_timesteps : (nr_ts ? nr_ts : 100000);
     j->nodes = (uint64_t)cop->N[0] * cop->N[1] * cop->N[2];
-    for (int a = 0; a < 3; ++a) j->N[a] = cop->N[a];
+    for (int a = 0; a < 3; ++a) {
+        j->N[a] = cop->N[a];
+        j->N0[a] = cop->N0[a];
+    }
     j->dT = cop->dT;
     j->footprint = engine_footprint(cop, j->interval, j->max_ts, sample_columns(j));
     if (j->footprint > s->budget || (j->opts.end_crit > 0 && j->interval == 0)) {
@@ -593,7 +597,7 @@ int fdtd_server_job_status(fdtd_server_t s, uint64_t id, fdtd_job_status* st) {
     st->num_samples = (uint32_t)j->s_ts.size();
     st->num_probes = (uint32_t)sample_columns(j);
     st->nodes = j->nodes;
-    for (int a = 0; a < 3; ++a) st->num_lines[a] = j->N[a];
+    for (int a = 0; a < 3; ++a) st->num_lines[a] = j->N0[a];
     st->dT = j->dT;
     st->footprint = j->footprint;
     st->probe_interval = j->interval;

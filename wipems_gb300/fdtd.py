@@ -449,16 +449,20 @@ class CompressedOperator:
 
     MODES = {"auto": 0, "exact": 1, "factorized": 2}
 
-    def __init__(self, op: Operator, mode: str = "auto"):
+    def __init__(self, op: Operator, mode: str = "auto", rotation: int | str = "auto"):
+        """rotation: the device axes (fdtd_compress_rot): "auto", or r in
+        0..2 for device axis a = the operator's axis (a + r) % 3."""
         h = C.c_void_p()
-        check(lib().fdtd_compress_ex(C.byref(op.desc), self.MODES[mode], C.byref(h)), "fdtd_compress")
+        rot = -1 if rotation == "auto" else int(rotation)
+        check(lib().fdtd_compress_rot(C.byref(op.desc), self.MODES[mode], rot, C.byref(h)), "fdtd_compress")
         self._h = h
         self.op = op
         info = _abi.FdtdCopInfo()
         check(lib().fdtd_cop_get_info(h, C.byref(info)), "fdtd_cop_get_info")
-        self.info = {k: (list(getattr(info, k)) if k in ("num_lines", "trim_e") else getattr(info, k))
+        self.info = {k: (list(getattr(info, k)) if k in ("num_lines", "trim_e", "device_lines") else getattr(info, k))
                      for k, _ in info._fields_}
         self.factorized = bool(self.info["geometry_factored"])
+        self.rotation = self.info["rotation"]
 
     def __del__(self):
         if getattr(self, "_h", None):
