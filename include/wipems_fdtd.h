@@ -621,6 +621,12 @@ typedef struct {
                            many MiB of device state; each bin runs graph_steps
                            steps in a row so its data is re-read from L2
                            (0 = one bin with every job) */
+    int chains;         /* each kernel-variant group is split into this many
+                           job ranges (balanced by node count) that advance
+                           as independent chains of kernels on their own
+                           streams, so one chain's last wave overlaps the
+                           others' work (0 = 1: one chain per group, the
+                           groups in sequence) */
 } fdtd_batch_opts;
 
 typedef struct {

@@ -59,6 +59,9 @@ __global__ void __launch_bounds__(256) k_batch_energy_planes(const AdvJob* __res
     if (threadIdx.x == 0) J.g.eplane[blockIdx.x] = r;
 }
 
+// The jobs of one kernel variant (index width, features, geometry mode) in
+// one bin, or one chain's share of them: a contiguous range of the batch's
+// job order, so the range's samplers are one launch.
 struct Group {
     int bin = 0;
     bool e16 = true, h16 = true, geo = false;
@@ -67,6 +70,8 @@ struct Group {
     DevBuf<WorkItem> itE, itH;
     int nE = 0, nH = 0, gridE = 0, gridH = 0;
     size_t smemE = 0, smemH = 0;
+    int first = 0, count = 0;  // job range
+    int max_planes = 1;        // largest Nx-1 of its jobs
 };
 
 template <typename IdxT, int FEAT, bool GEO>
@@ -225,6 +230,9 @@ struct fdtd_batch_s {
     std::vector<Bin> bins;
     uint64_t bin_bytes = 0;
     int XC = 8, stages = 3, blocks_per_sm = 0;
+    int chains = 1;                    // chains per kernel-variant group
+    std::vector<cudaStream_t> side;    // one stream per chain of a bin
+    std::vector<cudaEvent_t> ev_fork, ev_join;
     uint32_t graph_steps = 8;
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -236,6 +244,9 @@ struct fdtd_batch_s {
         if (graph) cudaGraphExecDestroy(graph);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
+        for (cudaEvent_t e : ev_fork) cudaEventDestroy(e);
+        for (cudaEvent_t e : ev_join) cudaEventDestroy(e);
+        for (cudaStream_t s : side) cudaStreamDestroy(s);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -247,7 +258,37 @@ namespace {
 // groups, their current kernels, then the bin's samplers.  (Running the
 // groups of a half-step concurrently on side streams was measured slower:
 // each persistent grid already fills the GPU.)
+// one timestep of chain G (a group's job range) on stream st: its voltage
+// kernel, its current kernel, then the samplers of its jobs
+void chain_step(fdtd_batch_s* b, const Group& G, cudaStream_t st) {
+    launch_group_volt(G, b->d_jobs.p, b->XC, b->stages, st);
+    launch_group_curr(G, b->d_jobs.p, b->XC, b->stages, st);
+    k_batch_energy_planes<<<dim3((unsigned)G.max_planes, (unsigned)G.count), 256, 0, st>>>(b->d_adv.p + G.first);
+    k_batch_advance<<<(unsigned)G.count, 256, 0, st>>>(b->d_adv.p + G.first, kEps0, kMue0);
+    b->last_launches += 4;
+}
+
+// `steps` timesteps of bin k as independent chains: fork the chains' streams
+// off the batch stream, run each chain's steps on its own stream, join
+int bin_chains(fdtd_batch_s* b, size_t k, uint32_t steps) {
+    const fdtd_batch_s::Bin& B = b->bins[k];
+    CK(cudaEventRecord(b->ev_fork[0], b->stream));
+    for (size_t i = 0; i < B.groups.size(); ++i) {
+        CK(cudaStreamWaitEvent(b->side[i], b->ev_fork[0], 0));
+        for (uint32_t s = 0; s < steps; ++s) chain_step(b, b->groups[B.groups[i]], b->side[i]);
+        CK(cudaEventRecord(b->ev_join[i], b->side[i]));
+    }
+    for (size_t i = 0; i < B.groups.size(); ++i) CK(cudaStreamWaitEvent(b->stream, b->ev_join[i], 0));
+    const cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) {
+        set_error(std::string("batch kernel launch: ") + cudaGetErrorString(err));
+        return FDTD_ERR_CUDA;
+    }
+    return FDTD_OK;
+}
+
 int bin_step(fdtd_batch_s* b, size_t k) {
+    if (b->chains > 1) return bin_chains(b, k, 1);
     const fdtd_batch_s::Bin& B = b->bins[k];
     const size_t ng = B.groups.size();
     for (int gi : B.groups) launch_group_volt(b->groups[gi], b->d_jobs.p, b->XC, b->stages, b->stream);
@@ -269,8 +310,13 @@ int batch_graph(fdtd_batch_s* b) {
     CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     int rc = FDTD_OK;
     const uint64_t saved = b->last_launches;
-    for (size_t bi = 0; bi < b->bins.size() && rc == FDTD_OK; ++bi)
+    for (size_t bi = 0; bi < b->bins.size() && rc == FDTD_OK; ++bi) {
+        if (b->chains > 1) {
+            rc = bin_chains(b, bi, b->graph_steps);
+            continue;
+        }
         for (uint32_t k = 0; k < b->graph_steps && rc == FDTD_OK; ++k) rc = bin_step(b, bi);
+    }
     b->last_launches = saved;
     const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
     if (rc) {
@@ -302,6 +348,7 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
     b->blocks_per_sm = (o && o->blocks_per_sm != 0) ? std::max(-1, o->blocks_per_sm) : 0;
     b->graph_steps = (o && o->graph_steps > 0) ? (uint32_t)o->graph_steps : 8;
     b->bin_bytes = (o && o->bin_mib > 0) ? (uint64_t)o->bin_mib << 20 : 0;
+    b->chains = (o && o->chains > 1) ? std::min(o->chains, 64) : 1;
     if (b->stages < 3 || b->stages > TMA_MAX_STAGES) {
         set_error("fdtd_batch_create: stages must be 3..8");
         return FDTD_ERR_ARG;
@@ -355,33 +402,69 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
             load[k] += e->device_bytes;
         }
     }
-    // jobs stored bin by bin; groups per (bin, kernel variant)
+    // jobs stored bin by bin and, within a bin, kernel variant by kernel
+    // variant; each variant's job range is split into `chains` ranges of
+    // about equal node count (one group each)
+    size_t max_groups = 1;
     for (size_t bi = 0; bi < binned.size(); ++bi) {
         fdtd_batch_s::Bin B;
         B.first = (int)b->jobs.size();
         B.count = (int)binned[bi].size();
-        std::map<std::tuple<int, int, int, int>, int> gidx;
-        for (fdtd_engine_s* e : binned[bi]) {
-            const int j = (int)b->jobs.size();
-            b->jobs.push_back(e);
-            b->total_nodes += (uint64_t)e->N[0] * e->N[1] * e->N[2];
-            B.max_planes = std::max(B.max_planes, (int)e->N[0] - 1);
-            auto key = std::make_tuple((int)e->E.idx16, (int)e->H.idx16, (int)e->geo_on, e->feat);
-            auto it = gidx.find(key);
-            if (it == gidx.end()) {
-                Group G;
-                G.bin = (int)bi;
-                G.e16 = e->E.idx16;
-                G.h16 = e->H.idx16;
-                G.geo = e->geo_on;
-                G.feat = e->feat;
-                b->groups.push_back(std::move(G));
-                it = gidx.emplace(key, (int)b->groups.size() - 1).first;
-                B.groups.push_back(it->second);
+        auto key_of = [](const fdtd_engine_s* e) {
+            return std::make_tuple((int)e->E.idx16, (int)e->H.idx16, (int)e->geo_on, e->feat);
+        };
+        std::vector<fdtd_engine_s*> jobs = binned[bi];
+        std::stable_sort(jobs.begin(), jobs.end(),
+                         [&](const fdtd_engine_s* a, const fdtd_engine_s* c) { return key_of(a) < key_of(c); });
+        for (size_t lo = 0; lo < jobs.size();) {
+            size_t hi = lo;
+            uint64_t nodes = 0;
+            while (hi < jobs.size() && key_of(jobs[hi]) == key_of(jobs[lo])) {
+                nodes += (uint64_t)jobs[hi]->N[0] * jobs[hi]->N[1] * jobs[hi]->N[2];
+                ++hi;
             }
-            b->groups[it->second].jobs.push_back(j);
+            const int parts = (int)std::min<size_t>((size_t)b->chains, hi - lo);
+            uint64_t acc = 0;
+            int part = -1;
+            for (size_t q = lo; q < hi; ++q) {
+                fdtd_engine_s* e = jobs[q];
+                const uint64_t en = (uint64_t)e->N[0] * e->N[1] * e->N[2];
+                // the part whose node share holds this job's midpoint
+                const int want = std::min(parts - 1, (int)((acc + en / 2) * (uint64_t)parts / std::max<uint64_t>(1, nodes)));
+                if (want != part || part < 0) {
+                    Group G;
+                    G.bin = (int)bi;
+                    G.e16 = e->E.idx16;
+                    G.h16 = e->H.idx16;
+                    G.geo = e->geo_on;
+                    G.feat = e->feat;
+                    G.first = (int)b->jobs.size();
+                    b->groups.push_back(std::move(G));
+                    B.groups.push_back((int)b->groups.size() - 1);
+                    part = want;
+                }
+                Group& G = b->groups.back();
+                const int j = (int)b->jobs.size();
+                b->jobs.push_back(e);
+                G.jobs.push_back(j);
+                G.count++;
+                G.max_planes = std::max(G.max_planes, (int)e->N[0] - 1);
+                b->total_nodes += en;
+                B.max_planes = std::max(B.max_planes, (int)e->N[0] - 1);
+                acc += en;
+            }
+            lo = hi;
         }
+        max_groups = std::max(max_groups, B.groups.size());
         b->bins.push_back(std::move(B));
+    }
+    if (b->chains > 1) {
+        b->side.resize(max_groups, nullptr);
+        b->ev_join.resize(max_groups, nullptr);
+        b->ev_fork.resize(1, nullptr);
+        for (cudaStream_t& s : b->side) CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        for (cudaEvent_t& e : b->ev_join) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&b->ev_fork[0], cudaEventDisableTiming));
     }
     // descriptors
     std::vector<TmaMaps> hmaps(n);  // the jobs' tensor maps for the batch's BATCH_TY-row tiles
@@ -519,7 +602,8 @@ int fdtd_batch_iterate(fdtd_batch_t b, uint32_t n) {
     while (left > 0) {
         if (b->graph && left >= b->graph_steps) {
             CK(cudaGraphLaunch(b->graph, b->stream));
-            b->last_launches += (2 * b->groups.size() + 2 * b->bins.size()) * b->graph_steps;
+            b->last_launches += (b->chains > 1 ? 4 * b->groups.size() : 2 * b->groups.size() + 2 * b->bins.size()) *
+                                b->graph_steps;
             left -= b->graph_steps;
             continue;
         }

@@ -166,6 +166,16 @@ __device__ __forceinline__ void update_node(const DevGrid& g, float fld[3], cons
 #pragma unroll
         for (int n = 0; n < 3; ++n) c2[n] = __fmul_rn(__fmul_rn(__fmul_rn(c2[n], gf.f[n][0]), gf.f[n][1]), gf.f[n][2]);
     }
+    // In tile planes that hold Lorentz/Drude nodes (the staged state
+    // pointer is set) the ADE coefficients are loaded with the main tuple,
+    // not after its flags: one table round trip per node instead of two.
+    const bool spec_a = (FEAT & FEAT_ADE) && asrc != nullptr;
+    float4 sa0 = make_float4(0.f, 0.f, 0.f, 0.f), sa1 = sa0, sa2 = sa0;
+    if (spec_a) {
+        sa0 = __ldg(&T.ade[TAB_ADE * t]);
+        sa1 = __ldg(&T.ade[TAB_ADE * t + 1]);
+        sa2 = __ldg(&T.ade[TAB_ADE * t + 2]);
+    }
     const uint32_t flags = __float_as_uint(tb.z);
     const long long C = g.comp;
     float* A = H ? g.AI : g.AV;
@@ -173,9 +183,9 @@ __device__ __forceinline__ void update_node(const DevGrid& g, float fld[3], cons
     float* Fl = fout ? fout : (H ? g.FI : g.FV);
     float ade[3] = {0.f, 0.f, 0.f};
     if ((FEAT & FEAT_ADE) && (flags & TF_ADE)) {
-        const float4 a0 = __ldg(&T.ade[TAB_ADE * t]);
-        const float4 a1 = __ldg(&T.ade[TAB_ADE * t + 1]);
-        const float4 a2 = __ldg(&T.ade[TAB_ADE * t + 2]);
+        const float4 a0 = spec_a ? sa0 : __ldg(&T.ade[TAB_ADE * t]);
+        const float4 a1 = spec_a ? sa1 : __ldg(&T.ade[TAB_ADE * t + 1]);
+        const float4 a2 = spec_a ? sa2 : __ldg(&T.ade[TAB_ADE * t + 2]);
         const float kint[3] = {a0.x, a0.y, a0.z};
         const float kext[3] = {a0.w, a1.x, a1.y};
         const float klor[3] = {a1.z, a1.w, a2.x};
