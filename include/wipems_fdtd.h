@@ -627,6 +627,8 @@ typedef struct {
                            streams, so one chain's last wave overlaps the
                            others' work (0 = 1: one chain per group, the
                            groups in sequence) */
+    int tile_y;         /* rows of the batched kernels' 32-lane tiles: 4 or 8
+                           (0 = 8) */
 } fdtd_batch_opts;
 
 typedef struct {

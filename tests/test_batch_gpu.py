@@ -31,14 +31,14 @@ def _check_same(solo, batched):
     assert np.array_equal(ss.energy, sb.energy)  # fixed-order energy: the same bits
 
 
-@pytest.mark.parametrize("graph_steps,bin_mib,bps,chains", [(8, 0, 0, 0), (1, 0, 0, 0), (8, 1, 0, 0),
-                                                            (8, 0, -1, 0), (8, 0, -1, 3), (1, 0, -1, 2),
-                                                            (8, 1, -1, 2)])
-def test_batch_equals_solo_runs(graph_steps, bin_mib, bps, chains):
-    """Persistent and one-block-per-item kernels, one chain per kernel
-    variant or several job-range chains on their own streams (graphs and
-    single steps, with and without L2 bins): every job bit-identical to its
-    solo run."""
+@pytest.mark.parametrize("graph_steps,bin_mib,bps,chains,ty", [(8, 0, 0, 0, 0), (1, 0, 0, 0, 0), (8, 1, 0, 0, 0),
+                                                               (8, 0, -1, 0, 0), (8, 0, -1, 3, 0), (1, 0, -1, 2, 4),
+                                                               (8, 1, -1, 2, 4), (8, 0, 0, 0, 4)])
+def test_batch_equals_solo_runs(graph_steps, bin_mib, bps, chains, ty):
+    """Persistent and one-block-per-item kernels, 8- and 4-row tiles, one
+    chain per kernel variant or several job-range chains on their own
+    streams (graphs and single steps, with and without L2 bins): every job
+    bit-identical to its solo run."""
     nsteps = 130
     ops = _ops(400)
     cops = [CompressedOperator(op) for op in ops]
@@ -46,7 +46,7 @@ def test_batch_equals_solo_runs(graph_steps, bin_mib, bps, chains):
     for e in solo:
         e.iterate(nsteps)
     jobs = [Engine(c, kernel="tma") for c in cops]
-    b = Batch(jobs, graph_steps=graph_steps, bin_mib=bin_mib, blocks_per_sm=bps, chains=chains)
+    b = Batch(jobs, graph_steps=graph_steps, bin_mib=bin_mib, blocks_per_sm=bps, chains=chains, tile_y=ty)
     st = b.stats()
     assert st["num_jobs"] == len(jobs) and st["num_groups"] >= 3
     assert (st["num_bins"] > 1) == (bin_mib > 0)

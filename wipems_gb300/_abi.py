@@ -99,7 +99,7 @@ class FdtdCopInfo(C.Structure):
 
 class FdtdBatchOpts(C.Structure):
     _fields_ = [("x_chunk", C.c_int), ("stages", C.c_int), ("blocks_per_sm", C.c_int), ("graph_steps", C.c_int),
-                ("bin_mib", C.c_int), ("chains", C.c_int)]
+                ("bin_mib", C.c_int), ("chains", C.c_int), ("tile_y", C.c_int)]
 
 
 class FdtdXmlInfo(C.Structure):

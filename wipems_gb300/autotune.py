@@ -67,38 +67,39 @@ def tune(cop, stages=DEFAULT_STAGES, xchunks=DEFAULT_XCHUNK, steps: int = 30, de
     return best, table
 
 
-def tune_batch(cops, xchunks=(8, 16, 32), graph_steps=(32,), blocks_per_sm=(0, 3, -1), chains=(1, 2, 4),
-               steps: int = 64, device: int = 0, verbose=False):
+def tune_batch(cops, xchunks=(16, 32, 64), graph_steps=(32,), blocks_per_sm=(0, 3, -1), chains=(1, 2, 4),
+               tile_ys=(8, 4), steps: int = 64, device: int = 0, verbose=False):
     """Batched mode: times the batch's kernels over the whole job set for
-    every (x_chunk, graph_steps, blocks_per_sm, chains) combination over
-    `steps` timesteps (fresh engines per candidate, device time from CUDA
-    events); blocks_per_sm caps the resident blocks each SM runs (0 = as
+    every (tile_y, x_chunk, graph_steps, blocks_per_sm, chains) combination
+    over `steps` timesteps (fresh engines per candidate, device time from
+    CUDA events); blocks_per_sm caps the resident blocks each SM runs (0 = as
     many as fit; -1 = no persistent blocks, one block per work item) and
     chains splits each kernel-variant group into job ranges advancing on
-    their own streams -- the jobs-per-SM schedule of the work list.  Chains
-    are tried with the non-persistent kernels only (persistent grids each
-    fill the GPU).  Returns (best, table)."""
+    their own streams -- the tile shape and the jobs-per-SM schedule of the
+    work list.  Chains and 4-row tiles are tried with the non-persistent
+    kernels only (persistent grids each fill the GPU).  Returns (best, table)."""
     from .fdtd import Batch, Engine
     table = []
     for bps in blocks_per_sm:
-        for ch in (chains if bps < 0 else (1,)):
-            for xc in xchunks:
-                for gs in graph_steps:
-                    engines = [Engine(c, device=device, max_timesteps=steps + 4 * gs, kernel="tma") for c in cops]
-                    b = Batch(engines, x_chunk=xc, graph_steps=gs, blocks_per_sm=bps, chains=ch)
-                    b.iterate(gs)  # warm-up, graph instantiation
-                    n = max(gs, steps // gs * gs)
-                    b.iterate(n)
-                    st = b.stats()
-                    ms = st["last_ms"] / n
-                    b.close()
-                    for e in engines:
-                        e.close()
-                    table.append(dict(x_chunk=xc, graph_steps=gs, blocks_per_sm=bps, chains=ch, tile_y=8,
-                                      persistent_blocks=st["persistent_blocks"], ms_per_step=ms))
-                    if verbose:
-                        print(f"blocks_per_sm={bps} chains={ch} x_chunk={xc:3d} graph_steps={gs:3d}  "
-                              f"{ms * 1e3:8.1f} us/step", flush=True)
+        for ty in (tile_ys if bps < 0 else (8,)):
+            for ch in (chains if bps < 0 else (1,)):
+                for xc in xchunks:
+                    for gs in graph_steps:
+                        engines = [Engine(c, device=device, max_timesteps=steps + 4 * gs, kernel="tma") for c in cops]
+                        b = Batch(engines, x_chunk=xc, graph_steps=gs, blocks_per_sm=bps, chains=ch, tile_y=ty)
+                        b.iterate(gs)  # warm-up, graph instantiation
+                        n = max(gs, steps // gs * gs)
+                        b.iterate(n)
+                        st = b.stats()
+                        ms = st["last_ms"] / n
+                        b.close()
+                        for e in engines:
+                            e.close()
+                        table.append(dict(x_chunk=xc, graph_steps=gs, blocks_per_sm=bps, chains=ch, tile_y=ty,
+                                          persistent_blocks=st["persistent_blocks"], ms_per_step=ms))
+                        if verbose:
+                            print(f"blocks_per_sm={bps} tile_y={ty} chains={ch} x_chunk={xc:3d} graph_steps={gs:3d}"
+                                  f"  {ms * 1e3:8.1f} us/step", flush=True)
     best = min(table, key=lambda r: r["ms_per_step"])
     return best, table
 

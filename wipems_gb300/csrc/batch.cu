@@ -74,84 +74,105 @@ struct Group {
     int max_planes = 1;        // largest Nx-1 of its jobs
 };
 
-template <typename IdxT, int FEAT, bool GEO>
+// The batched kernels come in two tile heights (TY rows of 32 z-lanes per
+// block, the same rows in every job's tensor maps): 8 (256 threads) or 4.
+template <typename IdxT, int FEAT, bool GEO, int TY>
 void volt_batch_launch(const Group& G, const BatchJob* jobs, int XC, int S, cudaStream_t st) {
-    k_volt_batch<IdxT, FEAT, GEO><<<G.gridE, dim3(32, BATCH_TY), G.smemE, st>>>(jobs, G.itE.p, G.nE, XC, S);
+    k_volt_batch<IdxT, FEAT, GEO, TY><<<G.gridE, dim3(32, TY), G.smemE, st>>>(jobs, G.itE.p, G.nE, XC, S);
 }
-template <typename IdxT, int FEAT, bool GEO>
+template <typename IdxT, int FEAT, bool GEO, int TY>
 void curr_batch_launch(const Group& G, const BatchJob* jobs, int XC, int S, cudaStream_t st) {
-    k_curr_batch<IdxT, FEAT, GEO><<<G.gridH, dim3(32, BATCH_TY), G.smemH, st>>>(jobs, G.itH.p, G.nH, XC, S);
+    k_curr_batch<IdxT, FEAT, GEO, TY><<<G.gridH, dim3(32, TY), G.smemH, st>>>(jobs, G.itH.p, G.nH, XC, S);
 }
 
-template <typename IdxT, bool GEO>
+template <typename IdxT, bool GEO, int TY>
 void volt_feat(const Group& G, const BatchJob* jobs, int XC, int S, cudaStream_t st) {
     switch (G.feat) {
-        case 0: volt_batch_launch<IdxT, 0, GEO>(G, jobs, XC, S, st); break;
-        case 1: volt_batch_launch<IdxT, 1, GEO>(G, jobs, XC, S, st); break;
-        case 2: volt_batch_launch<IdxT, 2, GEO>(G, jobs, XC, S, st); break;
-        default: volt_batch_launch<IdxT, 3, GEO>(G, jobs, XC, S, st); break;
+        case 0: volt_batch_launch<IdxT, 0, GEO, TY>(G, jobs, XC, S, st); break;
+        case 1: volt_batch_launch<IdxT, 1, GEO, TY>(G, jobs, XC, S, st); break;
+        case 2: volt_batch_launch<IdxT, 2, GEO, TY>(G, jobs, XC, S, st); break;
+        default: volt_batch_launch<IdxT, 3, GEO, TY>(G, jobs, XC, S, st); break;
     }
 }
-template <typename IdxT, bool GEO>
+template <typename IdxT, bool GEO, int TY>
 void curr_feat(const Group& G, const BatchJob* jobs, int XC, int S, cudaStream_t st) {
     switch (G.feat) {
-        case 0: curr_batch_launch<IdxT, 0, GEO>(G, jobs, XC, S, st); break;
-        case 1: curr_batch_launch<IdxT, 1, GEO>(G, jobs, XC, S, st); break;
-        case 2: curr_batch_launch<IdxT, 2, GEO>(G, jobs, XC, S, st); break;
-        default: curr_batch_launch<IdxT, 3, GEO>(G, jobs, XC, S, st); break;
+        case 0: curr_batch_launch<IdxT, 0, GEO, TY>(G, jobs, XC, S, st); break;
+        case 1: curr_batch_launch<IdxT, 1, GEO, TY>(G, jobs, XC, S, st); break;
+        case 2: curr_batch_launch<IdxT, 2, GEO, TY>(G, jobs, XC, S, st); break;
+        default: curr_batch_launch<IdxT, 3, GEO, TY>(G, jobs, XC, S, st); break;
     }
 }
 
-void launch_group_volt(const Group& G, const BatchJob* jobs, int XC, int S, cudaStream_t st) {
+template <int TY>
+void group_volt_ty(const Group& G, const BatchJob* jobs, int XC, int S, cudaStream_t st) {
     if (G.e16) {
-        if (G.geo) volt_feat<uint16_t, true>(G, jobs, XC, S, st);
-        else volt_feat<uint16_t, false>(G, jobs, XC, S, st);
+        if (G.geo) volt_feat<uint16_t, true, TY>(G, jobs, XC, S, st);
+        else volt_feat<uint16_t, false, TY>(G, jobs, XC, S, st);
     } else {
-        if (G.geo) volt_feat<uint32_t, true>(G, jobs, XC, S, st);
-        else volt_feat<uint32_t, false>(G, jobs, XC, S, st);
+        if (G.geo) volt_feat<uint32_t, true, TY>(G, jobs, XC, S, st);
+        else volt_feat<uint32_t, false, TY>(G, jobs, XC, S, st);
     }
 }
-void launch_group_curr(const Group& G, const BatchJob* jobs, int XC, int S, cudaStream_t st) {
+template <int TY>
+void group_curr_ty(const Group& G, const BatchJob* jobs, int XC, int S, cudaStream_t st) {
     if (G.h16) {
-        if (G.geo) curr_feat<uint16_t, true>(G, jobs, XC, S, st);
-        else curr_feat<uint16_t, false>(G, jobs, XC, S, st);
+        if (G.geo) curr_feat<uint16_t, true, TY>(G, jobs, XC, S, st);
+        else curr_feat<uint16_t, false, TY>(G, jobs, XC, S, st);
     } else {
-        if (G.geo) curr_feat<uint32_t, true>(G, jobs, XC, S, st);
-        else curr_feat<uint32_t, false>(G, jobs, XC, S, st);
+        if (G.geo) curr_feat<uint32_t, true, TY>(G, jobs, XC, S, st);
+        else curr_feat<uint32_t, false, TY>(G, jobs, XC, S, st);
     }
+}
+void launch_group_volt(const Group& G, const BatchJob* jobs, int XC, int S, cudaStream_t st, int ty) {
+    if (ty == 4) group_volt_ty<4>(G, jobs, XC, S, st);
+    else group_volt_ty<8>(G, jobs, XC, S, st);
+}
+void launch_group_curr(const Group& G, const BatchJob* jobs, int XC, int S, cudaStream_t st, int ty) {
+    if (ty == 4) group_curr_ty<4>(G, jobs, XC, S, st);
+    else group_curr_ty<8>(G, jobs, XC, S, st);
 }
 
 // occupancy of one batched kernel variant (blocks per SM)
-template <typename IdxT, int FEAT, bool GEO>
+template <typename IdxT, int FEAT, bool GEO, int TY>
 int occ_one(bool volt, size_t smem) {
     int n = 0;
     if (volt)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_volt_batch<IdxT, FEAT, GEO>, 32 * BATCH_TY, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_volt_batch<IdxT, FEAT, GEO, TY>, 32 * TY, smem);
     else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_curr_batch<IdxT, FEAT, GEO>, 32 * BATCH_TY, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_curr_batch<IdxT, FEAT, GEO, TY>, 32 * TY, smem);
     return n;
 }
-template <typename IdxT, bool GEO>
+template <typename IdxT, bool GEO, int TY>
 int occ_feat(int feat, bool volt, size_t smem) {
     switch (feat) {
-        case 0: return occ_one<IdxT, 0, GEO>(volt, smem);
-        case 1: return occ_one<IdxT, 1, GEO>(volt, smem);
-        case 2: return occ_one<IdxT, 2, GEO>(volt, smem);
-        default: return occ_one<IdxT, 3, GEO>(volt, smem);
+        case 0: return occ_one<IdxT, 0, GEO, TY>(volt, smem);
+        case 1: return occ_one<IdxT, 1, GEO, TY>(volt, smem);
+        case 2: return occ_one<IdxT, 2, GEO, TY>(volt, smem);
+        default: return occ_one<IdxT, 3, GEO, TY>(volt, smem);
     }
 }
-int occupancy(const Group& G, bool volt, size_t smem) {
+template <int TY>
+int occupancy_ty(const Group& G, bool volt, size_t smem) {
     const bool i16 = volt ? G.e16 : G.h16;
-    if (i16) return G.geo ? occ_feat<uint16_t, true>(G.feat, volt, smem) : occ_feat<uint16_t, false>(G.feat, volt, smem);
-    return G.geo ? occ_feat<uint32_t, true>(G.feat, volt, smem) : occ_feat<uint32_t, false>(G.feat, volt, smem);
+    if (i16)
+        return G.geo ? occ_feat<uint16_t, true, TY>(G.feat, volt, smem) : occ_feat<uint16_t, false, TY>(G.feat, volt, smem);
+    return G.geo ? occ_feat<uint32_t, true, TY>(G.feat, volt, smem) : occ_feat<uint32_t, false, TY>(G.feat, volt, smem);
+}
+int occupancy(const Group& G, bool volt, size_t smem, int ty) {
+    return ty == 4 ? occupancy_ty<4>(G, volt, smem) : occupancy_ty<8>(G, volt, smem);
 }
 
 template <typename IdxT, int FEAT, bool GEO>
 cudaError_t batch_smem_attr_one(int bytes) {
     const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    cudaError_t r1 = cudaFuncSetAttribute(k_volt_batch<IdxT, FEAT, GEO>, a, bytes);
-    cudaError_t r2 = cudaFuncSetAttribute(k_curr_batch<IdxT, FEAT, GEO>, a, bytes);
-    return r1 != cudaSuccess ? r1 : r2;
+    const cudaError_t r[4] = {cudaFuncSetAttribute(k_volt_batch<IdxT, FEAT, GEO, 8>, a, bytes),
+                              cudaFuncSetAttribute(k_curr_batch<IdxT, FEAT, GEO, 8>, a, bytes),
+                              cudaFuncSetAttribute(k_volt_batch<IdxT, FEAT, GEO, 4>, a, bytes),
+                              cudaFuncSetAttribute(k_curr_batch<IdxT, FEAT, GEO, 4>, a, bytes)};
+    for (cudaError_t x : r)
+        if (x != cudaSuccess) return x;
+    return cudaSuccess;
 }
 
 int batch_smem_attrs(int bytes) {
@@ -194,8 +215,8 @@ int batch_refusal(const fdtd_engine_s* e) {
     return FDTD_OK;
 }
 
-size_t stage_smem(bool i16, bool upml, bool ade, int S) {  // the batched kernels' BATCH_TY-row stages
-    constexpr int T = BATCH_TY;
+template <int T>
+size_t stage_smem_ty(bool i16, bool upml, bool ade, int S) {
     if (ade) {  // voltage kernels of groups with Lorentz/Drude nodes stage their states too
         if (i16)
             return upml ? StageLayout<uint16_t, true, true, T>::smem(S) : StageLayout<uint16_t, false, true, T>::smem(S);
@@ -203,6 +224,9 @@ size_t stage_smem(bool i16, bool upml, bool ade, int S) {  // the batched kernel
     }
     if (i16) return upml ? StageLayout<uint16_t, true, false, T>::smem(S) : StageLayout<uint16_t, false, false, T>::smem(S);
     return upml ? StageLayout<uint32_t, true, false, T>::smem(S) : StageLayout<uint32_t, false, false, T>::smem(S);
+}
+size_t stage_smem(bool i16, bool upml, bool ade, int S, int ty) {  // the batched kernels' stages
+    return ty == 4 ? stage_smem_ty<4>(i16, upml, ade, S) : stage_smem_ty<8>(i16, upml, ade, S);
 }
 
 }  // namespace
@@ -231,6 +255,7 @@ struct fdtd_batch_s {
     uint64_t bin_bytes = 0;
     int XC = 8, stages = 3, blocks_per_sm = 0;
     int chains = 1;                    // chains per kernel-variant group
+    int ty = BATCH_TY;                 // tile rows of the batched kernels (4 or 8)
     std::vector<cudaStream_t> side;    // one stream per chain of a bin
     std::vector<cudaEvent_t> ev_fork, ev_join;
     uint32_t graph_steps = 8;
@@ -261,8 +286,8 @@ namespace {
 // one timestep of chain G (a group's job range) on stream st: its voltage
 // kernel, its current kernel, then the samplers of its jobs
 void chain_step(fdtd_batch_s* b, const Group& G, cudaStream_t st) {
-    launch_group_volt(G, b->d_jobs.p, b->XC, b->stages, st);
-    launch_group_curr(G, b->d_jobs.p, b->XC, b->stages, st);
+    launch_group_volt(G, b->d_jobs.p, b->XC, b->stages, st, b->ty);
+    launch_group_curr(G, b->d_jobs.p, b->XC, b->stages, st, b->ty);
     k_batch_energy_planes<<<dim3((unsigned)G.max_planes, (unsigned)G.count), 256, 0, st>>>(b->d_adv.p + G.first);
     k_batch_advance<<<(unsigned)G.count, 256, 0, st>>>(b->d_adv.p + G.first, kEps0, kMue0);
     b->last_launches += 4;
@@ -291,8 +316,8 @@ int bin_step(fdtd_batch_s* b, size_t k) {
     if (b->chains > 1) return bin_chains(b, k, 1);
     const fdtd_batch_s::Bin& B = b->bins[k];
     const size_t ng = B.groups.size();
-    for (int gi : B.groups) launch_group_volt(b->groups[gi], b->d_jobs.p, b->XC, b->stages, b->stream);
-    for (int gi : B.groups) launch_group_curr(b->groups[gi], b->d_jobs.p, b->XC, b->stages, b->stream);
+    for (int gi : B.groups) launch_group_volt(b->groups[gi], b->d_jobs.p, b->XC, b->stages, b->stream, b->ty);
+    for (int gi : B.groups) launch_group_curr(b->groups[gi], b->d_jobs.p, b->XC, b->stages, b->stream, b->ty);
     k_batch_energy_planes<<<dim3((unsigned)B.max_planes, (unsigned)B.count), 256, 0, b->stream>>>(b->d_adv.p + B.first);
     k_batch_advance<<<(unsigned)B.count, 256, 0, b->stream>>>(b->d_adv.p + B.first, kEps0, kMue0);
     b->last_launches += 2 * ng + 2;
@@ -349,6 +374,11 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
     b->graph_steps = (o && o->graph_steps > 0) ? (uint32_t)o->graph_steps : 8;
     b->bin_bytes = (o && o->bin_mib > 0) ? (uint64_t)o->bin_mib << 20 : 0;
     b->chains = (o && o->chains > 1) ? std::min(o->chains, 64) : 1;
+    b->ty = (o && o->tile_y == 4) ? 4 : BATCH_TY;
+    if (o && o->tile_y != 0 && o->tile_y != 4 && o->tile_y != 8) {
+        set_error("fdtd_batch_create: tile_y must be 4 or 8 (0 = 8)");
+        return FDTD_ERR_ARG;
+    }
     if (b->stages < 3 || b->stages > TMA_MAX_STAGES) {
         set_error("fdtd_batch_create: stages must be 3..8");
         return FDTD_ERR_ARG;
@@ -467,9 +497,9 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
         CK(cudaEventCreateWithFlags(&b->ev_fork[0], cudaEventDisableTiming));
     }
     // descriptors
-    std::vector<TmaMaps> hmaps(n);  // the jobs' tensor maps for the batch's BATCH_TY-row tiles
+    std::vector<TmaMaps> hmaps(n);  // the jobs' tensor maps for the batch's ty-row tiles
     for (uint32_t j = 0; j < n; ++j)
-        if ((rc = engine_tma_maps(b->jobs[j], &hmaps[j], BATCH_TY))) return rc;
+        if ((rc = engine_tma_maps(b->jobs[j], &hmaps[j], (uint32_t)b->ty))) return rc;
     if ((rc = b->d_maps.alloc(n, b->device_bytes)) || (rc = b->d_jobs.alloc(n, b->device_bytes)) ||
         (rc = b->d_adv.alloc(n, b->device_bytes)) || (rc = b->d_status.alloc(4 * (size_t)n, b->device_bytes)))
         return rc;
@@ -504,20 +534,20 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
     if (b->XC == 0) {
         std::vector<const uint32_t*> lines;
         for (const fdtd_engine_s* e : b->jobs) lines.push_back(e->N);
-        b->XC = auto_x_chunk(lines, (uint64_t)WIPEMS_BATCH_MIN_BLOCKS * (uint64_t)sms, BATCH_TY);
+        b->XC = auto_x_chunk(lines, (uint64_t)(1024 / (32 * b->ty)) * (uint64_t)sms, b->ty);
     }
-    const size_t maxsm = stage_smem(false, true, true, b->stages);
+    const size_t maxsm = std::max(stage_smem(false, true, true, b->stages, 8), stage_smem(false, true, true, b->stages, 4));
     if (maxsm > 48 * 1024 && (rc = batch_smem_attrs((int)maxsm))) return rc;
     for (Group& G : b->groups) {
         std::vector<WorkItem> wE, wH;
         for (int j : G.jobs) {
             const fdtd_engine_s* e = b->jobs[j];
-            const int bxE = (e->ti.ne[2] + 31) / 32, byE = (e->ti.ne[1] + BATCH_TY - 1) / BATCH_TY,
+            const int bxE = (e->ti.ne[2] + 31) / 32, byE = (e->ti.ne[1] + b->ty - 1) / b->ty,
                       bzE = (e->ti.ne[0] + b->XC - 1) / b->XC;
             for (int z = 0; z < bzE; ++z)
                 for (int y = 0; y < byE; ++y)
                     for (int x = 0; x < bxE; ++x) wE.push_back(WorkItem{j, x, y, z});
-            const int bxH = ((int)e->N[2] - 1 + 31) / 32, byH = ((int)e->N[1] - 1 + BATCH_TY - 1) / BATCH_TY,
+            const int bxH = ((int)e->N[2] - 1 + 31) / 32, byH = ((int)e->N[1] - 1 + b->ty - 1) / b->ty,
                       bzH = ((int)e->N[0] - 1 + b->XC - 1) / b->XC;
             for (int z = 0; z < bzH; ++z)
                 for (int y = 0; y < byH; ++y)
@@ -529,9 +559,9 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
         CK(cudaMemcpyAsync(G.itE.p, wE.data(), wE.size() * sizeof(WorkItem), cudaMemcpyHostToDevice, b->stream));
         CK(cudaMemcpyAsync(G.itH.p, wH.data(), wH.size() * sizeof(WorkItem), cudaMemcpyHostToDevice, b->stream));
         const bool up = (G.feat & FEAT_UPML) != 0;
-        G.smemE = stage_smem(G.e16, up, (G.feat & FEAT_ADE) != 0, b->stages);
-        G.smemH = stage_smem(G.h16, up, false, b->stages);
-        int oE = occupancy(G, true, G.smemE), oH = occupancy(G, false, G.smemH);
+        G.smemE = stage_smem(G.e16, up, (G.feat & FEAT_ADE) != 0, b->stages, b->ty);
+        G.smemH = stage_smem(G.h16, up, false, b->stages, b->ty);
+        int oE = occupancy(G, true, G.smemE, b->ty), oH = occupancy(G, false, G.smemH, b->ty);
         if (b->blocks_per_sm > 0) {
             oE = std::min(oE, b->blocks_per_sm);
             oH = std::min(oH, b->blocks_per_sm);

@@ -43,15 +43,11 @@ constexpr int TMA_MAX_STAGES = 8;
 // Batches: 32 x 8 -- a persistent block pays a ring prologue per work item,
 // and with half-size items the B96 batch fell from 44.7 to 33.8 G.
 constexpr int TMA_TY = 4;
-constexpr int BATCH_TY = 8;
-
-// minimum resident blocks per SM the batched kernels are compiled for:
-// 1024 threads per SM, which caps their registers at 64 (the per-job
-// descriptor fields they read from global memory cost registers that the
-// single-job kernels take from constant memory)
-#ifndef WIPEMS_BATCH_MIN_BLOCKS
-#define WIPEMS_BATCH_MIN_BLOCKS (1024 / (32 * BATCH_TY))
-#endif
+constexpr int BATCH_TY = 8;  // default tile rows of the batched kernels (4 is the other choice)
+// The batched kernels are compiled for 1024 resident threads per SM
+// (__launch_bounds__(TY * 32, 1024 / (32 * TY))), which caps their registers
+// at 64: the per-job descriptor fields they read from global memory cost
+// registers that the single-job kernels take from constant memory.
 constexpr unsigned long long TMA_WAIT_CYCLES = 4000000000ull;  // ~2 s at 2 GHz
 
 struct TmaMaps {
@@ -500,11 +496,11 @@ struct WorkItem {
 // Persistent voltage half-step over the work items of many jobs: block b
 // takes items b, b + gridDim.x, ...  Every job's numTS is read from its own
 // counter, so jobs need not be in step.
-template <typename IdxT, int FEAT, bool GEO>
-__global__ void __launch_bounds__(BATCH_TY * 32, WIPEMS_BATCH_MIN_BLOCKS) k_volt_batch(const BatchJob* __restrict__ jobs,
+template <typename IdxT, int FEAT, bool GEO, int TY = BATCH_TY>
+__global__ void __launch_bounds__(TY * 32, 1024 / (32 * TY)) k_volt_batch(const BatchJob* __restrict__ jobs,
                                                             const WorkItem* __restrict__ items, int nitems, int XC,
                                                             int STAGES) {
-    using L = StageLayout<IdxT, (FEAT & FEAT_UPML) != 0, (FEAT & FEAT_ADE) != 0, BATCH_TY>;
+    using L = StageLayout<IdxT, (FEAT & FEAT_UPML) != 0, (FEAT & FEAT_ADE) != 0, TY>;
     extern __shared__ __align__(128) float smem_raw[];
     float* smem = aligned_smem(smem_raw);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * STAGES);
@@ -519,17 +515,17 @@ __global__ void __launch_bounds__(BATCH_TY * 32, WIPEMS_BATCH_MIN_BLOCKS) k_volt
             if (threadIdx.x == 0 && threadIdx.y == 0) tensormap_acquire(J.maps);
             last_job = w.job;
         }
-        if (!volt_tile<IdxT, FEAT, GEO, BATCH_TY>(J.g, *J.maps, J.ti, w.bx, w.by, w.bz, XC, STAGES, smem, bars, ring,
+        if (!volt_tile<IdxT, FEAT, GEO, TY>(J.g, *J.maps, J.ti, w.bx, w.by, w.bz, XC, STAGES, smem, bars, ring,
                                         *J.g.d_ts))
             break;
     }
 }
 
-template <typename IdxT, int FEAT, bool GEO>
-__global__ void __launch_bounds__(BATCH_TY * 32, WIPEMS_BATCH_MIN_BLOCKS) k_curr_batch(const BatchJob* __restrict__ jobs,
+template <typename IdxT, int FEAT, bool GEO, int TY = BATCH_TY>
+__global__ void __launch_bounds__(TY * 32, 1024 / (32 * TY)) k_curr_batch(const BatchJob* __restrict__ jobs,
                                                             const WorkItem* __restrict__ items, int nitems, int XC,
                                                             int STAGES) {
-    using L = StageLayout<IdxT, (FEAT & FEAT_UPML) != 0, false, BATCH_TY>;
+    using L = StageLayout<IdxT, (FEAT & FEAT_UPML) != 0, false, TY>;
     extern __shared__ __align__(128) float smem_raw[];
     float* smem = aligned_smem(smem_raw);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)L::STAGE * STAGES);
@@ -547,7 +543,7 @@ __global__ void __launch_bounds__(BATCH_TY * 32, WIPEMS_BATCH_MIN_BLOCKS) k_curr
         // energy on the job's sample steps (the sample after this step)
         const int numTS = *J.g.d_ts;
         const bool energy = J.interval > 0 && J.energy && ((numTS + 1) % J.interval) == 0;
-        const bool ok = curr_tile<IdxT, FEAT, GEO, BATCH_TY>(J.g, *J.maps, J.ti, w.bx, w.by, w.bz, XC, STAGES, smem, bars,
+        const bool ok = curr_tile<IdxT, FEAT, GEO, TY>(J.g, *J.maps, J.ti, w.bx, w.by, w.bz, XC, STAGES, smem, bars,
                                                    ring, numTS, energy);
         if (!ok) break;
     }

@@ -737,11 +737,11 @@ class Batch:
     engines must outlive the batch."""
 
     def __init__(self, engines, x_chunk: int = 0, stages: int = 0, blocks_per_sm: int = 0, graph_steps: int = 0,
-                 bin_mib: int = 0, chains: int = 0):
+                 bin_mib: int = 0, chains: int = 0, tile_y: int = 0):
         self.engines = list(engines)
         arr = (C.c_void_p * len(self.engines))(*[e._h.value for e in self.engines])
         o = _abi.FdtdBatchOpts(int(x_chunk), int(stages), int(blocks_per_sm), int(graph_steps), int(bin_mib),
-                               int(chains))
+                               int(chains), int(tile_y))
         h = C.c_void_p()
         check(lib().fdtd_batch_create(arr, len(self.engines), C.byref(o), C.byref(h)), "fdtd_batch_create")
         self._h = h

@@ -115,7 +115,7 @@ def b96(n_jobs: int = 96, timesteps: int = 1500, device: int = 0) -> dict:
     best, table = autotune.tune_batch(cops, device=device)
     engines = [Engine(c, device=device, max_timesteps=timesteps, kernel="tma") for c in cops]
     b = Batch(engines, x_chunk=best["x_chunk"], graph_steps=best["graph_steps"], blocks_per_sm=best["blocks_per_sm"],
-              chains=best.get("chains", 1))
+              chains=best.get("chains", 1), tile_y=best.get("tile_y", 8))
     b.iterate(timesteps)
     st = b.stats()
     b.close()
