@@ -2,6 +2,7 @@
 external profiler (ncu) can capture the half-step kernels.
 
     python -m wipems_gb300.profile --workload l256|p64|d192|l160|b96|l256mur --steps 8 [--graphs]
+        [--tile-y 4|8] [--x-chunk N] [--blocks-per-sm B --chains C (b96)]
 
 Kernels are launched individually (no CUDA graph) unless --graphs is given,
 so a launch list shows every E / H kernel separately.
@@ -20,13 +21,16 @@ def main():
     ap.add_argument("--graphs", action="store_true")
     ap.add_argument("--tile-y", type=int, default=0)
     ap.add_argument("--x-chunk", type=int, default=0)
+    ap.add_argument("--blocks-per-sm", type=int, default=0, help="b96: batch schedule (-1 = one block per item)")
+    ap.add_argument("--chains", type=int, default=0, help="b96: job-range chains per kernel variant")
     args = ap.parse_args()
     from . import Batch, CompressedOperator, Engine, Operator, scenes
     if args.workload == "b96":  # batched mode, one step per launch sequence (no graph)
         t0 = time.perf_counter()
         cops = [CompressedOperator(Operator(scenes.b96_job(s))) for s in range(args.jobs)]
         engines = [Engine(c, kernel="tma") for c in cops]
-        b = Batch(engines, x_chunk=args.x_chunk, graph_steps=1)
+        b = Batch(engines, x_chunk=args.x_chunk, graph_steps=1, blocks_per_sm=args.blocks_per_sm, chains=args.chains,
+                  tile_y=args.tile_y)
         t1 = time.perf_counter()
         b.iterate(args.steps)
         st = b.stats()
