@@ -414,9 +414,7 @@ int make_tma_maps(const fdtd_engine_s* e, TmaMaps* m, uint32_t rows) {
         (rc = index_map(&m->idxH, e->H.idx.p, e, e->H.idx16, 32, rows)))
         return rc;
     if (e->FV.p && ((rc = field_map(&m->FV_own, e->FV.p, e, 32, rows)) ||
-                    (rc = field_map(&m->FI_own, e->FI.p, e, 32, rows)) ||
-                    (rc = field_map(&m->FV_own8, e->FV.p, e, 8, rows)) ||
-                    (rc = field_map(&m->FI_own8, e->FI.p, e, 8, rows))))
+                    (rc = field_map(&m->FI_own, e->FI.p, e, 32, rows))))
         return rc;
     if (e->AV.p && (rc = field_map(&m->AV_own, e->AV.p, e, 32, rows))) return rc;
     if (e->LV.p && (rc = field_map(&m->LV_own, e->LV.p, e, 32, rows))) return rc;

@@ -52,7 +52,6 @@ constexpr unsigned long long TMA_WAIT_CYCLES = 4000000000ull;  // ~2 s at 2 GHz
 
 struct TmaMaps {
     CUtensorMap I_halo, I_own, V_halo, V_own, FV_own, FI_own, idxE, idxH, AV_own, LV_own;
-    CUtensorMap FV_own8, FI_own8;  // UPML flux in 8-lane boxes (tiles that only graze a z face of the shell)
 };
 
 // geometry of the UPML slabs: a node is in a slab iff one coordinate is
@@ -156,24 +155,6 @@ __device__ __forceinline__ bool tile_has_upml(const TileInfo& ti, int x, int y0,
     return false;
 }
 
-// The UPML flux a tile plane stages: 0 = none; 1 = the whole 32-lane box;
-// 2 = one 8-lane box at lane w0 (a multiple of 8), when the plane is inside
-// the shell in x and y and its UPML nodes -- those below the inner box on
-// z, or above it -- all lie in that window (an 8-cell z face grazed by the
-// first or the last z tile).  The lanes outside the window have no UPML
-// node, so they never read the staged flux.
-__device__ __forceinline__ int flux_window(const TileInfo& ti, int x, int y0, int y1, int z0, int z1, int& w0) {
-    w0 = z0;
-    if (x < ti.lo[0] || x > ti.hi[0] || y0 < ti.lo[1] || y1 > ti.hi[1]) return 1;
-    const bool below = z0 < ti.lo[2], above = z1 > ti.hi[2];
-    if (!below && !above) return 0;
-    if (below && above) return 1;
-    const int a = below ? z0 : ti.hi[2] + 1;  // first UPML lane
-    const int b = below ? ti.lo[2] - 1 : z1;  // last UPML lane
-    w0 = a & ~7;
-    return (b < w0 + 8) ? 2 : 1;
-}
-
 // ------------------------------------------------------------- E half-step
 // One tile of the voltage update: the 32 x TY tile (bx, by) over the
 // x-chunk bz.  ring counts the planes this block has pushed through its
@@ -220,18 +201,15 @@ __device__ __forceinline__ bool volt_tile(const DevGrid& g, const TmaMaps& m, co
         const int s = (int)(q % (uint32_t)STAGES);
         const int x = x0 + r;
         float* st = smem + (size_t)s * L::STAGE;
-        int w0;
-        const int fw = UPML ? flux_window(ti, x, y0, yl, z0, zl, w0) : 0;
+        const bool up = UPML && tile_has_upml(ti, x, y0, yl, z0, zl);
         const uint32_t af = ADE ? ade_tile_flags<TY>(g, x, bx, by) : 0u;
-        const uint32_t bytes = L::HALO_BYTES + L::OWN_BYTES + L::IDX_BYTES +
-                               (fw == 1 ? L::OWN_BYTES : fw == 2 ? L::OWN_BYTES / 4 : 0) +
+        const uint32_t bytes = L::HALO_BYTES + L::OWN_BYTES + L::IDX_BYTES + (up ? L::OWN_BYTES : 0) +
                                ((af & 1u) ? L::OWN_BYTES : 0) + ((af & 2u) ? L::OWN_BYTES : 0);
         mbar_expect_tx(&bars[s], bytes);
         tma_4d(st, &m.I_halo, &bars[s], z0 - 4, y0 - 1, x, 0);
         tma_4d(st + L::HALO_A, &m.V_own, &bars[s], z0, y0, x, 0);
         tma_3d(st + L::HALO_A + L::OWN, &m.idxE, &bars[s], z0, y0, x);
-        if (fw == 1) tma_4d(st + L::OFF_FLUX, &m.FV_own, &bars[s], z0, y0, x, 0);
-        if (fw == 2) tma_4d(st + L::OFF_FLUX, &m.FV_own8, &bars[s], w0, y0, x, 0);
+        if (up) tma_4d(st + L::OFF_FLUX, &m.FV_own, &bars[s], z0, y0, x, 0);
         if (af & 1u) tma_4d(st + L::OFF_ADE, &m.AV_own, &bars[s], z0, y0, x, 0);
         if (af & 2u) tma_4d(st + L::OFF_ADE + L::OWN, &m.LV_own, &bars[s], z0, y0, x, 0);
     };
@@ -293,12 +271,8 @@ __device__ __forceinline__ bool volt_tile(const DevGrid& g, const TmaMaps& m, co
             const int oi = ty * 32 + tz;
             const float* sV = st + L::HALO_A;
             const uint32_t t = (uint32_t)reinterpret_cast<const IdxT*>(st + L::HALO_A + L::OWN)[oi];
-            int w0;
-            const int fw = UPML ? flux_window(ti, x, y0, yl, z0, zl, w0) : 0;
-            // the staged flux: [3][TY][32] from the whole box, [3][TY][8] from a window
-            const float* sF = fw == 1 ? st + L::OFF_FLUX + oi
-                            : fw == 2 ? st + L::OFF_FLUX + ty * 8 + min(max(z - w0, 0), 7) : nullptr;
-            const int fs = fw == 2 ? TY * 8 : TY * 32;
+            const bool up = UPML && tile_has_upml(ti, x, y0, yl, z0, zl);
+            const float* sF = up ? st + L::OFF_FLUX + oi : nullptr;
             const uint32_t af = ADE ? ade_tile_flags<TY>(g, x, bx, by) : 0u;
             const float* sA = (af & 1u) ? st + L::OFF_ADE + oi : nullptr;
             const float* sL = (af & 2u) ? st + L::OFF_ADE + L::OWN + oi : nullptr;
@@ -310,8 +284,8 @@ __device__ __forceinline__ bool volt_tile(const DevGrid& g, const TmaMaps& m, co
                 gf.f[1][0] = gyE; gf.f[1][1] = gzI; gf.f[1][2] = gxI;
                 gf.f[2][0] = gzE; gf.f[2][1] = gxI; gf.f[2][2] = gyI;
             }
-            update_node<false, FEAT, GEO>(g, v, curl, t, (long long)x * g.sx + yz, numTS, sF, fs, gf,
-                                          nullptr, true, sA, sL, TY * 32);
+            update_node<false, FEAT, GEO>(g, v, curl, t, (long long)x * g.sx + yz, numTS, sF, TY * 32, gf,
+                                          nullptr, true, sA, sL);
             Vp[0] = v[0];
             Vp[C] = v[1];
             Vp[2 * C] = v[2];
@@ -364,18 +338,16 @@ __device__ __forceinline__ bool curr_tile(const DevGrid& g, const TmaMaps& m, co
         const int x = x0 + r;
         float* st = smem + (size_t)s * L::STAGE;
         const bool upd = r < nplanes;  // plane x1 only contributes V
-        int w0;
-        const int fw = (UPML && upd) ? flux_window(ti, x, y0, yl, z0, zl, w0) : 0;
-        const uint32_t bytes = L::HALO_BYTES + (upd ? L::OWN_BYTES + L::IDX_BYTES : 0) +
-                               (fw == 1 ? L::OWN_BYTES : fw == 2 ? L::OWN_BYTES / 4 : 0);
+        const bool up = UPML && upd && tile_has_upml(ti, x, y0, yl, z0, zl);
+        const uint32_t bytes =
+            L::HALO_BYTES + (upd ? L::OWN_BYTES + L::IDX_BYTES : 0) + (up ? L::OWN_BYTES : 0);
         mbar_expect_tx(&bars[s], bytes);
         tma_4d(st, &m.V_halo, &bars[s], z0, y0, x, 0);
         if (upd) {
             tma_4d(st + L::HALO_A, &m.I_own, &bars[s], z0, y0, x, 0);
             tma_3d(st + L::HALO_A + L::OWN, &m.idxH, &bars[s], z0, y0, x);
         }
-        if (fw == 1) tma_4d(st + L::OFF_FLUX, &m.FI_own, &bars[s], z0, y0, x, 0);
-        if (fw == 2) tma_4d(st + L::OFF_FLUX, &m.FI_own8, &bars[s], w0, y0, x, 0);
+        if (up) tma_4d(st + L::OFF_FLUX, &m.FI_own, &bars[s], z0, y0, x, 0);
     };
 
     int issued = 0;
@@ -425,11 +397,8 @@ __device__ __forceinline__ bool curr_tile(const DevGrid& g, const TmaMaps& m, co
             const int oi = ty * 32 + tz;
             const float* sI = st + L::HALO_A;
             const uint32_t t = (uint32_t)reinterpret_cast<const IdxT*>(st + L::HALO_A + L::OWN)[oi];
-            int w0;
-            const int fw = UPML ? flux_window(ti, x, y0, yl, z0, zl, w0) : 0;
-            const float* sF = fw == 1 ? st + L::OFF_FLUX + oi
-                            : fw == 2 ? st + L::OFF_FLUX + ty * 8 + min(max(z - w0, 0), 7) : nullptr;
-            const int fs = fw == 2 ? TY * 8 : TY * 32;
+            const bool up = UPML && tile_has_upml(ti, x, y0, yl, z0, zl);
+            const float* sF = up ? st + L::OFF_FLUX + oi : nullptr;
             float cu[3] = {sI[oi], sI[TY * 32 + oi], sI[2 * TY * 32 + oi]};
             GeoF gf;
             if (GEO) {
@@ -439,7 +408,7 @@ __device__ __forceinline__ bool curr_tile(const DevGrid& g, const TmaMaps& m, co
                 gf.f[1][0] = gyE; gf.f[1][1] = gzI; gf.f[1][2] = gxI;
                 gf.f[2][0] = gzE; gf.f[2][1] = gxI; gf.f[2][2] = gyI;
             }
-            update_node<true, FEAT, GEO>(g, cu, curl, t, (long long)x * g.sx + yz, numTS, sF, fs, gf);
+            update_node<true, FEAT, GEO>(g, cu, curl, t, (long long)x * g.sx + yz, numTS, sF, TY * 32, gf);
             Ip[0] = cu[0];
             Ip[C] = cu[1];
             Ip[2 * C] = cu[2];

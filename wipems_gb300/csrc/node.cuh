@@ -156,9 +156,7 @@ template <bool H, int FEAT, bool GEO>
 __device__ __forceinline__ void update_node(const DevGrid& g, float fld[3], const float curl[3], uint32_t t,
                                             long long o, int numTS, const float* fsrc, int fstride,
                                             const GeoF& gf, float* fout = nullptr, bool fwrite = true,
-                                            const float* asrc = nullptr, const float* lsrc = nullptr,
-                                            int astride = 0) {
-    if (astride == 0) astride = fstride;  // the staged ADE states' component stride
+                                            const float* asrc = nullptr, const float* lsrc = nullptr) {
     const DevHalf& T = H ? g.h : g.e;
     const float4 ta = __ldg(&T.main[TAB_MAIN * t]);
     const float4 tb = __ldg(&T.main[TAB_MAIN * t + 1]);
@@ -194,8 +192,8 @@ __device__ __forceinline__ void update_node(const DevGrid& g, float fld[3], cons
         if (flags & TF_LOR) {
 #pragma unroll
             for (int n = 0; n < 3; ++n) {
-                float lor = lsrc ? lsrc[n * astride] : Lr[n * C + o];
-                float a = asrc ? asrc[n * astride] : A[n * C + o];
+                float lor = lsrc ? lsrc[n * fstride] : Lr[n * C + o];
+                float a = asrc ? asrc[n * fstride] : A[n * C + o];
                 lor = __fadd_rn(lor, __fmul_rn(klor[n], a));
                 a = __fmul_rn(a, kint[n]);
                 a = __fadd_rn(a, __fmul_rn(kext[n], __fsub_rn(fld[n], lor)));
@@ -206,7 +204,7 @@ __device__ __forceinline__ void update_node(const DevGrid& g, float fld[3], cons
         } else {
 #pragma unroll
             for (int n = 0; n < 3; ++n) {
-                float a = asrc ? asrc[n * astride] : A[n * C + o];
+                float a = asrc ? asrc[n * fstride] : A[n * C + o];
                 a = __fmul_rn(a, kint[n]);
                 a = __fadd_rn(a, __fmul_rn(kext[n], fld[n]));
                 A[n * C + o] = a;
