@@ -120,6 +120,28 @@ def test_excitation_signal_operators_identical(kind, etype, f):
         assert O.nyquist == 1 and O.probe_interval == 1
 
 
+def test_voltage_probes_need_a_line():
+    """A voltage probe box that is a point or spans more than one axis is
+    skipped, with no sample column (openems.cpp:481-486); current and field
+    probes on a point are kept (disabled where the reference disables them).
+    Product and oracle agree, and the scene's probe names follow the kept
+    probes."""
+    from wipems_gb300 import Scene
+    lines = [np.arange(4, dtype=np.float64)] * 3
+    s = Scene(*lines, 1e-3)
+    s.set_boundary([0] * 6, [0] * 6)
+    s.set_gauss_excite(5e9, 5e9, 100)
+    s.add_probe([1, 1, 1], [1, 1, 1], 0, name="point")
+    s.add_probe([1, 1, 1], [1, 1, 1], 1, name="i_point")
+    s.add_probe([0, 0, 0], [2, 2, 0], 0, name="diagonal")
+    s.add_probe([0, 1, 1], [3, 1, 1], 0, name="line")
+    s.add_probe([1, 2, 1], [1, 2, 1], 2, name="e_point")
+    P, O = both(s)
+    assert oracle.probe_tuples(P.probes) == oracle.probe_tuples(O.probes)
+    assert [p.type for p in P.probes] == [1, 0, 2]
+    assert [p["name"] for p in s.probes] == ["i_point", "line", "e_point"]
+
+
 def test_comparison_sees_a_planted_mistake():
     """The comparison is not vacuous: the oracle built from a scene whose one
     brick has eps_r raised by 1e-6 (a few float ulps), or whose UPML is one line thinner on one

@@ -1520,6 +1520,11 @@ static int build_operator(const fdtd_scene_s& S, int threads, fdtd_operator_s& o
                 so[n] = si[n];
             }
         } else if (p.probe_type == 0) {
+            // a voltage probe needs a box of dimension 1 (a line); any other
+            // box is skipped with an error message (openems.cpp:481-486)
+            int dimension = 0;
+            for (int n = 0; n < 3; ++n) dimension += p.start[n] != p.stop[n];
+            if (dimension != 1) continue;
             // ProcessVoltage::DefineStartStopCoord: SnapToMesh on the main mesh
             g.snap_mesh(p.start, d.start, false, si);
             g.snap_mesh(p.stop, d.stop, false, so);

@@ -153,7 +153,13 @@ class SceneSpec:
                    eps_pole_f=fam[2], mue_plasma_f=fam[3], mue_relax_t=fam[4], mue_pole_f=fam[5])
 
     def add_probe(self, start, stop, ptype: int, weight=1.0, norm_dir=-1, name=""):
+        """A voltage (0), current (1), E-field (2) or H-field (3) probe box.
+        A voltage probe needs a line (one coordinate differing between start
+        and stop); the operator skips any other voltage box, as openEMS does
+        (openems.cpp:481-486), so it gets no sample column."""
         self._prim("probe", 0, start, stop, probe_type=int(ptype), weight=float(weight), norm_dir=int(norm_dir))
+        if int(ptype) == 0 and sum(float(a) != float(b) for a, b in zip(start, stop)) != 1:
+            return
         self.probes.append(dict(name=name or f"probe{len(self.probes)}", type=ptype))
 
     def add_lumped_port(self, start, stop, direction, R, excite=1.0, priority=5, name="port"):
