@@ -95,10 +95,12 @@ def test_server_rejects_oversized_job_and_keeps_serving():
 
 def test_batch_mode_runs_unbatchable_jobs_beside_the_batch():
     """With batch rounds on, jobs the persistent batch cannot take (Mur
-    faces, lumped RLC edges) run as concurrent engines next to it; every job
-    still gets its solo result."""
+    faces, lumped RLC edges, dispersion of order > 1) run as concurrent
+    engines next to it, and magnetic Lorentz/Drude jobs join the batch;
+    every job still gets its solo result."""
     srv = Server(round_steps=40, build_workers=2, batch_min_jobs=2)
-    kinds = [("upml", 3), ("mur", 3), ("pec", 4), ("rlc", 3), ("drude", 4), ("rlc_mur", 5)]
+    kinds = [("upml", 3), ("mur", 3), ("pec", 4), ("rlc", 3), ("drude", 4), ("rlc_mur", 5), ("multipole", 3),
+             ("magnetic", 4)]
     ids = {(k, s): srv.submit(scenes.mini(k, seed=s, nr_ts=NR_TS), end_crit=CRIT, keep_fields=True)
            for k, s in kinds}
     srv.wait(0, timeout=600)
