@@ -225,3 +225,30 @@ def test_operator_independent_of_build_threads(make):
     ref = _operator_bytes(Operator(make(), threads=1))
     for th in (3, 8):
         assert _operator_bytes(Operator(make(), threads=th)) == ref
+
+
+def test_device_axes_rotation_choice_and_expansion():
+    """fdtd_compress_rot: the automatic rotation puts the axis that pads
+    least to 32-lane z tiles on z (a cube stays as it is; a 36-line z
+    extent next to a 208-line x extent moves), and the tables expanded back
+    to the operator's axes are the same arrays whatever the rotation."""
+    from wipems_gb300 import CompressedOperator, Scene
+    def grid(nx, ny, nz):
+        s = Scene(*[np.arange(n, dtype=np.float64) for n in (nx, ny, nz)], 1e-3)
+        s.set_boundary([0] * 6, [0] * 6)
+        s.set_gauss_excite(5e9, 5e9, 50)
+        return Operator(s)
+    assert CompressedOperator(grid(40, 40, 40)).rotation == 0
+    c = CompressedOperator(grid(208, 148, 36))
+    assert c.rotation == 1 and c.info["device_lines"] == [148, 36, 208]
+    assert CompressedOperator(grid(21, 4, 1001)).rotation == 0
+    op = Operator(scenes.mini("rlc_mur"))
+    ref = CompressedOperator(op, rotation=0)
+    e0, x0 = ref.expand(), [ref.expand_ext(h) for h in (0, 1)]
+    for r in (1, 2):
+        c = CompressedOperator(op, rotation=r)
+        n = op.num_lines
+        assert c.info["device_lines"] == [n[r % 3], n[(1 + r) % 3], n[(2 + r) % 3]]
+        assert all(np.array_equal(a, b) for a, b in zip(e0, c.expand()))
+        assert all(np.array_equal(x0[h][k], c.expand_ext(h)[k]) for h in (0, 1) for k in (0, 1))
+        assert c.info["num_tuples_e"] == ref.info["num_tuples_e"]

@@ -65,7 +65,8 @@ __global__ void __launch_bounds__(256) k_batch_energy_planes(const AdvJob* __res
 struct Group {
     int bin = 0;
     bool e16 = true, h16 = true, geo = false;
-    int feat = 0;
+    int feat = 0;    // the voltage kernel's feature set
+    int feat_h = 0;  // the current kernel's
     std::vector<int> jobs;
     DevBuf<WorkItem> itE, itH;
     int nE = 0, nH = 0, gridE = 0, gridH = 0;
@@ -96,7 +97,7 @@ void volt_feat(const Group& G, const BatchJob* jobs, int XC, int S, cudaStream_t
 }
 template <typename IdxT, bool GEO, int TY>
 void curr_feat(const Group& G, const BatchJob* jobs, int XC, int S, cudaStream_t st) {
-    switch (G.feat) {
+    switch (G.feat_h) {
         case 0: curr_batch_launch<IdxT, 0, GEO, TY>(G, jobs, XC, S, st); break;
         case 1: curr_batch_launch<IdxT, 1, GEO, TY>(G, jobs, XC, S, st); break;
         case 2: curr_batch_launch<IdxT, 2, GEO, TY>(G, jobs, XC, S, st); break;
@@ -156,8 +157,10 @@ template <int TY>
 int occupancy_ty(const Group& G, bool volt, size_t smem) {
     const bool i16 = volt ? G.e16 : G.h16;
     if (i16)
-        return G.geo ? occ_feat<uint16_t, true, TY>(G.feat, volt, smem) : occ_feat<uint16_t, false, TY>(G.feat, volt, smem);
-    return G.geo ? occ_feat<uint32_t, true, TY>(G.feat, volt, smem) : occ_feat<uint32_t, false, TY>(G.feat, volt, smem);
+        return G.geo ? occ_feat<uint16_t, true, TY>(volt ? G.feat : G.feat_h, volt, smem)
+                     : occ_feat<uint16_t, false, TY>(volt ? G.feat : G.feat_h, volt, smem);
+    return G.geo ? occ_feat<uint32_t, true, TY>(volt ? G.feat : G.feat_h, volt, smem)
+                 : occ_feat<uint32_t, false, TY>(volt ? G.feat : G.feat_h, volt, smem);
 }
 int occupancy(const Group& G, bool volt, size_t smem, int ty) {
     return ty == 4 ? occupancy_ty<4>(G, volt, smem) : occupancy_ty<8>(G, volt, smem);
@@ -441,7 +444,7 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
         B.first = (int)b->jobs.size();
         B.count = (int)binned[bi].size();
         auto key_of = [](const fdtd_engine_s* e) {
-            return std::make_tuple((int)e->E.idx16, (int)e->H.idx16, (int)e->geo_on, e->feat);
+            return std::make_tuple((int)e->E.idx16, (int)e->H.idx16, (int)e->geo_on, e->feat_e * 8 + e->feat_h);
         };
         std::vector<fdtd_engine_s*> jobs = binned[bi];
         std::stable_sort(jobs.begin(), jobs.end(),
@@ -467,7 +470,8 @@ int build_batch(const fdtd_engine_t* engines, uint32_t n, const fdtd_batch_opts*
                     G.e16 = e->E.idx16;
                     G.h16 = e->H.idx16;
                     G.geo = e->geo_on;
-                    G.feat = e->feat;
+                    G.feat = e->feat_e;
+                    G.feat_h = e->feat_h;
                     G.first = (int)b->jobs.size();
                     b->groups.push_back(std::move(G));
                     B.groups.push_back((int)b->groups.size() - 1);

@@ -30,7 +30,7 @@ namespace {
 // dispersion orders 1..3 are instantiated in engine_adex.cu)
 template <typename IdxT, bool GEO>
 void launch_volt_f(fdtd_engine_s* e, int ts_off) {
-    switch (e->feat) {
+    switch (e->feat_e) {
         case 0: launch_volt_t<IdxT, 0, GEO>(e, ts_off); break;
         case 1: launch_volt_t<IdxT, 1, GEO>(e, ts_off); break;
         case 2: launch_volt_t<IdxT, 2, GEO>(e, ts_off); break;
@@ -41,7 +41,7 @@ void launch_volt_f(fdtd_engine_s* e, int ts_off) {
 
 template <typename IdxT, bool GEO, bool EN>
 void launch_curr_f(fdtd_engine_s* e, int ts_off) {
-    switch (e->feat) {
+    switch (e->feat_h) {
         case 0: launch_curr_t<IdxT, 0, GEO, EN>(e, ts_off); break;
         case 1: launch_curr_t<IdxT, 1, GEO, EN>(e, ts_off); break;
         case 2: launch_curr_t<IdxT, 2, GEO, EN>(e, ts_off); break;
@@ -563,6 +563,15 @@ int upload_engine(const fdtd_cop_s* c, const fdtd_engine_opts* opts, fdtd_engine
     const bool any_adex = c->E.adex_orders || c->H.adex_orders;
     const bool any_ade = c->E.any_ade || c->H.any_ade || any_adex;
     e->feat = (any_upml ? FEAT_UPML : 0) | (any_ade ? FEAT_ADE : 0) | (any_adex ? FEAT_ADEX : 0);
+    // each half-step kernel carries only the extensions its own tuples use
+    // (a scene with electric dispersion only runs the current kernel
+    // without the ADE terms: fewer registers, more resident blocks)
+    auto half_feat = [&](const HalfTables& T) {
+        return (any_upml ? FEAT_UPML : 0) | ((T.any_ade || T.adex_orders) ? FEAT_ADE : 0) |
+               (T.adex_orders ? FEAT_ADEX : 0);
+    };
+    e->feat_e = half_feat(c->E);
+    e->feat_h = half_feat(c->H);
     if (e->fused && (any_ade || c->geo)) {
         set_error("the fused single-pass kernel does not cover Lorentz/Drude nodes or factorized geometry "
                   "(use the two-pass TMA kernels)");

@@ -157,7 +157,8 @@ struct fdtd_engine_s {
     uint32_t ts = 0;
     bool started = false;
     bool need_initial_sample = true;
-    int feat = 0;
+    int feat = 0;                // union of the two halves' feature sets
+    int feat_e = 0, feat_h = 0;  // the voltage / current kernels' feature sets (FEAT_*)
     bool geo_on = false;
     int TY = 8;       // direct kernels: tile rows
     int tma_ty = 4;   // two-pass TMA kernels: tile rows (4 or 8)
