@@ -219,7 +219,9 @@ def cpu_baseline(threads: int):
 
 
 def batch_and_serve(args, device: int) -> dict:
-    """The two patterns beside the plain engine, measured on this GPU:
+    """D192 on the plain engine (the graded / dispersive configuration, with
+    its voltage kernel's algorithmic bandwidth), and the two patterns beside
+    the plain engine, measured on this GPU:
     batch -- the 96-job B96 sweep (1500 timesteps each) as one persistent
     batch against the plain engine job by job and against the same engines
     run concurrently on their own streams (CUDA events / wall clock);
@@ -229,6 +231,17 @@ def batch_and_serve(args, device: int) -> dict:
     first submission), with p50 / p99 job latency."""
     from wipems_gb300 import workloads
     out = {}
+    d = workloads.single("d192", device=device)
+    peak, _ = _peaks()
+    out["d192"] = {
+        "workload": "D192: 192^3 cells (193^3 nodes) on a seeded graded mesh (0.2-1 mm), UPML-8, Drude (~25 %) and "
+                    "Lorentz (~15 %) bricks; 3000 timesteps, factorized geometry",
+        "mcells": round(d["mcells"], 1), "device_ms": round(d["device_ms"], 2), "tiling": d["tiling"],
+        "tuples_e": d["tuples_e"], "tuples_h": d["tuples_h"],
+        "ms_volt": round(d["ms_volt"], 5), "ms_curr": round(d["ms_curr"], 5),
+        "volt_algorithmic_bytes": d["volt_algorithmic_bytes"], "volt_gbs": round(d["volt_gbs"], 1),
+        "volt_frac": round(d["volt_gbs"] / peak, 4),
+        "timing": "CUDA events; kernel times from 20 single launches each"}
     b = workloads.b96(96, 1500, device)
     out["batch"] = {
         "workload": "B96: 96 seeded jobs, grid edges 48-160 cells per axis, half PEC / half UPML-8, 1-10 "

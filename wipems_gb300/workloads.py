@@ -36,12 +36,21 @@ def single(kind: str, steps: int = 0, device: int = 0) -> dict:
     mv, mc = eng.profile_kernels(20)
     n = op.num_nodes
     info = cop.info
+    ade_e = lor_e = 0
+    if info["num_ade_nodes"]:  # voltage-side Lorentz/Drude nodes and the Lorentz ones among them (flag words)
+        fe = cop.expand()[4]
+        ade_e = int(np.count_nonzero(fe & 2))
+        lor_e = int(np.count_nonzero(fe & 4))
+    # algorithmic bytes of one voltage launch: 38 B per node, 24 B per UPML
+    # node (flux read + write), 24 B per Lorentz/Drude state read + write
+    volt_bytes = 38 * n + 24 * info["num_upml_nodes"] + 24 * ade_e + 24 * lor_e
     return dict(workload=kind, nodes=n, timesteps=nts, device_ms=ms, mcells=n * nts / (ms / 1e3) / 1e6,
                 kernel=best["kernel"],
                 ms_volt=mv, ms_curr=mc, launches=launches, setup_s=round(setup, 3), tiling=best,
                 tuples_e=info["num_tuples_e"], tuples_h=info["num_tuples_h"],
                 geometry_factored=info["geometry_factored"], upml_nodes=info["num_upml_nodes"],
-                ade_nodes=info["num_ade_nodes"])
+                ade_nodes=info["num_ade_nodes"], ade_volt_nodes=ade_e, lorentz_volt_nodes=lor_e,
+                volt_algorithmic_bytes=volt_bytes, volt_gbs=volt_bytes / (mv / 1e3) / 1e9)
 
 
 def extensions(steps: int = 1000, device: int = 0) -> list:
