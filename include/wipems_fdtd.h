@@ -99,6 +99,15 @@ int fdtd_scene_set_sinus_excite(fdtd_scene_t s, double f0, uint32_t nr_ts);
  * (Nyquist number 1).  f_max = <FDTD f_max>. */
 int fdtd_scene_set_dirac_excite(fdtd_scene_t s, double f_max, uint32_t nr_ts);
 int fdtd_scene_set_step_excite(fdtd_scene_t s, double f_max, uint32_t nr_ts);
+/* Custom signal: `function` is an expression of the time t (seconds) with
+ * the constants pi and e, Excitation::SetupCustomExcite /
+ * CalcCustomExcitation (excitation.cpp:87-94, 233-271): nr_ts samples,
+ * voltages at t = n dT and currents at t = (n + 1/2) dT, probes sampled at
+ * the Nyquist number of f0.  Arithmetic (+ - * / % ^), parentheses and the
+ * usual one- and two-argument functions are covered; comparisons, logical
+ * operators and if() are refused. */
+int fdtd_scene_set_custom_excite(fdtd_scene_t s, const char* function, double f0, double f_max,
+                                 uint32_t nr_ts);
 /* <FDTD OverSampling=...> (openems.cpp:830-832, default 4). */
 int fdtd_scene_set_oversampling(fdtd_scene_t s, uint32_t oversampling);
 

@@ -93,6 +93,9 @@ def _scene_struct(spec: dict):
     sc.f0, sc.fc = spec["f0"], spec["fc"]
     sc.excite_type = spec.get("excite_type", 0)
     sc.f_max = spec.get("f_max", 0.0)
+    fn = spec.get("function", "").encode()
+    keep.append(fn)
+    sc.function = fn
     sc.nr_ts = spec["nr_ts"]
     sc.oversampling = spec["oversampling"]
     prims = (abi.OraclePrim * max(1, len(spec["prims"])))()

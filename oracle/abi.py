@@ -33,7 +33,7 @@ class OracleScene(C.Structure):
                 ("bc", C.c_int * 6), ("pml_size", u32 * 6), ("mur_vph", C.c_double * 6),
                 ("f0", C.c_double), ("fc", C.c_double), ("nr_ts", u32), ("oversampling", u32),
                 ("num_prims", u32), ("prims", C.POINTER(OraclePrim)), ("excite_type", C.c_int),
-                ("f_max", C.c_double)]
+                ("f_max", C.c_double), ("function", C.c_char_p)]
 
 
 class OracleOpInfo(C.Structure):

@@ -51,11 +51,14 @@
 // function, parsed by fparser in the reference, is evaluated as the C++
 // expression of its default string.
 #include <algorithm>
+#include <cctype>
 #include <climits>
+#include <cstdlib>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <memory>
+#include <string>
 #include <thread>
 #include <vector>
 
@@ -98,8 +101,9 @@ typedef struct {
     uint32_t oversampling;
     uint32_t num_prims;
     const oracle_prim* prims;
-    int excite_type;  // Excitation::ExciteTypes: 0 Gaussian, 1 sinusoid, 2 Dirac, 3 step
+    int excite_type;  // Excitation::ExciteTypes: 0 Gaussian, 1 sinusoid, 2 Dirac, 3 step, 10 custom
     double f_max;
+    const char* function;  // the custom signal (a function of t)
 } oracle_scene;
 
 typedef struct {
@@ -227,6 +231,151 @@ struct AdeO {
 
 }  // namespace
 
+// The custom excitation's function of t, evaluated the way the function
+// parser openEMS calls does arithmetic (excitation.cpp:233-271): tokens to
+// postfix by operator precedence (shunting yard: ^ right-associative above
+// unary minus, then * / %, then + -), then a stack machine in double.
+struct OracleFunction {
+    struct Tok {
+        int kind;  // 0 number, 1 t, 2 operator, 3 function, 4 '(', 5 ')', 6 ','
+        double v;
+        char op;        // + - * / % ^ and 'u' for unary minus
+        std::string fn;
+    };
+    std::vector<Tok> rpn;
+    std::string err;
+
+    static int prec(char op) { return op == '^' ? 4 : op == 'u' ? 3 : (op == '*' || op == '/' || op == '%') ? 2 : 1; }
+    static bool right(char op) { return op == '^' || op == 'u'; }
+    static int arity(const std::string& f) {
+        static const char* two[] = {"atan2", "hypot", "max", "min", "pow"};
+        for (const char* n : two)
+            if (f == n) return 2;
+        return 1;
+    }
+
+    bool parse(const std::string& s) {
+        std::vector<Tok> toks;
+        size_t i = 0;
+        bool expect_operand = true;
+        while (i < s.size()) {
+            const char c = s[i];
+            if (c == ' ' || c == '\t') { ++i; continue; }
+            if ((c >= '0' && c <= '9') || c == '.') {
+                char* end = nullptr;
+                const double v = std::strtod(s.c_str() + i, &end);
+                i = (size_t)(end - s.c_str());
+                toks.push_back(Tok{0, v, 0, ""});
+                expect_operand = false;
+            } else if ((c >= 'a' && c <= 'z') || (c >= 'A' && c <= 'Z') || c == '_') {
+                size_t e = i;
+                while (e < s.size() && (std::isalnum((unsigned char)s[e]) || s[e] == '_')) ++e;
+                const std::string id = s.substr(i, e - i);
+                i = e;
+                if (id == "t") toks.push_back(Tok{1, 0, 0, ""});
+                else if (id == "pi") toks.push_back(Tok{0, 3.14159265358979323846, 0, ""});
+                else if (id == "e") toks.push_back(Tok{0, 2.71828182845904523536, 0, ""});
+                else { toks.push_back(Tok{3, 0, 0, id}); expect_operand = true; continue; }
+                expect_operand = false;
+            } else if (c == '(') { toks.push_back(Tok{4, 0, 0, ""}); ++i; expect_operand = true; }
+            else if (c == ')') { toks.push_back(Tok{5, 0, 0, ""}); ++i; expect_operand = false; }
+            else if (c == ',') { toks.push_back(Tok{6, 0, 0, ""}); ++i; expect_operand = true; }
+            else if (std::strchr("+-*/%^", c)) {
+                toks.push_back(Tok{2, 0, (c == '-' && expect_operand) ? 'u' : c, ""});
+                ++i;
+                expect_operand = true;
+            } else { err = std::string("unsupported character ") + c; return false; }
+        }
+        std::vector<Tok> ops;
+        for (const Tok& t : toks) {
+            if (t.kind <= 1) rpn.push_back(t);
+            else if (t.kind == 3) ops.push_back(t);
+            else if (t.kind == 2) {
+                if (t.op != 'u')
+                    while (!ops.empty() && ops.back().kind == 2 &&
+                           (prec(ops.back().op) > prec(t.op) || (prec(ops.back().op) == prec(t.op) && !right(t.op)))) {
+                        rpn.push_back(ops.back());
+                        ops.pop_back();
+                    }
+                ops.push_back(t);
+            } else if (t.kind == 4) ops.push_back(t);
+            else if (t.kind == 6 || t.kind == 5) {
+                while (!ops.empty() && ops.back().kind != 4) { rpn.push_back(ops.back()); ops.pop_back(); }
+                if (ops.empty()) { err = "unbalanced parentheses"; return false; }
+                if (t.kind == 5) {
+                    ops.pop_back();
+                    if (!ops.empty() && ops.back().kind == 3) { rpn.push_back(ops.back()); ops.pop_back(); }
+                }
+            }
+        }
+        while (!ops.empty()) {
+            if (ops.back().kind == 4) { err = "unbalanced parentheses"; return false; }
+            rpn.push_back(ops.back());
+            ops.pop_back();
+        }
+        return true;
+    }
+
+    double eval(double t) const {
+        std::vector<double> st;
+        for (const Tok& k : rpn) {
+            if (k.kind == 0) { st.push_back(k.v); continue; }
+            if (k.kind == 1) { st.push_back(t); continue; }
+            if (k.kind == 2 && k.op == 'u') { st.back() = -st.back(); continue; }
+            if (k.kind == 2) {
+                const double b = st.back(); st.pop_back();
+                double& a = st.back();
+                switch (k.op) {
+                    case '+': a = a + b; break;
+                    case '-': a = a - b; break;
+                    case '*': a = a * b; break;
+                    case '/': a = a / b; break;
+                    case '%': a = std::fmod(a, b); break;
+                    default: a = std::pow(a, b); break;
+                }
+                continue;
+            }
+            const std::string& f = k.fn;
+            if (arity(f) == 2) {
+                const double b = st.back(); st.pop_back();
+                double& a = st.back();
+                if (f == "atan2") a = std::atan2(a, b);
+                else if (f == "hypot") a = std::hypot(a, b);
+                else if (f == "max") a = a > b ? a : b;
+                else if (f == "min") a = a < b ? a : b;
+                else a = std::pow(a, b);
+                continue;
+            }
+            double& x = st.back();
+            if (f == "abs") x = std::fabs(x);
+            else if (f == "acos") x = std::acos(x);
+            else if (f == "acosh") x = std::acosh(x);
+            else if (f == "asin") x = std::asin(x);
+            else if (f == "asinh") x = std::asinh(x);
+            else if (f == "atan") x = std::atan(x);
+            else if (f == "atanh") x = std::atanh(x);
+            else if (f == "cbrt") x = std::cbrt(x);
+            else if (f == "ceil") x = std::ceil(x);
+            else if (f == "cos") x = std::cos(x);
+            else if (f == "cosh") x = std::cosh(x);
+            else if (f == "exp") x = std::exp(x);
+            else if (f == "exp2") x = std::exp2(x);
+            else if (f == "floor") x = std::floor(x);
+            else if (f == "int") x = std::floor(x + 0.5);
+            else if (f == "log") x = std::log(x);
+            else if (f == "log10") x = std::log10(x);
+            else if (f == "log2") x = std::log2(x);
+            else if (f == "sin") x = std::sin(x);
+            else if (f == "sinh") x = std::sinh(x);
+            else if (f == "sqrt") x = std::sqrt(x);
+            else if (f == "tan") x = std::tan(x);
+            else if (f == "tanh") x = std::tanh(x);
+            else x = std::trunc(x);
+        }
+        return st.empty() ? 0.0 : st.back();
+    }
+};
+
 struct oracle_operator_s {
     uint32_t N[3];
     size_t NN;
@@ -239,6 +388,7 @@ struct oracle_operator_s {
     double f0, fc;
     int excite_type = 0;
     double signal_period = 0;  // Excitation::m_SignalPeriod
+    std::string function;      // the custom signal
     uint32_t nr_ts, oversampling;
     int threads;
     Csx csx;
@@ -1332,11 +1482,29 @@ struct oracle_operator_s {
         sig_c = {step ? 1.0f : 0.0f, 1.0f};
         nyquist = 1;
     }
+    // Excitation::CalcCustomExcitation (excitation.cpp:233-271)
+    bool CalcCustomExcitation() {
+        OracleFunction F;
+        if (!F.parse(function)) return false;
+        length = nr_ts;
+        sig_v.resize(length);
+        sig_c.resize(length);
+        double vars[1];
+        for (uint32_t n = 0; n < length; ++n) {
+            vars[0] = n * dT;
+            sig_v[n] = (float)F.eval(vars[0]);
+            vars[0] += 0.5 * dT;
+            sig_c[n] = (float)F.eval(vars[0]);
+        }
+        nyquist = CalcNyquistNum(f0);
+        return true;
+    }
     // Excitation::buildExcitationSignal (excitation.cpp:96-134)
-    void BuildSignal() {
+    bool BuildSignal() {
         switch (excite_type) {
             case 0: CalcGaussianPulsExcitation(); break;
             case 1: CalcSinusExcitation(); break;
+            case 10: if (!CalcCustomExcitation()) return false; break;
             default: CalcUnitExcitation(excite_type == 3); break;
         }
         // Engine_Ext_Excitation's period (engine_ext_excitation.cpp:44-46)
@@ -1349,6 +1517,7 @@ struct oracle_operator_s {
                 maxAmp = std::fabs(sig_v[n]);
                 max_exc_ts = n;
             }
+        return true;
     }
 
     // openEMS::SetupProcessing probe loop (openems.cpp:470-540)
@@ -1474,7 +1643,7 @@ struct oracle_operator_s {
         if (have_lorentz) BuildLorentz();
         if (!csx.by_type(T_LUMPED).empty()) BuildRLC();
 
-        BuildSignal();
+        if (!BuildSignal()) return -1;
         // Engine_Ext_Mur_ABC start timestep (engine_ext_mur_abc.cpp:43-58)
         for (MurO& M : mur) {
             int maxDelay = -1;
@@ -1513,7 +1682,8 @@ int oracle_operator_build(const oracle_scene* S, int threads, oracle_operator_s*
     // excitation.cpp:56-85): the Dirac and step leave m_f0 / m_fc unset in
     // the reference; 0 here
     op->excite_type = S->excite_type;
-    op->f0 = S->excite_type <= 1 ? S->f0 : 0.0;
+    op->function = S->function ? S->function : "";
+    op->f0 = (S->excite_type <= 1 || S->excite_type == 10) ? S->f0 : 0.0;
     op->fc = S->excite_type == 0 ? S->fc : 0.0;
     op->signal_period = S->excite_type == 1 ? 1 / S->f0 : 0.0;
     op->nr_ts = S->nr_ts;

@@ -10,7 +10,7 @@ reader, independent of the engine library's, restating:
         endCriteria, OverSampling only when > 1, BoundaryCond codes or
         PEC / PMC / MUR / PML_n names, MUR_PhaseVelocity[_face], the
         <Excitation> of Type 0 (Gaussian: f0 fc), 1 (sinusoid: f0), 2 / 3
-        (Dirac / step: <FDTD f_max>))
+        (Dirac / step: <FDTD f_max>), 10 (custom: Function, f0))
     default PML size 8               openems.cpp:101
     CSXCAD ContinuousStructure::ReadFromXML, for rectilinear grids
         (DeltaUnit, X/Y/ZLines as sorted unique number lists), the
@@ -76,11 +76,12 @@ def xml_spec(path_or_text: str) -> dict:
             raise ValueError(f"<FDTD {k}>")
     exc = fdtd.find("Excitation")
     etype = -1 if exc is None else int(_num(exc, "Type", -1))
-    if etype not in (0, 1, 2, 3):
-        raise ValueError("only the Gaussian (0), sinusoid (1), Dirac (2) and step (3) excitations")
-    f0 = _num(exc, "f0", 0.0) if etype <= 1 else 0.0
+    if etype not in (0, 1, 2, 3, 10):
+        raise ValueError("only the Gaussian (0), sinusoid (1), Dirac (2), step (3) and custom (10) excitations")
+    f0 = _num(exc, "f0", 0.0) if etype in (0, 1, 10) else 0.0
     fc = _num(exc, "fc", 0.0) if etype == 0 else 0.0
     f_max = _num(fdtd, "f_max", 0.0) if etype >= 2 else 0.0
+    function = exc.get("Function", "") if etype == 10 else ""
     bcn = fdtd.find("BoundaryCond")
     if bcn is None:
         raise ValueError("<BoundaryCond> missing")
@@ -185,4 +186,5 @@ def xml_spec(path_or_text: str) -> dict:
         else:
             raise ValueError(f"property <{p.tag}>")
     return dict(lines=lines, unit=unit, background=background, bc=bc, pml_size=pml, mur_vph=vph, f0=f0, fc=fc,
-                nr_ts=nr_ts, oversampling=oversampling, prims=prims, excite_type=etype, f_max=f_max)
+                nr_ts=nr_ts, oversampling=oversampling, prims=prims, excite_type=etype, f_max=f_max,
+                function=function)

@@ -240,14 +240,15 @@ def oracle_inputs(prod_op):
     return ref.desc, ref.probes
 
 
-def with_signal(scene, excite_type: int, f: float = 0.0):
+def with_signal(scene, excite_type: int, f: float = 0.0, function: str = ""):
     """The scene with its Gaussian pulse replaced by another signal of the
-    reference: 1 sinusoid of frequency f, 2 Dirac pulse, 3 step (f = f_max)."""
+    reference: 1 sinusoid of frequency f, 2 Dirac pulse, 3 step (f = f_max),
+    10 the custom `function` of t (f = f0)."""
     import copy
     from wipems_gb300 import Scene, SceneSpec
     src = copy.deepcopy(scene.spec)
     sp = SceneSpec(*src["lines"], src["unit"])
-    src.update(excite_type=int(excite_type), f0=float(f) if excite_type == 1 else 0.0, fc=0.0,
-               f_max=float(f) if excite_type >= 2 else 0.0)
+    src.update(excite_type=int(excite_type), f0=float(f) if excite_type in (1, 10) else 0.0, fc=0.0,
+               f_max=float(f) if excite_type in (2, 3) else 0.0, function=function)
     sp.spec = src
     return Scene.from_spec(sp)

@@ -120,6 +120,39 @@ def test_excitation_signal_operators_identical(kind, etype, f):
         assert O.nyquist == 1 and O.probe_interval == 1
 
 
+CUSTOM = ["sin(2*pi*6e9*t)*exp(-((t-3e-10)/1e-10)^2)", "-t^2*1e18 + 2^-3",
+          "sin(2*pi*5e9*t)^3 - cos(atan2(t, 1e-10))", "max(0, 1 - t/5e-10) * (1 - exp(-t/1e-11))",
+          "pow(2, 3^2)*1e-3 + log10(1+t*1e9) % 0.7", "-(-t)*-1e9*-2"]
+
+
+@pytest.mark.parametrize("fn", CUSTOM)
+def test_custom_signal_matches_oracle_and_numpy(fn):
+    """Excitation::CalcCustomExcitation (excitation.cpp:233-271): the
+    product's expression compiler (recursive descent), the oracle's
+    (shunting yard) and numpy evaluating the same formula give the same
+    float samples at t = n dT; the Nyquist number follows f0."""
+    s = with_signal(scenes.mini("rlc", nr_ts=400), 10, 6e9, fn)
+    P, O = both(s)
+    assert_same_operator(P, O)
+    d = P.desc
+    assert d.signal_length == 400 and P.nyquist == int(np.floor(1 / 6e9 / 2 / P.dT))
+    sig = np.ctypeslib.as_array(d.signal_volt, shape=(400,))
+    t = np.arange(400) * P.dT
+    env = {"t": t, "pi": np.pi, "e": np.e, "sin": np.sin, "cos": np.cos, "exp": np.exp, "atan2": np.arctan2,
+           "max": np.maximum, "pow": np.power, "log10": np.log10}
+    ref = np.asarray(eval(fn.replace("^", "**"), {"__builtins__": {}}, env) * np.ones_like(t), np.float32)
+    assert np.array_equal(sig, ref)
+
+
+def test_custom_signal_refuses_what_it_does_not_cover():
+    from wipems_gb300 import Scene
+    from wipems_gb300._abi import FdtdError
+    s = Scene(*[np.arange(5, dtype=np.float64)] * 3, 1e-3)
+    for bad in ("t < 1e-9", "if(t, 1, 0)", "sin(t", "foo(t)", "x + 1", "2 ** t"):
+        with pytest.raises(FdtdError):
+            s.set_custom_excite(bad, 1e9, 100)
+
+
 def test_voltage_probes_need_a_line():
     """A voltage probe box that is a point or spans more than one axis is
     skipped, with no sample column (openems.cpp:481-486); current and field

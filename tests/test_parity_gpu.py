@@ -73,11 +73,13 @@ def test_mini_scenes_match_oracle(kind, kernel):
 
 
 @pytest.mark.parametrize("kind", ["upml", "rlc_mur"])
-@pytest.mark.parametrize("etype,f", [(1, 6e9), (2, 2e10), (3, 0.0)])
+@pytest.mark.parametrize("etype,f", [(1, 6e9), (2, 2e10), (3, 0.0), (10, 6e9)])
 def test_excitation_signals_match_oracle(kind, etype, f):
     """Sinusoid (periodic: the signal index wraps with the period), Dirac
-    pulse and step through the graph-chunked TMA engine: bit-identical."""
-    op = Operator(with_signal(scenes.mini(kind, nr_ts=700), etype, f))
+    pulse, step and a custom function of t through the graph-chunked TMA
+    engine: bit-identical."""
+    fn = "sin(2*pi*6e9*t)*exp(-((t-3e-10)/1e-10)^2)" if etype == 10 else ""
+    op = Operator(with_signal(scenes.mini(kind, nr_ts=700), etype, f, fn))
     ref = oracle.run(*oracle_inputs(op), 700, op.probe_interval, engine=oracle.BASIC)
     eng = Engine(CompressedOperator(op), kernel="tma")
     eng.iterate(700)

@@ -100,7 +100,7 @@ def test_xml_magnetic_lorentz_material():
 
 @pytest.mark.parametrize("edit,needle", [
     (('<Box Priority="20">', '<Cylinder Priority="20" Radius="1">'), "Cylinder"),
-    (('<Excitation Type="0" f0="1e+10"', '<Excitation Type="10" f0="1e+10"'), "excitation Type 10"),
+    (('<Excitation Type="0" f0="1e+10"', '<Excitation Type="11" f0="1e+10"'), "excitation Type 11"),
     (('Epsilon="3.66"', 'Epsilon="3.66,3.66,4"'), "anisotropic"),
     (('<Weight Epsilon="1"', '<Weight Epsilon="2*x"'), "weighting"),
     (('<Metal ID="1" Name="plate">', '<ConductingSheet ID="1" Name="plate">'), "ConductingSheet"),
@@ -183,7 +183,7 @@ def test_xml_field_probes():
     assert types[-2:] == [2, 3] and op.probes[-1].weight == 2.0
 
 
-@pytest.mark.parametrize("etype", [1, 2, 3])
+@pytest.mark.parametrize("etype", [1, 2, 3, 10])
 def test_xml_excitation_signals(etype):
     """<Excitation Type="1" f0> (sinusoid), Type 2 / 3 (Dirac / step, with
     <FDTD f_max>): the engine library's reader equals the API scene and the
@@ -191,13 +191,16 @@ def test_xml_excitation_signals(etype):
     import oracle
     from oracle.xml_spec import xml_spec
     from helpers import assert_same_operator
+    fn = ' Function="sin(2*pi*7e9*t)*(1-exp(-t/2e-10))"' if etype == 10 else ""
     text = (GOLDEN / "port_box.xml").read_text().replace(
-        '<Excitation Type="0" f0="1e+10" fc="5e+09"/>', f'<Excitation Type="{etype}" f0="7e+09" fc="5e+09"/>')
+        '<Excitation Type="0" f0="1e+10" fc="5e+09"/>', f'<Excitation Type="{etype}" f0="7e+09" fc="5e+09"{fn}/>')
     sx = Scene.from_xml(text)
     assert sx.xml_info["excite_type"] == etype
     s = _api_scene()
     if etype == 1:
         s.set_sinus_excite(7e9, 600)
+    elif etype == 10:
+        s.set_custom_excite("sin(2*pi*7e9*t)*(1-exp(-t/2e-10))", 7e9, 600, 1.5e10)
     else:
         (s.set_dirac_excite if etype == 2 else s.set_step_excite)(1.5e10, 600)
     _same_operator(Operator(sx), Operator(s))

@@ -161,6 +161,7 @@ SIGNATURES = [
     ("fdtd_scene_set_sinus_excite", C.c_int, [_P, C.c_double, u32]),
     ("fdtd_scene_set_dirac_excite", C.c_int, [_P, C.c_double, u32]),
     ("fdtd_scene_set_step_excite", C.c_int, [_P, C.c_double, u32]),
+    ("fdtd_scene_set_custom_excite", C.c_int, [_P, C.c_char_p, C.c_double, C.c_double, u32]),
     ("fdtd_scene_set_oversampling", C.c_int, [_P, u32]),
     ("fdtd_scene_add_material", C.c_int, [_P, C.c_int, PD, PD, C.c_double, C.c_double, C.c_double, C.c_double]),
     ("fdtd_scene_add_metal", C.c_int, [_P, C.c_int, PD, PD]),

@@ -505,7 +505,7 @@ int compress_impl(const fdtd_op_desc* d, int mode, int want_rot, fdtd_cop_s* c) 
             std::vector<HalfTuple>& tv = pt[h][x];
             std::vector<uint32_t>& lv = pl[h][x];
             lv.resize((size_t)Dy * Dz);
-            HalfTuple t, last;
+            HalfTuple t{}, last{};  // value-initialized: bytes past the compared key stay zero
             uint32_t last_id = UINT32_MAX;
             uint32_t o[3];
             o[ax] = x;

@@ -80,10 +80,12 @@ struct fdtd_scene_s {
     double mur_vph[6] = {0, 0, 0, 0, 0, 0};
     double f0 = 0, fc = 0;
     // Excitation::ExciteTypes (excitation.h:28): 0 Gaussian pulse,
-    // 1 sinusoid, 2 Dirac pulse, 3 step; f_max is the Dirac / step's
-    // <FDTD f_max> (recorded, it changes nothing on this path)
+    // 1 sinusoid, 2 Dirac pulse, 3 step, 10 custom function of t; f_max is
+    // the Dirac / step / custom <FDTD f_max> (recorded, it changes nothing on
+    // this path)
     int excite_type = 0;
     double f_max = 0;
+    std::string exc_function;  // the custom signal's expression
     bool have_excite = false;
     uint32_t nr_ts = 0;
     uint32_t oversampling = 4;

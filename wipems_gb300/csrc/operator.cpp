@@ -39,6 +39,7 @@
 #include <thread>
 
 #include "fdtd_host.h"
+#include "signal_expr.h"
 
 namespace wipems {
 
@@ -1429,6 +1430,24 @@ static int build_operator(const fdtd_scene_s& S, int threads, fdtd_operator_s& o
         // the engine's period p = int(GetSignalPeriod() / dT)
         // (engine_ext_excitation.cpp:45-46)
         op.signal_period_ts = (uint32_t)(int)((1 / f0) / dT);
+    } else if (S.have_excite && S.excite_type == 10) {
+        // CalcCustomExcitation (excitation.cpp:233-271): nr_ts samples of the
+        // function at t = n dT (currents at t + dT / 2), Nyquist number of f0
+        SignalExpr ex;
+        std::string err;
+        if (!ex.compile(S.exc_function, err)) {
+            set_error("custom excitation: " + err);
+            return FDTD_ERR_ARG;
+        }
+        op.sig_volt.resize(S.nr_ts);
+        op.sig_curr.resize(S.nr_ts);
+        for (uint32_t n = 0; n < S.nr_ts; ++n) {
+            double t = n * dT;
+            op.sig_volt[n] = (float)ex.eval(t);
+            t += 0.5 * dT;
+            op.sig_curr[n] = (float)ex.eval(t);
+        }
+        op.nyquist = nyquist_num(S.f0);
     } else if (S.have_excite) {
         // CalcDiracPulsExcitation / CalcStepExcitation (excitation.cpp:179-218)
         const float first = S.excite_type == 3 ? 1.f : 0.f;
@@ -1715,6 +1734,27 @@ static int set_unit_excite(fdtd_scene_t s, int type, double f_max, uint32_t nr_t
     s->f_max = f_max;
     s->nr_ts = nr_ts;
     s->excite_type = type;
+    s->have_excite = true;
+    return FDTD_OK;
+}
+
+int fdtd_scene_set_custom_excite(fdtd_scene_t s, const char* function, double f0, double f_max, uint32_t nr_ts) {
+    if (!s || !function || nr_ts == 0 || !(f0 >= 0)) {
+        set_error("fdtd_scene_set_custom_excite: need a function, f0 >= 0 and nr_ts > 0");
+        return FDTD_ERR_ARG;
+    }
+    SignalExpr ex;
+    std::string err;
+    if (!ex.compile(function, err)) {
+        set_error("fdtd_scene_set_custom_excite: " + err);
+        return FDTD_ERR_ARG;
+    }
+    s->f0 = f0;
+    s->fc = 0;
+    s->f_max = f_max;
+    s->nr_ts = nr_ts;
+    s->exc_function = function;
+    s->excite_type = 10;
     s->have_excite = true;
     return FDTD_OK;
 }

@@ -9,8 +9,8 @@
 // InitFDTD.m, SetGaussExcite.m, SetBoundaryCond.m).
 //
 // Covered: <FDTD NumberOfTimesteps endCriteria OverSampling f_max>, its
-// <Excitation> of Type 0 (Gaussian, f0 fc), 1 (sinusoid, f0), 2 (Dirac) or
-// 3 (step), and <BoundaryCond> (numeric codes or
+// <Excitation> of Type 0 (Gaussian, f0 fc), 1 (sinusoid, f0), 2 (Dirac),
+// 3 (step) or 10 (custom: Function f0), and <BoundaryCond> (numeric codes or
 // PEC / PMC / MUR / PML_n, MUR_PhaseVelocity[_face]); the <RectilinearGrid DeltaUnit> with its X/Y/ZLines,
 // <BackgroundMaterial>, and the properties Material, Metal, LumpedElement,
 // Excitation, ProbeBox (voltage and current) and LorentzMaterial (order 1,
@@ -329,18 +329,23 @@ int fdtd_scene_load_xml(const char* text, fdtd_scene_t* out, fdtd_xml_info* info
     const XNode* exc = fdtd->child("Excitation");
     if (!exc) L.bad(FDTD_ERR_ARG, "<FDTD> has no <Excitation> (openems.cpp:892-896)");
     // the signal (openems.cpp:898-926): Type 0 Gaussian (f0, fc), 1 sinusoid
-    // (f0), 2 Dirac and 3 step (<FDTD f_max>); 10 (a custom function of t)
-    // is not covered
+    // (f0), 2 Dirac and 3 step (<FDTD f_max>), 10 custom (Function, f0,
+    // <FDTD f_max>)
     double f0 = 0, fc = 0, f_max = 0;
+    std::string function;
     if (exc) {
         L.num(*exc, "Type", d, -1);
         inf.excite_type = (int)d;
-        if ((int)d < 0 || (int)d > 3)
+        if (((int)d < 0 || (int)d > 3) && (int)d != 10)
             L.bad(FDTD_ERR_UNSUPPORTED, "excitation Type " + std::to_string((int)d) +
-                                            " (Gaussian 0, sinusoid 1, Dirac 2 and step 3 are covered)");
-        if ((int)d <= 1) L.num(*exc, "f0", f0, 0);
+                                            " (Gaussian 0, sinusoid 1, Dirac 2, step 3 and custom 10 are covered)");
+        if ((int)d <= 1 || (int)d == 10) L.num(*exc, "f0", f0, 0);
         if ((int)d == 0) L.num(*exc, "fc", fc, 0);
         if ((int)d >= 2) L.num(*fdtd, "f_max", f_max, 0);
+        if ((int)d == 10) {
+            if (exc->attr("Function")) function = *exc->attr("Function");
+            else L.bad(FDTD_ERR_ARG, "<Excitation Type=\"10\"> needs a Function attribute");
+        }
     }
     inf.f0 = f0;
     inf.fc = fc;
@@ -430,6 +435,8 @@ int fdtd_scene_load_xml(const char* text, fdtd_scene_t* out, fdtd_xml_info* info
         return fail(rc, "Dirac excitation");
     if (inf.excite_type == 3 && (rc = fdtd_scene_set_step_excite(sc, f_max, inf.nr_ts)))
         return fail(rc, "step excitation");
+    if (inf.excite_type == 10 && (rc = fdtd_scene_set_custom_excite(sc, function.c_str(), f0, f_max, inf.nr_ts)))
+        return fail(rc, "custom excitation");
     if (inf.oversampling && (rc = fdtd_scene_set_oversampling(sc, inf.oversampling))) return fail(rc, "OverSampling");
     // ---- properties
     const XNode* props = csx->child("Properties");

@@ -111,6 +111,13 @@ class SceneSpec:
         self.nr_ts = int(nr_ts)
         self._record(f0=0.0, fc=0.0, nr_ts=int(nr_ts), excite_type=3, f_max=float(f_max))
 
+    def set_custom_excite(self, function: str, f0: float, nr_ts: int, f_max: float = 0.0):
+        """Custom signal, an expression of t (openEMS SetCustomExcite),
+        sampled for nr_ts timesteps; probes sample at f0's Nyquist rate."""
+        self.nr_ts = int(nr_ts)
+        self._record(f0=float(f0), fc=0.0, nr_ts=int(nr_ts), excite_type=10, f_max=float(f_max),
+                     function=str(function))
+
     def set_oversampling(self, os_: int):
         self._record(oversampling=int(os_))
 
@@ -219,6 +226,8 @@ class Scene(SceneSpec):
             s.set_sinus_excite(d["f0"], d["nr_ts"])
         elif et in (2, 3):
             (s.set_dirac_excite if et == 2 else s.set_step_excite)(d["f_max"], d["nr_ts"])
+        elif et == 10:
+            s.set_custom_excite(d["function"], d["f0"], d["nr_ts"], d["f_max"])
         elif d["fc"] > 0:
             s.set_gauss_excite(d["f0"], d["fc"], d["nr_ts"])
         if d["oversampling"] != 4:
@@ -320,6 +329,11 @@ class Scene(SceneSpec):
     def set_step_excite(self, f_max: float, nr_ts: int):
         check(lib().fdtd_scene_set_step_excite(self._h, f_max, int(nr_ts)), "set_step_excite")
         super().set_step_excite(f_max, nr_ts)
+
+    def set_custom_excite(self, function: str, f0: float, nr_ts: int, f_max: float = 0.0):
+        check(lib().fdtd_scene_set_custom_excite(self._h, str(function).encode(), float(f0), float(f_max),
+                                                 int(nr_ts)), "set_custom_excite")
+        super().set_custom_excite(function, f0, nr_ts, f_max)
 
     def set_oversampling(self, os_: int):
         check(lib().fdtd_scene_set_oversampling(self._h, int(os_)), "set_oversampling")
