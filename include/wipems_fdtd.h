@@ -747,6 +747,9 @@ int fdtd_server_wait(fdtd_server_t srv, uint64_t job_id, double timeout_s);
 int fdtd_server_read_samples(fdtd_server_t srv, uint64_t job_id, uint32_t* ts, double* vals,
                              double* energy);
 int fdtd_server_get_fields(fdtd_server_t srv, uint64_t job_id, float* volt, float* curr);
+/* The probe type (0..3) of each sample column of a built job (a field
+ * probe fills three columns): types[num_probes] of fdtd_job_status. */
+int fdtd_server_probe_types(fdtd_server_t srv, uint64_t job_id, int* types, uint32_t cap);
 /* Drops a finished job's host results. */
 int fdtd_server_release(fdtd_server_t srv, uint64_t job_id);
 int fdtd_server_get_stats(fdtd_server_t srv, fdtd_server_stats* st);

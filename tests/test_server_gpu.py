@@ -130,4 +130,22 @@ def test_server_job_with_field_probes():
     e.iterate(NR_TS)
     _same(e, srv, jid)
     assert srv.samples(jid).times(4)[1] - srv.samples(jid).times(4)[0] > 0
+    assert srv.samples(jid).probe_types == e.samples().probe_types == [0, 1, 2, 2, 2, 3, 3, 3]
+    srv.close()
+
+
+def test_server_serves_an_xml_scene():
+    """A scene read from an openEMS XML document (no Python-side probe
+    list) through the server: sample columns and their types come from the
+    server, and the result equals the document run alone."""
+    import os
+    from wipems_gb300 import Scene
+    path = os.path.join(os.path.dirname(__file__), "golden", "lorentz_mur.xml")
+    srv = Server(round_steps=64)
+    jid = srv.submit(Scene.from_xml(path), end_crit=CRIT, keep_fields=True)
+    srv.wait(0, timeout=300)
+    e = Engine(Operator(Scene.from_xml(path)), end_crit=CRIT)
+    e.iterate(Scene.from_xml(path).nr_ts)
+    _same(e, srv, jid)
+    assert srv.samples(jid).probe_types == e.samples().probe_types
     srv.close()

@@ -230,6 +230,7 @@ SIGNATURES = [
     ("fdtd_server_job_status", C.c_int, [_P, C.c_uint64, C.POINTER(FdtdJobStatus)]),
     ("fdtd_server_wait", C.c_int, [_P, C.c_uint64, C.c_double]),
     ("fdtd_server_read_samples", C.c_int, [_P, C.c_uint64, PU32, PD, PD]),
+    ("fdtd_server_probe_types", C.c_int, [_P, C.c_uint64, C.POINTER(C.c_int), u32]),
     ("fdtd_server_get_fields", C.c_int, [_P, C.c_uint64, PF, PF]),
     ("fdtd_server_release", C.c_int, [_P, C.c_uint64]),
     ("fdtd_server_get_stats", C.c_int, [_P, C.POINTER(FdtdServerStats)]),

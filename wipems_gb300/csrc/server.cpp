@@ -609,6 +609,24 @@ int fdtd_server_job_status(fdtd_server_t s, uint64_t id, fdtd_job_status* st) {
     return FDTD_OK;
 }
 
+int fdtd_server_probe_types(fdtd_server_t s, uint64_t id, int* types, uint32_t cap) {
+    if (!s || !types) return FDTD_ERR_ARG;
+    std::lock_guard<std::mutex> lock(s->mu);
+    Job* j = find(s, id);
+    if (!j) {
+        set_error("fdtd_server_probe_types: unknown job id");
+        return FDTD_ERR_ARG;
+    }
+    if (cap < sample_columns(j)) {
+        set_error("fdtd_server_probe_types: buffer smaller than the job's sample columns");
+        return FDTD_ERR_ARG;
+    }
+    uint32_t k = 0;
+    for (const fdtd_probe_desc& p : j->probes)
+        for (int c = 0; c < ((p.type == 2 || p.type == 3) ? 3 : 1); ++c) types[k++] = p.type;
+    return FDTD_OK;
+}
+
 int fdtd_server_wait(fdtd_server_t s, uint64_t id, double timeout_s) {
     if (!s) return FDTD_ERR_ARG;
     std::unique_lock<std::mutex> lock(s->mu);

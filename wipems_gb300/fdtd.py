@@ -812,7 +812,6 @@ class Server:
         h = C.c_void_p()
         check(lib().fdtd_server_create(C.byref(o), C.byref(h)), "fdtd_server_create")
         self._h = h
-        self._probe_types: dict[int, list] = {}
 
     def submit(self, scene: Scene, end_crit: float = 0.0, max_timesteps: int = 0, probe_interval: int = 0,
                keep_fields: bool = False) -> int:
@@ -822,7 +821,6 @@ class Server:
         jid = C.c_uint64()
         check(lib().fdtd_server_submit(self._h, scene._h, C.byref(o), C.byref(jid)), "fdtd_server_submit")
         scene._h = None
-        self._probe_types[jid.value] = [p["type"] for p in scene.probes for _ in range(3 if p["type"] in (2, 3) else 1)]
         return jid.value
 
     def status(self, job: int) -> dict:
@@ -848,9 +846,10 @@ class Server:
         check(lib().fdtd_server_read_samples(self._h, int(job), ts.ctypes.data_as(_abi.PU32),
                                              vals.ctypes.data_as(_abi.PD), en.ctypes.data_as(_abi.PD)),
               "fdtd_server_read_samples")
-        types = self._probe_types.get(job, [0] * npr)
+        types = (C.c_int * max(1, npr))()
+        check(lib().fdtd_server_probe_types(self._h, int(job), types, max(1, npr)), "fdtd_server_probe_types")
         return Samples(ts=ts.astype(np.int64), values=vals[:, :npr], energy=en, dT=st["dT"],
-                       probe_types=list(types))
+                       probe_types=list(types)[:npr])
 
     def fields(self, job: int):
         shape = (3,) + self.status(job)["num_lines"]
@@ -862,7 +861,6 @@ class Server:
 
     def release(self, job: int):
         check(lib().fdtd_server_release(self._h, int(job)), "fdtd_server_release")
-        self._probe_types.pop(job, None)
 
     def stats(self) -> dict:
         st = _abi.FdtdServerStats()
