@@ -13,9 +13,9 @@ are larger than the 129 MB L2, so no explicit flush is done.
             time = CUDA events on the engine stream around each step
     e2e     the same metric through the C ABI with host buffers: per step,
             fdtd_engine_create_compressed from the pinned compressed operator
-            (host -> device), fdtd_engine_iterate in probe-interval chunks
-            with each new probe/energy sample read back (device -> host),
-            fdtd_engine_destroy
+            (host -> device), fdtd_engine_iterate over all timesteps (the
+            probe / energy samples collect in the device ring), the sample
+            record read back (device -> host), fdtd_engine_destroy
     roofline  the dominant half-step kernel against the measured HBM copy
             bandwidth (MEASURED_PEAKS.json)
     cpu_baseline  the oracle's restated SSE-compressed multithreaded engine
@@ -392,18 +392,14 @@ def run_gpu(args, rank, world, local_rank):
     torch.cuda.synchronize()
     te = time.perf_counter()
     for _ in range(e2e_steps):
+        # one simulation through the API: upload the compressed operator,
+        # run all timesteps (the samples stay in the device ring), read the
+        # probe / energy record back
         e = Engine(cop, device=local_rank, max_timesteps=TIMESTEPS, **tiling)
-        done = 0
-        nread = 0
-        while done < TIMESTEPS:
-            k = min(e.interval, TIMESTEPS - done)
-            e.iterate(k)
-            done += k
-            n = e.num_samples()
-            if n > nread:
-                ts, vals, en = e.read_samples(nread, n - nread)
-                d2h += ts.nbytes + vals.nbytes + en.nbytes + 4
-                nread = n
+        e.iterate(TIMESTEPS)
+        n = e.num_samples()
+        ts, vals, en = e.read_samples(0, n)
+        d2h += ts.nbytes + vals.nbytes + en.nbytes + 4
         e.close()
     torch.cuda.synchronize()
     te = time.perf_counter() - te
