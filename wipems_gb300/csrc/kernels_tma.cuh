@@ -155,6 +155,24 @@ __device__ __forceinline__ bool tile_has_upml(const TileInfo& ti, int x, int y0,
     return false;
 }
 
+// A plane's place in the mbarrier ring: plane q of a block's running count
+// sits in stage q % STAGES and completes phase (q / STAGES) & 1 of that
+// stage's barrier.  The position is derived once per tile and then stepped
+// plane by plane, so the loops carry no integer division by the runtime
+// stage count.
+struct RingPos {
+    int s;
+    uint32_t ph;
+    __device__ __forceinline__ RingPos(uint32_t q, int stages)
+        : s((int)(q % (uint32_t)stages)), ph((q / (uint32_t)stages) & 1u) {}
+    __device__ __forceinline__ void next(int stages) {
+        if (++s == stages) {
+            s = 0;
+            ph ^= 1u;
+        }
+    }
+};
+
 // ------------------------------------------------------------- E half-step
 // One tile of the voltage update: the 32 x TY tile (bx, by) over the
 // x-chunk bz.  ring counts the planes this block has pushed through its
@@ -196,9 +214,7 @@ __device__ __forceinline__ bool volt_tile(const DevGrid& g, const TmaMaps& m, co
     const int zl = min(z0 + 31, g.Nz - 1), yl = min(y0 + TY - 1, g.Ny - 1);
     const uint32_t base = ring;
 
-    auto issue = [&](int r) {  // thread 0: plane x0+r into the ring
-        const uint32_t q = base + (uint32_t)r;
-        const int s = (int)(q % (uint32_t)STAGES);
+    auto issue = [&](int r, int s) {  // thread 0: plane x0+r into ring stage s
         const int x = x0 + r;
         float* st = smem + (size_t)s * L::STAGE;
         const bool up = UPML && tile_has_upml(ti, x, y0, yl, z0, zl);
@@ -217,7 +233,8 @@ __device__ __forceinline__ bool volt_tile(const DevGrid& g, const TmaMaps& m, co
     int issued = 0;
     if (tid == 0) {
         fence_proxy_async();
-        for (; issued < min(STAGES - 1, nplanes); ++issued) issue(issued);
+        for (RingPos ip(base, STAGES); issued < min(STAGES - 1, nplanes); ++issued, ip.next(STAGES))
+            issue(issued, ip.s);
     }
     float p1 = 0.f, p2 = 0.f;  // I1, I2 at x-1
     const long long yz = (long long)y * g.Nzp + z;
@@ -238,17 +255,17 @@ __device__ __forceinline__ bool volt_tile(const DevGrid& g, const TmaMaps& m, co
     float* Vp = g.V + (long long)x0 * g.sx + yz;  // node (x0, y, z), advanced by sx per plane
     bool aborted = false;
     int r = 0;
-    for (; r < nplanes; ++r, Vp += g.sx) {
+    RingPos cp(base, STAGES);  // stage of plane r
+    for (; r < nplanes; ++r, Vp += g.sx, cp.next(STAGES)) {
         if (tid == 0 && issued < nplanes && issued == r + STAGES - 1) {
+            // plane r + STAGES - 1 goes into the stage plane r - 1 freed
             fence_proxy_async();
-            issue(issued);
+            issue(issued, cp.s == 0 ? STAGES - 1 : cp.s - 1);
             ++issued;
         }
-        const uint32_t q = base + (uint32_t)r;
-        const int s = (int)(q % (uint32_t)STAGES);
-        const bool ok = mbar_wait(&bars[s], (q / (uint32_t)STAGES) & 1u);
+        const bool ok = mbar_wait(&bars[cp.s], cp.ph);
         const int x = x0 + r;
-        const float* st = smem + (size_t)s * L::STAGE;
+        const float* st = smem + (size_t)cp.s * L::STAGE;
         float c1 = 0.f, c2 = 0.f;
         if (ok && valid) {
             const int hi = (ty + 1) * HW + 4 + tz;  // own position in the halo box
@@ -332,9 +349,7 @@ __device__ __forceinline__ bool curr_tile(const DevGrid& g, const TmaMaps& m, co
     const int zl = min(z0 + 31, g.Nz - 1), yl = min(y0 + TY - 1, g.Ny - 1);
     const uint32_t base = ring;
 
-    auto issue = [&](int r) {
-        const uint32_t q = base + (uint32_t)r;
-        const int s = (int)(q % (uint32_t)STAGES);
+    auto issue = [&](int r, int s) {  // thread 0: plane x0+r into ring stage s
         const int x = x0 + r;
         float* st = smem + (size_t)s * L::STAGE;
         const bool upd = r < nplanes;  // plane x1 only contributes V
@@ -353,7 +368,8 @@ __device__ __forceinline__ bool curr_tile(const DevGrid& g, const TmaMaps& m, co
     int issued = 0;
     if (nplanes > 0 && tid == 0) {
         fence_proxy_async();
-        for (; issued < min(STAGES - 1, nload); ++issued) issue(issued);
+        for (RingPos ip(base, STAGES); issued < min(STAGES - 1, nload); ++issued, ip.next(STAGES))
+            issue(issued, ip.s);
     }
     const long long yz = (long long)y * g.Nzp + z;
     float gyE = 0.f, gyI = 0.f, gzE = 0.f, gzI = 0.f;  // dH / iM parts
@@ -367,17 +383,18 @@ __device__ __forceinline__ bool curr_tile(const DevGrid& g, const TmaMaps& m, co
     float* Ip = g.I + (long long)x0 * g.sx + yz;
     bool aborted = false;
     int r = 0;
-    for (; r < nplanes; ++r, Ip += g.sx) {
+    RingPos cp(base, STAGES);  // stage of plane r
+    for (; r < nplanes; ++r, Ip += g.sx, cp.next(STAGES)) {
         if (tid == 0 && issued < nload && issued == r + STAGES - 1) {
+            // plane r + STAGES - 1 goes into the stage plane r - 1 freed
             fence_proxy_async();
-            issue(issued);
+            issue(issued, cp.s == 0 ? STAGES - 1 : cp.s - 1);
             ++issued;
         }
-        const uint32_t q = base + (uint32_t)r;
-        const int s = (int)(q % (uint32_t)STAGES);
-        const int sn = (int)((q + 1) % (uint32_t)STAGES);
-        bool ok = mbar_wait(&bars[s], (q / (uint32_t)STAGES) & 1u);
-        ok = ok && mbar_wait(&bars[sn], ((q + 1) / (uint32_t)STAGES) & 1u);
+        const int s = cp.s;
+        const int sn = s + 1 == STAGES ? 0 : s + 1;  // plane r + 1 (its V is the x+1 neighbour)
+        bool ok = mbar_wait(&bars[s], cp.ph);
+        ok = ok && mbar_wait(&bars[sn], cp.ph ^ (uint32_t)(sn == 0));
         const int x = x0 + r;
         float ev[3] = {0.f, 0.f, 0.f}, eh[3] = {0.f, 0.f, 0.f};  // energy terms of this node
         if (ok && active) {
