@@ -489,8 +489,14 @@ __global__ void __launch_bounds__(TY * 32) k_curr_tma(const DevGrid g, const __g
     if (*g.d_done) return;
     init_ring(bars, STAGES);
     uint32_t ring = 0;
-    curr_tile<IdxT, FEAT, GEO, TY>(g, m, ti, blockIdx.x, blockIdx.y, blockIdx.z, XC, STAGES, smem, bars, ring,
-                                   *g.d_ts + ts_off, ENERGY);
+    // x-chunks in descending order: blocks are dispatched roughly in
+    // blockIdx order, and the voltage kernel before this one ended on the
+    // highest chunks, whose voltages (just written) and currents (just read)
+    // are still partly in L2.  The next voltage kernel, in ascending order,
+    // starts where this one ends.  No block reads what another block of the
+    // same kernel writes, so the order does not change any result.
+    curr_tile<IdxT, FEAT, GEO, TY>(g, m, ti, blockIdx.x, blockIdx.y, gridDim.z - 1 - blockIdx.z, XC, STAGES, smem,
+                                   bars, ring, *g.d_ts + ts_off, ENERGY);
 }
 
 // ---------------------------------------------------------- batched jobs
