@@ -75,7 +75,11 @@ int fdtd_scene_destroy(fdtd_scene_t scene);
 /* CSBackgroundMaterial (operator.cpp:825-830). */
 int fdtd_scene_set_background(fdtd_scene_t s, double eps_r, double mue_r,
                               double kappa, double sigma);
-/* bc[6] = xmin,xmax,ymin,ymax,zmin,zmax; pml_size[6] cells (PML_n).
+/* bc[6] = xmin,xmax,ymin,ymax,zmin,zmax; pml_size[6] cells (PML_n), read
+ * for PML faces only: every other face keeps openEMS's default size 8
+ * (openems.cpp:101), which openEMS's UPML build still uses for the opposite
+ * face's grading and the y/z slab ranges (operator_ext_upml.cpp:163,337).
+ * pml_size may be null (every PML face 8 cells).
  * openEMS::SetupBoundaryConditions (openems.cpp:380-406). */
 int fdtd_scene_set_boundary(fdtd_scene_t s, const int bc[6],
                             const uint32_t pml_size[6]);

@@ -1675,7 +1675,9 @@ int oracle_operator_build(const oracle_scene* S, int threads, oracle_operator_s*
     op->bg[3] = S->bg_sigma;
     for (int k = 0; k < 6; ++k) {
         op->BC[k] = S->bc[k];
-        op->pml[k] = S->bc[k] == 3 ? S->pml_size[k] : 0;
+        // a face that is not PML keeps openEMS's default size 8
+        // (openems.cpp:101), which Create_UPML / CalcGradingKappa still read
+        op->pml[k] = S->bc[k] == 3 ? S->pml_size[k] : 8;
         op->mur_vph[k] = S->mur_vph[k];
     }
     // openEMS::Parse_XML_FDTDSetup / Excitation::Setup* (openems.cpp:900-927,

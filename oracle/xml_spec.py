@@ -85,16 +85,13 @@ def xml_spec(path_or_text: str) -> dict:
     bcn = fdtd.find("BoundaryCond")
     if bcn is None:
         raise ValueError("<BoundaryCond> missing")
-    bc, pml = [0] * 6, [0] * 6
+    bc, pml = [0] * 6, [8] * 6  # openEMS's default PML size for every face
     for n, name in enumerate(_BNAMES):
         v = bcn.get(name)
         if v is None:
             continue
         try:
-            code = int(v)
-            bc[n] = code
-            if code == 3:
-                pml[n] = 8
+            bc[n] = int(v)  # a bare code keeps the default size
             continue
         except ValueError:
             pass

@@ -252,3 +252,54 @@ def test_device_axes_rotation_choice_and_expansion():
         assert all(np.array_equal(a, b) for a, b in zip(e0, c.expand()))
         assert all(np.array_equal(x0[h][k], c.expand_ext(h)[k]) for h in (0, 1) for k in (0, 1))
         assert c.info["num_tuples_e"] == ref.info["num_tuples_e"]
+
+
+def test_overlapping_upml_slabs_are_refused():
+    """openEMS ends its y and z UPML slabs size[0]+1 lines before the x-max
+    face (operator_ext_upml.cpp:163), size[0] being 8 when x-min is not PML
+    (openems.cpp:101), so an x-max UPML thicker than that makes them reach
+    into the x-max slab, where two UPML extensions would update the same
+    nodes.  The operator build keeps openEMS's ranges; the compressor refuses
+    the overlap with an error that says why."""
+    from wipems_gb300._abi import FdtdError
+    from wipems_gb300.fdtd import BC_PEC, BC_PML
+    lines = [scenes.uniform_lines(n, 1.0) for n in (40, 24, 12)]
+
+    def op(bc, size):
+        s = Scene(*lines, 1e-3)
+        s.set_boundary(bc, size)
+        s.set_gauss_excite(10e9, 10e9, 50)
+        return Operator(s)
+
+    y_pml = [BC_PML, BC_PEC, BC_PEC, BC_PEC]
+    for xbc, size in (([BC_PEC, BC_PML], [0, 10]), ([BC_PML, BC_PML], [3, 5])):
+        o = op(xbc + y_pml, size + [3, 0, 0, 0])
+        sl = [(list(o.desc.upml[k].start), list(o.desc.upml[k].num_lines)) for k in range(o.desc.num_upml)]
+        ymin = sl[-1]
+        x_min_size = size[0] if xbc[0] == BC_PML else 8
+        assert ymin[0][0] + ymin[1][0] - 1 == len(lines[0]) - 1 - (x_min_size + 1)  # the y slab's last x line
+        with pytest.raises(FdtdError, match="UPML slabs overlap"):
+            CompressedOperator(o)
+    # an x-max UPML no thicker than the x-min size (8 for PEC) leaves them disjoint
+    for xbc, size in (([BC_PEC, BC_PML], [0, 8]), ([BC_PML, BC_PML], [5, 5]), ([BC_PML, BC_PML], [6, 3])):
+        CompressedOperator(op(xbc + y_pml, size + [3, 0, 0, 0]))
+
+
+def test_pml_on_one_face_of_an_axis_grades_with_the_default_size():
+    """zmin PEC, zmax PML_8 (the reference's Coax test sets this): openEMS
+    grades the upper layer with dl = width / size[zmin], and size[zmin] is
+    its default 8 (operator_ext_upml.cpp:337, openems.cpp:101), so every
+    coefficient is finite -- in the product's build and in the oracle's."""
+    import oracle
+    from wipems_gb300.fdtd import BC_PEC, BC_PML
+    lines = [scenes.uniform_lines(n, 1.0) for n in (14, 12, 30)]
+    s = Scene(*lines, 1e-3)
+    s.set_boundary([BC_PEC] * 5 + [BC_PML], [0, 0, 0, 0, 0, 8])
+    s.set_gauss_excite(10e9, 10e9, 50)
+    o = Operator(s)
+    arrs = oracle.desc_arrays(o.desc)
+    assert all(np.isfinite(v).all() for v in arrs.values() if v.dtype.kind == "f")
+    ref = oracle.Operator(s.spec)
+    b = oracle.desc_arrays(ref.desc)
+    assert sorted(arrs) == sorted(b) and all(arrs[k].tobytes() == b[k].tobytes() for k in arrs)
+    CompressedOperator(o)

@@ -112,7 +112,16 @@ int prepare(const fdtd_op_desc* d, Plan& P) {
                     for (uint32_t z = 0; z < u.num_lines[2]; ++z) {
                         size_t gi = ((size_t)(x + u.start[0]) * Ny + (y + u.start[1])) * Nz + (z + u.start[2]);
                         if (P.slab[gi] >= 0) {
-                            set_error("UPML slabs overlap");
+                            // openEMS builds such slabs when the x-max UPML is
+                            // thicker than the x-min size (8 for a face that is
+                            // not PML): the y and z slabs end size[0]+1 lines
+                            // before the x-max face (operator_ext_upml.cpp:163),
+                            // so they run into the x-max slab and both
+                            // extensions update the nodes they share.  One UPML
+                            // update per node is all the fused kernels do.
+                            set_error("UPML slabs overlap (the x-max UPML is thicker than the x-min size -- 8 for a "
+                                      "face that is not PML -- so the y/z slabs reach into it, as openEMS builds "
+                                      "them); keep the x-max UPML no thicker than that");
                             return FDTD_ERR_ARG;
                         }
                         P.slab[gi] = (int8_t)s;

@@ -76,7 +76,7 @@ struct fdtd_scene_s {
     double unit = 1;
     double bg_eps = 1, bg_mue = 1, bg_kappa = 0, bg_sigma = 0;
     int bc[6] = {0, 0, 0, 0, 0, 0};
-    uint32_t pml_size[6] = {0, 0, 0, 0, 0, 0};
+    uint32_t pml_size[6] = {8, 8, 8, 8, 8, 8};  // openEMS default (openems.cpp:101)
     double mur_vph[6] = {0, 0, 0, 0, 0, 0};
     double f0 = 0, fc = 0;
     // Excitation::ExciteTypes (excitation.h:28): 0 Gaussian pulse,

@@ -1656,7 +1656,11 @@ int fdtd_scene_set_boundary(fdtd_scene_t s, const int bc[6], const uint32_t pml_
             return FDTD_ERR_ARG;
         }
         s->bc[i] = bc[i];
-        s->pml_size[i] = (bc[i] == FDTD_BC_PML && pml_size) ? pml_size[i] : 0;
+        // openEMS gives every face a PML size of 8 (openems.cpp:101) and
+        // changes it only for PML_n faces; its UPML build reads the size of a
+        // face that is not PML too (the grading of the opposite face,
+        // operator_ext_upml.cpp:337, and the y/z slab ranges, :163)
+        s->pml_size[i] = (bc[i] == FDTD_BC_PML && pml_size) ? pml_size[i] : 8;
     }
     return FDTD_OK;
 }

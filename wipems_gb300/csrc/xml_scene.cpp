@@ -350,7 +350,7 @@ int fdtd_scene_load_xml(const char* text, fdtd_scene_t* out, fdtd_xml_info* info
     inf.f0 = f0;
     inf.fc = fc;
     int bc[6] = {0, 0, 0, 0, 0, 0};
-    uint32_t pml[6] = {0, 0, 0, 0, 0, 0};
+    uint32_t pml[6] = {8, 8, 8, 8, 8, 8};  // openEMS's default for every face (openems.cpp:101)
     const XNode* bcn = fdtd->child("BoundaryCond");
     if (!bcn) L.bad(FDTD_ERR_ARG, "<FDTD> has no <BoundaryCond> (openems.cpp:835-840)");
     const char* bnames[6] = {"xmin", "xmax", "ymin", "ymax", "zmin", "zmax"};
@@ -360,7 +360,6 @@ int fdtd_scene_load_xml(const char* text, fdtd_scene_t* out, fdtd_xml_info* info
         double code;
         if (to_double(*v, code)) {
             bc[n] = (int)code;
-            if (bc[n] == 3) pml[n] = 8;  // a bare 3 keeps the default 8-cell PML (openems.cpp:101)
         } else if (*v == "PEC") {
             bc[n] = 0;
         } else if (*v == "PMC") {
