@@ -168,3 +168,138 @@ def test_random_scenes_in_one_batch_match_oracle():
     for op, eng, ref in zip(ops, jobs, refs):
         assert eng.num_timesteps == NR_TS
         compare(op, eng, ref)
+
+
+# ------------------------------------------------------------------ the wider sweep
+EXT_SEEDS = list(range(200, 212))
+
+
+def random_scene_ext(seed: int) -> Scene:
+    """The extensions around the hot path, drawn at random: Mur faces, one
+    signal of the reference's five (Gaussian, sinusoid, Dirac, step, custom
+    function of t), soft excitations with random vectors, lumped RLC
+    elements (series or parallel), Lorentz / Drude of dispersion order 2,
+    voltage lines and current loops.  Placements keep to what the engine
+    provides: no Lorentz / Drude or excitation within a line of a Mur face,
+    no RLC element on an excited edge or inside a Lorentz / Drude brick."""
+    from wipems_gb300.fdtd import BC_MUR
+    rng = np.random.default_rng(seed)
+    cells = [int(rng.integers(14, 45)) for _ in range(3)]
+    delta = float(rng.choice([0.5, 1.0]))
+    lines = [uniform_lines(c, delta) for c in cells]
+    s = Scene(*lines, 1e-3)
+    bc, pml = [], []
+    for a in range(3):
+        r = rng.random()
+        if r < 0.3 and cells[a] >= 18:
+            k = int(rng.integers(2, min(6, (cells[a] - 14) // 2) + 1))
+            bc += [BC_PML, BC_PML]
+            pml += [k, k]
+        else:
+            bc += [int(rng.choice([BC_PEC, BC_PMC, BC_MUR, BC_MUR])) for _ in range(2)]
+            pml += [0, 0]
+    s.set_boundary(bc, pml)
+    nts = NR_TS
+    f0 = float(rng.uniform(3e9, 15e9))
+    kind = int(rng.integers(0, 5))
+    if kind == 0:
+        s.set_gauss_excite(f0, f0, nts)
+    elif kind == 1:
+        s.set_sinus_excite(f0, nts)
+    elif kind == 2:
+        s.set_dirac_excite(f0, nts)
+    elif kind == 3:
+        s.set_step_excite(f0, nts)
+    else:
+        s.set_custom_excite(f"sin(2*pi*{f0:.6g}*t)*exp(-((t-2e-10)/8e-11)^2)", f0, nts)
+    # margins: 3 lines from a Mur face or the UPML for everything placed inside
+    lo = [(pml[2 * a] + 1) if bc[2 * a] == BC_PML else 3 for a in range(3)]
+    hi = [(cells[a] - pml[2 * a + 1] - 1) if bc[2 * a + 1] == BC_PML else cells[a] - 3 for a in range(3)]
+    prio = 10
+    for _ in range(int(rng.integers(0, 4))):
+        start, stop = _box(rng, lines, lo, hi, 8)
+        s.add_material(start, stop, eps_r=float(rng.uniform(1, 8)),
+                       kappa=float(math.exp(rng.uniform(math.log(1e-4), 0.0))) if rng.random() < 0.5 else 0.0,
+                       priority=prio)
+        prio += 1
+    disp_boxes = []
+    if rng.random() < 0.5:
+        start, stop = _box(rng, lines, lo, hi, 6)
+        fL = float(rng.uniform(4e9, 12e9))
+        s.add_lorentz(start, stop, eps_r=2.0, plasma_f=[fL, float(rng.uniform(3e9, 8e9))], relax_t=[1e-9, 2e-9],
+                      pole_f=[fL * 0.8, 0.0], priority=prio)
+        disp_boxes.append((start, stop))
+        prio += 1
+
+    def inside(p, box):
+        return all(box[0][a] <= p[a] <= box[1][a] for a in range(3))
+
+    def pick_edge():
+        """A z/y/x edge at least two lines inside the margins and clear of
+        the Lorentz / Drude bricks."""
+        for _ in range(100):
+            d = int(rng.integers(0, 3))
+            c = [int(rng.integers(lo[a] + 2, max(lo[a] + 3, hi[a] - 2))) for a in range(3)]
+            p0 = [float(lines[a][c[a]]) for a in range(3)]
+            p1 = list(p0)
+            p1[d] = float(lines[d][c[d] + 1])
+            if not any(inside(p0, b) or inside(p1, b) for b in disp_boxes):
+                return d, c, p0, p1
+        raise RuntimeError("no free edge")
+
+    used = set()
+    d, c, p0, p1 = pick_edge()  # a soft excitation on one edge, random vector
+    vec = [0.0, 0.0, 0.0]
+    vec[d] = float(rng.choice([-1.0, 1.0])) * float(rng.uniform(0.5, 2.0))
+    s.add_excitation(p0, p1, vec, priority=500)
+    used.add(tuple(c))
+    s.add_probe(p0, p1, 0, name="v_exc")
+    for k in range(int(rng.integers(0, 3))):
+        d, c, p0, p1 = pick_edge()
+        if tuple(c) in used:
+            continue
+        used.add(tuple(c))
+        series = bool(rng.random() < 0.5)
+        # a series element whose impedance at the signal's maximum frequency
+        # is far above the edge's own capacitance gets that capacitance cut
+        # to 1/20 of its impedance (operator_ext_lumpedRLC.cpp:357-364) after
+        # the timestep is fixed, and grows; series elements stay low-ohmic
+        R = float(rng.uniform(5, 40)) if series else float(rng.uniform(10, 200))
+        s.add_lumped_rlc(p0, p1, d, R=R, L=float(rng.uniform(0.1e-9, 1e-9)) if series else float(rng.uniform(0.5e-9, 5e-9)),
+                         Cap=float(rng.uniform(1e-12, 5e-12)) if series else float(rng.uniform(0.1e-12, 2e-12)),
+                         series=series, caps=False, priority=900 + k)
+        s.add_probe(p0, p1, 0, name=f"v_rlc{k}")
+    # a current loop around a random edge and the field at a random node
+    d, c, p0, p1 = pick_edge()
+    half = [0.5 * (lines[a][c[a]] + lines[a][c[a] + 1]) for a in range(3)]
+    a_lo = [float(lines[a][c[a]]) - 0.5 * delta for a in range(3)]
+    a_hi = [float(lines[a][c[a]]) + 0.5 * delta for a in range(3)]
+    a_lo[d] = a_hi[d] = half[d]
+    s.add_probe(a_lo, a_hi, 1, norm_dir=d, name="i_loop")
+    q = [float(lines[a][int(rng.integers(0, len(lines[a])))]) for a in range(3)]
+    s.add_probe(q, q, int(rng.choice([2, 3])), name="field")
+    return s
+
+
+@pytest.mark.parametrize("seed", EXT_SEEDS)
+def test_random_extension_scene_matches_oracle(seed):
+    """The wider sweep, with a checkpoint taken mid-run and restored into a
+    fresh engine for half of the seeds: bit-identical to the oracle."""
+    op = Operator(random_scene_ext(seed))
+    ref = _reference(op, seed)
+    cop = CompressedOperator(op)
+    rng = np.random.default_rng(1000 + seed)
+    kw = _engine_options(rng)
+    eng = Engine(cop, **kw)
+    parts = _splits(rng, NR_TS)
+    if rng.random() < 0.5 and len(parts) > 1:
+        eng.iterate(parts[0])
+        blob = eng.checkpoint()
+        eng.close()
+        eng = Engine(cop, **kw)
+        eng.restore(blob)
+        parts = parts[1:]
+    for n in parts:
+        eng.iterate(n)
+    assert eng.num_timesteps == NR_TS
+    compare(op, eng, ref)
