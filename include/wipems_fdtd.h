@@ -708,7 +708,9 @@ typedef struct {
 } fdtd_server_opts;
 
 typedef struct {
-    double   end_crit;        /* energy decay stop, e.g. 1e-4 = -40 dB (0 = off) */
+    double   end_crit;        /* energy decay stop, e.g. 1e-4 = -40 dB (0 = off:
+                                 the job runs exactly max_timesteps; such jobs
+                                 run as concurrent engines, not in batches) */
     uint32_t max_timesteps;   /* timestep cap (0 = the scene's NrTS) */
     uint32_t probe_interval;  /* 0 = the operator's Nyquist-derived interval */
     int      keep_fields;     /* copy the final fields to the host at retirement */

@@ -303,3 +303,35 @@ def test_random_extension_scene_matches_oracle(seed):
         eng.iterate(n)
     assert eng.num_timesteps == NR_TS
     compare(op, eng, ref)
+
+
+class _ServedJob:
+    """A served job's results with the Engine methods compare() reads."""
+
+    def __init__(self, srv, jid):
+        self.srv, self.jid = srv, jid
+
+    def samples(self):
+        return self.srv.samples(self.jid)
+
+    def fields(self):
+        return self.srv.fields(self.jid)
+
+
+def test_random_scenes_through_the_server_match_oracle():
+    """Both sweeps as one stream through the server, with persistent-batch
+    rounds for the jobs a batch takes and plain engines beside them for the
+    rest (Mur faces, lumped RLC, dispersion of order 2): every job's samples
+    and fields equal the oracle's."""
+    from wipems_gb300 import Server
+    cases = [(s, lambda s=s: random_scene(s)) for s in SEEDS] + [(s, lambda s=s: random_scene_ext(s)) for s in EXT_SEEDS]
+    srv = Server(round_steps=41, build_workers=2, batch_min_jobs=3)
+    ids = {seed: srv.submit(make(), keep_fields=True) for seed, make in cases}
+    srv.wait(0, timeout=600)
+    st = srv.stats()
+    assert st["jobs_done"] == len(ids) and st["jobs_failed"] == 0
+    for seed, make in cases:
+        op = Operator(make())
+        assert srv.status(ids[seed])["timesteps"] == NR_TS
+        compare(op, _ServedJob(srv, ids[seed]), _reference(op, seed))
+    srv.close()

@@ -149,3 +149,26 @@ def test_server_serves_an_xml_scene():
     _same(e, srv, jid)
     assert srv.samples(jid).probe_types == e.samples().probe_types
     srv.close()
+
+
+def test_server_job_without_end_criterion_runs_its_timesteps():
+    """A job submitted without an energy criterion runs exactly its scene's
+    NumberOfTimesteps (or max_timesteps), whatever the round length, in
+    batch mode too (such jobs run beside the batch), and equals the plain
+    engine run for that many timesteps."""
+    srv = Server(round_steps=37, batch_min_jobs=2)
+    ids = {}
+    for seed in (3, 4):
+        for k in ("upml", "drude"):
+            ids[(k, seed, 0)] = srv.submit(scenes.mini(k, seed=seed, nr_ts=250), keep_fields=True)
+            ids[(k, seed, 1)] = srv.submit(scenes.mini(k, seed=seed, nr_ts=250), max_timesteps=111,
+                                           keep_fields=True)
+    srv.wait(0, timeout=600)
+    st = srv.stats()
+    assert st["jobs_done"] == len(ids) and st["jobs_failed"] == 0
+    for (k, seed, capped), jid in ids.items():
+        n = 111 if capped else 250
+        e = Engine(Operator(scenes.mini(k, seed=seed, nr_ts=250)), max_timesteps=n)
+        e.iterate(n)
+        _same(e, srv, jid)
+    srv.close()

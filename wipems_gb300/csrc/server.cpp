@@ -424,8 +424,11 @@ void gpu_loop(fdtd_server_s* s) {
         std::vector<Job*> bjobs, solo;
         if (s->opts.batch_min_jobs > 0) {
             for (Job* j : s->active) {
+                // a batch steps its jobs together; a job without an energy
+                // criterion is bounded by its timestep count alone, which the
+                // host keeps (the rounds below), so it runs on its own
                 int ok = 0;
-                fdtd_batch_accepts(j->eng, &ok);
+                if (j->opts.end_crit > 0) fdtd_batch_accepts(j->eng, &ok);
                 (ok ? bjobs : solo).push_back(j);
             }
             if (bjobs.size() < s->opts.batch_min_jobs) {
@@ -452,12 +455,21 @@ void gpu_loop(fdtd_server_s* s) {
             }
             int rc = fdtd_engine_wait(j->eng);  // collects steps that finished since the pass above
             int done = 0;
+            uint32_t steps = s->opts.round_steps;
             if (!rc) fdtd_engine_done(j->eng, &done);
+            if (!rc && !done && j->opts.end_crit <= 0) {
+                // no energy criterion: the job ends after its max_ts
+                // timesteps (NumberOfTimesteps), and no round passes them
+                uint32_t ts = 0;
+                fdtd_engine_num_timesteps(j->eng, &ts);
+                if (ts >= j->max_ts) done = 1;
+                else steps = std::min(steps, j->max_ts - ts);
+            }
             if (!rc && done) {
                 retire(s, j, FDTD_OK, "");
                 continue;
             }
-            if (!rc) rc = fdtd_engine_iterate_async(j->eng, s->opts.round_steps);
+            if (!rc) rc = fdtd_engine_iterate_async(j->eng, steps);
             if (rc) {
                 retire(s, j, rc, last_error());
                 continue;
