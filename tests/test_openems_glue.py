@@ -92,6 +92,20 @@ def test_bridge_rebuilds_the_description_bitwise(kind):
         assert a[k].tobytes() == c[k].tobytes(), k
 
 
+@pytest.mark.parametrize("seed", [0, 1, 5, 8, 10, 13, 200, 202, 204, 207, 209, 211])
+def test_bridge_rebuilds_random_scenes_bitwise(seed):
+    """The seeded random scenes (UPML per axis, Lorentz / Drude of both
+    families and of order 2, Mur faces, lumped RLC) through openEMS-layout
+    pointer trees and the bridge: the same description, array for array."""
+    from test_random_gpu import random_scene, random_scene_ext
+    op = Operator(random_scene_ext(seed) if seed >= 200 else random_scene(seed))
+    b = BridgedOperator(op)
+    a, c = oracle.desc_arrays(op.desc), oracle.desc_arrays(b.desc)
+    assert sorted(a) == sorted(c)
+    for k in a:
+        assert a[k].tobytes() == c[k].tobytes(), k
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("kind", ["upml", "mixed", "rlc_mur", "magnetic"])
 def test_engine_from_the_bridged_description_matches_oracle(kind):
