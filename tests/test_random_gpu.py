@@ -158,11 +158,18 @@ def test_random_scene_matches_oracle(seed):
     compare(op, eng, ref, bitwise=not cop.factorized)
 
 
-def test_random_scenes_in_one_batch_match_oracle():
+@pytest.mark.parametrize("cfg", [dict(graph_steps=8, chains=2),
+                                 dict(graph_steps=1, tile_y=4, blocks_per_sm=2, x_chunk=5, stages=4),
+                                 dict(graph_steps=16, tile_y=8, blocks_per_sm=-1, chains=3, x_chunk=32),
+                                 dict(graph_steps=5, tile_y=4, blocks_per_sm=-1, x_chunk=2, stages=6)])
+def test_random_scenes_in_one_batch_match_oracle(cfg):
+    """The uniform random scenes as one batch, under persistent and
+    one-block-per-item schedules, both tile heights, job-range chains and
+    several x-chunks, stage counts and graph lengths."""
     ops = [Operator(random_scene(seed)) for seed in SEEDS]
     refs = [_reference(op, seed) for op, seed in zip(ops, SEEDS)]
     jobs = [Engine(CompressedOperator(op), kernel="tma") for op in ops]
-    b = Batch(jobs, graph_steps=8, chains=2)
+    b = Batch(jobs, **cfg)
     b.iterate(NR_TS - 41)
     b.iterate(41)
     for op, eng, ref in zip(ops, jobs, refs):
