@@ -342,3 +342,26 @@ def test_random_scenes_through_the_server_match_oracle():
         assert srv.status(ids[seed])["timesteps"] == NR_TS
         compare(op, _ServedJob(srv, ids[seed]), _reference(op, seed))
     srv.close()
+
+
+@pytest.mark.parametrize("seed", SEEDS[:4] + EXT_SEEDS[:6])
+def test_random_fd_accumulation_matches_oracle_dft(seed):
+    """Frequency-domain accumulation on the device (integral and field
+    probes) in random scenes and tilings against the DFT over the oracle's
+    samples at the FD steps."""
+    op = Operator(random_scene_ext(seed) if seed in EXT_SEEDS else random_scene(seed))
+    rng = np.random.default_rng(3000 + seed)
+    eng = Engine(CompressedOperator(op), **_engine_options(rng))
+    freqs = eng.set_frequencies(np.linspace(1e9, float(rng.uniform(5e9, 15e9)), 7))
+    fdint = eng.fd_interval
+    for n in _splits(rng, NR_TS):
+        eng.iterate(n)
+    got, count = eng.fd_results()
+    ref = oracle.run(*oracle_inputs(op), NR_TS, fdint, engine=oracle.BASIC)
+    assert count == len(ref["ts"]) == NR_TS // fdint + 1
+    dual = np.array([0.5 if t in (1, 3) else 0.0 for t in eng.probe_types])
+    t = (ref["ts"][:, None] + dual[None, :]) * op.dT
+    phase = np.exp(-2j * np.pi * freqs[None, None, :] * t[:, :, None])
+    want = np.einsum("sp,spf->pf", ref["values"], phase) * 2 * op.dT * fdint
+    scale = max(np.abs(want).max(), 1e-300)
+    assert np.max(np.abs(got - want)) <= 1e-12 * scale
