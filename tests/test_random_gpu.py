@@ -365,3 +365,31 @@ def test_random_fd_accumulation_matches_oracle_dft(seed):
     want = np.einsum("sp,spf->pf", ref["values"], phase) * 2 * op.dT * fdint
     scale = max(np.abs(want).max(), 1e-300)
     assert np.max(np.abs(got - want)) <= 1e-12 * scale
+
+
+@pytest.mark.parametrize("seed", SEEDS[:3] + GRADED_SEEDS[:2] + EXT_SEEDS[:3])
+def test_random_field_dumps_equal_reference_interpolation(seed):
+    """Field dumps of random boxes (corners in either order, sub-sampling
+    steps 1 to 4, boxes on the boundary lines) after a random run: E and H
+    with no, node and cell interpolation equal the reference interpolation
+    (engine_interface_fdtd.cpp:60-200, restated in tests/helpers.py) of the
+    engine's own fields, bit for bit."""
+    from helpers import dump_reference
+    graded = seed in GRADED_SEEDS
+    op = Operator(random_scene_ext(seed) if seed in EXT_SEEDS else random_scene(seed, graded=graded))
+    rng = np.random.default_rng(4000 + seed)
+    eng = Engine(CompressedOperator(op), **_engine_options(rng))
+    eng.iterate(int(rng.integers(20, NR_TS)))
+    V, I = eng.fields()
+    lines = [np.ctypeslib.as_array(op.desc.lines[a], shape=(op.num_lines[a],)).copy() for a in range(3)]
+    unit, N = float(op.desc.unit), op.num_lines
+    for _ in range(6):
+        a = [int(rng.integers(0, n)) for n in N]
+        b = [int(rng.integers(0, n)) for n in N]
+        step = tuple(int(rng.integers(1, 5)) for _ in range(3))
+        for field in ("E", "H"):
+            for interp in ("none", "node", "cell"):
+                got = eng.dump_field(field, interp, tuple(a), tuple(b), step)
+                ref = dump_reference(V, I, lines, unit, field, interp, tuple(a), tuple(b), step)
+                assert got.shape == ref.shape, (field, interp, a, b, step)
+                assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (field, interp, a, b, step)
