@@ -393,3 +393,43 @@ def test_random_field_dumps_equal_reference_interpolation(seed):
                 ref = dump_reference(V, I, lines, unit, field, interp, tuple(a), tuple(b), step)
                 assert got.shape == ref.shape, (field, interp, a, b, step)
                 assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (field, interp, a, b, step)
+
+
+@pytest.mark.parametrize("stream_seed", [0, 1])
+def test_random_server_stream_equals_solo_runs(stream_seed):
+    """A random stream through the server under load: random scenes of both
+    sweeps with their own timestep counts, half of them with an energy
+    criterion, an HBM budget that holds only part of the stream (admission
+    waits for retirements), batch rounds, a random round length and tile
+    share.  Every job ends exactly as the plain engine does with the same
+    settings alone: stopping timestep, samples, energies and fields."""
+    from wipems_gb300 import Server
+    from test_server_gpu import _same
+    rng = np.random.default_rng(7000 + stream_seed)
+    picks = rng.permutation(SEEDS + EXT_SEEDS)[:18]
+    jobs = []
+    for s in picks:
+        s = int(s)
+        nts = int(rng.integers(60, 400))
+        crit = float(rng.choice([0.0, 1e-2, 1e-3]))
+        jobs.append((s, nts, crit))
+
+    def make(s, nts):  # the run length is the job's max_timesteps (nts), on both sides
+        return random_scene_ext(s) if s in EXT_SEEDS else random_scene(s)
+
+    probe = Server(max_active=1)
+    j0 = probe.submit(make(*jobs[0][:2]), max_timesteps=jobs[0][1])
+    probe.wait(j0, timeout=300)
+    foot = probe.status(j0)["footprint"]
+    probe.close()
+    srv = Server(hbm_budget=int(6 * foot), round_steps=int(rng.integers(17, 90)), build_workers=2,
+                 batch_min_jobs=3, tile_share=int(rng.choice([2, 4, 8])))
+    ids = [srv.submit(make(s, nts), end_crit=crit, max_timesteps=nts, keep_fields=True) for s, nts, crit in jobs]
+    srv.wait(0, timeout=900)
+    st = srv.stats()
+    assert st["jobs_done"] == len(ids) and st["jobs_failed"] == 0
+    for (s, nts, crit), jid in zip(jobs, ids):
+        e = Engine(Operator(make(s, nts)), end_crit=crit, max_timesteps=nts)
+        e.iterate(nts)
+        _same(e, srv, jid)
+    srv.close()
