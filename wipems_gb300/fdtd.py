@@ -85,6 +85,11 @@ class SceneSpec:
         self._record(background=(float(eps_r), float(mue_r), float(kappa), float(sigma)))
 
     def set_boundary(self, bc, pml_size=(0,) * 6):
+        """Boundary per face (xmin, xmax, ymin, ymax, zmin, zmax): BC_PEC,
+        BC_PMC, BC_MUR or BC_PML, with pml_size the layers of each PML face.
+        A face that is not PML counts as 8 layers, openEMS's default, which
+        openEMS's UPML build still reads: in the grading of a UPML on the
+        opposite face and in the extent of the y / z slabs."""
         self._record(bc=[int(x) for x in bc], pml_size=[int(x) for x in pml_size])
 
     def set_mur_velocity(self, v_phase):
