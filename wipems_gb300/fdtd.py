@@ -84,12 +84,13 @@ class SceneSpec:
     def set_background(self, eps_r=1.0, mue_r=1.0, kappa=0.0, sigma=0.0):
         self._record(background=(float(eps_r), float(mue_r), float(kappa), float(sigma)))
 
-    def set_boundary(self, bc, pml_size=(0,) * 6):
+    def set_boundary(self, bc, pml_size=(8,) * 6):
         """Boundary per face (xmin, xmax, ymin, ymax, zmin, zmax): BC_PEC,
-        BC_PMC, BC_MUR or BC_PML, with pml_size the layers of each PML face.
-        A face that is not PML counts as 8 layers, openEMS's default, which
-        openEMS's UPML build still reads: in the grading of a UPML on the
-        opposite face and in the extent of the y / z slabs."""
+        BC_PMC, BC_MUR or BC_PML, with pml_size the layers of each PML face
+        (8 by default, openEMS's size for a bare PML code).  A face that is
+        not PML counts as 8 layers, openEMS's default, which openEMS's UPML
+        build still reads: in the grading of a UPML on the opposite face and
+        in the extent of the y / z slabs."""
         self._record(bc=[int(x) for x in bc], pml_size=[int(x) for x in pml_size])
 
     def set_mur_velocity(self, v_phase):
@@ -309,7 +310,7 @@ class Scene(SceneSpec):
         check(lib().fdtd_scene_set_background(self._h, eps_r, mue_r, kappa, sigma), "set_background")
         super().set_background(eps_r, mue_r, kappa, sigma)
 
-    def set_boundary(self, bc, pml_size=(0,) * 6):
+    def set_boundary(self, bc, pml_size=(8,) * 6):
         b = (C.c_int * 6)(*bc)
         s = (C.c_uint32 * 6)(*pml_size)
         check(lib().fdtd_scene_set_boundary(self._h, b, s), "set_boundary")
