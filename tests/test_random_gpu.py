@@ -433,3 +433,29 @@ def test_random_server_stream_equals_solo_runs(stream_seed):
         e.iterate(nts)
         _same(e, srv, jid)
     srv.close()
+
+
+def test_random_scenes_on_the_fused_kernel_match_oracle():
+    """The optional single-pass kernel (kernel="fused": uniform meshes
+    without Lorentz / Drude, Mur or lumped RLC) on the random scenes it
+    takes, with random x-chunks, stage counts and run splits: bitwise."""
+    import copy
+    from wipems_gb300 import SceneSpec
+    ran = 0
+    for seed in SEEDS:
+        spec = copy.deepcopy(random_scene(seed).spec)  # the scene without its Lorentz / Drude bricks
+        spec["prims"] = [p for p in spec["prims"] if not p.get("disp_order")]
+        sp = SceneSpec(*spec["lines"], spec["unit"])
+        sp.spec = spec
+        op = Operator(Scene.from_spec(sp))
+        cop = CompressedOperator(op)
+        if cop.factorized or cop.info["num_ade_nodes"]:
+            continue
+        rng = np.random.default_rng(6000 + seed)
+        eng = Engine(cop, kernel="fused", x_chunk=int(rng.integers(1, 17)), stages=int(rng.integers(3, 6)),
+                     use_graphs=bool(rng.random() < 0.5))
+        for n in _splits(rng, NR_TS):
+            eng.iterate(n)
+        compare(op, eng, _reference(op, ("no dispersion", seed)))
+        ran += 1
+    assert ran >= 12
