@@ -58,6 +58,7 @@
 #include <cstdint>
 #include <cstring>
 #include <memory>
+#include <new>
 #include <string>
 #include <thread>
 #include <vector>
@@ -1050,7 +1051,10 @@ struct oracle_operator_s {
     }
 
     // Operator_Ext_UPML::Create_UPML (operator_ext_upml.cpp:77-201), Cartesian part
-    void CreateUPML() {
+    // false when a slab's range leaves the grid: the reference computes the
+    // ranges in unsigned arithmetic, so the y / z slabs of a grid with fewer
+    // than size[0]+2 x-lines (size[0] = 8 when x-min is not PML) wrap around
+    bool CreateUPML() {
         int BC[6];
         uint32_t size[6];
         for (int k = 0; k < 6; ++k) {
@@ -1086,6 +1090,10 @@ struct oracle_operator_s {
         stop[1] = N[1] - 1 - (size[3] + 1) * (BC[3] == 3);
         if (BC[4] == 3) { start[2] = 0; stop[2] = size[4]; add(); }
         if (BC[5] == 3) { start[2] = N[2] - 1 - size[5]; stop[2] = N[2] - 1; add(); }
+        for (const UpmlSlabO& s : upml)
+            for (int n = 0; n < 3; ++n)
+                if (s.nl[n] == 0 || (uint64_t)s.start[n] + s.nl[n] > N[n]) return false;
+        return true;
     }
 
     // default grading function " -log(1e-6)*log(2.5)/(2*dl*Z*(pow(2.5,W/dl)-1)) * pow(2.5, D/dl) "
@@ -1635,7 +1643,7 @@ struct oracle_operator_s {
             BuildMur(M);
             mur.push_back(std::move(M));
         }
-        CreateUPML();
+        if (!CreateUPML()) return -3;
         for (UpmlSlabO& u : upml) BuildUPML(u);
         bool have_lorentz = false;
         for (const oracle_prim& p : csx.P)
@@ -1693,7 +1701,12 @@ int oracle_operator_build(const oracle_scene* S, int threads, oracle_operator_s*
     op->threads = threads > 0 ? threads : (int)std::max(1u, std::thread::hardware_concurrency());
     op->csx.P.assign(S->prims, S->prims + S->num_prims);
     op->csx.init();
-    if (op->build() != 0) return -2;
+    try {
+        const int rc = op->build();
+        if (rc != 0) return rc == -3 ? -3 : -2;
+    } catch (const std::bad_alloc&) {
+        return -4;
+    }
     *out = op.release();
     return 0;
 }

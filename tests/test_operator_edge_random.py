@@ -1,0 +1,110 @@
+"""Seeded hostile scenes for the two operator builds: boxes reaching out of
+the grid or lying wholly outside it, corners given in either order,
+zero-thickness sheets and single lines, primitives tied on priority (the
+first added wins), extreme material values (large epsilon, kappa and sigma,
+metal-like conductors), probes outside the grid or degenerate, excitations
+with zero components and delays.  The product's operator build
+and the oracle's independent one must agree on every array, dT and every
+snapped probe, or both refuse the scene.  CPU only."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from wipems_gb300 import Operator, Scene
+from wipems_gb300._abi import FdtdError
+from wipems_gb300.fdtd import BC_MUR, BC_PEC, BC_PMC, BC_PML
+from wipems_gb300.scenes import graded_lines, uniform_lines
+
+from helpers import assert_same_operator
+
+pytestmark = pytest.mark.usefixtures("libs")
+
+
+def _coord(rng, ln, margin=3):
+    """A coordinate on a line, between lines, or beyond the grid."""
+    r = rng.random()
+    lo, hi = float(ln[0]), float(ln[-1])
+    if r < 0.55:
+        return float(ln[int(rng.integers(0, len(ln)))])
+    if r < 0.85:
+        k = int(rng.integers(0, len(ln) - 1))
+        return float(ln[k] + rng.uniform(0.05, 0.95) * (ln[k + 1] - ln[k]))
+    span = hi - lo
+    return float(rng.choice([lo - rng.uniform(0.1, 0.3) * span, hi + rng.uniform(0.1, 0.3) * span]))
+
+
+def _box(rng, lines):
+    a = [_coord(rng, ln) for ln in lines]
+    b = [_coord(rng, ln) for ln in lines]
+    for k in range(3):
+        r = rng.random()
+        if r < 0.15:
+            b[k] = a[k]            # a sheet (or a line, or a point)
+    return a, b
+
+
+def hostile_scene(seed: int) -> Scene:
+    rng = np.random.default_rng(seed)
+    cells = [int(rng.integers(4, 26)) for _ in range(3)]
+    if rng.random() < 0.3:
+        lines = [graded_lines(c, rng) for c in cells]
+    else:
+        lines = [uniform_lines(c, float(rng.choice([0.25, 1.0]))) for c in cells]
+    s = Scene(*lines, 1e-3)
+    bc = [int(rng.choice([BC_PEC, BC_PMC, BC_MUR, BC_PML])) for _ in range(6)]
+    pml = [int(rng.integers(1, 6)) if b == BC_PML else 0 for b in bc]
+    s.set_boundary(bc, pml)
+    if rng.random() < 0.3:
+        s.set_background(eps_r=float(rng.uniform(1, 4)), kappa=float(rng.uniform(0, 1e-3)))
+    f0 = float(rng.uniform(1e9, 30e9))
+    s.set_gauss_excite(f0, f0 * float(rng.uniform(0.3, 1.0)), 100)
+    prio = lambda: int(rng.integers(-3, 4))  # noqa: E731  (ties on purpose)
+    for _ in range(int(rng.integers(1, 9))):
+        a, b = _box(rng, lines)
+        r = rng.random()
+        if r < 0.2:
+            s.add_metal(a, b, priority=prio())
+        elif r < 0.35:
+            s.add_material(a, b, eps_r=float(rng.choice([1.0, 80.0, 1e4])), kappa=float(rng.choice([0.0, 1e3, 5e7])),
+                           mue_r=float(rng.choice([1.0, 50.0])), sigma=float(rng.choice([0.0, 1e4])), priority=prio())
+        elif r < 0.5:
+            fp = float(rng.uniform(1e9, 2e10))
+            s.add_lorentz(a, b, eps_r=float(rng.uniform(1, 5)), plasma_f=[fp], relax_t=[float(rng.uniform(1e-11, 1e-8))],
+                          pole_f=[float(rng.choice([0.0, fp / 2]))], priority=prio())
+        else:
+            s.add_material(a, b, eps_r=float(rng.uniform(1, 12)), kappa=float(rng.uniform(0, 1.0)), priority=prio())
+    for _ in range(int(rng.integers(1, 3))):
+        a, b = _box(rng, lines)
+        vec = [float(rng.choice([0.0, -1.0, 2.5])) for _ in range(3)]
+        s.add_excitation(a, b, vec, delay=float(rng.choice([0.0, 1e-10, 3.7e-11])), priority=prio())
+    for _ in range(int(rng.integers(0, 4))):
+        a, b = _box(rng, lines)
+        s.add_probe(a, b, int(rng.integers(0, 4)), weight=float(rng.choice([1.0, -1.0, 0.5])),
+                    norm_dir=int(rng.integers(-1, 3)))
+    return s
+
+
+def _build(make):
+    try:
+        return make(), None
+    except FdtdError as ex:
+        return None, ex
+    except (RuntimeError, ValueError) as ex:
+        return None, ex
+
+
+@pytest.mark.parametrize("seed", range(60))
+def test_hostile_scenes_build_identically(seed):
+    scene = hostile_scene(seed)
+    prod, perr = _build(lambda: Operator(scene))
+    ref, rerr = _build(lambda: oracle.Operator(scene.spec))
+    assert (prod is None) == (ref is None), (perr, rerr)
+    if prod is None:
+        return
+    assert_same_operator(prod, ref)
+    for arr in oracle.desc_arrays(prod.desc).values():
+        if arr.dtype.kind == "f" and not np.all(np.isfinite(arr)):
+            pytest.fail("non-finite coefficients in a scene both builds accept")
+    assert math.isfinite(prod.dT) and prod.dT > 0

@@ -1064,6 +1064,20 @@ static int build_operator(const fdtd_scene_s& S, int threads, fdtd_operator_s& o
     // the boundary settings; their edges' effective materials come out of the
     // EC pass
     std::vector<UpmlBuild> ub = create_upml(B.N, S.bc, S.pml_size);
+    // openEMS computes the slab ranges in unsigned arithmetic
+    // (operator_ext_upml.cpp:139-201): where an axis has fewer lines than its
+    // two faces' sizes + 2 (a face that is not PML counts as 8 on x, the
+    // y / z slabs ending size[0]+1 lines before the x-max face, :163), a
+    // range ends before it starts and wraps around; such an operator cannot
+    // be built
+    for (const UpmlBuild& u : ub)
+        for (int a = 0; a < 3; ++a)
+            if (u.nl[a] == 0 || (uint64_t)u.start[a] + u.nl[a] > B.N[a]) {
+                set_error("fdtd_operator_build: a UPML slab range leaves the grid (openEMS's ranges wrap around on an "
+                          "axis with fewer lines than its faces' UPML sizes + 2; a face that is not PML counts as 8 "
+                          "on x)");
+                return FDTD_ERR_ARG;
+            }
     std::vector<SlabEff> slab_eff(ub.size());
     for (size_t k = 0; k < ub.size(); ++k)
         for (int a = 0; a < 3; ++a) {
@@ -1531,13 +1545,13 @@ static int build_operator(const fdtd_scene_s& S, int threads, fdtd_operator_s& o
         d.enabled = 1;
         bool si[3] = {false, false, false}, so[3] = {false, false, false};
         if (p.probe_type == 2 || p.probe_type == 3) {
-            // ProcessFieldProbe: the start point snapped to the main mesh (E)
-            // or the dual mesh (H, SetDualMesh, openems.cpp:520-524)
-            d.enabled = g.snap_mesh(p.start, d.start, p.probe_type == 3, si) ? 1 : 0;
-            for (int n = 0; n < 3; ++n) {
-                d.stop[n] = d.start[n];
-                so[n] = si[n];
-            }
+            // ProcessFieldProbe: Processing::DefineStartStopCoord snaps the
+            // box (SnapBox2Mesh with snap method 0, operator.cpp:289-314: the
+            // corners sorted per axis) to the main mesh (E) or the dual mesh
+            // (H, SetDualMesh, openems.cpp:520-524) and turns the probe off
+            // when the box misses the grid; the probe reads the field at the
+            // snapped lower corner (processfieldprobe.cpp:79-92)
+            d.enabled = g.snap_box(p.start, p.stop, d.start, d.stop, p.probe_type == 3, 0, si, so) >= 0 ? 1 : 0;
         } else if (p.probe_type == 0) {
             // a voltage probe needs a box of dimension 1 (a line); any other
             // box is skipped with an error message (openems.cpp:481-486)
