@@ -215,7 +215,11 @@ def assert_same_operator(prod_op, ref_op):
     assert prod_op.dT == ref_op.dT
     assert prod_op.probe_interval == ref_op.probe_interval
     assert prod_op.nyquist == ref_op.nyquist
-    assert oracle.probe_tuples(prod_op.probes) == oracle.probe_tuples(ref_op.probes)
+    # a disabled probe is read by nobody: its type, weight and state are
+    # compared, not the placeholder corners each build leaves in it
+    def probes(op):
+        return [t if t[-1] else (t[0], t[6], t[7]) for t in oracle.probe_tuples(op.probes)]
+    assert probes(prod_op) == probes(ref_op)
 
 
 def oracle_operator(prod_op, threads: int = 0):

@@ -757,6 +757,21 @@ int compress_impl(const fdtd_op_desc* d, int mode, int want_rot, fdtd_cop_s* c) 
                 set_error("a voltage excitation on a lumped RLC edge: not provided");
                 return FDTD_ERR_UNSUPPORTED;
             }
+        // openEMS turns an unset (negative) R, L or C into NaN
+        // (operator_ext_lumpedRLC.cpp:188-196); a series element without
+        // all three, or a parallel one with L but no R, then has NaN
+        // coefficients (:271-273, :307), and its run would turn every
+        // field to NaN.  Refused here, before a timestep is spent.
+        for (uint32_t k = 0; k < r.count; ++k) {
+            const float v[9] = {r.ilv[k], r.i2v[k], r.vv2[k], r.vj1[k], r.vj2[k],
+                                r.vvd[k], r.ib0[k], r.b1[k], r.b2[k]};
+            for (float x : v)
+                if (!std::isfinite(x)) {
+                    set_error("a lumped RLC element has non-finite coefficients (openEMS turns an unset R, L or C "
+                              "into NaN: a series element needs all three, a parallel one with an L needs its R)");
+                    return FDTD_ERR_ARG;
+                }
+        }
         RlcList& q = c->rlc;  // in device axes
         for (int a = 0; a < 3; ++a) q.pos[a].assign(r.pos[(a + P.rot) % 3], r.pos[(a + P.rot) % 3] + r.count);
         q.dir.resize(r.count);
