@@ -129,3 +129,18 @@ def test_hostile_scenes_build_identically(seed):
     if bad:  # refused (by this check, or by an earlier one)
         with pytest.raises(FdtdError):
             CompressedOperator(prod)
+
+
+@pytest.mark.parametrize("seed", range(0, 150, 3))
+def test_hostile_scenes_as_xml_read_identically(seed):
+    """The hostile scenes written as openEMS XML documents (random spellings,
+    as in test_xml_random.py): the engine library's reader + operator build
+    and the oracle's reader + operator build agree, or both refuse."""
+    from oracle.xml_spec import xml_spec
+    from test_xml_random import spec_xml
+    text = spec_xml(hostile_scene(seed).spec, np.random.default_rng(9000 + seed))
+    prod, perr = _build(lambda: Operator(Scene.from_xml(text)))
+    ref, rerr = _build(lambda: oracle.Operator(xml_spec(text)))
+    assert (prod is None) == (ref is None), (perr, rerr)
+    if prod is not None:
+        assert_same_operator(prod, ref)
