@@ -144,3 +144,50 @@ def test_hostile_scenes_as_xml_read_identically(seed):
     assert (prod is None) == (ref is None), (perr, rerr)
     if prod is not None:
         assert_same_operator(prod, ref)
+
+
+@pytest.mark.parametrize("seed", range(40))
+def test_scene_api_survives_bad_values(seed):
+    """NaN, infinite, negative and huge values in the scene calls: every
+    call either takes the value or refuses it with a status, and the
+    operator build and compression end in a result or a status, never in a
+    crash (a crash here ends the test process)."""
+    rng = np.random.default_rng(11000 + seed)
+    bad = [float("nan"), float("inf"), -float("inf"), -1.0, 0.0, 1e300, -1e300, 1e-300]
+
+    def v():
+        return float(rng.choice(bad)) if rng.random() < 0.08 else float(rng.uniform(0, 10))
+
+    lines = [np.arange(0, 10.5, 0.5)] * 3
+    s = Scene(*lines, 1e-3)
+    try:
+        s.set_boundary([int(rng.choice([0, 1, 2, 3, 3, 3])) for _ in range(6)],
+                       [int(rng.choice([0, 2, 8, 3, 1])) for _ in range(6)])
+    except FdtdError:
+        return
+    for _ in range(6):
+        k = int(rng.integers(0, 6))
+        a, b = [v() for _ in range(3)], [v() for _ in range(3)]
+        try:
+            if k == 0:
+                s.add_material(a, b, eps_r=v(), kappa=v(), mue_r=v(), sigma=v(), priority=int(rng.integers(-5, 5)))
+            elif k == 1:
+                s.add_metal(a, b)
+            elif k == 2:
+                s.add_excitation(a, b, [v(), v(), v()], delay=v())
+            elif k == 3:
+                s.add_probe(a, b, int(rng.integers(-1, 5)), weight=v(), norm_dir=int(rng.integers(-2, 4)))
+            elif k == 4:
+                s.add_lumped(a, b, int(rng.integers(-1, 4)), R=v(), Cap=v())
+            else:
+                s.add_lorentz(a, b, eps_r=v(), plasma_f=[v()], relax_t=[v()], pole_f=[v()])
+        except FdtdError:
+            pass
+    try:
+        s.set_gauss_excite(v(), v(), int(rng.integers(1, 50)))
+    except FdtdError:
+        pass
+    try:
+        CompressedOperator(Operator(s))
+    except FdtdError:
+        pass
